@@ -1,0 +1,179 @@
+/*
+ * izem_gpu.h -- C ABI of the GB300 (sm_103a) implementation of the IZEM
+ * right-hand-side hot path: characteristic WENO convective fluxes, fitted or
+ * EGLIB mixture transport viscous fluxes, stiff CHEMKIN chemistry integrated
+ * per cell by a BDF method, and the SSP-RK3 conservative update.
+ *
+ * The Fortran host keeps its module interfaces (module_solver, module_weno,
+ * module_viscflux, module_reaction) and forwards their bodies through
+ * iso_c_binding to these entry points.  Every array argument is the base
+ * address of a Fortran column-major array with the reference's own bounds
+ * (sx-ng:ex+ng, sy-ng:ey+ng, sz-ng:ez+ng[, 1:nv]); i is fastest, the variable
+ * index slowest.  Plain pointers and sizes only: no C++ or torch types.
+ *
+ * Every entry point returns 0 (IZEM_OK) on success or one of the IZEM_ERR_*
+ * codes; izem_gpu_last_error() gives the message.  The reference maps these
+ * conditions to abort_mpi (devel-izem/src/module_parallel.f90:200).
+ */
+#ifndef IZEM_GPU_H
+#define IZEM_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define IZEM_NSMAX 10      /* maximum reactive species (9-species H2/air set) */
+#define IZEM_NPOLY 4       /* transport fit order (tranfit.out: Npoly = 4)    */
+
+/* Boundary kinds of the faces W,E,S,N,B,F (module_parameters: bc(1:6)). */
+enum { IZEM_BC_PERIODIC = 0, IZEM_BC_EXTRAPOLATION = 1 };
+enum { IZEM_FACE_W = 0, IZEM_FACE_E, IZEM_FACE_S, IZEM_FACE_N, IZEM_FACE_B, IZEM_FACE_F };
+
+/* Status codes. */
+enum {
+  IZEM_OK = 0,
+  IZEM_ERR_ARG = 1,            /* bad argument / unsupported configuration          */
+  IZEM_ERR_CUDA = 2,           /* CUDA runtime failure (message has the detail)    */
+  IZEM_ERR_NEG_PRESSURE = 3,   /* euler_LLF_*: P <= 0 (module_weno.f90:1027-1036)  */
+  IZEM_ERR_NEG_TEMPERATURE = 4,/* prim_inv_var: T < 0 (module_thermodynamics:125)  */
+  IZEM_ERR_NAN = 5,            /* Newton error is NaN (module_thermodynamics:182)  */
+  IZEM_ERR_CHEM = 6,           /* stiff integrator failed on at least one cell     */
+  IZEM_ERR_TIMEOUT = 7,        /* a bounded device-side wait gave up               */
+  IZEM_ERR_NOMEM = 8,          /* device allocation failed                         */
+  IZEM_ERR_STATE = 9           /* call made in the wrong order (e.g. no grid set)  */
+};
+
+/* Hot-path switches and sizes: the subset of the reference's globals that the
+ * RHS reads (module_parameters.f90:35-56, module_input.f90:266-400,622-770). */
+typedef struct izem_cfg {
+  int    nx, ny, nz;        /* interior points of this block: ex-sx+1, ...      */
+  int    ng;                /* ghost depth = (order_weno+1)/2; 3 = WENO5        */
+  int    ndim;              /* must be 3                                        */
+  int    nrv;               /* reactive species, 2..IZEM_NSMAX                  */
+  int    bc[6];             /* IZEM_BC_* per face W,E,S,N,B,F                   */
+  int    weno_avg;          /* [WENO] WEIGHTS: nonlinear weights where sensed   */
+  double max_rel_weight;    /* [WENO] PERCENT_WEIGHT (Adams-Shariff threshold)  */
+  int    vis;               /* [GENERAL] VIS                                    */
+  int    eglib;             /* [GENERAL] EGLIB (EGLIB transport, precision 1)   */
+  int    forcesum;          /* [GENERAL] FORCESUM                               */
+  int    reaction;          /* [REACTING] REACTION                              */
+  int    vis_dt;            /* [TIMESTEPPING] VIS_DT (Fourier criteria)         */
+  double cfl, cflmin, cpr, fo;   /* [TIMESTEPPING] CFL CFLMIN CPR FO            */
+  int    weno5_linear_fix;  /* 0: reference linear WENO5 stencil (mirrored);
+                               1: textbook upwind-biased stencil                 */
+} izem_cfg;
+
+/* Species data in code units (thd_type, thd/type_thd.f90:10-92), filled from
+ * therm.dat + tranfit.out by thd_init (thd/thd_tools_perfectgas.f90:12-229). */
+typedef struct izem_thd {
+  int    nspc;
+  double gam2;              /* (gamma_inf-1)/gamma_inf                          */
+  double tinf;              /* T_ref [K]                                        */
+  double pinf, p0;          /* p_ref [Pa], 101325 Pa                            */
+  double muinf, laminf;     /* mu_ref [kg/m/s], lambda_ref [W/m/K]              */
+  double dinf[IZEM_NSMAX];  /* D_ref [m^2/s]                                    */
+  double W[IZEM_NSMAX];     /* molar masses [kg/mol]                            */
+  double Wc[IZEM_NSMAX];    /* W / W_ref                                        */
+  double Wc_i[IZEM_NSMAX];  /* 1 / Wc                                           */
+  double tpolymin[IZEM_NSMAX], tpolymax[IZEM_NSMAX], tpolylim[IZEM_NSMAX];
+  double heatcap[IZEM_NSMAX][2][7];   /* [species][0 low / 1 high][a1..a7]      */
+  double cofd[IZEM_NSMAX][IZEM_NSMAX][IZEM_NPOLY]; /* ln D_kl fit in ln T       */
+  double coflam[IZEM_NSMAX][IZEM_NPOLY];           /* ln lambda_k fit           */
+  double cofeta[IZEM_NSMAX][IZEM_NPOLY];           /* ln eta_k fit              */
+} izem_thd;
+
+/* Non-dimensional references (adi_type, module_adim.f90:31-90), computed by
+ * constants (module_tools.f90:453-571). */
+typedef struct izem_adi {
+  double gamma_inf, re, pr, le, ma, sc;
+  double sqgmr, ggmopr;
+  double t_ref, l_ref, r_ref, w_ref, cp_ref, mu_ref, c_inf, u_ref, time_ref;
+  double rho_ref, p_ref, lbda_ref, d_ref;
+} izem_adi;
+
+typedef struct izem_ctx izem_ctx;
+
+/* Create a context on the current CUDA device.  Allocates the device-resident
+ * state (v, T, W_i, cp, ha, shock sensor) and the RK3 scratch (v0, f).
+ * Replaces the allocations at module_solver.f90:736-739 and the per-call
+ * temporaries of module_weno.f90:588-607, module_viscflux.f90:1708-1714. */
+int  izem_gpu_init(const izem_cfg* cfg, const izem_thd* thd, const izem_adi* adi,
+                   izem_ctx** out);
+void izem_gpu_destroy(izem_ctx* ctx);
+int  izem_gpu_last_error(izem_ctx* ctx, char* buf, int n);
+
+/* Inverted metrics dx_i(sx-ng:ex+ng) etc. (module_tools.f90:223-452, already
+ * multiplied by L_ref as in adimensionalize, module_tools.f90:185-187). */
+int  izem_gpu_set_grid(izem_ctx* ctx, const double* dx_i, const double* dy_i,
+                       const double* dz_i);
+
+/* Host <-> device copies of the ghosted state.  shock_sensor is one byte per
+ * ghosted point (Fortran logical converted by the shim).  Any pointer may be
+ * NULL to skip that array. */
+int  izem_gpu_upload_state(izem_ctx* ctx, const double* v, const double* T,
+                           const double* W_i, const double* cp, const double* ha,
+                           const uint8_t* shock_sensor);
+int  izem_gpu_download_state(izem_ctx* ctx, double* v, double* T, double* W_i,
+                             double* cp, double* ha, uint8_t* shock_sensor);
+/* Copy the RK flux array f(sx:ex,sy:ey,sz:ez,1:nv) to the host. */
+int  izem_gpu_download_flux(izem_ctx* ctx, double* fl);
+/* Zero the device flux array (test helper for the accumulating y/z sweeps). */
+int  izem_gpu_zero_flux(izem_ctx* ctx);
+
+/* shock_sensor_modified_adams_shariff (module_tools.f90:2733-2814): sets the
+ * sticky mask (never cleared) on the device. */
+int  izem_gpu_shock_sensor(izem_ctx* ctx);
+
+/* euler_LLF_x/_y/_z (module_weno.f90:537,1055,1595): dir 0 overwrites f,
+ * dir 1 and 2 accumulate into f. */
+int  izem_gpu_euler_flux(izem_ctx* ctx, int dir);
+
+/* viscflux_xyz (module_viscflux.f90:1660-2189): accumulates into f. */
+int  izem_gpu_visc_flux(izem_ctx* ctx);
+
+/* upd_prim_var_domain + comm_cons + upd_boundaries + upd_prim_var_ghost
+ * (module_BCs.f90:41-296): force_sumY, Newton temperature per sub-domain with
+ * the reference's global stopping test, halo wrap / extrapolation. */
+int  izem_gpu_update_primitives(izem_ctx* ctx);
+
+/* Initial-condition closure of the reference's init routines (e.g.
+ * module_ICs.f90:2874-2879): comm_cons, prim_inv_var_err_mach on the interior,
+ * upd_extrapolation, prim_inv_var_err_mach on each ghost face. */
+int  izem_gpu_finalize_ic(izem_ctx* ctx);
+
+/* rk3 (module_solver.f90:694-856): three SSP-RK3 stages on the device
+ * state, captured once into a CUDA graph and replayed. */
+int  izem_gpu_rk3(izem_ctx* ctx, double dt, double time0);
+
+/* timestep (module_solver.f90:202-408): dt_4 and dtmin (non-dimensional).
+ * dtmin is in/out: its input value is the previous step's dtmin (used by the
+ * chemical criterion), DTmax the previous chemistry's max |dT|. */
+int  izem_gpu_timestep(izem_ctx* ctx, double DTmax, double dt_4[4], double* dtmin);
+
+/* Device timing of the calls above on the context's stream (CUDA events). */
+int  izem_gpu_timer_start(izem_ctx* ctx);
+int  izem_gpu_timer_stop(izem_ctx* ctx, float* ms);
+/* Per-kernel timing: when enabled, every kernel launch is bracketed by CUDA
+ * events on the context's stream; izem_gpu_kernel_times returns, for each
+ * kernel id, the launch count and the summed device milliseconds. */
+int  izem_gpu_set_kernel_timing(izem_ctx* ctx, int enable);
+int  izem_gpu_kernel_times(izem_ctx* ctx, int max_kernels, char* names, int name_len,
+                           int* launches, double* ms, int* n_kernels);
+int  izem_gpu_synchronize(izem_ctx* ctx);
+
+/* Helper used by the host to build dx_i: dscalar on the global coordinate
+ * array (module_deriv.f90:80-205) followed by the inversion in metrics
+ * (module_tools.f90:424-426).  coord has n entries; d_i receives n entries. */
+int  izem_metrics_dscalar(int n, int ng, const double* coord, double* d_i);
+
+/* sizeof of the three configuration structures, for binding generators and
+ * layout checks (izem_cfg, izem_thd, izem_adi).  No device call. */
+int  izem_abi_sizes(size_t* cfg, size_t* thd, size_t* adi);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* IZEM_GPU_H */

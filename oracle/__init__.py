@@ -1,0 +1,154 @@
+"""CPU oracle of the IZEM hot path -- TEST INFRASTRUCTURE ONLY.
+
+A ctypes wrapper over oracle/_build/libizem_oracle.so, the C++ restatement of
+the reference Fortran routines (see izem_oracle.cpp).  Only the tests, the
+smoke check and the CPU-baseline leg of bench.py may import this package; the
+product library never calls it.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from phd_gb300.capi import IzemAdi, IzemCfg, IzemThd
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libizem_oracle.so")
+_LIB = None
+_dp = C.POINTER(C.c_double)
+_u8p = C.POINTER(C.c_uint8)
+
+
+def load():
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.exists(LIB_PATH):
+        from phd_gb300.build import build_oracle
+        build_oracle()
+    lib = C.CDLL(LIB_PATH)
+    P = C.c_void_p
+    sig = {
+        "or_create": (P, [C.POINTER(IzemCfg), C.POINTER(IzemThd), C.POINTER(IzemAdi), _dp, _dp, _dp]),
+        "or_destroy": (None, [P]),
+        "or_last_error": (C.c_int, [P, C.c_char_p, C.c_int]),
+        "or_cp_scalar": (None, [P, C.c_double, _dp, _dp]),
+        "or_ha_scalar": (None, [P, C.c_double, _dp]),
+        "or_shock_sensor": (C.c_int, [P, _dp, _dp, _dp, _u8p]),
+        "or_euler_flux": (C.c_int, [P, C.c_int, _dp, _dp, _dp, _dp, _dp, _u8p, _dp]),
+        "or_visc_flux": (C.c_int, [P, _dp, _dp, _dp, _dp, _dp, _dp]),
+        "or_prim_inv_var": (C.c_int, [P, C.c_int, C.c_int, _dp, _dp, _dp, _dp, _dp]),
+        "or_force_sumY": (C.c_int, [P, C.c_int, _dp]),
+        "or_update_primitives": (C.c_int, [P, _dp, _dp, _dp, _dp, _dp]),
+        "or_finalize_ic": (C.c_int, [P, _dp, _dp, _dp, _dp, _dp]),
+        "or_rk3": (C.c_int, [P, C.c_double, _dp, _dp, _dp, _dp, _dp, _u8p]),
+        "or_timestep": (C.c_int, [P, C.c_double, _dp, _dp, _dp, _dp, _dp, _dp]),
+        "or_metrics_dscalar": (None, [C.c_int, C.c_int, _dp, _dp]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _LIB = lib
+    return lib
+
+
+def _p(a, kind=_dp):
+    if a.ndim > 1 and not a.flags.f_contiguous:
+        raise ValueError("oracle arrays must be Fortran-ordered")
+    if (kind is _dp and a.dtype != np.float64) or (kind is _u8p and a.dtype != np.uint8):
+        raise ValueError("oracle array has dtype %s" % a.dtype)
+    return a.ctypes.data_as(kind)
+
+
+class OracleError(RuntimeError):
+    pass
+
+
+def metrics_dscalar(coord, ng=3):
+    lib = load()
+    coord = np.ascontiguousarray(coord, dtype=np.float64)
+    out = np.empty_like(coord)
+    lib.or_metrics_dscalar(len(coord), ng, _p(coord), _p(out))
+    return out
+
+
+class Oracle:
+    """Reference restatement operating in place on a host state dictionary
+    {"v", "T", "W_i", "cp", "ha", "shock_sensor"} (Fortran-ordered arrays)."""
+
+    def __init__(self, cfg, thd, adi, dx_i, dy_i, dz_i):
+        self.lib = load()
+        self.cfg = cfg
+        self.nv = 5 + cfg.nrv
+        self._grid = [np.ascontiguousarray(a, dtype=np.float64) for a in (dx_i, dy_i, dz_i)]
+        self.h = self.lib.or_create(C.byref(cfg), C.byref(thd), C.byref(adi), *[_p(a) for a in self._grid])
+        if not self.h:
+            raise OracleError("unsupported configuration")
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib.or_destroy(self.h)
+            self.h = None
+
+    def _rc(self, rc, what):
+        if rc:
+            buf = C.create_string_buffer(256)
+            self.lib.or_last_error(self.h, buf, 256)
+            raise OracleError("%s failed (%d): %s" % (what, rc, buf.value.decode()))
+
+    def newton_warnings(self):
+        return self.lib.or_last_error(self.h, None, 0)
+
+    def cp_scalar(self, T, Y):
+        Y = np.ascontiguousarray(Y, dtype=np.float64)
+        out = C.c_double()
+        self.lib.or_cp_scalar(self.h, float(T), _p(Y), C.byref(out))
+        return out.value
+
+    def ha_scalar(self, T):
+        out = np.zeros(self.cfg.nrv)
+        self.lib.or_ha_scalar(self.h, float(T), _p(out))
+        return out
+
+    @staticmethod
+    def _arrs(s):
+        return s["v"], s["T"], s["W_i"], s["cp"], s["ha"]
+
+    def shock_sensor(self, s):
+        self._rc(self.lib.or_shock_sensor(self.h, _p(s["v"]), _p(s["T"]), _p(s["W_i"]), _p(s["shock_sensor"], _u8p)),
+                 "shock_sensor")
+
+    def euler_flux(self, s, direction, fl):
+        v, T, W_i, cp, ha = self._arrs(s)
+        self._rc(self.lib.or_euler_flux(self.h, direction, _p(v), _p(T), _p(W_i), _p(cp), _p(ha),
+                                        _p(s["shock_sensor"], _u8p), _p(fl)), "euler_flux")
+
+    def visc_flux(self, s, fl):
+        v, T, W_i, cp, ha = self._arrs(s)
+        self._rc(self.lib.or_visc_flux(self.h, _p(v), _p(T), _p(W_i), _p(cp), _p(ha), _p(fl)), "visc_flux")
+
+    def prim_inv_var(self, s, domain_id, err_mach=False):
+        v, T, W_i, cp, ha = self._arrs(s)
+        self._rc(self.lib.or_prim_inv_var(self.h, domain_id, int(err_mach), _p(v), _p(W_i), _p(T), _p(cp), _p(ha)),
+                 "prim_inv_var")
+
+    def update_primitives(self, s):
+        v, T, W_i, cp, ha = self._arrs(s)
+        self._rc(self.lib.or_update_primitives(self.h, _p(v), _p(T), _p(W_i), _p(cp), _p(ha)), "update_primitives")
+
+    def finalize_ic(self, s):
+        v, T, W_i, cp, ha = self._arrs(s)
+        self._rc(self.lib.or_finalize_ic(self.h, _p(v), _p(T), _p(W_i), _p(cp), _p(ha)), "finalize_ic")
+
+    def rk3(self, s, dt):
+        v, T, W_i, cp, ha = self._arrs(s)
+        self._rc(self.lib.or_rk3(self.h, float(dt), _p(v), _p(T), _p(W_i), _p(cp), _p(ha),
+                                 _p(s["shock_sensor"], _u8p)), "rk3")
+
+    def timestep(self, s, DTmax=0.0, dtmin=1.0):
+        v, T, W_i, cp, _ = self._arrs(s)
+        dt4 = np.zeros(4)
+        dtm = C.c_double(dtmin)
+        self.lib.or_timestep(self.h, float(DTmax), _p(v), _p(T), _p(W_i), _p(cp), _p(dt4), C.byref(dtm))
+        return dt4, dtm.value

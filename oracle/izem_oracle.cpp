@@ -1,0 +1,1053 @@
+// CPU oracle for the IZEM right-hand-side hot path -- TEST INFRASTRUCTURE ONLY.
+//
+// This file restates, in C++17 and loop by loop, the Fortran routines of the
+// reference solver (saras13015/Phd, devel-izem/src) that the GPU library
+// replaces.  It is the checker for the CUDA path: only tests, the smoke check
+// and the CPU-baseline leg of the benchmark may load it; the product never
+// links or calls it.  The reference cannot be compiled here (no Fortran
+// compiler, MPI or HDF5), so this restatement is the oracle.  Each function
+// cites the reference lines it follows; floating-point expressions keep the
+// reference's operation order so that results agree to rounding.  Build with
+// -ffp-contract=off so that no multiply-add is fused on either machine.
+//
+// Parity pinning: the non-reacting WENO path is pinned against the stored
+// Sod run of the reference (testcases/sod); see tests/test_oracle_sod.py.
+//
+// Layout: one block of nx*ny*nz interior points with ng ghost layers,
+// Fortran column-major, variable index slowest, exactly the reference's
+// v(sx-ng:ex+ng, sy-ng:ey+ng, sz-ng:ez+ng, 1:nv) with sx = sy = sz = 1.
+
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <algorithm>
+#include <vector>
+#include <string>
+
+#include "../include/izem_gpu.h"
+
+namespace {
+
+constexpr int NIV = 5;
+
+// ---------------------------------------------------------------- block ----
+struct Block {
+  int nx, ny, nz, ng, nrv, nv;
+  int gx, gy, gz;
+  size_t ncell, nint;
+  bool bnd[6];   // face is a physical boundary (neigh == MPI_PROC_NULL)
+  int bc[6];
+  size_t id(int i, int j, int k) const {
+    return (size_t)(i - 1 + ng) + (size_t)gx * ((size_t)(j - 1 + ng) + (size_t)gy * (size_t)(k - 1 + ng));
+  }
+  size_t fid(int i, int j, int k) const {
+    return (size_t)(i - 1) + (size_t)nx * ((size_t)(j - 1) + (size_t)ny * (size_t)(k - 1));
+  }
+  int n(int d) const { return d == 0 ? nx : (d == 1 ? ny : nz); }
+};
+
+struct Ctx {
+  izem_cfg cfg;
+  izem_thd thd;
+  izem_adi adi;
+  Block b;
+  std::vector<double> dxi[3];   // indexed (i-1+ng), length n+2ng
+  int newton_warn = 0;
+  std::string err;
+};
+
+// domain_select (module_parallel.f90:1936-2020), restricted to the ids used
+// on the hot path: 0 interior, -1/1 x-ghost slabs, -2/2 y, -3/3 z.
+void domain_select(const Block& b, int id, int& i0, int& i1, int& j0, int& j1, int& k0, int& k1) {
+  i0 = 1; i1 = b.nx; j0 = 1; j1 = b.ny; k0 = 1; k1 = b.nz;
+  switch (id) {
+    case -3: k0 = 1 - b.ng; k1 = 0; break;
+    case -2: j0 = 1 - b.ng; j1 = 0; break;
+    case -1: i0 = 1 - b.ng; i1 = 0; break;
+    case 0: break;
+    case 1: i0 = b.nx + 1; i1 = b.nx + b.ng; break;
+    case 2: j0 = b.ny + 1; j1 = b.ny + b.ng; break;
+    case 3: k0 = b.nz + 1; k1 = b.nz + b.ng; break;
+    default: break;
+  }
+}
+
+// ------------------------------------------------------------ thermo -------
+// cp_scalar (module_thermodynamics.f90:767-862)
+double cp_scalar(const izem_thd& t, double temp, const double* Y) {
+  double cp = 0.0;
+  for (int is = 0; is < t.nspc; ++is) {
+    double t1 = temp * t.tinf, t2 = t1 * t1, t3 = t2 * t1, t4 = t3 * t1;
+    const double* lo = t.heatcap[is][0];
+    const double* hi = t.heatcap[is][1];
+    double fac = Y[is] * t.gam2 * t.Wc_i[is];
+    if (t1 < t.tpolymin[is]) {
+      t1 = t.tpolymin[is]; t2 = t1 * t1; t3 = t2 * t1; t4 = t3 * t1;
+      double cp0 = lo[0] + lo[1] * t1 + lo[2] * t2 + lo[3] * t3 + lo[4] * t4;
+      double dcp0 = lo[1] + lo[2] * t1 * 2.0 + lo[3] * t2 * 3.0 + lo[4] * t3 * 4.0;
+      cp = cp + fac * (dcp0 * (temp * t.tinf - t.tpolymin[is]) + cp0);
+    } else if (t1 < t.tpolylim[is]) {
+      cp = cp + fac * (lo[0] + lo[1] * t1 + lo[2] * t2 + lo[3] * t3 + lo[4] * t4);
+    } else if (t1 < t.tpolymax[is]) {
+      cp = cp + fac * (hi[0] + hi[1] * t1 + hi[2] * t2 + hi[3] * t3 + hi[4] * t4);
+    } else {
+      t1 = t.tpolymax[is]; t2 = t1 * t1; t3 = t2 * t1; t4 = t3 * t1;
+      double cp0 = hi[0] + hi[1] * t1 + hi[2] * t2 + hi[3] * t3 + hi[4] * t4;
+      double dcp0 = hi[1] + hi[2] * t1 * 2.0 + hi[3] * t2 * 3.0 + hi[4] * t3 * 4.0;
+      cp = cp + fac * (dcp0 * (temp * t.tinf - t.tpolymax[is]) + cp0);
+    }
+  }
+  return cp;
+}
+
+inline double h_poly(const double* a, double t1, double t2, double t3, double t4, double t5, double onethird) {
+  return a[0] * t1 + a[1] * t2 * 0.50 + a[2] * t3 * onethird + a[3] * t4 * 0.25 + a[4] * t5 * 0.20 + a[5];
+}
+inline double cp_poly(const double* a, double t1, double t2, double t3, double t4) {
+  return a[0] + a[1] * t1 + a[2] * t2 + a[3] * t3 + a[4] * t4;
+}
+inline double dcp_poly(const double* a, double t1, double t2, double t3) {
+  return a[1] + a[2] * t1 * 2.0 + a[3] * t2 * 3.0 + a[4] * t3 * 4.0;
+}
+
+// ha_scalar (module_thermodynamics.f90:873-978)
+void ha_scalar(const izem_thd& t, double temp, double* ha) {
+  const double tinf_i = 1.0 / t.tinf, onethird = 1.0 / 3.0;
+  for (int is = 0; is < t.nspc; ++is) {
+    double t1 = temp * t.tinf, t2 = t1 * t1, t3 = t2 * t1, t4 = t3 * t1, t5 = t4 * t1;
+    const double* lo = t.heatcap[is][0];
+    const double* hi = t.heatcap[is][1];
+    double h;
+    if (t1 < t.tpolymin[is]) {
+      t1 = t.tpolymin[is]; t2 = t1 * t1; t3 = t2 * t1; t4 = t3 * t1; t5 = t4 * t1;
+      double ha0 = h_poly(lo, t1, t2, t3, t4, t5, onethird);
+      double dha0 = cp_poly(lo, t1, t2, t3, t4);
+      h = t.Wc_i[is] * tinf_i * (dha0 * (temp * t.tinf - t.tpolymin[is]) + ha0);
+    } else if (t1 < t.tpolylim[is]) {
+      h = t.Wc_i[is] * tinf_i * h_poly(lo, t1, t2, t3, t4, t5, onethird);
+    } else if (t1 < t.tpolymax[is]) {
+      h = t.Wc_i[is] * tinf_i * h_poly(hi, t1, t2, t3, t4, t5, onethird);
+    } else {
+      t1 = t.tpolymax[is]; t2 = t1 * t1; t3 = t2 * t1; t4 = t3 * t1; t5 = t4 * t1;
+      double ha0 = h_poly(hi, t1, t2, t3, t4, t5, onethird);
+      double dha0 = cp_poly(hi, t1, t2, t3, t4);
+      h = t.Wc_i[is] * tinf_i * (dha0 * (temp * t.tinf - t.tpolymax[is]) + ha0);
+    }
+    ha[is] = 0.0 + h;
+  }
+}
+
+// Wmix_i (module_thermodynamics.f90:700-728) on one sub-domain
+void wmix_i(const Ctx& c, int dom, const double* v, double* W_i) {
+  const Block& b = c.b;
+  int i0, i1, j0, j1, k0, k1;
+  domain_select(b, dom, i0, i1, j0, j1, k0, k1);
+  for (int k = k0; k <= k1; ++k)
+    for (int j = j0; j <= j1; ++j)
+      for (int i = i0; i <= i1; ++i) W_i[b.id(i, j, k)] = 0.0;
+  for (int l = 0; l < b.nrv; ++l)
+    for (int k = k0; k <= k1; ++k)
+      for (int j = j0; j <= j1; ++j)
+        for (int i = i0; i <= i1; ++i) {
+          size_t p = b.id(i, j, k);
+          W_i[p] = W_i[p] + (v[(NIV + l) * b.ncell + p] / v[p]) * c.thd.Wc_i[l];
+        }
+}
+
+// newton (module_thermodynamics.f90:271-508) for one cell; returns DF and
+// writes cp and ha at the input temperature.
+double newton_cell(const izem_thd& t, const Block& b, const double* v, size_t p, double T, double* cp_out, double* ha_out) {
+  const double tinf_i = 1.0 / t.tinf, onethird = 1.0 / 3.0, gam2_i = 1.0 / t.gam2;
+  const size_t nc = b.ncell;
+  double rho_i = 1.0 / v[p];
+  double v2 = v[nc + p], v3 = v[2 * nc + p], v4 = v[3 * nc + p];
+  double F = -v[4 * nc + p] * rho_i + 0.5 * (v2 * v2 + v3 * v3 + v4 * v4) * (rho_i * rho_i);
+  double Ya[IZEM_NSMAX];
+  for (int is = 0; is < b.nrv; ++is) Ya[is] = v[(NIV + is) * nc + p] * rho_i;
+  double cp = 0.0;
+  for (int is = 0; is < b.nrv; ++is) {
+    double t1 = T * t.tinf, t2 = t1 * t1, t3 = t2 * t1, t4 = t3 * t1, t5 = t4 * t1;
+    double wrk1 = -T;
+    const double* lo = t.heatcap[is][0];
+    const double* hi = t.heatcap[is][1];
+    double h;
+    double fac = Ya[is] * t.gam2 * t.Wc_i[is];
+    if (t1 < t.tpolymin[is]) {
+      t1 = t.tpolymin[is]; t2 = t1 * t1; t3 = t2 * t1; t4 = t3 * t1; t5 = t4 * t1;
+      double ha0 = h_poly(lo, t1, t2, t3, t4, t5, onethird);
+      double dha0 = cp_poly(lo, t1, t2, t3, t4);
+      h = 0.0 + t.Wc_i[is] * tinf_i * (dha0 * (T * t.tinf - t.tpolymin[is]) + ha0);
+      double cp0 = dha0;
+      double dcp0 = dcp_poly(lo, t1, t2, t3);
+      cp = cp + fac * (dcp0 * (T * t.tinf - t.tpolymin[is]) + cp0);
+    } else if (t1 < t.tpolylim[is]) {
+      h = 0.0 + t.Wc_i[is] * tinf_i * h_poly(lo, t1, t2, t3, t4, t5, onethird);
+      cp = cp + fac * cp_poly(lo, t1, t2, t3, t4);
+    } else if (t1 < t.tpolymax[is]) {
+      h = 0.0 + t.Wc_i[is] * tinf_i * h_poly(hi, t1, t2, t3, t4, t5, onethird);
+      cp = cp + fac * cp_poly(hi, t1, t2, t3, t4);
+    } else {
+      t1 = t.tpolymax[is]; t2 = t1 * t1; t3 = t2 * t1; t4 = t3 * t1; t5 = t4 * t1;
+      double ha0 = h_poly(hi, t1, t2, t3, t4, t5, onethird);
+      double dha0 = cp_poly(hi, t1, t2, t3, t4);
+      h = 0.0 + t.Wc_i[is] * tinf_i * (dha0 * (T * t.tinf - t.tpolymax[is]) + ha0);
+      double cp0 = dha0;
+      double dcp0 = dcp_poly(hi, t1, t2, t3);
+      cp = cp + fac * (dcp0 * (T * t.tinf - t.tpolymax[is]) + cp0);
+    }
+    ha_out[is] = h;
+    F = F + Ya[is] * (h + wrk1 * t.Wc_i[is]);
+  }
+  double wrk = 0.0;
+  for (int is = 0; is < b.nrv; ++is) wrk = wrk + Ya[is] * t.Wc_i[is];
+  *cp_out = cp;
+  return F / (wrk - cp * gam2_i);
+}
+
+// prim_inv_var (module_thermodynamics.f90:79-186) / prim_inv_var_err_mach
+// (:201-260) on one sub-domain: a global Newton loop whose stopping test is
+// the maximum temperature correction over the whole sub-domain.
+int prim_inv_var(Ctx& c, int dom, bool err_mach, double* v, double* W_i, double* T, double* cp, double* ha) {
+  const Block& b = c.b;
+  const int itmax = err_mach ? 100 : 200;
+  const double eps = err_mach ? 1.0e-10 : 1.0e-5;
+  int i0, i1, j0, j1, k0, k1;
+  domain_select(b, dom, i0, i1, j0, j1, k0, k1);
+  wmix_i(c, dom, v, W_i);
+  int it = 0;
+  double error = 0.0;
+  bool negT = false;
+  while (true) {
+    it = it + 1;
+    if (it > itmax) break;
+    double maxdf = 0.0;
+    bool anynan = false;
+    for (int k = k0; k <= k1; ++k)
+      for (int j = j0; j <= j1; ++j)
+        for (int i = i0; i <= i1; ++i) {
+          size_t p = b.id(i, j, k);
+          double hak[IZEM_NSMAX];
+          double cpp;
+          double DF = newton_cell(c.thd, b, v, p, T[p], &cpp, hak);
+          cp[p] = cpp;
+          for (int is = 0; is < b.nrv; ++is) ha[is * b.ncell + p] = hak[is];
+          T[p] = T[p] + DF;
+          DF = DF * DF;
+          if (!err_mach && T[p] < 0.0) negT = true;
+          if (std::isnan(DF)) anynan = true;
+          else if (DF > maxdf) maxdf = DF;
+        }
+    if (negT) {
+      c.err = "negative temperature in prim_inv_var";
+      return IZEM_ERR_NEG_TEMPERATURE;
+    }
+    error = anynan ? std::nan("") : std::sqrt(maxdf);
+    if (error < eps) break;
+  }
+  if (it > itmax) c.newton_warn++;
+  if (!err_mach && error != error) {
+    c.err = "Newton error is a NaN";
+    return IZEM_ERR_NAN;
+  }
+  return IZEM_OK;
+}
+
+// force_sumY (module_thermodynamics.f90:1709-1860), npv = nvv = 0 branch
+void force_sumY(const Ctx& c, int dom, double* v) {
+  const Block& b = c.b;
+  int i0, i1, j0, j1, k0, k1;
+  domain_select(b, dom, i0, i1, j0, j1, k0, k1);
+  for (int k = k0; k <= k1; ++k)
+    for (int j = j0; j <= j1; ++j)
+      for (int i = i0; i <= i1; ++i) {
+        size_t p = b.id(i, j, k);
+        double rho = v[p], rho_i = 1.0 / rho, sum = 0.0, Ya;
+        for (int l = 0; l < b.nrv - 1; ++l) {
+          Ya = v[(NIV + l) * b.ncell + p] * rho_i;
+          Ya = std::min(std::max(Ya, 0.0), 1.0);
+          v[(NIV + l) * b.ncell + p] = rho * Ya;
+          sum = sum + Ya;
+        }
+        Ya = 1.0 - sum;
+        Ya = std::min(std::max(Ya, 0.0), 1.0);
+        v[(NIV + b.nrv - 1) * b.ncell + p] = rho * Ya;
+      }
+}
+
+// ---------------------------------------------------------- halos / BC -----
+// comm_cons (module_parallel.f90:1715-1786) for a single periodic block:
+// face-only ghost slabs are filled from the opposite interior side.
+void comm_periodic(const Block& b, int nvar, double* a, size_t stride) {
+  for (int l = 0; l < nvar; ++l) {
+    double* q = a + l * stride;
+    if (b.bc[0] == IZEM_BC_PERIODIC)
+      for (int k = 1; k <= b.nz; ++k)
+        for (int j = 1; j <= b.ny; ++j)
+          for (int g = 1; g <= b.ng; ++g) {
+            q[b.id(1 - g, j, k)] = q[b.id(b.nx + 1 - g, j, k)];
+            q[b.id(b.nx + g, j, k)] = q[b.id(g, j, k)];
+          }
+    if (b.bc[2] == IZEM_BC_PERIODIC)
+      for (int k = 1; k <= b.nz; ++k)
+        for (int g = 1; g <= b.ng; ++g)
+          for (int i = 1; i <= b.nx; ++i) {
+            q[b.id(i, 1 - g, k)] = q[b.id(i, b.ny + 1 - g, k)];
+            q[b.id(i, b.ny + g, k)] = q[b.id(i, g, k)];
+          }
+    if (b.bc[4] == IZEM_BC_PERIODIC)
+      for (int g = 1; g <= b.ng; ++g)
+        for (int j = 1; j <= b.ny; ++j)
+          for (int i = 1; i <= b.nx; ++i) {
+            q[b.id(i, j, 1 - g)] = q[b.id(i, j, b.nz + 1 - g)];
+            q[b.id(i, j, b.nz + g)] = q[b.id(i, j, g)];
+          }
+  }
+}
+
+// bc_extrapolation (module_BCs.f90:327-410)
+void bc_extrapolation(const Block& b, int face, double* v) {
+  for (int l = 0; l < b.nv; ++l) {
+    double* q = v + l * b.ncell;
+    if (face == 0 || face == 1) {
+      for (int k = 1; k <= b.nz; ++k)
+        for (int j = 1; j <= b.ny; ++j)
+          for (int g = 1; g <= b.ng; ++g) {
+            if (face == 0) q[b.id(1 - g, j, k)] = q[b.id(1, j, k)];
+            else q[b.id(b.nx + g, j, k)] = q[b.id(b.nx, j, k)];
+          }
+    } else if (face == 2 || face == 3) {
+      for (int k = 1; k <= b.nz; ++k)
+        for (int g = 1; g <= b.ng; ++g)
+          for (int i = 1; i <= b.nx; ++i) {
+            if (face == 2) q[b.id(i, 1 - g, k)] = q[b.id(i, 1, k)];
+            else q[b.id(i, b.ny + g, k)] = q[b.id(i, b.ny, k)];
+          }
+    } else {
+      for (int g = 1; g <= b.ng; ++g)
+        for (int j = 1; j <= b.ny; ++j)
+          for (int i = 1; i <= b.nx; ++i) {
+            if (face == 4) q[b.id(i, j, 1 - g)] = q[b.id(i, j, 1)];
+            else q[b.id(i, j, b.nz + g)] = q[b.id(i, j, b.nz)];
+          }
+    }
+  }
+}
+
+const int kFaceDomain[6] = {-1, 1, -2, 2, -3, 3};
+
+// upd_prim_var_domain + comm_cons + upd_boundaries + upd_prim_var_ghost
+// (module_solver.f90:839-845, module_BCs.f90:41-296)
+int update_primitives(Ctx& c, double* v, double* T, double* W_i, double* cp, double* ha) {
+  const Block& b = c.b;
+  if (c.cfg.forcesum) force_sumY(c, 0, v);
+  int rc = prim_inv_var(c, 0, false, v, W_i, T, cp, ha);
+  if (rc) return rc;
+  comm_periodic(b, b.nv, v, b.ncell);
+  for (int f = 0; f < 6; ++f)
+    if (b.bnd[f] && b.bc[f] == IZEM_BC_EXTRAPOLATION) bc_extrapolation(b, f, v);
+  for (int f = 0; f < 6; ++f) {
+    if (c.cfg.forcesum) force_sumY(c, kFaceDomain[f], v);
+    rc = prim_inv_var(c, kFaceDomain[f], false, v, W_i, T, cp, ha);
+    if (rc) return rc;
+  }
+  return IZEM_OK;
+}
+
+// closure of the initial conditions (module_ICs.f90:2874-2879)
+int finalize_ic(Ctx& c, double* v, double* T, double* W_i, double* cp, double* ha) {
+  const Block& b = c.b;
+  comm_periodic(b, b.nv, v, b.ncell);
+  int rc = prim_inv_var(c, 0, true, v, W_i, T, cp, ha);
+  if (rc) return rc;
+  for (int f = 0; f < 6; ++f) bc_extrapolation(b, f, v);   // upd_extrapolation: every face
+  for (int f = 0; f < 6; ++f) {
+    rc = prim_inv_var(c, kFaceDomain[f], true, v, W_i, T, cp, ha);
+    if (rc) return rc;
+  }
+  return IZEM_OK;
+}
+
+// ------------------------------------------------------------ derivatives --
+// module_deriv.f90 coefficient tables (:25-66) for ng = 3
+const double alpha6[7] = {-1.0 / 60.0, 9.0 / 60.0, -45.0 / 60.0, 0.0, 45.0 / 60.0, -9.0 / 60.0, 1.0 / 60.0};
+const double alph4[5] = {1.0 / 12.0, -8.0 / 12.0, 0.0, 8.0 / 12.0, -1.0 / 12.0};
+const double alph4ol[5] = {-25.0 / 12.0, 48.0 / 12.0, -36.0 / 12.0, 16.0 / 12.0, -3.0 / 12.0};   // l = 0..4
+const double alph4ul[5] = {-3.0 / 12.0, -10.0 / 12.0, 18.0 / 12.0, -6.0 / 12.0, 1.0 / 12.0};    // l = -1..3
+const double alph4ur[5] = {1.0 / 12.0, -6.0 / 12.0, 18.0 / 12.0, -10.0 / 12.0, -3.0 / 12.0};    // l = -3..1
+const double alph4or[5] = {-3.0 / 12.0, 16.0 / 12.0, -36.0 / 12.0, 48.0 / 12.0, -25.0 / 12.0}; // l = -4..0
+
+// dx/dy/dz, d?_fixed1, d?_fixed2 (module_deriv.f90:212-2354): the three
+// families share one arithmetic; `out_interior` selects the interior-sized
+// output of d?_fixed2.  Only interior points are written.
+void deriv(const Ctx& c, int d, const double* in, double* out, bool out_interior) {
+  const Block& b = c.b;
+  const int n = b.n(d), ng = b.ng;
+  const double* di = c.dxi[d].data();
+  const bool lo_b = b.bnd[2 * d], hi_b = b.bnd[2 * d + 1];
+#pragma omp parallel for collapse(2) schedule(static)
+  for (int k = 1; k <= b.nz; ++k)
+    for (int j = 1; j <= b.ny; ++j)
+      for (int i = 1; i <= b.nx; ++i) {
+        int s = d == 0 ? i : (d == 1 ? j : k);
+        auto at = [&](int off) {
+          int ii = i, jj = j, kk = k;
+          if (d == 0) ii += off; else if (d == 1) jj += off; else kk += off;
+          return in[b.id(ii, jj, kk)];
+        };
+        double dd = 0.0, res;
+        double dis = di[s - 1 + ng];
+        if (lo_b && s == 1) {
+          for (int l = 0; l <= 4; ++l) dd = dd + alph4ol[l] * at(l);
+          res = dd * dis;
+        } else if (lo_b && s == 2) {
+          for (int l = -1; l <= 3; ++l) dd = dd + alph4ul[l + 1] * at(l);
+          res = dd * dis;
+        } else if (lo_b && s == 3) {
+          for (int l = -2; l <= 2; ++l) dd = dd + alph4[l + 2] * at(l);
+          res = dd * dis;
+        } else if (hi_b && s == n - 2) {
+          for (int l = -2; l <= 2; ++l) dd = dd + alph4[l + 2] * at(l);
+          res = dd * dis;
+        } else if (hi_b && s == n - 1) {
+          for (int l = -3; l <= 1; ++l) dd = dd + alph4ur[l + 3] * at(l);
+          res = -dd * dis;
+        } else if (hi_b && s == n) {
+          for (int l = -4; l <= 0; ++l) dd = dd + alph4or[l + 4] * at(l);
+          res = -dd * dis;
+        } else {
+          for (int l = -3; l <= 3; ++l) dd = dd + alpha6[l + 3] * at(l);
+          res = dd * dis;
+        }
+        if (out_interior) out[b.fid(i, j, k)] = res;
+        else out[b.id(i, j, k)] = res;
+      }
+}
+
+// ------------------------------------------------------------------ WENO ---
+struct Weno {
+  double cweno[5][3];  // cweno(-1:ng-1, 0:ng-1) stored at [r+1][j]
+  double dweno[3], dtweno[3];
+  double z1, z2, za, zb, zc, zd;
+};
+
+// wenopar (module_weno.f90:60-225), ng = 3 branch
+Weno wenopar() {
+  Weno w;
+  w.cweno[0][0] = 11.0 / 6.0; w.cweno[0][1] = -7.0 / 6.0; w.cweno[0][2] = 1.0 / 3.0;
+  w.cweno[1][0] = 1.0 / 3.0;  w.cweno[1][1] = 5.0 / 6.0;  w.cweno[1][2] = -1.0 / 6.0;
+  w.cweno[2][0] = -1.0 / 6.0; w.cweno[2][1] = 5.0 / 6.0;  w.cweno[2][2] = 1.0 / 3.0;
+  w.cweno[3][0] = 1.0 / 3.0;  w.cweno[3][1] = -7.0 / 6.0; w.cweno[3][2] = 11.0 / 6.0;
+  w.dweno[0] = 3.0 / 10.0; w.dweno[1] = 3.0 / 5.0; w.dweno[2] = 1.0 / 10.0;
+  w.dtweno[0] = w.dweno[2]; w.dtweno[1] = w.dweno[1]; w.dtweno[2] = w.dweno[0];
+  w.z1 = 13.0 / 12.0; w.z2 = 1.0 / 4.0; w.za = -2.0; w.zb = -4.0; w.zc = 3.0; w.zd = -1.0;
+  return w;
+}
+
+// wenorec_nw (module_weno.f90:236-275), ng = 3.  vp/vm are 1-based arrays
+// of length 2ng.  `fix` selects the textbook upwind-biased stencil instead of
+// the reference's mirrored one.
+void wenorec_nw(const double* vp, const double* vm, double& vminus, double& vplus, bool fix) {
+  const double denom = 1.0 / 60.0;
+  if (!fix) {
+    vminus = (-3.0 * vp[1] + 27.0 * vp[2] + 47.0 * vp[3] - 13.0 * vp[4] + 2.0 * vp[5]) * denom;
+    vplus = (-3.0 * vm[6] + 27.0 * vm[5] + 47.0 * vm[4] - 13.0 * vm[3] + 2.0 * vm[2]) * denom;
+  } else {
+    vminus = (2.0 * vp[1] - 13.0 * vp[2] + 47.0 * vp[3] + 27.0 * vp[4] - 3.0 * vp[5]) * denom;
+    vplus = (2.0 * vm[6] - 13.0 * vm[5] + 47.0 * vm[4] + 27.0 * vm[3] - 3.0 * vm[2]) * denom;
+  }
+}
+
+// wenorec (module_weno.f90:286-527), ng = 3
+void wenorec(const Weno& w, const double* vp, const double* vm, double& vminus, double& vplus) {
+  const double eps_weno = 1.0e-10;
+  double vpr[3], vmr[3], beta[3], alfa[3], omega[3], sum;
+  int i = 3;
+  for (int r = 0; r < 3; ++r) {
+    vpr[r] = 0.0;
+    for (int j = 0; j < 3; ++j) vpr[r] = vpr[r] + w.cweno[r + 1][j] * vp[i - r + j];
+  }
+  auto betas = [&](const double* q, int ii) {
+    double a = q[ii] + w.za * q[ii + 1] + q[ii + 2];
+    double bq = w.zc * q[ii] + w.zb * q[ii + 1] + q[ii + 2];
+    beta[0] = w.z1 * a * a + w.z2 * bq * bq;
+    a = q[ii - 1] + w.za * q[ii] + q[ii + 1];
+    bq = q[ii - 1] + w.zd * q[ii + 1];
+    beta[1] = w.z1 * a * a + w.z2 * bq * bq;
+    a = q[ii - 2] + w.za * q[ii - 1] + q[ii];
+    bq = q[ii - 2] + w.zb * q[ii - 1] + w.zc * q[ii];
+    beta[2] = w.z1 * a * a + w.z2 * bq * bq;
+  };
+  betas(vp, i);
+  sum = 0.0;
+  for (int r = 0; r < 3; ++r) {
+    alfa[r] = w.dweno[r] / ((eps_weno + beta[r]) * (eps_weno + beta[r]));
+    sum = sum + alfa[r];
+  }
+  sum = 1.0 / sum;
+  for (int r = 0; r < 3; ++r) omega[r] = alfa[r] * sum;
+  vminus = 0.0;
+  for (int r = 0; r < 3; ++r) vminus = vminus + omega[r] * vpr[r];
+
+  i = 4;
+  for (int r = 0; r < 3; ++r) {
+    vmr[r] = 0.0;
+    for (int j = 0; j < 3; ++j) vmr[r] = vmr[r] + w.cweno[r][j] * vm[i - r + j];
+  }
+  betas(vm, i);
+  sum = 0.0;
+  for (int r = 0; r < 3; ++r) {
+    alfa[r] = w.dtweno[r] / ((eps_weno + beta[r]) * (eps_weno + beta[r]));
+    sum = sum + alfa[r];
+  }
+  sum = 1.0 / sum;
+  for (int r = 0; r < 3; ++r) omega[r] = alfa[r] * sum;
+  vplus = 0.0;
+  for (int r = 0; r < 3; ++r) vplus = vplus + omega[r] * vmr[r];
+}
+
+// euler_LLF_x/_y/_z (module_weno.f90:537-1044, 1055-1590, 1595-2125).
+// The three routines differ only in the sweep axis d and in which velocity
+// components are normal / tangential; they are restated once over d.
+int euler_flux(Ctx& c, int d, const double* v, const double* T, const double* W_i, const double* cp,
+               const double* ha, const uint8_t* sensor, double* fl) {
+  const Block& b = c.b;
+  const izem_thd& t = c.thd;
+  const int ng = b.ng, nv = b.nv, nrv = b.nrv, st_m1 = 2 * ng;
+  const size_t nc = b.ncell;
+  const Weno w = wenopar();
+  const int n = b.n(d);
+  const int t1 = d == 0 ? 1 : 0, t2 = d == 2 ? 1 : 2;  // tangential components
+  const double* di = c.dxi[d].data();
+  const bool fixlin = c.cfg.weno5_linear_fix != 0;
+  int m1 = d == 0 ? b.ny : b.nx, m2 = d == 2 ? b.ny : b.nz;
+  bool negp = false;
+#pragma omp parallel for collapse(2) schedule(dynamic)
+  for (int q2 = 1; q2 <= m2; ++q2)
+    for (int q1 = 1; q1 <= m1; ++q1) {
+      auto cell = [&](int s) {
+        if (d == 0) return b.id(s, q1, q2);
+        if (d == 1) return b.id(q1, s, q2);
+        return b.id(q1, q2, s);
+      };
+      const int len = n + 2 * ng;
+      std::vector<double> rho_i(len), uu[3], P(len), gam(len), cs(len), ht(len), et(len), Ya(len * nrv);
+      for (int a = 0; a < 3; ++a) uu[a].assign(len, 0.0);
+      std::vector<double> fhat((n + 1) * nv);
+      auto ix = [&](int s) { return s - 1 + ng; };
+      for (int s = 1 - ng; s <= n + ng; ++s) {
+        size_t p = cell(s);
+        rho_i[ix(s)] = 1.0 / v[p];
+        uu[d][ix(s)] = v[(1 + d) * nc + p] * rho_i[ix(s)];
+        P[ix(s)] = v[p] * T[p] * W_i[p];
+        if (P[ix(s)] <= 0.0) {
+#pragma omp atomic write
+          negp = true;
+        }
+        gam[ix(s)] = t.gam2 * W_i[p] / cp[p];
+        gam[ix(s)] = 1.0 / (1.0 - gam[ix(s)]);
+        cs[ix(s)] = std::sqrt(gam[ix(s)] * P[ix(s)] * rho_i[ix(s)]);
+      }
+      for (int s = 0; s <= n + 1; ++s) {
+        size_t p = cell(s);
+        uu[t1][ix(s)] = v[(1 + t1) * nc + p] * rho_i[ix(s)];
+        uu[t2][ix(s)] = v[(1 + t2) * nc + p] * rho_i[ix(s)];
+        for (int l = 0; l < nrv; ++l) Ya[ix(s) * nrv + l] = v[(NIV + l) * nc + p] * rho_i[ix(s)];
+        double h = 0.0;
+        for (int l = 0; l < nrv; ++l) h = h + ha[l * nc + p] * Ya[ix(s) * nrv + l];
+        double ux = uu[0][ix(s)], vy = uu[1][ix(s)], wz = uu[2][ix(s)];
+        ht[ix(s)] = h + 0.5 * (ux * ux + vy * vy + wz * wz);
+        et[ix(s)] = v[4 * nc + p] * rho_i[ix(s)];
+      }
+      double f_s[8][2 * IZEM_NSMAX + 6], L_s[8][2 * IZEM_NSMAX + 6];
+      double el[IZEM_NSMAX + 5][IZEM_NSMAX + 5], er[IZEM_NSMAX + 5][IZEM_NSMAX + 5];
+      double gplus[8], gminus[8], ghat[IZEM_NSMAX + 5];
+      for (int il = 0; il <= n; ++il) {
+        int ir = il + 1;
+        for (int st = 1; st <= st_m1; ++st) {
+          int is = il + st - ng;
+          size_t p = cell(is);
+          double un = uu[d][ix(is)];
+          f_s[st][0] = v[(1 + d) * nc + p];
+          for (int a = 0; a < 3; ++a) f_s[st][1 + a] = v[(1 + a) * nc + p] * un;
+          f_s[st][1 + d] = v[(1 + d) * nc + p] * un + P[ix(is)];
+          f_s[st][4] = un * (v[4 * nc + p] + P[ix(is)]);
+          for (int l = NIV; l < nv; ++l) f_s[st][l] = v[l * nc + p] * un;
+          L_s[st][0] = std::fabs(un - cs[ix(is)]);
+          L_s[st][1] = std::fabs(un);
+          L_s[st][2] = std::fabs(un + cs[ix(is)]);
+          for (int l = 3; l < nv; ++l) L_s[st][l] = L_s[st][1];
+        }
+        // Roe's average (module_weno.f90:726-761)
+        size_t pl = cell(il), pr = cell(ir);
+        double r = std::sqrt(v[pr] * rho_i[ix(il)]);
+        double r1 = 1.0 / (r + 1.0);
+        double uc[3];
+        for (int a = 0; a < 3; ++a) uc[a] = (r * uu[a][ix(ir)] + uu[a][ix(il)]) * r1;
+        double Yc[IZEM_NSMAX];
+        for (int l = 0; l < nrv; ++l) Yc[l] = (r * (Ya[ix(ir) * nrv + l]) + Ya[ix(il) * nrv + l]) * r1;
+        double ht_c = (r * ht[ix(ir)] + ht[ix(il)]) * r1;
+        double et_c = (r * et[ix(ir)] + et[ix(il)]) * r1;
+        (void)pl;
+        double W_i_c = 0.0;
+        for (int l = 0; l < nrv; ++l) W_i_c = W_i_c + Yc[l] * t.Wc_i[l];
+        double T_c = (ht_c - et_c) / W_i_c;
+        double cp_c = cp_scalar(t, T_c, Yc);
+        double gam_c = t.gam2 * W_i_c / cp_c;
+        gam_c = 1.0 / (1.0 - gam_c);
+        double cs_c = std::sqrt(gam_c * T_c * W_i_c);
+        double ha_c[IZEM_NSMAX], psi_c[IZEM_NSMAX];
+        ha_scalar(t, T_c, ha_c);
+        double wrk = (gam_c / (gam_c - 1.0)) * T_c;
+        for (int l = 0; l < nrv; ++l) {
+          psi_c[l] = -(r * ha_c[l] + ha_c[l]) * r1;
+          psi_c[l] = psi_c[l] + wrk * t.Wc_i[l];
+        }
+        double cs_c_i = 1.0 / cs_c, cs_c_2 = cs_c * cs_c;
+        double q = 0.5 * (uc[0] * uc[0] + uc[1] * uc[1] + uc[2] * uc[2]);
+        double b2 = (gam_c - 1.0) / cs_c_2;
+        double b1 = b2 * q;
+        double xi = b1 - b2 * ht_c;
+        double un = uc[d];
+        // left eigenvectors (module_weno.f90:775-874)
+        for (int a = 0; a < nv; ++a)
+          for (int e = 0; e < nv; ++e) el[a][e] = 0.0;
+        el[0][0] = 0.5 * (b1 + un * cs_c_i);
+        el[2][0] = 0.5 * (b1 - un * cs_c_i);
+        for (int a = 0; a < 3; ++a) {
+          if (a == d) {
+            el[0][1 + a] = -0.5 * (b2 * un + cs_c_i);
+            el[2][1 + a] = -0.5 * (b2 * un - cs_c_i);
+          } else {
+            el[0][1 + a] = -0.5 * (b2 * uc[a]);
+            el[2][1 + a] = -0.5 * (b2 * uc[a]);
+          }
+          el[1][1 + a] = b2 * uc[a];
+        }
+        el[0][4] = 0.5 * b2; el[2][4] = 0.5 * b2;
+        el[1][0] = 1.0 - b1; el[1][4] = -b2;
+        el[3][0] = -uc[t1]; el[3][1 + t1] = 1.0;
+        el[4][0] = -uc[t2]; el[4][1 + t2] = 1.0;
+        wrk = 0.5 * b2;
+        for (int l = NIV; l < nv; ++l) el[0][l] = wrk * psi_c[l - NIV];
+        for (int l = NIV; l < nv; ++l) el[1][l] = -el[0][l] - el[0][l];
+        for (int l = NIV; l < nv; ++l) el[2][l] = el[0][l];
+        el[5][0] = (1 + xi) * q;
+        for (int a = 0; a < 3; ++a) el[5][1 + a] = -(1 + xi) * uc[a];
+        el[5][4] = (1 + xi);
+        for (int l = NIV; l < nv; ++l) el[5][l] = xi * psi_c[l - NIV];
+        for (int l = 6; l < nv; ++l) {
+          double Y = Yc[l - 6];
+          el[l][0] = -b1 * Y;
+          for (int a = 0; a < 3; ++a) el[l][1 + a] = b2 * uc[a] * Y;
+          el[l][4] = -b2 * Y;
+        }
+        for (int s1 = 1; s1 <= nrv - 1; ++s1)
+          for (int s2 = 1; s2 <= nrv; ++s2) el[s1 + 5][s2 + 4] = -b2 * Yc[s1 - 1] * psi_c[s2 - 1];
+        for (int l = 1; l <= nrv - 1; ++l) el[l + 5][l + 4] = el[l + 5][l + 4] + 1.0;
+        // right eigenvectors (module_weno.f90:881-951)
+        for (int a = 0; a < nv; ++a)
+          for (int e = 0; e < nv; ++e) er[a][e] = 0.0;
+        er[0][0] = 1.0; er[0][1] = 1.0; er[0][2] = 1.0;
+        er[1 + d][0] = un - cs_c; er[1 + d][1] = un; er[1 + d][2] = un + cs_c;
+        er[1 + t1][0] = uc[t1]; er[1 + t1][1] = uc[t1]; er[1 + t1][2] = uc[t1]; er[1 + t1][3] = 1.0;
+        er[1 + t2][0] = uc[t2]; er[1 + t2][1] = uc[t2]; er[1 + t2][2] = uc[t2]; er[1 + t2][4] = 1.0;
+        er[4][0] = ht_c - un * cs_c; er[4][1] = q; er[4][2] = ht_c + un * cs_c; er[4][3] = uc[t1]; er[4][4] = uc[t2];
+        for (int l = NIV; l < nv; ++l) { er[l][0] = Yc[l - NIV]; er[l][2] = Yc[l - NIV]; }
+        for (int l = NIV + 1; l <= nv; ++l) er[l - 2][l - 1] = 1.0;
+        er[nv - 1][5] = -1.0 / psi_c[nrv - 1];
+        wrk = -1.0 / psi_c[nrv - 1];
+        for (int l = 1; l <= nrv - 1; ++l) er[nv - 1][l + 5] = wrk * psi_c[l - 1];
+        // characteristic LLF-WENO (module_weno.f90:953-989)
+        bool shk = false;
+        for (int s = il - ng + 1; s <= il + ng; ++s) shk = shk || (sensor[cell(s)] != 0);
+        shk = shk && c.cfg.weno_avg;
+        for (int m = 0; m < nv; ++m) {
+          double eigenmax = -1.0;
+          for (int st = 1; st <= st_m1; ++st) eigenmax = std::max(L_s[st][m], eigenmax);
+          for (int st = 1; st <= st_m1; ++st) {
+            double wc = 0.0, gc = 0.0;
+            int is = il + st - ng;
+            size_t p = cell(is);
+            for (int mm = 0; mm < nv; ++mm) {
+              wc = wc + el[m][mm] * v[mm * nc + p];
+              gc = gc + el[m][mm] * f_s[st][mm];
+            }
+            gplus[st] = 0.5 * (gc + eigenmax * wc);
+            gminus[st] = gc - gplus[st];
+          }
+          double gl, gr;
+          if (shk) wenorec(w, gplus, gminus, gl, gr);
+          else wenorec_nw(gplus, gminus, gl, gr, fixlin);
+          ghat[m] = gl + gr;
+        }
+        for (int m = 0; m < nv; ++m) {
+          double fh = 0.0;
+          for (int mm = 0; mm < nv; ++mm) fh = fh + er[m][mm] * ghat[mm];
+          fhat[il * nv + m] = fh;
+        }
+      }
+      for (int m = 0; m < nv; ++m)
+        for (int s = 1; s <= n; ++s) {
+          double df = (fhat[s * nv + m] - fhat[(s - 1) * nv + m]) * di[s - 1 + ng];
+          int i, j, k;
+          if (d == 0) { i = s; j = q1; k = q2; }
+          else if (d == 1) { i = q1; j = s; k = q2; }
+          else { i = q1; j = q2; k = s; }
+          size_t f = (size_t)m * b.nint + b.fid(i, j, k);
+          if (d == 0) fl[f] = df * 1.0;
+          else fl[f] = fl[f] + df * 1.0;
+        }
+    }
+  if (negp) {
+    c.err = "negative pressure in euler_LLF";
+    return IZEM_ERR_NEG_PRESSURE;
+  }
+  return IZEM_OK;
+}
+
+// shock_sensor_modified_adams_shariff (module_tools.f90:2733-2814)
+void shock_sensor(const Ctx& c, const double* v, const double* T, const double* W_i, uint8_t* sensor) {
+  const Block& b = c.b;
+  const double mrw = c.cfg.max_rel_weight;
+  std::vector<double> rho_i(b.ncell, 0.0), P(b.ncell, 0.0);
+  for (int k = 1; k <= b.nz; ++k)
+    for (int j = 1; j <= b.ny; ++j)
+      for (int i = 1; i <= b.nx; ++i) {
+        size_t p = b.id(i, j, k);
+        rho_i[p] = 1.0 / v[p];
+        P[p] = v[p] * T[p] * W_i[p];
+      }
+  auto test = [&](size_t p, size_t q) {
+    double drho = std::fabs(v[q] - v[p]) * std::min(rho_i[p], rho_i[q]);
+    double dpres = std::fabs(P[q] - P[p]) / std::min(P[p], P[q]);
+    if (drho > mrw && dpres > mrw) sensor[p] = 1;
+  };
+  for (int k = 1; k <= b.nz; ++k)
+    for (int j = 1; j <= b.ny; ++j)
+      for (int i = 1; i <= b.nx - 1; ++i) test(b.id(i, j, k), b.id(std::min(i + 1, b.nx), j, k));
+  for (int k = 1; k <= b.nz; ++k)
+    for (int i = 1; i <= b.nx; ++i)
+      for (int j = 1; j <= b.ny - 1; ++j) test(b.id(i, j, k), b.id(i, std::min(j + 1, b.ny), k));
+  for (int i = 1; i <= b.nx; ++i)
+    for (int j = 1; j <= b.ny; ++j)
+      for (int k = 1; k <= b.nz - 1; ++k) test(b.id(i, j, k), b.id(i, j, std::min(k + 1, b.nz)));
+}
+
+// prim_vis_vars (module_thermodynamics.f90:989-1230) for one point
+void prim_vis_point(const Ctx& c, double rho, double T, double W_i, const double* Xa, double* dm, double* mu, double* ct) {
+  const izem_thd& t = c.thd;
+  const int ns = c.b.nrv;
+  const double epsm12 = 1.0e-12;
+  const double Kl = 0.5 * 1.0e-5 / t.laminf;
+  const double Ku = 1.0e-1 / t.muinf;
+  double lt[4];
+  lt[0] = 1.0;
+  lt[1] = std::log(T * t.tinf);
+  lt[2] = lt[1] * lt[1];
+  lt[3] = lt[2] * lt[1];
+  double P = rho * T * W_i;
+  for (int m = 0; m < ns; ++m) {
+    double wrk1 = 0.0, dsum = 0.0;
+    for (int l = 0; l < ns; ++l) {
+      if (m != l) {
+        double dkj = 0.0;
+        for (int n = 0; n < 4; ++n) dkj = dkj + t.cofd[m][l][n] * lt[n];
+        wrk1 = wrk1 + (Xa[l] + epsm12) * t.Wc[l] * W_i;
+        dsum = dsum + (Xa[l] + epsm12) * (1.0 / std::exp(dkj));
+      }
+    }
+    double Kd = 1.0e-4 * t.p0 / (t.pinf * t.dinf[m]);
+    dm[m] = wrk1 * Kd / (dsum * P);
+  }
+  double ctsum = 0.0, w1 = 0.0, wrk2[IZEM_NSMAX];
+  for (int l = 0; l < ns; ++l) {
+    double a = 0.0;
+    for (int m = 0; m < 4; ++m) a = a + t.coflam[l][m] * lt[m];
+    double c1 = std::exp(a);
+    double c2 = Xa[l];
+    ctsum = ctsum + c2 / c1;
+    w1 = w1 + c2 * c1;
+  }
+  *ct = Kl * (1.0 / ctsum + w1);
+  for (int l = 0; l < ns; ++l) {
+    double a = 0.0;
+    for (int m = 0; m < 4; ++m) a = a + t.cofeta[l][m] * lt[m];
+    wrk2[l] = std::exp(a);
+  }
+  double mus = 0.0;
+  for (int m = 0; m < ns; ++m) {
+    double c4 = 0.0;
+    for (int l = 0; l < ns; ++l) {
+      double c1 = std::pow(t.W[l] / t.W[m], 0.25);
+      double c2 = 1.0 / std::sqrt((1.0 + t.W[m] / t.W[l]) * 8.0);
+      double c3 = 1.0 + c1 * std::sqrt(wrk2[m] / wrk2[l]);
+      c2 = c3 * c3 * c2;
+      c4 = c4 + c2 * Xa[l];
+    }
+    mus = mus + Ku * (wrk2[m] * Xa[m] / c4);
+  }
+  *mu = mus;
+}
+
+// viscflux_xyz (module_viscflux.f90:1660-2189)
+int visc_flux(Ctx& c, const double* v, const double* T, const double* W_i, const double* cp, const double* ha, double* fl) {
+  (void)cp;
+  const Block& b = c.b;
+  const izem_thd& t = c.thd;
+  const izem_adi& a = c.adi;
+  const int nrv = b.nrv;
+  const size_t nc = b.ncell;
+  const int nfluid = 12, nderiv = nfluid + 3 * nrv;
+  const double twothirds = 2.0 / 3.0;
+  const double rvd0 = a.sqgmr / a.sc, rlam0 = a.sqgmr * a.ggmopr;
+  std::vector<double> ux(nc, 0.0), vy(nc, 0.0), wz(nc, 0.0), Xa(nc * nrv, 0.0);
+  std::vector<double> fd(nc * nderiv, std::nan(""));
+  for (int dom = -3; dom <= 3; ++dom) {
+    int i0, i1, j0, j1, k0, k1;
+    domain_select(b, dom, i0, i1, j0, j1, k0, k1);
+    for (int k = k0; k <= k1; ++k)
+      for (int j = j0; j <= j1; ++j)
+        for (int i = i0; i <= i1; ++i) {
+          size_t p = b.id(i, j, k);
+          for (int l = 0; l < nrv; ++l) Xa[l * nc + p] = v[(NIV + l) * nc + p] / (v[p] * W_i[p] * t.Wc[l]);
+          double rho_i = 1.0 / v[p];
+          ux[p] = v[nc + p] * rho_i;
+          vy[p] = v[2 * nc + p] * rho_i;
+          wz[p] = v[3 * nc + p] * rho_i;
+        }
+  }
+  const double* src[4] = {ux.data(), vy.data(), wz.data(), T};
+  for (int s = 0; s < 4; ++s)
+    for (int d = 0; d < 3; ++d) deriv(c, d, src[s], fd.data() + (size_t)(3 * s + d) * nc, false);
+  for (int l = 0; l < nrv; ++l)
+    for (int d = 0; d < 3; ++d) deriv(c, d, Xa.data() + (size_t)l * nc, fd.data() + (size_t)(nfluid + 3 * l + d) * nc, false);
+  comm_periodic(b, nderiv, fd.data(), nc);   // comm_deriv
+
+  std::vector<double> sxx(nc, 0.0), sxy(nc, 0.0), sxz(nc, 0.0), syy(nc, 0.0), syz(nc, 0.0), szz(nc, 0.0);
+  std::vector<double> qx(nc, 0.0), qy(nc, 0.0), qz(nc, 0.0);
+  for (int dom = -3; dom <= 3; ++dom) {
+    int i0, i1, j0, j1, k0, k1;
+    domain_select(b, dom, i0, i1, j0, j1, k0, k1);
+    // a non-periodic face has no ghost stresses in use; skip its slab
+    if (dom != 0) {
+      int f = dom < 0 ? 2 * (-dom - 1) : 2 * (dom - 1) + 1;
+      if (b.bnd[f]) continue;
+    }
+    for (int k = k0; k <= k1; ++k)
+      for (int j = j0; j <= j1; ++j)
+        for (int i = i0; i <= i1; ++i) {
+          size_t p = b.id(i, j, k);
+          double X[IZEM_NSMAX], dm[IZEM_NSMAX], mu, ct;
+          for (int l = 0; l < nrv; ++l) X[l] = Xa[l * nc + p];
+          prim_vis_point(c, v[p], T[p], W_i[p], X, dm, &mu, &ct);
+          auto F = [&](int idx) -> double& { return fd[(size_t)(idx - 1) * nc + p]; };
+          double rho_i = 1.0 / v[p];
+          double uxs = v[nc + p] * rho_i, vys = v[2 * nc + p] * rho_i, wzs = v[3 * nc + p] * rho_i;
+          double rmu = -a.sqgmr * mu;
+          double rvd = rvd0 * v[p];
+          sxx[p] = twothirds * rmu * (F(1) + F(1) - (F(5) + F(9)));
+          sxy[p] = rmu * (F(4) + F(2));
+          sxz[p] = rmu * (F(7) + F(3));
+          syy[p] = twothirds * rmu * (F(5) + F(5) - (F(1) + F(9)));
+          syz[p] = rmu * (F(8) + F(6));
+          szz[p] = twothirds * rmu * (F(9) + F(9) - (F(1) + F(5)));
+          double vdcx = 0.0, vdcy = 0.0, vdcz = 0.0;
+          for (int l = 1; l <= nrv; ++l) {
+            double wrk = dm[l - 1] * t.Wc[l - 1] * W_i[p];
+            vdcx = vdcx + wrk * F(nfluid + 3 * l - 2);
+            vdcy = vdcy + wrk * F(nfluid + 3 * l - 1);
+            vdcz = vdcz + wrk * F(nfluid + 3 * l);
+          }
+          double vdhx = 0.0, vdhy = 0.0, vdhz = 0.0;
+          for (int l = 1; l <= nrv; ++l) {
+            double Ya = v[(NIV + l - 1) * nc + p] * rho_i;
+            double vdtx = vdcx * Ya, vdty = vdcy * Ya, vdtz = vdcz * Ya;
+            double wrk = -dm[l - 1] * t.Wc[l - 1] * W_i[p];
+            vdtx = vdtx + wrk * F(nfluid + 3 * l - 2);
+            vdty = vdty + wrk * F(nfluid + 3 * l - 1);
+            vdtz = vdtz + wrk * F(nfluid + 3 * l);
+            F(nfluid + 3 * l - 2) = rvd * vdtx;
+            F(nfluid + 3 * l - 1) = rvd * vdty;
+            F(nfluid + 3 * l) = rvd * vdtz;
+            double h = ha[(l - 1) * nc + p];
+            vdhx = vdhx + h * F(nfluid + 3 * l - 2);
+            vdhy = vdhy + h * F(nfluid + 3 * l - 1);
+            vdhz = vdhz + h * F(nfluid + 3 * l);
+          }
+          double rlam = -rlam0 * ct;
+          qx[p] = uxs * sxx[p] + vys * sxy[p] + wzs * sxz[p] + rlam * F(10) + vdhx;
+          qy[p] = uxs * sxy[p] + vys * syy[p] + wzs * syz[p] + rlam * F(11) + vdhy;
+          qz[p] = uxs * sxz[p] + vys * syz[p] + wzs * szz[p] + rlam * F(12) + vdhz;
+        }
+  }
+  const size_t ni = b.nint;
+  std::vector<double> wx(ni), wy(ni), wzv(ni);
+  auto accum = [&](int var, const double* ax, const double* ay, const double* az) {
+    deriv(c, 0, ax, wx.data(), true);
+    deriv(c, 1, ay, wy.data(), true);
+    deriv(c, 2, az, wzv.data(), true);
+    for (size_t p = 0; p < ni; ++p) fl[var * ni + p] = fl[var * ni + p] + (wx[p] + wy[p] + wzv[p]);
+  };
+  accum(1, sxx.data(), sxy.data(), sxz.data());
+  accum(2, sxy.data(), syy.data(), syz.data());
+  accum(3, sxz.data(), syz.data(), szz.data());
+  accum(4, qx.data(), qy.data(), qz.data());
+  for (int l = 0; l < nrv; ++l)
+    accum(NIV + l, fd.data() + (size_t)(nfluid + 3 * l) * nc, fd.data() + (size_t)(nfluid + 3 * l + 1) * nc,
+          fd.data() + (size_t)(nfluid + 3 * l + 2) * nc);
+  return IZEM_OK;
+}
+
+// rk3 (module_solver.f90:694-856)
+int rk3(Ctx& c, double dt, double* v, double* T, double* W_i, double* cp, double* ha, uint8_t* sensor) {
+  const Block& b = c.b;
+  const double bk3[3] = {0.00, 0.75, 1.00 / 3.00};
+  const double ck3[3] = {1.00, 0.25, 2.00 / 3.00};
+  const size_t ni = b.nint, nc = b.ncell;
+  std::vector<double> v0(ni * b.nv), f(ni * b.nv, 0.0);
+  for (int l = 0; l < b.nv; ++l)
+    for (int k = 1; k <= b.nz; ++k)
+      for (int j = 1; j <= b.ny; ++j)
+        for (int i = 1; i <= b.nx; ++i) v0[l * ni + b.fid(i, j, k)] = v[l * nc + b.id(i, j, k)];
+  for (int ik = 0; ik < 3; ++ik) {
+    shock_sensor(c, v, T, W_i, sensor);
+    int rc;
+    for (int d = 0; d < 3; ++d)
+      if ((rc = euler_flux(c, d, v, T, W_i, cp, ha, sensor, f.data()))) return rc;
+    if (c.cfg.vis)
+      if ((rc = visc_flux(c, v, T, W_i, cp, ha, f.data()))) return rc;
+    for (int l = 0; l < b.nv; ++l)
+      for (int k = 1; k <= b.nz; ++k)
+        for (int j = 1; j <= b.ny; ++j)
+          for (int i = 1; i <= b.nx; ++i) {
+            size_t p = l * nc + b.id(i, j, k), q = l * ni + b.fid(i, j, k);
+            v[p] = v0[q] * bk3[ik] + ck3[ik] * (v[p] - dt * f[q]);
+          }
+    if ((rc = update_primitives(c, v, T, W_i, cp, ha))) return rc;
+  }
+  return IZEM_OK;
+}
+
+// timestep (module_solver.f90:202-408): convective and chemical criteria
+void timestep(const Ctx& c, double DTmax, const double* v, const double* T, const double* W_i, const double* cp,
+              double* dt4, double* dtmin) {
+  const Block& b = c.b;
+  const izem_thd& t = c.thd;
+  double dtc = 1.0;
+  for (int q = 0; q < 4; ++q) dt4[q] = 1.0;
+  for (int k = 1; k <= b.nz; ++k)
+    for (int j = 1; j <= b.ny; ++j)
+      for (int i = 1; i <= b.nx; ++i) {
+        size_t p = b.id(i, j, k), nc = b.ncell;
+        double rho_i = 1.0 / v[p];
+        double ux = v[nc + p] * rho_i, vy = v[2 * nc + p] * rho_i, wz = v[3 * nc + p] * rho_i;
+        double gamma = t.gam2 * W_i[p] / cp[p];
+        gamma = 1.0 / (1.0 - gamma);
+        double P = v[p] * T[p] * W_i[p];
+        double csound = std::sqrt(gamma * P * rho_i);
+        double ax = (std::fabs(ux) + csound) * c.dxi[0][i - 1 + b.ng];
+        double ay = (std::fabs(vy) + csound) * c.dxi[1][j - 1 + b.ng];
+        double az = (std::fabs(wz) + csound) * c.dxi[2][k - 1 + b.ng];
+        dtc = std::max(std::max(std::max(dtc, ax), ay), az);
+      }
+  dt4[0] = c.cfg.cfl / dtc;
+  if (c.cfg.reaction) {
+    dt4[3] = *dtmin * c.cfg.cpr / DTmax;
+    dt4[3] = std::min(dt4[3], 1.0);
+    dt4[3] = std::max(dt4[3], dt4[0] * c.cfg.cflmin / c.cfg.cfl);
+  }
+  *dtmin = std::min(std::min(dt4[0], dt4[1]), std::min(dt4[2], dt4[3]));
+}
+
+}  // namespace
+
+// ============================================================== C API =====
+extern "C" {
+
+void* or_create(const izem_cfg* cfg, const izem_thd* thd, const izem_adi* adi, const double* dx_i,
+                const double* dy_i, const double* dz_i) {
+  if (!cfg || !thd || !adi || cfg->ng != 3 || cfg->nrv < 2 || cfg->nrv > IZEM_NSMAX) return nullptr;
+  Ctx* c = new Ctx();
+  c->cfg = *cfg;
+  c->thd = *thd;
+  c->adi = *adi;
+  Block& b = c->b;
+  b.nx = cfg->nx; b.ny = cfg->ny; b.nz = cfg->nz; b.ng = cfg->ng; b.nrv = cfg->nrv; b.nv = NIV + cfg->nrv;
+  b.gx = b.nx + 2 * b.ng; b.gy = b.ny + 2 * b.ng; b.gz = b.nz + 2 * b.ng;
+  b.ncell = (size_t)b.gx * b.gy * b.gz;
+  b.nint = (size_t)b.nx * b.ny * b.nz;
+  for (int f = 0; f < 6; ++f) {
+    b.bc[f] = cfg->bc[f];
+    b.bnd[f] = cfg->bc[f] != IZEM_BC_PERIODIC;
+  }
+  const double* di[3] = {dx_i, dy_i, dz_i};
+  for (int d = 0; d < 3; ++d) c->dxi[d].assign(di[d], di[d] + b.n(d) + 2 * b.ng);
+  return c;
+}
+
+void or_destroy(void* h) { delete static_cast<Ctx*>(h); }
+
+int or_last_error(void* h, char* buf, int n) {
+  Ctx* c = static_cast<Ctx*>(h);
+  if (buf && n > 0) { std::snprintf(buf, n, "%s", c->err.c_str()); }
+  return c->newton_warn;
+}
+
+void or_cp_scalar(void* h, double T, const double* Y, double* cp) { *cp = cp_scalar(static_cast<Ctx*>(h)->thd, T, Y); }
+void or_ha_scalar(void* h, double T, double* ha) { ha_scalar(static_cast<Ctx*>(h)->thd, T, ha); }
+
+int or_shock_sensor(void* h, const double* v, const double* T, const double* W_i, uint8_t* sensor) {
+  shock_sensor(*static_cast<Ctx*>(h), v, T, W_i, sensor);
+  return 0;
+}
+int or_euler_flux(void* h, int dir, const double* v, const double* T, const double* W_i, const double* cp,
+                  const double* ha, const uint8_t* sensor, double* fl) {
+  return euler_flux(*static_cast<Ctx*>(h), dir, v, T, W_i, cp, ha, sensor, fl);
+}
+int or_visc_flux(void* h, const double* v, const double* T, const double* W_i, const double* cp,
+                 const double* ha, double* fl) {
+  return visc_flux(*static_cast<Ctx*>(h), v, T, W_i, cp, ha, fl);
+}
+int or_prim_inv_var(void* h, int dom, int err_mach, double* v, double* W_i, double* T, double* cp, double* ha) {
+  return prim_inv_var(*static_cast<Ctx*>(h), dom, err_mach != 0, v, W_i, T, cp, ha);
+}
+int or_force_sumY(void* h, int dom, double* v) {
+  force_sumY(*static_cast<Ctx*>(h), dom, v);
+  return 0;
+}
+int or_update_primitives(void* h, double* v, double* T, double* W_i, double* cp, double* ha) {
+  return update_primitives(*static_cast<Ctx*>(h), v, T, W_i, cp, ha);
+}
+int or_finalize_ic(void* h, double* v, double* T, double* W_i, double* cp, double* ha) {
+  return finalize_ic(*static_cast<Ctx*>(h), v, T, W_i, cp, ha);
+}
+int or_rk3(void* h, double dt, double* v, double* T, double* W_i, double* cp, double* ha, uint8_t* sensor) {
+  return rk3(*static_cast<Ctx*>(h), dt, v, T, W_i, cp, ha, sensor);
+}
+int or_timestep(void* h, double DTmax, const double* v, const double* T, const double* W_i, const double* cp,
+                double* dt4, double* dtmin) {
+  timestep(*static_cast<Ctx*>(h), DTmax, v, T, W_i, cp, dt4, dtmin);
+  return 0;
+}
+
+// dscalar + inversion (module_deriv.f90:80-205, module_tools.f90:374-426)
+void or_metrics_dscalar(int n, int ng, const double* coord, double* d_i) {
+  (void)ng;
+  std::vector<double> dv(n, 1.0);
+  auto v = [&](int m) { return coord[m - 1]; };
+  for (int m = 1 + 3; m <= n - 3; ++m) {
+    double dd = 0.0;
+    for (int l = -3; l <= 3; ++l) dd = dd + alpha6[l + 3] * v(m + l);
+    dv[m - 1] = dd * 1.0;
+  }
+  { int m = 1; double dd = 0.0; for (int l = 0; l <= 4; ++l) dd = dd + alph4ol[l] * v(m + l); dv[m - 1] = dd * 1.0; }
+  { int m = 2; double dd = 0.0; for (int l = -1; l <= 3; ++l) dd = dd + alph4ul[l + 1] * v(m + l); dv[m - 1] = dd * 1.0; }
+  { int m = 3; double dd = 0.0; for (int l = -2; l <= 2; ++l) dd = dd + alph4[l + 2] * v(m + l); dv[m - 1] = dd * 1.0; }
+  { int m = n - 2; double dd = 0.0; for (int l = -2; l <= 2; ++l) dd = dd + alph4[l + 2] * v(m + l); dv[m - 1] = dd * 1.0; }
+  { int m = n - 1; double dd = 0.0; for (int l = -3; l <= 1; ++l) dd = dd + alph4ur[l + 3] * v(m + l); dv[m - 1] = -dd * 1.0; }
+  { int m = n; double dd = 0.0; for (int l = -4; l <= 0; ++l) dd = dd + alph4or[l + 4] * v(m + l); dv[m - 1] = -dd * 1.0; }
+  for (int m = 0; m < n; ++m) d_i[m] = 1.0 / dv[m];
+}
+
+}  // extern "C"

@@ -1,0 +1,69 @@
+"""ctypes mirror of include/izem_gpu.h (structures and status codes).
+
+The layout of every structure here must match the C header field for field;
+tests/test_capi_layout.py checks the sizes against the compiled library.
+"""
+import ctypes as C
+
+NSMAX = 10
+NPOLY = 4
+
+BC_PERIODIC = 0
+BC_EXTRAPOLATION = 1
+
+OK = 0
+ERR_ARG = 1
+ERR_CUDA = 2
+ERR_NEG_PRESSURE = 3
+ERR_NEG_TEMPERATURE = 4
+ERR_NAN = 5
+ERR_CHEM = 6
+ERR_TIMEOUT = 7
+ERR_NOMEM = 8
+ERR_STATE = 9
+
+ERR_NAMES = {
+    OK: "ok", ERR_ARG: "bad argument", ERR_CUDA: "CUDA error",
+    ERR_NEG_PRESSURE: "negative pressure", ERR_NEG_TEMPERATURE: "negative temperature",
+    ERR_NAN: "NaN in Newton temperature", ERR_CHEM: "stiff integrator failure",
+    ERR_TIMEOUT: "device wait timed out", ERR_NOMEM: "out of device memory",
+    ERR_STATE: "call out of order",
+}
+
+
+class IzemCfg(C.Structure):
+    _fields_ = [
+        ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
+        ("ng", C.c_int), ("ndim", C.c_int), ("nrv", C.c_int),
+        ("bc", C.c_int * 6),
+        ("weno_avg", C.c_int),
+        ("max_rel_weight", C.c_double),
+        ("vis", C.c_int), ("eglib", C.c_int), ("forcesum", C.c_int),
+        ("reaction", C.c_int), ("vis_dt", C.c_int),
+        ("cfl", C.c_double), ("cflmin", C.c_double), ("cpr", C.c_double), ("fo", C.c_double),
+        ("weno5_linear_fix", C.c_int),
+    ]
+
+
+class IzemThd(C.Structure):
+    _fields_ = [
+        ("nspc", C.c_int),
+        ("gam2", C.c_double), ("tinf", C.c_double),
+        ("pinf", C.c_double), ("p0", C.c_double),
+        ("muinf", C.c_double), ("laminf", C.c_double),
+        ("dinf", C.c_double * NSMAX),
+        ("W", C.c_double * NSMAX), ("Wc", C.c_double * NSMAX), ("Wc_i", C.c_double * NSMAX),
+        ("tpolymin", C.c_double * NSMAX), ("tpolymax", C.c_double * NSMAX),
+        ("tpolylim", C.c_double * NSMAX),
+        ("heatcap", ((C.c_double * 7) * 2) * NSMAX),
+        ("cofd", ((C.c_double * NPOLY) * NSMAX) * NSMAX),
+        ("coflam", (C.c_double * NPOLY) * NSMAX),
+        ("cofeta", (C.c_double * NPOLY) * NSMAX),
+    ]
+
+
+class IzemAdi(C.Structure):
+    _fields_ = [(n, C.c_double) for n in (
+        "gamma_inf", "re", "pr", "le", "ma", "sc", "sqgmr", "ggmopr",
+        "t_ref", "l_ref", "r_ref", "w_ref", "cp_ref", "mu_ref", "c_inf", "u_ref", "time_ref",
+        "rho_ref", "p_ref", "lbda_ref", "d_ref")]

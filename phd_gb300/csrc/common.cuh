@@ -1,0 +1,69 @@
+// Shared device definitions for the IZEM RHS kernels (sm_103a).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+#include "../../include/izem_gpu.h"
+
+#define IZEM_NIV 5
+#define IZEM_NVMAX (IZEM_NIV + IZEM_NSMAX)
+
+// Block geometry: one block of nx*ny*nz interior points with ng ghost layers
+// in the reference's Fortran column-major layout (sx = sy = sz = 1).
+struct Geo {
+  int n[3];
+  int ng;
+  int g[3];        // ghosted extents n+2ng
+  long long ncell; // ghosted points
+  long long nint;  // interior points
+  int bnd[6];      // face is a physical (non-periodic) boundary
+  int bc[6];
+};
+
+__host__ __device__ inline long long gid(const Geo& g, int i, int j, int k) {
+  return (long long)(i - 1 + g.ng) + (long long)g.g[0] * ((long long)(j - 1 + g.ng) + (long long)g.g[1] * (long long)(k - 1 + g.ng));
+}
+__host__ __device__ inline long long fidx(const Geo& g, int i, int j, int k) {
+  return (long long)(i - 1) + (long long)g.n[0] * ((long long)(j - 1) + (long long)g.n[1] * (long long)(k - 1));
+}
+
+// Species data in code units, broadcast from constant memory.  Pairwise
+// constants of the Wilke viscosity rule are precomputed on the host with the
+// same IEEE operations the reference evaluates per point.
+struct DevThd {
+  int nspc;
+  double gam2, gam2_i, tinf, tinf_i, onethird;
+  double Wc[IZEM_NSMAX], Wc_i[IZEM_NSMAX];
+  double tpolymin[IZEM_NSMAX], tpolymax[IZEM_NSMAX], tpolylim[IZEM_NSMAX];
+  double hc[IZEM_NSMAX][2][7];
+  double cofd[IZEM_NSMAX][IZEM_NSMAX][IZEM_NPOLY];
+  double coflam[IZEM_NSMAX][IZEM_NPOLY];
+  double cofeta[IZEM_NSMAX][IZEM_NPOLY];
+  double wilke_c1[IZEM_NSMAX][IZEM_NSMAX];   // (W_l/W_m)^0.25      [m][l]
+  double wilke_c2[IZEM_NSMAX][IZEM_NSMAX];   // 1/sqrt((1+W_m/W_l)*8) [m][l]
+  double Kd[IZEM_NSMAX];
+  double Kl, Ku;
+  // viscous-flux constants (module_viscflux.f90:1717-1719)
+  double sqgmr, rvd0, rlam0;
+};
+
+// One copy per translation unit (whole-program compilation); each unit that
+// uses it uploads the same host structure.
+static __constant__ DevThd c_thd;
+
+// Device status word shared by all kernels of a context.
+struct DevStatus {
+  unsigned long long maxdf_bits[8];  // per sub-domain max dT^2 (bit pattern of a non-negative double)
+  int it[8];
+  int done[8];
+  int neg_pressure;
+  int neg_temperature;
+  int newton_nan;
+  int newton_unconverged;
+  unsigned long long dtc_bits;       // timestep: max (|u|+c)/dx (bit pattern)
+  int timeout;
+  int chem_fail;
+};
+
+__device__ inline void atomic_max_nonneg(unsigned long long* addr, double v) {
+  atomicMax(addr, (unsigned long long)__double_as_longlong(v));
+}

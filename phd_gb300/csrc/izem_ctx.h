@@ -1,0 +1,44 @@
+// Host-side context of the IZEM GPU library (one per block / per process).
+#pragma once
+#include <string>
+#include <vector>
+#include <utility>
+#include <cuda_runtime.h>
+#include "common.cuh"
+
+struct izem_ctx {
+  izem_cfg cfg;
+  izem_thd thd;
+  izem_adi adi;
+  DevThd devthd;
+  Geo g;
+  int nv = 0;
+  cudaStream_t stream = nullptr;
+  // device state (reference layout) and scratch
+  double *v = nullptr, *T = nullptr, *W_i = nullptr, *cp = nullptr, *ha = nullptr;
+  double *v0 = nullptr, *f = nullptr, *prim = nullptr, *Xa = nullptr, *fhat = nullptr;
+  double *fd = nullptr, *tau = nullptr, *qv = nullptr, *d_dt = nullptr;
+  double* dxi[3] = {nullptr, nullptr, nullptr};
+  uint8_t* sensor = nullptr;
+  DevStatus* d_status = nullptr;
+  DevStatus* h_status = nullptr;
+  double* h_dt = nullptr;
+  std::vector<double*> allocs;
+  bool grid_set = false;
+  // CUDA graph of one RK3 step
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
+  bool capturing = false;
+  // timing
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
+  bool kt_enabled = false;
+  std::vector<std::string> kt_names;
+  std::vector<int> kt_launches;
+  std::vector<double> kt_ms;
+  std::vector<std::vector<std::pair<cudaEvent_t, cudaEvent_t>>> kt_pending;
+  int newton_warn = 0;
+  std::string err;
+};
+
+int ctx_alloc(izem_ctx* c);
+int ctx_fail(izem_ctx* c, int code, const char* what, cudaError_t e);

@@ -1,0 +1,627 @@
+// C-ABI context of the GB300 IZEM RHS library: device-resident state, kernel
+// sequencing of one SSP-RK3 step, CUDA-graph capture, timing and status.
+//
+// Reference sequencing: rk3 (module_solver.f90:694-856) calls the shock
+// sensor, euler_LLF_x/y/z, viscflux_xyz, the stage update, then
+// upd_prim_var_domain, comm_cons, upd_boundaries and upd_prim_var_ghost.
+#include <cstdio>
+#include <cstring>
+#include <cmath>
+#include <string>
+#include <vector>
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+#include "thermo.cuh"
+#include "kernels_euler.cuh"
+#include "kernels_visc.cuh"
+#include "kernels_state.cuh"
+#include "izem_ctx.h"
+
+
+
+namespace {
+
+constexpr int kThreads = 128;
+constexpr int kNewtonIters = 12;   // Newton iterations captured per sub-domain and stage
+
+unsigned grid_for(long long n, int threads = kThreads) { return (unsigned)((n + threads - 1) / threads); }
+
+}  // namespace
+
+// ------------------------------------------------------------ helpers -------
+int ctx_fail(izem_ctx* c, int code, const char* what, cudaError_t e) {
+  char buf[512];
+  if (e != cudaSuccess) std::snprintf(buf, sizeof(buf), "%s: %s", what, cudaGetErrorString(e));
+  else std::snprintf(buf, sizeof(buf), "%s", what);
+  c->err = buf;
+  return code;
+}
+
+#define CK(call)                                                        \
+  do {                                                                  \
+    cudaError_t e_ = (call);                                            \
+    if (e_ != cudaSuccess) return ctx_fail(c, IZEM_ERR_CUDA, #call, e_); \
+  } while (0)
+
+int kt_id(izem_ctx* c, const char* name) {
+  for (size_t q = 0; q < c->kt_names.size(); ++q)
+    if (c->kt_names[q] == name) return (int)q;
+  c->kt_names.push_back(name);
+  c->kt_launches.push_back(0);
+  c->kt_ms.push_back(0.0);
+  c->kt_pending.push_back({});
+  return (int)c->kt_names.size() - 1;
+}
+
+// Launch wrapper: with kernel timing on, bracket the launch by events on the
+// context stream and keep the pair for later accumulation.
+template <typename F>
+int launch(izem_ctx* c, const char* name, F&& fn) {
+  if (c->kt_enabled && !c->capturing) {
+    int id = kt_id(c, name);
+    cudaEvent_t a, b;
+    CK(cudaEventCreate(&a));
+    CK(cudaEventCreate(&b));
+    CK(cudaEventRecord(a, c->stream));
+    fn();
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(b, c->stream));
+    c->kt_pending[id].push_back({a, b});
+    return IZEM_OK;
+  }
+  fn();
+  CK(cudaGetLastError());
+  return IZEM_OK;
+}
+
+int kt_collect(izem_ctx* c) {
+  for (size_t q = 0; q < c->kt_names.size(); ++q) {
+    for (auto& pr : c->kt_pending[q]) {
+      CK(cudaEventSynchronize(pr.second));
+      float ms = 0.f;
+      CK(cudaEventElapsedTime(&ms, pr.first, pr.second));
+      c->kt_ms[q] += ms;
+      c->kt_launches[q] += 1;
+      cudaEventDestroy(pr.first);
+      cudaEventDestroy(pr.second);
+    }
+    c->kt_pending[q].clear();
+  }
+  return IZEM_OK;
+}
+
+int read_status(izem_ctx* c) {
+  CK(cudaMemcpyAsync(c->h_status, c->d_status, sizeof(DevStatus), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  DevStatus& s = *c->h_status;
+  int rc = IZEM_OK;
+  if (s.neg_pressure) rc = ctx_fail(c, IZEM_ERR_NEG_PRESSURE, "negative pressure in the convective flux pre-pass", cudaSuccess);
+  else if (s.neg_temperature) rc = ctx_fail(c, IZEM_ERR_NEG_TEMPERATURE, "negative temperature in the Newton solve", cudaSuccess);
+  else if (s.newton_nan) rc = ctx_fail(c, IZEM_ERR_NAN, "Newton temperature correction is NaN", cudaSuccess);
+  else if (s.timeout) rc = ctx_fail(c, IZEM_ERR_TIMEOUT, "bounded device wait gave up", cudaSuccess);
+  else if (s.chem_fail) rc = ctx_fail(c, IZEM_ERR_CHEM, "stiff chemistry integration failed on some cells", cudaSuccess);
+  c->newton_warn += s.newton_unconverged;
+  if (rc != IZEM_OK || s.newton_unconverged) {
+    // clear sticky flags so that the context stays usable
+    CK(cudaMemsetAsync(c->d_status, 0, sizeof(DevStatus), c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+  }
+  return rc;
+}
+
+// ------------------------------------------------------- stage building -----
+template <int NRV>
+int enq_newton(izem_ctx* c, int ghost, double eps, int itmax, int niter, int check_negT) {
+  const Geo& g = c->g;
+  int d0 = ghost ? 1 : 0, d1 = ghost ? 6 : 0;
+  long long n = ghost ? slab_count(g) - g.nint : g.nint;
+  int rc;
+  if ((rc = launch(c, "newton_reset", [&] { k_newton_reset<<<1, 8, 0, c->stream>>>(c->d_status, d0, d1); }))) return rc;
+  for (int it = 0; it < niter; ++it) {
+    if ((rc = launch(c, ghost ? "newton_iter_ghost" : "newton_iter", [&] {
+           k_newton_iter<NRV><<<grid_for(n), kThreads, 0, c->stream>>>(g, ghost, c->v, c->T, c->cp, c->ha, c->d_status, check_negT);
+         })))
+      return rc;
+    if ((rc = launch(c, "newton_check", [&] { k_newton_check<<<1, 1, 0, c->stream>>>(c->d_status, d0, d1, eps, itmax); })))
+      return rc;
+  }
+  return launch(c, "newton_final", [&] { k_newton_final<<<1, 1, 0, c->stream>>>(c->d_status, d0, d1); });
+}
+
+template <int NRV>
+int enq_prim(izem_ctx* c) {
+  const Geo& g = c->g;
+  long long n = slab_count(g);
+  return launch(c, "prim", [&] {
+    k_prim<NRV><<<grid_for(n), kThreads, 0, c->stream>>>(g, c->v, c->T, c->W_i, c->cp, c->ha, c->prim,
+                                                          c->cfg.vis ? c->Xa : nullptr, c->d_status);
+  });
+}
+
+template <int NRV>
+int enq_euler(izem_ctx* c, int d) {
+  const Geo& g = c->g;
+  constexpr int NV = IZEM_NIV + NRV;
+  long long nf = (long long)(g.n[0] + (d == 0)) * (g.n[1] + (d == 1)) * (g.n[2] + (d == 2));
+  int rc;
+  const char* names[3] = {"euler_face_x", "euler_face_y", "euler_face_z"};
+  rc = launch(c, names[d], [&] {
+    if (d == 0) k_euler_face<NRV, 0><<<grid_for(nf), kThreads, 0, c->stream>>>(g, c->cfg.weno_avg, c->cfg.weno5_linear_fix, c->v, c->prim, c->sensor, c->fhat, nf);
+    if (d == 1) k_euler_face<NRV, 1><<<grid_for(nf), kThreads, 0, c->stream>>>(g, c->cfg.weno_avg, c->cfg.weno5_linear_fix, c->v, c->prim, c->sensor, c->fhat, nf);
+    if (d == 2) k_euler_face<NRV, 2><<<grid_for(nf), kThreads, 0, c->stream>>>(g, c->cfg.weno_avg, c->cfg.weno5_linear_fix, c->v, c->prim, c->sensor, c->fhat, nf);
+  });
+  if (rc) return rc;
+  return launch(c, "flux_diff", [&] {
+    if (d == 0) k_flux_diff<0><<<grid_for(g.nint), kThreads, 0, c->stream>>>(g, NV, c->fhat, nf, c->dxi[0], c->f, 0);
+    if (d == 1) k_flux_diff<1><<<grid_for(g.nint), kThreads, 0, c->stream>>>(g, NV, c->fhat, nf, c->dxi[1], c->f, 1);
+    if (d == 2) k_flux_diff<2><<<grid_for(g.nint), kThreads, 0, c->stream>>>(g, NV, c->fhat, nf, c->dxi[2], c->f, 1);
+  });
+}
+
+template <int NRV>
+int enq_visc(izem_ctx* c) {
+  const Geo& g = c->g;
+  Metrics mt;
+  for (int d = 0; d < 3; ++d) mt.dxi[d] = c->dxi[d];
+  const int nderiv = 12 + 3 * NRV;
+  int rc;
+  if ((rc = launch(c, "visc_grad", [&] { k_grad<NRV><<<grid_for(g.nint), kThreads, 0, c->stream>>>(g, mt, c->prim, c->T, c->Xa, c->fd); })))
+    return rc;
+  long long ns = slab_count(g) - g.nint;
+  if ((rc = launch(c, "visc_wrap", [&] { k_wrap_periodic<<<grid_for(ns), kThreads, 0, c->stream>>>(g, nderiv, c->fd); })))
+    return rc;
+  if ((rc = launch(c, "visc_point", [&] {
+         k_visc_point<NRV><<<grid_for(slab_count(g)), kThreads, 0, c->stream>>>(g, c->v, c->T, c->W_i, c->ha, c->Xa, c->fd, c->tau, c->qv);
+       })))
+    return rc;
+  return launch(c, "visc_div", [&] { k_visc_div<NRV><<<grid_for(g.nint), kThreads, 0, c->stream>>>(g, mt, c->tau, c->qv, c->fd, c->f); });
+}
+
+template <int NRV>
+int enq_update_primitives_after(izem_ctx* c) {
+  const Geo& g = c->g;
+  int rc;
+  if ((rc = enq_newton<NRV>(c, 0, 1.0e-5, 200, kNewtonIters, 1))) return rc;
+  long long ns = slab_count(g) - g.nint;
+  if ((rc = launch(c, "halo", [&] { k_halo<NRV><<<grid_for(ns), kThreads, 0, c->stream>>>(g, 0, c->cfg.forcesum, c->v, c->W_i); })))
+    return rc;
+  return enq_newton<NRV>(c, 1, 1.0e-5, 200, kNewtonIters, 1);
+}
+
+template <int NRV>
+int enq_stage(izem_ctx* c, int stage) {
+  const Geo& g = c->g;
+  int rc;
+  if ((rc = launch(c, "sensor", [&] { k_sensor<<<grid_for(g.nint), kThreads, 0, c->stream>>>(g, c->cfg.max_rel_weight, c->v, c->T, c->W_i, c->sensor); })))
+    return rc;
+  if ((rc = enq_prim<NRV>(c))) return rc;
+  for (int d = 0; d < 3; ++d)
+    if ((rc = enq_euler<NRV>(c, d))) return rc;
+  if (c->cfg.vis)
+    if ((rc = enq_visc<NRV>(c))) return rc;
+  if ((rc = launch(c, "rk_update", [&] {
+         k_rk_update<NRV><<<grid_for(g.nint), kThreads, 0, c->stream>>>(g, stage, c->cfg.forcesum, c->d_dt, c->v, c->v0, c->f, c->W_i);
+       })))
+    return rc;
+  return enq_update_primitives_after<NRV>(c);
+}
+
+// ------------------------------------------------------ NRV dispatch --------
+#define IZEM_DISPATCH(c, FN, ...)                          \
+  ((c)->cfg.nrv == 2 ? FN<2>(__VA_ARGS__)                  \
+   : (c)->cfg.nrv == 9 ? FN<9>(__VA_ARGS__)                \
+   : ctx_fail((c), IZEM_ERR_ARG, "nrv not compiled", cudaSuccess))
+
+template <int NRV>
+int do_rk3_enqueue(izem_ctx* c) {
+  for (int s = 0; s < 3; ++s) {
+    int rc = enq_stage<NRV>(c, s);
+    if (rc) return rc;
+  }
+  return IZEM_OK;
+}
+
+template <int NRV>
+int do_finalize_ic(izem_ctx* c) {
+  const Geo& g = c->g;
+  int rc;
+  if ((rc = launch(c, "wmix", [&] { k_wmix_interior<NRV><<<grid_for(g.nint), kThreads, 0, c->stream>>>(g, c->v, c->W_i); })))
+    return rc;
+  if ((rc = enq_newton<NRV>(c, 0, 1.0e-10, 100, 100, 0))) return rc;
+  long long ns = slab_count(g) - g.nint;
+  if ((rc = launch(c, "halo", [&] { k_halo<NRV><<<grid_for(ns), kThreads, 0, c->stream>>>(g, 1, 0, c->v, c->W_i); }))) return rc;
+  return enq_newton<NRV>(c, 1, 1.0e-10, 100, 100, 0);
+}
+
+template <int NRV>
+int do_update_primitives(izem_ctx* c) {
+  const Geo& g = c->g;
+  int rc;
+  // upd_prim_var_domain on the current interior state (force_sumY + W_i)
+  if ((rc = launch(c, "prep_interior", [&] {
+         k_prep_interior<NRV><<<grid_for(g.nint), kThreads, 0, c->stream>>>(g, c->cfg.forcesum, c->v, c->W_i);
+       })))
+    return rc;
+  return enq_update_primitives_after<NRV>(c);
+}
+
+template <int NRV>
+int do_timestep(izem_ctx* c) {
+  const Geo& g = c->g;
+  Metrics mt;
+  for (int d = 0; d < 3; ++d) mt.dxi[d] = c->dxi[d];
+  return launch(c, "timestep", [&] {
+    k_dtc<NRV><<<grid_for(g.nint), kThreads, 0, c->stream>>>(g, mt, c->v, c->T, c->W_i, c->cp, c->d_status);
+  });
+}
+
+template <int NRV>
+int do_sensor(izem_ctx* c) {
+  const Geo& g = c->g;
+  return launch(c, "sensor", [&] { k_sensor<<<grid_for(g.nint), kThreads, 0, c->stream>>>(g, c->cfg.max_rel_weight, c->v, c->T, c->W_i, c->sensor); });
+}
+
+template <int NRV>
+int do_euler(izem_ctx* c, int d) {
+  int rc = enq_prim<NRV>(c);
+  if (rc) return rc;
+  return enq_euler<NRV>(c, d);
+}
+
+template <int NRV>
+int do_visc(izem_ctx* c) {
+  int rc = enq_prim<NRV>(c);
+  if (rc) return rc;
+  return enq_visc<NRV>(c);
+}
+
+// ================================================================ C ABI =====
+extern "C" {
+
+int izem_gpu_init(const izem_cfg* cfg, const izem_thd* thd, const izem_adi* adi, izem_ctx** out) {
+  if (!cfg || !thd || !adi || !out) return IZEM_ERR_ARG;
+  *out = nullptr;
+  if (cfg->ng != 3 || cfg->ndim != 3 || !(cfg->nrv == 2 || cfg->nrv == 9) || thd->nspc != cfg->nrv) return IZEM_ERR_ARG;
+  if (cfg->nx < 7 || cfg->ny < 7 || cfg->nz < 7) return IZEM_ERR_ARG;
+  for (int f = 0; f < 6; ++f)
+    if (cfg->bc[f] != IZEM_BC_PERIODIC && cfg->bc[f] != IZEM_BC_EXTRAPOLATION) return IZEM_ERR_ARG;
+  for (int d = 0; d < 3; ++d)
+    if ((cfg->bc[2 * d] == IZEM_BC_PERIODIC) != (cfg->bc[2 * d + 1] == IZEM_BC_PERIODIC)) return IZEM_ERR_ARG;
+  izem_ctx* c = new izem_ctx();
+  c->cfg = *cfg;
+  c->thd = *thd;
+  c->adi = *adi;
+  Geo& g = c->g;
+  g.n[0] = cfg->nx; g.n[1] = cfg->ny; g.n[2] = cfg->nz; g.ng = cfg->ng;
+  for (int d = 0; d < 3; ++d) g.g[d] = g.n[d] + 2 * g.ng;
+  g.ncell = (long long)g.g[0] * g.g[1] * g.g[2];
+  g.nint = (long long)g.n[0] * g.n[1] * g.n[2];
+  for (int f = 0; f < 6; ++f) { g.bc[f] = cfg->bc[f]; g.bnd[f] = cfg->bc[f] != IZEM_BC_PERIODIC; }
+  c->nv = IZEM_NIV + cfg->nrv;
+
+  // constant species data in code units (thd_init) plus derived constants
+  DevThd h;
+  std::memset(&h, 0, sizeof(h));
+  h.nspc = thd->nspc;
+  h.gam2 = thd->gam2;
+  h.gam2_i = 1.0 / thd->gam2;
+  h.tinf = thd->tinf;
+  h.tinf_i = 1.0 / thd->tinf;
+  h.onethird = 1.0 / 3.0;
+  for (int k = 0; k < thd->nspc; ++k) {
+    h.Wc[k] = thd->Wc[k];
+    h.Wc_i[k] = thd->Wc_i[k];
+    h.tpolymin[k] = thd->tpolymin[k];
+    h.tpolymax[k] = thd->tpolymax[k];
+    h.tpolylim[k] = thd->tpolylim[k];
+    std::memcpy(h.hc[k], thd->heatcap[k], sizeof(h.hc[k]));
+    for (int l = 0; l < thd->nspc; ++l) {
+      std::memcpy(h.cofd[k][l], thd->cofd[k][l], sizeof(h.cofd[k][l]));
+      h.wilke_c1[k][l] = std::pow(thd->W[l] / thd->W[k], 0.25);
+      h.wilke_c2[k][l] = 1.0 / std::sqrt((1.0 + thd->W[k] / thd->W[l]) * 8.0);
+    }
+    std::memcpy(h.coflam[k], thd->coflam[k], sizeof(h.coflam[k]));
+    std::memcpy(h.cofeta[k], thd->cofeta[k], sizeof(h.cofeta[k]));
+    h.Kd[k] = 1.0e-4 * thd->p0 / (thd->pinf * thd->dinf[k]);
+  }
+  h.Kl = 0.5 * 1.0e-5 / thd->laminf;
+  h.Ku = 1.0e-1 / thd->muinf;
+  h.sqgmr = adi->sqgmr;
+  h.rvd0 = adi->sqgmr / adi->sc;
+  h.rlam0 = adi->sqgmr * adi->ggmopr;
+  c->devthd = h;
+
+  int rc = ctx_alloc(c);
+  if (rc) {
+    std::fprintf(stderr, "izem_gpu_init: %s\n", c->err.c_str());
+    izem_gpu_destroy(c);
+    return rc;
+  }
+  *out = c;
+  return IZEM_OK;
+}
+
+}  // extern "C"
+
+int ctx_alloc(izem_ctx* c) {
+  const Geo& g = c->g;
+  const int nv = c->nv, nrv = c->cfg.nrv;
+  CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  CK(cudaMemcpyToSymbol(c_thd, &c->devthd, sizeof(DevThd)));
+  auto alloc = [&](double** p, size_t n) -> cudaError_t {
+    cudaError_t e = cudaMalloc(p, n * sizeof(double));
+    if (e == cudaSuccess) c->allocs.push_back(*p);
+    return e;
+  };
+  const size_t nc = (size_t)g.ncell, ni = (size_t)g.nint;
+  size_t maxf = 0;
+  for (int d = 0; d < 3; ++d) {
+    size_t nf = (size_t)(g.n[0] + (d == 0)) * (g.n[1] + (d == 1)) * (g.n[2] + (d == 2));
+    if (nf > maxf) maxf = nf;
+  }
+  cudaError_t e = cudaSuccess;
+  if ((e = alloc(&c->v, nv * nc)) || (e = alloc(&c->T, nc)) || (e = alloc(&c->W_i, nc)) || (e = alloc(&c->cp, nc)) ||
+      (e = alloc(&c->ha, nrv * nc)) || (e = alloc(&c->v0, nv * ni)) || (e = alloc(&c->f, nv * ni)) ||
+      (e = alloc(&c->prim, PR_N * nc)) || (e = alloc(&c->Xa, nrv * nc)) || (e = alloc(&c->fhat, nv * maxf)) ||
+      (e = alloc(&c->fd, (12 + 3 * nrv) * nc)) || (e = alloc(&c->tau, 6 * nc)) || (e = alloc(&c->qv, 3 * nc)) ||
+      (e = alloc(&c->d_dt, 1)))
+    return ctx_fail(c, e == cudaErrorMemoryAllocation ? IZEM_ERR_NOMEM : IZEM_ERR_CUDA, "device allocation", e);
+  for (int d = 0; d < 3; ++d)
+    if ((e = alloc(&c->dxi[d], g.g[d]))) return ctx_fail(c, IZEM_ERR_CUDA, "device allocation", e);
+  CK(cudaMalloc(&c->sensor, nc));
+  CK(cudaMemset(c->sensor, 0, nc));
+  CK(cudaMalloc(&c->d_status, sizeof(DevStatus)));
+  CK(cudaMemset(c->d_status, 0, sizeof(DevStatus)));
+  CK(cudaMallocHost(&c->h_status, sizeof(DevStatus)));
+  CK(cudaMallocHost(&c->h_dt, sizeof(double)));
+  // zero the arrays whose ghost corners are never written
+  CK(cudaMemset(c->v, 0, nv * nc * sizeof(double)));
+  CK(cudaMemset(c->fd, 0, (12 + 3 * nrv) * nc * sizeof(double)));
+  CK(cudaMemset(c->tau, 0, 6 * nc * sizeof(double)));
+  CK(cudaMemset(c->qv, 0, 3 * nc * sizeof(double)));
+  CK(cudaMemset(c->f, 0, nv * ni * sizeof(double)));
+  CK(cudaEventCreate(&c->t0));
+  CK(cudaEventCreate(&c->t1));
+  return IZEM_OK;
+}
+
+extern "C" {
+
+void izem_gpu_destroy(izem_ctx* c) {
+  if (!c) return;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+  if (c->graph) cudaGraphDestroy(c->graph);
+  for (double* p : c->allocs) cudaFree(p);
+  if (c->sensor) cudaFree(c->sensor);
+  if (c->d_status) cudaFree(c->d_status);
+  if (c->h_status) cudaFreeHost(c->h_status);
+  if (c->h_dt) cudaFreeHost(c->h_dt);
+  for (auto& v : c->kt_pending)
+    for (auto& pr : v) { cudaEventDestroy(pr.first); cudaEventDestroy(pr.second); }
+  if (c->t0) cudaEventDestroy(c->t0);
+  if (c->t1) cudaEventDestroy(c->t1);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+int izem_gpu_last_error(izem_ctx* c, char* buf, int n) {
+  if (!c) return IZEM_ERR_ARG;
+  if (buf && n > 0) std::snprintf(buf, n, "%s", c->err.c_str());
+  return c->newton_warn;
+}
+
+int izem_gpu_set_grid(izem_ctx* c, const double* dx_i, const double* dy_i, const double* dz_i) {
+  if (!c || !dx_i || !dy_i || !dz_i) return IZEM_ERR_ARG;
+  const double* s[3] = {dx_i, dy_i, dz_i};
+  for (int d = 0; d < 3; ++d) CK(cudaMemcpy(c->dxi[d], s[d], c->g.g[d] * sizeof(double), cudaMemcpyHostToDevice));
+  c->grid_set = true;
+  return IZEM_OK;
+}
+
+int izem_gpu_upload_state(izem_ctx* c, const double* v, const double* T, const double* W_i, const double* cp,
+                          const double* ha, const uint8_t* sensor) {
+  if (!c) return IZEM_ERR_ARG;
+  const size_t nc = (size_t)c->g.ncell;
+  if (v) CK(cudaMemcpyAsync(c->v, v, c->nv * nc * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  if (T) CK(cudaMemcpyAsync(c->T, T, nc * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  if (W_i) CK(cudaMemcpyAsync(c->W_i, W_i, nc * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  if (cp) CK(cudaMemcpyAsync(c->cp, cp, nc * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  if (ha) CK(cudaMemcpyAsync(c->ha, ha, c->cfg.nrv * nc * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  if (sensor) CK(cudaMemcpyAsync(c->sensor, sensor, nc, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return IZEM_OK;
+}
+
+int izem_gpu_download_state(izem_ctx* c, double* v, double* T, double* W_i, double* cp, double* ha, uint8_t* sensor) {
+  if (!c) return IZEM_ERR_ARG;
+  const size_t nc = (size_t)c->g.ncell;
+  if (v) CK(cudaMemcpyAsync(v, c->v, c->nv * nc * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  if (T) CK(cudaMemcpyAsync(T, c->T, nc * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  if (W_i) CK(cudaMemcpyAsync(W_i, c->W_i, nc * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  if (cp) CK(cudaMemcpyAsync(cp, c->cp, nc * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  if (ha) CK(cudaMemcpyAsync(ha, c->ha, c->cfg.nrv * nc * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  if (sensor) CK(cudaMemcpyAsync(sensor, c->sensor, nc, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return IZEM_OK;
+}
+
+int izem_gpu_download_flux(izem_ctx* c, double* fl) {
+  if (!c || !fl) return IZEM_ERR_ARG;
+  CK(cudaMemcpyAsync(fl, c->f, c->nv * (size_t)c->g.nint * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return IZEM_OK;
+}
+
+int izem_gpu_zero_flux(izem_ctx* c) {
+  if (!c) return IZEM_ERR_ARG;
+  CK(cudaMemsetAsync(c->f, 0, c->nv * (size_t)c->g.nint * sizeof(double), c->stream));
+  return IZEM_OK;
+}
+
+int izem_gpu_shock_sensor(izem_ctx* c) {
+  if (!c) return IZEM_ERR_ARG;
+  int rc = IZEM_DISPATCH(c, do_sensor, c);
+  if (rc) return rc;
+  return read_status(c);
+}
+
+int izem_gpu_euler_flux(izem_ctx* c, int dir) {
+  if (!c || dir < 0 || dir > 2) return IZEM_ERR_ARG;
+  if (!c->grid_set) return ctx_fail(c, IZEM_ERR_STATE, "grid not set", cudaSuccess);
+  int rc = IZEM_DISPATCH(c, do_euler, c, dir);
+  if (rc) return rc;
+  return read_status(c);
+}
+
+int izem_gpu_visc_flux(izem_ctx* c) {
+  if (!c) return IZEM_ERR_ARG;
+  if (!c->grid_set) return ctx_fail(c, IZEM_ERR_STATE, "grid not set", cudaSuccess);
+  int rc = IZEM_DISPATCH(c, do_visc, c);
+  if (rc) return rc;
+  return read_status(c);
+}
+
+int izem_gpu_update_primitives(izem_ctx* c) {
+  if (!c) return IZEM_ERR_ARG;
+  int rc = IZEM_DISPATCH(c, do_update_primitives, c);
+  if (rc) return rc;
+  return read_status(c);
+}
+
+int izem_gpu_finalize_ic(izem_ctx* c) {
+  if (!c) return IZEM_ERR_ARG;
+  int rc = IZEM_DISPATCH(c, do_finalize_ic, c);
+  if (rc) return rc;
+  return read_status(c);
+}
+
+int izem_gpu_rk3(izem_ctx* c, double dt, double time0) {
+  (void)time0;
+  if (!c) return IZEM_ERR_ARG;
+  if (!c->grid_set) return ctx_fail(c, IZEM_ERR_STATE, "grid not set", cudaSuccess);
+  *c->h_dt = dt;
+  CK(cudaMemcpyAsync(c->d_dt, c->h_dt, sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  int rc;
+  if (c->kt_enabled) {
+    // timed mode: direct launches, each bracketed by events
+    rc = IZEM_DISPATCH(c, do_rk3_enqueue, c);
+    if (rc) return rc;
+  } else {
+    if (!c->graph_exec) {
+      c->capturing = true;
+      CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+      rc = IZEM_DISPATCH(c, do_rk3_enqueue, c);
+      cudaGraph_t graph = nullptr;
+      cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
+      c->capturing = false;
+      if (rc) { if (graph) cudaGraphDestroy(graph); return rc; }
+      if (e != cudaSuccess) return ctx_fail(c, IZEM_ERR_CUDA, "cudaStreamEndCapture", e);
+      c->graph = graph;
+      CK(cudaGraphInstantiate(&c->graph_exec, c->graph, 0));
+    }
+    CK(cudaGraphLaunch(c->graph_exec, c->stream));
+  }
+  return read_status(c);
+}
+
+int izem_gpu_timestep(izem_ctx* c, double DTmax, double dt_4[4], double* dtmin) {
+  if (!c || !dt_4 || !dtmin) return IZEM_ERR_ARG;
+  CK(cudaMemsetAsync(&c->d_status->dtc_bits, 0, sizeof(unsigned long long), c->stream));
+  int rc = IZEM_DISPATCH(c, do_timestep, c);
+  if (rc) return rc;
+  rc = read_status(c);
+  if (rc) return rc;
+  double m;
+  std::memcpy(&m, &c->h_status->dtc_bits, sizeof(double));
+  double dtc = std::fmax(1.0, m);
+  for (int q = 0; q < 4; ++q) dt_4[q] = 1.0;
+  dt_4[0] = c->cfg.cfl / dtc;
+  if (c->cfg.reaction) {
+    dt_4[3] = *dtmin * c->cfg.cpr / DTmax;
+    dt_4[3] = std::fmin(dt_4[3], 1.0);
+    dt_4[3] = std::fmax(dt_4[3], dt_4[0] * c->cfg.cflmin / c->cfg.cfl);
+  }
+  *dtmin = std::fmin(std::fmin(dt_4[0], dt_4[1]), std::fmin(dt_4[2], dt_4[3]));
+  return IZEM_OK;
+}
+
+int izem_gpu_timer_start(izem_ctx* c) {
+  if (!c) return IZEM_ERR_ARG;
+  CK(cudaEventRecord(c->t0, c->stream));
+  return IZEM_OK;
+}
+
+int izem_gpu_timer_stop(izem_ctx* c, float* ms) {
+  if (!c || !ms) return IZEM_ERR_ARG;
+  CK(cudaEventRecord(c->t1, c->stream));
+  CK(cudaEventSynchronize(c->t1));
+  CK(cudaEventElapsedTime(ms, c->t0, c->t1));
+  return IZEM_OK;
+}
+
+int izem_gpu_set_kernel_timing(izem_ctx* c, int enable) {
+  if (!c) return IZEM_ERR_ARG;
+  int rc = kt_collect(c);
+  if (rc) return rc;
+  c->kt_enabled = enable != 0;
+  for (size_t q = 0; q < c->kt_names.size(); ++q) { c->kt_ms[q] = 0.0; c->kt_launches[q] = 0; }
+  return IZEM_OK;
+}
+
+int izem_gpu_kernel_times(izem_ctx* c, int max_kernels, char* names, int name_len, int* launches, double* ms, int* n_kernels) {
+  if (!c || !n_kernels) return IZEM_ERR_ARG;
+  int rc = kt_collect(c);
+  if (rc) return rc;
+  int n = (int)c->kt_names.size();
+  *n_kernels = n;
+  for (int q = 0; q < n && q < max_kernels; ++q) {
+    if (names) std::snprintf(names + (size_t)q * name_len, name_len, "%s", c->kt_names[q].c_str());
+    if (launches) launches[q] = c->kt_launches[q];
+    if (ms) ms[q] = c->kt_ms[q];
+  }
+  return IZEM_OK;
+}
+
+int izem_gpu_synchronize(izem_ctx* c) {
+  if (!c) return IZEM_ERR_ARG;
+  CK(cudaStreamSynchronize(c->stream));
+  return read_status(c);
+}
+
+int izem_abi_sizes(size_t* a, size_t* b, size_t* d) {
+  if (!a || !b || !d) return IZEM_ERR_ARG;
+  *a = sizeof(izem_cfg);
+  *b = sizeof(izem_thd);
+  *d = sizeof(izem_adi);
+  return IZEM_OK;
+}
+
+int izem_metrics_dscalar(int n, int ng, const double* coord, double* d_i) {
+  (void)ng;
+  if (n < 7 || !coord || !d_i) return IZEM_ERR_ARG;
+  std::vector<double> dv(n, 1.0);
+  const double a6[7] = {-1.0 / 60.0, 9.0 / 60.0, -45.0 / 60.0, 0.0, 45.0 / 60.0, -9.0 / 60.0, 1.0 / 60.0};
+  const double a4[5] = {1.0 / 12.0, -8.0 / 12.0, 0.0, 8.0 / 12.0, -1.0 / 12.0};
+  const double a4ol[5] = {-25.0 / 12.0, 48.0 / 12.0, -36.0 / 12.0, 16.0 / 12.0, -3.0 / 12.0};
+  const double a4ul[5] = {-3.0 / 12.0, -10.0 / 12.0, 18.0 / 12.0, -6.0 / 12.0, 1.0 / 12.0};
+  const double a4ur[5] = {1.0 / 12.0, -6.0 / 12.0, 18.0 / 12.0, -10.0 / 12.0, -3.0 / 12.0};
+  const double a4or[5] = {-3.0 / 12.0, 16.0 / 12.0, -36.0 / 12.0, 48.0 / 12.0, -25.0 / 12.0};
+  auto x = [&](int m) { return coord[m - 1]; };
+  for (int m = 4; m <= n - 3; ++m) {
+    double dd = 0.0;
+    for (int l = -3; l <= 3; ++l) dd = dd + a6[l + 3] * x(m + l);
+    dv[m - 1] = dd * 1.0;
+  }
+  { double dd = 0.0; for (int l = 0; l <= 4; ++l) dd = dd + a4ol[l] * x(1 + l); dv[0] = dd * 1.0; }
+  { double dd = 0.0; for (int l = -1; l <= 3; ++l) dd = dd + a4ul[l + 1] * x(2 + l); dv[1] = dd * 1.0; }
+  { double dd = 0.0; for (int l = -2; l <= 2; ++l) dd = dd + a4[l + 2] * x(3 + l); dv[2] = dd * 1.0; }
+  { double dd = 0.0; for (int l = -2; l <= 2; ++l) dd = dd + a4[l + 2] * x(n - 2 + l); dv[n - 3] = dd * 1.0; }
+  { double dd = 0.0; for (int l = -3; l <= 1; ++l) dd = dd + a4ur[l + 3] * x(n - 1 + l); dv[n - 2] = -dd * 1.0; }
+  { double dd = 0.0; for (int l = -4; l <= 0; ++l) dd = dd + a4or[l + 4] * x(n + l); dv[n - 1] = -dd * 1.0; }
+  for (int m = 0; m < n; ++m) d_i[m] = 1.0 / dv[m];
+  return IZEM_OK;
+}
+
+}  // extern "C"

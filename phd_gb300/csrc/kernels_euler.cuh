@@ -1,0 +1,417 @@
+// Convective part of the RHS: primitive pre-pass (K1), characteristic
+// LLF-WENO face fluxes (K2), flux difference, Adams-Shariff sensor (K3).
+//
+// Reference: module_weno.f90 euler_LLF_x/_y/_z (:537-2125), wenorec_nw
+// (:236-275), wenorec (:286-527); module_tools.f90 sensor (:2733-2814).
+#pragma once
+#include "common.cuh"
+#include "thermo.cuh"
+
+enum { PR_RHOI = 0, PR_U = 1, PR_V = 2, PR_W = 3, PR_P = 4, PR_CS = 5, PR_HT = 6, PR_ET = 7, PR_N = 8 };
+
+// Maps a linear index over the interior + face-ghost slabs (the points the
+// reference's pencil pre-passes touch) to (i,j,k).  Returns false past the end.
+__device__ __forceinline__ bool slab_point(const Geo& g, long long idx, int& i, int& j, int& k, int& dom) {
+  const long long nin = g.nint;
+  if (idx < nin) {
+    i = (int)(idx % g.n[0]) + 1;
+    long long r = idx / g.n[0];
+    j = (int)(r % g.n[1]) + 1;
+    k = (int)(r / g.n[1]) + 1;
+    dom = 0;
+    return true;
+  }
+  idx -= nin;
+  // face f: ng layers x the two interior extents of the other axes
+  for (int f = 0; f < 6; ++f) {
+    int d = f >> 1;
+    int a1 = d == 0 ? 1 : 0, a2 = d == 2 ? 1 : 2;
+    long long sz = (long long)g.ng * g.n[a1] * g.n[a2];
+    if (idx < sz) {
+      int c1 = (int)(idx % g.n[a1]) + 1;
+      long long r = idx / g.n[a1];
+      int c2 = (int)(r % g.n[a2]) + 1;
+      int layer = (int)(r / g.n[a2]) + 1;     // 1..ng
+      int s = (f & 1) ? g.n[d] + layer : 1 - layer;
+      int c[3];
+      c[d] = s; c[a1] = c1; c[a2] = c2;
+      i = c[0]; j = c[1]; k = c[2];
+      dom = 1 + f;
+      return true;
+    }
+    idx -= sz;
+  }
+  return false;
+}
+
+__host__ __device__ inline long long slab_count(const Geo& g) {
+  long long s = g.nint;
+  for (int d = 0; d < 3; ++d) {
+    int a1 = d == 0 ? 1 : 0, a2 = d == 2 ? 1 : 2;
+    s += 2LL * g.ng * g.n[a1] * g.n[a2];
+  }
+  return s;
+}
+
+// K1: per-point primitives used by the sweeps (module_weno.f90:634-667 and
+// the y/z copies): 1/rho, u, v, w, P = rho T W_i, c = sqrt(gam P / rho),
+// h_t = sum h_k Y_k + |u|^2/2, e_t = rho e_t / rho.  Also the mole fractions
+// of molefrac (module_thermodynamics.f90:1669-1697) for the viscous flux.
+template <int NRV>
+__global__ void k_prim(Geo g, const double* __restrict__ v, const double* __restrict__ T,
+                       const double* __restrict__ W_i, const double* __restrict__ cp,
+                       const double* __restrict__ ha, double* __restrict__ prim,
+                       double* __restrict__ Xa, DevStatus* st) {
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  int i, j, k, dom;
+  if (!slab_point(g, idx, i, j, k, dom)) return;
+  const long long nc = g.ncell;
+  long long p = gid(g, i, j, k);
+  double rho = v[p];
+  double rho_i = 1.0 / rho;
+  double ux = v[nc + p] * rho_i, vy = v[2 * nc + p] * rho_i, wz = v[3 * nc + p] * rho_i;
+  double Wi = W_i[p];
+  double P = rho * T[p] * Wi;
+  if (P <= 0.0) atomicExch(&st->neg_pressure, 1);
+  double gam = c_thd.gam2 * Wi / cp[p];
+  gam = 1.0 / (1.0 - gam);
+  double cs = sqrt(gam * P * rho_i);
+  double ht = 0.0;
+#pragma unroll
+  for (int l = 0; l < NRV; ++l) {
+    double rY = v[(IZEM_NIV + l) * nc + p];
+    ht = ht + ha[l * nc + p] * (rY * rho_i);
+    if (Xa) Xa[l * nc + p] = rY / (rho * Wi * c_thd.Wc[l]);
+  }
+  ht = ht + 0.5 * (ux * ux + vy * vy + wz * wz);
+  prim[PR_RHOI * nc + p] = rho_i;
+  prim[PR_U * nc + p] = ux;
+  prim[PR_V * nc + p] = vy;
+  prim[PR_W * nc + p] = wz;
+  prim[PR_P * nc + p] = P;
+  prim[PR_CS * nc + p] = cs;
+  prim[PR_HT * nc + p] = ht;
+  prim[PR_ET * nc + p] = v[4 * nc + p] * rho_i;
+}
+
+// Nonlinear WENO5 reconstruction (wenorec, ng = 3) of one characteristic
+// field; gp/gm hold the 2ng = 6 stencil values (index 0 = point il-2).
+__device__ __forceinline__ double weno5_nl(const double* vp, const double* vm) {
+  const double eps = 1.0e-10;
+  const double z1 = 13.0 / 12.0, z2 = 1.0 / 4.0;
+  // '-' state at i+1/2, centre vp[2]
+  double a, b, b0, b1, b2;
+  double q0 = (1.0 / 3.0) * vp[2] + (5.0 / 6.0) * vp[3] + (-1.0 / 6.0) * vp[4];
+  double q1 = (-1.0 / 6.0) * vp[1] + (5.0 / 6.0) * vp[2] + (1.0 / 3.0) * vp[3];
+  double q2 = (1.0 / 3.0) * vp[0] + (-7.0 / 6.0) * vp[1] + (11.0 / 6.0) * vp[2];
+  a = vp[2] + -2.0 * vp[3] + vp[4]; b = 3.0 * vp[2] + -4.0 * vp[3] + vp[4];
+  b0 = z1 * a * a + z2 * b * b;
+  a = vp[1] + -2.0 * vp[2] + vp[3]; b = vp[1] + -1.0 * vp[3];
+  b1 = z1 * a * a + z2 * b * b;
+  a = vp[0] + -2.0 * vp[1] + vp[2]; b = vp[0] + -4.0 * vp[1] + 3.0 * vp[2];
+  b2 = z1 * a * a + z2 * b * b;
+  double al0 = (3.0 / 10.0) / ((eps + b0) * (eps + b0));
+  double al1 = (3.0 / 5.0) / ((eps + b1) * (eps + b1));
+  double al2 = (1.0 / 10.0) / ((eps + b2) * (eps + b2));
+  double s = 1.0 / (al0 + al1 + al2);
+  double vminus = al0 * s * q0 + al1 * s * q1 + al2 * s * q2;
+  // '+' state at i+1/2, centre vm[3]
+  q0 = (11.0 / 6.0) * vm[3] + (-7.0 / 6.0) * vm[4] + (1.0 / 3.0) * vm[5];
+  q1 = (1.0 / 3.0) * vm[2] + (5.0 / 6.0) * vm[3] + (-1.0 / 6.0) * vm[4];
+  q2 = (-1.0 / 6.0) * vm[1] + (5.0 / 6.0) * vm[2] + (1.0 / 3.0) * vm[3];
+  a = vm[3] + -2.0 * vm[4] + vm[5]; b = 3.0 * vm[3] + -4.0 * vm[4] + vm[5];
+  b0 = z1 * a * a + z2 * b * b;
+  a = vm[2] + -2.0 * vm[3] + vm[4]; b = vm[2] + -1.0 * vm[4];
+  b1 = z1 * a * a + z2 * b * b;
+  a = vm[1] + -2.0 * vm[2] + vm[3]; b = vm[1] + -4.0 * vm[2] + 3.0 * vm[3];
+  b2 = z1 * a * a + z2 * b * b;
+  al0 = (1.0 / 10.0) / ((eps + b0) * (eps + b0));
+  al1 = (3.0 / 5.0) / ((eps + b1) * (eps + b1));
+  al2 = (3.0 / 10.0) / ((eps + b2) * (eps + b2));
+  s = 1.0 / (al0 + al1 + al2);
+  double vplus = al0 * s * q0 + al1 * s * q1 + al2 * s * q2;
+  return vminus + vplus;
+}
+
+// K2: one thread per cell face along axis D.  Characteristic projections use
+// the structure of the left eigenvectors (module_weno.f90:775-874): the three
+// acoustic/entropy rows are dense over (rho, m, rho e_t) plus a rank-one
+// species term psi.w; the shear rows have two entries; the species rows are
+// Y_s (a.w) + w_s.  The result equals the reference's dense nv x nv product
+// up to rounding.  Linear (sensor-off) faces accumulate the WENO5 stencil
+// while streaming over the 6 stencil points; sensed faces keep the 6 values.
+template <int NRV, int D>
+__global__ void __launch_bounds__(128) k_euler_face(Geo g, int weno_avg, int linfix,
+                                                    const double* __restrict__ v,
+                                                    const double* __restrict__ prim,
+                                                    const uint8_t* __restrict__ sensor,
+                                                    double* __restrict__ fhat, long long nfaces) {
+  constexpr int NV = IZEM_NIV + NRV;
+  constexpr int T1 = D == 0 ? 1 : 0;
+  constexpr int T2 = D == 2 ? 1 : 2;
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= nfaces) return;
+  int c[3];
+  {
+    long long r = idx;
+    int e0 = D == 0 ? g.n[0] + 1 : g.n[0];
+    int e1 = D == 1 ? g.n[1] + 1 : g.n[1];
+    c[0] = (int)(r % e0); r /= e0;
+    c[1] = (int)(r % e1); r /= e1;
+    c[2] = (int)r;
+    // faces run 0..n along D (face s between cells s and s+1); cells 1..n across
+    if (D != 0) c[0] += 1;
+    if (D != 1) c[1] += 1;
+    if (D != 2) c[2] += 1;
+  }
+  const long long nc = g.ncell;
+  const long long stride = D == 0 ? 1LL : (D == 1 ? (long long)g.g[0] : (long long)g.g[0] * g.g[1]);
+  const long long pl = gid(g, c[0], c[1], c[2]);   // cell il
+  const long long pr = pl + stride;                  // cell il+1
+  const long long p0 = pl - 2 * stride;              // stencil point il-2
+
+  // ---- Roe average compatible with the EOS (module_weno.f90:726-761)
+  const double rho_i_l = prim[PR_RHOI * nc + pl], rho_i_r = prim[PR_RHOI * nc + pr];
+  const double r = sqrt(v[pr] * rho_i_l);
+  const double r1 = 1.0 / (r + 1.0);
+  double uc[3];
+  uc[0] = (r * prim[PR_U * nc + pr] + prim[PR_U * nc + pl]) * r1;
+  uc[1] = (r * prim[PR_V * nc + pr] + prim[PR_V * nc + pl]) * r1;
+  uc[2] = (r * prim[PR_W * nc + pr] + prim[PR_W * nc + pl]) * r1;
+  double Yc[NRV];
+  double W_i_c = 0.0;
+#pragma unroll
+  for (int l = 0; l < NRV; ++l) {
+    Yc[l] = (r * (v[(IZEM_NIV + l) * nc + pr] * rho_i_r) + v[(IZEM_NIV + l) * nc + pl] * rho_i_l) * r1;
+    W_i_c = W_i_c + Yc[l] * c_thd.Wc_i[l];
+  }
+  const double ht_c = (r * prim[PR_HT * nc + pr] + prim[PR_HT * nc + pl]) * r1;
+  const double et_c = (r * prim[PR_ET * nc + pr] + prim[PR_ET * nc + pl]) * r1;
+  const double T_c = (ht_c - et_c) / W_i_c;
+  double psi[NRV];
+  const double cp_c = th_cp_ha<NRV>(T_c, Yc, psi);   // psi <- h_k(T_c)
+  double gam_c = c_thd.gam2 * W_i_c / cp_c;
+  gam_c = 1.0 / (1.0 - gam_c);
+  const double cs_c = sqrt(gam_c * T_c * W_i_c);
+  {
+    const double wrk = (gam_c / (gam_c - 1.0)) * T_c;
+#pragma unroll
+    for (int l = 0; l < NRV; ++l) psi[l] = -(r * psi[l] + psi[l]) * r1 + wrk * c_thd.Wc_i[l];
+  }
+  const double cs_c_i = 1.0 / cs_c;
+  const double q = 0.5 * (uc[0] * uc[0] + uc[1] * uc[1] + uc[2] * uc[2]);
+  const double b2 = (gam_c - 1.0) / (cs_c * cs_c);
+  const double b1 = b2 * q;
+  const double xi = b1 - b2 * ht_c;
+  const double un = uc[D];
+  // left-eigenvector coefficients
+  const double A0 = 0.5 * (b1 + un * cs_c_i), An = -0.5 * (b2 * un + cs_c_i);
+  const double C0 = 0.5 * (b1 - un * cs_c_i), Cn = -0.5 * (b2 * un - cs_c_i);
+  const double At1 = -0.5 * (b2 * uc[T1]), At2 = -0.5 * (b2 * uc[T2]);
+  const double hb2 = 0.5 * b2;
+  const double B1 = b2 * uc[0], B2 = b2 * uc[1], B3 = b2 * uc[2];
+  const double opx = 1.0 + xi;
+  const double E0 = opx * q, E1 = -opx * uc[0], E2 = -opx * uc[1], E3 = -opx * uc[2];
+
+  // ---- stencil eigenvalue maxima (LLF) and shock flag
+  double lm0 = -1.0, lm1 = -1.0, lm2 = -1.0;
+  bool shk = false;
+#pragma unroll
+  for (int st = 0; st < 6; ++st) {
+    const long long ps = p0 + st * stride;
+    const double u_s = prim[(PR_U + D) * nc + ps], c_s = prim[PR_CS * nc + ps];
+    lm0 = fmax(fabs(u_s - c_s), lm0);
+    lm1 = fmax(fabs(u_s), lm1);
+    lm2 = fmax(fabs(u_s + c_s), lm2);
+    shk = shk || (sensor[ps] != 0);
+  }
+  shk = shk && (weno_avg != 0);
+
+  double gh[NV];
+  if (!shk) {
+    // linear WENO5 (wenorec_nw): accumulate while streaming over the stencil
+    double am[NV], ap[NV];
+#pragma unroll
+    for (int m = 0; m < NV; ++m) { am[m] = 0.0; ap[m] = 0.0; }
+    // reference (mirrored) coefficients on points 0..4 ('-') and 1..5 ('+')
+    const double cmr[6] = {-3.0, 27.0, 47.0, -13.0, 2.0, 0.0};
+    const double cpr[6] = {0.0, 2.0, -13.0, 47.0, 27.0, -3.0};
+    const double cmf[6] = {2.0, -13.0, 47.0, 27.0, -3.0, 0.0};
+    const double cpf[6] = {0.0, -3.0, 27.0, 47.0, -13.0, 2.0};
+#pragma unroll
+    for (int st = 0; st < 6; ++st) {
+      const long long ps = p0 + st * stride;
+      double w[NV], f[NV];
+#pragma unroll
+      for (int m = 0; m < NV; ++m) w[m] = v[m * nc + ps];
+      const double u_s = prim[(PR_U + D) * nc + ps], P_s = prim[PR_P * nc + ps];
+      f[0] = w[1 + D];
+      f[1] = w[1] * u_s; f[2] = w[2] * u_s; f[3] = w[3] * u_s;
+      f[1 + D] = w[1 + D] * u_s + P_s;
+      f[4] = u_s * (w[4] + P_s);
+#pragma unroll
+      for (int l = IZEM_NIV; l < NV; ++l) f[l] = w[l] * u_s;
+      const double ccm = linfix ? cmf[st] : cmr[st];
+      const double ccp = linfix ? cpf[st] : cpr[st];
+      // project w and f
+      double sw = 0.0, sf = 0.0;
+#pragma unroll
+      for (int l = 0; l < NRV; ++l) { sw = sw + psi[l] * w[IZEM_NIV + l]; sf = sf + psi[l] * f[IZEM_NIV + l]; }
+      const double Gw = -b1 * w[0] + B1 * w[1] + B2 * w[2] + B3 * w[3] - b2 * w[4] - b2 * sw;
+      const double Gf = -b1 * f[0] + B1 * f[1] + B2 * f[2] + B3 * f[3] - b2 * f[4] - b2 * sf;
+      double pw[NV], pf[NV];
+      pw[0] = A0 * w[0] + An * w[1 + D] + At1 * w[1 + T1] + At2 * w[1 + T2] + hb2 * w[4] + hb2 * sw;
+      pf[0] = A0 * f[0] + An * f[1 + D] + At1 * f[1 + T1] + At2 * f[1 + T2] + hb2 * f[4] + hb2 * sf;
+      pw[1] = w[0] + Gw;
+      pf[1] = f[0] + Gf;
+      pw[2] = C0 * w[0] + Cn * w[1 + D] + At1 * w[1 + T1] + At2 * w[1 + T2] + hb2 * w[4] + hb2 * sw;
+      pf[2] = C0 * f[0] + Cn * f[1 + D] + At1 * f[1 + T1] + At2 * f[1 + T2] + hb2 * f[4] + hb2 * sf;
+      pw[3] = -uc[T1] * w[0] + w[1 + T1];
+      pf[3] = -uc[T1] * f[0] + f[1 + T1];
+      pw[4] = -uc[T2] * w[0] + w[1 + T2];
+      pf[4] = -uc[T2] * f[0] + f[1 + T2];
+      pw[5] = E0 * w[0] + E1 * w[1] + E2 * w[2] + E3 * w[3] + opx * w[4] + xi * sw;
+      pf[5] = E0 * f[0] + E1 * f[1] + E2 * f[2] + E3 * f[3] + opx * f[4] + xi * sf;
+#pragma unroll
+      for (int s = 0; s < NRV - 1; ++s) {
+        pw[6 + s] = Yc[s] * Gw + w[IZEM_NIV + s];
+        pf[6 + s] = Yc[s] * Gf + f[IZEM_NIV + s];
+      }
+#pragma unroll
+      for (int m = 0; m < NV; ++m) {
+        const double lam = m == 0 ? lm0 : (m == 2 ? lm2 : lm1);
+        const double gp = 0.5 * (pf[m] + lam * pw[m]);
+        const double gmn = pf[m] - gp;
+        am[m] = am[m] + ccm * gp;
+        ap[m] = ap[m] + ccp * gmn;
+      }
+    }
+#pragma unroll
+    for (int m = 0; m < NV; ++m) gh[m] = am[m] * (1.0 / 60.0) + ap[m] * (1.0 / 60.0);
+  } else {
+    // nonlinear WENO5 (wenorec): keep the 6 stencil values of every field
+    double gpl[NV][6], gmi[NV][6];
+#pragma unroll 1
+    for (int st = 0; st < 6; ++st) {
+      const long long ps = p0 + st * stride;
+      double w[NV], f[NV];
+#pragma unroll
+      for (int m = 0; m < NV; ++m) w[m] = v[m * nc + ps];
+      const double u_s = prim[(PR_U + D) * nc + ps], P_s = prim[PR_P * nc + ps];
+      f[0] = w[1 + D];
+      f[1] = w[1] * u_s; f[2] = w[2] * u_s; f[3] = w[3] * u_s;
+      f[1 + D] = w[1 + D] * u_s + P_s;
+      f[4] = u_s * (w[4] + P_s);
+#pragma unroll
+      for (int l = IZEM_NIV; l < NV; ++l) f[l] = w[l] * u_s;
+      double sw = 0.0, sf = 0.0;
+#pragma unroll
+      for (int l = 0; l < NRV; ++l) { sw = sw + psi[l] * w[IZEM_NIV + l]; sf = sf + psi[l] * f[IZEM_NIV + l]; }
+      const double Gw = -b1 * w[0] + B1 * w[1] + B2 * w[2] + B3 * w[3] - b2 * w[4] - b2 * sw;
+      const double Gf = -b1 * f[0] + B1 * f[1] + B2 * f[2] + B3 * f[3] - b2 * f[4] - b2 * sf;
+      double pw[NV], pf[NV];
+      pw[0] = A0 * w[0] + An * w[1 + D] + At1 * w[1 + T1] + At2 * w[1 + T2] + hb2 * w[4] + hb2 * sw;
+      pf[0] = A0 * f[0] + An * f[1 + D] + At1 * f[1 + T1] + At2 * f[1 + T2] + hb2 * f[4] + hb2 * sf;
+      pw[1] = w[0] + Gw;
+      pf[1] = f[0] + Gf;
+      pw[2] = C0 * w[0] + Cn * w[1 + D] + At1 * w[1 + T1] + At2 * w[1 + T2] + hb2 * w[4] + hb2 * sw;
+      pf[2] = C0 * f[0] + Cn * f[1 + D] + At1 * f[1 + T1] + At2 * f[1 + T2] + hb2 * f[4] + hb2 * sf;
+      pw[3] = -uc[T1] * w[0] + w[1 + T1];
+      pf[3] = -uc[T1] * f[0] + f[1 + T1];
+      pw[4] = -uc[T2] * w[0] + w[1 + T2];
+      pf[4] = -uc[T2] * f[0] + f[1 + T2];
+      pw[5] = E0 * w[0] + E1 * w[1] + E2 * w[2] + E3 * w[3] + opx * w[4] + xi * sw;
+      pf[5] = E0 * f[0] + E1 * f[1] + E2 * f[2] + E3 * f[3] + opx * f[4] + xi * sf;
+#pragma unroll
+      for (int s = 0; s < NRV - 1; ++s) {
+        pw[6 + s] = Yc[s] * Gw + w[IZEM_NIV + s];
+        pf[6 + s] = Yc[s] * Gf + f[IZEM_NIV + s];
+      }
+#pragma unroll
+      for (int m = 0; m < NV; ++m) {
+        const double lam = m == 0 ? lm0 : (m == 2 ? lm2 : lm1);
+        const double gp = 0.5 * (pf[m] + lam * pw[m]);
+        gpl[m][st] = gp;
+        gmi[m][st] = pf[m] - gp;
+      }
+    }
+#pragma unroll 1
+    for (int m = 0; m < NV; ++m) gh[m] = weno5_nl(gpl[m], gmi[m]);
+  }
+
+  // ---- fhat = R ghat (module_weno.f90:881-989)
+  double fh[NV];
+  fh[0] = gh[0] + gh[1] + gh[2];
+  fh[1 + D] = (un - cs_c) * gh[0] + un * gh[1] + (un + cs_c) * gh[2];
+  fh[1 + T1] = uc[T1] * gh[0] + uc[T1] * gh[1] + uc[T1] * gh[2] + gh[3];
+  fh[1 + T2] = uc[T2] * gh[0] + uc[T2] * gh[1] + uc[T2] * gh[2] + gh[4];
+  fh[4] = (ht_c - un * cs_c) * gh[0] + q * gh[1] + (ht_c + un * cs_c) * gh[2] + uc[T1] * gh[3] + uc[T2] * gh[4] + gh[5];
+#pragma unroll
+  for (int s = 0; s < NRV - 1; ++s) fh[IZEM_NIV + s] = Yc[s] * gh[0] + Yc[s] * gh[2] + gh[6 + s];
+  {
+    const double wrk = -1.0 / psi[NRV - 1];
+    double acc = Yc[NRV - 1] * gh[0] + Yc[NRV - 1] * gh[2] + wrk * gh[5];
+#pragma unroll
+    for (int s = 0; s < NRV - 1; ++s) acc = acc + (wrk * psi[s]) * gh[6 + s];
+    fh[NV - 1] = acc;
+  }
+#pragma unroll
+  for (int m = 0; m < NV; ++m) fhat[m * nfaces + idx] = fh[m];
+}
+
+// fl(i) = (fhat(i) - fhat(i-1)) * dx_i(i); the x sweep overwrites, y and z
+// accumulate (module_weno.f90:995-1020, 1534-1558).
+template <int D>
+__global__ void k_flux_diff(Geo g, int nv, const double* __restrict__ fhat, long long nfaces,
+                            const double* __restrict__ dxi, double* __restrict__ fl, int accumulate) {
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= g.nint) return;
+  int i = (int)(idx % g.n[0]) + 1;
+  long long r = idx / g.n[0];
+  int j = (int)(r % g.n[1]) + 1;
+  int k = (int)(r / g.n[1]) + 1;
+  // face index of the right face (s) in the face grid of axis D
+  long long fr, fl_;
+  int s;
+  if (D == 0) { s = i; fr = (long long)i + (long long)(g.n[0] + 1) * ((j - 1) + (long long)g.n[1] * (k - 1)); fl_ = fr - 1; }
+  else if (D == 1) { s = j; fr = (long long)(i - 1) + (long long)g.n[0] * (j + (long long)(g.n[1] + 1) * (k - 1)); fl_ = fr - g.n[0]; }
+  else { s = k; fr = (long long)(i - 1) + (long long)g.n[0] * ((j - 1) + (long long)g.n[1] * k); fl_ = fr - (long long)g.n[0] * g.n[1]; }
+  const double di = dxi[s - 1 + g.ng];
+  for (int m = 0; m < nv; ++m) {
+    double df = (fhat[m * nfaces + fr] - fhat[m * nfaces + fl_]) * di;
+    long long o = (long long)m * g.nint + idx;
+    fl[o] = accumulate ? fl[o] + df : df;
+  }
+}
+
+// K3: Adams-Shariff sensor, sticky (only ever sets).  Interior neighbour tests
+// along +x, +y, +z (module_tools.f90:2756-2812).
+__global__ void k_sensor(Geo g, double mrw, const double* __restrict__ v, const double* __restrict__ T,
+                         const double* __restrict__ W_i, uint8_t* __restrict__ sensor) {
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= g.nint) return;
+  int c[3];
+  c[0] = (int)(idx % g.n[0]) + 1;
+  long long r = idx / g.n[0];
+  c[1] = (int)(r % g.n[1]) + 1;
+  c[2] = (int)(r / g.n[1]) + 1;
+  const long long p = gid(g, c[0], c[1], c[2]);
+  const double rho = v[p];
+  const double rho_i = 1.0 / rho;
+  const double P = rho * T[p] * W_i[p];
+  bool set = false;
+  const long long strides[3] = {1LL, (long long)g.g[0], (long long)g.g[0] * g.g[1]};
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    if (c[d] <= g.n[d] - 1) {
+      const long long q = p + strides[d];
+      const double rq = v[q];
+      const double rho_iq = 1.0 / rq;
+      const double Pq = rq * T[q] * W_i[q];
+      const double drho = fabs(rq - rho) * fmin(rho_i, rho_iq);
+      const double dpres = fabs(Pq - P) / fmin(P, Pq);
+      if (drho > mrw && dpres > mrw) set = true;
+    }
+  }
+  if (set) sensor[p] = 1;
+}

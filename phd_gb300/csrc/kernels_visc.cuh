@@ -1,0 +1,248 @@
+// Viscous and species-diffusion fluxes with fitted mixture transport:
+// viscflux_xyz (module_viscflux.f90:1660-2189), prim_vis_vars
+// (module_thermodynamics.f90:989-1230), the central / one-sided first
+// derivatives of module_deriv.f90 (dx, d?_fixed1, d?_fixed2 share one
+// arithmetic) and comm_deriv (module_parallel.f90:1788) as a periodic wrap.
+#pragma once
+#include "common.cuh"
+#include "kernels_euler.cuh"
+
+// module_deriv.f90:25-66 (ng = 3)
+__device__ __forceinline__ double deriv_at(const double* __restrict__ a, long long p, long long stride, int s, int n,
+                                           int lo_b, int hi_b, double di) {
+  if (lo_b && s <= 3) {
+    if (s == 1) {
+      double dd = (-25.0 / 12.0) * a[p] + (48.0 / 12.0) * a[p + stride] + (-36.0 / 12.0) * a[p + 2 * stride] +
+                  (16.0 / 12.0) * a[p + 3 * stride] + (-3.0 / 12.0) * a[p + 4 * stride];
+      return dd * di;
+    } else if (s == 2) {
+      double dd = (-3.0 / 12.0) * a[p - stride] + (-10.0 / 12.0) * a[p] + (18.0 / 12.0) * a[p + stride] +
+                  (-6.0 / 12.0) * a[p + 2 * stride] + (1.0 / 12.0) * a[p + 3 * stride];
+      return dd * di;
+    } else {
+      double dd = (1.0 / 12.0) * a[p - 2 * stride] + (-8.0 / 12.0) * a[p - stride] + (8.0 / 12.0) * a[p + stride] +
+                  (-1.0 / 12.0) * a[p + 2 * stride];
+      return dd * di;
+    }
+  }
+  if (hi_b && s >= n - 2) {
+    if (s == n - 2) {
+      double dd = (1.0 / 12.0) * a[p - 2 * stride] + (-8.0 / 12.0) * a[p - stride] + (8.0 / 12.0) * a[p + stride] +
+                  (-1.0 / 12.0) * a[p + 2 * stride];
+      return dd * di;
+    } else if (s == n - 1) {
+      double dd = (1.0 / 12.0) * a[p - 3 * stride] + (-6.0 / 12.0) * a[p - 2 * stride] + (18.0 / 12.0) * a[p - stride] +
+                  (-10.0 / 12.0) * a[p] + (-3.0 / 12.0) * a[p + stride];
+      return -dd * di;
+    } else {
+      double dd = (-3.0 / 12.0) * a[p - 4 * stride] + (16.0 / 12.0) * a[p - 3 * stride] + (-36.0 / 12.0) * a[p - 2 * stride] +
+                  (48.0 / 12.0) * a[p - stride] + (-25.0 / 12.0) * a[p];
+      return -dd * di;
+    }
+  }
+  double dd = (-1.0 / 60.0) * a[p - 3 * stride] + (9.0 / 60.0) * a[p - 2 * stride] + (-45.0 / 60.0) * a[p - stride] +
+              (45.0 / 60.0) * a[p + stride] + (-9.0 / 60.0) * a[p + 2 * stride] + (1.0 / 60.0) * a[p + 3 * stride];
+  return dd * di;
+}
+
+struct Metrics {
+  const double* dxi[3];   // indexed (s - 1 + ng)
+};
+
+// First derivatives of u, v, w, T (fd 1..12) and of the mole fractions
+// (fd 13.. : 3 per species) at interior points (module_viscflux.f90:1764-1804).
+template <int NRV>
+__global__ void k_grad(Geo g, Metrics mt, const double* __restrict__ prim, const double* __restrict__ T,
+                       const double* __restrict__ Xa, double* __restrict__ fd) {
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= g.nint) return;
+  int c[3];
+  c[0] = (int)(idx % g.n[0]) + 1;
+  long long r = idx / g.n[0];
+  c[1] = (int)(r % g.n[1]) + 1;
+  c[2] = (int)(r / g.n[1]) + 1;
+  const long long nc = g.ncell;
+  const long long p = gid(g, c[0], c[1], c[2]);
+  const long long strides[3] = {1LL, (long long)g.g[0], (long long)g.g[0] * g.g[1]};
+  const double* src[4] = {prim + PR_U * nc, prim + PR_V * nc, prim + PR_W * nc, T};
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const double di = mt.dxi[d][c[d] - 1 + g.ng];
+    const int lo = g.bnd[2 * d], hi = g.bnd[2 * d + 1];
+#pragma unroll
+    for (int s = 0; s < 4; ++s) fd[(3 * s + d) * nc + p] = deriv_at(src[s], p, strides[d], c[d], g.n[d], lo, hi, di);
+#pragma unroll
+    for (int l = 0; l < NRV; ++l)
+      fd[(12 + 3 * l + d) * nc + p] = deriv_at(Xa + l * nc, p, strides[d], c[d], g.n[d], lo, hi, di);
+  }
+}
+
+// Periodic wrap of the face-ghost slabs of an ncomp-component ghosted array.
+__global__ void k_wrap_periodic(Geo g, int ncomp, double* __restrict__ a) {
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long ntot = slab_count(g) - g.nint;
+  if (idx >= ntot) return;
+  int i, j, k, dom;
+  if (!slab_point(g, idx + g.nint, i, j, k, dom)) return;
+  const int f = dom - 1, d = f >> 1;
+  if (g.bc[f] != IZEM_BC_PERIODIC) return;
+  int c[3] = {i, j, k};
+  c[d] = (f & 1) ? c[d] - g.n[d] : c[d] + g.n[d];
+  const long long p = gid(g, i, j, k), q = gid(g, c[0], c[1], c[2]);
+  for (int m = 0; m < ncomp; ++m) a[(long long)m * g.ncell + p] = a[(long long)m * g.ncell + q];
+}
+
+// Transport properties, stresses, diffusion velocities with correction
+// velocity, and heat flux at interior points and at the ghost slabs of
+// periodic faces (domain_id = -3..3).  Writes tau (6), q (3) and overwrites
+// the species gradients of fd with rho Y_k V_k (module_viscflux.f90:1943-2062).
+template <int NRV>
+__global__ void k_visc_point(Geo g, const double* __restrict__ v, const double* __restrict__ T,
+                             const double* __restrict__ W_i, const double* __restrict__ ha,
+                             const double* __restrict__ Xa, double* __restrict__ fd,
+                             double* __restrict__ tau, double* __restrict__ qv) {
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  int i, j, k, dom;
+  if (!slab_point(g, idx, i, j, k, dom)) return;
+  if (dom > 0 && g.bnd[dom - 1]) return;
+  const long long nc = g.ncell;
+  const long long p = gid(g, i, j, k);
+  const double rho = v[p], Tp = T[p], Wi = W_i[p];
+  double X[NRV];
+#pragma unroll
+  for (int l = 0; l < NRV; ++l) X[l] = Xa[l * nc + p];
+  // ---- prim_vis_vars for one point
+  const double lt1 = log(Tp * c_thd.tinf);
+  const double lt2 = lt1 * lt1, lt3 = lt2 * lt1;
+  const double P = rho * Tp * Wi;
+  const double epsm12 = 1.0e-12;
+  double dm[NRV], wk1[NRV], xe[NRV], aw[NRV];
+#pragma unroll
+  for (int l = 0; l < NRV; ++l) {
+    xe[l] = X[l] + epsm12;
+    aw[l] = xe[l] * c_thd.Wc[l] * Wi;
+    dm[l] = 0.0;
+    wk1[l] = 0.0;
+  }
+#pragma unroll
+  for (int m = 0; m < NRV; ++m)
+#pragma unroll
+    for (int l = m + 1; l < NRV; ++l) {
+      const double* cf = c_thd.cofd[m][l];
+      const double dkj = 0.0 + cf[0] * 1.0 + cf[1] * lt1 + cf[2] * lt2 + cf[3] * lt3;
+      const double e = 1.0 / exp(dkj);
+      dm[m] = dm[m] + xe[l] * e;   // order over l preserved for every m
+      dm[l] = dm[l] + xe[m] * e;
+      wk1[m] = wk1[m] + aw[l];
+      wk1[l] = wk1[l] + aw[m];
+    }
+#pragma unroll
+  for (int m = 0; m < NRV; ++m) dm[m] = wk1[m] * c_thd.Kd[m] / (dm[m] * P);
+  double ct = 0.0, w1 = 0.0, eta[NRV], seta[NRV], reta[NRV];
+#pragma unroll
+  for (int l = 0; l < NRV; ++l) {
+    const double* cl = c_thd.coflam[l];
+    const double c1 = exp(0.0 + cl[0] * 1.0 + cl[1] * lt1 + cl[2] * lt2 + cl[3] * lt3);
+    ct = ct + X[l] / c1;
+    w1 = w1 + X[l] * c1;
+    const double* ce = c_thd.cofeta[l];
+    eta[l] = exp(0.0 + ce[0] * 1.0 + ce[1] * lt1 + ce[2] * lt2 + ce[3] * lt3);
+    seta[l] = sqrt(eta[l]);
+    reta[l] = 1.0 / seta[l];
+  }
+  ct = c_thd.Kl * (1.0 / ct + w1);
+  double mu = 0.0;
+#pragma unroll
+  for (int m = 0; m < NRV; ++m) {
+    double c4 = 0.0;
+#pragma unroll
+    for (int l = 0; l < NRV; ++l) {
+      const double c3 = 1.0 + c_thd.wilke_c1[m][l] * (seta[m] * reta[l]);
+      c4 = c4 + c3 * c3 * c_thd.wilke_c2[m][l] * X[l];
+    }
+    mu = mu + c_thd.Ku * (eta[m] * X[m] / c4);
+  }
+  // ---- stresses, diffusion and heat fluxes
+  auto F = [&](int q1) -> double { return fd[(long long)(q1 - 1) * nc + p]; };
+  const double rho_i = 1.0 / rho;
+  const double uxs = v[nc + p] * rho_i, vys = v[2 * nc + p] * rho_i, wzs = v[3 * nc + p] * rho_i;
+  const double rmu = -c_thd.sqgmr * mu;
+  const double rvd = c_thd.rvd0 * rho;
+  const double twothirds = 2.0 / 3.0;
+  const double sxx = twothirds * rmu * (F(1) + F(1) - (F(5) + F(9)));
+  const double sxy = rmu * (F(4) + F(2));
+  const double sxz = rmu * (F(7) + F(3));
+  const double syy = twothirds * rmu * (F(5) + F(5) - (F(1) + F(9)));
+  const double syz = rmu * (F(8) + F(6));
+  const double szz = twothirds * rmu * (F(9) + F(9) - (F(1) + F(5)));
+  double vdcx = 0.0, vdcy = 0.0, vdcz = 0.0;
+#pragma unroll
+  for (int l = 0; l < NRV; ++l) {
+    const double wrk = dm[l] * c_thd.Wc[l] * Wi;
+    vdcx = vdcx + wrk * F(13 + 3 * l);
+    vdcy = vdcy + wrk * F(14 + 3 * l);
+    vdcz = vdcz + wrk * F(15 + 3 * l);
+  }
+  double vdhx = 0.0, vdhy = 0.0, vdhz = 0.0;
+#pragma unroll
+  for (int l = 0; l < NRV; ++l) {
+    const double Ya = v[(IZEM_NIV + l) * nc + p] * rho_i;
+    const double wrk = -dm[l] * c_thd.Wc[l] * Wi;
+    const double vtx = vdcx * Ya + wrk * F(13 + 3 * l);
+    const double vty = vdcy * Ya + wrk * F(14 + 3 * l);
+    const double vtz = vdcz * Ya + wrk * F(15 + 3 * l);
+    const double jx = rvd * vtx, jy = rvd * vty, jz = rvd * vtz;
+    fd[(long long)(12 + 3 * l) * nc + p] = jx;
+    fd[(long long)(13 + 3 * l) * nc + p] = jy;
+    fd[(long long)(14 + 3 * l) * nc + p] = jz;
+    const double h = ha[l * nc + p];
+    vdhx = vdhx + h * jx;
+    vdhy = vdhy + h * jy;
+    vdhz = vdhz + h * jz;
+  }
+  const double rlam = -c_thd.rlam0 * ct;
+  tau[0 * nc + p] = sxx; tau[1 * nc + p] = sxy; tau[2 * nc + p] = sxz;
+  tau[3 * nc + p] = syy; tau[4 * nc + p] = syz; tau[5 * nc + p] = szz;
+  qv[0 * nc + p] = uxs * sxx + vys * sxy + wzs * sxz + rlam * F(10) + vdhx;
+  qv[1 * nc + p] = uxs * sxy + vys * syy + wzs * syz + rlam * F(11) + vdhy;
+  qv[2 * nc + p] = uxs * sxz + vys * syz + wzs * szz + rlam * F(12) + vdhz;
+}
+
+// Divergence of the viscous fluxes added to f (module_viscflux.f90:2098-2183).
+template <int NRV>
+__global__ void k_visc_div(Geo g, Metrics mt, const double* __restrict__ tau, const double* __restrict__ qv,
+                           const double* __restrict__ fd, double* __restrict__ fl) {
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= g.nint) return;
+  int c[3];
+  c[0] = (int)(idx % g.n[0]) + 1;
+  long long r = idx / g.n[0];
+  c[1] = (int)(r % g.n[1]) + 1;
+  c[2] = (int)(r / g.n[1]) + 1;
+  const long long nc = g.ncell;
+  const long long p = gid(g, c[0], c[1], c[2]);
+  const long long st[3] = {1LL, (long long)g.g[0], (long long)g.g[0] * g.g[1]};
+  double di[3];
+  int lo[3], hi[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    di[d] = mt.dxi[d][c[d] - 1 + g.ng];
+    lo[d] = g.bnd[2 * d];
+    hi[d] = g.bnd[2 * d + 1];
+  }
+  auto div3 = [&](const double* ax, const double* ay, const double* az) {
+    const double wx = deriv_at(ax, p, st[0], c[0], g.n[0], lo[0], hi[0], di[0]);
+    const double wy = deriv_at(ay, p, st[1], c[1], g.n[1], lo[1], hi[1], di[1]);
+    const double wz = deriv_at(az, p, st[2], c[2], g.n[2], lo[2], hi[2], di[2]);
+    return wx + wy + wz;
+  };
+  const long long ni = g.nint;
+  fl[1 * ni + idx] = fl[1 * ni + idx] + div3(tau + 0 * nc, tau + 1 * nc, tau + 2 * nc);
+  fl[2 * ni + idx] = fl[2 * ni + idx] + div3(tau + 1 * nc, tau + 3 * nc, tau + 4 * nc);
+  fl[3 * ni + idx] = fl[3 * ni + idx] + div3(tau + 2 * nc, tau + 4 * nc, tau + 5 * nc);
+  fl[4 * ni + idx] = fl[4 * ni + idx] + div3(qv + 0 * nc, qv + 1 * nc, qv + 2 * nc);
+#pragma unroll
+  for (int l = 0; l < NRV; ++l)
+    fl[(IZEM_NIV + l) * ni + idx] = fl[(IZEM_NIV + l) * ni + idx] +
+        div3(fd + (12 + 3 * l) * nc, fd + (13 + 3 * l) * nc, fd + (14 + 3 * l) * nc);
+}

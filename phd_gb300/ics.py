@@ -1,0 +1,167 @@
+"""Seeded synthetic workloads (initial conditions, grids, switches).
+
+The reference hard-codes every initial condition in module_ICs.f90 and has no
+Taylor-Green or temporal mixing-layer case that matches the benchmark
+configurations, so these generators build them.  Each returns the raw state
+(interior filled, ghosts extrapolated, temperature guess everywhere) in code
+units; the caller closes it with ``finalize_ic`` (module_ICs.f90:2874-2879),
+on the GPU (IzemGPU.finalize_ic) or on the oracle, exactly as the reference's
+init routines end.
+
+Workloads:
+* ``tgv``           Taylor-Green vortex, periodic n^3 box of side 2*pi*L0,
+                    Mach 0.1, Re = 1600, calorically perfect air (gamma 1.4).
+* ``mixing_layer``  temporal H2/air mixing layer, 9 species, x/z periodic,
+                    y zero-gradient; tanh profile of thickness 0.5 mm,
+                    dU = 100 m/s, 1% seeded white-noise velocity.
+"""
+import math
+
+import numpy as np
+
+from .capi import BC_EXTRAPOLATION, BC_PERIODIC, IzemCfg
+from .thd import adi_struct, constants, load_species, thd_init
+
+SEED = 20261203
+
+
+def make_cfg(nx, ny, nz, nrv, bc=(BC_PERIODIC,) * 6, vis=1, weno_avg=1, max_rel_weight=0.15, forcesum=1,
+             reaction=0, eglib=0, cfl=0.5, cflmin=0.1, cpr=0.1, fo=0.5, vis_dt=0, linfix=0):
+    c = IzemCfg()
+    c.nx, c.ny, c.nz, c.ng, c.ndim, c.nrv = nx, ny, nz, 3, 3, nrv
+    for f in range(6):
+        c.bc[f] = bc[f]
+    c.weno_avg = weno_avg
+    c.max_rel_weight = max_rel_weight
+    c.vis, c.eglib, c.forcesum, c.reaction, c.vis_dt = vis, eglib, forcesum, reaction, vis_dt
+    c.cfl, c.cflmin, c.cpr, c.fo = cfl, cflmin, cpr, fo
+    c.weno5_linear_fix = linfix
+    return c
+
+
+def ha_code(thd, T):
+    """Species enthalpies in code units at code temperature T (array), the
+    NASA-7 evaluation of ha_scalar (module_thermodynamics.f90:873-978)."""
+    T = np.asarray(T, dtype=np.float64)
+    ns = thd.nspc
+    out = np.empty(T.shape + (ns,))
+    for k in range(ns):
+        tk = T * thd.tinf
+        res = np.empty_like(tk)
+        for rng, mask in ((0, tk < thd.tpolylim[k]), (1, tk >= thd.tpolylim[k])):
+            a = [thd.heatcap[k][rng][c] for c in range(7)]
+            t = np.clip(tk, thd.tpolymin[k], thd.tpolymax[k])
+            h = a[0] * t + a[1] * t ** 2 * 0.5 + a[2] * t ** 3 / 3.0 + a[3] * t ** 4 * 0.25 + a[4] * t ** 5 * 0.2 + a[5]
+            cp = a[0] + a[1] * t + a[2] * t ** 2 + a[3] * t ** 3 + a[4] * t ** 4
+            h = h + cp * (tk - t)
+            res = np.where(mask, h, res)
+        out[..., k] = thd.Wc_i[k] / thd.tinf * res
+    return out
+
+
+def grid_dxi(coord_m, ng, adi, lib_dscalar):
+    """dx_i over (1-ng .. n+ng) in code units: dscalar on the global
+    coordinates, inverted, times L_ref; ghost entries stay 1*L_ref
+    (module_tools.f90:374-432, 185-187)."""
+    n = len(coord_m)
+    inner = lib_dscalar(np.asarray(coord_m, dtype=np.float64), ng)
+    out = np.full(n + 2 * ng, 1.0)
+    out[ng:ng + n] = inner
+    return out * adi["l_ref"]
+
+
+def _state_from_primitives(thd, a, rho_d, u_d, v_d, w_d, T_d, Y, ng):
+    """Fill a ghosted state from dimensional interior primitives (interior
+    arrays of shape (nx,ny,nz)), ghosts by zero-gradient extension."""
+    nx, ny, nz = rho_d.shape
+    nrv = thd.nspc
+    rho = rho_d / a["rho_ref"]
+    u, v, w = u_d / a["u_ref"], v_d / a["u_ref"], w_d / a["u_ref"]
+    T = T_d / a["t_ref"]
+    W_i = np.zeros_like(T)
+    for k in range(nrv):
+        W_i += Y[..., k] * thd.Wc_i[k]
+    P = rho * T * W_i
+    ha = ha_code(thd, T)
+    hm = np.einsum("...k,...k->...", ha, Y)
+    cons = np.empty((nx, ny, nz, 5 + nrv))
+    cons[..., 0] = rho
+    cons[..., 1] = rho * u
+    cons[..., 2] = rho * v
+    cons[..., 3] = rho * w
+    cons[..., 4] = rho * hm - P + 0.5 * rho * (u * u + v * v + w * w)
+    for k in range(nrv):
+        cons[..., 5 + k] = rho * Y[..., k]
+    pad = ((ng, ng), (ng, ng), (ng, ng))
+    vg = np.empty((nx + 2 * ng, ny + 2 * ng, nz + 2 * ng, 5 + nrv), order="F")
+    for q in range(5 + nrv):
+        vg[..., q] = np.pad(cons[..., q], pad, mode="edge")
+    Tg = np.asfortranarray(np.pad(T, pad, mode="edge"))
+    shp = vg.shape[:3]
+    return {"v": vg, "T": Tg, "W_i": np.zeros(shp, order="F"), "cp": np.zeros(shp, order="F"),
+            "ha": np.zeros(shp + (nrv,), order="F"), "shock_sensor": np.zeros(shp, dtype=np.uint8, order="F")}
+
+
+def tgv(n=64, lib_dscalar=None):
+    """Taylor-Green vortex: periodic n^3, box 2*pi*L0, Mach 0.1, Re 1600."""
+    a = constants()
+    sp = load_species("air2")
+    thd = thd_init(sp, a)
+    W = sp["W_gmol"][0] * 1e-3
+    Rm = a["r_ref"] / W
+    T0, p0 = 300.0, 101325.0
+    c0 = math.sqrt(1.4 * Rm * T0)
+    U0 = 0.1 * c0
+    rho0 = p0 / (Rm * T0)
+    ce = sp["cofeta"][0]
+    mu0 = math.exp(ce[0] + ce[1] * math.log(T0)) * 0.1
+    L0 = 1600.0 * mu0 / (rho0 * U0)
+    h = 2.0 * math.pi * L0 / n
+    x = np.arange(n) * h
+    X, Y_, Z = np.meshgrid(x / L0, x / L0, x / L0, indexing="ij")
+    u = U0 * np.sin(X) * np.cos(Y_) * np.cos(Z)
+    v = -U0 * np.cos(X) * np.sin(Y_) * np.cos(Z)
+    w = np.zeros_like(u)
+    p = p0 + rho0 * U0 * U0 / 16.0 * (np.cos(2 * X) + np.cos(2 * Y_)) * (np.cos(2 * Z) + 2.0)
+    T = np.full_like(u, T0)
+    rho = p / (Rm * T)
+    Ys = np.zeros(u.shape + (2,))
+    Ys[..., 0] = 0.5
+    Ys[..., 1] = 0.5
+    state = _state_from_primitives(thd, a, rho, u, v, w, T, Ys, 3)
+    cfg = make_cfg(n, n, n, 2)
+    dxi = [grid_dxi(x, 3, a, lib_dscalar) for _ in range(3)]
+    info = {"L0": L0, "U0": U0, "rho0": rho0, "T0": T0, "p0": p0, "mu0": mu0,
+            "t_conv": L0 / U0, "name": "TGV %d^3 Ma 0.1 Re 1600" % n}
+    return cfg, thd, adi_struct(a), dxi, state, info
+
+
+def mixing_layer(nx=256, ny=256, nz=128, Lx=12e-3, Ly=12e-3, Lz=6e-3, seed=SEED, lib_dscalar=None):
+    """Temporal H2/air mixing layer (9 species), x and z periodic, y extrapolation."""
+    a = constants()
+    sp = load_species("h2air9")
+    thd = thd_init(sp, a)
+    names = sp["names"]
+    ix = {nm: q for q, nm in enumerate(names)}
+    delta, dU, p0 = 0.5e-3, 100.0, 101325.0
+    x = np.arange(nx) * (Lx / nx)
+    z = np.arange(nz) * (Lz / nz)
+    y = -0.5 * Ly + np.arange(ny) * (Ly / (ny - 1))
+    Xg, Yg, Zg = np.meshgrid(x, y, z, indexing="ij")
+    f = 0.5 * (1.0 + np.tanh(Yg / delta))
+    Yf = np.zeros(len(names)); Yf[ix["H2"]] = 0.5; Yf[ix["N2"]] = 0.5
+    Yo = np.zeros(len(names)); Yo[ix["O2"]] = 0.233; Yo[ix["N2"]] = 0.767
+    Ys = (1.0 - f)[..., None] * Yf + f[..., None] * Yo
+    T = (1.0 - f) * 1000.0 + f * 1200.0
+    rng = np.random.Generator(np.random.PCG64(seed))
+    u = 0.5 * dU * np.tanh(Yg / delta) + 0.01 * dU * rng.standard_normal(Xg.shape)
+    v = 0.01 * dU * rng.standard_normal(Xg.shape)
+    w = 0.01 * dU * rng.standard_normal(Xg.shape)
+    Wmix_i = np.einsum("...k,k->...", Ys, 1.0 / (np.array(sp["W_gmol"]) * 1e-3))
+    rho = p0 / (a["r_ref"] * Wmix_i * T)
+    state = _state_from_primitives(thd, a, rho, u, v, w, T, Ys, 3)
+    bc = (BC_PERIODIC, BC_PERIODIC, BC_EXTRAPOLATION, BC_EXTRAPOLATION, BC_PERIODIC, BC_PERIODIC)
+    cfg = make_cfg(nx, ny, nz, 9, bc=bc)
+    dxi = [grid_dxi(x, 3, a, lib_dscalar), grid_dxi(y, 3, a, lib_dscalar), grid_dxi(z, 3, a, lib_dscalar)]
+    info = {"name": "H2/air temporal mixing layer %dx%dx%d" % (nx, ny, nz), "delta": delta, "dU": dU, "seed": seed}
+    return cfg, thd, adi_struct(a), dxi, state, info

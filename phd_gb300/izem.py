@@ -1,0 +1,223 @@
+"""Python host mirror of the IZEM hot-path interface over the C ABI.
+
+The reference's Fortran driver calls, per time step (izem.f90:242-389):
+``timestep`` (module_solver.f90:202), then ``rk3`` (module_solver.f90:694),
+whose stages call the shock sensor, ``euler_LLF_x/_y/_z``
+(module_weno.f90:537/1055/1595) and ``viscflux_xyz`` (module_viscflux.f90:
+1660).  ``IzemGPU`` exposes the same operations, with the same argument
+meaning and error behaviour (a non-zero status raises ``IzemError``; the
+reference aborts through abort_mpi), on a device-resident state held by the
+``libizem_gpu.so`` C library.  Arrays are numpy arrays in the reference's
+Fortran layout: ``v`` has shape (nx+2ng, ny+2ng, nz+2ng, nv), order='F'.
+
+There is no CPU fallback: if the CUDA library cannot be loaded this module
+raises at import of the library.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import capi
+from .capi import IzemAdi, IzemCfg, IzemThd
+
+_LIB = None
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "libizem_gpu.so")
+
+_dp = C.POINTER(C.c_double)
+_u8p = C.POINTER(C.c_uint8)
+
+
+class IzemError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s (%d): %s" % (capi.ERR_NAMES.get(code, "error"), code, msg))
+        self.code = code
+
+
+def load_library(path=None):
+    """Load the CUDA library (built by phd_gb300.build.build_gpu)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise RuntimeError("libizem_gpu.so is not built (%s); run __graft_entry__.build()" % path)
+    lib = C.CDLL(path)
+    P = C.c_void_p
+    sig = {
+        "izem_gpu_init": (C.c_int, [C.POINTER(IzemCfg), C.POINTER(IzemThd), C.POINTER(IzemAdi), C.POINTER(P)]),
+        "izem_gpu_destroy": (None, [P]),
+        "izem_gpu_last_error": (C.c_int, [P, C.c_char_p, C.c_int]),
+        "izem_gpu_set_grid": (C.c_int, [P, _dp, _dp, _dp]),
+        "izem_gpu_upload_state": (C.c_int, [P, _dp, _dp, _dp, _dp, _dp, _u8p]),
+        "izem_gpu_download_state": (C.c_int, [P, _dp, _dp, _dp, _dp, _dp, _u8p]),
+        "izem_gpu_download_flux": (C.c_int, [P, _dp]),
+        "izem_gpu_zero_flux": (C.c_int, [P]),
+        "izem_gpu_shock_sensor": (C.c_int, [P]),
+        "izem_gpu_euler_flux": (C.c_int, [P, C.c_int]),
+        "izem_gpu_visc_flux": (C.c_int, [P]),
+        "izem_gpu_update_primitives": (C.c_int, [P]),
+        "izem_gpu_finalize_ic": (C.c_int, [P]),
+        "izem_gpu_rk3": (C.c_int, [P, C.c_double, C.c_double]),
+        "izem_gpu_timestep": (C.c_int, [P, C.c_double, _dp, _dp]),
+        "izem_gpu_timer_start": (C.c_int, [P]),
+        "izem_gpu_timer_stop": (C.c_int, [P, C.POINTER(C.c_float)]),
+        "izem_gpu_set_kernel_timing": (C.c_int, [P, C.c_int]),
+        "izem_gpu_kernel_times": (C.c_int, [P, C.c_int, C.c_char_p, C.c_int, C.POINTER(C.c_int), _dp,
+                                            C.POINTER(C.c_int)]),
+        "izem_gpu_synchronize": (C.c_int, [P]),
+        "izem_metrics_dscalar": (C.c_int, [C.c_int, C.c_int, _dp, _dp]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _LIB = lib
+    return lib
+
+
+def _ptr(a, kind=_dp):
+    return None if a is None else a.ctypes.data_as(kind)
+
+
+def metrics_dscalar(coord, ng=3):
+    """dscalar + inversion of the reference's metrics for one direction."""
+    lib = load_library()
+    coord = np.ascontiguousarray(coord, dtype=np.float64)
+    out = np.empty_like(coord)
+    rc = lib.izem_metrics_dscalar(len(coord), ng, _ptr(coord), _ptr(out))
+    if rc:
+        raise IzemError(rc, "izem_metrics_dscalar")
+    return out
+
+
+class IzemGPU:
+    """One device-resident block of the IZEM state (one GPU, one process)."""
+
+    def __init__(self, cfg, thd, adi):
+        self.lib = load_library()
+        self.cfg, self.thd, self.adi = cfg, thd, adi
+        self.nv = 5 + cfg.nrv
+        self.ng = cfg.ng
+        self.shape = (cfg.nx + 2 * cfg.ng, cfg.ny + 2 * cfg.ng, cfg.nz + 2 * cfg.ng)
+        h = C.c_void_p()
+        rc = self.lib.izem_gpu_init(C.byref(cfg), C.byref(thd), C.byref(adi), C.byref(h))
+        if rc:
+            raise IzemError(rc, "izem_gpu_init")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.izem_gpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def _check(self, rc, what):
+        if rc:
+            buf = C.create_string_buffer(512)
+            self.lib.izem_gpu_last_error(self.h, buf, 512)
+            raise IzemError(rc, "%s: %s" % (what, buf.value.decode()))
+
+    def newton_warnings(self):
+        return self.lib.izem_gpu_last_error(self.h, None, 0)
+
+    # ---- state ----------------------------------------------------------
+    def set_grid(self, dx_i, dy_i, dz_i):
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (dx_i, dy_i, dz_i)]
+        for a, n in zip(arrs, self.shape):
+            if a.shape != (n,):
+                raise ValueError("metric array has %s entries, expected %d" % (a.shape, n))
+        self._grid = arrs
+        self._check(self.lib.izem_gpu_set_grid(self.h, *[_ptr(a) for a in arrs]), "set_grid")
+
+    def upload(self, v=None, T=None, W_i=None, cp=None, ha=None, shock_sensor=None):
+        def prep(a, dt=np.float64):
+            return None if a is None else np.asfortranarray(a, dtype=dt)
+        v, T, W_i, cp, ha = (prep(a) for a in (v, T, W_i, cp, ha))
+        ss = prep(shock_sensor, np.uint8)
+        self._check(self.lib.izem_gpu_upload_state(self.h, _ptr(v), _ptr(T), _ptr(W_i), _ptr(cp), _ptr(ha),
+                                                   _ptr(ss, _u8p)), "upload_state")
+
+    def download(self):
+        gx, gy, gz = self.shape
+        v = np.empty((gx, gy, gz, self.nv), order="F")
+        T = np.empty((gx, gy, gz), order="F")
+        W_i = np.empty((gx, gy, gz), order="F")
+        cp = np.empty((gx, gy, gz), order="F")
+        ha = np.empty((gx, gy, gz, self.cfg.nrv), order="F")
+        ss = np.empty((gx, gy, gz), dtype=np.uint8, order="F")
+        self._check(self.lib.izem_gpu_download_state(self.h, _ptr(v), _ptr(T), _ptr(W_i), _ptr(cp), _ptr(ha),
+                                                     _ptr(ss, _u8p)), "download_state")
+        return {"v": v, "T": T, "W_i": W_i, "cp": cp, "ha": ha, "shock_sensor": ss}
+
+    def flux(self):
+        fl = np.empty((self.cfg.nx, self.cfg.ny, self.cfg.nz, self.nv), order="F")
+        self._check(self.lib.izem_gpu_download_flux(self.h, _ptr(fl)), "download_flux")
+        return fl
+
+    def zero_flux(self):
+        self._check(self.lib.izem_gpu_zero_flux(self.h), "zero_flux")
+
+    # ---- reference operations ---------------------------------------------
+    def shock_sensor(self):
+        self._check(self.lib.izem_gpu_shock_sensor(self.h), "shock_sensor")
+
+    def euler_LLF(self, direction):
+        self._check(self.lib.izem_gpu_euler_flux(self.h, int(direction)), "euler_LLF")
+
+    def euler_LLF_x(self):
+        self.euler_LLF(0)
+
+    def euler_LLF_y(self):
+        self.euler_LLF(1)
+
+    def euler_LLF_z(self):
+        self.euler_LLF(2)
+
+    def viscflux_xyz(self):
+        self._check(self.lib.izem_gpu_visc_flux(self.h), "viscflux_xyz")
+
+    def update_primitives(self):
+        self._check(self.lib.izem_gpu_update_primitives(self.h), "update_primitives")
+
+    def finalize_ic(self):
+        self._check(self.lib.izem_gpu_finalize_ic(self.h), "finalize_ic")
+
+    def rk3(self, dt, time0=0.0):
+        self._check(self.lib.izem_gpu_rk3(self.h, float(dt), float(time0)), "rk3")
+
+    def timestep(self, DTmax=0.0, dtmin=1.0):
+        dt4 = np.zeros(4)
+        dtm = C.c_double(dtmin)
+        self._check(self.lib.izem_gpu_timestep(self.h, float(DTmax), _ptr(dt4), C.byref(dtm)), "timestep")
+        return dt4, dtm.value
+
+    # ---- timing -----------------------------------------------------------
+    def timer_start(self):
+        self._check(self.lib.izem_gpu_timer_start(self.h), "timer_start")
+
+    def timer_stop(self):
+        ms = C.c_float()
+        self._check(self.lib.izem_gpu_timer_stop(self.h, C.byref(ms)), "timer_stop")
+        return ms.value
+
+    def set_kernel_timing(self, enable):
+        self._check(self.lib.izem_gpu_set_kernel_timing(self.h, int(bool(enable))), "set_kernel_timing")
+
+    def kernel_times(self):
+        n = C.c_int()
+        cap, nl = 64, 48
+        names = C.create_string_buffer(cap * nl)
+        launches = (C.c_int * cap)()
+        ms = (C.c_double * cap)()
+        self._check(self.lib.izem_gpu_kernel_times(self.h, cap, names, nl, launches, ms, C.byref(n)), "kernel_times")
+        out = {}
+        for q in range(min(n.value, cap)):
+            nm = names.raw[q * nl:(q + 1) * nl].split(b"\0")[0].decode()
+            out[nm] = (launches[q], ms[q])
+        return out
+
+    def synchronize(self):
+        self._check(self.lib.izem_gpu_synchronize(self.h), "synchronize")

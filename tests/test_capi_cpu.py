@@ -1,0 +1,57 @@
+"""The C-ABI library loads and exports every entry point of include/*.h
+(no device call is made: this runs without a GPU)."""
+import ctypes as C
+import glob
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        src = open(h).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        for m in re.finditer(r"^\s*(?:int|void|double|float|size_t)\s*\*?\s*(izem_\w+)\s*\(", src, flags=re.M):
+            names.add(m.group(1))
+    return sorted(names)
+
+
+def test_header_declares_entry_points():
+    names = declared_symbols()
+    assert "izem_gpu_init" in names and "izem_gpu_rk3" in names
+    assert len(names) >= 20
+
+
+def test_library_exports_every_declared_symbol():
+    from phd_gb300.build import build_gpu
+    lib_path = build_gpu()
+    lib = C.CDLL(lib_path)
+    missing = [n for n in declared_symbols() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_struct_layout_matches_header():
+    from phd_gb300.build import build_gpu
+    from phd_gb300.capi import IzemAdi, IzemCfg, IzemThd
+    lib = C.CDLL(build_gpu())
+    fn = lib.izem_abi_sizes
+    fn.restype = C.c_int
+    fn.argtypes = [C.POINTER(C.c_size_t)] * 3
+    s = [C.c_size_t() for _ in range(3)]
+    assert fn(*[C.byref(x) for x in s]) == 0
+    assert [x.value for x in s] == [C.sizeof(IzemCfg), C.sizeof(IzemThd), C.sizeof(IzemAdi)]
+
+
+def test_host_metrics_match_oracle():
+    import numpy as np
+    import oracle
+    from phd_gb300.izem import metrics_dscalar
+    from phd_gb300.build import build_gpu
+    build_gpu()
+    rng = np.random.Generator(np.random.PCG64(1))
+    x = np.cumsum(0.5 + rng.random(40))
+    assert np.array_equal(metrics_dscalar(x), oracle.metrics_dscalar(x))

@@ -1,0 +1,49 @@
+"""Small seeded cases shared by the parity tests (sizes the oracle finishes
+in well under a second)."""
+import numpy as np
+
+import oracle
+from phd_gb300 import ics
+
+
+def _copy(state):
+    return {k: np.array(v, order="F", copy=True) for k, v in state.items()}
+
+
+def case(name, n=12, seed=ics.SEED):
+    """Returns cfg, thd, adi, dxi, finalized state (oracle-closed), info."""
+    if name == "tgv":
+        cfg, thd, adi, dxi, st, info = ics.tgv(n, lib_dscalar=oracle.metrics_dscalar)
+    elif name == "mix":
+        cfg, thd, adi, dxi, st, info = ics.mixing_layer(n, n, max(n // 2, 8), Lx=n * 47e-6, Ly=n * 47e-6,
+                                                         Lz=max(n // 2, 8) * 47e-6, seed=seed,
+                                                         lib_dscalar=oracle.metrics_dscalar)
+    else:
+        raise KeyError(name)
+    orc = oracle.Oracle(cfg, thd, adi, *dxi)
+    orc.finalize_ic(st)
+    return cfg, thd, adi, dxi, st, info, orc
+
+
+def perturb(state, amp, seed=7):
+    """Add seeded relative noise to the interior conserved variables (for
+    sensor and nonlinear-WENO coverage)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    v = state["v"]
+    noise = 1.0 + amp * rng.standard_normal(v.shape[:3])
+    for q in range(v.shape[3]):
+        v[..., q] *= noise
+    return state
+
+
+def copy(state):
+    return _copy(state)
+
+
+def normwise(a, b):
+    """max |a-b| / max |b| per trailing component."""
+    a = np.asarray(a); b = np.asarray(b)
+    num = np.abs(a - b).reshape(-1, a.shape[-1]).max(axis=0)
+    den = np.abs(b).reshape(-1, b.shape[-1]).max(axis=0)
+    den = np.where(den == 0, 1.0, den)
+    return num / den
