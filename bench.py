@@ -1,0 +1,307 @@
+"""Benchmark of the IZEM RHS hot path on GB300: Mcell-steps/s.
+
+Workload (one "step" = one full time step of the reference driver,
+izem.f90:242-389: timestep, then the three SSP-RK3 stages, plus the two
+Strang chemistry half-steps when chemistry is on): the temporal H2/air mixing
+layer on 256 x 256 x 128 cells, 9 species, WENO5 characteristic fluxes,
+mixture-averaged viscous and diffusive fluxes, Newton temperature, seeded
+synthetic initial field (numpy PCG64 seed 20261203).
+
+Printed JSON (one line, rank 0):
+  value       device throughput, inputs resident in HBM
+  e2e         the same metric through the C ABI with host arrays: every step
+              uploads the state from pinned host memory and downloads it back
+  roofline    dominant kernel: algorithmic bytes / measured launch time vs the
+              measured HBM copy bandwidth; fp64 gives its FP64 rate vs the
+              measured FP64 FMA peak of this GPU
+  cpu_baseline the C++ restatement of the reference (the oracle) on the host
+              cores on a bounded sub-block of the same workload
+
+--impl reference times that CPU restatement alone (the reference is Fortran
+and cannot be built here or on the GPU host).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+HBM_FALLBACK_GBS = 6800.0
+FP64_PEAK_GFLOPS = 1194.4   # measured FP64 FMA rate of this GB300 pool (profiles/fp64_peak_probe.md)
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d.get("hbm_gbs", HBM_FALLBACK_GBS)), "measured"
+    return HBM_FALLBACK_GBS, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, idx=0):
+        self.idx = idx
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm = [float(s[1]) for s in self.samples if len(s) > 8 and s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if len(s) > 8 and s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for s in self.samples:
+            if len(s) > 8:
+                for nm, val in zip(names, s[5:9]):
+                    if val.strip().lower() == "active":
+                        reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.samples)}
+
+
+def build_workload(args):
+    from phd_gb300 import ics
+    from phd_gb300.izem import metrics_dscalar
+    if args.workload == "tgv":
+        return ics.tgv(args.n, lib_dscalar=metrics_dscalar)
+    return ics.mixing_layer(args.nx, args.ny, args.nz, lib_dscalar=metrics_dscalar)
+
+
+def euler_face_bytes(cfg):
+    """Algorithmic bytes of one x-face-flux launch: each of the nfaces faces
+    reads its cell's conserved variables and 8 primitives once (the stencil
+    re-reads are cache hits) and writes nv face fluxes."""
+    nv = 5 + cfg.nrv
+    nf = (cfg.nx + 1) * cfg.ny * cfg.nz
+    return nf * (nv * 8 + 8 * 8 + 1 + nv * 8)
+
+
+EULER_FLOP_PER_FACE = {2: 1400, 9: 2260}   # FP64 flops per face (linear branch), from the ncu instruction counts
+
+
+def run_gpu(args, rank, world):
+    from phd_gb300.izem import IzemGPU
+    cfg, thd, adi, dxi, st, info = build_workload(args)
+    g = IzemGPU(cfg, thd, adi)
+    g.set_grid(*dxi)
+    g.upload(**st)
+    g.finalize_ic()
+    ncell = cfg.nx * cfg.ny * cfg.nz
+    # warm-up (also captures the CUDA graph)
+    for _ in range(args.warmup):
+        _, dt = g.timestep()
+        g.rk3(dt)
+    g.synchronize()
+    barrier(world)
+    g.set_kernel_timing(True)
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+        g.timer_start()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            _, dt = g.timestep()
+            g.rk3(dt)
+        ms = g.timer_stop()
+        wall = time.perf_counter() - t0
+    kt = g.kernel_times()
+    g.set_kernel_timing(False)
+    ms = max_over_ranks(ms, world)
+    value = world * ncell * args.steps / (ms * 1e-3) / 1e6
+    # ---- end-to-end through the C ABI with host (pinned) arrays
+    host = g.download()
+    e2e_steps = max(1, min(args.steps, 3))
+    pinned = {k: pin(a) for k, a in host.items()}
+    h2d = sum(a.nbytes for a in pinned.values())
+    g.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        g.upload(**pinned)
+        _, dt = g.timestep()
+        g.rk3(dt)
+        out = g.download()
+    e2e_s = time.perf_counter() - t0
+    d2h = sum(a.nbytes for a in out.values())
+    e2e_value = world * ncell * e2e_steps / e2e_s / 1e6
+    # ---- roofline of the dominant kernel
+    hbm, hbm_src = measured_peaks()
+    dom = max(kt.items(), key=lambda kv: kv[1][1])
+    dom_name, (dom_n, dom_ms) = dom
+    fx = kt.get("euler_face_x", (0, 0.0))
+    rl = None
+    if fx[0]:
+        avg_s = fx[1] / fx[0] * 1e-3
+        byts = euler_face_bytes(cfg)
+        nf = (cfg.nx + 1) * cfg.ny * cfg.nz
+        flops = nf * EULER_FLOP_PER_FACE.get(cfg.nrv, 2000)
+        rl = {"bound": "hbm", "kernel": "k_euler_face (x sweep)", "achieved": byts / avg_s / 1e9, "peak": hbm,
+              "unit": "GB/s", "frac": byts / avg_s / 1e9 / hbm, "traffic": TRAFFIC_PER_LAUNCH.get(args.workload),
+              "peak_source": hbm_src + " (MEASURED_PEAKS.json hbm_gbs)",
+              "fp64": {"achieved": flops / avg_s / 1e9, "peak": FP64_PEAK_GFLOPS, "unit": "GFLOP/s",
+                       "frac": flops / avg_s / 1e9 / FP64_PEAK_GFLOPS}}
+    launches = sum(n for n, _ in kt.values())
+    res = {
+        "metric": "reacting RHS Mcell-steps/s, FP64 plain vs MLP-chem (<=1% dT err) on 1 GB300",
+        "value": value, "unit": "Mcell-steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded PCG64 %d)" % info.get("seed", 0),
+        "config": {"workload": info["name"] + WORKLOAD_NOTE, "cells": ncell, "nv": 5 + cfg.nrv,
+                   "transport": "fitted mixture-averaged (tranfit)", "chemistry": "off",
+                   "l2": "inputs larger than L2 (state %.2f GB)" % (host["v"].nbytes / 1e9),
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "e2e": {"value": e2e_value, "unit": "Mcell-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "steps": e2e_steps},
+        "roofline": rl,
+        "dominant_kernel": {"name": dom_name, "launches": dom_n, "ms": dom_ms},
+        "kernel_ms": {k: round(v[1], 3) for k, v in sorted(kt.items(), key=lambda kv: -kv[1][1])},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+        "wall_s_timed": wall,
+    }
+    g.close()
+    return res
+
+
+WORKLOAD_NOTE = " (WENO5 + fitted viscous + RK3; chemistry and EGLIB not in this line)"
+TRAFFIC_PER_LAUNCH = {}
+
+
+def pin(a):
+    try:
+        import torch
+        t = torch.empty(a.shape[::-1], dtype=torch.float64 if a.dtype == np.float64 else torch.uint8).pin_memory()
+        b = t.numpy().T
+        b[...] = a
+        return b
+    except Exception:
+        return np.asfortranarray(a)
+
+
+def cpu_baseline(args, steps=2):
+    """The oracle (C++ restatement of the reference, OpenMP) on a 64x64x32
+    sub-block of the same workload, all host threads."""
+    import oracle
+    from phd_gb300 import ics
+    nx, ny, nz = 64, 64, 32
+    if args.workload == "tgv":
+        cfg, thd, adi, dxi, st, info = ics.tgv(48, lib_dscalar=oracle.metrics_dscalar)
+        nx = ny = nz = 48
+    else:
+        cfg, thd, adi, dxi, st, info = ics.mixing_layer(nx, ny, nz, Lx=nx * 47e-6, Ly=ny * 47e-6, Lz=nz * 47e-6,
+                                                        lib_dscalar=oracle.metrics_dscalar)
+    orc = oracle.Oracle(cfg, thd, adi, *dxi)
+    orc.finalize_ic(st)
+    _, dt = orc.timestep(st)
+    orc.rk3(st, dt)   # warm
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        _, dt = orc.timestep(st)
+        orc.rk3(st, dt)
+    s = time.perf_counter() - t0
+    cores = os.cpu_count()
+    return {"value": nx * ny * nz * steps / s / 1e6, "unit": "Mcell-steps/s", "cores": cores, "kind": "port",
+            "sample": "%d steps of a %dx%dx%d sub-block of the same workload, OpenMP over pencils, %d threads"
+                      % (steps, nx, ny, nz, cores)}
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="mix", choices=["mix", "tgv"])
+    ap.add_argument("--nx", type=int, default=256)
+    ap.add_argument("--ny", type=int, default=256)
+    ap.add_argument("--nz", type=int, default=128)
+    ap.add_argument("--n", type=int, default=64)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    if args.impl == "reference":
+        if rank == 0:
+            cb = cpu_baseline(args, steps=max(1, args.steps // 2))
+            line = {"impl": "reference", "metric": "reacting RHS Mcell-steps/s, FP64 plain vs MLP-chem (<=1% dT err) on 1 GB300",
+                    "value": cb["value"], "unit": cb["unit"], "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+                    "higher_is_better": True, "dtype": "f64", "data": "synthetic",
+                    "config": {"workload": "H2/air temporal mixing layer (sub-block) " + WORKLOAD_NOTE},
+                    "cpu_baseline": cb, "e2e": {"value": cb["value"], "unit": cb["unit"], "h2d_bytes_per_step": 0,
+                                                "d2h_bytes_per_step": 0},
+                    "note": "C++ restatement of the reference Fortran (no Fortran compiler on either host)"}
+            print(json.dumps(line))
+        return
+    if args.impl == "ours":
+        from phd_gb300.build import build_gpu
+        if rank == 0:
+            build_gpu()
+        barrier(world)
+        if world > 1:
+            # one replica per GPU: restrict this process to its local device
+            local = int(os.environ.get("LOCAL_RANK", "0"))
+            vis = os.environ.get("CUDA_VISIBLE_DEVICES")
+            devs = vis.split(",") if vis else [str(q) for q in range(world)]
+            os.environ["CUDA_VISIBLE_DEVICES"] = devs[local % len(devs)]
+    res = run_gpu(args, rank, world)
+    if rank == 0:
+        if not args.no_cpu_baseline:
+            res["cpu_baseline"] = cpu_baseline(args)
+        print(json.dumps(res))
+
+
+if __name__ == "__main__":
+    main()

@@ -40,10 +40,15 @@ def copy(state):
     return _copy(state)
 
 
-def normwise(a, b):
-    """max |a-b| / max |b| per trailing component."""
+def normwise(a, b, floor=1e-6):
+    """max |a-b| / max |b| per trailing component.
+
+    A component whose reference values are pure rounding noise (e.g. the
+    diffusive flux of a uniform mixture) is scaled by ``floor`` times the
+    largest component instead of by its own size."""
     a = np.asarray(a); b = np.asarray(b)
     num = np.abs(a - b).reshape(-1, a.shape[-1]).max(axis=0)
     den = np.abs(b).reshape(-1, b.shape[-1]).max(axis=0)
+    den = np.maximum(den, floor * den.max())
     den = np.where(den == 0, 1.0, den)
     return num / den
