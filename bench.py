@@ -113,7 +113,7 @@ def euler_face_bytes(cfg):
     return nf * (nv * 8 + 8 * 8 + 1 + nv * 8)
 
 
-EULER_FLOP_PER_FACE = {2: 1400, 9: 2260}   # FP64 flops per face (linear branch), from the ncu instruction counts
+EULER_FLOP_PER_FACE = {2: 1400, 9: 2481}   # FP64 flops per face (sensor-off branch): ncu DFMA x2 + DADD + DMUL counts (profiles/euler_face_mix128.md)
 
 
 def run_gpu(args, rank, world):

@@ -94,6 +94,33 @@ typedef struct izem_adi {
   double rho_ref, p_ref, lbda_ref, d_ref;
 } izem_adi;
 
+/* Gas-phase mechanism in CHEMKIN-II form (the linking data that ckinterp
+ * writes to chem.bin and CKINIT reads, devel-izem/src/chemkin/vode.f:391):
+ * species molar masses, NASA-7 thermo with CHEMKIN's mid-temperature switch,
+ * and per reaction: stoichiometry (up to 3 reactants, 3 products), forward
+ * Arrhenius (A, b, E/R), reverse kind, third-body efficiencies, fall-off
+ * (LOW + Troe).  Units: mol, cm, s, K, erg. */
+#define IZEM_MAXREAC 32
+typedef struct izem_mech {
+  int    kk, ii;
+  double ru, patm;                        /* erg/mol/K, dyn/cm^2              */
+  double wt[IZEM_NSMAX];                  /* g/mol                           */
+  double tmid[IZEM_NSMAX];                /* T > tmid: high-T coefficients    */
+  double a[IZEM_NSMAX][2][7];             /* [k][0 low / 1 high][a1..a7]      */
+  int    nuk[IZEM_MAXREAC][6];            /* species index, -1 = none;
+                                             slots 0-2 reactants, 3-5 products */
+  int    nu[IZEM_MAXREAC][6];             /* stoichiometric coefficients      */
+  double par[IZEM_MAXREAC][3];            /* A, b, E/R                        */
+  int    rev[IZEM_MAXREAC];               /* 0 irreversible, 1 equilibrium,
+                                             2 explicit REV                   */
+  double rpar[IZEM_MAXREAC][3];           /* REV A, b, E/R                    */
+  int    thb[IZEM_MAXREAC];               /* 1: +M or (+M) third body         */
+  double eff[IZEM_MAXREAC][IZEM_NSMAX];   /* third-body efficiencies          */
+  int    fall[IZEM_MAXREAC];              /* 0 none, 1 Lindemann, 3/4 Troe    */
+  double low[IZEM_MAXREAC][3];            /* LOW A, b, E/R                    */
+  double troe[IZEM_MAXREAC][4];           /* a, T***, T*, T**                 */
+} izem_mech;
+
 typedef struct izem_ctx izem_ctx;
 
 /* Create a context on the current CUDA device.  Allocates the device-resident
@@ -152,6 +179,28 @@ int  izem_gpu_rk3(izem_ctx* ctx, double dt, double time0);
  * dtmin is in/out: its input value is the previous step's dtmin (used by the
  * chemical criterion), DTmax the previous chemistry's max |dT|. */
 int  izem_gpu_timestep(izem_ctx* ctx, double DTmax, double dt_4[4], double* dtmin);
+
+/* Mechanism for the chemistry steps (the chem.bin data; see izem_mech). */
+int  izem_gpu_set_mechanism(izem_ctx* ctx, const izem_mech* mech);
+
+/* reaction_selec with reaction_dvode (module_reaction.f90:47-321): one
+ * Strang half step of length dt (code units) on every cell of the interior
+ * window (ng+1 cells are skipped at every global face, as in the reference),
+ * each integrated as a constant-volume reactor by the BDF method (DVODE
+ * MF=22, RTOL 1e-6, ATOL 1e-10, <= 20 restarts) in a persistent
+ * work-stealing kernel; then upd_prim_var_woT, halo fill and the ghost
+ * Newton solve.  mode 0 = BDF on every cell.  DTmax receives max |dT| [K]. */
+int  izem_gpu_chem_step(izem_ctx* ctx, double dt, int mode, double* DTmax);
+/* Statistics of the last chemistry step: cells whose integration failed
+ * (ISTATE <= -2), largest and summed BDF step counts. */
+int  izem_gpu_chem_stats(izem_ctx* ctx, int* failed, int* max_steps, unsigned long long* total_steps);
+
+/* Independent constant-volume reactors (PSR_CHEMKIN per cell, chemkin/
+ * psr_chemkin.f): T [K] in/out, rho [g/cm^3], Y (n rows of kk) in/out,
+ * dt [s] per cell.  istate/nsteps may be NULL.  With device_ptrs = 1 every
+ * array is a device pointer (no copies); kernel_ms receives the kernel time. */
+int  izem_gpu_psr_batch(const izem_mech* mech, int n, double* T, const double* rho, double* Y,
+                        const double* dt, int* istate, int* nsteps, int device_ptrs, float* kernel_ms);
 
 /* Device timing of the calls above on the context's stream (CUDA events). */
 int  izem_gpu_timer_start(izem_ctx* ctx);

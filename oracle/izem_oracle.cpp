@@ -960,6 +960,79 @@ void timestep(const Ctx& c, double DTmax, const double* v, const double* T, cons
   *dtmin = std::min(std::min(dt4[0], dt4[1]), std::min(dt4[2], dt4[3]));
 }
 
+#include "chem_oracle.inc"
+
+// reaction_dvode (module_reaction.f90:102-321, dvodesimp = F) followed by
+// the rest of reaction_selec (:83-86): upd_prim_var_woT on the interior,
+// comm_cons, upd_boundaries, upd_prim_var_ghost.
+int chem_step(Ctx& c, const izem_mech& mech, double dt, double* v, double* T, double* W_i, double* cp, double* ha,
+              double* DTmax_out, int* max_steps) {
+  const Block& b = c.b;
+  const izem_adi& a = c.adi;
+  const double dt_phys = dt * a.time_ref;
+  const double tref_i = 1.0 / a.t_ref;
+  const double rho_cgs = a.rho_ref * 1.0e-3;
+  const int ng = b.ng, nrv = b.nrv;
+  const int ix = std::max(ng + 1, 1), fx = std::min(b.nx, b.nx - ng - 1);
+  const int iy = std::max(ng + 1, 1), fy = std::min(b.ny, b.ny - ng - 1);
+  const int iz = std::max(ng + 1, 1), fz = std::min(b.ny, b.nz - ng - 1);   // reference: min(ey, ...)
+  double DTmax = 0.0;
+  int fail = 0, mxs = 0;
+#pragma omp parallel for collapse(2) schedule(dynamic) reduction(max : DTmax, mxs) reduction(+ : fail)
+  for (int k = iz; k <= fz; ++k)
+    for (int j = iy; j <= fy; ++j)
+      for (int i = ix; i <= fx; ++i) {
+        const size_t p = b.id(i, j, k);
+        const double rho_i = 1.0 / v[p];
+        double z[IZEM_NSMAX + 1];
+        for (int l = 0; l < nrv; ++l) z[1 + l] = v[(NIV + l) * b.ncell + p] * rho_i;
+        const double rho0 = v[p];
+        const double rho_phys = rho0 * rho_cgs;
+        const double T0_phys = T[p] * a.t_ref;
+        z[0] = T0_phys;
+        int nst = 0;
+        const int istate = reaction_v(mech, rho_phys, z, dt_phys, &nst);
+        if (istate <= -2) fail += 1;
+        mxs = std::max(mxs, nst);
+        const double T_phys = z[0];
+        T[p] = T_phys * tref_i;
+        DTmax = std::max(DTmax, std::fabs(T_phys - T0_phys));
+        double sumY = 0.0;
+        for (int l = 0; l < nrv - 1; ++l) {
+          double Ya = std::min(std::max(z[1 + l], 0.0), 1.0);
+          v[(NIV + l) * b.ncell + p] = rho0 * Ya;
+          sumY = sumY + Ya;
+        }
+        v[(NIV + nrv - 1) * b.ncell + p] = rho0 * (1.0 - sumY);
+      }
+  *DTmax_out = DTmax;
+  if (max_steps) *max_steps = mxs;
+  // upd_prim_var_woT on the interior (module_thermodynamics.f90:522-689)
+  wmix_i(c, 0, v, W_i);
+  for (int k = 1; k <= b.nz; ++k)
+    for (int j = 1; j <= b.ny; ++j)
+      for (int i = 1; i <= b.nx; ++i) {
+        size_t p = b.id(i, j, k);
+        double hak[IZEM_NSMAX], cpp;
+        (void)newton_cell(c.thd, b, v, p, T[p], &cpp, hak);
+        cp[p] = cpp;
+        for (int is = 0; is < nrv; ++is) ha[is * b.ncell + p] = hak[is];
+      }
+  comm_periodic(b, b.nv, v, b.ncell);
+  for (int f = 0; f < 6; ++f)
+    if (b.bnd[f] && b.bc[f] == IZEM_BC_EXTRAPOLATION) bc_extrapolation(b, f, v);
+  for (int f = 0; f < 6; ++f) {
+    if (c.cfg.forcesum) force_sumY(c, kFaceDomain[f], v);
+    int rc = prim_inv_var(c, kFaceDomain[f], false, v, W_i, T, cp, ha);
+    if (rc) return rc;
+  }
+  if (fail) {
+    c.err = "DVODE failed (ISTATE <= -2) on some cells";
+    return IZEM_ERR_CHEM;
+  }
+  return IZEM_OK;
+}
+
 }  // namespace
 
 // ============================================================== C API =====
@@ -1029,6 +1102,34 @@ int or_timestep(void* h, double DTmax, const double* v, const double* T, const d
                 double* dt4, double* dtmin) {
   timestep(*static_cast<Ctx*>(h), DTmax, v, T, W_i, cp, dt4, dtmin);
   return 0;
+}
+
+int or_chem_step(void* h, const izem_mech* mech, double dt, double* v, double* T, double* W_i, double* cp, double* ha,
+                 double* DTmax, int* max_steps) {
+  return chem_step(*static_cast<Ctx*>(h), *mech, dt, v, T, W_i, cp, ha, DTmax, max_steps);
+}
+
+// Independent constant-volume reactors (PSR_CHEMKIN per cell): T [K],
+// rho [g/cm^3], Y (n x kk, row per cell), dt [s] per cell.
+void or_psr_cells(const izem_mech* mech, int n, double* T, const double* rho, double* Y, const double* dt, int* istate,
+                  int* nsteps) {
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int q = 0; q < n; ++q) {
+    double z[IZEM_NSMAX + 1];
+    z[0] = T[q];
+    for (int k = 0; k < mech->kk; ++k) z[1 + k] = Y[(size_t)q * mech->kk + k];
+    int nst = 0;
+    istate[q] = reaction_v(*mech, rho[q], z, dt[q], &nst);
+    nsteps[q] = nst;
+    T[q] = z[0];
+    for (int k = 0; k < mech->kk; ++k) Y[(size_t)q * mech->kk + k] = z[1 + k];
+  }
+}
+
+// Reactor right-hand side FUN (for cross-checks against other integrators).
+void or_ck_fun(const izem_mech* mech, double rho, const double* z, double* zp) { ck_fun(*mech, rho, z, zp); }
+void or_ck_wdot(const izem_mech* mech, double rho, double T, const double* Y, double* wdot) {
+  ck_wyr(*mech, rho, T, Y, wdot);
 }
 
 // dscalar + inversion (module_deriv.f90:80-205, module_tools.f90:374-426)

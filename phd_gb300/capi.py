@@ -62,6 +62,24 @@ class IzemThd(C.Structure):
     ]
 
 
+MAXREAC = 32
+
+
+class IzemMech(C.Structure):
+    _fields_ = [
+        ("kk", C.c_int), ("ii", C.c_int),
+        ("ru", C.c_double), ("patm", C.c_double),
+        ("wt", C.c_double * NSMAX), ("tmid", C.c_double * NSMAX),
+        ("a", ((C.c_double * 7) * 2) * NSMAX),
+        ("nuk", (C.c_int * 6) * MAXREAC), ("nu", (C.c_int * 6) * MAXREAC),
+        ("par", (C.c_double * 3) * MAXREAC),
+        ("rev", C.c_int * MAXREAC), ("rpar", (C.c_double * 3) * MAXREAC),
+        ("thb", C.c_int * MAXREAC), ("eff", (C.c_double * NSMAX) * MAXREAC),
+        ("fall", C.c_int * MAXREAC), ("low", (C.c_double * 3) * MAXREAC),
+        ("troe", (C.c_double * 4) * MAXREAC),
+    ]
+
+
 class IzemAdi(C.Structure):
     _fields_ = [(n, C.c_double) for n in (
         "gamma_inf", "re", "pr", "le", "ma", "sc", "sqgmr", "ggmopr",

@@ -1,0 +1,28 @@
+// Host interface of the batched chemistry kernels (chem.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include "../../include/izem_gpu.h"
+
+// One chemistry half-step over the reference's interior window of a field.
+struct ChemField {
+  double* v;        // ghosted conserved variables (device)
+  double* T;        // ghosted temperature, code units (device)
+  double* dT_out;   // optional: per-window-cell temperature increment [K]
+  long long ncell;
+  int gx, gy, ng;
+  int ix, iy, iz;   // first cell of the window (1-based interior index)
+  int wx, wy, wz;   // window extents
+  double t_ref, tref_i, rho_cgs, dt_phys;
+};
+
+struct ChemStats {
+  int failed;                      // cells whose final ISTATE <= -2
+  int max_steps;                   // largest BDF step count of a cell
+  unsigned long long total_steps;  // summed BDF steps
+  unsigned long long dtmax_bits;   // max |dT| [K] as a double bit pattern
+};
+
+cudaError_t chem_upload_mech(const izem_mech* m);
+cudaError_t chem_launch_field(const ChemField& f, unsigned* d_counter, ChemStats* d_stats, cudaStream_t s, int kk);
+cudaError_t chem_launch_batch(int n, double* T, const double* rho, double* Y, const double* dt, int* istate,
+                              int* nsteps, unsigned* d_counter, ChemStats* d_stats, cudaStream_t s, int kk);

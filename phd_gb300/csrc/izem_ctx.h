@@ -36,6 +36,12 @@ struct izem_ctx {
   std::vector<int> kt_launches;
   std::vector<double> kt_ms;
   std::vector<std::vector<std::pair<cudaEvent_t, cudaEvent_t>>> kt_pending;
+  // chemistry
+  bool have_mech = false;
+  izem_mech mech;
+  unsigned* d_counter = nullptr;
+  void* d_chem_stats = nullptr;   // ChemStats
+  void* h_chem_stats = nullptr;
   int newton_warn = 0;
   std::string err;
 };

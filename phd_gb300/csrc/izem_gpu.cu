@@ -9,6 +9,7 @@
 #include <cmath>
 #include <string>
 #include <vector>
+#include <algorithm>
 #include <cuda_runtime.h>
 
 #include "common.cuh"
@@ -17,6 +18,7 @@
 #include "kernels_visc.cuh"
 #include "kernels_state.cuh"
 #include "izem_ctx.h"
+#include "chem.h"
 
 
 
@@ -246,6 +248,21 @@ int do_update_primitives(izem_ctx* c) {
   return enq_update_primitives_after<NRV>(c);
 }
 
+// reaction_selec tail (module_reaction.f90:83-86)
+template <int NRV>
+int do_chem_after(izem_ctx* c) {
+  const Geo& g = c->g;
+  int rc;
+  if ((rc = launch(c, "prim_woT", [&] {
+         k_prim_woT<NRV><<<grid_for(g.nint), kThreads, 0, c->stream>>>(g, c->v, c->T, c->W_i, c->cp, c->ha);
+       })))
+    return rc;
+  long long ns = slab_count(g) - g.nint;
+  if ((rc = launch(c, "halo", [&] { k_halo<NRV><<<grid_for(ns), kThreads, 0, c->stream>>>(g, 0, c->cfg.forcesum, c->v, c->W_i); })))
+    return rc;
+  return enq_newton<NRV>(c, 1, 1.0e-5, 200, kNewtonIters, 1);
+}
+
 template <int NRV>
 int do_timestep(izem_ctx* c) {
   const Geo& g = c->g;
@@ -396,6 +413,9 @@ void izem_gpu_destroy(izem_ctx* c) {
   for (double* p : c->allocs) cudaFree(p);
   if (c->sensor) cudaFree(c->sensor);
   if (c->d_status) cudaFree(c->d_status);
+  if (c->d_counter) cudaFree(c->d_counter);
+  if (c->d_chem_stats) cudaFree(c->d_chem_stats);
+  if (c->h_chem_stats) cudaFreeHost(c->h_chem_stats);
   if (c->h_status) cudaFreeHost(c->h_status);
   if (c->h_dt) cudaFreeHost(c->h_dt);
   for (auto& v : c->kt_pending)
@@ -545,6 +565,122 @@ int izem_gpu_timestep(izem_ctx* c, double DTmax, double dt_4[4], double* dtmin) 
   }
   *dtmin = std::fmin(std::fmin(dt_4[0], dt_4[1]), std::fmin(dt_4[2], dt_4[3]));
   return IZEM_OK;
+}
+
+int izem_gpu_set_mechanism(izem_ctx* c, const izem_mech* mech) {
+  if (!c || !mech) return IZEM_ERR_ARG;
+  if (mech->kk != c->cfg.nrv || mech->kk != 9 || mech->ii > IZEM_MAXREAC)
+    return ctx_fail(c, IZEM_ERR_ARG, "mechanism species count must match nrv (9-species set)", cudaSuccess);
+  c->mech = *mech;
+  CK(chem_upload_mech(mech));
+  if (!c->d_counter) {
+    CK(cudaMalloc(&c->d_counter, sizeof(unsigned)));
+    CK(cudaMalloc(&c->d_chem_stats, sizeof(ChemStats)));
+    CK(cudaMallocHost(&c->h_chem_stats, sizeof(ChemStats)));
+  }
+  c->have_mech = true;
+  return IZEM_OK;
+}
+
+int izem_gpu_chem_step(izem_ctx* c, double dt, int mode, double* DTmax) {
+  if (!c || !DTmax) return IZEM_ERR_ARG;
+  if (!c->have_mech) return ctx_fail(c, IZEM_ERR_STATE, "no mechanism set", cudaSuccess);
+  if (mode != 0) return ctx_fail(c, IZEM_ERR_ARG, "unknown chemistry mode", cudaSuccess);
+  const Geo& g = c->g;
+  ChemField f;
+  f.v = c->v;
+  f.T = c->T;
+  f.dT_out = nullptr;
+  f.ncell = g.ncell;
+  f.gx = g.g[0];
+  f.gy = g.g[1];
+  f.ng = g.ng;
+  const int ng = g.ng;
+  // reaction_dvode window (module_reaction.f90:155-159): fz uses ey
+  f.ix = ng + 1; f.iy = ng + 1; f.iz = ng + 1;
+  const int fx = std::min(g.n[0], g.n[0] - ng - 1), fy = std::min(g.n[1], g.n[1] - ng - 1);
+  const int fz = std::min(g.n[1], g.n[2] - ng - 1);
+  f.wx = fx - f.ix + 1; f.wy = fy - f.iy + 1; f.wz = fz - f.iz + 1;
+  f.t_ref = c->adi.t_ref;
+  f.tref_i = 1.0 / c->adi.t_ref;
+  f.rho_cgs = c->adi.rho_ref * 1.0e-3;
+  f.dt_phys = dt * c->adi.time_ref;
+  CK(cudaMemsetAsync(c->d_chem_stats, 0, sizeof(ChemStats), c->stream));
+  if (f.wx > 0 && f.wy > 0 && f.wz > 0) {
+    int rc = launch(c, "chem_psr", [&] { (void)chem_launch_field(f, c->d_counter, (ChemStats*)c->d_chem_stats, c->stream, 9); });
+    if (rc) return rc;
+  }
+  int rc = IZEM_DISPATCH(c, do_chem_after, c);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(c->h_chem_stats, c->d_chem_stats, sizeof(ChemStats), cudaMemcpyDeviceToHost, c->stream));
+  rc = read_status(c);
+  if (rc) return rc;
+  const ChemStats& cs = *(const ChemStats*)c->h_chem_stats;
+  std::memcpy(DTmax, &cs.dtmax_bits, sizeof(double));
+  if (cs.failed) return ctx_fail(c, IZEM_ERR_CHEM, "stiff integration failed (ISTATE <= -2) on some cells", cudaSuccess);
+  return IZEM_OK;
+}
+
+int izem_gpu_chem_stats(izem_ctx* c, int* failed, int* max_steps, unsigned long long* total_steps) {
+  if (!c || !c->h_chem_stats) return IZEM_ERR_ARG;
+  const ChemStats& cs = *(const ChemStats*)c->h_chem_stats;
+  if (failed) *failed = cs.failed;
+  if (max_steps) *max_steps = cs.max_steps;
+  if (total_steps) *total_steps = cs.total_steps;
+  return IZEM_OK;
+}
+
+int izem_gpu_psr_batch(const izem_mech* mech, int n, double* T, const double* rho, double* Y, const double* dt,
+                       int* istate, int* nsteps, int device_ptrs, float* kernel_ms) {
+  if (!mech || n <= 0 || !T || !rho || !Y || !dt || mech->kk != 9) return IZEM_ERR_ARG;
+  cudaStream_t s = nullptr;
+  if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return IZEM_ERR_CUDA;
+  unsigned* counter = nullptr;
+  ChemStats* st = nullptr;
+  double *dT = nullptr, *drho = nullptr, *dY = nullptr, *ddt = nullptr;
+  int *dis = nullptr, *dns = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int rc = IZEM_OK;
+  const size_t kk = mech->kk;
+  auto fail = [&](int code) { rc = code; };
+  do {
+    if (chem_upload_mech(mech) != cudaSuccess) { fail(IZEM_ERR_CUDA); break; }
+    if (cudaMalloc(&counter, sizeof(unsigned)) != cudaSuccess || cudaMalloc(&st, sizeof(ChemStats)) != cudaSuccess) {
+      fail(IZEM_ERR_NOMEM); break;
+    }
+    cudaMemsetAsync(st, 0, sizeof(ChemStats), s);
+    if (device_ptrs) {
+      dT = T; drho = const_cast<double*>(rho); dY = Y; ddt = const_cast<double*>(dt); dis = istate; dns = nsteps;
+    } else {
+      if (cudaMalloc(&dT, n * sizeof(double)) || cudaMalloc(&drho, n * sizeof(double)) ||
+          cudaMalloc(&dY, n * kk * sizeof(double)) || cudaMalloc(&ddt, n * sizeof(double)) ||
+          cudaMalloc(&dis, n * sizeof(int)) || cudaMalloc(&dns, n * sizeof(int))) { fail(IZEM_ERR_NOMEM); break; }
+      cudaMemcpyAsync(dT, T, n * sizeof(double), cudaMemcpyHostToDevice, s);
+      cudaMemcpyAsync(drho, rho, n * sizeof(double), cudaMemcpyHostToDevice, s);
+      cudaMemcpyAsync(dY, Y, n * kk * sizeof(double), cudaMemcpyHostToDevice, s);
+      cudaMemcpyAsync(ddt, dt, n * sizeof(double), cudaMemcpyHostToDevice, s);
+    }
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, s);
+    if (chem_launch_batch(n, dT, drho, dY, ddt, dis, dns, counter, st, s, 9) != cudaSuccess) { fail(IZEM_ERR_CUDA); break; }
+    cudaEventRecord(e1, s);
+    if (!device_ptrs) {
+      cudaMemcpyAsync(T, dT, n * sizeof(double), cudaMemcpyDeviceToHost, s);
+      cudaMemcpyAsync(Y, dY, n * kk * sizeof(double), cudaMemcpyDeviceToHost, s);
+      if (istate) cudaMemcpyAsync(istate, dis, n * sizeof(int), cudaMemcpyDeviceToHost, s);
+      if (nsteps) cudaMemcpyAsync(nsteps, dns, n * sizeof(int), cudaMemcpyDeviceToHost, s);
+    }
+    if (cudaStreamSynchronize(s) != cudaSuccess) { fail(IZEM_ERR_CUDA); break; }
+    if (kernel_ms) cudaEventElapsedTime(kernel_ms, e0, e1);
+  } while (0);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (!device_ptrs) { cudaFree(dT); cudaFree(drho); cudaFree(dY); cudaFree(ddt); cudaFree(dis); cudaFree(dns); }
+  cudaFree(counter);
+  cudaFree(st);
+  cudaStreamDestroy(s);
+  return rc;
 }
 
 int izem_gpu_timer_start(izem_ctx* c) {

@@ -93,6 +93,34 @@ __global__ void k_prep_interior(Geo g, int forcesum, double* __restrict__ v, dou
   W_i[p] = wmix_cell<NRV>(v, g.ncell, p);
 }
 
+// upd_prim_var_woT on the interior (module_thermodynamics.f90:522-689):
+// W_i, cp and h_k at the current temperature, no Newton solve.
+template <int NRV>
+__global__ void k_prim_woT(Geo g, const double* __restrict__ v, const double* __restrict__ T, double* __restrict__ W_i,
+                           double* __restrict__ cp, double* __restrict__ ha) {
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= g.nint) return;
+  int i = (int)(idx % g.n[0]) + 1;
+  long long r = idx / g.n[0];
+  int j = (int)(r % g.n[1]) + 1;
+  int k = (int)(r / g.n[1]) + 1;
+  const long long nc = g.ncell;
+  const long long p = gid(g, i, j, k);
+  W_i[p] = wmix_cell<NRV>(v, nc, p);
+  const double rho_i = 1.0 / v[p];
+  const double Tp = T[p];
+  double cpm = 0.0;
+#pragma unroll
+  for (int l = 0; l < NRV; ++l) {
+    double cpk;
+    const double h = th_species(l, Tp, &cpk);
+    ha[l * nc + p] = h;
+    const double Ya = v[(IZEM_NIV + l) * nc + p] * rho_i;
+    cpm = cpm + Ya * c_thd.gam2 * c_thd.Wc_i[l] * cpk;
+  }
+  cp[p] = cpm;
+}
+
 // Ghost slabs: fill v from the periodic partner or by zero-gradient
 // extrapolation, then force_sumY and W_i on the ghost point.
 // mode 0: periodic faces wrap, boundary faces extrapolate (comm_cons +
