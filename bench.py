@@ -116,18 +116,43 @@ def euler_face_bytes(cfg):
 EULER_FLOP_PER_FACE = {2: 1400, 9: 2481}   # FP64 flops per face (sensor-off branch): ncu DFMA x2 + DADD + DMUL counts (profiles/euler_face_mix128.md)
 
 
+class Stepper:
+    """One time step of the reference driver (izem.f90:252-283): timestep,
+    then with chemistry the Strang sequence chem(dt/2), rk3(dt), chem(dt/2)."""
+
+    def __init__(self, g, chem):
+        self.g, self.chem = g, chem
+        self.dtmin, self.DTmax = 1.0, 0.0
+
+    def step(self):
+        g = self.g
+        _, dt = g.timestep(DTmax=self.DTmax, dtmin=self.dtmin)
+        if self.chem:
+            g.reaction_selec(0.5 * dt)
+        g.rk3(dt)
+        if self.chem:
+            self.DTmax = g.reaction_selec(0.5 * dt)
+        self.dtmin = dt
+        return dt
+
+
 def run_gpu(args, rank, world):
     from phd_gb300.izem import IzemGPU
+    from phd_gb300.mech import h2_mechanism
     cfg, thd, adi, dxi, st, info = build_workload(args)
+    chem = args.workload == "mix" and not args.no_chem
+    cfg.reaction = 1 if chem else 0
     g = IzemGPU(cfg, thd, adi)
     g.set_grid(*dxi)
     g.upload(**st)
     g.finalize_ic()
+    if chem:
+        g.set_mechanism(h2_mechanism())
+    stp = Stepper(g, chem)
     ncell = cfg.nx * cfg.ny * cfg.nz
     # warm-up (also captures the CUDA graph)
     for _ in range(args.warmup):
-        _, dt = g.timestep()
-        g.rk3(dt)
+        stp.step()
     g.synchronize()
     barrier(world)
     g.set_kernel_timing(True)
@@ -135,8 +160,7 @@ def run_gpu(args, rank, world):
         g.timer_start()
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            _, dt = g.timestep()
-            g.rk3(dt)
+            stp.step()
         ms = g.timer_stop()
         wall = time.perf_counter() - t0
     kt = g.kernel_times()
@@ -152,8 +176,7 @@ def run_gpu(args, rank, world):
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         g.upload(**pinned)
-        _, dt = g.timestep()
-        g.rk3(dt)
+        stp.step()
         out = g.download()
     e2e_s = time.perf_counter() - t0
     d2h = sum(a.nbytes for a in out.values())
@@ -180,8 +203,10 @@ def run_gpu(args, rank, world):
         "value": value, "unit": "Mcell-steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded PCG64 %d)" % info.get("seed", 0),
-        "config": {"workload": info["name"] + WORKLOAD_NOTE, "cells": ncell, "nv": 5 + cfg.nrv,
-                   "transport": "fitted mixture-averaged (tranfit)", "chemistry": "off",
+        "config": {"workload": info["name"] + (NOTE_CHEM if chem else WORKLOAD_NOTE), "cells": ncell,
+                   "nv": 5 + cfg.nrv, "transport": "fitted mixture-averaged (tranfit)",
+                   "chemistry": ("Strang: 2 x BDF (DVODE MF=22) half-steps per step, 9 species / 12 reactions"
+                                 if chem else "off"),
                    "l2": "inputs larger than L2 (state %.2f GB)" % (host["v"].nbytes / 1e9),
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "e2e": {"value": e2e_value, "unit": "Mcell-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
@@ -198,6 +223,7 @@ def run_gpu(args, rank, world):
 
 
 WORKLOAD_NOTE = " (WENO5 + fitted viscous + RK3; chemistry and EGLIB not in this line)"
+NOTE_CHEM = " (WENO5 + fitted viscous + RK3 + BDF chemistry; EGLIB transport not in this line)"
 TRAFFIC_PER_LAUNCH = {}
 
 
@@ -226,12 +252,24 @@ def cpu_baseline(args, steps=2):
                                                         lib_dscalar=oracle.metrics_dscalar)
     orc = oracle.Oracle(cfg, thd, adi, *dxi)
     orc.finalize_ic(st)
-    _, dt = orc.timestep(st)
-    orc.rk3(st, dt)   # warm
+    chem = args.workload == "mix" and not args.no_chem
+    mech = None
+    if chem:
+        from phd_gb300.mech import h2_mechanism
+        mech = h2_mechanism()
+
+    def step():
+        _, dt = orc.timestep(st)
+        if chem:
+            orc.chem_step(st, mech, 0.5 * dt)
+        orc.rk3(st, dt)
+        if chem:
+            orc.chem_step(st, mech, 0.5 * dt)
+
+    step()   # warm
     t0 = time.perf_counter()
     for _ in range(steps):
-        _, dt = orc.timestep(st)
-        orc.rk3(st, dt)
+        step()
     s = time.perf_counter() - t0
     cores = os.cpu_count()
     return {"value": nx * ny * nz * steps / s / 1e6, "unit": "Mcell-steps/s", "cores": cores, "kind": "port",
@@ -267,6 +305,7 @@ def main():
     ap.add_argument("--nz", type=int, default=128)
     ap.add_argument("--n", type=int, default=64)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-chem", action="store_true", help="mixing layer without the chemistry half-steps")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -10,7 +10,7 @@ import os
 
 import numpy as np
 
-from phd_gb300.capi import IzemAdi, IzemCfg, IzemThd
+from phd_gb300.capi import IzemAdi, IzemCfg, IzemMech, IzemThd
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libizem_oracle.so")
@@ -44,6 +44,12 @@ def load():
         "or_rk3": (C.c_int, [P, C.c_double, _dp, _dp, _dp, _dp, _dp, _u8p]),
         "or_timestep": (C.c_int, [P, C.c_double, _dp, _dp, _dp, _dp, _dp, _dp]),
         "or_metrics_dscalar": (None, [C.c_int, C.c_int, _dp, _dp]),
+        "or_chem_step": (C.c_int, [P, C.POINTER(IzemMech), C.c_double, _dp, _dp, _dp, _dp, _dp, _dp,
+                                   C.POINTER(C.c_int)]),
+        "or_psr_cells": (None, [C.POINTER(IzemMech), C.c_int, _dp, _dp, _dp, _dp, C.POINTER(C.c_int),
+                                C.POINTER(C.c_int)]),
+        "or_ck_fun": (None, [C.POINTER(IzemMech), C.c_double, _dp, _dp]),
+        "or_ck_wdot": (None, [C.POINTER(IzemMech), C.c_double, C.c_double, _dp, _dp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -71,6 +77,38 @@ def metrics_dscalar(coord, ng=3):
     out = np.empty_like(coord)
     lib.or_metrics_dscalar(len(coord), ng, _p(coord), _p(out))
     return out
+
+
+def psr_cells(mech, T, rho, Y, dt):
+    """Independent constant-volume reactors (PSR per cell, DVODE restated),
+    arrays updated in place; returns (istate, nsteps)."""
+    lib = load()
+    n = len(T)
+    istate = np.zeros(n, dtype=np.int32)
+    nsteps = np.zeros(n, dtype=np.int32)
+    for a in (T, rho, dt):
+        assert a.dtype == np.float64 and a.flags.c_contiguous
+    assert Y.shape == (n, mech.kk) and Y.flags.c_contiguous
+    lib.or_psr_cells(C.byref(mech), n, T.ctypes.data_as(_dp), rho.ctypes.data_as(_dp), Y.ctypes.data_as(_dp),
+                     dt.ctypes.data_as(_dp), istate.ctypes.data_as(C.POINTER(C.c_int)),
+                     nsteps.ctypes.data_as(C.POINTER(C.c_int)))
+    return istate, nsteps
+
+
+def ck_fun(mech, rho, z):
+    lib = load()
+    z = np.ascontiguousarray(z, dtype=np.float64)
+    zp = np.zeros_like(z)
+    lib.or_ck_fun(C.byref(mech), float(rho), z.ctypes.data_as(_dp), zp.ctypes.data_as(_dp))
+    return zp
+
+
+def ck_wdot(mech, rho, T, Y):
+    lib = load()
+    Y = np.ascontiguousarray(Y, dtype=np.float64)
+    w = np.zeros(mech.kk)
+    lib.or_ck_wdot(C.byref(mech), float(rho), float(T), Y.ctypes.data_as(_dp), w.ctypes.data_as(_dp))
+    return w
 
 
 class Oracle:
@@ -145,6 +183,14 @@ class Oracle:
         v, T, W_i, cp, ha = self._arrs(s)
         self._rc(self.lib.or_rk3(self.h, float(dt), _p(v), _p(T), _p(W_i), _p(cp), _p(ha),
                                  _p(s["shock_sensor"], _u8p)), "rk3")
+
+    def chem_step(self, s, mech, dt):
+        v, T, W_i, cp, ha = self._arrs(s)
+        dtm = C.c_double()
+        mx = C.c_int()
+        self._rc(self.lib.or_chem_step(self.h, C.byref(mech), float(dt), _p(v), _p(T), _p(W_i), _p(cp), _p(ha),
+                                       C.byref(dtm), C.byref(mx)), "chem_step")
+        return dtm.value
 
     def timestep(self, s, DTmax=0.0, dtmin=1.0):
         v, T, W_i, cp, _ = self._arrs(s)

@@ -26,7 +26,7 @@ SEED = 20261203
 
 
 def make_cfg(nx, ny, nz, nrv, bc=(BC_PERIODIC,) * 6, vis=1, weno_avg=1, max_rel_weight=0.15, forcesum=1,
-             reaction=0, eglib=0, cfl=0.5, cflmin=0.1, cpr=0.1, fo=0.5, vis_dt=0, linfix=0):
+             reaction=0, eglib=0, cfl=0.5, cflmin=0.1, cpr=20.0, fo=0.1, vis_dt=0, linfix=0):
     c = IzemCfg()
     c.nx, c.ny, c.nz, c.ng, c.ndim, c.nrv = nx, ny, nz, 3, 3, nrv
     for f in range(6):
@@ -165,3 +165,34 @@ def mixing_layer(nx=256, ny=256, nz=128, Lx=12e-3, Ly=12e-3, Lz=6e-3, seed=SEED,
     dxi = [grid_dxi(x, 3, a, lib_dscalar), grid_dxi(y, 3, a, lib_dscalar), grid_dxi(z, 3, a, lib_dscalar)]
     info = {"name": "H2/air temporal mixing layer %dx%dx%d" % (nx, ny, nz), "delta": delta, "dU": dU, "seed": seed}
     return cfg, thd, adi_struct(a), dxi, state, info
+
+
+def batched_reactors(n, seed=SEED):
+    """Independent H2/air reactors: T ~ U[800, 2400] K, p ~ U[1, 10] atm,
+    equivalence ratio ~ U[0.3, 3], progress c ~ U[0, 1] blending the unburnt
+    mixture linearly toward the complete-combustion major products (H2O, N2
+    and the excess O2 or H2), dt log-uniform in [1e-8, 1e-6] s.  Returns
+    T [K], rho [g/cm^3], Y (n, 9) in the h2air9 species order, dt [s]."""
+    sp = load_species("h2air9")
+    names = sp["names"]
+    ix = {nm: q for q, nm in enumerate(names)}
+    W = np.array(sp["W_gmol"])
+    rng = np.random.Generator(np.random.PCG64(seed))
+    T = rng.uniform(800.0, 2400.0, n)
+    p = rng.uniform(1.0, 10.0, n) * 101325.0
+    phi = rng.uniform(0.3, 3.0, n)
+    c = rng.uniform(0.0, 1.0, n)
+    dt = 10.0 ** rng.uniform(-8.0, -6.0, n)
+    Xu = np.zeros((n, 9)); Xb = np.zeros((n, 9))
+    Xu[:, ix["H2"]] = 2.0 * phi; Xu[:, ix["O2"]] = 1.0; Xu[:, ix["N2"]] = 3.76
+    lean = phi <= 1.0
+    Xb[:, ix["H2O"]] = np.where(lean, 2.0 * phi, 2.0)
+    Xb[:, ix["O2"]] = np.where(lean, 1.0 - phi, 0.0)
+    Xb[:, ix["H2"]] = np.where(lean, 0.0, 2.0 * phi - 2.0)
+    Xb[:, ix["N2"]] = 3.76
+    Yu = Xu * W; Yu /= Yu.sum(axis=1, keepdims=True)
+    Yb = Xb * W; Yb /= Yb.sum(axis=1, keepdims=True)
+    Y = (1.0 - c)[:, None] * Yu + c[:, None] * Yb
+    Wmix = 1.0 / (Y / W).sum(axis=1)
+    rho = p * Wmix * 1e-3 / (8.314510 * T) * 1e-3    # kg/m^3 -> g/cm^3
+    return np.ascontiguousarray(T), np.ascontiguousarray(rho), np.ascontiguousarray(Y), np.ascontiguousarray(dt)

@@ -19,7 +19,7 @@ import os
 import numpy as np
 
 from . import capi
-from .capi import IzemAdi, IzemCfg, IzemThd
+from .capi import IzemAdi, IzemCfg, IzemMech, IzemThd
 
 _LIB = None
 LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "libizem_gpu.so")
@@ -67,6 +67,11 @@ def load_library(path=None):
                                             C.POINTER(C.c_int)]),
         "izem_gpu_synchronize": (C.c_int, [P]),
         "izem_metrics_dscalar": (C.c_int, [C.c_int, C.c_int, _dp, _dp]),
+        "izem_gpu_set_mechanism": (C.c_int, [P, C.POINTER(IzemMech)]),
+        "izem_gpu_chem_step": (C.c_int, [P, C.c_double, C.c_int, _dp]),
+        "izem_gpu_chem_stats": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_ulonglong)]),
+        "izem_gpu_psr_batch": (C.c_int, [C.POINTER(IzemMech), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                         C.c_void_p, C.c_void_p, C.c_int, C.POINTER(C.c_float)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -89,6 +94,35 @@ def metrics_dscalar(coord, ng=3):
     if rc:
         raise IzemError(rc, "izem_metrics_dscalar")
     return out
+
+
+def psr_batch(mech, T, rho, Y, dt, device_ptrs=False):
+    """Independent constant-volume reactors on the GPU (PSR_CHEMKIN per
+    cell).  Host numpy arrays (T [K], rho [g/cm^3], Y (n, kk), dt [s]) are
+    updated in place; returns (istate, nsteps, kernel_ms).  With
+    device_ptrs the arguments are raw device addresses (ints) and the
+    istate/nsteps outputs are not returned."""
+    lib = load_library()
+    ms = C.c_float()
+    if device_ptrs:
+        n = int(device_ptrs)
+        rc = lib.izem_gpu_psr_batch(C.byref(mech), n, T, rho, Y, dt, None, None, 1, C.byref(ms))
+        if rc:
+            raise IzemError(rc, "izem_gpu_psr_batch")
+        return None, None, ms.value
+    n = len(T)
+    for a in (T, rho, dt):
+        if a.dtype != np.float64 or not a.flags.c_contiguous:
+            raise ValueError("psr_batch arrays must be contiguous float64")
+    if Y.shape != (n, mech.kk) or not Y.flags.c_contiguous:
+        raise ValueError("Y must be a C-ordered (n, kk) array")
+    istate = np.zeros(n, dtype=np.int32)
+    nsteps = np.zeros(n, dtype=np.int32)
+    rc = lib.izem_gpu_psr_batch(C.byref(mech), n, T.ctypes.data, rho.ctypes.data, Y.ctypes.data, dt.ctypes.data,
+                                istate.ctypes.data, nsteps.ctypes.data, 0, C.byref(ms))
+    if rc:
+        raise IzemError(rc, "izem_gpu_psr_batch")
+    return istate, nsteps, ms.value
 
 
 class IzemGPU:
@@ -193,6 +227,23 @@ class IzemGPU:
         dtm = C.c_double(dtmin)
         self._check(self.lib.izem_gpu_timestep(self.h, float(DTmax), _ptr(dt4), C.byref(dtm)), "timestep")
         return dt4, dtm.value
+
+    # ---- chemistry ----------------------------------------------------------
+    def set_mechanism(self, mech):
+        self._mech = mech
+        self._check(self.lib.izem_gpu_set_mechanism(self.h, C.byref(mech)), "set_mechanism")
+
+    def reaction_selec(self, dt, mode=0):
+        """One Strang chemistry half step of length dt (code units); returns
+        DTmax [K] (module_reaction.f90:47-100)."""
+        d = C.c_double()
+        self._check(self.lib.izem_gpu_chem_step(self.h, float(dt), int(mode), C.byref(d)), "chem_step")
+        return d.value
+
+    def chem_stats(self):
+        f, m, t = C.c_int(), C.c_int(), C.c_ulonglong()
+        self._check(self.lib.izem_gpu_chem_stats(self.h, C.byref(f), C.byref(m), C.byref(t)), "chem_stats")
+        return {"failed": f.value, "max_steps": m.value, "total_steps": t.value}
 
     # ---- timing -----------------------------------------------------------
     def timer_start(self):
