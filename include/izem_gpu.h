@@ -202,6 +202,35 @@ int  izem_gpu_chem_stats(izem_ctx* ctx, int* failed, int* max_steps, unsigned lo
 int  izem_gpu_psr_batch(const izem_mech* mech, int n, double* T, const double* rho, double* Y,
                         const double* dt, int* istate, int* nsteps, int device_ptrs, float* kernel_ms);
 
+/* ---- learned chemistry surrogate (no counterpart in the reference) -------
+ * A 12 -> 4 x 256 (GELU) -> 10 MLP, BF16 weights and activations with FP32
+ * accumulation on the tensor cores, trained on the GPU (Adam) on samples
+ * labelled by izem_gpu_psr_batch.  Inputs: T [K], ln p [atm], ln(Y+1e-10)
+ * for the 9 species, ln dt [s]; outputs dY (9) and dT [K]; both normalised
+ * by norm = {in_mean[12], in_std[12], out_mean[10], out_std[10]}.
+ * Parameters W_l are [in][out] row-major FP32 with padded sizes
+ * 16-256-256-256-256-16. */
+typedef struct izem_mlp izem_mlp;
+int  izem_mlp_create(izem_mlp** out);
+void izem_mlp_destroy(izem_mlp* m);
+int  izem_mlp_set_params(izem_mlp* m, const float* const* W, const float* const* b);
+int  izem_mlp_get_params(izem_mlp* m, float* const* W, float* const* b);
+int  izem_mlp_set_norm(izem_mlp* m, const float* norm);
+int  izem_mlp_forward(izem_mlp* m, int M, const float* x, float* y);
+int  izem_mlp_grads(izem_mlp* m, int M, const float* x, const float* t, double* loss,
+                    float* const* gW, float* const* gb);
+int  izem_mlp_train(izem_mlp* m, long long n, const float* x, const float* t, int device_ptrs,
+                    int epochs, int batch, float lr, unsigned seed, double* losses);
+/* Surrogate chemistry step on independent reactors with the per-cell error
+ * gate (training envelope, element conservation of dY, internal-energy
+ * consistency of dT); rejected cells are integrated by the BDF method.
+ * gate7 = {Tmin, Tmax, dtmin, dtmax, tol_el, tol_T_abs, tol_T_rel};
+ * kncf[kk][nele] element counts; stats3 = {fallback cells, max BDF steps,
+ * failed cells}; ms2 = {total ms, MLP ms}. */
+int  izem_gpu_psr_batch_mlp(izem_mlp* m, const izem_mech* mech, int n, double* T, const double* rho,
+                            double* Y, const double* dt, int device_ptrs, const double* gate7,
+                            const int* kncf, int nele, double* dT_pred, int* stats3, float* ms2);
+
 /* Device timing of the calls above on the context's stream (CUDA events). */
 int  izem_gpu_timer_start(izem_ctx* ctx);
 int  izem_gpu_timer_stop(izem_ctx* ctx, float* ms);

@@ -18,17 +18,34 @@
 #include <cstring>
 #include <cmath>
 #include <cuda_runtime.h>
+#include <cuda_bf16.h>
 #include "../../include/izem_gpu.h"
 #include "chem.h"
 
 namespace {
 
-__constant__ izem_mech c_mech;
-__constant__ int c_need_eqk;   // some reaction uses the equilibrium reverse rate
+__constant__ izem_mech c_mech_dev;
+__constant__ int c_need_eqk_dev;   // some reaction uses the equilibrium reverse rate
+#ifdef IZEM_CHEM_HOST_TEST
+izem_mech c_mech_host;
+int c_need_eqk_host = 0;
+#define HD __host__ __device__
+#ifdef __CUDA_ARCH__
+#define c_mech c_mech_dev
+#define c_need_eqk c_need_eqk_dev
+#else
+#define c_mech c_mech_host
+#define c_need_eqk c_need_eqk_host
+#endif
+#else
+#define HD __device__
+#define c_mech c_mech_dev
+#define c_need_eqk c_need_eqk_dev
+#endif
 
 constexpr int MXSP = 6;
 
-__device__ __forceinline__ double powi(double x, int m) {
+HD __forceinline__ double powi(double x, int m) {
   unsigned n = m < 0 ? -m : m;
   double y = (n % 2) ? x : 1.0;
   while (n >>= 1) {
@@ -41,7 +58,7 @@ __device__ __forceinline__ double powi(double x, int m) {
 template <int KK>
 struct Thermo {
   // cv (mean, mass) and h_k at T (CKCVBS, CKHMS)
-  __device__ static void cv_h(double T, const double* Y, double* cvb, double* h) {
+  HD static void cv_h(double T, const double* Y, double* cvb, double* h) {
     const double T2 = T * T, T3 = T * T2, T4 = T2 * T2;
     const double rut = T * c_mech.ru;
     double cv = 0.0;
@@ -60,10 +77,10 @@ struct Thermo {
 
 // CKWYR: molar production rates (mol cm^-3 s^-1)
 template <int KK>
-__device__ void ck_wyr(double rho, double T, const double* Y, double* wdot) {
+HD void ck_wyr(double rho, double T, const double* Y, double* wdot) {
   const int ii = c_mech.ii;
   const double alogt = log(T);
-  double C[KK];
+  double C[KK], rop[IZEM_MAXREAC];
   double ctot = 0.0;
 #pragma unroll
   for (int k = 0; k < KK; ++k) {
@@ -141,17 +158,19 @@ __device__ void ck_wyr(double rho, double T, const double* Y, double* wdot) {
         if (c_mech.nuk[i][5] >= 0) rkr = rkr * powi(C[c_mech.nuk[i][5]], c_mech.nu[i][5]);
       }
     }
-    const double rop = rkf - rkr;
-    for (int n = 0; n < MXSP; ++n) {
-      const int k = c_mech.nuk[i][n];
-      if (k >= 0) wdot[k] = wdot[k] + rop * double(c_mech.nu[i][n]);
-    }
+    rop[i] = rkf - rkr;
   }
+  // CKWYR accumulation order: stoichiometric slot outer, reaction inner
+  for (int n = 0; n < MXSP; ++n)
+    for (int i = 0; i < ii; ++i) {
+      const int k = c_mech.nuk[i][n];
+      if (k >= 0) wdot[k] = wdot[k] + rop[i] * double(c_mech.nu[i][n]);
+    }
 }
 
 // FUN: z = [T, Y], dz/dt for the constant-volume reactor
 template <int KK>
-__device__ void ck_fun(double rho, const double* z, double* zp) {
+HD void ck_fun(double rho, const double* z, double* zp) {
   double wdot[KK], h[KK], cvb;
   Thermo<KK>::cv_h(z[0], z + 1, &cvb, h);
   ck_wyr<KK>(rho, z[0], z + 1, wdot);
@@ -182,7 +201,7 @@ constexpr double kUround = 2.220446049250313e-16;   // D1MACH(4) for IEEE double
 constexpr double kRtol = 1.0e-6, kAtol = 1.0e-10;
 
 template <int N>
-__device__ __forceinline__ double dvnorm(const double* v, const double* w) {
+HD __forceinline__ double dvnorm(const double* v, const double* w) {
   double s = 0.0;
 #pragma unroll
   for (int i = 0; i < N; ++i) { const double x = v[i] * w[i]; s = s + x * x; }
@@ -190,7 +209,7 @@ __device__ __forceinline__ double dvnorm(const double* v, const double* w) {
 }
 
 template <int N>
-__device__ int dgefa(double* a, int* ipvt) {
+HD int dgefa(double* a, int* ipvt) {
   int info = 0;
   for (int k = 0; k < N - 1; ++k) {
     int l = k;
@@ -217,7 +236,7 @@ __device__ int dgefa(double* a, int* ipvt) {
 }
 
 template <int N>
-__device__ void dgesl(const double* a, const int* ipvt, double* b) {
+HD void dgesl(const double* a, const int* ipvt, double* b) {
   for (int k = 0; k < N - 1; ++k) {
     const int l = ipvt[k];
     const double t = b[l];
@@ -234,7 +253,7 @@ __device__ void dgesl(const double* a, const int* ipvt, double* b) {
 }
 
 template <int N>
-__device__ void dvset(Dv<N>& d) {
+HD void dvset(Dv<N>& d) {
   const int nq = d.nq, L = d.l;
   double* el = d.el;
   for (int i = 2; i < L; ++i) el[i] = 0.0;
@@ -282,7 +301,7 @@ __device__ void dvset(Dv<N>& d) {
 }
 
 template <int N>
-__device__ void dvjust(Dv<N>& d, int iord) {
+HD void dvjust(Dv<N>& d, int iord) {
   const int nq = d.nq;
   if (nq == 2 && iord != 1) return;
   double* el = d.el;
@@ -326,7 +345,7 @@ __device__ void dvjust(Dv<N>& d, int iord) {
 }
 
 template <int N>
-__device__ int dvjac(Dv<N>& d, double* y, double* ftem) {
+HD int dvjac(Dv<N>& d, double* y, double* ftem) {
   int jok = 1;
   if (d.nst == 0 || d.nst > d.nslj + 50) jok = -1;
   if (d.icf == 1 && d.drc < 0.2) jok = -1;
@@ -357,7 +376,7 @@ __device__ int dvjac(Dv<N>& d, double* y, double* ftem) {
 }
 
 template <int N>
-__device__ int dvnlsd(Dv<N>& d, double* y, double* ftem, int nflag) {
+HD int dvnlsd(Dv<N>& d, double* y, double* ftem, int nflag) {
   if (d.jstart == 0) d.nslp = 0;
   if (nflag == 0) d.icf = 0;
   if (nflag == -2) d.ipup = 2;
@@ -413,7 +432,7 @@ __device__ int dvnlsd(Dv<N>& d, double* y, double* ftem, int nflag) {
 
 // one DVSTEP; returns KFLAG (0, -1 error test, -2 convergence)
 template <int N>
-__device__ int dvstep(Dv<N>& d, double* y, double* ftem) {
+HD int dvstep(Dv<N>& d, double* y, double* ftem) {
   d.kflag = 0;
   const double told = d.tn;
   int ncf = 0, nflag = 0;
@@ -572,7 +591,7 @@ __device__ int dvstep(Dv<N>& d, double* y, double* ftem) {
 
 // DVODE (ISTATE = 1 fresh start, ITASK = 1): returns ISTATE
 template <int N>
-__device__ int dvode(Dv<N>& d, double* y, double* t, double tout, int* nst_total) {
+HD int dvode(Dv<N>& d, double* y, double* t, double tout, int* nst_total) {
   double ftem[N];
   if (tout == *t) return 1;
   d.tn = *t;
@@ -677,7 +696,7 @@ __device__ int dvode(Dv<N>& d, double* y, double* t, double tout, int* nst_total
 
 // REACTION_V: up to 20 fresh DVODE starts
 template <int N>
-__device__ int reaction_v(double rho, double* z, double tf, int* nsteps) {
+HD int reaction_v(double rho, double* z, double tf, int* nsteps) {
   Dv<N> d;
   d.rho = rho;
   double ti = 0.0;
@@ -752,6 +771,127 @@ __global__ void __launch_bounds__(128) k_psr_batch(int n, double* T, const doubl
   }
 }
 
+// ------------------------------------------------ surrogate support --------
+// Inputs of the learned surrogate: T [K], ln p [atm], ln(Y_k + 1e-10),
+// ln dt [s], normalised by the training means / standard deviations.
+template <int KK>
+__global__ void k_featurize(int n, const double* T, const double* rho, const double* Y, const double* dt,
+                            const float* norm, __nv_bfloat16* x, int ldx) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  double f[KK + 3];
+  const double Tq = T[q];
+  double wmi = 0.0;
+#pragma unroll
+  for (int k = 0; k < KK; ++k) wmi += fmax(Y[(size_t)q * KK + k], 0.0) / c_mech.wt[k];
+  const double p_atm = rho[q] * c_mech.ru * Tq * wmi / c_mech.patm;
+  f[0] = Tq;
+  f[1] = log(p_atm);
+#pragma unroll
+  for (int k = 0; k < KK; ++k) f[2 + k] = log(fmax(Y[(size_t)q * KK + k], 0.0) + 1.0e-10);
+  f[KK + 2] = log(dt[q]);
+#pragma unroll
+  for (int c = 0; c < KK + 3; ++c) x[(size_t)q * ldx + c] = __float2bfloat16((float)((f[c] - norm[c]) / norm[KK + 3 + c]));
+  for (int c = KK + 3; c < ldx; ++c) x[(size_t)q * ldx + c] = __float2bfloat16(0.f);
+}
+
+struct GateArgs {
+  double tmin, tmax, dtmin, dtmax;   // training envelope
+  double tol_el;                     // relative element residual
+  double tol_T_abs, tol_T_rel;       // energy-consistency of dT [K]
+};
+
+// Decode the surrogate output, gate it, and write accepted cells in place.
+// Gate: (1) state inside the training envelope; (2) element conservation of
+// the predicted dY (H, O, N, from the species composition); (3) the
+// predicted dT agrees with the temperature that conserves internal energy
+// (constant-volume reactor) for the predicted composition.  Accepted cells
+// take the energy-consistent temperature.  Rejected cells are appended to
+// `list` for the BDF integrator.
+template <int KK>
+__global__ void k_decode_gate(int n, const float* out, int ldo, const float* norm, double* T, const double* rho, double* Y,
+                              const double* dt, GateArgs ga, const int* kncf, int nele, int* list, unsigned* count,
+                              double* dT_pred, ChemStats* stats) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const int NI = KK + 3, NO = KK + 1;
+  const float* mo = norm + 2 * NI;
+  const float* so = norm + 2 * NI + NO;
+  double dY[KK], Yn[KK];
+  const double T0 = T[q];
+  bool ok = T0 >= ga.tmin && T0 <= ga.tmax && dt[q] >= ga.dtmin && dt[q] <= ga.dtmax;
+#pragma unroll
+  for (int k = 0; k < KK; ++k) dY[k] = (double)out[(size_t)q * ldo + k] * so[k] + mo[k];
+  const double dTp = (double)out[(size_t)q * ldo + KK] * so[KK] + mo[KK];
+  if (dT_pred) dT_pred[q] = dTp;
+  // element residuals
+  for (int e = 0; e < nele && ok; ++e) {
+    double r = 0.0, sc = 0.0;
+    for (int k = 0; k < KK; ++k) {
+      const double nk = (double)kncf[k * nele + e] / c_mech.wt[k];
+      r += nk * dY[k];
+      sc += nk * fmax(Y[(size_t)q * KK + k], 0.0);
+    }
+    if (sc > 0.0 && fabs(r) > ga.tol_el * sc) ok = false;
+  }
+  double sum = 0.0;
+#pragma unroll
+  for (int k = 0; k < KK; ++k) { Yn[k] = fmax(Y[(size_t)q * KK + k] + dY[k], 0.0); sum += Yn[k]; }
+#pragma unroll
+  for (int k = 0; k < KK; ++k) Yn[k] = Yn[k] / sum;
+  // internal energy balance: sum Y0 u(T0) = sum Yn u(T1), Newton on T1
+  double e0 = 0.0;
+  {
+    double h[KK], cvb;
+    Thermo<KK>::cv_h(T0, Y + (size_t)q * KK, &cvb, h);
+#pragma unroll
+    for (int k = 0; k < KK; ++k) e0 += Y[(size_t)q * KK + k] * (h[k] - c_mech.ru * T0 / c_mech.wt[k]);
+  }
+  double T1 = T0 + dTp;
+  if (!(T1 > 200.0 && T1 < 6000.0)) ok = false;
+  for (int it = 0; it < 4 && ok; ++it) {
+    double h[KK], cvb, e1 = 0.0;
+    Thermo<KK>::cv_h(T1, Yn, &cvb, h);
+#pragma unroll
+    for (int k = 0; k < KK; ++k) e1 += Yn[k] * (h[k] - c_mech.ru * T1 / c_mech.wt[k]);
+    T1 = T1 - (e1 - e0) / cvb;
+  }
+  const double dTe = T1 - T0;
+  if (ok && fabs(dTp - dTe) > ga.tol_T_abs + ga.tol_T_rel * fabs(dTe)) ok = false;
+  if (ok) {
+    T[q] = T1;
+#pragma unroll
+    for (int k = 0; k < KK; ++k) Y[(size_t)q * KK + k] = Yn[k];
+  } else {
+    const unsigned slot = atomicAdd(count, 1u);
+    list[slot] = q;
+  }
+}
+
+template <int KK>
+__global__ void __launch_bounds__(128) k_psr_list(const int* list, const unsigned* count, double* T, const double* rho,
+                                                  double* Y, const double* dt, unsigned* counter, ChemStats* stats) {
+  constexpr int N = KK + 1;
+  const unsigned n = *count;
+  while (true) {
+    const unsigned w = atomicAdd(counter, 1u);
+    if (w >= n) break;
+    const int q = list[w];
+    double z[N];
+    z[0] = T[q];
+#pragma unroll
+    for (int l = 0; l < KK; ++l) z[1 + l] = Y[(size_t)q * KK + l];
+    int nst = 0;
+    const int is = reaction_v<N>(rho[q], z, dt[q], &nst);
+    if (is <= -2) atomicAdd(&stats->failed, 1);
+    atomicMax(&stats->max_steps, nst);
+    atomicAdd(&stats->total_steps, (unsigned long long)nst);
+    T[q] = z[0];
+#pragma unroll
+    for (int l = 0; l < KK; ++l) Y[(size_t)q * KK + l] = z[1 + l];
+  }
+}
+
 int chem_grid(int* blocks) {
   int dev = 0, sms = 0, per = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return -1;
@@ -765,11 +905,11 @@ int chem_grid(int* blocks) {
 
 // ---------------------------------------------------------- host side -------
 cudaError_t chem_upload_mech(const izem_mech* m) {
-  cudaError_t e = cudaMemcpyToSymbol(c_mech, m, sizeof(izem_mech));
+  cudaError_t e = cudaMemcpyToSymbol(c_mech_dev, m, sizeof(izem_mech));
   if (e != cudaSuccess) return e;
   int need = 0;
   for (int i = 0; i < m->ii; ++i) need |= (m->rev[i] == 1);
-  return cudaMemcpyToSymbol(c_need_eqk, &need, sizeof(int));
+  return cudaMemcpyToSymbol(c_need_eqk_dev, &need, sizeof(int));
 }
 
 cudaError_t chem_launch_field(const ChemField& f, unsigned* d_counter, ChemStats* d_stats, cudaStream_t s, int kk) {
@@ -790,5 +930,30 @@ cudaError_t chem_launch_batch(int n, double* T, const double* rho, double* Y, co
   if (e != cudaSuccess) return e;
   if (kk != 9) return cudaErrorInvalidValue;
   k_psr_batch<9><<<blocks, 128, 0, s>>>(n, T, rho, Y, dt, istate, nsteps, d_counter, d_stats);
+  return cudaGetLastError();
+}
+
+cudaError_t chem_launch_featurize(int n, const double* T, const double* rho, const double* Y, const double* dt,
+                                  const float* d_norm, void* x_bf16, int ldx, cudaStream_t s) {
+  k_featurize<9><<<(n + 127) / 128, 128, 0, s>>>(n, T, rho, Y, dt, d_norm, (__nv_bfloat16*)x_bf16, ldx);
+  return cudaGetLastError();
+}
+
+cudaError_t chem_launch_decode_gate(int n, const float* out, int ldo, const float* d_norm, double* T, const double* rho,
+                                    double* Y, const double* dt, const double* gate7, const int* d_kncf, int nele,
+                                    int* list, unsigned* count, double* dT_pred, ChemStats* stats, cudaStream_t s) {
+  GateArgs ga{gate7[0], gate7[1], gate7[2], gate7[3], gate7[4], gate7[5], gate7[6]};
+  k_decode_gate<9><<<(n + 127) / 128, 128, 0, s>>>(n, out, ldo, d_norm, T, rho, Y, dt, ga, d_kncf, nele, list, count,
+                                                   dT_pred, stats);
+  return cudaGetLastError();
+}
+
+cudaError_t chem_launch_list(const int* list, const unsigned* count, double* T, const double* rho, double* Y,
+                             const double* dt, unsigned* d_counter, ChemStats* d_stats, cudaStream_t s) {
+  int blocks = 0;
+  if (chem_grid(&blocks)) return cudaErrorUnknown;
+  cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(unsigned), s);
+  if (e != cudaSuccess) return e;
+  k_psr_list<9><<<blocks, 128, 0, s>>>(list, count, T, rho, Y, dt, d_counter, d_stats);
   return cudaGetLastError();
 }

@@ -26,3 +26,12 @@ cudaError_t chem_upload_mech(const izem_mech* m);
 cudaError_t chem_launch_field(const ChemField& f, unsigned* d_counter, ChemStats* d_stats, cudaStream_t s, int kk);
 cudaError_t chem_launch_batch(int n, double* T, const double* rho, double* Y, const double* dt, int* istate,
                               int* nsteps, unsigned* d_counter, ChemStats* d_stats, cudaStream_t s, int kk);
+
+// learned-surrogate support (chem.cu)
+cudaError_t chem_launch_featurize(int n, const double* T, const double* rho, const double* Y, const double* dt,
+                                  const float* d_norm, void* x_bf16, int ldx, cudaStream_t s);
+cudaError_t chem_launch_decode_gate(int n, const float* out, int ldo, const float* d_norm, double* T, const double* rho,
+                                    double* Y, const double* dt, const double* gate7, const int* d_kncf, int nele,
+                                    int* list, unsigned* count, double* dT_pred, ChemStats* stats, cudaStream_t s);
+cudaError_t chem_launch_list(const int* list, const unsigned* count, double* T, const double* rho, double* Y,
+                             const double* dt, unsigned* d_counter, ChemStats* d_stats, cudaStream_t s);

@@ -1,0 +1,22 @@
+// Host build of the GPU stiff-chemistry integrator (phd_gb300/csrc/chem.cu,
+// compiled with IZEM_CHEM_HOST_TEST so that its __device__ integrator
+// functions are also host functions).  Used by tests/test_chem_cpu.py to
+// show that the device algorithm reproduces the oracle bit for bit when both
+// run without fused multiply-adds on the same CPU.
+#define IZEM_CHEM_HOST_TEST 1
+#include "../../phd_gb300/csrc/chem.cu"
+
+extern "C" void host_psr(const izem_mech* m, int n, double* T, const double* rho, double* Y, const double* dt,
+                         int* nst_out) {
+  c_mech_host = *m;
+  for (int q = 0; q < n; ++q) {
+    double z[10];
+    z[0] = T[q];
+    for (int k = 0; k < 9; ++k) z[1 + k] = Y[q * 9 + k];
+    int nst = 0;
+    reaction_v<10>(rho[q], z, dt[q], &nst);
+    nst_out[q] = nst;
+    T[q] = z[0];
+    for (int k = 0; k < 9; ++k) Y[q * 9 + k] = z[1 + k];
+  }
+}
