@@ -1,0 +1,205 @@
+"""Learned chemistry surrogate (host side).
+
+A 12 -> 4 x 256 (GELU) -> 10 MLP replaces, per cell, the chemistry increment
+that reaction_dvode (module_reaction.f90:102-321) computes with DVODE.  It
+runs in BF16 with FP32 accumulation on the tensor cores (libizem_gpu.so,
+izem_mlp_*), is trained on the GPU by the library's forward, backward and
+Adam kernels on samples labelled by the library's own FP64 BDF integrator
+(izem_gpu_psr_batch), and is used behind an error gate that sends rejected
+cells back to that integrator (izem_gpu_psr_batch_mlp).
+
+Features (same formula as the device featurisation kernel):
+    T [K], ln p [atm], ln(max(Y_k, 0) + 1e-10) for the 9 species, ln dt [s]
+Targets: dY_k (9 species) and dT [K] over dt.
+"""
+import ctypes as C
+
+import numpy as np
+
+from .capi import IzemMech
+from .izem import IzemError, load_library, psr_batch
+from .thd import load_species
+
+IN, OUT, H = 12, 10, 256
+LIN = [16, H, H, H, H]
+LOUT = [H, H, H, H, 16]
+NL = 5
+
+RU = 8.314510e7
+PATM = 1.01325e6
+
+
+def _bind(lib):
+    if getattr(lib, "_mlp_bound", False):
+        return lib
+    P = C.c_void_p
+    fpp = C.POINTER(C.POINTER(C.c_float))
+    sig = {
+        "izem_mlp_create": (C.c_int, [C.POINTER(P)]),
+        "izem_mlp_destroy": (None, [P]),
+        "izem_mlp_set_params": (C.c_int, [P, fpp, fpp]),
+        "izem_mlp_get_params": (C.c_int, [P, fpp, fpp]),
+        "izem_mlp_set_norm": (C.c_int, [P, C.POINTER(C.c_float)]),
+        "izem_mlp_forward": (C.c_int, [P, C.c_int, C.c_void_p, C.c_void_p]),
+        "izem_mlp_grads": (C.c_int, [P, C.c_int, C.c_void_p, C.c_void_p, C.POINTER(C.c_double), fpp, fpp]),
+        "izem_mlp_train": (C.c_int, [P, C.c_longlong, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_float,
+                                     C.c_uint, C.c_void_p]),
+        "izem_gpu_psr_batch_mlp": (C.c_int, [P, C.POINTER(IzemMech), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                             C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,
+                                             C.c_void_p, C.c_void_p]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    lib._mlp_bound = True
+    return lib
+
+
+def features(T, rho, Y, dt, wt):
+    """Raw (un-normalised) surrogate inputs, shape (n, 12)."""
+    Yc = np.maximum(Y, 0.0)
+    p_atm = rho * RU * T * (Yc / wt).sum(axis=1) / PATM
+    f = np.empty((len(T), IN))
+    f[:, 0] = T
+    f[:, 1] = np.log(p_atm)
+    f[:, 2:11] = np.log(Yc + 1e-10)
+    f[:, 11] = np.log(dt)
+    return f
+
+
+def he_init(seed):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    W, b = [], []
+    for l in range(NL):
+        fan_in = IN if l == 0 else H
+        w = np.zeros((LIN[l], LOUT[l]), dtype=np.float32)
+        rows = IN if l == 0 else LIN[l]
+        cols = OUT if l == NL - 1 else LOUT[l]
+        w[:rows, :cols] = rng.standard_normal((rows, cols)) * np.sqrt(2.0 / fan_in)
+        W.append(w)
+        b.append(np.zeros(LOUT[l], dtype=np.float32))
+    return W, b
+
+
+class Surrogate:
+    """Device MLP handle (izem_mlp) with its normalisation."""
+
+    def __init__(self, seed=20261203):
+        self.lib = _bind(load_library())
+        h = C.c_void_p()
+        rc = self.lib.izem_mlp_create(C.byref(h))
+        if rc:
+            raise IzemError(rc, "izem_mlp_create")
+        self.h = h
+        W, b = he_init(seed)
+        self.set_params(W, b)
+        self.norm = np.concatenate([np.zeros(IN), np.ones(IN), np.zeros(OUT), np.ones(OUT)]).astype(np.float32)
+        self.set_norm(self.norm)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.izem_mlp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    @staticmethod
+    def _pp(arrs):
+        t = (C.POINTER(C.c_float) * len(arrs))(*[a.ctypes.data_as(C.POINTER(C.c_float)) for a in arrs])
+        return t
+
+    def set_params(self, W, b):
+        self._W = [np.ascontiguousarray(w, dtype=np.float32) for w in W]
+        self._b = [np.ascontiguousarray(x, dtype=np.float32) for x in b]
+        rc = self.lib.izem_mlp_set_params(self.h, self._pp(self._W), self._pp(self._b))
+        if rc:
+            raise IzemError(rc, "izem_mlp_set_params")
+
+    def get_params(self):
+        W = [np.zeros((LIN[l], LOUT[l]), dtype=np.float32) for l in range(NL)]
+        b = [np.zeros(LOUT[l], dtype=np.float32) for l in range(NL)]
+        rc = self.lib.izem_mlp_get_params(self.h, self._pp(W), self._pp(b))
+        if rc:
+            raise IzemError(rc, "izem_mlp_get_params")
+        return W, b
+
+    def set_norm(self, norm):
+        self.norm = np.ascontiguousarray(norm, dtype=np.float32)
+        self.lib.izem_mlp_set_norm(self.h, self.norm.ctypes.data_as(C.POINTER(C.c_float)))
+
+    def fit_norm(self, X, Yt):
+        n = np.concatenate([X.mean(0), X.std(0) + 1e-6, Yt.mean(0), Yt.std(0) + 1e-12]).astype(np.float32)
+        self.set_norm(n)
+        return n
+
+    def normalise(self, X, Yt=None):
+        nx = ((X - self.norm[:IN]) / self.norm[IN:2 * IN]).astype(np.float32)
+        if Yt is None:
+            return np.ascontiguousarray(nx)
+        ny = ((Yt - self.norm[2 * IN:2 * IN + OUT]) / self.norm[2 * IN + OUT:]).astype(np.float32)
+        return np.ascontiguousarray(nx), np.ascontiguousarray(ny)
+
+    def forward(self, xn):
+        xn = np.ascontiguousarray(xn, dtype=np.float32)
+        y = np.zeros((len(xn), OUT), dtype=np.float32)
+        rc = self.lib.izem_mlp_forward(self.h, len(xn), xn.ctypes.data, y.ctypes.data)
+        if rc:
+            raise IzemError(rc, "izem_mlp_forward")
+        return y
+
+    def grads(self, xn, tn):
+        xn = np.ascontiguousarray(xn, dtype=np.float32)
+        tn = np.ascontiguousarray(tn, dtype=np.float32)
+        gW = [np.zeros((LIN[l], LOUT[l]), dtype=np.float32) for l in range(NL)]
+        gb = [np.zeros(LOUT[l], dtype=np.float32) for l in range(NL)]
+        loss = C.c_double()
+        rc = self.lib.izem_mlp_grads(self.h, len(xn), xn.ctypes.data, tn.ctypes.data, C.byref(loss),
+                                     self._pp(gW), self._pp(gb))
+        if rc:
+            raise IzemError(rc, "izem_mlp_grads")
+        return loss.value, gW, gb
+
+    def train(self, xn, tn, epochs=20, batch=4096, lr=1e-3, seed=7):
+        xn = np.ascontiguousarray(xn, dtype=np.float32)
+        tn = np.ascontiguousarray(tn, dtype=np.float32)
+        losses = np.zeros(epochs)
+        rc = self.lib.izem_mlp_train(self.h, len(xn), xn.ctypes.data, tn.ctypes.data, 0, epochs, batch, lr, seed,
+                                     losses.ctypes.data)
+        if rc:
+            raise IzemError(rc, "izem_mlp_train")
+        return losses
+
+    def chem_step(self, mech, T, rho, Y, dt, gate):
+        """Surrogate + gate + BDF fallback on independent reactors (host
+        arrays updated in place).  Returns dict with fallback count, times
+        and the raw predicted dT."""
+        kncf = np.ascontiguousarray(np.array(load_species("h2air9")["kncf"], dtype=np.int32))
+        g7 = np.ascontiguousarray(np.array(gate, dtype=np.float64))
+        dTp = np.zeros(len(T))
+        st3 = np.zeros(3, dtype=np.int32)
+        ms2 = np.zeros(2, dtype=np.float32)
+        rc = self.lib.izem_gpu_psr_batch_mlp(self.h, C.byref(mech), len(T), T.ctypes.data, rho.ctypes.data,
+                                             Y.ctypes.data, dt.ctypes.data, 0, g7.ctypes.data, kncf.ctypes.data,
+                                             kncf.shape[1], dTp.ctypes.data, st3.ctypes.data, ms2.ctypes.data)
+        if rc:
+            raise IzemError(rc, "izem_gpu_psr_batch_mlp")
+        return {"fallback": int(st3[0]), "max_steps": int(st3[1]), "failed": int(st3[2]), "ms": float(ms2[0]),
+                "ms_mlp": float(ms2[1]), "dT_pred": dTp}
+
+
+DEFAULT_GATE = (800.0, 2400.0, 1e-8, 1e-6, 2e-3, 2.0, 0.02)
+
+
+def training_set(mech, n, seed):
+    """n reactors from the batched-chemistry distribution labelled by the
+    FP64 BDF integrator on the GPU: returns raw features and targets."""
+    from .ics import batched_reactors
+    T, rho, Y, dt = batched_reactors(n, seed=seed)
+    wt = np.array([mech.wt[k] for k in range(mech.kk)])
+    X = features(T, rho, Y, dt, wt)
+    T1, Y1 = T.copy(), Y.copy()
+    psr_batch(mech, T1, rho.copy(), Y1, dt.copy())
+    Yt = np.concatenate([Y1 - Y, (T1 - T)[:, None]], axis=1)
+    return X, Yt
