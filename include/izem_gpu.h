@@ -223,13 +223,15 @@ int  izem_mlp_train(izem_mlp* m, long long n, const float* x, const float* t, in
                     int epochs, int batch, float lr, unsigned seed, double* losses);
 /* Surrogate chemistry step on independent reactors with the per-cell error
  * gate (training envelope, element conservation of dY, internal-energy
- * consistency of dT); rejected cells are integrated by the BDF method.
- * gate7 = {Tmin, Tmax, dtmin, dtmax, tol_el, tol_T_abs, tol_T_rel};
- * kncf[kk][nele] element counts; stats3 = {fallback cells, max BDF steps,
- * failed cells}; ms2 = {total ms, MLP ms}. */
-int  izem_gpu_psr_batch_mlp(izem_mlp* m, const izem_mech* mech, int n, double* T, const double* rho,
-                            double* Y, const double* dt, int device_ptrs, const double* gate7,
-                            const int* kncf, int nele, double* dT_pred, int* stats3, float* ms2);
+ * consistency of dT, agreement with a second independently trained network
+ * m2 when m2 is not NULL); rejected cells are integrated by the BDF method.
+ * gate9 = {Tmin, Tmax, dtmin, dtmax, tol_el, tol_T_abs, tol_T_rel,
+ * tol_ens_abs, tol_ens_rel}; kncf[kk][nele] element counts; stats3 =
+ * {fallback cells, max BDF steps, failed cells}; ms2 = {total ms, MLP ms}. */
+int  izem_gpu_psr_batch_mlp(izem_mlp* m, izem_mlp* m2, const izem_mech* mech, int n, double* T,
+                            const double* rho, double* Y, const double* dt, int device_ptrs,
+                            const double* gate9, const int* kncf, int nele, double* dT_pred,
+                            int* stats3, float* ms2);
 
 /* Device timing of the calls above on the context's stream (CUDA events). */
 int  izem_gpu_timer_start(izem_ctx* ctx);

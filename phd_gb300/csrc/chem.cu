@@ -799,6 +799,7 @@ struct GateArgs {
   double tmin, tmax, dtmin, dtmax;   // training envelope
   double tol_el;                     // relative element residual
   double tol_T_abs, tol_T_rel;       // energy-consistency of dT [K]
+  double tol_ens_abs, tol_ens_rel;   // agreement of two independently trained networks on dT [K]
 };
 
 // Decode the surrogate output, gate it, and write accepted cells in place.
@@ -809,9 +810,9 @@ struct GateArgs {
 // take the energy-consistent temperature.  Rejected cells are appended to
 // `list` for the BDF integrator.
 template <int KK>
-__global__ void k_decode_gate(int n, const float* out, int ldo, const float* norm, double* T, const double* rho, double* Y,
-                              const double* dt, GateArgs ga, const int* kncf, int nele, int* list, unsigned* count,
-                              double* dT_pred, ChemStats* stats) {
+__global__ void k_decode_gate(int n, const float* out, const float* out2, int ldo, const float* norm, const float* norm2,
+                              double* T, const double* rho, double* Y, const double* dt, GateArgs ga, const int* kncf,
+                              int nele, int* list, unsigned* count, double* dT_pred, ChemStats* stats) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= n) return;
   const int NI = KK + 3, NO = KK + 1;
@@ -824,6 +825,10 @@ __global__ void k_decode_gate(int n, const float* out, int ldo, const float* nor
   for (int k = 0; k < KK; ++k) dY[k] = (double)out[(size_t)q * ldo + k] * so[k] + mo[k];
   const double dTp = (double)out[(size_t)q * ldo + KK] * so[KK] + mo[KK];
   if (dT_pred) dT_pred[q] = dTp;
+  if (out2) {
+    const double dT2 = (double)out2[(size_t)q * ldo + KK] * norm2[2 * NI + NO + KK] + norm2[2 * NI + KK];
+    if (fabs(dT2 - dTp) > ga.tol_ens_abs + ga.tol_ens_rel * fabs(dTp)) ok = false;
+  }
   // element residuals
   for (int e = 0; e < nele && ok; ++e) {
     double r = 0.0, sc = 0.0;
@@ -939,12 +944,13 @@ cudaError_t chem_launch_featurize(int n, const double* T, const double* rho, con
   return cudaGetLastError();
 }
 
-cudaError_t chem_launch_decode_gate(int n, const float* out, int ldo, const float* d_norm, double* T, const double* rho,
-                                    double* Y, const double* dt, const double* gate7, const int* d_kncf, int nele,
-                                    int* list, unsigned* count, double* dT_pred, ChemStats* stats, cudaStream_t s) {
-  GateArgs ga{gate7[0], gate7[1], gate7[2], gate7[3], gate7[4], gate7[5], gate7[6]};
-  k_decode_gate<9><<<(n + 127) / 128, 128, 0, s>>>(n, out, ldo, d_norm, T, rho, Y, dt, ga, d_kncf, nele, list, count,
-                                                   dT_pred, stats);
+cudaError_t chem_launch_decode_gate(int n, const float* out, const float* out2, int ldo, const float* d_norm,
+                                    const float* d_norm2, double* T, const double* rho, double* Y, const double* dt,
+                                    const double* gate9, const int* d_kncf, int nele, int* list, unsigned* count,
+                                    double* dT_pred, ChemStats* stats, cudaStream_t s) {
+  GateArgs ga{gate9[0], gate9[1], gate9[2], gate9[3], gate9[4], gate9[5], gate9[6], gate9[7], gate9[8]};
+  k_decode_gate<9><<<(n + 127) / 128, 128, 0, s>>>(n, out, out2, ldo, d_norm, d_norm2, T, rho, Y, dt, ga, d_kncf, nele,
+                                                   list, count, dT_pred, stats);
   return cudaGetLastError();
 }
 

@@ -530,19 +530,24 @@ int izem_mlp_train(izem_mlp* m, long long n, const float* x, const float* t, int
 
 // Surrogate chemistry on n independent reactors (same arrays as
 // izem_gpu_psr_batch): MLP inference in chunks, the error gate, and the BDF
-// integrator on every rejected cell.  gate7 = {Tmin, Tmax, dtmin, dtmax,
-// tol_el, tol_T_abs, tol_T_rel}; kncf = element counts [kk][nele].
+// integrator on every rejected cell.  gate9 = {Tmin, Tmax, dtmin, dtmax,
+// tol_el, tol_T_abs, tol_T_rel, tol_ens_abs, tol_ens_rel}; m2 (optional) is
+// a second, independently trained network whose dT must agree with m's;
+// kncf = element counts [kk][nele].
 // dT_pred (optional, device or host like the other arrays) receives the raw
 // network temperature increment.  stats3 = {fallback cells, max BDF steps,
 // failed}; ms2 = {total kernel ms, MLP-only ms}.
-int izem_gpu_psr_batch_mlp(izem_mlp* m, const izem_mech* mech, int n, double* T, const double* rho, double* Y,
-                           const double* dt, int device_ptrs, const double* gate7, const int* kncf, int nele,
+int izem_gpu_psr_batch_mlp(izem_mlp* m, izem_mlp* m2, const izem_mech* mech, int n, double* T, const double* rho,
+                           double* Y, const double* dt, int device_ptrs, const double* gate9, const int* kncf, int nele,
                            double* dT_pred, int* stats3, float* ms2) {
-  if (!m || !mech || n <= 0 || !T || !rho || !Y || !dt || !gate7 || !kncf || mech->kk != 9) return IZEM_ERR_ARG;
+  if (!m || !mech || n <= 0 || !T || !rho || !Y || !dt || !gate9 || !kncf || mech->kk != 9) return IZEM_ERR_ARG;
   const int CH = 1 << 20;
   const int chunk = n < CH ? n : CH;
   cudaStream_t s = m->s;
   if (mlp_infer_ensure(m, chunk) != cudaSuccess) return IZEM_ERR_NOMEM;
+  if (m2 && mlp_infer_ensure(m2, chunk) != cudaSuccess) return IZEM_ERR_NOMEM;
+  if (m2 && !m2->d_norm && cudaMalloc(&m2->d_norm, sizeof(m2->norm)) != cudaSuccess) return IZEM_ERR_NOMEM;
+  if (m2) cudaMemcpyAsync(m2->d_norm, m2->norm, sizeof(m2->norm), cudaMemcpyHostToDevice, s);
   if (chem_upload_mech(mech) != cudaSuccess) return IZEM_ERR_CUDA;
   int* d_kncf = nullptr;
   int* d_list = nullptr;
@@ -580,10 +585,15 @@ int izem_gpu_psr_batch_mlp(izem_mlp* m, const izem_mech* mech, int n, double* T,
     cudaEventRecord(a0, s);
     chem_launch_featurize(cn, dT + c0, drho + c0, dY + (size_t)c0 * kk, ddt + c0, m->d_norm, m->ib[0], INP, s);
     if (mlp_infer(m, cn, s) != cudaSuccess) { rc = IZEM_ERR_CUDA; break; }
+    if (m2) {
+      chem_launch_featurize(cn, dT + c0, drho + c0, dY + (size_t)c0 * kk, ddt + c0, m2->d_norm, m2->ib[0], INP, s);
+      if (mlp_infer(m2, cn, s) != cudaSuccess) { rc = IZEM_ERR_CUDA; break; }
+    }
     cudaEventRecord(a1, s);
     cudaMemsetAsync(d_count, 0, sizeof(unsigned), s);
-    chem_launch_decode_gate(cn, m->iout, OUTP, m->d_norm, dT + c0, drho + c0, dY + (size_t)c0 * kk, ddt + c0, gate7,
-                            d_kncf, nele, d_list, d_count, ddTp ? ddTp + c0 : nullptr, d_st, s);
+    chem_launch_decode_gate(cn, m->iout, m2 ? m2->iout : nullptr, OUTP, m->d_norm, m2 ? m2->d_norm : nullptr, dT + c0,
+                            drho + c0, dY + (size_t)c0 * kk, ddt + c0, gate9, d_kncf, nele, d_list, d_count,
+                            ddTp ? ddTp + c0 : nullptr, d_st, s);
     chem_launch_list(d_list, d_count, dT + c0, drho + c0, dY + (size_t)c0 * kk, ddt + c0, d_counter, d_st, s);
     unsigned hc = 0;
     cudaMemcpyAsync(&hc, d_count, sizeof(unsigned), cudaMemcpyDeviceToHost, s);

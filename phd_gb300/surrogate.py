@@ -44,9 +44,9 @@ def _bind(lib):
         "izem_mlp_grads": (C.c_int, [P, C.c_int, C.c_void_p, C.c_void_p, C.POINTER(C.c_double), fpp, fpp]),
         "izem_mlp_train": (C.c_int, [P, C.c_longlong, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_float,
                                      C.c_uint, C.c_void_p]),
-        "izem_gpu_psr_batch_mlp": (C.c_int, [P, C.POINTER(IzemMech), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
-                                             C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,
-                                             C.c_void_p, C.c_void_p]),
+        "izem_gpu_psr_batch_mlp": (C.c_int, [P, P, C.POINTER(IzemMech), C.c_int, C.c_void_p, C.c_void_p,
+                                             C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int,
+                                             C.c_void_p, C.c_void_p, C.c_void_p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -171,16 +171,18 @@ class Surrogate:
             raise IzemError(rc, "izem_mlp_train")
         return losses
 
-    def chem_step(self, mech, T, rho, Y, dt, gate):
+    def chem_step(self, mech, T, rho, Y, dt, gate, partner=None):
         """Surrogate + gate + BDF fallback on independent reactors (host
-        arrays updated in place).  Returns dict with fallback count, times
-        and the raw predicted dT."""
+        arrays updated in place).  partner: a second Surrogate whose dT must
+        agree.  Returns dict with fallback count, times and the raw
+        predicted dT."""
         kncf = np.ascontiguousarray(np.array(load_species("h2air9")["kncf"], dtype=np.int32))
         g7 = np.ascontiguousarray(np.array(gate, dtype=np.float64))
         dTp = np.zeros(len(T))
         st3 = np.zeros(3, dtype=np.int32)
         ms2 = np.zeros(2, dtype=np.float32)
-        rc = self.lib.izem_gpu_psr_batch_mlp(self.h, C.byref(mech), len(T), T.ctypes.data, rho.ctypes.data,
+        rc = self.lib.izem_gpu_psr_batch_mlp(self.h, partner.h if partner is not None else None, C.byref(mech),
+                                             len(T), T.ctypes.data, rho.ctypes.data,
                                              Y.ctypes.data, dt.ctypes.data, 0, g7.ctypes.data, kncf.ctypes.data,
                                              kncf.shape[1], dTp.ctypes.data, st3.ctypes.data, ms2.ctypes.data)
         if rc:
@@ -189,7 +191,28 @@ class Surrogate:
                 "ms_mlp": float(ms2[1]), "dT_pred": dTp}
 
 
-DEFAULT_GATE = (800.0, 2400.0, 1e-8, 1e-6, 2e-3, 2.0, 0.02)
+# Tmin, Tmax, dtmin, dtmax, tol_el, tol_T_abs [K], tol_T_rel, tol_ens_abs [K], tol_ens_rel
+DEFAULT_GATE = (800.0, 2400.0, 1e-8, 1e-6, 2e-3, 2.0, 0.02, 1.0, 0.005)
+
+
+def train_ensemble(mech, n=1 << 22, seed=31, epochs=30, batch=4096, lr=1e-3, members=2, log=None):
+    """Train `members` networks on n reactors labelled by the GPU BDF
+    integrator (same samples, different initialisations and shuffles), with
+    a step-decayed learning rate.  Returns the list of Surrogates."""
+    X, Yt = training_set(mech, n, seed)
+    nets = []
+    for q in range(members):
+        s = Surrogate(seed=seed + 1000 * (q + 1))
+        s.fit_norm(X, Yt)
+        xn, tn = s.normalise(X, Yt)
+        hist = []
+        for stage, f in enumerate((1.0, 0.3, 0.1)):
+            ep = max(1, epochs // 3)
+            hist += list(s.train(xn, tn, epochs=ep, batch=batch, lr=lr * f, seed=seed + 17 * q + stage))
+        if log is not None:
+            log.append({"member": q, "loss": hist})
+        nets.append(s)
+    return nets
 
 
 def training_set(mech, n, seed):

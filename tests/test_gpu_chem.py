@@ -11,7 +11,7 @@ Bounds, with tol(y) = RTOL |y| + ATOL (RTOL = 1e-6):
   * temperature, every cell:   |dT| <= 100 tol(T)   (1e-4 relative)
   * temperature, 99 % of cells: |dT| <= 10 tol(T)
   * species, every cell:       |dY_k| <= 1e-3 max_cells |Y_k|
-  * median cell: relative T difference below 1e-12"""
+  * median cell: relative T difference below 1e-10 (rounding level)"""
 import numpy as np
 import pytest
 
@@ -38,7 +38,7 @@ def test_psr_batch_matches_oracle():
     msg = "T: max %.3g p99 %.3g (units of tol); Y: max normwise %.3g" % (rT.max(), np.percentile(rT, 99), rYn)
     assert rT.max() <= 100 and np.percentile(rT, 99) <= 10, msg
     assert rYn <= 1e-3, msg
-    assert np.median(np.abs(Tg - To) / To) < 1e-12, msg
+    assert np.median(np.abs(Tg - To) / To) < 1e-10, msg
 
 
 def test_field_chem_step_matches_oracle():

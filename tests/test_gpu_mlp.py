@@ -14,7 +14,7 @@ from oracle import mlp_oracle as mo
 from phd_gb300 import ics
 from phd_gb300.izem import psr_batch
 from phd_gb300.mech import h2_mechanism
-from phd_gb300.surrogate import DEFAULT_GATE, Surrogate, features, training_set
+from phd_gb300.surrogate import DEFAULT_GATE, Surrogate, features, train_ensemble, training_set
 
 pytestmark = pytest.mark.gpu
 
@@ -64,17 +64,13 @@ def test_surrogate_gains_over_bdf_with_gate():
     active its temperature increments stay within 1 % of the largest FP64
     increment."""
     mech = h2_mechanism()
-    X, Yt = training_set(mech, 1 << 18, seed=31)
-    s = Surrogate(seed=14)
-    s.fit_norm(X, Yt)
-    xn, tn = s.normalise(X, Yt)
-    s.train(xn, tn, epochs=25, batch=4096, lr=1e-3)
+    s, s2 = train_ensemble(mech, n=1 << 19, seed=31, epochs=24)
     T, rho, Y, dt = ics.batched_reactors(1 << 17, seed=77)
     Tb, Yb = T.copy(), Y.copy()
     t0 = time.perf_counter()
     _, _, ms_bdf = psr_batch(mech, Tb, rho.copy(), Yb, dt.copy())
     Ts, Ys = T.copy(), Y.copy()
-    r = s.chem_step(mech, Ts, rho.copy(), Ys, dt.copy(), DEFAULT_GATE)
+    r = s.chem_step(mech, Ts, rho.copy(), Ys, dt.copy(), DEFAULT_GATE, partner=s2)
     dT_ref = Tb - T
     err = np.abs((Ts - T) - dT_ref)
     scale = np.abs(dT_ref).max()
