@@ -10,8 +10,9 @@
 // reference's operation order so that results agree to rounding.  Build with
 // -ffp-contract=off so that no multiply-add is fused on either machine.
 //
-// Parity pinning: the non-reacting WENO path is pinned against the stored
-// Sod run of the reference (testcases/sod); see tests/test_oracle_sod.py.
+// Parity pinning: the chemistry restatement is cross-checked against an
+// independent DVODE (scipy's BDF integrator) on the same reactor equations;
+// the flow path is not yet pinned against stored outputs of the reference.
 //
 // Layout: one block of nx*ny*nz interior points with ng ghost layers,
 // Fortran column-major, variable index slowest, exactly the reference's
