@@ -43,7 +43,8 @@ enum {
   IZEM_ERR_CHEM = 6,           /* stiff integrator failed on at least one cell     */
   IZEM_ERR_TIMEOUT = 7,        /* a bounded device-side wait gave up               */
   IZEM_ERR_NOMEM = 8,          /* device allocation failed                         */
-  IZEM_ERR_STATE = 9           /* call made in the wrong order (e.g. no grid set)  */
+  IZEM_ERR_STATE = 9,          /* call made in the wrong order (e.g. no grid set)  */
+  IZEM_ERR_TOO_LARGE = 10      /* request above a fixed capacity (no-alloc calls)  */
 };
 
 /* Hot-path switches and sizes: the subset of the reference's globals that the
@@ -232,6 +233,24 @@ int  izem_gpu_psr_batch_mlp(izem_mlp* m, izem_mlp* m2, const izem_mech* mech, in
                             const double* rho, double* Y, const double* dt, int device_ptrs,
                             const double* gate9, const int* kncf, int nele, double* dT_pred,
                             int* stats3, float* ms2);
+/* No counterpart in the reference.  Inference for callers that cannot
+ * allocate device memory while they run -- a solver whose own arena (or a
+ * framework's caching allocator) already holds the GPU's memory, or one that
+ * calls the surrogate inside its time-step loop, where cudaMalloc/cudaFree
+ * would synchronise the whole device.  Same result as izem_mlp_forward, but
+ * d_x (M x 12) and d_y (M x 10) are FP32 device arrays, the work is queued
+ * on `stream` (a cudaStream_t; NULL is the default stream) and the call
+ * returns without waiting.  No memory is allocated or freed: the
+ * activations use one fixed device array of about 4.3 MiB per GPU, which
+ * every GPU that loads the library holds until the process exits, so M is
+ * at most IZEM_MLP_NOALLOC_MAX_ROWS (larger M returns IZEM_ERR_TOO_LARGE;
+ * split the batch).  The first call on a device looks up that array's
+ * address; make it before any stream capture.  All calls share the array:
+ * calls that may overlap on the GPU (different streams, or several host
+ * threads) race and must be serialised by the caller.  The handle's
+ * parameters are allocated once by izem_mlp_create. */
+#define IZEM_MLP_NOALLOC_MAX_ROWS 4096
+int  izem_mlp_forward_noalloc(izem_mlp* m, int M, const float* d_x, float* d_y, void* stream);
 
 /* Device timing of the calls above on the context's stream (CUDA events). */
 int  izem_gpu_timer_start(izem_ctx* ctx);

@@ -21,13 +21,14 @@ ERR_CHEM = 6
 ERR_TIMEOUT = 7
 ERR_NOMEM = 8
 ERR_STATE = 9
+ERR_TOO_LARGE = 10
 
 ERR_NAMES = {
     OK: "ok", ERR_ARG: "bad argument", ERR_CUDA: "CUDA error",
     ERR_NEG_PRESSURE: "negative pressure", ERR_NEG_TEMPERATURE: "negative temperature",
     ERR_NAN: "NaN in Newton temperature", ERR_CHEM: "stiff integrator failure",
     ERR_TIMEOUT: "device wait timed out", ERR_NOMEM: "out of device memory",
-    ERR_STATE: "call out of order",
+    ERR_STATE: "call out of order", ERR_TOO_LARGE: "above a fixed capacity",
 }
 
 

@@ -13,6 +13,7 @@
 #include <cstdio>
 #include <cstring>
 #include <cmath>
+#include <mutex>
 #include <vector>
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
@@ -624,3 +625,97 @@ int izem_gpu_psr_batch_mlp(izem_mlp* m, izem_mlp* m2, const izem_mech* mech, int
 }
 
 }  // extern "C"
+
+// ===================================================== no-alloc inference ===
+// Surrogate inference for callers that cannot allocate device memory while
+// they run: a flow solver that hands the whole GPU to its own memory arena
+// (or to a framework's caching allocator) at start-up, or that calls the
+// surrogate inside its time-step loop, where a cudaMalloc/cudaFree would
+// synchronise the whole device and stall its other streams.  The activations
+// that izem_mlp_forward keeps in per-handle buffers live here in one
+// file-scope device array instead, sized for IZEM_MLP_NOALLOC_MAX_ROWS rows.
+//
+// The array exists once per device for the life of the process.  Its name,
+// used in host code, is only a host-side stand-in: host code passes kernels
+// the device address looked up with cudaGetSymbolAddress, once per device.
+namespace {
+
+constexpr int NA_ROWS = IZEM_MLP_NOALLOC_MAX_ROWS;
+constexpr size_t NA_ACT_BYTES = (size_t)NA_ROWS * H * sizeof(__nv_bfloat16);   // one activation buffer
+constexpr size_t NA_OUT_BYTES = (size_t)NA_ROWS * OUTP * sizeof(float);
+constexpr size_t NA_BYTES = 2 * NA_ACT_BYTES + NA_OUT_BYTES;                    // 4 MiB + 256 KiB
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NA_BYTES];
+
+constexpr int NA_MAX_DEV = 64;
+unsigned char* g_noalloc_addr[NA_MAX_DEV] = {};   // device address per device ordinal
+std::mutex g_noalloc_mu;
+
+// The array's device address on the current device (looked up on the first
+// call per device).
+cudaError_t noalloc_scratch(unsigned char** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= NA_MAX_DEV) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_addr[dev]) {
+    void* p = nullptr;
+    if ((e = cudaGetSymbolAddress(&p, g_noalloc_scratch)) != cudaSuccess) return e;
+    g_noalloc_addr[dev] = static_cast<unsigned char*>(p);
+  }
+  *out = g_noalloc_addr[dev];
+  return cudaSuccess;
+}
+
+// x (M x 12 FP32) -> BF16 rows padded to 16 columns.  The padding columns are
+// written as zeros on every call: the array keeps the previous call's data.
+__global__ void k_na_pack(const float* __restrict__ x, int M, __nv_bfloat16* __restrict__ a) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= (long long)M * INP) return;
+  const int r = (int)(i / INP), c = (int)(i % INP);
+  a[i] = __float2bfloat16(c < IN ? x[(size_t)r * IN + c] : 0.0f);
+}
+
+// network output (M x 16 FP32) -> y (M x 10 FP32)
+__global__ void k_na_unpack(const float* __restrict__ o, int M, float* __restrict__ y) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= (long long)M * OUT) return;
+  const int r = (int)(i / OUT), c = (int)(i % OUT);
+  y[i] = o[(size_t)r * OUTP + c];
+}
+
+}  // namespace
+
+extern "C" int izem_mlp_forward_noalloc(izem_mlp* m, int M, const float* d_x, float* d_y, void* stream) {
+  if (!m || !d_x || !d_y || M <= 0) return IZEM_ERR_ARG;
+  if (M > NA_ROWS) return IZEM_ERR_TOO_LARGE;
+  unsigned char* base = nullptr;
+  if (noalloc_scratch(&base) != cudaSuccess) return IZEM_ERR_CUDA;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  __nv_bfloat16* buf[2] = {reinterpret_cast<__nv_bfloat16*>(base),
+                           reinterpret_cast<__nv_bfloat16*>(base + NA_ACT_BYTES)};
+  float* out = reinterpret_cast<float*>(base + 2 * NA_ACT_BYTES);
+  k_na_pack<<<g1((long long)M * INP), 256, 0, s>>>(d_x, M, buf[0]);
+  int cur = 0;
+  for (int l = 0; l < NL; ++l) {
+    GemmArgs a{};
+    a.A = buf[cur];
+    a.B = m->Wb[l];
+    a.M = M; a.N = LOUT[l]; a.K = LIN[l];
+    a.lda = LIN[l]; a.ldb = LOUT[l]; a.ldc = LOUT[l];
+    a.bias = m->b[l];
+    cudaError_t e;
+    if (l < NL - 1) {
+      a.Cb = buf[1 - cur];
+      e = gemm<0, 0, EPI_BIAS_GELU>(a, s);
+      cur = 1 - cur;
+    } else {
+      a.Cf = out;
+      e = gemm<0, 0, EPI_BIAS>(a, s);
+    }
+    if (e != cudaSuccess) return IZEM_ERR_CUDA;
+  }
+  k_na_unpack<<<g1((long long)M * OUT), 256, 0, s>>>(out, M, d_y);
+  return cudaGetLastError() == cudaSuccess ? IZEM_OK : IZEM_ERR_CUDA;
+}
