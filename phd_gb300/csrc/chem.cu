@@ -9,11 +9,15 @@
 //
 // Execution model: a persistent kernel whose threads each take the next
 // cell from a global counter (atomicAdd) when their current cell finishes,
-// so cells with few BDF steps do not wait for cells with many.  Every loop
-// is bounded (MXSTEP = 500 steps per DVODE call, 20 calls, at most 10
-// corrector failures and 7 error-test failures per step): the kernel
-// cannot spin.  Per-thread DVODE arrays (Nordsieck history, iteration
-// matrix and its saved Jacobian) live in local memory.
+// so cells with few BDF steps do not wait for cells with many.  The method
+// is written as a resumable state machine (rc_advance) that stops at every
+// right-hand-side evaluation, so the threads of a warp -- each on its own
+// cell, at its own point of the method -- evaluate FUN together instead of
+// one divergent branch at a time.  Every loop is bounded (MXSTEP = 500
+// steps per DVODE call, 20 calls, at most 10 corrector failures and 7
+// error-test failures per step): the kernel cannot spin.  Per-thread DVODE
+// arrays (Nordsieck history, iteration matrix and its saved Jacobian) live
+// in local memory.
 #include <cstdio>
 #include <cstring>
 #include <cmath>
@@ -344,431 +348,642 @@ HD void dvjust(Dv<N>& d, int iord) {
   }
 }
 
-template <int N>
-HD int dvjac(Dv<N>& d, double* y, double* ftem) {
-  int jok = 1;
-  if (d.nst == 0 || d.nst > d.nslj + 50) jok = -1;
-  if (d.icf == 1 && d.drc < 0.2) jok = -1;
-  if (d.icf == 2) jok = -1;
-  if (jok == -1) {
-    d.nslj = d.nst;
-    d.jcur = 1;
-    double fac = dvnorm<N>(d.savf, d.ewt);
-    double r0 = 1000.0 * fabs(d.h) * kUround * double(N) * fac;
-    if (r0 == 0.0) r0 = 1.0;
-    const double srur = 1.4901161193847656e-08;   // sqrt(UROUND)
-    for (int j = 0; j < N; ++j) {
-      const double yj = y[j];
-      const double r = fmax(srur * fabs(yj), r0 / d.ewt[j]);
-      y[j] = y[j] + r;
-      fac = 1.0 / r;
-      ck_fun<N - 1>(d.rho, y, ftem);
-      for (int i = 0; i < N; ++i) d.wmjs[i + j * N] = (ftem[i] - d.savf[i]) * fac;
-      y[j] = yj;
-    }
-  } else {
-    d.jcur = 0;
-  }
-  const double con = -(d.h * d.rl1);
-  for (int q = 0; q < N * N; ++q) d.wm[q] = con * d.wmjs[q];
-  for (int i = 0; i < N; ++i) d.wm[i + i * N] = d.wm[i + i * N] + 1.0;
-  return dgefa<N>(d.wm, d.ipvt) != 0 ? 1 : 0;
-}
+// ------------------------------------------ DVODE as a resumable machine ----
+// The integrator below is DVODE's BDF path (DVODE -> DVHIN, DVSTEP -> DVNLSD
+// -> DVJAC, vode.f:4286-7790) inside REACTION_V's restart loop, written in
+// reverse-communication form: rc_advance() runs the control logic of one
+// cell until it needs the right-hand side FUN at the current y, stores its
+// position in `pc` and returns true; the caller evaluates FUN(y) into fo and
+// calls rc_advance() again.  Every right-hand-side evaluation of the method
+// is one of six such requests:
+//   F0    the initial derivative (DVODE, before DVHIN)
+//   HIN   a trial derivative of the initial-step iteration (DVHIN)
+//   PRED  f at the predicted state (DVNLSD, each pass)
+//   JAC   one column of the finite-difference Jacobian (DVJAC)
+//   CORR  f after a corrector update (DVNLSD)
+//   ERRF  f after repeated error-test failures at order 1 (DVSTEP)
+// A warp's threads, each on its own cell and at its own point of the method,
+// so all evaluate FUN together in one converged call per round, and only the
+// (cheaper) control logic diverges.  The arithmetic and its order are those
+// of a straight-line restatement of DVODE; results are identical to it.
+enum : int {
+  ST_DVODE = 0, ST_F0, ST_HIN_ITER, ST_HIN_F, ST_MAIN, ST_STEP_BEGIN, ST_STEP_LOOP, ST_NLS_PASS, ST_NLS_PRED_F,
+  ST_JAC_COL, ST_JAC_COL_F, ST_NLS_ITER, ST_NLS_CORR_F, ST_ERRF_F, ST_DONE
+};
 
 template <int N>
-HD int dvnlsd(Dv<N>& d, double* y, double* ftem, int nflag) {
-  if (d.jstart == 0) d.nslp = 0;
-  if (nflag == 0) d.icf = 0;
-  if (nflag == -2) d.ipup = 2;
-  if (d.jstart == 0) d.ipup = 2;
-  d.drc = fabs(d.rc - 1.0);
-  if (d.drc > 0.3 || d.nst >= d.nslp + 20) d.ipup = 2;
-  for (int pass = 0; pass < 2; ++pass) {
-    int m = 0;
-    double delp = 0.0;
-    for (int i = 0; i < N; ++i) y[i] = d.yh[i];
-    ck_fun<N - 1>(d.rho, y, d.savf);
-    if (d.ipup > 0) {
-      const int ierpj = dvjac<N>(d, y, ftem);
-      d.ipup = 0;
-      d.rc = 1.0;
-      d.drc = 0.0;
-      d.crate = 1.0;
-      d.nslp = d.nst;
-      if (ierpj != 0) { d.icf = 2; d.ipup = 2; return -1; }
-    }
-    for (int i = 0; i < N; ++i) d.acor[i] = 0.0;
-    for (int it = 0; it < 3; ++it) {
-      for (int i = 0; i < N; ++i) y[i] = (d.rl1 * d.h) * d.savf[i] - (d.rl1 * d.yh[i + N] + d.acor[i]);
-      dgesl<N>(d.wm, d.ipvt, y);
-      if (d.rc != 1.0) {
-        const double cscale = 2.0 / (1.0 + d.rc);
-        for (int i = 0; i < N; ++i) y[i] = cscale * y[i];
-      }
-      const double del = dvnorm<N>(y, d.ewt);
-      for (int i = 0; i < N; ++i) d.acor[i] = d.acor[i] + y[i];
-      for (int i = 0; i < N; ++i) y[i] = d.yh[i] + d.acor[i];
-      if (m != 0) d.crate = fmax(0.3 * d.crate, del / delp);
-      const double dcon = del * fmin(1.0, d.crate) / d.tq[3];
-      if (dcon <= 1.0) {
-        d.jcur = 0;
-        d.icf = 0;
-        d.acnrm = (m == 0) ? del : dvnorm<N>(d.acor, d.ewt);
-        return 0;
-      }
-      m = m + 1;
-      if (m == 3 || (m >= 2 && del > 2.0 * delp)) break;
-      delp = del;
-      ck_fun<N - 1>(d.rho, y, d.savf);
-    }
-    if (d.jcur == 1) break;
-    d.icf = 1;
-    d.ipup = 2;
-  }
-  d.icf = 2;
-  d.ipup = 2;
-  return -1;
+struct Rc : Dv<N> {
+  double y[N], fo[N];                       // FUN argument / result
+  double tcur, tout;                        // REACTION_V's time and target
+  double hg, hub, hlb, hnew;                // DVHIN
+  double told;                              // DVSTEP
+  double delp;                              // DVNLSD
+  double yj, rfac, r0;                      // DVJAC
+  int pc, ib, istate, nsteps;               // REACTION_V
+  int first, mguard, iter;                  // DVODE main loop, DVHIN
+  int ncf, nflag, rescale, sguard;          // DVSTEP
+  int pass, m, it, jcol;                    // DVNLSD, DVJAC
+};
+
+template <int N>
+HD void rc_start(Rc<N>& r, double rho, const double* z, double tf) {
+  r.rho = rho;
+  for (int i = 0; i < N; ++i) r.y[i] = z[i];
+  r.tcur = 0.0;
+  r.tout = tf;
+  r.istate = 1;
+  r.ib = 0;
+  r.nsteps = 0;
+  r.pc = ST_DVODE;
 }
 
-// one DVSTEP; returns KFLAG (0, -1 error test, -2 convergence)
+// REACTION_V: after each DVODE return, restart while ISTATE != 2, at most 20 calls.
 template <int N>
-HD int dvstep(Dv<N>& d, double* y, double* ftem) {
-  d.kflag = 0;
-  const double told = d.tn;
-  int ncf = 0, nflag = 0;
-  d.jcur = 0;
-  bool rescale;
-  if (d.jstart > 0) {
-    rescale = false;
-    if (d.newh != 0) {
-      if (d.newq < d.nq) { dvjust<N>(d, -1); d.nq = d.newq; d.l = d.nq + 1; d.nqwait = d.l; }
-      else if (d.newq > d.nq) { dvjust<N>(d, 1); d.nq = d.newq; d.l = d.nq + 1; d.nqwait = d.l; }
-      rescale = true;
-    }
-  } else {
-    d.lmax = 6;
-    d.nq = 1;
-    d.l = 2;
-    d.nqnyh = N;
-    d.tau[0] = d.h;
-    d.prl1 = 1.0;
-    d.rc = 0.0;
-    d.etamax = 1.0e4;
-    d.nqwait = 2;
-    d.hscal = d.h;
-    rescale = false;
+HD __forceinline__ void rc_after_dvode(Rc<N>& r, int istate) {
+  r.istate = istate;
+  r.ib = r.ib + 1;
+  r.pc = (r.ib < 20 && istate != 2) ? ST_DVODE : ST_DONE;
+}
+
+// DVODE after DVHIN: scale the first Nordsieck column and enter the step loop.
+template <int N>
+HD __forceinline__ void rc_hin_finish(Rc<N>& r, double h0) {
+  h0 = copysign(h0, r.tout - r.tcur);
+  r.h = h0;
+  for (int i = 0; i < N; ++i) r.yh[i + N] = h0 * r.yh[i + N];
+  r.first = 1;
+  r.mguard = 0;
+  r.pc = ST_MAIN;
+}
+
+// DVODE after a DVSTEP return with flag kflag.
+template <int N>
+HD void rc_step_return(Rc<N>& r, int kflag) {
+  if (kflag != 0) {
+    for (int i = 0; i < N; ++i) r.y[i] = r.yh[i];
+    r.tcur = r.tn;
+    r.nsteps += r.nst;
+    rc_after_dvode(r, kflag == -1 ? -4 : -5);
+    return;
   }
-  for (int guard = 0; guard < 64; ++guard) {
-    if (rescale) {
-      double r = 1.0;
-      for (int j = 2; j <= d.l; ++j) {
-        r = r * d.eta;
-        for (int i = 0; i < N; ++i) d.yh[i + (j - 1) * N] = r * d.yh[i + (j - 1) * N];
-      }
-      d.h = d.hscal * d.eta;
-      d.hscal = d.h;
-      d.rc = d.rc * d.eta;
-      d.nqnyh = d.nq * N;
+  if ((r.tn - r.tout) * r.h < 0.0) {
+    r.mguard = r.mguard + 1;
+    r.pc = ST_MAIN;
+    return;
+  }
+  // DVINDY (K = 0)
+  const double s = (r.tout - r.tn) / r.h;
+  for (int i = 0; i < N; ++i) r.y[i] = r.yh[i + (r.l - 1) * N];
+  for (int jb = 1; jb <= r.nq; ++jb) {
+    const int j = r.nq - jb;
+    for (int i = 0; i < N; ++i) r.y[i] = r.yh[i + j * N] + s * r.y[i];
+  }
+  r.tcur = r.tout;
+  r.nsteps += r.nst;
+  rc_after_dvode(r, 2);
+}
+
+// DVNLSD's exit: sets the flag and continues DVSTEP.  Returns true when
+// DVSTEP needs FUN (the order-1 restart after repeated error-test failures).
+template <int N>
+HD bool rc_nls_return(Rc<N>& r, int ret) {
+  r.nflag = ret;
+  if (r.nflag != 0) {
+    r.ncf = r.ncf + 1;
+    r.etamax = 1.0;
+    r.tn = r.told;
+    for (int jb = 1; jb <= r.nq; ++jb)
+      for (int i = r.nqnyh - jb * N; i < r.nqnyh; ++i) r.yh[i] = r.yh[i] - r.yh[i + N];
+    if (r.ncf == 10) { r.kflag = -2; r.jstart = 1; rc_step_return(r, r.kflag); return false; }
+    r.eta = 0.25;
+    r.nflag = -1;
+    r.sguard = r.sguard + 1;
+    r.pc = ST_STEP_LOOP;
+    return false;
+  }
+  const double dsm = r.acnrm / r.tq[1];
+  if (dsm <= 1.0) {
+    r.kflag = 0;
+    r.nst = r.nst + 1;
+    r.hu = r.h;
+    for (int iback = 1; iback <= r.nq; ++iback) {
+      const int i = r.l - iback;
+      r.tau[i] = r.tau[i - 1];
     }
-    rescale = true;
-    d.tn = d.tn + d.h;
-    for (int jb = 1; jb <= d.nq; ++jb)
-      for (int i = d.nqnyh - jb * N; i < d.nqnyh; ++i) d.yh[i] = d.yh[i] + d.yh[i + N];
-    dvset<N>(d);
-    d.rl1 = 1.0 / d.el[1];
-    d.rc = d.rc * (d.rl1 / d.prl1);
-    d.prl1 = d.rl1;
-    nflag = dvnlsd<N>(d, y, ftem, nflag);
-    if (nflag != 0) {
-      ncf = ncf + 1;
-      d.etamax = 1.0;
-      d.tn = told;
-      for (int jb = 1; jb <= d.nq; ++jb)
-        for (int i = d.nqnyh - jb * N; i < d.nqnyh; ++i) d.yh[i] = d.yh[i] - d.yh[i + N];
-      if (ncf == 10) { d.kflag = -2; d.jstart = 1; return d.kflag; }
-      d.eta = 0.25;
-      nflag = -1;
-      continue;
+    r.tau[0] = r.h;
+    for (int j = 1; j <= r.l; ++j) {
+      const double a = r.el[j - 1];
+      if (a != 0.0)
+        for (int i = 0; i < N; ++i) r.yh[i + (j - 1) * N] = r.yh[i + (j - 1) * N] + a * r.acor[i];
     }
-    const double dsm = d.acnrm / d.tq[1];
-    if (dsm <= 1.0) {
-      d.kflag = 0;
-      d.nst = d.nst + 1;
-      d.hu = d.h;
-      for (int iback = 1; iback <= d.nq; ++iback) {
-        const int i = d.l - iback;
-        d.tau[i] = d.tau[i - 1];
-      }
-      d.tau[0] = d.h;
-      for (int j = 1; j <= d.l; ++j) {
-        const double a = d.el[j - 1];
-        if (a != 0.0)
-          for (int i = 0; i < N; ++i) d.yh[i + (j - 1) * N] = d.yh[i + (j - 1) * N] + a * d.acor[i];
-      }
-      d.nqwait = d.nqwait - 1;
-      if (!(d.l == d.lmax || d.nqwait != 1)) {
-        for (int i = 0; i < N; ++i) d.yh[i + (d.lmax - 1) * N] = d.acor[i];
-        d.conp = d.tq[4];
-      }
-      if (d.etamax != 1.0) {
-        const double flotl = double(d.l);
-        d.etaq = 1.0 / (pow(6.0 * dsm, 1.0 / flotl) + 1.0e-6);
-        if (d.nqwait != 0) {
-          d.eta = d.etaq;
-          d.newq = d.nq;
-        } else {
-          d.nqwait = 2;
-          d.etaqm1 = 0.0;
-          if (d.nq != 1) {
-            double col[N];
-            for (int i = 0; i < N; ++i) col[i] = d.yh[i + (d.l - 1) * N];
-            const double ddn = dvnorm<N>(col, d.ewt) / d.tq[0];
-            d.etaqm1 = 1.0 / (pow(6.0 * ddn, 1.0 / (flotl - 1.0)) + 1.0e-6);
-          }
-          double etaqp1 = 0.0;
-          if (d.l != d.lmax) {
-            const double cnquot = (d.tq[4] / d.conp) * powi(d.h / d.tau[1], d.l);
-            for (int i = 0; i < N; ++i) d.savf[i] = d.acor[i] - cnquot * d.yh[i + (d.lmax - 1) * N];
-            const double dup = dvnorm<N>(d.savf, d.ewt) / d.tq[2];
-            etaqp1 = 1.0 / (pow(10.0 * dup, 1.0 / (flotl + 1.0)) + 1.0e-6);
-          }
-          if (d.etaq >= etaqp1) {
-            if (d.etaq < d.etaqm1) { d.eta = d.etaqm1; d.newq = d.nq - 1; }
-            else { d.eta = d.etaq; d.newq = d.nq; }
-          } else if (etaqp1 > d.etaqm1) {
-            d.eta = etaqp1;
-            d.newq = d.nq + 1;
-            for (int i = 0; i < N; ++i) d.yh[i + (d.lmax - 1) * N] = d.acor[i];
-          } else { d.eta = d.etaqm1; d.newq = d.nq - 1; }
-        }
-        if (d.eta < 1.5 || d.etamax == 1.0) { d.newq = d.nq; d.newh = 0; d.eta = 1.0; d.hnew = d.h; }
-        else { d.eta = fmin(d.eta, d.etamax); d.newh = 1; d.hnew = d.h * d.eta; }
+    r.nqwait = r.nqwait - 1;
+    if (!(r.l == r.lmax || r.nqwait != 1)) {
+      for (int i = 0; i < N; ++i) r.yh[i + (r.lmax - 1) * N] = r.acor[i];
+      r.conp = r.tq[4];
+    }
+    if (r.etamax != 1.0) {
+      const double flotl = double(r.l);
+      r.etaq = 1.0 / (pow(6.0 * dsm, 1.0 / flotl) + 1.0e-6);
+      if (r.nqwait != 0) {
+        r.eta = r.etaq;
+        r.newq = r.nq;
       } else {
-        if (d.nqwait < 2) d.nqwait = 2;
-        d.newq = d.nq; d.newh = 0; d.eta = 1.0; d.hnew = d.h;
+        r.nqwait = 2;
+        r.etaqm1 = 0.0;
+        if (r.nq != 1) {
+          double col[N];
+          for (int i = 0; i < N; ++i) col[i] = r.yh[i + (r.l - 1) * N];
+          const double ddn = dvnorm<N>(col, r.ewt) / r.tq[0];
+          r.etaqm1 = 1.0 / (pow(6.0 * ddn, 1.0 / (flotl - 1.0)) + 1.0e-6);
+        }
+        double etaqp1 = 0.0;
+        if (r.l != r.lmax) {
+          const double cnquot = (r.tq[4] / r.conp) * powi(r.h / r.tau[1], r.l);
+          for (int i = 0; i < N; ++i) r.savf[i] = r.acor[i] - cnquot * r.yh[i + (r.lmax - 1) * N];
+          const double dup = dvnorm<N>(r.savf, r.ewt) / r.tq[2];
+          etaqp1 = 1.0 / (pow(10.0 * dup, 1.0 / (flotl + 1.0)) + 1.0e-6);
+        }
+        if (r.etaq >= etaqp1) {
+          if (r.etaq < r.etaqm1) { r.eta = r.etaqm1; r.newq = r.nq - 1; }
+          else { r.eta = r.etaq; r.newq = r.nq; }
+        } else if (etaqp1 > r.etaqm1) {
+          r.eta = etaqp1;
+          r.newq = r.nq + 1;
+          for (int i = 0; i < N; ++i) r.yh[i + (r.lmax - 1) * N] = r.acor[i];
+        } else { r.eta = r.etaqm1; r.newq = r.nq - 1; }
       }
-      d.etamax = 10.0;   // ETAMX2 = ETAMX3 = 10
-      const double r = 1.0 / d.tq[1];
-      for (int i = 0; i < N; ++i) d.acor[i] = r * d.acor[i];
-      d.jstart = 1;
-      return 0;
-    }
-    // error test failed
-    d.kflag = d.kflag - 1;
-    nflag = -2;
-    d.tn = told;
-    for (int jb = 1; jb <= d.nq; ++jb)
-      for (int i = d.nqnyh - jb * N; i < d.nqnyh; ++i) d.yh[i] = d.yh[i] - d.yh[i + N];
-    d.etamax = 1.0;
-    if (d.kflag > -3) {
-      d.eta = 1.0 / (pow(6.0 * dsm, 1.0 / double(d.l)) + 1.0e-6);
-      d.eta = fmax(d.eta, 0.1);
-      if (d.kflag <= -2 && d.eta > 0.2) d.eta = 0.2;
-      continue;
-    }
-    if (d.kflag == -7) { d.kflag = -1; d.jstart = 1; return d.kflag; }
-    if (d.nq != 1) {
-      d.eta = 0.1;
-      dvjust<N>(d, -1);
-      d.l = d.nq;
-      d.nq = d.nq - 1;
-      d.nqwait = d.l;
-      continue;
-    }
-    d.eta = 0.1;
-    d.h = d.h * d.eta;
-    d.hscal = d.h;
-    d.tau[0] = d.h;
-    ck_fun<N - 1>(d.rho, y, d.savf);
-    for (int i = 0; i < N; ++i) d.yh[i + N] = d.h * d.savf[i];
-    d.nqwait = 10;
-    rescale = false;
-  }
-  d.kflag = -2;
-  d.jstart = 1;
-  return d.kflag;
-}
-
-// DVODE (ISTATE = 1 fresh start, ITASK = 1): returns ISTATE
-template <int N>
-HD int dvode(Dv<N>& d, double* y, double* t, double tout, int* nst_total) {
-  double ftem[N];
-  if (tout == *t) return 1;
-  d.tn = *t;
-  d.jstart = 0;
-  d.nslj = 0;
-  d.nst = 0;
-  d.hu = 0.0;
-  d.icf = 0;
-  d.ipup = 0;
-  d.jcur = 0;
-  d.newh = 0;
-  d.newq = 1;
-  d.conp = 0.0;
-  d.crate = 0.0;
-  d.drc = 0.0;
-  d.acnrm = 0.0;
-  d.nslp = 0;
-  ck_fun<N - 1>(d.rho, y, d.yh + N);
-  for (int i = 0; i < N; ++i) d.yh[i] = y[i];
-  d.nq = 1;
-  d.h = 1.0;
-  for (int i = 0; i < N; ++i) d.ewt[i] = 1.0 / (kRtol * fabs(d.yh[i]) + kAtol);
-  // DVHIN
-  double h0;
-  {
-    const double tdist = fabs(tout - *t);
-    const double tround = kUround * fmax(fabs(*t), fabs(tout));
-    if (tdist < 2.0 * tround) return -3;
-    const double hlb = 100.0 * tround;
-    double hub = 0.1 * tdist;
-    for (int i = 0; i < N; ++i) {
-      const double delyi = 0.1 * fabs(d.yh[i]) + kAtol;
-      const double afi = fabs(d.yh[i + N]);
-      if (afi * hub > delyi) hub = delyi / afi;
-    }
-    double hg = sqrt(hlb * hub), hnew = hg;
-    if (hub < hlb) {
-      h0 = hg;
+      if (r.eta < 1.5 || r.etamax == 1.0) { r.newq = r.nq; r.newh = 0; r.eta = 1.0; r.hnew = r.h; }
+      else { r.eta = fmin(r.eta, r.etamax); r.newh = 1; r.hnew = r.h * r.eta; }
     } else {
-      int iter = 0;
-      while (true) {
-        for (int i = 0; i < N; ++i) y[i] = d.yh[i] + hg * d.yh[i + N];
-        ck_fun<N - 1>(d.rho, y, ftem);
-        for (int i = 0; i < N; ++i) ftem[i] = (ftem[i] - d.yh[i + N]) / hg;
-        const double yddnrm = dvnorm<N>(ftem, d.ewt);
-        hnew = (yddnrm * hub * hub > 2.0) ? sqrt(2.0 / yddnrm) : sqrt(hg * hub);
-        iter = iter + 1;
-        if (iter >= 4) break;
-        const double hrat = hnew / hg;
-        if (hrat > 0.5 && hrat < 2.0) break;
-        if (iter >= 2 && hnew > 2.0 * hg) { hnew = hg; break; }
-        hg = hnew;
-      }
-      h0 = hnew * 0.5;
-      if (h0 < hlb) h0 = hlb;
-      if (h0 > hub) h0 = hub;
+      if (r.nqwait < 2) r.nqwait = 2;
+      r.newq = r.nq; r.newh = 0; r.eta = 1.0; r.hnew = r.h;
     }
-    h0 = copysign(h0, tout - *t);
+    r.etamax = 10.0;   // ETAMX2 = ETAMX3 = 10
+    const double rr = 1.0 / r.tq[1];
+    for (int i = 0; i < N; ++i) r.acor[i] = rr * r.acor[i];
+    r.jstart = 1;
+    rc_step_return(r, 0);
+    return false;
   }
-  d.h = h0;
-  for (int i = 0; i < N; ++i) d.yh[i + N] = h0 * d.yh[i + N];
-  bool first = true;
-  for (int guard = 0; guard < 600; ++guard) {
-    if (!first) {
-      if (d.nst >= 500) {
-        for (int i = 0; i < N; ++i) y[i] = d.yh[i];
-        *t = d.tn;
-        *nst_total += d.nst;
-        return -1;
-      }
-      for (int i = 0; i < N; ++i) d.ewt[i] = 1.0 / (kRtol * fabs(d.yh[i]) + kAtol);
-    }
-    first = false;
-    if (kUround * dvnorm<N>(d.yh, d.ewt) > 1.0) {
-      for (int i = 0; i < N; ++i) y[i] = d.yh[i];
-      *t = d.tn;
-      *nst_total += d.nst;
-      return -2;
-    }
-    const int kflag = dvstep<N>(d, y, ftem);
-    if (kflag != 0) {
-      for (int i = 0; i < N; ++i) y[i] = d.yh[i];
-      *t = d.tn;
-      *nst_total += d.nst;
-      return kflag == -1 ? -4 : -5;
-    }
-    if ((d.tn - tout) * d.h < 0.0) continue;
-    // DVINDY (K = 0)
-    const double s = (tout - d.tn) / d.h;
-    for (int i = 0; i < N; ++i) y[i] = d.yh[i + (d.l - 1) * N];
-    for (int jb = 1; jb <= d.nq; ++jb) {
-      const int j = d.nq - jb;
-      for (int i = 0; i < N; ++i) y[i] = d.yh[i + j * N] + s * y[i];
-    }
-    *t = tout;
-    *nst_total += d.nst;
-    return 2;
+  // error test failed
+  r.kflag = r.kflag - 1;
+  r.nflag = -2;
+  r.tn = r.told;
+  for (int jb = 1; jb <= r.nq; ++jb)
+    for (int i = r.nqnyh - jb * N; i < r.nqnyh; ++i) r.yh[i] = r.yh[i] - r.yh[i + N];
+  r.etamax = 1.0;
+  if (r.kflag > -3) {
+    r.eta = 1.0 / (pow(6.0 * dsm, 1.0 / double(r.l)) + 1.0e-6);
+    r.eta = fmax(r.eta, 0.1);
+    if (r.kflag <= -2 && r.eta > 0.2) r.eta = 0.2;
+    r.sguard = r.sguard + 1;
+    r.pc = ST_STEP_LOOP;
+    return false;
   }
-  *nst_total += d.nst;
-  return -1;
+  if (r.kflag == -7) { r.kflag = -1; r.jstart = 1; rc_step_return(r, r.kflag); return false; }
+  if (r.nq != 1) {
+    r.eta = 0.1;
+    dvjust<N>(r, -1);
+    r.l = r.nq;
+    r.nq = r.nq - 1;
+    r.nqwait = r.l;
+    r.sguard = r.sguard + 1;
+    r.pc = ST_STEP_LOOP;
+    return false;
+  }
+  r.eta = 0.1;
+  r.h = r.h * r.eta;
+  r.hscal = r.h;
+  r.tau[0] = r.h;
+  r.pc = ST_ERRF_F;
+  return true;
 }
 
-// REACTION_V: up to 20 fresh DVODE starts
+// Second half of DVJAC (iteration matrix and LU) and its return into DVNLSD.
+// Returns true when the Newton iteration starts (ST_NLS_ITER), false when
+// DVNLSD returned (state already advanced).
+template <int N>
+HD void rc_jac_lu(Rc<N>& r) {
+  const double con = -(r.h * r.rl1);
+  for (int q = 0; q < N * N; ++q) r.wm[q] = con * r.wmjs[q];
+  for (int i = 0; i < N; ++i) r.wm[i + i * N] = r.wm[i + i * N] + 1.0;
+  const int ierpj = dgefa<N>(r.wm, r.ipvt) != 0 ? 1 : 0;
+  r.ipup = 0;
+  r.rc = 1.0;
+  r.drc = 0.0;
+  r.crate = 1.0;
+  r.nslp = r.nst;
+  if (ierpj != 0) {
+    r.icf = 2;
+    r.ipup = 2;
+    if (rc_nls_return(r, -1)) return;   // pc already ST_ERRF_F
+    return;
+  }
+  for (int i = 0; i < N; ++i) r.acor[i] = 0.0;
+  r.it = 0;
+  r.pc = ST_NLS_ITER;
+}
+
+// Runs the method until FUN(y) is needed (returns true; the result goes to
+// fo) or the cell is finished (returns false; pc == ST_DONE, y holds the
+// final state, istate and nsteps are REACTION_V's).
+template <int N>
+HD bool rc_advance(Rc<N>& r) {
+  for (int guard = 0; guard < 512; ++guard) {
+    switch (r.pc) {
+      case ST_DVODE: {   // DVODE entry (ISTATE = 1, ITASK = 1)
+        if (r.tout == r.tcur) { rc_after_dvode(r, 1); break; }
+        r.tn = r.tcur;
+        r.jstart = 0; r.nslj = 0; r.nst = 0; r.hu = 0.0; r.icf = 0; r.ipup = 0; r.jcur = 0; r.newh = 0;
+        r.newq = 1; r.conp = 0.0; r.crate = 0.0; r.drc = 0.0; r.acnrm = 0.0; r.nslp = 0;
+        r.pc = ST_F0;
+        return true;
+      }
+      case ST_F0: {
+        for (int i = 0; i < N; ++i) r.yh[i + N] = r.fo[i];
+        for (int i = 0; i < N; ++i) r.yh[i] = r.y[i];
+        r.nq = 1;
+        r.h = 1.0;
+        for (int i = 0; i < N; ++i) r.ewt[i] = 1.0 / (kRtol * fabs(r.yh[i]) + kAtol);
+        // DVHIN
+        const double tdist = fabs(r.tout - r.tcur);
+        const double tround = kUround * fmax(fabs(r.tcur), fabs(r.tout));
+        if (tdist < 2.0 * tround) { rc_after_dvode(r, -3); break; }
+        r.hlb = 100.0 * tround;
+        r.hub = 0.1 * tdist;
+        for (int i = 0; i < N; ++i) {
+          const double delyi = 0.1 * fabs(r.yh[i]) + kAtol;
+          const double afi = fabs(r.yh[i + N]);
+          if (afi * r.hub > delyi) r.hub = delyi / afi;
+        }
+        r.hg = sqrt(r.hlb * r.hub);
+        r.hnew = r.hg;
+        if (r.hub < r.hlb) { rc_hin_finish(r, r.hg); break; }
+        r.iter = 0;
+        r.pc = ST_HIN_ITER;
+        break;
+      }
+      case ST_HIN_ITER: {
+        for (int i = 0; i < N; ++i) r.y[i] = r.yh[i] + r.hg * r.yh[i + N];
+        r.pc = ST_HIN_F;
+        return true;
+      }
+      case ST_HIN_F: {
+        double ft[N];
+        for (int i = 0; i < N; ++i) ft[i] = (r.fo[i] - r.yh[i + N]) / r.hg;
+        const double yddnrm = dvnorm<N>(ft, r.ewt);
+        r.hnew = (yddnrm * r.hub * r.hub > 2.0) ? sqrt(2.0 / yddnrm) : sqrt(r.hg * r.hub);
+        r.iter = r.iter + 1;
+        bool done = r.iter >= 4;
+        if (!done) {
+          const double hrat = r.hnew / r.hg;
+          if (hrat > 0.5 && hrat < 2.0) done = true;
+          else if (r.iter >= 2 && r.hnew > 2.0 * r.hg) { r.hnew = r.hg; done = true; }
+        }
+        if (!done) { r.hg = r.hnew; r.pc = ST_HIN_ITER; break; }
+        double h0 = r.hnew * 0.5;
+        if (h0 < r.hlb) h0 = r.hlb;
+        if (h0 > r.hub) h0 = r.hub;
+        rc_hin_finish(r, h0);
+        break;
+      }
+      case ST_MAIN: {   // one pass of DVODE's step loop (at most 600)
+        if (r.mguard >= 600) { r.nsteps += r.nst; rc_after_dvode(r, -1); break; }
+        if (!r.first) {
+          if (r.nst >= 500) {
+            for (int i = 0; i < N; ++i) r.y[i] = r.yh[i];
+            r.tcur = r.tn;
+            r.nsteps += r.nst;
+            rc_after_dvode(r, -1);
+            break;
+          }
+          for (int i = 0; i < N; ++i) r.ewt[i] = 1.0 / (kRtol * fabs(r.yh[i]) + kAtol);
+        }
+        r.first = 0;
+        if (kUround * dvnorm<N>(r.yh, r.ewt) > 1.0) {
+          for (int i = 0; i < N; ++i) r.y[i] = r.yh[i];
+          r.tcur = r.tn;
+          r.nsteps += r.nst;
+          rc_after_dvode(r, -2);
+          break;
+        }
+        r.pc = ST_STEP_BEGIN;
+        break;
+      }
+      case ST_STEP_BEGIN: {   // DVSTEP entry
+        r.kflag = 0;
+        r.told = r.tn;
+        r.ncf = 0;
+        r.nflag = 0;
+        r.jcur = 0;
+        if (r.jstart > 0) {
+          r.rescale = 0;
+          if (r.newh != 0) {
+            if (r.newq < r.nq) { dvjust<N>(r, -1); r.nq = r.newq; r.l = r.nq + 1; r.nqwait = r.l; }
+            else if (r.newq > r.nq) { dvjust<N>(r, 1); r.nq = r.newq; r.l = r.nq + 1; r.nqwait = r.l; }
+            r.rescale = 1;
+          }
+        } else {
+          r.lmax = 6;
+          r.nq = 1;
+          r.l = 2;
+          r.nqnyh = N;
+          r.tau[0] = r.h;
+          r.prl1 = 1.0;
+          r.rc = 0.0;
+          r.etamax = 1.0e4;
+          r.nqwait = 2;
+          r.hscal = r.h;
+          r.rescale = 0;
+        }
+        r.sguard = 0;
+        r.pc = ST_STEP_LOOP;
+        break;
+      }
+      case ST_STEP_LOOP: {   // one attempt of DVSTEP (at most 64)
+        if (r.sguard >= 64) { r.kflag = -2; r.jstart = 1; rc_step_return(r, r.kflag); break; }
+        if (r.rescale) {
+          double rr = 1.0;
+          for (int j = 2; j <= r.l; ++j) {
+            rr = rr * r.eta;
+            for (int i = 0; i < N; ++i) r.yh[i + (j - 1) * N] = rr * r.yh[i + (j - 1) * N];
+          }
+          r.h = r.hscal * r.eta;
+          r.hscal = r.h;
+          r.rc = r.rc * r.eta;
+          r.nqnyh = r.nq * N;
+        }
+        r.rescale = 1;
+        r.tn = r.tn + r.h;
+        for (int jb = 1; jb <= r.nq; ++jb)
+          for (int i = r.nqnyh - jb * N; i < r.nqnyh; ++i) r.yh[i] = r.yh[i] + r.yh[i + N];
+        dvset<N>(r);
+        r.rl1 = 1.0 / r.el[1];
+        r.rc = r.rc * (r.rl1 / r.prl1);
+        r.prl1 = r.rl1;
+        // DVNLSD entry
+        if (r.jstart == 0) r.nslp = 0;
+        if (r.nflag == 0) r.icf = 0;
+        if (r.nflag == -2) r.ipup = 2;
+        if (r.jstart == 0) r.ipup = 2;
+        r.drc = fabs(r.rc - 1.0);
+        if (r.drc > 0.3 || r.nst >= r.nslp + 20) r.ipup = 2;
+        r.pass = 0;
+        r.pc = ST_NLS_PASS;
+        break;
+      }
+      case ST_NLS_PASS: {
+        if (r.pass >= 2) {
+          r.icf = 2;
+          r.ipup = 2;
+          if (rc_nls_return(r, -1)) return true;
+          break;
+        }
+        r.m = 0;
+        r.delp = 0.0;
+        for (int i = 0; i < N; ++i) r.y[i] = r.yh[i];
+        r.pc = ST_NLS_PRED_F;
+        return true;
+      }
+      case ST_NLS_PRED_F: {
+        for (int i = 0; i < N; ++i) r.savf[i] = r.fo[i];
+        if (r.ipup > 0) {   // DVJAC
+          int jok = 1;
+          if (r.nst == 0 || r.nst > r.nslj + 50) jok = -1;
+          if (r.icf == 1 && r.drc < 0.2) jok = -1;
+          if (r.icf == 2) jok = -1;
+          if (jok == -1) {
+            r.nslj = r.nst;
+            r.jcur = 1;
+            const double fac = dvnorm<N>(r.savf, r.ewt);
+            r.r0 = 1000.0 * fabs(r.h) * kUround * double(N) * fac;
+            if (r.r0 == 0.0) r.r0 = 1.0;
+            r.jcol = 0;
+            r.pc = ST_JAC_COL;
+            break;
+          }
+          r.jcur = 0;
+          rc_jac_lu(r);
+          if (r.pc == ST_ERRF_F) return true;
+          break;
+        }
+        for (int i = 0; i < N; ++i) r.acor[i] = 0.0;
+        r.it = 0;
+        r.pc = ST_NLS_ITER;
+        break;
+      }
+      case ST_JAC_COL: {
+        if (r.jcol >= N) {
+          rc_jac_lu(r);
+          if (r.pc == ST_ERRF_F) return true;
+          break;
+        }
+        const double srur = 1.4901161193847656e-08;   // sqrt(UROUND)
+        const int j = r.jcol;
+        r.yj = r.y[j];
+        const double rj = fmax(srur * fabs(r.yj), r.r0 / r.ewt[j]);
+        r.y[j] = r.y[j] + rj;
+        r.rfac = 1.0 / rj;
+        r.pc = ST_JAC_COL_F;
+        return true;
+      }
+      case ST_JAC_COL_F: {
+        const int j = r.jcol;
+        for (int i = 0; i < N; ++i) r.wmjs[i + j * N] = (r.fo[i] - r.savf[i]) * r.rfac;
+        r.y[j] = r.yj;
+        r.jcol = j + 1;
+        r.pc = ST_JAC_COL;
+        break;
+      }
+      case ST_NLS_ITER: {   // corrector iteration (at most 3)
+        bool fail = r.it >= 3;
+        if (!fail) {
+          for (int i = 0; i < N; ++i) r.y[i] = (r.rl1 * r.h) * r.savf[i] - (r.rl1 * r.yh[i + N] + r.acor[i]);
+          dgesl<N>(r.wm, r.ipvt, r.y);
+          if (r.rc != 1.0) {
+            const double cscale = 2.0 / (1.0 + r.rc);
+            for (int i = 0; i < N; ++i) r.y[i] = cscale * r.y[i];
+          }
+          const double del = dvnorm<N>(r.y, r.ewt);
+          for (int i = 0; i < N; ++i) r.acor[i] = r.acor[i] + r.y[i];
+          for (int i = 0; i < N; ++i) r.y[i] = r.yh[i] + r.acor[i];
+          if (r.m != 0) r.crate = fmax(0.3 * r.crate, del / r.delp);
+          const double dcon = del * fmin(1.0, r.crate) / r.tq[3];
+          if (dcon <= 1.0) {
+            r.jcur = 0;
+            r.icf = 0;
+            r.acnrm = (r.m == 0) ? del : dvnorm<N>(r.acor, r.ewt);
+            if (rc_nls_return(r, 0)) return true;
+            break;
+          }
+          r.m = r.m + 1;
+          if (r.m == 3 || (r.m >= 2 && del > 2.0 * r.delp)) {
+            fail = true;
+          } else {
+            r.delp = del;
+            r.pc = ST_NLS_CORR_F;
+            return true;
+          }
+        }
+        // corrector failed on this pass
+        if (r.jcur == 1) {
+          r.icf = 2;
+          r.ipup = 2;
+          if (rc_nls_return(r, -1)) return true;
+          break;
+        }
+        r.icf = 1;
+        r.ipup = 2;
+        r.pass = r.pass + 1;
+        r.pc = ST_NLS_PASS;
+        break;
+      }
+      case ST_NLS_CORR_F: {
+        for (int i = 0; i < N; ++i) r.savf[i] = r.fo[i];
+        r.it = r.it + 1;
+        r.pc = ST_NLS_ITER;
+        break;
+      }
+      case ST_ERRF_F: {
+        for (int i = 0; i < N; ++i) r.savf[i] = r.fo[i];
+        for (int i = 0; i < N; ++i) r.yh[i + N] = r.h * r.savf[i];
+        r.nqwait = 10;
+        r.rescale = 0;
+        r.sguard = r.sguard + 1;
+        r.pc = ST_STEP_LOOP;
+        break;
+      }
+      default:
+        return false;   // ST_DONE
+    }
+  }
+  // no path of the method takes this many transitions without a FUN request
+  r.istate = -99;
+  r.pc = ST_DONE;
+  return false;
+}
+
+// One cell from start to finish on the calling thread (host checks, and any
+// caller that does not batch FUN evaluations across threads).
 template <int N>
 HD int reaction_v(double rho, double* z, double tf, int* nsteps) {
-  Dv<N> d;
-  d.rho = rho;
-  double ti = 0.0;
-  int istate = 1;
-  *nsteps = 0;
-  for (int ib = 0; ib < 20 && istate != 2; ++ib) istate = dvode<N>(d, z, &ti, tf, nsteps);
-  return istate;
+  Rc<N> r;
+  rc_start<N>(r, rho, z, tf);
+  while (rc_advance<N>(r)) ck_fun<N - 1>(r.rho, r.y, r.fo);
+  for (int i = 0; i < N; ++i) z[i] = r.y[i];
+  *nsteps = r.nsteps;
+  return r.istate;
 }
 
 // ---------------------------------------------------------------- kernels ---
+// Persistent driver shared by the chemistry kernels: each thread takes cells
+// from *counter until all n are taken.  Per round, a thread either finishes
+// its cell (store) or advances it to its next right-hand-side request; the
+// requests of all threads are then evaluated in one converged FUN call.
+// The loop ends: every cell's integration is bounded by DVODE's own limits
+// (20 restarts, 600 steps, 64 attempts per step, 2 corrector passes), and
+// kMaxFun caps the FUN rounds of one cell above that bound.
+constexpr long long kMaxFun = 1LL << 25;
+
+template <int KK, class Load, class Store>
+__device__ __forceinline__ void rc_drive(unsigned n, unsigned* counter, Load load, Store store) {
+  constexpr int N = KK + 1;
+  Rc<N> r;
+  unsigned q = 0;
+  bool active = false;
+  long long nfun = 0;
+  while (true) {
+    if (!active) {
+      q = atomicAdd(counter, 1u);
+      if (q >= n) return;
+      double rho, tf, z[N];
+      load(q, rho, z, tf);
+      rc_start<N>(r, rho, z, tf);
+      active = true;
+      nfun = 0;
+    }
+    bool need = rc_advance<N>(r);
+    if (need && ++nfun > kMaxFun) { r.istate = -99; need = false; }
+    if (need) {
+      ck_fun<KK>(r.rho, r.y, r.fo);
+    } else {
+      store(q, r);
+      active = false;
+    }
+  }
+}
+
+template <int KK>
+__device__ __forceinline__ void chem_stats_add(ChemStats* stats, int istate, int nst) {
+  if (istate <= -2) atomicAdd(&stats->failed, 1);
+  atomicMax(&stats->max_steps, nst);
+  atomicAdd(&stats->total_steps, (unsigned long long)nst);
+}
+
 template <int KK>
 __global__ void __launch_bounds__(128) k_psr_field(ChemField f, unsigned* counter, ChemStats* stats) {
   constexpr int N = KK + 1;
   const long long ncell = (long long)f.wx * f.wy * f.wz;
-  while (true) {
-    const long long q = atomicAdd(counter, 1u);
-    if (q >= ncell) break;
+  const long long nc = f.ncell;
+  auto point = [&](unsigned q) {
     const int i = f.ix + (int)(q % f.wx);
     const long long r = q / f.wx;
     const int j = f.iy + (int)(r % f.wy);
     const int k = f.iz + (int)(r / f.wy);
-    const long long p = (long long)(i - 1 + f.ng) + (long long)f.gx * ((long long)(j - 1 + f.ng) + (long long)f.gy * (long long)(k - 1 + f.ng));
-    const long long nc = f.ncell;
+    return (long long)(i - 1 + f.ng) +
+           (long long)f.gx * ((long long)(j - 1 + f.ng) + (long long)f.gy * (long long)(k - 1 + f.ng));
+  };
+  auto load = [&](unsigned q, double& rho, double* z, double& tf) {
+    const long long p = point(q);
     const double rho0 = f.v[p];
     const double rho_i = 1.0 / rho0;
-    double z[N];
 #pragma unroll
     for (int l = 0; l < KK; ++l) z[1 + l] = f.v[(5 + l) * nc + p] * rho_i;
+    z[0] = f.T[p] * f.t_ref;
+    rho = rho0 * f.rho_cgs;
+    tf = f.dt_phys;
+  };
+  auto store = [&](unsigned q, const Rc<N>& r) {
+    const long long p = point(q);
+    const double rho0 = f.v[p];
     const double T0 = f.T[p] * f.t_ref;
-    z[0] = T0;
-    int nst = 0;
-    const int istate = reaction_v<N>(rho0 * f.rho_cgs, z, f.dt_phys, &nst);
-    if (istate <= -2) atomicAdd(&stats->failed, 1);
-    atomicMax(&stats->max_steps, nst);
-    atomicAdd(&stats->total_steps, (unsigned long long)nst);
-    f.T[p] = z[0] * f.tref_i;
-    const double dT = fabs(z[0] - T0);
+    chem_stats_add<KK>(stats, r.istate, r.nsteps);
+    f.T[p] = r.y[0] * f.tref_i;
+    const double dT = fabs(r.y[0] - T0);
     atomicMax(&stats->dtmax_bits, (unsigned long long)__double_as_longlong(dT));
     double sumY = 0.0;
 #pragma unroll
     for (int l = 0; l < KK - 1; ++l) {
-      const double Ya = fmin(fmax(z[1 + l], 0.0), 1.0);
+      const double Ya = fmin(fmax(r.y[1 + l], 0.0), 1.0);
       f.v[(5 + l) * nc + p] = rho0 * Ya;
       sumY = sumY + Ya;
     }
     f.v[(5 + KK - 1) * nc + p] = rho0 * (1.0 - sumY);
-    if (f.dT_out) f.dT_out[q] = z[0] - T0;
-  }
+    if (f.dT_out) f.dT_out[q] = r.y[0] - T0;
+  };
+  rc_drive<KK>((unsigned)ncell, counter, load, store);
 }
 
 template <int KK>
 __global__ void __launch_bounds__(128) k_psr_batch(int n, double* T, const double* rho, double* Y, const double* dt,
                                                    int* istate, int* nsteps, unsigned* counter, ChemStats* stats) {
   constexpr int N = KK + 1;
-  while (true) {
-    const unsigned q = atomicAdd(counter, 1u);
-    if (q >= (unsigned)n) break;
-    double z[N];
+  auto load = [&](unsigned q, double& rh, double* z, double& tf) {
     z[0] = T[q];
 #pragma unroll
     for (int l = 0; l < KK; ++l) z[1 + l] = Y[(size_t)q * KK + l];
-    int nst = 0;
-    const int is = reaction_v<N>(rho[q], z, dt[q], &nst);
-    if (is <= -2) atomicAdd(&stats->failed, 1);
-    atomicMax(&stats->max_steps, nst);
-    atomicAdd(&stats->total_steps, (unsigned long long)nst);
-    T[q] = z[0];
+    rh = rho[q];
+    tf = dt[q];
+  };
+  auto store = [&](unsigned q, const Rc<N>& r) {
+    chem_stats_add<KK>(stats, r.istate, r.nsteps);
+    T[q] = r.y[0];
 #pragma unroll
-    for (int l = 0; l < KK; ++l) Y[(size_t)q * KK + l] = z[1 + l];
-    if (istate) istate[q] = is;
-    if (nsteps) nsteps[q] = nst;
-  }
+    for (int l = 0; l < KK; ++l) Y[(size_t)q * KK + l] = r.y[1 + l];
+    if (istate) istate[q] = r.istate;
+    if (nsteps) nsteps[q] = r.nsteps;
+  };
+  rc_drive<KK>((unsigned)n, counter, load, store);
 }
 
 // ------------------------------------------------ surrogate support --------
@@ -877,24 +1092,22 @@ template <int KK>
 __global__ void __launch_bounds__(128) k_psr_list(const int* list, const unsigned* count, double* T, const double* rho,
                                                   double* Y, const double* dt, unsigned* counter, ChemStats* stats) {
   constexpr int N = KK + 1;
-  const unsigned n = *count;
-  while (true) {
-    const unsigned w = atomicAdd(counter, 1u);
-    if (w >= n) break;
+  auto load = [&](unsigned w, double& rh, double* z, double& tf) {
     const int q = list[w];
-    double z[N];
     z[0] = T[q];
 #pragma unroll
     for (int l = 0; l < KK; ++l) z[1 + l] = Y[(size_t)q * KK + l];
-    int nst = 0;
-    const int is = reaction_v<N>(rho[q], z, dt[q], &nst);
-    if (is <= -2) atomicAdd(&stats->failed, 1);
-    atomicMax(&stats->max_steps, nst);
-    atomicAdd(&stats->total_steps, (unsigned long long)nst);
-    T[q] = z[0];
+    rh = rho[q];
+    tf = dt[q];
+  };
+  auto store = [&](unsigned w, const Rc<N>& r) {
+    const int q = list[w];
+    chem_stats_add<KK>(stats, r.istate, r.nsteps);
+    T[q] = r.y[0];
 #pragma unroll
-    for (int l = 0; l < KK; ++l) Y[(size_t)q * KK + l] = z[1 + l];
-  }
+    for (int l = 0; l < KK; ++l) Y[(size_t)q * KK + l] = r.y[1 + l];
+  };
+  rc_drive<KK>(*count, counter, load, store);
 }
 
 int chem_grid(int* blocks) {

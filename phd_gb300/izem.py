@@ -125,6 +125,25 @@ def psr_batch(mech, T, rho, Y, dt, device_ptrs=False):
     return istate, nsteps, ms.value
 
 
+def psr_batch_device(mech, n, T, rho, Y, dt, istate=None, nsteps=None):
+    """psr_batch on arrays already on the device: torch CUDA tensors (or raw
+    device addresses) T (n), rho (n), Y (n, kk) row-major, dt (n); istate and
+    nsteps (int32, n) are optional outputs.  The caller's work on these arrays
+    must be complete (the library runs on its own stream and waits for it).
+    Returns the kernel time in ms."""
+    lib = load_library()
+
+    def ptr(a):
+        return None if a is None else (a if isinstance(a, int) else a.data_ptr())
+
+    ms = C.c_float()
+    rc = lib.izem_gpu_psr_batch(C.byref(mech), n, ptr(T), ptr(rho), ptr(Y), ptr(dt), ptr(istate), ptr(nsteps), 1,
+                                C.byref(ms))
+    if rc:
+        raise IzemError(rc, "izem_gpu_psr_batch")
+    return ms.value
+
+
 class IzemGPU:
     """One device-resident block of the IZEM state (one GPU, one process)."""
 
