@@ -212,9 +212,13 @@ HD __forceinline__ double dvnorm(const double* v, const double* w) {
   return sqrt(s / double(N));
 }
 
+// LINPACK DGEFA/DGESL (vode.f:7033/7630).  The outer loops stay rolled: the
+// integrator's control code runs divergently across a warp, and unrolled it
+// is large enough to miss in the instruction cache.
 template <int N>
 HD int dgefa(double* a, int* ipvt) {
   int info = 0;
+#pragma unroll 1
   for (int k = 0; k < N - 1; ++k) {
     int l = k;
     double dmax = fabs(a[k + k * N]);
@@ -227,6 +231,7 @@ HD int dgefa(double* a, int* ipvt) {
     if (l != k) { const double t = a[l + k * N]; a[l + k * N] = a[k + k * N]; a[k + k * N] = t; }
     const double t = -1.0 / a[k + k * N];
     for (int i = k + 1; i < N; ++i) a[i + k * N] = t * a[i + k * N];
+#pragma unroll 1
     for (int j = k + 1; j < N; ++j) {
       double tj = a[l + j * N];
       if (l != k) { a[l + j * N] = a[k + j * N]; a[k + j * N] = tj; }
@@ -241,6 +246,7 @@ HD int dgefa(double* a, int* ipvt) {
 
 template <int N>
 HD void dgesl(const double* a, const int* ipvt, double* b) {
+#pragma unroll 1
   for (int k = 0; k < N - 1; ++k) {
     const int l = ipvt[k];
     const double t = b[l];
@@ -248,6 +254,7 @@ HD void dgesl(const double* a, const int* ipvt, double* b) {
     if (t != 0.0)
       for (int i = k + 1; i < N; ++i) b[i] = b[i] + t * a[i + k * N];
   }
+#pragma unroll 1
   for (int k = N - 1; k >= 0; --k) {
     b[k] = b[k] / a[k + k * N];
     const double t = -b[k];
@@ -565,6 +572,7 @@ HD bool rc_nls_return(Rc<N>& r, int ret) {
 template <int N>
 HD void rc_jac_lu(Rc<N>& r) {
   const double con = -(r.h * r.rl1);
+#pragma unroll 1
   for (int q = 0; q < N * N; ++q) r.wm[q] = con * r.wmjs[q];
   for (int i = 0; i < N; ++i) r.wm[i + i * N] = r.wm[i + i * N] + 1.0;
   const int ierpj = dgefa<N>(r.wm, r.ipvt) != 0 ? 1 : 0;
