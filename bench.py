@@ -120,18 +120,18 @@ class Stepper:
     """One time step of the reference driver (izem.f90:252-283): timestep,
     then with chemistry the Strang sequence chem(dt/2), rk3(dt), chem(dt/2)."""
 
-    def __init__(self, g, chem):
-        self.g, self.chem = g, chem
+    def __init__(self, g, chem, mode=0):
+        self.g, self.chem, self.mode = g, chem, mode
         self.dtmin, self.DTmax = 1.0, 0.0
 
     def step(self):
         g = self.g
         _, dt = g.timestep(DTmax=self.DTmax, dtmin=self.dtmin)
         if self.chem:
-            g.reaction_selec(0.5 * dt)
+            g.reaction_selec(0.5 * dt, mode=self.mode)
         g.rk3(dt)
         if self.chem:
-            self.DTmax = g.reaction_selec(0.5 * dt)
+            self.DTmax = g.reaction_selec(0.5 * dt, mode=self.mode)
         self.dtmin = dt
         return dt
 
@@ -198,6 +198,7 @@ def run_gpu(args, rank, world):
               "fp64": {"achieved": flops / avg_s / 1e9, "peak": FP64_PEAK_GFLOPS, "unit": "GFLOP/s",
                        "frac": flops / avg_s / 1e9 / FP64_PEAK_GFLOPS}}
     launches = sum(n for n, _ in kt.values())
+    mlp = run_mlp_chem(args, g, stp, ncell, world) if chem and not args.no_mlp else None
     res = {
         "metric": "reacting RHS Mcell-steps/s, FP64 plain vs MLP-chem (<=1% dT err) on 1 GB300",
         "value": value, "unit": "Mcell-steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -218,8 +219,68 @@ def run_gpu(args, rank, world):
         "clocks": clk.summary(),
         "wall_s_timed": wall,
     }
+    if mlp is not None:
+        res["mlp_chem"] = mlp
     g.close()
     return res
+
+
+def run_mlp_chem(args, g, stp, ncell, world):
+    """The same reacting step with the learned chemistry (IZEM_CHEM_MLP):
+    two networks trained on the GPU on 2^19 of the flow's own window reactors
+    (half step scaled by 10**U[-0.05, 0.05], labelled by the FP64 BDF
+    integrator), gated, rejected cells by BDF.  Accuracy: one chemistry half
+    step from the same state both ways, |dT| errors over the window against
+    the largest BDF increment."""
+    from phd_gb300.mech import h2_mechanism
+    from phd_gb300.surrogate import flow_gate, flow_training_set, train_on
+    mech = h2_mechanism()
+    _, dt = g.timestep(DTmax=stp.DTmax, dtmin=stp.dtmin)
+    t0 = time.perf_counter()
+    X, Yt = flow_training_set(g, mech, 0.5 * dt, n_max=1 << 19, spread=0.05)
+    t_label = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    nets = train_on(X, Yt, epochs=30, batch=4096)
+    t_train = time.perf_counter() - t0
+    gate = flow_gate(X, Yt)
+    g.set_surrogate(nets[0], nets[1], gate=gate)
+    st0 = g.download()
+    T0 = st0["T"].copy()
+    g.set_kernel_timing(True)
+    g.kernel_times()
+    g.reaction_selec(0.5 * dt, mode=0)
+    bdf_ms = sum(v[1] for k, v in g.kernel_times().items() if k == "chem_psr")
+    dref = (g.download()["T"] - T0) * g.adi.t_ref
+    g.upload(**st0)
+    g.reaction_selec(0.5 * dt, mode=1)
+    sst = g.surrogate_stats()
+    dgot = (g.download()["T"] - T0) * g.adi.t_ref
+    g.set_kernel_timing(False)
+    g.upload(**st0)
+    err = np.abs(dgot - dref)
+    scale = float(np.abs(dref).max())
+    mstp = Stepper(g, True, mode=1)
+    mstp.dtmin, mstp.DTmax = stp.dtmin, stp.DTmax
+    mstp.step()
+    g.synchronize()
+    barrier(world)
+    steps = max(1, args.steps)
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+        g.timer_start()
+        for _ in range(steps):
+            mstp.step()
+        ms = g.timer_stop()
+    ms = max_over_ranks(ms, world)
+    return {"value": world * ncell * steps / (ms * 1e-3) / 1e6, "unit": "Mcell-steps/s", "steps": steps,
+            "ms_per_step": ms / steps,
+            "chem_half_step_ms": {"bdf": bdf_ms, "surrogate": sst["ms"], "network": sst["ms_network"]},
+            "fallback_frac": sst["fallback"] / max(1, sst["cells"]),
+            "max_dT_err_K": float(err.max()), "max_dT_K": scale,
+            "max_dT_err_frac": float(err.max()) / scale if scale > 0 else None,
+            "rms_dT_err_K": float(np.sqrt((err ** 2).mean())),
+            "training": {"samples": int(len(X)), "networks": 2, "epochs": 30, "label_s": t_label,
+                         "train_s": t_train},
+            "gate": list(gate), "clocks": clk.summary()}
 
 
 def run_batch(args):
@@ -357,6 +418,7 @@ def main():
     ap.add_argument("--n", type=int, default=64)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-chem", action="store_true", help="mixing layer without the chemistry half-steps")
+    ap.add_argument("--no-mlp", action="store_true", help="skip the learned-chemistry leg of the reacting step")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

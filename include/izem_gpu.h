@@ -190,7 +190,11 @@ int  izem_gpu_set_mechanism(izem_ctx* ctx, const izem_mech* mech);
  * each integrated as a constant-volume reactor by the BDF method (DVODE
  * MF=22, RTOL 1e-6, ATOL 1e-10, <= 20 restarts) in a persistent
  * work-stealing kernel; then upd_prim_var_woT, halo fill and the ghost
- * Newton solve.  mode 0 = BDF on every cell.  DTmax receives max |dT| [K]. */
+ * Newton solve.  mode IZEM_CHEM_BDF: the BDF method on every cell;
+ * IZEM_CHEM_MLP: the learned surrogate set by izem_gpu_set_surrogate with its
+ * error gate, rejected cells by the BDF method (no counterpart in the
+ * reference).  DTmax receives max |dT| [K]. */
+enum { IZEM_CHEM_BDF = 0, IZEM_CHEM_MLP = 1 };
 int  izem_gpu_chem_step(izem_ctx* ctx, double dt, int mode, double* DTmax);
 /* Statistics of the last chemistry step: cells whose integration failed
  * (ISTATE <= -2), largest and summed BDF step counts. */
@@ -251,6 +255,16 @@ int  izem_gpu_psr_batch_mlp(izem_mlp* m, izem_mlp* m2, const izem_mech* mech, in
  * parameters are allocated once by izem_mlp_create. */
 #define IZEM_MLP_NOALLOC_MAX_ROWS 4096
 int  izem_mlp_forward_noalloc(izem_mlp* m, int M, const float* d_x, float* d_y, void* stream);
+/* Surrogate used by izem_gpu_chem_step(..., IZEM_CHEM_MLP, ...): networks m
+ * (and optional partner m2, see izem_gpu_psr_batch_mlp), gate9 and the
+ * element counts kncf[nrv][nele] (no counterpart in the reference).  The
+ * handles stay owned by the caller.  izem_gpu_chem_surrogate_stats reports
+ * the last such step: window cells, cells sent to the BDF method, total and
+ * network-only milliseconds. */
+int  izem_gpu_set_surrogate(izem_ctx* ctx, izem_mlp* m, izem_mlp* m2, const double* gate9,
+                            const int* kncf, int nele);
+int  izem_gpu_chem_surrogate_stats(izem_ctx* ctx, long long* cells, int* fallback, float* ms_total,
+                                   float* ms_network);
 
 /* Device timing of the calls above on the context's stream (CUDA events). */
 int  izem_gpu_timer_start(izem_ctx* ctx);

@@ -23,6 +23,9 @@ ERR_NOMEM = 8
 ERR_STATE = 9
 ERR_TOO_LARGE = 10
 
+CHEM_BDF = 0
+CHEM_MLP = 1
+
 ERR_NAMES = {
     OK: "ok", ERR_ARG: "bad argument", ERR_CUDA: "CUDA error",
     ERR_NEG_PRESSURE: "negative pressure", ERR_NEG_TEMPERATURE: "negative temperature",

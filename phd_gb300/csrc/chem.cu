@@ -928,19 +928,66 @@ __device__ __forceinline__ void chem_stats_add(ChemStats* stats, int istate, int
   atomicAdd(&stats->total_steps, (unsigned long long)nst);
 }
 
+// Ghosted linear index of window cell q (i fastest): the reaction_dvode
+// loop order over the chemistry window (module_reaction.f90:155-171).
+__device__ __forceinline__ long long window_point(const ChemField& f, unsigned q) {
+  const int i = f.ix + (int)(q % f.wx);
+  const long long r = q / f.wx;
+  const int j = f.iy + (int)(r % f.wy);
+  const int k = f.iz + (int)(r / f.wy);
+  return (long long)(i - 1 + f.ng) + (long long)f.gx * ((long long)(j - 1 + f.ng) + (long long)f.gy * (long long)(k - 1 + f.ng));
+}
+
+// Window -> independent reactors in physical units: T [K], rho [g/cm^3],
+// Y (n x KK, row-major), dt [s] (the inputs reaction_dvode hands PSR_CHEMKIN).
+template <int KK>
+__global__ void k_chem_gather(ChemField f, double* T, double* rho, double* Y, double* dt) {
+  const long long n = (long long)f.wx * f.wy * f.wz;
+  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const long long p = window_point(f, (unsigned)q);
+  const long long nc = f.ncell;
+  const double rho0 = f.v[p];
+  const double rho_i = 1.0 / rho0;
+#pragma unroll
+  for (int l = 0; l < KK; ++l) Y[q * KK + l] = f.v[(5 + l) * nc + p] * rho_i;
+  T[q] = f.T[p] * f.t_ref;
+  rho[q] = rho0 * f.rho_cgs;
+  dt[q] = f.dt_phys;
+}
+
+// Reactors -> window, with reaction_dvode's post-processing (module_reaction.f90:
+// 275-290): Y clipped to [0,1], the last species closes the sum, T back to code
+// units; max |dT| into the statistics.
+template <int KK>
+__global__ void k_chem_scatter(ChemField f, const double* T, const double* Y, ChemStats* stats) {
+  const long long n = (long long)f.wx * f.wy * f.wz;
+  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const long long p = window_point(f, (unsigned)q);
+  const long long nc = f.ncell;
+  const double rho0 = f.v[p];
+  const double T0 = f.T[p] * f.t_ref;
+  f.T[p] = T[q] * f.tref_i;
+  const double dT = fabs(T[q] - T0);
+  atomicMax(&stats->dtmax_bits, (unsigned long long)__double_as_longlong(dT));
+  double sumY = 0.0;
+#pragma unroll
+  for (int l = 0; l < KK - 1; ++l) {
+    const double Ya = fmin(fmax(Y[q * KK + l], 0.0), 1.0);
+    f.v[(5 + l) * nc + p] = rho0 * Ya;
+    sumY = sumY + Ya;
+  }
+  f.v[(5 + KK - 1) * nc + p] = rho0 * (1.0 - sumY);
+  if (f.dT_out) f.dT_out[q] = T[q] - T0;
+}
+
 template <int KK>
 __global__ void __launch_bounds__(128) k_psr_field(ChemField f, unsigned* counter, ChemStats* stats) {
   constexpr int N = KK + 1;
   const long long ncell = (long long)f.wx * f.wy * f.wz;
   const long long nc = f.ncell;
-  auto point = [&](unsigned q) {
-    const int i = f.ix + (int)(q % f.wx);
-    const long long r = q / f.wx;
-    const int j = f.iy + (int)(r % f.wy);
-    const int k = f.iz + (int)(r / f.wy);
-    return (long long)(i - 1 + f.ng) +
-           (long long)f.gx * ((long long)(j - 1 + f.ng) + (long long)f.gy * (long long)(k - 1 + f.ng));
-  };
+  auto point = [&](unsigned q) { return window_point(f, q); };
   auto load = [&](unsigned q, double& rho, double* z, double& tf) {
     const long long p = point(q);
     const double rho0 = f.v[p];
@@ -1156,6 +1203,18 @@ cudaError_t chem_launch_batch(int n, double* T, const double* rho, double* Y, co
   if (e != cudaSuccess) return e;
   if (kk != 9) return cudaErrorInvalidValue;
   k_psr_batch<9><<<blocks, 128, 0, s>>>(n, T, rho, Y, dt, istate, nsteps, d_counter, d_stats);
+  return cudaGetLastError();
+}
+
+cudaError_t chem_launch_gather(const ChemField& f, double* T, double* rho, double* Y, double* dt, cudaStream_t s) {
+  const long long n = (long long)f.wx * f.wy * f.wz;
+  k_chem_gather<9><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(f, T, rho, Y, dt);
+  return cudaGetLastError();
+}
+
+cudaError_t chem_launch_scatter(const ChemField& f, const double* T, const double* Y, ChemStats* d_stats, cudaStream_t s) {
+  const long long n = (long long)f.wx * f.wy * f.wz;
+  k_chem_scatter<9><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(f, T, Y, d_stats);
   return cudaGetLastError();
 }
 

@@ -27,6 +27,10 @@ cudaError_t chem_launch_field(const ChemField& f, unsigned* d_counter, ChemStats
 cudaError_t chem_launch_batch(int n, double* T, const double* rho, double* Y, const double* dt, int* istate,
                               int* nsteps, unsigned* d_counter, ChemStats* d_stats, cudaStream_t s, int kk);
 
+// chemistry window <-> independent reactors (physical units)
+cudaError_t chem_launch_gather(const ChemField& f, double* T, double* rho, double* Y, double* dt, cudaStream_t s);
+cudaError_t chem_launch_scatter(const ChemField& f, const double* T, const double* Y, ChemStats* d_stats, cudaStream_t s);
+
 // learned-surrogate support (chem.cu)
 cudaError_t chem_launch_featurize(int n, const double* T, const double* rho, const double* Y, const double* dt,
                                   const float* d_norm, void* x_bf16, int ldx, cudaStream_t s);

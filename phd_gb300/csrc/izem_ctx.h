@@ -42,6 +42,17 @@ struct izem_ctx {
   unsigned* d_counter = nullptr;
   void* d_chem_stats = nullptr;   // ChemStats
   void* h_chem_stats = nullptr;
+  // learned surrogate for chemistry mode IZEM_CHEM_MLP
+  izem_mlp* sur_m = nullptr;
+  izem_mlp* sur_m2 = nullptr;
+  double sur_gate[9] = {};
+  std::vector<int> sur_kncf;
+  int sur_nele = 0;
+  long long sur_cap = 0;                  // reactor buffers for the window
+  double *b_T = nullptr, *b_rho = nullptr, *b_Y = nullptr, *b_dt = nullptr;
+  int sur_stats[3] = {};                  // fallback cells, max BDF steps, failed
+  float sur_ms[2] = {};                   // total, network
+  long long sur_cells = 0;
   int newton_warn = 0;
   std::string err;
 };

@@ -416,6 +416,7 @@ void izem_gpu_destroy(izem_ctx* c) {
   if (c->d_counter) cudaFree(c->d_counter);
   if (c->d_chem_stats) cudaFree(c->d_chem_stats);
   if (c->h_chem_stats) cudaFreeHost(c->h_chem_stats);
+  cudaFree(c->b_T); cudaFree(c->b_rho); cudaFree(c->b_Y); cudaFree(c->b_dt);
   if (c->h_status) cudaFreeHost(c->h_status);
   if (c->h_dt) cudaFreeHost(c->h_dt);
   for (auto& v : c->kt_pending)
@@ -582,10 +583,30 @@ int izem_gpu_set_mechanism(izem_ctx* c, const izem_mech* mech) {
   return IZEM_OK;
 }
 
+int izem_gpu_set_surrogate(izem_ctx* c, izem_mlp* m, izem_mlp* m2, const double* gate9, const int* kncf, int nele) {
+  if (!c || !m || !gate9 || !kncf || nele <= 0) return IZEM_ERR_ARG;
+  c->sur_m = m;
+  c->sur_m2 = m2;
+  std::memcpy(c->sur_gate, gate9, sizeof(c->sur_gate));
+  c->sur_kncf.assign(kncf, kncf + (size_t)c->cfg.nrv * nele);
+  c->sur_nele = nele;
+  return IZEM_OK;
+}
+
+int izem_gpu_chem_surrogate_stats(izem_ctx* c, long long* cells, int* fallback, float* ms_total, float* ms_network) {
+  if (!c) return IZEM_ERR_ARG;
+  if (cells) *cells = c->sur_cells;
+  if (fallback) *fallback = c->sur_stats[0];
+  if (ms_total) *ms_total = c->sur_ms[0];
+  if (ms_network) *ms_network = c->sur_ms[1];
+  return IZEM_OK;
+}
+
 int izem_gpu_chem_step(izem_ctx* c, double dt, int mode, double* DTmax) {
   if (!c || !DTmax) return IZEM_ERR_ARG;
   if (!c->have_mech) return ctx_fail(c, IZEM_ERR_STATE, "no mechanism set", cudaSuccess);
-  if (mode != 0) return ctx_fail(c, IZEM_ERR_ARG, "unknown chemistry mode", cudaSuccess);
+  if (mode != IZEM_CHEM_BDF && mode != IZEM_CHEM_MLP) return ctx_fail(c, IZEM_ERR_ARG, "unknown chemistry mode", cudaSuccess);
+  if (mode == IZEM_CHEM_MLP && !c->sur_m) return ctx_fail(c, IZEM_ERR_STATE, "no surrogate set", cudaSuccess);
   const Geo& g = c->g;
   ChemField f;
   f.v = c->v;
@@ -606,8 +627,32 @@ int izem_gpu_chem_step(izem_ctx* c, double dt, int mode, double* DTmax) {
   f.rho_cgs = c->adi.rho_ref * 1.0e-3;
   f.dt_phys = dt * c->adi.time_ref;
   CK(cudaMemsetAsync(c->d_chem_stats, 0, sizeof(ChemStats), c->stream));
-  if (f.wx > 0 && f.wy > 0 && f.wz > 0) {
+  int sur_rc = IZEM_OK;
+  if (f.wx > 0 && f.wy > 0 && f.wz > 0 && mode == IZEM_CHEM_BDF) {
     int rc = launch(c, "chem_psr", [&] { (void)chem_launch_field(f, c->d_counter, (ChemStats*)c->d_chem_stats, c->stream, 9); });
+    if (rc) return rc;
+  } else if (f.wx > 0 && f.wy > 0 && f.wz > 0) {
+    // window -> reactors, gated surrogate with BDF fallback (its own stream), reactors -> window
+    const long long n = (long long)f.wx * f.wy * f.wz;
+    if (n > INT32_MAX) return ctx_fail(c, IZEM_ERR_ARG, "chemistry window too large for the surrogate path", cudaSuccess);
+    if (n > c->sur_cap) {
+      cudaFree(c->b_T); cudaFree(c->b_rho); cudaFree(c->b_Y); cudaFree(c->b_dt);
+      c->b_T = c->b_rho = c->b_Y = c->b_dt = nullptr;
+      CK(cudaMalloc(&c->b_T, n * sizeof(double)));
+      CK(cudaMalloc(&c->b_rho, n * sizeof(double)));
+      CK(cudaMalloc(&c->b_Y, n * 9 * sizeof(double)));
+      CK(cudaMalloc(&c->b_dt, n * sizeof(double)));
+      c->sur_cap = n;
+    }
+    int rc = launch(c, "chem_gather", [&] { (void)chem_launch_gather(f, c->b_T, c->b_rho, c->b_Y, c->b_dt, c->stream); });
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(c->stream));
+    sur_rc = izem_gpu_psr_batch_mlp(c->sur_m, c->sur_m2, &c->mech, (int)n, c->b_T, c->b_rho, c->b_Y, c->b_dt, 1,
+                                    c->sur_gate, c->sur_kncf.data(), c->sur_nele, nullptr, c->sur_stats, c->sur_ms);
+    c->sur_cells = n;
+    if (sur_rc != IZEM_OK && sur_rc != IZEM_ERR_CHEM)
+      return ctx_fail(c, sur_rc, "surrogate chemistry step failed", cudaSuccess);
+    rc = launch(c, "chem_scatter", [&] { (void)chem_launch_scatter(f, c->b_T, c->b_Y, (ChemStats*)c->d_chem_stats, c->stream); });
     if (rc) return rc;
   }
   int rc = IZEM_DISPATCH(c, do_chem_after, c);
@@ -615,9 +660,11 @@ int izem_gpu_chem_step(izem_ctx* c, double dt, int mode, double* DTmax) {
   CK(cudaMemcpyAsync(c->h_chem_stats, c->d_chem_stats, sizeof(ChemStats), cudaMemcpyDeviceToHost, c->stream));
   rc = read_status(c);
   if (rc) return rc;
-  const ChemStats& cs = *(const ChemStats*)c->h_chem_stats;
+  ChemStats& cs = *(ChemStats*)c->h_chem_stats;
+  if (mode == IZEM_CHEM_MLP) { cs.failed = c->sur_stats[2]; cs.max_steps = c->sur_stats[1]; }
   std::memcpy(DTmax, &cs.dtmax_bits, sizeof(double));
-  if (cs.failed) return ctx_fail(c, IZEM_ERR_CHEM, "stiff integration failed (ISTATE <= -2) on some cells", cudaSuccess);
+  if (cs.failed || sur_rc == IZEM_ERR_CHEM)
+    return ctx_fail(c, IZEM_ERR_CHEM, "stiff integration failed (ISTATE <= -2) on some cells", cudaSuccess);
   return IZEM_OK;
 }
 

@@ -72,6 +72,9 @@ def load_library(path=None):
         "izem_gpu_chem_stats": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_ulonglong)]),
         "izem_gpu_psr_batch": (C.c_int, [C.POINTER(IzemMech), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                          C.c_void_p, C.c_void_p, C.c_int, C.POINTER(C.c_float)]),
+        "izem_gpu_set_surrogate": (C.c_int, [P, P, P, _dp, C.POINTER(C.c_int), C.c_int]),
+        "izem_gpu_chem_surrogate_stats": (C.c_int, [P, C.POINTER(C.c_longlong), C.POINTER(C.c_int),
+                                                    C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -252,9 +255,34 @@ class IzemGPU:
         self._mech = mech
         self._check(self.lib.izem_gpu_set_mechanism(self.h, C.byref(mech)), "set_mechanism")
 
+    def set_surrogate(self, net, partner=None, gate=None, kncf=None):
+        """Learned chemistry for reaction_selec(mode=CHEM_MLP): a
+        phd_gb300.surrogate.Surrogate (and optional partner network), the
+        error gate (9 numbers) and the element counts kncf[nrv][nele]."""
+        from .surrogate import DEFAULT_GATE
+        from .thd import load_species
+        if kncf is None:
+            kncf = load_species("h2air9")["kncf"]
+        self._sur = (net, partner)
+        self._gate = np.ascontiguousarray(np.array(DEFAULT_GATE if gate is None else gate, dtype=np.float64))
+        self._kncf = np.ascontiguousarray(np.array(kncf, dtype=np.int32))
+        self._check(self.lib.izem_gpu_set_surrogate(self.h, net.h, partner.h if partner is not None else None,
+                                                    _ptr(self._gate), _ptr(self._kncf, C.POINTER(C.c_int)),
+                                                    self._kncf.shape[1]), "set_surrogate")
+
+    def surrogate_stats(self):
+        """Last surrogate chemistry step: window cells, BDF fallback cells,
+        total and network-only milliseconds."""
+        n, fb, a, b = C.c_longlong(), C.c_int(), C.c_float(), C.c_float()
+        self._check(self.lib.izem_gpu_chem_surrogate_stats(self.h, C.byref(n), C.byref(fb), C.byref(a), C.byref(b)),
+                    "chem_surrogate_stats")
+        return {"cells": n.value, "fallback": fb.value, "ms": a.value, "ms_network": b.value}
+
     def reaction_selec(self, dt, mode=0):
         """One Strang chemistry half step of length dt (code units); returns
-        DTmax [K] (module_reaction.f90:47-100)."""
+        DTmax [K] (module_reaction.f90:47-100).  mode CHEM_BDF (0) integrates
+        every cell with the BDF method, CHEM_MLP (1) uses the surrogate set by
+        set_surrogate with BDF fallback."""
         d = C.c_double()
         self._check(self.lib.izem_gpu_chem_step(self.h, float(dt), int(mode), C.byref(d)), "chem_step")
         return d.value

@@ -226,3 +226,65 @@ def training_set(mech, n, seed):
     psr_batch(mech, T1, rho.copy(), Y1, dt.copy())
     Yt = np.concatenate([Y1 - Y, (T1 - T)[:, None]], axis=1)
     return X, Yt
+
+
+def window_reactors(g, dt):
+    """The reactors of one chemistry half step of an IzemGPU block: the
+    reaction_dvode window (ng+1 cells skipped at every face; the z bound
+    uses ey, module_reaction.f90:155-171) in physical units, i fastest.
+    Returns T [K], rho [g/cm^3], Y (n, nrv), dt [s] (n values)."""
+    cfg, adi = g.cfg, g.adi
+    st = g.download()
+    ng = cfg.ng
+    fx, fy = min(cfg.nx, cfg.nx - ng - 1), min(cfg.ny, cfg.ny - ng - 1)
+    fz = min(cfg.ny, cfg.nz - ng - 1)
+    sl = (slice(2 * ng, fx + ng), slice(2 * ng, fy + ng), slice(2 * ng, fz + ng))
+    v = st["v"][sl]
+    rho = v[..., 0]
+    n = rho.size
+    Y = (v[..., 5:5 + cfg.nrv] / rho[..., None]).reshape(n, cfg.nrv, order="F")
+    T = (st["T"][sl] * adi.t_ref).reshape(n, order="F")
+    rho_c = (rho * adi.rho_ref * 1e-3).reshape(n, order="F")
+    return (np.ascontiguousarray(T), np.ascontiguousarray(rho_c), np.ascontiguousarray(Y),
+            np.full(n, dt * adi.time_ref))
+
+
+def flow_training_set(g, mech, dt, n_max=1 << 20, spread=0.5, seed=5):
+    """Samples drawn from a flow block as the surrogate will meet them: its
+    window reactors with the half step scaled by 10**U[-spread, spread],
+    labelled by the FP64 BDF integrator.  Returns raw features and targets."""
+    T, rho, Y, dtp = window_reactors(g, dt)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    idx = rng.choice(len(T), size=min(n_max, len(T)), replace=False) if len(T) > n_max else np.arange(len(T))
+    T, rho, Y, dtp = T[idx].copy(), rho[idx].copy(), np.ascontiguousarray(Y[idx]), dtp[idx].copy()
+    dtp = dtp * 10.0 ** rng.uniform(-spread, spread, len(T))
+    wt = np.array([mech.wt[k] for k in range(mech.kk)])
+    X = features(T, rho, Y, dtp, wt)
+    T1, Y1 = T.copy(), Y.copy()
+    psr_batch(mech, T1, rho.copy(), Y1, dtp.copy())
+    Yt = np.concatenate([Y1 - Y, (T1 - T)[:, None]], axis=1)
+    return X, Yt
+
+
+def train_on(X, Yt, members=2, seed=31, epochs=24, batch=4096, lr=1e-3):
+    """Train `members` networks on raw features/targets (different
+    initialisations and shuffles, step-decayed learning rate)."""
+    nets = []
+    for q in range(members):
+        s = Surrogate(seed=seed + 1000 * (q + 1))
+        s.fit_norm(X, Yt)
+        xn, tn = s.normalise(X, Yt)
+        for stage, f in enumerate((1.0, 0.3, 0.1)):
+            s.train(xn, tn, epochs=max(1, epochs // 3), batch=batch, lr=lr * f, seed=seed + 17 * q + stage)
+        nets.append(s)
+    return nets
+
+
+def flow_gate(X, Yt, dT_tol_frac=0.002):
+    """Gate for a flow-trained surrogate: the envelope of its training
+    temperatures and steps, element tolerance 2e-3, and temperature
+    tolerances scaled to the largest trained increment."""
+    scale = float(np.abs(Yt[:, -1]).max())
+    dt = np.exp(X[:, 11])
+    a = dT_tol_frac * scale
+    return (float(X[:, 0].min()), float(X[:, 0].max()), float(dt.min()), float(dt.max()), 2e-3, a, 0.02, 0.5 * a, 0.005)
