@@ -142,7 +142,12 @@ def run_gpu(args, rank, world):
     cfg, thd, adi, dxi, st, info = build_workload(args)
     chem = args.workload == "mix" and not args.no_chem
     cfg.reaction = 1 if chem else 0
+    eg = args.workload == "mix" and args.transport == "eglib"
+    cfg.eglib = 1 if eg else 0
     g = IzemGPU(cfg, thd, adi)
+    if eg:
+        from phd_gb300.thd import eglib_link, load_species
+        g.set_eglib(eglib_link(load_species("h2air9")))
     g.set_grid(*dxi)
     g.upload(**st)
     g.finalize_ic()
@@ -204,8 +209,9 @@ def run_gpu(args, rank, world):
         "value": value, "unit": "Mcell-steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded PCG64 %d)" % info.get("seed", 0),
-        "config": {"workload": info["name"] + (NOTE_CHEM if chem else WORKLOAD_NOTE), "cells": ncell,
-                   "nv": 5 + cfg.nrv, "transport": "fitted mixture-averaged (tranfit)",
+        "config": {"workload": info["name"] + workload_note(chem, eg), "cells": ncell,
+                   "nv": 5 + cfg.nrv,
+                   "transport": "EGLIB precision 1 (EGSE2, EGSLCT2, EGSDR1)" if eg else "fitted mixture-averaged (tranfit)",
                    "chemistry": ("Strang: 2 x BDF (DVODE MF=22) half-steps per step, 9 species / 12 reactions"
                                  if chem else "off"),
                    "l2": "inputs larger than L2 (state %.2f GB)" % (host["v"].nbytes / 1e9),
@@ -333,8 +339,9 @@ def run_batch(args):
     }
 
 
-WORKLOAD_NOTE = " (WENO5 + fitted viscous + RK3; chemistry and EGLIB not in this line)"
-NOTE_CHEM = " (WENO5 + fitted viscous + RK3 + BDF chemistry; EGLIB transport not in this line)"
+def workload_note(chem, eg):
+    return " (WENO5 + %s viscous fluxes + RK3%s)" % ("EGLIB precision-1" if eg else "fitted-transport",
+                                                       " + Strang BDF chemistry" if chem else ", no chemistry")
 TRAFFIC_PER_LAUNCH = {}
 
 
@@ -361,7 +368,13 @@ def cpu_baseline(args, steps=2):
     else:
         cfg, thd, adi, dxi, st, info = ics.mixing_layer(nx, ny, nz, Lx=nx * 47e-6, Ly=ny * 47e-6, Lz=nz * 47e-6,
                                                         lib_dscalar=oracle.metrics_dscalar)
+    eg = args.workload == "mix" and args.transport == "eglib"
+    if eg:
+        from phd_gb300.thd import eglib_link, load_species
+        cfg.eglib = 1
     orc = oracle.Oracle(cfg, thd, adi, *dxi)
+    if eg:
+        orc.set_eglib(eglib_link(load_species("h2air9")))
     orc.finalize_ic(st)
     chem = args.workload == "mix" and not args.no_chem
     mech = None
@@ -419,6 +432,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-chem", action="store_true", help="mixing layer without the chemistry half-steps")
     ap.add_argument("--no-mlp", action="store_true", help="skip the learned-chemistry leg of the reacting step")
+    ap.add_argument("--transport", default="eglib", choices=["eglib", "fitted"],
+                    help="viscous transport of the mixing layer (EGLIB precision 1 or the tranfit fits)")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -431,8 +446,9 @@ def main():
             line = {"impl": "reference", "metric": "reacting RHS Mcell-steps/s, FP64 plain vs MLP-chem (<=1% dT err) on 1 GB300",
                     "value": cb["value"], "unit": cb["unit"], "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
                     "higher_is_better": True, "dtype": "f64", "data": "synthetic",
-                    "config": {"workload": "H2/air temporal mixing layer (sub-block) "
-                               + (WORKLOAD_NOTE if args.no_chem or args.workload == "tgv" else NOTE_CHEM)},
+                    "config": {"workload": "H2/air temporal mixing layer (sub-block)"
+                               + workload_note(args.workload == "mix" and not args.no_chem,
+                                               args.workload == "mix" and args.transport == "eglib")},
                     "cpu_baseline": cb, "e2e": {"value": cb["value"], "unit": cb["unit"], "h2d_bytes_per_step": 0,
                                                 "d2h_bytes_per_step": 0},
                     "note": "C++ restatement of the reference Fortran (no Fortran compiler on either host)"}

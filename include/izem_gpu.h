@@ -122,6 +122,22 @@ typedef struct izem_mech {
   double troe[IZEM_MAXREAC][4];           /* a, T***, T*, T**                 */
 } izem_mech;
 
+/* EGLIB linking data (the contents of the Linkeg file that EGINI reads,
+ * devel-izem/src/eglib/EGini.f:265-276): per species molar mass, geometry
+ * (0 atom, 1 linear, 2 nonlinear), Lennard-Jones eps/k [K] and diameter
+ * [Angstrom], dipole [Debye], polarizability [Angstrom^3], rotational
+ * relaxation number at 298 K, and the fits ln(eta [g/cm/s]) and
+ * ln(D_kl [cm^2/s] at 1 atm) as cubics in ln T.  Used by the EGLIB
+ * precision-1 viscous flux (cfg.eglib = 1). */
+typedef struct izem_eglib {
+  int    ns;
+  int    lin[IZEM_NSMAX];
+  double wt[IZEM_NSMAX], eps[IZEM_NSMAX], sig[IZEM_NSMAX];
+  double dip[IZEM_NSMAX], pol[IZEM_NSMAX], zrot[IZEM_NSMAX];
+  double cofe[IZEM_NSMAX][4];
+  double cofd[IZEM_NSMAX][IZEM_NSMAX][4];
+} izem_eglib;
+
 typedef struct izem_ctx izem_ctx;
 
 /* Create a context on the current CUDA device.  Allocates the device-resident
@@ -159,8 +175,15 @@ int  izem_gpu_shock_sensor(izem_ctx* ctx);
  * dir 1 and 2 accumulate into f. */
 int  izem_gpu_euler_flux(izem_ctx* ctx, int dir);
 
-/* viscflux_xyz (module_viscflux.f90:1660-2189): accumulates into f. */
+/* viscflux_xyz (module_viscflux.f90:1660-2189), or with cfg.eglib = 1
+ * viscflux_eg_xyz (module_eg_lib.f90:2140-2676, EGLIB precision 1):
+ * accumulates into f. */
 int  izem_gpu_visc_flux(izem_ctx* ctx);
+
+/* EGLIB linking data for cfg.eglib = 1 (init_eglib + EGINI,
+ * module_eg_lib.f90:44-96, eglib/EGini.f:58-301); call once after
+ * izem_gpu_init and before any viscous flux. */
+int  izem_gpu_set_eglib(izem_ctx* ctx, const izem_eglib* eglib);
 
 /* upd_prim_var_domain + comm_cons + upd_boundaries + upd_prim_var_ghost
  * (module_BCs.f90:41-296): force_sumY, Newton temperature per sub-domain with

@@ -10,7 +10,7 @@ import os
 
 import numpy as np
 
-from phd_gb300.capi import IzemAdi, IzemCfg, IzemMech, IzemThd
+from phd_gb300.capi import IzemAdi, IzemCfg, IzemEglib, IzemMech, IzemThd
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libizem_oracle.so")
@@ -49,6 +49,8 @@ def load():
         "or_psr_cells": (None, [C.POINTER(IzemMech), C.c_int, _dp, _dp, _dp, _dp, C.POINTER(C.c_int),
                                 C.POINTER(C.c_int)]),
         "or_ck_fun": (None, [C.POINTER(IzemMech), C.c_double, _dp, _dp]),
+        "or_set_eglib": (C.c_int, [P, C.POINTER(IzemEglib)]),
+        "or_eg_point": (None, [C.POINTER(IzemEglib), C.c_double, _dp, _dp, _dp, C.c_double, _dp, _dp, _dp, _dp]),
         "or_ck_wdot": (None, [C.POINTER(IzemMech), C.c_double, C.c_double, _dp, _dp]),
     }
     for name, (res, args) in sig.items():
@@ -95,6 +97,21 @@ def psr_cells(mech, T, rho, Y, dt):
     return istate, nsteps
 
 
+def eg_point(link, T, X, Y, cp, ww):
+    """EGLIB precision 1 at one point (EGSPAR, EGSE2, EGSLCT2, EGSDR1):
+    T [K], mole and mass fractions, species cp [erg/g/K], mean molar mass
+    [g/mol] -> (eta [g/cm/s], lambda [erg/cm/s/K], chi, rho*D [l][m])."""
+    lib = load()
+    n = link.ns
+    X, Y, cp = (np.ascontiguousarray(a, dtype=np.float64) for a in (X, Y, cp))
+    eta, tc = C.c_double(), C.c_double()
+    chit = np.zeros(n)
+    D = np.zeros((n, n))
+    lib.or_eg_point(C.byref(link), float(T), _p(X), _p(Y), _p(cp), float(ww), C.byref(eta), C.byref(tc), _p(chit),
+                    D.ctypes.data_as(_dp))   # row-major [l][m]
+    return eta.value, tc.value, chit, D
+
+
 def ck_fun(mech, rho, z):
     lib = load()
     z = np.ascontiguousarray(z, dtype=np.float64)
@@ -134,6 +151,10 @@ class Oracle:
             buf = C.create_string_buffer(256)
             self.lib.or_last_error(self.h, buf, 256)
             raise OracleError("%s failed (%d): %s" % (what, rc, buf.value.decode()))
+
+    def set_eglib(self, link):
+        self._eglib = link
+        self._rc(self.lib.or_set_eglib(self.h, C.byref(link)), "set_eglib")
 
     def newton_warnings(self):
         return self.lib.or_last_error(self.h, None, 0)

@@ -24,6 +24,7 @@
 #include <cstring>
 #include <algorithm>
 #include <vector>
+#include <memory>
 #include <string>
 
 #include "../include/izem_gpu.h"
@@ -48,10 +49,13 @@ struct Block {
   int n(int d) const { return d == 0 ? nx : (d == 1 ? ny : nz); }
 };
 
+struct EgInit;   // EGLIB initialisation data (eglib_oracle.inc)
+
 struct Ctx {
   izem_cfg cfg;
   izem_thd thd;
   izem_adi adi;
+  std::shared_ptr<EgInit> eg;   // set by or_set_eglib for cfg.eglib = 1
   Block b;
   std::vector<double> dxi[3];   // indexed (i-1+ng), length n+2ng
   int newton_warn = 0;
@@ -792,7 +796,8 @@ void prim_vis_point(const Ctx& c, double rho, double T, double W_i, const double
 }
 
 // viscflux_xyz (module_viscflux.f90:1660-2189)
-int visc_flux(Ctx& c, const double* v, const double* T, const double* W_i, const double* cp, const double* ha, double* fl) {
+int visc_flux_fit(Ctx& c, const double* v, const double* T, const double* W_i, const double* cp, const double* ha,
+                  double* fl) {
   (void)cp;
   const Block& b = c.b;
   const izem_thd& t = c.thd;
@@ -835,6 +840,7 @@ int visc_flux(Ctx& c, const double* v, const double* T, const double* W_i, const
       int f = dom < 0 ? 2 * (-dom - 1) : 2 * (dom - 1) + 1;
       if (b.bnd[f]) continue;
     }
+#pragma omp parallel for collapse(2) schedule(dynamic)
     for (int k = k0; k <= k1; ++k)
       for (int j = j0; j <= j1; ++j)
         for (int i = i0; i <= i1; ++i) {
@@ -898,6 +904,18 @@ int visc_flux(Ctx& c, const double* v, const double* T, const double* W_i, const
     accum(NIV + l, fd.data() + (size_t)(nfluid + 3 * l) * nc, fd.data() + (size_t)(nfluid + 3 * l + 1) * nc,
           fd.data() + (size_t)(nfluid + 3 * l + 2) * nc);
   return IZEM_OK;
+}
+
+#include "eglib_oracle.inc"
+
+// viscflux_xyz or, with EGLIB, viscflux_eg_xyz (the choice in rk3, module_solver.f90:777-820)
+int visc_flux(Ctx& c, const double* v, const double* T, const double* W_i, const double* cp, const double* ha,
+              double* fl) {
+  if (c.cfg.eglib) {
+    if (!c.eg) { c.err = "EGLIB transport requested but no linking data set"; return IZEM_ERR_STATE; }
+    return visc_flux_eg(c, *c.eg, v, T, W_i, ha, fl);
+  }
+  return visc_flux_fit(c, v, T, W_i, cp, ha, fl);
 }
 
 // rk3 (module_solver.f90:694-856)
@@ -1082,6 +1100,24 @@ int or_euler_flux(void* h, int dir, const double* v, const double* T, const doub
 int or_visc_flux(void* h, const double* v, const double* T, const double* W_i, const double* cp,
                  const double* ha, double* fl) {
   return visc_flux(*static_cast<Ctx*>(h), v, T, W_i, cp, ha, fl);
+}
+int or_set_eglib(void* h, const izem_eglib* L) {
+  if (!h || !L || L->ns != static_cast<Ctx*>(h)->b.nrv) return IZEM_ERR_ARG;
+  auto e = std::make_shared<EgInit>();
+  eg_init(*L, *e);
+  static_cast<Ctx*>(h)->eg = e;
+  return IZEM_OK;
+}
+// One point of EGLIB precision 1 (no context): T [K], X, Y, cp [erg/g/K],
+// mean molar mass [g/mol] -> eta, lambda, chi (ns), rho*D (ns x ns, [l][m]).
+void or_eg_point(const izem_eglib* L, double T, const double* X, const double* Y, const double* cp, double ww,
+                 double* eta, double* tc, double* chit, double* D) {
+  EgInit E;
+  eg_init(*L, E);
+  double Dm[EGN][EGN];
+  eg_point(E, T, X, Y, cp, ww, eta, tc, chit, Dm);
+  for (int l = 0; l < L->ns; ++l)
+    for (int m = 0; m < L->ns; ++m) D[l * L->ns + m] = Dm[l][m];
 }
 int or_prim_inv_var(void* h, int dom, int err_mach, double* v, double* W_i, double* T, double* cp, double* ha) {
   return prim_inv_var(*static_cast<Ctx*>(h), dom, err_mach != 0, v, W_i, T, cp, ha);

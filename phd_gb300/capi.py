@@ -84,6 +84,16 @@ class IzemMech(C.Structure):
     ]
 
 
+class IzemEglib(C.Structure):
+    _fields_ = [
+        ("ns", C.c_int), ("lin", C.c_int * NSMAX),
+        ("wt", C.c_double * NSMAX), ("eps", C.c_double * NSMAX), ("sig", C.c_double * NSMAX),
+        ("dip", C.c_double * NSMAX), ("pol", C.c_double * NSMAX), ("zrot", C.c_double * NSMAX),
+        ("cofe", (C.c_double * 4) * NSMAX),
+        ("cofd", ((C.c_double * 4) * NSMAX) * NSMAX),
+    ]
+
+
 class IzemAdi(C.Structure):
     _fields_ = [(n, C.c_double) for n in (
         "gamma_inf", "re", "pr", "le", "ma", "sc", "sqgmr", "ggmopr",

@@ -36,6 +36,7 @@ struct izem_ctx {
   std::vector<int> kt_launches;
   std::vector<double> kt_ms;
   std::vector<std::vector<std::pair<cudaEvent_t, cudaEvent_t>>> kt_pending;
+  bool have_eg = false;   // EGLIB linking data uploaded (izem_gpu_set_eglib)
   // chemistry
   bool have_mech = false;
   izem_mech mech;

@@ -16,6 +16,7 @@
 #include "thermo.cuh"
 #include "kernels_euler.cuh"
 #include "kernels_visc.cuh"
+#include "kernels_eglib.cuh"
 #include "kernels_state.cuh"
 #include "izem_ctx.h"
 #include "chem.h"
@@ -166,14 +167,24 @@ int enq_visc(izem_ctx* c) {
   const Geo& g = c->g;
   Metrics mt;
   for (int d = 0; d < 3; ++d) mt.dxi[d] = c->dxi[d];
-  const int nderiv = 12 + 3 * NRV;
+  const bool eg = c->cfg.eglib != 0;
+  const int nderiv = (eg ? 15 : 12) + 3 * NRV;
   int rc;
   if ((rc = launch(c, "visc_grad", [&] { k_grad<NRV><<<grid_for(g.nint), kThreads, 0, c->stream>>>(g, mt, c->prim, c->T, c->Xa, c->fd); })))
+    return rc;
+  if (eg && (rc = launch(c, "visc_grad_p", [&] { k_grad_p<NRV><<<grid_for(g.nint), kThreads, 0, c->stream>>>(g, mt, c->prim, c->fd); })))
     return rc;
   long long ns = slab_count(g) - g.nint;
   if ((rc = launch(c, "visc_wrap", [&] { k_wrap_periodic<<<grid_for(ns), kThreads, 0, c->stream>>>(g, nderiv, c->fd); })))
     return rc;
-  if ((rc = launch(c, "visc_point", [&] {
+  if (eg) {
+    const long long ns_all = slab_count(g);
+    if ((rc = launch(c, "visc_point_eg", [&] {
+           k_visc_point_eg<NRV><<<(unsigned)((ns_all + 127) / 128), 128, 0, c->stream>>>(g, c->v, c->T, c->W_i, c->ha, c->Xa,
+                                                                                         c->prim, c->fd, c->tau, c->qv);
+         })))
+      return rc;
+  } else if ((rc = launch(c, "visc_point", [&] {
          k_visc_point<NRV><<<grid_for(slab_count(g)), kThreads, 0, c->stream>>>(g, c->v, c->T, c->W_i, c->ha, c->Xa, c->fd, c->tau, c->qv);
        })))
     return rc;
@@ -381,7 +392,7 @@ int ctx_alloc(izem_ctx* c) {
   if ((e = alloc(&c->v, nv * nc)) || (e = alloc(&c->T, nc)) || (e = alloc(&c->W_i, nc)) || (e = alloc(&c->cp, nc)) ||
       (e = alloc(&c->ha, nrv * nc)) || (e = alloc(&c->v0, nv * ni)) || (e = alloc(&c->f, nv * ni)) ||
       (e = alloc(&c->prim, PR_N * nc)) || (e = alloc(&c->Xa, nrv * nc)) || (e = alloc(&c->fhat, nv * maxf)) ||
-      (e = alloc(&c->fd, (12 + 3 * nrv) * nc)) || (e = alloc(&c->tau, 6 * nc)) || (e = alloc(&c->qv, 3 * nc)) ||
+      (e = alloc(&c->fd, (15 + 3 * nrv) * nc)) || (e = alloc(&c->tau, 6 * nc)) || (e = alloc(&c->qv, 3 * nc)) ||
       (e = alloc(&c->d_dt, 1)))
     return ctx_fail(c, e == cudaErrorMemoryAllocation ? IZEM_ERR_NOMEM : IZEM_ERR_CUDA, "device allocation", e);
   for (int d = 0; d < 3; ++d)
@@ -394,7 +405,7 @@ int ctx_alloc(izem_ctx* c) {
   CK(cudaMallocHost(&c->h_dt, sizeof(double)));
   // zero the arrays whose ghost corners are never written
   CK(cudaMemset(c->v, 0, nv * nc * sizeof(double)));
-  CK(cudaMemset(c->fd, 0, (12 + 3 * nrv) * nc * sizeof(double)));
+  CK(cudaMemset(c->fd, 0, (15 + 3 * nrv) * nc * sizeof(double)));
   CK(cudaMemset(c->tau, 0, 6 * nc * sizeof(double)));
   CK(cudaMemset(c->qv, 0, 3 * nc * sizeof(double)));
   CK(cudaMemset(c->f, 0, nv * ni * sizeof(double)));
@@ -497,6 +508,8 @@ int izem_gpu_euler_flux(izem_ctx* c, int dir) {
 }
 
 int izem_gpu_visc_flux(izem_ctx* c) {
+  if (c && c->cfg.eglib && !c->have_eg)
+    return ctx_fail(c, IZEM_ERR_STATE, "EGLIB transport requested (cfg.eglib) but izem_gpu_set_eglib not called", cudaSuccess);
   if (!c) return IZEM_ERR_ARG;
   if (!c->grid_set) return ctx_fail(c, IZEM_ERR_STATE, "grid not set", cudaSuccess);
   int rc = IZEM_DISPATCH(c, do_visc, c);
@@ -522,6 +535,8 @@ int izem_gpu_rk3(izem_ctx* c, double dt, double time0) {
   (void)time0;
   if (!c) return IZEM_ERR_ARG;
   if (!c->grid_set) return ctx_fail(c, IZEM_ERR_STATE, "grid not set", cudaSuccess);
+  if (c->cfg.vis && c->cfg.eglib && !c->have_eg)
+    return ctx_fail(c, IZEM_ERR_STATE, "EGLIB transport requested (cfg.eglib) but izem_gpu_set_eglib not called", cudaSuccess);
   *c->h_dt = dt;
   CK(cudaMemcpyAsync(c->d_dt, c->h_dt, sizeof(double), cudaMemcpyHostToDevice, c->stream));
   int rc;
@@ -565,6 +580,17 @@ int izem_gpu_timestep(izem_ctx* c, double DTmax, double dt_4[4], double* dtmin) 
     dt_4[3] = std::fmax(dt_4[3], dt_4[0] * c->cfg.cflmin / c->cfg.cfl);
   }
   *dtmin = std::fmin(std::fmin(dt_4[0], dt_4[1]), std::fmin(dt_4[2], dt_4[3]));
+  return IZEM_OK;
+}
+
+int izem_gpu_set_eglib(izem_ctx* c, const izem_eglib* L) {
+  if (!c || !L) return IZEM_ERR_ARG;
+  if (L->ns != c->cfg.nrv)
+    return ctx_fail(c, IZEM_ERR_ARG, "EGLIB linking data must have nrv species", cudaSuccess);
+  DevEg e;
+  eg_prepare(*L, c->thd, c->adi, e);
+  CK(cudaMemcpyToSymbol(c_eg, &e, sizeof(DevEg)));
+  c->have_eg = true;
   return IZEM_OK;
 }
 

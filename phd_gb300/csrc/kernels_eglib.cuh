@@ -1,0 +1,491 @@
+// EGLIB precision-1 mixture transport and the viscous flux that uses it:
+// viscflux_eg_xyz with egvars (module_eg_lib.f90:106-310, 2140-2676).
+//
+// Per point, the kernel evaluates the EGlib 3.4 routines that egvars calls
+// with eglib_precision = 1 (A. Ern and V. Giovangigli, devel-izem/src/eglib/
+// EGSlib.f): EGSPAR/LSPAR with IFLAG = 7 (pure viscosities, reciprocal binary
+// diffusion coefficients, collision-integral ratios A*, B*, C*, internal heat
+// capacities and Parker's rotational relaxation), EGSE2 (shear viscosity, one
+// conjugate-gradient step on the matrix H with the 1000 K A*), EGSLCT2
+// (conductivity and rescaled thermal diffusion ratios, a direct
+// factorisation of Lambda_[e]) and EGSDR1 (rho times the flux diffusion
+// matrix, two stationary steps on L_[00] and the mass-conservation
+// projection), in the reference's operation order.  EGSL2 and EGSK2, also
+// called there, only produce values that the reference discards (the
+// conductivity is recomputed by EGSLCT2 and the volume viscosity is set to
+// zero, module_eg_lib.f90:288).
+//
+// The species gradients keep the fitted-transport layout of fd
+// (12 + 3 l + d) so that k_visc_div is shared; the pressure gradients of
+// the EGLIB flux (fd 13-15 in the reference) sit after them (12 + 3 NRV + d).
+#pragma once
+#include <cmath>
+#include "common.cuh"
+#include "kernels_visc.cuh"
+
+struct DevEg {
+  int ns;
+  int lin[IZEM_NSMAX];
+  double wt[IZEM_NSMAX], eps[IZEM_NSMAX], dip[IZEM_NSMAX], zrot[IZEM_NSMAX];
+  double cofe[IZEM_NSMAX][4];
+  double cofd[IZEM_NSMAX][IZEM_NSMAX][4];
+  double ctaij[IZEM_NSMAX][IZEM_NSMAX];              // A*_ij at 1000 K
+  double fita[IZEM_NSMAX][IZEM_NSMAX][7];            // A*, B*, C* in powers of ln T
+  double fitb[IZEM_NSMAX][IZEM_NSMAX][7];
+  double fitc[IZEM_NSMAX][IZEM_NSMAX][7];
+  // egvars scalings (module_eg_lib.f90:140-145)
+  double cp_cgs, eta_adim, lbda_adim, rd_adim;
+};
+
+static __constant__ DevEg c_eg;
+
+// Host: EGINI's set-up (EGini.f:58-301) from the linking data -- pair well
+// depths with the polar correction (LEVEPS), A* at 1000 K, and the A*, B*,
+// C* fits re-expanded in ln T for every pair (EGABC).  The fit constants are
+// EGLIB's published collision-integral ratio fits.
+inline void eg_prepare(const izem_eglib& L, const izem_thd& t, const izem_adi& a, DevEg& E) {
+  static const double fa0[7] = {.1106910525e+01, -.7065517161e-02, -.1671975393e-01, .1188708609e-01,
+                                .7569367323e-03, -.1313998345e-02, .1720853282e-03};
+  static const double fb0[7] = {.1199673577e+01, -.1140928763e+00, -.2147636665e-02, .2512965407e-01,
+                                -.3030372973e-02, -.1445009039e-02, .2492954809e-03};
+  static const double fc0[7] = {.8386993788e+00, .4748325276e-01, .3250097527e-01, -.1625859588e-01,
+                                -.2260153363e-02, .1844922811e-02, -.2115417788e-03};
+  const int n = L.ns;
+  E = DevEg{};
+  E.ns = n;
+  for (int k = 0; k < n; ++k) {
+    E.lin[k] = L.lin[k];
+    E.wt[k] = L.wt[k];
+    E.eps[k] = L.eps[k];
+    E.dip[k] = L.dip[k];
+    E.zrot[k] = L.zrot[k];
+    for (int q = 0; q < 4; ++q) E.cofe[k][q] = L.cofe[k][q];
+    for (int l = 0; l < n; ++l)
+      for (int q = 0; q < 4; ++q) E.cofd[k][l][q] = L.cofd[k][l][q];
+  }
+  double lneps[IZEM_NSMAX][IZEM_NSMAX];
+  const double fac = 1.0e-12, dipmin = 1.0e-20, boltz = 1.38056e-16;
+  auto cube = [](double s) { return s * s * s; };
+  for (int j = 0; j < n; ++j)
+    for (int k = 0; k <= j; ++k) {
+      double e = std::sqrt(L.eps[j] * L.eps[k]);
+      int polar = -1, nonpolar = -1;
+      if (L.dip[j] < dipmin && L.dip[k] > dipmin) { polar = k; nonpolar = j; }
+      else if (L.dip[j] > dipmin && L.dip[k] < dipmin) { polar = j; nonpolar = k; }
+      if (polar >= 0) {
+        const double xi = 1.0 + 0.25 * (L.pol[nonpolar] / cube(L.sig[nonpolar])) * (fac / boltz) *
+                                    (L.dip[polar] * L.dip[polar] / (L.eps[polar] * cube(L.sig[polar]))) *
+                                    std::sqrt(L.eps[polar] / L.eps[nonpolar]);
+        e = e * (xi * xi);
+      }
+      lneps[k][j] = lneps[j][k] = std::log(e);
+    }
+  const double l1000 = std::log(1.0e3);
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i < n; ++i) {
+      const double t1 = l1000 - lneps[i][j];
+      const double t2 = t1 * t1, t3 = t1 * t2, t4 = t1 * t3, t5 = t1 * t4, t6 = t1 * t5;
+      E.ctaij[i][j] = fa0[0] + fa0[1] * t1 + fa0[2] * t2 + fa0[3] * t3 + fa0[4] * t4 + fa0[5] * t5 + fa0[6] * t6;
+    }
+  for (int j = 0; j < n; ++j)
+    for (int i = j; i < n; ++i)
+      for (int m = 0; m < 7; ++m) {
+        double sa = 0.0, sb = 0.0, sc = 0.0;
+        for (int k = m; k <= 6; ++k) {
+          double prod = 1.0;
+          for (int l = 1; l <= k - m; ++l) prod = prod * (-lneps[i][j]) * double(m + l) / double(l);
+          sa = sa + fa0[k] * prod;
+          sb = sb + fb0[k] * prod;
+          sc = sc + fc0[k] * prod;
+        }
+        E.fita[i][j][m] = E.fita[j][i][m] = sa;
+        E.fitb[i][j][m] = E.fitb[j][i][m] = sb;
+        E.fitc[i][j][m] = E.fitc[j][i][m] = sc;
+      }
+  E.cp_cgs = 1.0e4 * a.cp_ref;
+  E.eta_adim = 1.0e-1 / t.muinf;
+  E.lbda_adim = 1.0e-5 / t.laminf;
+  E.rd_adim = 1.0e-1 / (a.rho_ref * t.dinf[0]);
+}
+
+// packed symmetric index of EGLIB (0-based, i <= j)
+template <int N>
+__device__ __forceinline__ int egs(int i, int j) { return N * i - (i * (i + 1)) / 2 + j; }
+
+template <int N>
+__device__ __forceinline__ double eg_poly6(const double* f, double d1, double d2, double d3, double d4, double d5,
+                                           double d6) {
+  return f[0] + f[1] * d1 + f[2] * d2 + f[3] * d3 + f[4] * d4 + f[5] * d5 + f[6] * d6;
+}
+
+// One point: T [K], mole fractions, species cp [erg/g/K] -> eta [g/cm/s],
+// lambda [erg/cm/s/K], chi (N), rho * D [g/cm/s] as D[l*N+m].
+template <int N>
+__device__ void eg_point_dev(double T, const double* X, const double* cpms, double& eta_mix, double& tc,
+                             double* chit, double* D) {
+  constexpr int NP = N * (N + 1) / 2;
+  const double ru = 8.314e7, patmos = 1.01325e6;
+  // ---- LSPAR (IFLAG = 7)
+  const double d1 = log(T);
+  const double d2 = d1 * d1, d3 = d2 * d1, d4 = d3 * d1, d5 = d4 * d1, d6 = d5 * d1;
+  double eta[N], bin[NP], cint[N], cxi[N];
+#pragma unroll
+  for (int k = 0; k < N; ++k) {
+    const double* ce = c_eg.cofe[k];
+    eta[k] = exp(ce[0] + ce[1] * d1 + ce[2] * d2 + ce[3] * d3);
+  }
+#pragma unroll
+  for (int k = 0; k < N; ++k)
+#pragma unroll
+    for (int l = k + 1; l < N; ++l) {
+      const double* cf = c_eg.cofd[k][l];
+      const double c1 = -cf[0], c2 = -cf[1], c3 = -cf[2], c4 = -cf[3];
+      bin[egs<N>(k, l)] = exp(c1 + c2 * d1 + c3 * d2 + c4 * d3);
+    }
+  const double pi = 3.1415926535, pi32o2 = 2.7842, p2o4p2 = 4.4674, pi32 = 5.5683;
+#pragma unroll
+  for (int k = 0; k < N; ++k) {
+    double crot = 0.0;
+    cint[k] = 0.0;
+    if (c_eg.lin[k] == 1) { crot = 1.0; cint[k] = cpms[k] * (c_eg.wt[k] / ru) - 2.5; }
+    else if (c_eg.lin[k] == 2) { crot = 1.5; cint[k] = cpms[k] * (c_eg.wt[k] / ru) - 2.5; }
+    const double dr = c_eg.eps[k] / 298.0;
+    const double sqdr = sqrt(dr);
+    const double aaaa = (1.0 + pi32o2 * sqdr + p2o4p2 * dr + pi32 * (sqdr * dr));
+    const double dd = c_eg.eps[k] / T;
+    const double sqdd = sqrt(dd);
+    const double bbbb = (1.0 + pi32o2 * sqdd + p2o4p2 * dd + pi32 * (sqdd * dd));
+    const double xi = (aaaa / bbbb) * fmax(1.0, c_eg.zrot[k]);
+    cxi[k] = crot / (xi * pi);
+  }
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    const double aii = eg_poly6<N>(c_eg.fita[i][i], d1, d2, d3, d4, d5, d6);
+    double b = 5.0 * patmos * c_eg.wt[i] / (6.0 * ru * T * aii * eta[i]);
+    if (c_eg.dip[i] != 0.0) b = b * (1.0 + 2.985e3 / pow(T, 1.5));
+    bin[egs<N>(i, i)] = b;
+  }
+  // ---- EGSPAR
+  double sum = 0.0;
+#pragma unroll
+  for (int i = 0; i < N; ++i) sum = sum + X[i];
+  const double sumtr = sum, xm = sum / double(N), sss = 1.0e-16;
+  double xtr[N], ytr[N], aux[N];
+  double wwtr = 0.0;
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    xtr[i] = X[i] + sss * (xm - X[i]);
+    wwtr = wwtr + xtr[i] * c_eg.wt[i];
+  }
+#pragma unroll
+  for (int i = 0; i < N; ++i) { ytr[i] = xtr[i] * c_eg.wt[i] / wwtr; aux[i] = 0.0; }
+#pragma unroll
+  for (int i = 0; i < N; ++i)
+#pragma unroll
+    for (int j = i + 1; j < N; ++j) { aux[i] = aux[i] + ytr[j]; aux[j] = aux[j] + ytr[i]; }
+  double g[NP], an[N], tmp[N];
+  // ---- EGSE2
+  {
+    const double fac = 6.0 * ru * T / (5.0 * patmos), ccc = 5.0 / 3.0;
+#pragma unroll
+    for (int i = 0; i < N; ++i) g[egs<N>(i, i)] = xtr[i] * xtr[i] / eta[i];
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+#pragma unroll
+      for (int j = i + 1; j < N; ++j) {
+        const double a = xtr[i] * xtr[j] * fac * bin[egs<N>(i, j)] / (c_eg.wt[i] + c_eg.wt[j]);
+        const double A = c_eg.ctaij[i][j];
+        g[egs<N>(i, j)] = a * (A - ccc);
+        g[egs<N>(i, i)] = g[egs<N>(i, i)] + a * (A * c_eg.wt[j] / c_eg.wt[i] + ccc);
+        g[egs<N>(j, j)] = g[egs<N>(j, j)] + a * (A * c_eg.wt[i] / c_eg.wt[j] + ccc);
+      }
+    double dmi[N], zn[N], aaa = 0.0;
+#pragma unroll
+    for (int i = 0; i < N; ++i) dmi[i] = 1.0 / g[egs<N>(i, i)];
+#pragma unroll
+    for (int i = 0; i < N; ++i) aaa = aaa + dmi[i] * xtr[i] * xtr[i];
+#pragma unroll
+    for (int i = 0; i < N; ++i) zn[i] = dmi[i] * xtr[i];   // first step: beta_n = 0
+#pragma unroll
+    for (int i = 0; i < N; ++i) tmp[i] = g[egs<N>(i, i)] * zn[i];
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+#pragma unroll
+      for (int j = i + 1; j < N; ++j) {
+        tmp[i] = tmp[i] + g[egs<N>(i, j)] * zn[j];
+        tmp[j] = tmp[j] + g[egs<N>(i, j)] * zn[i];
+      }
+    double bbb = 0.0;
+#pragma unroll
+    for (int i = 0; i < N; ++i) bbb = bbb + zn[i] * tmp[i];
+    double dot = 0.0;
+#pragma unroll
+    for (int i = 0; i < N; ++i) dot = dot + (aaa / bbb * zn[i]) * xtr[i];   // an . beta
+    eta_mix = dot;
+  }
+  // ---- EGSLCT2
+  {
+    double beta[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      beta[i] = (2.5 + cint[i]) * xtr[i];
+      const double fac = (5.0 * patmos / (3.0 * T)) * c_eg.wt[i] / ru / eta[i];
+      g[egs<N>(i, i)] = fac * xtr[i] * xtr[i] * (1.0 + 8.0 * cxi[i] / 1.5e1) + xtr[i] * xtr[i] * cint[i] * bin[egs<N>(i, i)];
+    }
+    const double ddd = 4.0 / 3.0, eee = 4.0 / 1.5e1, fff = 2.0e1 / 3.0;
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+#pragma unroll
+      for (int j = i + 1; j < N; ++j) {
+        const double A = eg_poly6<N>(c_eg.fita[i][j], d1, d2, d3, d4, d5, d6);
+        const double B = eg_poly6<N>(c_eg.fitb[i][j], d1, d2, d3, d4, d5, d6);
+        const double wi = c_eg.wt[i], wj = c_eg.wt[j];
+        const double wwi = wi / (wi + wj), wwj = wj / (wi + wj);
+        const double wioj = 3.0 * wi / wj - 2.0, wjoi = 3.0 * wj / wi - 2.0;
+        const double tti = ddd * A * wioj * cxi[i], ttj = ddd * A * wjoi * cxi[j];
+        const double a = xtr[i] * xtr[j] * bin[egs<N>(i, j)];
+        const double bbb = wwi * wwj * (13.75 - 3.0 * B - 4.0 * A + tti + ttj);
+        const double bbj = 7.5 * wwi * wwi + (6.25 - 3.0 * B) * wwj * wwj + 4.0 * A * wwi * wwj +
+                           eee * A * cxi[i] * wwi * wwj * wioj * wioj + fff * A * cxi[j] * wwi * wwj;
+        const double bbi = 7.5 * wwj * wwj + (6.25 - 3.0 * B) * wwi * wwi + 4.0 * A * wwi * wwj +
+                           eee * A * cxi[j] * wwi * wwj * wjoi * wjoi + fff * A * cxi[i] * wwi * wwj;
+        g[egs<N>(i, j)] = -bbb * a;
+        g[egs<N>(i, i)] = g[egs<N>(i, i)] + bbj * a + a * cint[i];
+        g[egs<N>(j, j)] = g[egs<N>(j, j)] + bbi * a + a * cint[j];
+      }
+    // EGSDEC
+#pragma unroll 1
+    for (int k = 0; k < N; ++k) {
+      double w[N];
+      for (int j = 0; j < k; ++j) w[j] = g[egs<N>(j, j)] * g[egs<N>(j, k)];
+      const int kk = egs<N>(k, k);
+      for (int j = 0; j < k; ++j) g[kk] = g[kk] - w[j] * g[egs<N>(j, k)];
+      for (int j = 0; j < k; ++j)
+        for (int i = k + 1; i < N; ++i) g[egs<N>(k, i)] = g[egs<N>(k, i)] - g[egs<N>(j, i)] * w[j];
+      for (int i = k + 1; i < N; ++i) g[egs<N>(k, i)] = g[egs<N>(k, i)] / g[kk];
+    }
+    // EGSSOL
+#pragma unroll
+    for (int i = 0; i < N; ++i) an[i] = beta[i];
+#pragma unroll 1
+    for (int j = 0; j < N - 1; ++j) {
+      const double f = -an[j];
+      for (int k = j + 1; k < N; ++k) an[k] = an[k] + g[egs<N>(j, k)] * f;
+    }
+#pragma unroll
+    for (int j = 0; j < N; ++j) an[j] = an[j] / g[egs<N>(j, j)];
+#pragma unroll 1
+    for (int j = N - 1; j >= 1; --j) {
+      const double f = -an[j];
+      for (int k = 0; k < j; ++k) an[k] = an[k] + g[egs<N>(k, j)] * f;
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int i = 0; i < N; ++i) s = s + an[i] * beta[i];
+    tc = s * patmos / T;
+#pragma unroll
+    for (int i = 0; i < N; ++i) chit[i] = 0.0;
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+#pragma unroll
+      for (int j = i + 1; j < N; ++j) {
+        const double C = eg_poly6<N>(c_eg.fitc[i][j], d1, d2, d3, d4, d5, d6);
+        const double wi = c_eg.wt[i], wj = c_eg.wt[j];
+        const double term = 0.5 * bin[egs<N>(i, j)] * (6.0 * C - 5.0) * (wi * an[j] - wj * an[i]) / (wi + wj);
+        chit[i] = chit[i] + xtr[j] * term;
+        chit[j] = chit[j] - xtr[i] * term;
+      }
+  }
+  // ---- EGSDR1
+  {
+#pragma unroll
+    for (int i = 0; i < N; ++i) g[egs<N>(i, i)] = 0.0;
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+#pragma unroll
+      for (int j = i + 1; j < N; ++j) {
+        const double a = xtr[i] * xtr[j] * bin[egs<N>(i, j)];
+        g[egs<N>(i, j)] = -a;
+        g[egs<N>(i, i)] = g[egs<N>(i, i)] + a;
+        g[egs<N>(j, j)] = g[egs<N>(j, j)] + a;
+      }
+    double dmi[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) dmi[i] = aux[i] / g[egs<N>(i, i)];
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      D[i * N + i] = ytr[i] * (dmi[i] * (1.0 + ytr[i]));
+#pragma unroll
+      for (int j = i + 1; j < N; ++j) {
+        const double dij = -dmi[i] * dmi[j] * g[egs<N>(i, j)];
+        D[i * N + j] = ytr[i] * dij;
+        D[j * N + i] = ytr[j] * dij;
+      }
+    }
+    // EGSPDP
+#pragma unroll
+    for (int i = 0; i < N; ++i) tmp[i] = 0.0;
+#pragma unroll
+    for (int j = 0; j < N; ++j)
+#pragma unroll
+      for (int i = 0; i < N; ++i) tmp[i] = tmp[i] + D[i * N + j] * ytr[j];
+    const double rsumy = 1.0 / sumtr;
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      const double a = tmp[i] * rsumy;
+#pragma unroll
+      for (int j = 0; j < N; ++j) D[i * N + j] = D[i * N + j] - a;
+    }
+#pragma unroll
+    for (int i = 0; i < N; ++i) tmp[i] = 0.0;
+#pragma unroll
+    for (int j = 0; j < N; ++j)
+#pragma unroll
+      for (int i = 0; i < N; ++i) tmp[i] = tmp[i] + D[j * N + i];
+    const double aa = patmos * wwtr / (ru * T);
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+#pragma unroll
+      for (int j = 0; j < N; ++j) D[i * N + j] = aa * (D[i * N + j] - ytr[i] * rsumy * tmp[j]);
+  }
+}
+
+// Species cp of egvars (module_eg_lib.f90:170-240): NASA-7 with the linear
+// extrapolation outside [Tpolymin, Tpolymax], in erg/g/K.
+template <int N>
+__device__ __forceinline__ void eg_species_cp(double T, double* cpk) {
+#pragma unroll
+  for (int is = 0; is < N; ++is) {
+    double t1 = T * c_thd.tinf, t2 = t1 * t1, t3 = t2 * t1, t4 = t3 * t1;
+    const double* lo = c_thd.hc[is][0];
+    const double* hi = c_thd.hc[is][1];
+    double cpv;
+    if (t1 < c_thd.tpolymin[is]) {
+      t1 = c_thd.tpolymin[is]; t2 = t1 * t1; t3 = t2 * t1; t4 = t3 * t1;
+      const double cp0 = lo[0] + lo[1] * t1 + lo[2] * t2 + lo[3] * t3 + lo[4] * t4;
+      const double dcp0 = lo[1] + lo[2] * t1 * 2.0 + lo[3] * t2 * 3.0 + lo[4] * t3 * 4.0;
+      cpv = c_thd.gam2 * c_thd.Wc_i[is] * (dcp0 * (T * c_thd.tinf - c_thd.tpolymin[is]) + cp0);
+    } else if (t1 < c_thd.tpolylim[is]) {
+      cpv = c_thd.gam2 * c_thd.Wc_i[is] * (lo[0] + lo[1] * t1 + lo[2] * t2 + lo[3] * t3 + lo[4] * t4);
+    } else if (t1 < c_thd.tpolymax[is]) {
+      cpv = c_thd.gam2 * c_thd.Wc_i[is] * (hi[0] + hi[1] * t1 + hi[2] * t2 + hi[3] * t3 + hi[4] * t4);
+    } else {
+      t1 = c_thd.tpolymax[is]; t2 = t1 * t1; t3 = t2 * t1; t4 = t3 * t1;
+      const double cp0 = hi[0] + hi[1] * t1 + hi[2] * t2 + hi[3] * t3 + hi[4] * t4;
+      const double dcp0 = hi[1] + hi[2] * t1 * 2.0 + hi[3] * t2 * 3.0 + hi[4] * t3 * 4.0;
+      cpv = c_thd.gam2 * c_thd.Wc_i[is] * (dcp0 * (T * c_thd.tinf - c_thd.tpolymax[is]) + cp0);
+    }
+    cpk[is] = cpv * c_eg.cp_cgs;
+  }
+}
+
+// Pressure gradients of the EGLIB flux (fd slots 12 + 3 NRV + d) from the
+// primitive pressure P = rho T W_i.
+template <int NRV>
+__global__ void k_grad_p(Geo g, Metrics mt, const double* __restrict__ prim, double* __restrict__ fd) {
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= g.nint) return;
+  int c[3];
+  c[0] = (int)(idx % g.n[0]) + 1;
+  long long r = idx / g.n[0];
+  c[1] = (int)(r % g.n[1]) + 1;
+  c[2] = (int)(r / g.n[1]) + 1;
+  const long long nc = g.ncell;
+  const long long p = gid(g, c[0], c[1], c[2]);
+  const long long strides[3] = {1LL, (long long)g.g[0], (long long)g.g[0] * g.g[1]};
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const double di = mt.dxi[d][c[d] - 1 + g.ng];
+    fd[(12 + 3 * NRV + d) * nc + p] =
+        deriv_at(prim + PR_P * nc, p, strides[d], c[d], g.n[d], g.bnd[2 * d], g.bnd[2 * d + 1], di);
+  }
+}
+
+// egvars + the stresses, rho Y_k V_k and heat flux of viscflux_eg_xyz at
+// interior points and the ghost slabs of periodic faces.  Writes tau (6),
+// q (3) and overwrites the species gradients of fd with rho Y_k V_k.
+template <int NRV>
+__global__ void __launch_bounds__(128) k_visc_point_eg(Geo g, const double* __restrict__ v,
+                                                       const double* __restrict__ T, const double* __restrict__ W_i,
+                                                       const double* __restrict__ ha, const double* __restrict__ Xa,
+                                                       const double* __restrict__ prim, double* __restrict__ fd,
+                                                       double* __restrict__ tau, double* __restrict__ qv) {
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  int i, j, k, dom;
+  if (!slab_point(g, idx, i, j, k, dom)) return;
+  if (dom > 0 && g.bnd[dom - 1]) return;
+  const long long nc = g.ncell;
+  const long long p = gid(g, i, j, k);
+  const double rho = v[p], Tp = T[p], Wi = W_i[p];
+  const double rho_i = 1.0 / rho;
+  // ---- egvars
+  double Xe[NRV], cpk[NRV];
+  {
+    const double wrk = rho_i * (1.0 / Wi);
+#pragma unroll
+    for (int l = 0; l < NRV; ++l) Xe[l] = v[(IZEM_NIV + l) * nc + p] * wrk * c_thd.Wc_i[l];
+    eg_species_cp<NRV>(Tp, cpk);
+  }
+  double eta_eg, ct_eg, tdr[NRV], rd[NRV * NRV];
+  eg_point_dev<NRV>(Tp * c_thd.tinf, Xe, cpk, eta_eg, ct_eg, tdr, rd);
+  const double mu = eta_eg * c_eg.eta_adim;
+  const double ct = ct_eg * c_eg.lbda_adim;
+  // ---- fluxes
+  auto F = [&](int q1) -> double { return fd[(long long)(q1 - 1) * nc + p]; };
+  const double rmu = -c_thd.sqgmr * mu;
+  const double rmk = -c_thd.sqgmr * 0.0;
+  const double bulk = rmk * (F(1) + F(5) + F(9));
+  const double twothirds = 2.0 / 3.0;
+  const double sxx = bulk + twothirds * rmu * (F(1) + F(1) - (F(5) + F(9)));
+  const double sxy = rmu * (F(4) + F(2));
+  const double sxz = rmu * (F(7) + F(3));
+  const double syy = bulk + twothirds * rmu * (F(5) + F(5) - (F(1) + F(9)));
+  const double syz = rmu * (F(8) + F(6));
+  const double szz = bulk + twothirds * rmu * (F(9) + F(9) - (F(1) + F(5)));
+  const double Ps = 1.0 / prim[PR_P * nc + p];
+  const double Ts = 1.0 / Tp;
+  const double w1 = F(10) * Ts, w2 = F(11) * Ts, w3 = F(12) * Ts;
+  const double w4 = fd[(12 + 3 * NRV) * nc + p] * Ps;
+  const double w5 = fd[(13 + 3 * NRV) * nc + p] * Ps;
+  const double w6 = fd[(14 + 3 * NRV) * nc + p] * Ps;
+  double dx[NRV], dy[NRV], dz[NRV], xt[NRV];
+#pragma unroll
+  for (int l = 0; l < NRV; ++l) {
+    const double X = Xa[l * nc + p];
+    const double xy = X - v[(IZEM_NIV + l) * nc + p] * rho_i;
+    dx[l] = F(13 + 3 * l) + xy * w4;
+    dy[l] = F(14 + 3 * l) + xy * w5;
+    dz[l] = F(15 + 3 * l) + xy * w6;
+    xt[l] = X * tdr[l];
+  }
+  const double rvd0 = c_thd.rvd0;
+  const double uxs = v[nc + p] * rho_i, vys = v[2 * nc + p] * rho_i, wzs = v[3 * nc + p] * rho_i;
+  double sx = 0.0, sy = 0.0, sz = 0.0;
+#pragma unroll
+  for (int l = 0; l < NRV; ++l) {
+    double jx = 0.0, jy = 0.0, jz = 0.0;
+#pragma unroll
+    for (int m = 0; m < NRV; ++m) {
+      const double r = rd[l * NRV + m] * c_eg.rd_adim;
+      jx = jx + r * (dx[m] + xt[m] * w1);
+      jy = jy + r * (dy[m] + xt[m] * w2);
+      jz = jz + r * (dz[m] + xt[m] * w3);
+    }
+    jx = -rvd0 * jx;
+    jy = -rvd0 * jy;
+    jz = -rvd0 * jz;
+    fd[(long long)(12 + 3 * l) * nc + p] = jx;
+    fd[(long long)(13 + 3 * l) * nc + p] = jy;
+    fd[(long long)(14 + 3 * l) * nc + p] = jz;
+    const double h = ha[l * nc + p] + Tp * c_thd.Wc_i[l] * tdr[l];
+    sx = sx + jx * h;
+    sy = sy + jy * h;
+    sz = sz + jz * h;
+  }
+  const double wl = -c_thd.rlam0 * ct;
+  tau[0 * nc + p] = sxx; tau[1 * nc + p] = sxy; tau[2 * nc + p] = sxz;
+  tau[3 * nc + p] = syy; tau[4 * nc + p] = syz; tau[5 * nc + p] = szz;
+  qv[0 * nc + p] = sx + wl * F(10) + uxs * sxx + vys * sxy + wzs * sxz;
+  qv[1 * nc + p] = sy + wl * F(11) + uxs * sxy + vys * syy + wzs * syz;
+  qv[2 * nc + p] = sz + wl * F(12) + uxs * sxz + vys * syz + wzs * szz;
+}

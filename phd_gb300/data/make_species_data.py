@@ -4,8 +4,9 @@ Reads the reference's own testcase data (CHEMKIN THERMO file and tranfit.out
 transport fits) and writes them as JSON for the library and its tests:
 
   species_h2air9.json : H H2 O O2 OH H2O HO2 H2O2 N2
-                        (testcases/shockedshearlayer/tranfit.out + testcases/sod/therm.dat)
-  species_o2n2.json   : O2 N2  (testcases/sod/tranfit.out + testcases/sod/therm.dat)
+                        (testcases/shockedshearlayer/tranfit.out + testcases/sod/therm.dat,
+                         molecular parameters from testcases/sod/tran.dat)
+  species_o2n2.json   : O2 N2  (testcases/sod/tranfit.out + testcases/sod/therm.dat + tran.dat)
   species_air2.json   : two identical calorically perfect pseudo-species of air
                         (cp/R = 3.5 exactly, so gamma = 1.4), with power-law
                         transport fits giving Pr = 0.71; written from formulas,
@@ -23,12 +24,34 @@ sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 from phd_gb300.thd import read_therm, read_tranfit  # noqa: E402
 
 
-def build(tranfit_path, therm_path):
+def read_tran_dat(path, names):
+    """Molecular parameters of the CHEMKIN transport database (tran.dat):
+    geometry (0 atom, 1 linear, 2 nonlinear), Lennard-Jones well depth eps/k
+    [K], collision diameter [Angstrom], dipole moment [Debye],
+    polarizability [Angstrom^3], rotational relaxation number at 298 K."""
+    out = {}
+    with open(path) as f:
+        for line in f:
+            tok = line.split("!")[0].split()
+            if len(tok) >= 7 and tok[0] in names and tok[0] not in out:
+                out[tok[0]] = [int(tok[1])] + [float(x) for x in tok[2:7]]
+    missing = [n for n in names if n not in out]
+    if missing:
+        raise ValueError("no transport data for %s in %s" % (missing, path))
+    return out
+
+
+def build(tranfit_path, therm_path, tran_path=None):
     tf = read_tranfit(tranfit_path)
     th = read_therm(therm_path, tf["names"])
-    return {"names": tf["names"], "W_gmol": tf["W_gmol"], "cofd": tf["cofd"], "coflam": tf["coflam"],
+    d = {"names": tf["names"], "W_gmol": tf["W_gmol"], "cofd": tf["cofd"], "coflam": tf["coflam"],
             "cofeta": tf["cofeta"], "awt_gmol": tf["awt_gmol"], "kncf": tf["kncf"], "therm": th,
             "source": [os.path.relpath(tranfit_path, REF), os.path.relpath(therm_path, REF)]}
+    if tran_path:
+        lj = read_tran_dat(tran_path, tf["names"])
+        d["molecular"] = [lj[n] for n in tf["names"]]   # lin, eps/k, sigma, dipole, polarizability, zrot
+        d["source"].append(os.path.relpath(tran_path, REF))
+    return d
 
 
 def air2():
@@ -61,8 +84,10 @@ if __name__ == "__main__":
     REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     tc = os.path.join(REF, "devel-izem", "testcases")
     sets = {
-        "h2air9": build(os.path.join(tc, "shockedshearlayer", "tranfit.out"), os.path.join(tc, "sod", "therm.dat")),
-        "o2n2": build(os.path.join(tc, "sod", "tranfit.out"), os.path.join(tc, "sod", "therm.dat")),
+        "h2air9": build(os.path.join(tc, "shockedshearlayer", "tranfit.out"), os.path.join(tc, "sod", "therm.dat"),
+                        os.path.join(tc, "sod", "tran.dat")),
+        "o2n2": build(os.path.join(tc, "sod", "tranfit.out"), os.path.join(tc, "sod", "therm.dat"),
+                      os.path.join(tc, "sod", "tran.dat")),
         "air2": air2(),
     }
     for name, data in sets.items():

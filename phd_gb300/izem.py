@@ -19,7 +19,7 @@ import os
 import numpy as np
 
 from . import capi
-from .capi import IzemAdi, IzemCfg, IzemMech, IzemThd
+from .capi import IzemAdi, IzemCfg, IzemEglib, IzemMech, IzemThd
 
 _LIB = None
 LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "libizem_gpu.so")
@@ -73,6 +73,7 @@ def load_library(path=None):
         "izem_gpu_psr_batch": (C.c_int, [C.POINTER(IzemMech), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                          C.c_void_p, C.c_void_p, C.c_int, C.POINTER(C.c_float)]),
         "izem_gpu_set_surrogate": (C.c_int, [P, P, P, _dp, C.POINTER(C.c_int), C.c_int]),
+        "izem_gpu_set_eglib": (C.c_int, [P, C.POINTER(IzemEglib)]),
         "izem_gpu_chem_surrogate_stats": (C.c_int, [P, C.POINTER(C.c_longlong), C.POINTER(C.c_int),
                                                     C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     }
@@ -249,6 +250,11 @@ class IzemGPU:
         dtm = C.c_double(dtmin)
         self._check(self.lib.izem_gpu_timestep(self.h, float(DTmax), _ptr(dt4), C.byref(dtm)), "timestep")
         return dt4, dtm.value
+
+    def set_eglib(self, link):
+        """EGLIB linking data (phd_gb300.thd.eglib_link) for cfg.eglib = 1."""
+        self._eglib = link
+        self._check(self.lib.izem_gpu_set_eglib(self.h, C.byref(link)), "set_eglib")
 
     # ---- chemistry ----------------------------------------------------------
     def set_mechanism(self, mech):

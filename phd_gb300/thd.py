@@ -222,3 +222,26 @@ def thd_init(species, a=None):
             t.coflam[k][n] = species["coflam"][k][n]
             t.cofeta[k][n] = species["cofeta"][k][n]
     return t
+
+
+def eglib_link(sp):
+    """EGLIB linking data (what the Linkeg file would hold) for a species
+    set: molar masses, the molecular parameters of tran.dat, and the ln(eta)
+    and ln(D_kl at 1 atm) fits of tranfit.out (CGS, cubic in ln T)."""
+    from .capi import IzemEglib
+    names = sp["names"]
+    n = len(names)
+    if "molecular" not in sp:
+        raise ValueError("species set has no molecular parameters for EGLIB")
+    L = IzemEglib()
+    L.ns = n
+    for k in range(n):
+        lin, eps, sig, dip, pol, zrot = sp["molecular"][k]
+        L.lin[k] = int(lin)
+        L.wt[k] = sp["W_gmol"][k]
+        L.eps[k], L.sig[k], L.dip[k], L.pol[k], L.zrot[k] = eps, sig, dip, pol, zrot
+        for q in range(4):
+            L.cofe[k][q] = sp["cofeta"][k][q]
+            for l in range(n):
+                L.cofd[k][l][q] = sp["cofd"][k][l][q]
+    return L

@@ -124,3 +124,42 @@ def test_rk3_steps(name):
     v = interior(got["v"])
     ysum = v[..., 5:].sum(axis=-1) / v[..., 0]
     assert np.max(np.abs(ysum - 1.0)) <= 1e-13
+
+
+def _eglib_gpu(cfg, thd, adi, dxi, st):
+    from phd_gb300.thd import eglib_link, load_species
+    g = gpu_from(cfg, thd, adi, dxi, st)
+    g.set_eglib(eglib_link(load_species("h2air9")))
+    return g
+
+
+def test_visc_flux_eglib():
+    """viscflux_eg_xyz with EGLIB precision-1 transport (9 species)."""
+    cfg, thd, adi, dxi, st, info, orc = W.case("mix", 12, eglib=True)
+    W.perturb(st, 0.01, seed=5)
+    orc.update_primitives(st)
+    g = _eglib_gpu(cfg, thd, adi, dxi, st)
+    nv = 5 + cfg.nrv
+    fl = np.zeros((cfg.nx, cfg.ny, cfg.nz, nv), order="F")
+    orc.visc_flux(st, fl)
+    g.zero_flux()
+    g.viscflux_xyz()
+    err = W.normwise(g.flux(), fl)
+    assert np.all(err <= TOL), err
+
+
+def test_rk3_steps_eglib():
+    cfg, thd, adi, dxi, st, info, orc = W.case("mix", 12, eglib=True)
+    W.perturb(st, 0.02, seed=3)
+    orc.update_primitives(st)
+    g = _eglib_gpu(cfg, thd, adi, dxi, st)
+    for step in range(2):
+        dt4, dt = orc.timestep(st)
+        dt4g, dtg = g.timestep()
+        assert abs(dtg - dt) <= 1e-14 * abs(dt)
+        orc.rk3(st, dt)
+        g.rk3(dt)
+    got = g.download()
+    err = W.normwise(interior(got["v"]), interior(st["v"]))
+    assert np.all(err <= TOL), err
+    assert np.max(np.abs(interior(got["T"]) - interior(st["T"]))) <= TOL * np.max(st["T"])

@@ -2,6 +2,8 @@
 in well under a second)."""
 import numpy as np
 
+from phd_gb300.thd import eglib_link, load_species
+
 import oracle
 from phd_gb300 import ics
 
@@ -10,8 +12,10 @@ def _copy(state):
     return {k: np.array(v, order="F", copy=True) for k, v in state.items()}
 
 
-def case(name, n=12, seed=ics.SEED):
-    """Returns cfg, thd, adi, dxi, finalized state (oracle-closed), info."""
+def case(name, n=12, seed=ics.SEED, eglib=False):
+    """Returns cfg, thd, adi, dxi, finalized state (oracle-closed), info.
+    eglib: EGLIB precision-1 transport (cfg.eglib = 1, linking data set on
+    the oracle; the caller sets it on the GPU context)."""
     if name == "tgv":
         cfg, thd, adi, dxi, st, info = ics.tgv(n, lib_dscalar=oracle.metrics_dscalar)
     elif name == "mix":
@@ -20,7 +24,11 @@ def case(name, n=12, seed=ics.SEED):
                                                          lib_dscalar=oracle.metrics_dscalar)
     else:
         raise KeyError(name)
+    if eglib:
+        cfg.eglib = 1
     orc = oracle.Oracle(cfg, thd, adi, *dxi)
+    if eglib:
+        orc.set_eglib(eglib_link(load_species("h2air9" if name == "mix" else "o2n2")))
     orc.finalize_ic(st)
     return cfg, thd, adi, dxi, st, info, orc
 
