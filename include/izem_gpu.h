@@ -252,7 +252,8 @@ int  izem_mlp_train(izem_mlp* m, long long n, const float* x, const float* t, in
 /* Surrogate chemistry step on independent reactors with the per-cell error
  * gate (training envelope, element conservation of dY, internal-energy
  * consistency of dT, agreement with a second independently trained network
- * m2 when m2 is not NULL); rejected cells are integrated by the BDF method.
+ * m2 when m2 is not NULL, the prediction then being the mean of the two);
+ * rejected cells are integrated by the BDF method.
  * gate9 = {Tmin, Tmax, dtmin, dtmax, tol_el, tol_T_abs, tol_T_rel,
  * tol_ens_abs, tol_ens_rel}; kncf[kk][nele] element counts; stats3 =
  * {fallback cells, max BDF steps, failed cells}; ms2 = {total ms, MLP ms}. */

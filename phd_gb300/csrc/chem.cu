@@ -1093,12 +1093,19 @@ __global__ void k_decode_gate(int n, const float* out, const float* out2, int ld
   bool ok = T0 >= ga.tmin && T0 <= ga.tmax && dt[q] >= ga.dtmin && dt[q] <= ga.dtmax;
 #pragma unroll
   for (int k = 0; k < KK; ++k) dY[k] = (double)out[(size_t)q * ldo + k] * so[k] + mo[k];
-  const double dTp = (double)out[(size_t)q * ldo + KK] * so[KK] + mo[KK];
-  if (dT_pred) dT_pred[q] = dTp;
+  double dTp = (double)out[(size_t)q * ldo + KK] * so[KK] + mo[KK];
   if (out2) {
-    const double dT2 = (double)out2[(size_t)q * ldo + KK] * norm2[2 * NI + NO + KK] + norm2[2 * NI + KK];
+    // two independently trained networks: predict with their mean, and
+    // reject the cell where their temperature increments disagree
+    const float* mo2 = norm2 + 2 * NI;
+    const float* so2 = norm2 + 2 * NI + NO;
+#pragma unroll
+    for (int k = 0; k < KK; ++k) dY[k] = 0.5 * (dY[k] + ((double)out2[(size_t)q * ldo + k] * so2[k] + mo2[k]));
+    const double dT2 = (double)out2[(size_t)q * ldo + KK] * so2[KK] + mo2[KK];
     if (fabs(dT2 - dTp) > ga.tol_ens_abs + ga.tol_ens_rel * fabs(dTp)) ok = false;
+    dTp = 0.5 * (dTp + dT2);
   }
+  if (dT_pred) dT_pred[q] = dTp;
   // element residuals
   for (int e = 0; e < nele && ok; ++e) {
     double r = 0.0, sc = 0.0;

@@ -533,7 +533,8 @@ int izem_mlp_train(izem_mlp* m, long long n, const float* x, const float* t, int
 // izem_gpu_psr_batch): MLP inference in chunks, the error gate, and the BDF
 // integrator on every rejected cell.  gate9 = {Tmin, Tmax, dtmin, dtmax,
 // tol_el, tol_T_abs, tol_T_rel, tol_ens_abs, tol_ens_rel}; m2 (optional) is
-// a second, independently trained network whose dT must agree with m's;
+// a second, independently trained network: the prediction is the mean of
+// the two, and cells where their dT disagree are rejected;
 // kncf = element counts [kk][nele].
 // dT_pred (optional, device or host like the other arrays) receives the raw
 // network temperature increment.  stats3 = {fallback cells, max BDF steps,

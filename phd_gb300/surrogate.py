@@ -173,8 +173,9 @@ class Surrogate:
 
     def chem_step(self, mech, T, rho, Y, dt, gate, partner=None):
         """Surrogate + gate + BDF fallback on independent reactors (host
-        arrays updated in place).  partner: a second Surrogate whose dT must
-        agree.  Returns dict with fallback count, times and the raw
+        arrays updated in place).  partner: a second Surrogate; the
+        prediction is the mean of the two and cells where their dT disagree
+        are rejected.  Returns dict with fallback count, times and the raw
         predicted dT."""
         kncf = np.ascontiguousarray(np.array(load_species("h2air9")["kncf"], dtype=np.int32))
         g7 = np.ascontiguousarray(np.array(gate, dtype=np.float64))
@@ -192,7 +193,7 @@ class Surrogate:
 
 
 # Tmin, Tmax, dtmin, dtmax, tol_el, tol_T_abs [K], tol_T_rel, tol_ens_abs [K], tol_ens_rel
-DEFAULT_GATE = (800.0, 2400.0, 1e-8, 1e-6, 2e-3, 2.0, 0.02, 1.0, 0.005)
+DEFAULT_GATE = (800.0, 2400.0, 1e-8, 1e-6, 2e-3, 2.0, 0.003, 1.0, 0.002)
 
 
 def train_ensemble(mech, n=1 << 22, seed=31, epochs=30, batch=4096, lr=1e-3, members=2, log=None):
