@@ -30,6 +30,24 @@ namespace {
 
 __constant__ izem_mech c_mech_dev;
 __constant__ int c_need_eqk_dev;   // some reaction uses the equilibrium reverse rate
+
+// Mechanism constants of the device right-hand side (ck_fun_fast).
+struct ChemFast {
+  double wt_inv[IZEM_NSMAX];          // 1 / W_k
+  double ru_wt[IZEM_NSMAX];           // RU / W_k
+  double troe_inv[IZEM_MAXREAC][2];   // 1 / T***, 1 / T*
+};
+__constant__ ChemFast c_fast_dev;
+#ifdef IZEM_CHEM_HOST_TEST
+ChemFast c_fast_host;
+#ifdef __CUDA_ARCH__
+#define c_fast c_fast_dev
+#else
+#define c_fast c_fast_host
+#endif
+#else
+#define c_fast c_fast_dev
+#endif
 #ifdef IZEM_CHEM_HOST_TEST
 izem_mech c_mech_host;
 int c_need_eqk_host = 0;
@@ -186,6 +204,139 @@ HD void ck_fun(double rho, const double* z, double* zp) {
     sum = sum + h[k] * wdot[k] * c_mech.wt[k] + (-c_mech.ru * z[0]) * wdot[k];
   }
   zp[0] = -sum / (rho * cvb);
+}
+
+
+inline ChemFast chem_fast_constants(const izem_mech& m) {
+  ChemFast f{};
+  for (int k = 0; k < m.kk && k < IZEM_NSMAX; ++k) {
+    f.wt_inv[k] = 1.0 / m.wt[k];
+    f.ru_wt[k] = m.ru / m.wt[k];
+  }
+  for (int i = 0; i < m.ii && i < IZEM_MAXREAC; ++i) {
+    f.troe_inv[i][0] = m.troe[i][1] != 0.0 ? 1.0 / m.troe[i][1] : 0.0;
+    f.troe_inv[i][1] = m.troe[i][2] != 0.0 ? 1.0 / m.troe[i][2] : 0.0;
+  }
+  return f;
+}
+
+// The constant-volume reactor right-hand side of ck_fun with the divisions
+// by T, by the molar masses and by the Troe temperatures replaced by
+// multiplications with reciprocals, and 10^x / log10 by exp / log: the same
+// CHEMKIN expressions (CKCVBS, CKHMS, CKRATT, CKRATX, CKWYR) with different
+// rounding (a few ulp per term) and about a sixth of the FP64 instructions
+// of the divisions.  The BDF kernels call this one; ck_fun above keeps the
+// reference's operation order for the host build that is compared with the
+// oracle bit for bit.
+template <int KK>
+HD void ck_fun_fast(double rho, const double* z, double* zp) {
+  constexpr double kLn10 = 2.302585092994045684, kInvLn10 = 0.4342944819032518277;
+  const double T = z[0];
+  const double* Y = z + 1;
+  const double Tinv = 1.0 / T;
+  const double alogt = log(T);
+  const double T2 = T * T, T3 = T * T2, T4 = T2 * T2;
+  const double rut = T * c_mech.ru;
+  double cv = 0.0, h[KK], C[KK], wdot[KK];
+  double ctot = 0.0;
+#pragma unroll
+  for (int k = 0; k < KK; ++k) {
+    const double* a = c_mech.a[k][T > c_mech.tmid[k] ? 1 : 0];
+    const double cps = a[0] + T * a[1] + T2 * a[2] + T3 * a[3] + T4 * a[4];
+    cv = cv + Y[k] * (c_fast.ru_wt[k] * (cps - 1.0));
+    const double hs = a[0] + (0.5 * T) * a[1] + (T2 * (1.0 / 3.0)) * a[2] + (0.25 * T3) * a[3] + (0.2 * T4) * a[4];
+    h[k] = rut * (hs + a[5] * Tinv) * c_fast.wt_inv[k];
+    C[k] = rho * Y[k] * c_fast.wt_inv[k];
+    ctot = ctot + C[k];
+    wdot[k] = 0.0;
+  }
+  double smh[KK];
+  if (c_need_eqk) {
+#pragma unroll
+    for (int k = 0; k < KK; ++k) {
+      const double* a = c_mech.a[k][T > c_mech.tmid[k] ? 1 : 0];
+      const double sv = (alogt - 1.0) * a[0] + (0.5 * T) * a[1] + (T2 * (1.0 / 6.0)) * a[2] +
+                        (T3 * (1.0 / 12.0)) * a[3] + (T4 * 0.05) * a[4];
+      smh[k] = sv + a[6] - a[5] * Tinv;
+    }
+  }
+  double rop[IZEM_MAXREAC];
+  const int ii = c_mech.ii;
+  for (int i = 0; i < ii; ++i) {
+    double rkft = c_mech.par[i][0] * exp(c_mech.par[i][1] * alogt - c_mech.par[i][2] * Tinv);
+    double rkrt = 0.0;
+    const int rv = c_mech.rev[i];
+    if (rv == 1) {
+      double sumsmh = 0.0;
+      int nus = 0;
+      for (int n = 0; n < MXSP; ++n) {
+        const int kk = c_mech.nuk[i][n];
+        if (kk >= 0) sumsmh = sumsmh + double(c_mech.nu[i][n]) * smh[kk];
+        nus += c_mech.nu[i][n];
+      }
+      double eqk = sumsmh != 0.0 ? exp(fmin(sumsmh, 690.77552789821368)) : 1.0;
+      eqk = eqk * powi(c_mech.patm * Tinv / c_mech.ru, nus);
+      rkrt = rkft / fmax(eqk, 1.0e-300);
+    } else if (rv == 2) {
+      rkrt = c_mech.rpar[i][0] * exp(c_mech.rpar[i][1] * alogt - c_mech.rpar[i][2] * Tinv);
+    }
+    double ctb = 1.0;
+    if (c_mech.thb[i]) {
+      ctb = ctot;
+      for (int k = 0; k < KK; ++k)
+        if (c_mech.eff[i][k] != 1.0) ctb = ctb + (c_mech.eff[i][k] - 1.0) * C[k];
+    }
+    const int fo = c_mech.fall[i];
+    if (fo) {
+      const double rklow = c_mech.low[i][0] * exp(c_mech.low[i][1] * alogt - c_mech.low[i][2] * Tinv);
+      const double pr = rklow * ctb / rkft;
+      ctb = 1.0;
+      double pcor = pr / (1.0 + pr);
+      if (fo > 1) {
+        const double prlog = log(fmax(pr, 1.0e-300)) * kInvLn10;
+        const double ta = c_mech.troe[i][0];
+        double fcent = (1.0 - ta) * exp(-T * c_fast.troe_inv[i][0]) + ta * exp(-T * c_fast.troe_inv[i][1]);
+        if (fo == 4) fcent = fcent + exp(-c_mech.troe[i][3] * Tinv);
+        const double fclog = log(fmax(fcent, 1.0e-300)) * kInvLn10;
+        const double xn = 0.75 - 1.27 * fclog;
+        const double cprlog = prlog - (0.4 + 0.67 * fclog);
+        const double q = cprlog / (xn - 0.14 * cprlog);
+        const double flog = fclog / (1.0 + q * q);
+        pcor = exp(flog * kLn10) * pcor;
+      }
+      rkft = rkft * pcor;
+      rkrt = rkrt * pcor;
+    }
+    rkft = rkft * ctb;
+    rkrt = rkrt * ctb;
+    double rkf = 0.0, rkr = 0.0;
+    if (c_mech.nu[i][0] != 0) {
+      rkf = rkft * powi(C[c_mech.nuk[i][0]], -c_mech.nu[i][0]);
+      rkr = rkrt * powi(C[c_mech.nuk[i][3]], c_mech.nu[i][3]);
+      if (c_mech.nuk[i][1] >= 0) {
+        rkf = rkf * powi(C[c_mech.nuk[i][1]], -c_mech.nu[i][1]);
+        if (c_mech.nuk[i][2] >= 0) rkf = rkf * powi(C[c_mech.nuk[i][2]], -c_mech.nu[i][2]);
+      }
+      if (c_mech.nuk[i][4] >= 0) {
+        rkr = rkr * powi(C[c_mech.nuk[i][4]], c_mech.nu[i][4]);
+        if (c_mech.nuk[i][5] >= 0) rkr = rkr * powi(C[c_mech.nuk[i][5]], c_mech.nu[i][5]);
+      }
+    }
+    rop[i] = rkf - rkr;
+  }
+  for (int n = 0; n < MXSP; ++n)
+    for (int i = 0; i < ii; ++i) {
+      const int k = c_mech.nuk[i][n];
+      if (k >= 0) wdot[k] = wdot[k] + rop[i] * double(c_mech.nu[i][n]);
+    }
+  const double rho_i = 1.0 / rho;
+  double sum = 0.0;
+#pragma unroll
+  for (int k = 0; k < KK; ++k) {
+    zp[k + 1] = wdot[k] * c_mech.wt[k] * rho_i;
+    sum = sum + h[k] * wdot[k] * c_mech.wt[k] + (-rut) * wdot[k];
+  }
+  zp[0] = -sum / (rho * cv);
 }
 
 // ------------------------------------------------------------- DVODE -------
@@ -913,7 +1064,7 @@ __device__ __forceinline__ void rc_drive(unsigned n, unsigned* counter, Load loa
     bool need = rc_advance<N>(r);
     if (need && ++nfun > kMaxFun) { r.istate = -99; need = false; }
     if (need) {
-      ck_fun<KK>(r.rho, r.y, r.fo);
+      ck_fun_fast<KK>(r.rho, r.y, r.fo);
     } else {
       store(q, r);
       active = false;
@@ -1187,6 +1338,8 @@ int chem_grid(int* blocks) {
 cudaError_t chem_upload_mech(const izem_mech* m) {
   cudaError_t e = cudaMemcpyToSymbol(c_mech_dev, m, sizeof(izem_mech));
   if (e != cudaSuccess) return e;
+  ChemFast f = chem_fast_constants(*m);
+  if ((e = cudaMemcpyToSymbol(c_fast_dev, &f, sizeof(ChemFast))) != cudaSuccess) return e;
   int need = 0;
   for (int i = 0; i < m->ii; ++i) need |= (m->rev[i] == 1);
   return cudaMemcpyToSymbol(c_need_eqk_dev, &need, sizeof(int));

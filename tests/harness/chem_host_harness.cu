@@ -20,3 +20,15 @@ extern "C" void host_psr(const izem_mech* m, int n, double* T, const double* rho
     for (int k = 0; k < 9; ++k) Y[q * 9 + k] = z[1 + k];
   }
 }
+
+// The device right-hand side with reciprocals (ck_fun_fast) next to the
+// reference-order one (ck_fun), both on the host.
+extern "C" void host_fun_pair(const izem_mech* m, int n, const double* rho, const double* z, double* zp_ref,
+                              double* zp_fast) {
+  c_mech_host = *m;
+  c_fast_host = chem_fast_constants(*m);
+  for (int q = 0; q < n; ++q) {
+    ck_fun<9>(rho[q], z + 10 * q, zp_ref + 10 * q);
+    ck_fun_fast<9>(rho[q], z + 10 * q, zp_fast + 10 * q);
+  }
+}
