@@ -35,6 +35,20 @@ struct DevEg {
   double fitc[IZEM_NSMAX][IZEM_NSMAX][7];
   // egvars scalings (module_eg_lib.f90:140-145)
   double cp_cgs, eta_adim, lbda_adim, rd_adim;
+  // species and pair constants of the device evaluation (molar masses,
+  // Parker's reference factor, EGLIB's fixed coefficients folded together)
+  double wtru[IZEM_NSMAX];        // W_k / RU
+  double cx[IZEM_NSMAX];          // CROT / (AAAA max(1, ZROT) pi): cxi = cx * BBBB
+  double bdiag[IZEM_NSMAX];       // 5 PATMOS W / (6 RU): D_int,kk = bdiag / (T A*_kk eta_k)
+  double lfac[IZEM_NSMAX];        // 5 PATMOS W / (3 RU): FAC of Lambda_[e] = lfac / (T eta_k)
+  double wsinv[IZEM_NSMAX][IZEM_NSMAX];                    // 1 / (W_i + W_j)
+  double hoff[IZEM_NSMAX][IZEM_NSMAX];                     // A*(1000) - 5/3
+  double hdi[IZEM_NSMAX][IZEM_NSMAX], hdj[IZEM_NSMAX][IZEM_NSMAX];   // A* W_j/W_i + 5/3, A* W_i/W_j + 5/3
+  double p1[IZEM_NSMAX][IZEM_NSMAX];                       // wwi wwj
+  double tti[IZEM_NSMAX][IZEM_NSMAX], ttj[IZEM_NSMAX][IZEM_NSMAX];   // 4/3 wioj, 4/3 wjoi
+  double c1j[IZEM_NSMAX][IZEM_NSMAX], c2j[IZEM_NSMAX][IZEM_NSMAX], c3j[IZEM_NSMAX][IZEM_NSMAX];
+  double c1i[IZEM_NSMAX][IZEM_NSMAX], c2i[IZEM_NSMAX][IZEM_NSMAX], c3i[IZEM_NSMAX][IZEM_NSMAX];
+  double c4[IZEM_NSMAX][IZEM_NSMAX];
 };
 
 static __constant__ DevEg c_eg;
@@ -102,6 +116,38 @@ inline void eg_prepare(const izem_eglib& L, const izem_thd& t, const izem_adi& a
         E.fitb[i][j][m] = E.fitb[j][i][m] = sb;
         E.fitc[i][j][m] = E.fitc[j][i][m] = sc;
       }
+  const double ru = 8.314e7, patmos = 1.01325e6, pi = 3.1415926535;
+  for (int k = 0; k < n; ++k) {
+    const double crot = L.lin[k] == 1 ? 1.0 : (L.lin[k] == 2 ? 1.5 : 0.0);
+    const double dr = L.eps[k] / 298.0, sqdr = std::sqrt(dr);
+    const double aaaa = 1.0 + 2.7842 * sqdr + 4.4674 * dr + 5.5683 * (sqdr * dr);
+    E.wtru[k] = L.wt[k] / ru;
+    E.cx[k] = crot / (aaaa * std::max(1.0, L.zrot[k]) * pi);
+    E.bdiag[k] = 5.0 * patmos * L.wt[k] / (6.0 * ru);
+    E.lfac[k] = 5.0 * patmos * L.wt[k] / (3.0 * ru);
+  }
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) {
+      const double wi = L.wt[i], wj = L.wt[j];
+      const double wwi = wi / (wi + wj), wwj = wj / (wi + wj);
+      const double wioj = 3.0 * wi / wj - 2.0, wjoi = 3.0 * wj / wi - 2.0;
+      const double A = E.ctaij[i][j];
+      E.wsinv[i][j] = 1.0 / (wi + wj);
+      E.hoff[i][j] = A - 5.0 / 3.0;
+      E.hdi[i][j] = A * wj / wi + 5.0 / 3.0;
+      E.hdj[i][j] = A * wi / wj + 5.0 / 3.0;
+      const double p1 = wwi * wwj;
+      E.p1[i][j] = p1;
+      E.tti[i][j] = 4.0 / 3.0 * wioj;
+      E.ttj[i][j] = 4.0 / 3.0 * wjoi;
+      E.c1j[i][j] = 7.5 * wwi * wwi;
+      E.c2j[i][j] = wwj * wwj;
+      E.c3j[i][j] = 4.0 / 15.0 * p1 * wioj * wioj;
+      E.c1i[i][j] = 7.5 * wwj * wwj;
+      E.c2i[i][j] = wwi * wwi;
+      E.c3i[i][j] = 4.0 / 15.0 * p1 * wjoi * wjoi;
+      E.c4[i][j] = 20.0 / 3.0 * p1;
+    }
   E.cp_cgs = 1.0e4 * a.cp_ref;
   E.eta_adim = 1.0e-1 / t.muinf;
   E.lbda_adim = 1.0e-5 / t.laminf;
@@ -119,57 +165,52 @@ __device__ __forceinline__ double eg_poly6(const double* f, double d1, double d2
 }
 
 // One point: T [K], mole fractions, species cp [erg/g/K] -> eta [g/cm/s],
-// lambda [erg/cm/s/K], chi (N), rho * D [g/cm/s] as D[l*N+m].
+// lambda [erg/cm/s/K], chi (N), rho * D [g/cm/s] as D[l*N+m].  The same
+// EGLIB formulas as the routines named above, with the factors that depend
+// only on the species (molar masses, EGLIB's fixed coefficients, Parker's
+// reference value) folded on the host, reciprocals instead of divisions,
+// 1/eta from exp(-ln eta), and the packed factorisation with its scaling
+// applied in place: the same quantities up to rounding.
 template <int N>
 __device__ void eg_point_dev(double T, const double* X, const double* cpms, double& eta_mix, double& tc,
                              double* chit, double* D) {
   constexpr int NP = N * (N + 1) / 2;
-  const double ru = 8.314e7, patmos = 1.01325e6;
-  // ---- LSPAR (IFLAG = 7)
+  const double patmos = 1.01325e6, ru = 8.314e7;
+  const double Tinv = 1.0 / T;
+  // ---- LSPAR (IFLAG = 7): pure viscosities, reciprocal binary diffusion
+  // coefficients, internal heat capacities, Parker's rotational relaxation,
+  // internal self-diffusion on the diagonal of BIN
   const double d1 = log(T);
   const double d2 = d1 * d1, d3 = d2 * d1, d4 = d3 * d1, d5 = d4 * d1, d6 = d5 * d1;
-  double eta[N], bin[NP], cint[N], cxi[N];
+  double eta_i[N], bin[NP], cint[N], cxi[N];
 #pragma unroll
   for (int k = 0; k < N; ++k) {
     const double* ce = c_eg.cofe[k];
-    eta[k] = exp(ce[0] + ce[1] * d1 + ce[2] * d2 + ce[3] * d3);
+    eta_i[k] = exp(-(ce[0] + ce[1] * d1 + ce[2] * d2 + ce[3] * d3));   // 1 / eta_k
   }
 #pragma unroll
   for (int k = 0; k < N; ++k)
 #pragma unroll
     for (int l = k + 1; l < N; ++l) {
       const double* cf = c_eg.cofd[k][l];
-      const double c1 = -cf[0], c2 = -cf[1], c3 = -cf[2], c4 = -cf[3];
-      bin[egs<N>(k, l)] = exp(c1 + c2 * d1 + c3 * d2 + c4 * d3);
+      bin[egs<N>(k, l)] = exp(-(cf[0] + cf[1] * d1 + cf[2] * d2 + cf[3] * d3));
     }
-  const double pi = 3.1415926535, pi32o2 = 2.7842, p2o4p2 = 4.4674, pi32 = 5.5683;
+  const double pfac = 1.0 + 2.985e3 / (T * sqrt(T));   // polar correction of D_int
 #pragma unroll
   for (int k = 0; k < N; ++k) {
-    double crot = 0.0;
-    cint[k] = 0.0;
-    if (c_eg.lin[k] == 1) { crot = 1.0; cint[k] = cpms[k] * (c_eg.wt[k] / ru) - 2.5; }
-    else if (c_eg.lin[k] == 2) { crot = 1.5; cint[k] = cpms[k] * (c_eg.wt[k] / ru) - 2.5; }
-    const double dr = c_eg.eps[k] / 298.0;
-    const double sqdr = sqrt(dr);
-    const double aaaa = (1.0 + pi32o2 * sqdr + p2o4p2 * dr + pi32 * (sqdr * dr));
-    const double dd = c_eg.eps[k] / T;
-    const double sqdd = sqrt(dd);
-    const double bbbb = (1.0 + pi32o2 * sqdd + p2o4p2 * dd + pi32 * (sqdd * dd));
-    const double xi = (aaaa / bbbb) * fmax(1.0, c_eg.zrot[k]);
-    cxi[k] = crot / (xi * pi);
+    cint[k] = c_eg.lin[k] ? cpms[k] * c_eg.wtru[k] - 2.5 : 0.0;
+    const double dd = c_eg.eps[k] * Tinv, sqdd = sqrt(dd);
+    cxi[k] = c_eg.cx[k] * (1.0 + 2.7842 * sqdd + 4.4674 * dd + 5.5683 * (sqdd * dd));
+    const double aii = eg_poly6<N>(c_eg.fita[k][k], d1, d2, d3, d4, d5, d6);
+    double b = c_eg.bdiag[k] * Tinv * eta_i[k] / aii;
+    if (c_eg.dip[k] != 0.0) b = b * pfac;
+    bin[egs<N>(k, k)] = b;
   }
-#pragma unroll
-  for (int i = 0; i < N; ++i) {
-    const double aii = eg_poly6<N>(c_eg.fita[i][i], d1, d2, d3, d4, d5, d6);
-    double b = 5.0 * patmos * c_eg.wt[i] / (6.0 * ru * T * aii * eta[i]);
-    if (c_eg.dip[i] != 0.0) b = b * (1.0 + 2.985e3 / pow(T, 1.5));
-    bin[egs<N>(i, i)] = b;
-  }
-  // ---- EGSPAR
+  // ---- EGSPAR: regularised mole and mass fractions
   double sum = 0.0;
 #pragma unroll
   for (int i = 0; i < N; ++i) sum = sum + X[i];
-  const double sumtr = sum, xm = sum / double(N), sss = 1.0e-16;
+  const double xm = sum * (1.0 / double(N)), sss = 1.0e-16;
   double xtr[N], ytr[N], aux[N];
   double wwtr = 0.0;
 #pragma unroll
@@ -177,37 +218,34 @@ __device__ void eg_point_dev(double T, const double* X, const double* cpms, doub
     xtr[i] = X[i] + sss * (xm - X[i]);
     wwtr = wwtr + xtr[i] * c_eg.wt[i];
   }
+  const double wwtr_i = 1.0 / wwtr;
+  double ysum = 0.0;
 #pragma unroll
-  for (int i = 0; i < N; ++i) { ytr[i] = xtr[i] * c_eg.wt[i] / wwtr; aux[i] = 0.0; }
+  for (int i = 0; i < N; ++i) { ytr[i] = xtr[i] * c_eg.wt[i] * wwtr_i; ysum = ysum + ytr[i]; }
 #pragma unroll
-  for (int i = 0; i < N; ++i)
-#pragma unroll
-    for (int j = i + 1; j < N; ++j) { aux[i] = aux[i] + ytr[j]; aux[j] = aux[j] + ytr[i]; }
-  double g[NP], an[N], tmp[N];
-  // ---- EGSE2
+  for (int i = 0; i < N; ++i) aux[i] = ysum - ytr[i];
+  double g[NP], an[N];
+  // ---- EGSE2: matrix H with the 1000 K A*, one conjugate-gradient step
   {
-    const double fac = 6.0 * ru * T / (5.0 * patmos), ccc = 5.0 / 3.0;
+    const double fac = (6.0 * ru / (5.0 * patmos)) * T;
 #pragma unroll
-    for (int i = 0; i < N; ++i) g[egs<N>(i, i)] = xtr[i] * xtr[i] / eta[i];
+    for (int i = 0; i < N; ++i) g[egs<N>(i, i)] = xtr[i] * xtr[i] * eta_i[i];
 #pragma unroll
     for (int i = 0; i < N; ++i)
 #pragma unroll
       for (int j = i + 1; j < N; ++j) {
-        const double a = xtr[i] * xtr[j] * fac * bin[egs<N>(i, j)] / (c_eg.wt[i] + c_eg.wt[j]);
-        const double A = c_eg.ctaij[i][j];
-        g[egs<N>(i, j)] = a * (A - ccc);
-        g[egs<N>(i, i)] = g[egs<N>(i, i)] + a * (A * c_eg.wt[j] / c_eg.wt[i] + ccc);
-        g[egs<N>(j, j)] = g[egs<N>(j, j)] + a * (A * c_eg.wt[i] / c_eg.wt[j] + ccc);
+        const double a = xtr[i] * xtr[j] * fac * bin[egs<N>(i, j)] * c_eg.wsinv[i][j];
+        g[egs<N>(i, j)] = a * c_eg.hoff[i][j];
+        g[egs<N>(i, i)] = g[egs<N>(i, i)] + a * c_eg.hdi[i][j];
+        g[egs<N>(j, j)] = g[egs<N>(j, j)] + a * c_eg.hdj[i][j];
       }
-    double dmi[N], zn[N], aaa = 0.0;
+    double zn[N], tmp[N], aaa = 0.0;
 #pragma unroll
-    for (int i = 0; i < N; ++i) dmi[i] = 1.0 / g[egs<N>(i, i)];
-#pragma unroll
-    for (int i = 0; i < N; ++i) aaa = aaa + dmi[i] * xtr[i] * xtr[i];
-#pragma unroll
-    for (int i = 0; i < N; ++i) zn[i] = dmi[i] * xtr[i];   // first step: beta_n = 0
-#pragma unroll
-    for (int i = 0; i < N; ++i) tmp[i] = g[egs<N>(i, i)] * zn[i];
+    for (int i = 0; i < N; ++i) {
+      zn[i] = xtr[i] / g[egs<N>(i, i)];
+      aaa = aaa + zn[i] * xtr[i];
+      tmp[i] = g[egs<N>(i, i)] * zn[i];
+    }
 #pragma unroll
     for (int i = 0; i < N; ++i)
 #pragma unroll
@@ -215,74 +253,68 @@ __device__ void eg_point_dev(double T, const double* X, const double* cpms, doub
         tmp[i] = tmp[i] + g[egs<N>(i, j)] * zn[j];
         tmp[j] = tmp[j] + g[egs<N>(i, j)] * zn[i];
       }
-    double bbb = 0.0;
+    double bbb = 0.0, dot = 0.0;
 #pragma unroll
-    for (int i = 0; i < N; ++i) bbb = bbb + zn[i] * tmp[i];
-    double dot = 0.0;
-#pragma unroll
-    for (int i = 0; i < N; ++i) dot = dot + (aaa / bbb * zn[i]) * xtr[i];   // an . beta
-    eta_mix = dot;
+    for (int i = 0; i < N; ++i) { bbb = bbb + zn[i] * tmp[i]; dot = dot + zn[i] * xtr[i]; }
+    eta_mix = aaa / bbb * dot;
   }
-  // ---- EGSLCT2
+  // ---- EGSLCT2: matrix Lambda_[e], factorisation, solve
   {
     double beta[N];
 #pragma unroll
     for (int i = 0; i < N; ++i) {
       beta[i] = (2.5 + cint[i]) * xtr[i];
-      const double fac = (5.0 * patmos / (3.0 * T)) * c_eg.wt[i] / ru / eta[i];
-      g[egs<N>(i, i)] = fac * xtr[i] * xtr[i] * (1.0 + 8.0 * cxi[i] / 1.5e1) + xtr[i] * xtr[i] * cint[i] * bin[egs<N>(i, i)];
+      const double xx = xtr[i] * xtr[i];
+      g[egs<N>(i, i)] = c_eg.lfac[i] * Tinv * eta_i[i] * xx * (1.0 + (8.0 / 15.0) * cxi[i]) + xx * cint[i] * bin[egs<N>(i, i)];
     }
-    const double ddd = 4.0 / 3.0, eee = 4.0 / 1.5e1, fff = 2.0e1 / 3.0;
 #pragma unroll
     for (int i = 0; i < N; ++i)
 #pragma unroll
       for (int j = i + 1; j < N; ++j) {
         const double A = eg_poly6<N>(c_eg.fita[i][j], d1, d2, d3, d4, d5, d6);
         const double B = eg_poly6<N>(c_eg.fitb[i][j], d1, d2, d3, d4, d5, d6);
-        const double wi = c_eg.wt[i], wj = c_eg.wt[j];
-        const double wwi = wi / (wi + wj), wwj = wj / (wi + wj);
-        const double wioj = 3.0 * wi / wj - 2.0, wjoi = 3.0 * wj / wi - 2.0;
-        const double tti = ddd * A * wioj * cxi[i], ttj = ddd * A * wjoi * cxi[j];
         const double a = xtr[i] * xtr[j] * bin[egs<N>(i, j)];
-        const double bbb = wwi * wwj * (13.75 - 3.0 * B - 4.0 * A + tti + ttj);
-        const double bbj = 7.5 * wwi * wwi + (6.25 - 3.0 * B) * wwj * wwj + 4.0 * A * wwi * wwj +
-                           eee * A * cxi[i] * wwi * wwj * wioj * wioj + fff * A * cxi[j] * wwi * wwj;
-        const double bbi = 7.5 * wwj * wwj + (6.25 - 3.0 * B) * wwi * wwi + 4.0 * A * wwi * wwj +
-                           eee * A * cxi[j] * wwi * wwj * wjoi * wjoi + fff * A * cxi[i] * wwi * wwj;
+        const double b3 = 6.25 - 3.0 * B;
+        const double bbb = c_eg.p1[i][j] * (13.75 - 3.0 * B - 4.0 * A + A * (c_eg.tti[i][j] * cxi[i] + c_eg.ttj[i][j] * cxi[j]));
+        const double a4 = 4.0 * A * c_eg.p1[i][j];
+        const double bbj = c_eg.c1j[i][j] + b3 * c_eg.c2j[i][j] + a4 + A * (c_eg.c3j[i][j] * cxi[i] + c_eg.c4[i][j] * cxi[j]);
+        const double bbi = c_eg.c1i[i][j] + b3 * c_eg.c2i[i][j] + a4 + A * (c_eg.c3i[i][j] * cxi[j] + c_eg.c4[i][j] * cxi[i]);
         g[egs<N>(i, j)] = -bbb * a;
-        g[egs<N>(i, i)] = g[egs<N>(i, i)] + bbj * a + a * cint[i];
-        g[egs<N>(j, j)] = g[egs<N>(j, j)] + bbi * a + a * cint[j];
+        g[egs<N>(i, i)] = g[egs<N>(i, i)] + a * (bbj + cint[i]);
+        g[egs<N>(j, j)] = g[egs<N>(j, j)] + a * (bbi + cint[j]);
       }
-    // EGSDEC
+    // EGSDEC (packed LDL^T) and EGSSOL
 #pragma unroll 1
     for (int k = 0; k < N; ++k) {
       double w[N];
       for (int j = 0; j < k; ++j) w[j] = g[egs<N>(j, j)] * g[egs<N>(j, k)];
       const int kk = egs<N>(k, k);
-      for (int j = 0; j < k; ++j) g[kk] = g[kk] - w[j] * g[egs<N>(j, k)];
-      for (int j = 0; j < k; ++j)
-        for (int i = k + 1; i < N; ++i) g[egs<N>(k, i)] = g[egs<N>(k, i)] - g[egs<N>(j, i)] * w[j];
-      for (int i = k + 1; i < N; ++i) g[egs<N>(k, i)] = g[egs<N>(k, i)] / g[kk];
+      double gkk = g[kk];
+      for (int j = 0; j < k; ++j) gkk = gkk - w[j] * g[egs<N>(j, k)];
+      g[kk] = gkk;
+      const double rk = 1.0 / gkk;
+      for (int i = k + 1; i < N; ++i) {
+        double gki = g[egs<N>(k, i)];
+        for (int j = 0; j < k; ++j) gki = gki - g[egs<N>(j, i)] * w[j];
+        g[egs<N>(k, i)] = gki * rk;
+      }
     }
-    // EGSSOL
 #pragma unroll
     for (int i = 0; i < N; ++i) an[i] = beta[i];
-#pragma unroll 1
-    for (int j = 0; j < N - 1; ++j) {
-      const double f = -an[j];
-      for (int k = j + 1; k < N; ++k) an[k] = an[k] + g[egs<N>(j, k)] * f;
-    }
+#pragma unroll
+    for (int j = 0; j < N - 1; ++j)
+#pragma unroll
+      for (int k = j + 1; k < N; ++k) an[k] = an[k] - g[egs<N>(j, k)] * an[j];
 #pragma unroll
     for (int j = 0; j < N; ++j) an[j] = an[j] / g[egs<N>(j, j)];
-#pragma unroll 1
-    for (int j = N - 1; j >= 1; --j) {
-      const double f = -an[j];
-      for (int k = 0; k < j; ++k) an[k] = an[k] + g[egs<N>(k, j)] * f;
-    }
+#pragma unroll
+    for (int j = N - 1; j >= 1; --j)
+#pragma unroll
+      for (int k = 0; k < j; ++k) an[k] = an[k] - g[egs<N>(k, j)] * an[j];
     double s = 0.0;
 #pragma unroll
     for (int i = 0; i < N; ++i) s = s + an[i] * beta[i];
-    tc = s * patmos / T;
+    tc = s * patmos * Tinv;
 #pragma unroll
     for (int i = 0; i < N; ++i) chit[i] = 0.0;
 #pragma unroll
@@ -290,49 +322,45 @@ __device__ void eg_point_dev(double T, const double* X, const double* cpms, doub
 #pragma unroll
       for (int j = i + 1; j < N; ++j) {
         const double C = eg_poly6<N>(c_eg.fitc[i][j], d1, d2, d3, d4, d5, d6);
-        const double wi = c_eg.wt[i], wj = c_eg.wt[j];
-        const double term = 0.5 * bin[egs<N>(i, j)] * (6.0 * C - 5.0) * (wi * an[j] - wj * an[i]) / (wi + wj);
+        const double term = 0.5 * bin[egs<N>(i, j)] * (6.0 * C - 5.0) *
+                            (c_eg.wt[i] * an[j] - c_eg.wt[j] * an[i]) * c_eg.wsinv[i][j];
         chit[i] = chit[i] + xtr[j] * term;
         chit[j] = chit[j] - xtr[i] * term;
       }
   }
-  // ---- EGSDR1
+  // ---- EGSDR1: matrix L_[00], two stationary steps, mass-conservation projection
   {
+    double gd[N], dmi[N], tmp[N];
 #pragma unroll
-    for (int i = 0; i < N; ++i) g[egs<N>(i, i)] = 0.0;
+    for (int i = 0; i < N; ++i) gd[i] = 0.0;
 #pragma unroll
     for (int i = 0; i < N; ++i)
 #pragma unroll
       for (int j = i + 1; j < N; ++j) {
         const double a = xtr[i] * xtr[j] * bin[egs<N>(i, j)];
-        g[egs<N>(i, j)] = -a;
-        g[egs<N>(i, i)] = g[egs<N>(i, i)] + a;
-        g[egs<N>(j, j)] = g[egs<N>(j, j)] + a;
+        g[egs<N>(i, j)] = a;   // holds -L_ij
+        gd[i] = gd[i] + a;
+        gd[j] = gd[j] + a;
       }
-    double dmi[N];
 #pragma unroll
-    for (int i = 0; i < N; ++i) dmi[i] = aux[i] / g[egs<N>(i, i)];
+    for (int i = 0; i < N; ++i) dmi[i] = aux[i] / gd[i];
 #pragma unroll
     for (int i = 0; i < N; ++i) {
       D[i * N + i] = ytr[i] * (dmi[i] * (1.0 + ytr[i]));
 #pragma unroll
       for (int j = i + 1; j < N; ++j) {
-        const double dij = -dmi[i] * dmi[j] * g[egs<N>(i, j)];
+        const double dij = dmi[i] * dmi[j] * g[egs<N>(i, j)];
         D[i * N + j] = ytr[i] * dij;
         D[j * N + i] = ytr[j] * dij;
       }
     }
-    // EGSPDP
-#pragma unroll
-    for (int i = 0; i < N; ++i) tmp[i] = 0.0;
-#pragma unroll
-    for (int j = 0; j < N; ++j)
-#pragma unroll
-      for (int i = 0; i < N; ++i) tmp[i] = tmp[i] + D[i * N + j] * ytr[j];
-    const double rsumy = 1.0 / sumtr;
+    const double rsumy = 1.0 / sum;
 #pragma unroll
     for (int i = 0; i < N; ++i) {
-      const double a = tmp[i] * rsumy;
+      double t = 0.0;
+#pragma unroll
+      for (int j = 0; j < N; ++j) t = t + D[i * N + j] * ytr[j];
+      const double a = t * rsumy;
 #pragma unroll
       for (int j = 0; j < N; ++j) D[i * N + j] = D[i * N + j] - a;
     }
@@ -342,11 +370,13 @@ __device__ void eg_point_dev(double T, const double* X, const double* cpms, doub
     for (int j = 0; j < N; ++j)
 #pragma unroll
       for (int i = 0; i < N; ++i) tmp[i] = tmp[i] + D[j * N + i];
-    const double aa = patmos * wwtr / (ru * T);
+    const double aa = (patmos / ru) * wwtr * Tinv;
 #pragma unroll
-    for (int i = 0; i < N; ++i)
+    for (int i = 0; i < N; ++i) {
+      const double yr = ytr[i] * rsumy;
 #pragma unroll
-      for (int j = 0; j < N; ++j) D[i * N + j] = aa * (D[i * N + j] - ytr[i] * rsumy * tmp[j]);
+      for (int j = 0; j < N; ++j) D[i * N + j] = aa * (D[i * N + j] - yr * tmp[j]);
+    }
   }
 }
 
