@@ -227,12 +227,19 @@ struct izem_mlp {
   double* d_loss = nullptr;
   int step = 0;
   cudaStream_t s = nullptr;
-  // inference buffers (ping-pong activations, FP32 output)
+  // inference buffers: BF16 features (rows x 16) and FP32 output (rows x 16)
   long long icap = 0;
   __nv_bfloat16* ib[2] = {};
   float* iout = nullptr;
   float* d_norm = nullptr;
+  // tensor-core inference: weights in the tcgen05 operand layout, rebuilt
+  // from Wb whenever the parameters change; wait-timeout flag
+  __nv_bfloat16* blob[NL] = {};
+  bool blob_dirty = true;
+  int* d_err = nullptr;
 };
+
+#include "mlp_tc.cuh"
 
 namespace {
 
@@ -311,38 +318,52 @@ cudaError_t mlp_backward(izem_mlp* m, int M) {
 
 cudaError_t mlp_infer_ensure(izem_mlp* m, long long rows) {
   if (rows <= m->icap) return cudaSuccess;
-  for (int q = 0; q < 2; ++q) if (m->ib[q]) cudaFree(m->ib[q]);
+  if (m->ib[0]) cudaFree(m->ib[0]);
   if (m->iout) cudaFree(m->iout);
   cudaError_t e;
-  for (int q = 0; q < 2; ++q)
-    if ((e = cudaMalloc(&m->ib[q], (size_t)rows * H * sizeof(__nv_bfloat16)))) return e;
+  if ((e = cudaMalloc(&m->ib[0], (size_t)rows * INP * sizeof(__nv_bfloat16)))) return e;
   if ((e = cudaMalloc(&m->iout, (size_t)rows * OUTP * sizeof(float)))) return e;
   m->icap = rows;
   return cudaSuccess;
 }
 
-// inference: input in ib[0] (rows x INP bf16), output FP32 in iout (rows x OUTP)
-cudaError_t mlp_infer(izem_mlp* m, int M, cudaStream_t s) {
+// Inference of M rows on the tensor cores: BF16 features x (M x 16) ->
+// FP32 outputs y (M x 16), one persistent CTA per SM (mlp_tc.cuh).
+cudaError_t mlp_infer_tc(izem_mlp* m, int M, const __nv_bfloat16* x, float* y, cudaStream_t s) {
   cudaError_t e;
-  int cur = 0;
-  for (int l = 0; l < NL; ++l) {
-    GemmArgs a{};
-    a.A = m->ib[cur];
-    a.B = m->Wb[l];
-    a.M = M; a.N = LOUT[l]; a.K = LIN[l];
-    a.lda = LIN[l]; a.ldb = LOUT[l]; a.ldc = LOUT[l];
-    a.bias = m->b[l];
-    if (l < NL - 1) {
-      a.Cf = nullptr;
-      a.Cb = m->ib[1 - cur];
-      if ((e = gemm<0, 0, EPI_BIAS_GELU>(a, s))) return e;
-      cur = 1 - cur;
-    } else {
-      a.Cf = m->iout;
-      if ((e = gemm<0, 0, EPI_BIAS>(a, s))) return e;
+  if (m->blob_dirty) {
+    for (int l = 0; l < NL; ++l) {
+      const int n = LIN[l] * LOUT[l];
+      mlptc::k_tc_blob<<<(n + 255) / 256, 256, 0, s>>>(m->Wb[l], LIN[l], LOUT[l], m->blob[l]);
     }
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    m->blob_dirty = false;
   }
-  return cudaSuccess;
+  static bool attr = false;
+  if (!attr) {
+    if ((e = cudaFuncSetAttribute(mlptc::k_mlp_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)mlptc::SMEM_BYTES)) != cudaSuccess)
+      return e;
+    attr = true;
+  }
+  int dev = 0, sms = 0;
+  if ((e = cudaGetDevice(&dev)) || (e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev))) return e;
+  const int ntiles = (M + mlptc::TM - 1) / mlptc::TM;
+  mlptc::TcArgs a{};
+  a.x = x;
+  a.out = y;
+  a.M = M;
+  for (int l = 0; l < NL; ++l) { a.blob[l] = m->blob[l]; a.bias[l] = m->b[l]; }
+  a.err = m->d_err;
+  mlptc::k_mlp_tc<<<ntiles < sms ? ntiles : sms, mlptc::THREADS, mlptc::SMEM_BYTES, s>>>(a);
+  return cudaGetLastError();
+}
+
+// the tensor-core kernel's wait-timeout flag (after the stream is synchronised)
+int mlp_tc_status(izem_mlp* m) {
+  int h = 0;
+  if (cudaMemcpy(&h, m->d_err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return IZEM_ERR_CUDA;
+  return h ? IZEM_ERR_TIMEOUT : IZEM_OK;
 }
 
 }  // namespace
@@ -365,6 +386,10 @@ int izem_mlp_create(izem_mlp** out) {
     cudaMemset(m->mb[l], 0, nb * 4); cudaMemset(m->vb[l], 0, nb * 4);
   }
   if (cudaMalloc(&m->d_loss, sizeof(double)) != cudaSuccess) return IZEM_ERR_NOMEM;
+  for (int l = 0; l < NL; ++l)
+    if (cudaMalloc(&m->blob[l], (size_t)LIN[l] * LOUT[l] * 2) != cudaSuccess) return IZEM_ERR_NOMEM;
+  if (cudaMalloc(&m->d_err, sizeof(int)) != cudaSuccess || cudaMemset(m->d_err, 0, sizeof(int)) != cudaSuccess)
+    return IZEM_ERR_NOMEM;
   *out = m;
   return IZEM_OK;
 }
@@ -379,6 +404,8 @@ void izem_mlp_destroy(izem_mlp* m) {
   for (int l = 0; l <= NL; ++l) cudaFree(m->act[l]);
   cudaFree(m->dzf); cudaFree(m->dzb[0]); cudaFree(m->dzb[1]); cudaFree(m->out); cudaFree(m->d_loss);
   cudaFree(m->ib[0]); cudaFree(m->ib[1]); cudaFree(m->iout); cudaFree(m->d_norm);
+  for (int l = 0; l < NL; ++l) cudaFree(m->blob[l]);
+  cudaFree(m->d_err);
   cudaStreamDestroy(m->s);
   delete m;
 }
@@ -388,6 +415,7 @@ void izem_mlp_destroy(izem_mlp* m) {
 // used by the tensor-core GEMMs are rounded from these.
 int izem_mlp_set_params(izem_mlp* m, const float* const* W, const float* const* b) {
   if (!m || !W || !b) return IZEM_ERR_ARG;
+  m->blob_dirty = true;
   for (int l = 0; l < NL; ++l) {
     const size_t nw = (size_t)LIN[l] * LOUT[l];
     if (cudaMemcpy(m->W[l], W[l], nw * 4, cudaMemcpyHostToDevice) != cudaSuccess) return IZEM_ERR_CUDA;
@@ -417,18 +445,19 @@ int izem_mlp_set_norm(izem_mlp* m, const float* norm) {
 // normalised outputs (M x 10, FP32, host).
 int izem_mlp_forward(izem_mlp* m, int M, const float* x, float* y) {
   if (!m || M <= 0 || !x || !y) return IZEM_ERR_ARG;
-  if (mlp_ensure(m, M) != cudaSuccess) return IZEM_ERR_NOMEM;
+  if (mlp_infer_ensure(m, M) != cudaSuccess) return IZEM_ERR_NOMEM;
   std::vector<float> xp((size_t)M * INP, 0.f);
   for (int r = 0; r < M; ++r)
     for (int c = 0; c < IN; ++c) xp[(size_t)r * INP + c] = x[(size_t)r * IN + c];
   float* dx = nullptr;
   if (cudaMalloc(&dx, xp.size() * 4) != cudaSuccess) return IZEM_ERR_NOMEM;
   cudaMemcpy(dx, xp.data(), xp.size() * 4, cudaMemcpyHostToDevice);
-  k_f32_to_bf16<<<g1(xp.size()), 256, 0, m->s>>>(dx, m->act[0], (long long)xp.size());
-  int rc = mlp_forward(m, M) == cudaSuccess ? IZEM_OK : IZEM_ERR_CUDA;
+  k_f32_to_bf16<<<g1(xp.size()), 256, 0, m->s>>>(dx, m->ib[0], (long long)xp.size());
+  int rc = mlp_infer_tc(m, M, m->ib[0], m->iout, m->s) == cudaSuccess ? IZEM_OK : IZEM_ERR_CUDA;
   std::vector<float> o((size_t)M * OUTP);
-  cudaMemcpyAsync(o.data(), m->out, o.size() * 4, cudaMemcpyDeviceToHost, m->s);
+  cudaMemcpyAsync(o.data(), m->iout, o.size() * 4, cudaMemcpyDeviceToHost, m->s);
   if (cudaStreamSynchronize(m->s) != cudaSuccess) rc = IZEM_ERR_CUDA;
+  if (rc == IZEM_OK) rc = mlp_tc_status(m);
   cudaFree(dx);
   for (int r = 0; r < M; ++r)
     for (int c = 0; c < OUT; ++c) y[(size_t)r * OUT + c] = o[(size_t)r * OUTP + c];
@@ -508,6 +537,7 @@ int izem_mlp_train(izem_mlp* m, long long n, const float* x, const float* t, int
       k_mse_grad<<<g1((long long)batch * OUTP), 256, 0, m->s>>>(m->out, bt, batch, m->dzf, m->dzb[0], m->d_loss);
       if (mlp_backward(m, batch) != cudaSuccess) { rc = IZEM_ERR_CUDA; break; }
       m->step += 1;
+      m->blob_dirty = true;
       const float b1 = 0.9f, b2 = 0.999f;
       const float c1 = 1.f - powf(b1, (float)m->step), c2 = 1.f - powf(b2, (float)m->step);
       for (int l = 0; l < NL; ++l) {
@@ -586,10 +616,10 @@ int izem_gpu_psr_batch_mlp(izem_mlp* m, izem_mlp* m2, const izem_mech* mech, int
     const int cn = (n - c0) < chunk ? (n - c0) : chunk;
     cudaEventRecord(a0, s);
     chem_launch_featurize(cn, dT + c0, drho + c0, dY + (size_t)c0 * kk, ddt + c0, m->d_norm, m->ib[0], INP, s);
-    if (mlp_infer(m, cn, s) != cudaSuccess) { rc = IZEM_ERR_CUDA; break; }
+    if (mlp_infer_tc(m, cn, m->ib[0], m->iout, s) != cudaSuccess) { rc = IZEM_ERR_CUDA; break; }
     if (m2) {
       chem_launch_featurize(cn, dT + c0, drho + c0, dY + (size_t)c0 * kk, ddt + c0, m2->d_norm, m2->ib[0], INP, s);
-      if (mlp_infer(m2, cn, s) != cudaSuccess) { rc = IZEM_ERR_CUDA; break; }
+      if (mlp_infer_tc(m2, cn, m2->ib[0], m2->iout, s) != cudaSuccess) { rc = IZEM_ERR_CUDA; break; }
     }
     cudaEventRecord(a1, s);
     cudaMemsetAsync(d_count, 0, sizeof(unsigned), s);
@@ -614,6 +644,8 @@ int izem_gpu_psr_batch_mlp(izem_mlp* m, izem_mlp* m2, const izem_mech* mech, int
     if (dT_pred) cudaMemcpyAsync(dT_pred, ddTp, n * 8, cudaMemcpyDeviceToHost, s);
   }
   if (cudaStreamSynchronize(s) != cudaSuccess) rc = IZEM_ERR_CUDA;
+  if (rc == IZEM_OK) rc = mlp_tc_status(m);
+  if (rc == IZEM_OK && m2) rc = mlp_tc_status(m2);
   float ms_tot = 0.f;
   cudaEventElapsedTime(&ms_tot, e0, e1);
   if (ms2) { ms2[0] = ms_tot; ms2[1] = ms_mlp; }
