@@ -339,6 +339,87 @@ def run_batch(args):
     }
 
 
+def run_surrogate(args):
+    """Learned chemistry on independent reactors: two networks trained on the
+    GPU on args.train reactors of the batched-chemistry distribution
+    (labelled by the FP64 BDF integrator), then the gated surrogate step --
+    tensor-core inference, error gate, BDF on the rejected cells -- on
+    args.cells reactors of the same distribution drawn with another seed,
+    against the BDF step on all of them.  Arrays resident on the device."""
+    import torch
+    from phd_gb300 import ics
+    from phd_gb300.izem import psr_batch_device
+    from phd_gb300.mech import h2_mechanism
+    from phd_gb300.surrogate import DEFAULT_GATE, STRICT_GATE, train_ensemble
+    gate = STRICT_GATE if args.gate == "strict" else DEFAULT_GATE
+    mech = h2_mechanism()
+    t0 = time.perf_counter()
+    nets = train_ensemble(mech, n=args.train, seed=31, epochs=args.epochs)
+    t_train = time.perf_counter() - t0
+    n = args.cells
+    T = torch.empty(n, dtype=torch.float64, device="cuda:0")
+    rho, dt = torch.empty_like(T), torch.empty_like(T)
+    Y = torch.empty((n, 9), dtype=torch.float64, device="cuda:0")
+    chunk = 1 << 22
+    for c0 in range(0, n, chunk):
+        c1 = min(n, c0 + chunk)
+        Tc, rc, Yc, dc = ics.batched_reactors(c1 - c0, seed=20270101 + c0 // chunk)
+        T[c0:c1].copy_(torch.from_numpy(Tc))
+        rho[c0:c1].copy_(torch.from_numpy(rc))
+        Y[c0:c1].copy_(torch.from_numpy(Yc))
+        dt[c0:c1].copy_(torch.from_numpy(dc))
+    T0, Y0 = T.clone(), Y.clone()
+
+    def reset():
+        T.copy_(T0)
+        Y.copy_(Y0)
+        torch.cuda.synchronize()
+
+    reset()
+    psr_batch_device(mech, n, T, rho, Y, dt)   # warm-up, and the FP64 reference increments
+    dT_ref = (T - T0).cpu().numpy()
+    reset()
+    bdf_ms = psr_batch_device(mech, n, T, rho, Y, dt)
+    for _ in range(args.warmup):
+        reset()
+        nets[0].chem_step_device(mech, n, T, rho, Y, dt, gate, partner=nets[1])
+    runs = []
+    with ClockSampler(0) as clk:
+        for _ in range(args.steps):
+            reset()
+            runs.append(nets[0].chem_step_device(mech, n, T, rho, Y, dt, gate, partner=nets[1]))
+    err = np.abs((T - T0).cpu().numpy() - dT_ref)
+    scale = float(np.abs(dT_ref).max())
+    ms = float(np.mean([r["ms"] for r in runs]))
+    ms_net = float(np.mean([r["ms_mlp"] for r in runs]))
+    flop = 2.0 * 2 * 202240 * n     # two networks, 202,240 MACs per row
+    tflops = flop / (ms_net * 1e-3) / 1e12
+    peak = 1932.2
+    pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pk):
+        with open(pk) as f:
+            peak = float(json.load(f).get("bf16_tflops", peak))
+    return {
+        "metric": "learned-chemistry step Mcells/s (gated BF16 tensor-core MLP + FP64 BDF fallback)",
+        "value": n / (ms * 1e-3) / 1e6, "unit": "Mcells/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "bf16 network, f64 integrator", "data": "synthetic (seeded PCG64)",
+        "config": {"workload": "independent H2/air reactors (batched-chemistry distribution)", "cells": n,
+                   "training": {"samples": args.train, "epochs": args.epochs, "networks": 2, "seconds": t_train},
+                   "gate": {"name": args.gate, "values": list(gate)}, "l2": "inputs larger than L2"},
+        "bdf": {"value": n / (bdf_ms * 1e-3) / 1e6, "unit": "Mcells/s", "ms": bdf_ms},
+        "speedup_vs_bdf": bdf_ms / ms,
+        "fallback_frac": float(np.mean([r["fallback"] for r in runs])) / n,
+        "max_dT_err_K": float(err.max()), "max_dT_K": scale, "max_dT_err_frac": float(err.max()) / scale,
+        "rms_dT_err_K": float(np.sqrt((err ** 2).mean())),
+        "roofline": {"bound": "tensor", "kernel": "k_mlp_tc (two networks, with the feature kernel)",
+                     "achieved": tflops, "peak": peak, "unit": "TFLOP/s", "frac": tflops / peak,
+                     "traffic": None, "network_ms": ms_net},
+        # per 2^20-reactor chunk: 2 feature kernels, 2 tensor-core networks, the gate, the BDF fallback
+        "gpu_launches": args.steps * 6 * ((n + (1 << 20) - 1) >> 20), "clocks": clk.summary(),
+    }
+
+
 def workload_note(chem, eg):
     return " (WENO5 + %s viscous fluxes + RK3%s)" % ("EGLIB precision-1" if eg else "fitted-transport",
                                                        " + Strang BDF chemistry" if chem else ", no chemistry")
@@ -423,8 +504,12 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="mix", choices=["mix", "tgv", "batch"])
-    ap.add_argument("--cells", type=int, default=1 << 20, help="reactors of the batch workload")
+    ap.add_argument("--workload", default="mix", choices=["mix", "tgv", "batch", "surrogate"])
+    ap.add_argument("--cells", type=int, default=None,
+                    help="reactors of the batch (default 2^20) and surrogate (default 512*256*256) workloads")
+    ap.add_argument("--train", type=int, default=1 << 21, help="training reactors of the surrogate workload")
+    ap.add_argument("--epochs", type=int, default=24, help="training epochs of the surrogate workload")
+    ap.add_argument("--gate", default="default", choices=["default", "strict"], help="surrogate error gate")
     ap.add_argument("--nx", type=int, default=256)
     ap.add_argument("--ny", type=int, default=256)
     ap.add_argument("--nz", type=int, default=128)
@@ -435,6 +520,8 @@ def main():
     ap.add_argument("--transport", default="eglib", choices=["eglib", "fitted"],
                     help="viscous transport of the mixing layer (EGLIB precision 1 or the tranfit fits)")
     args = ap.parse_args()
+    if args.cells is None:
+        args.cells = 512 * 256 * 256 if args.workload == "surrogate" else 1 << 20
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if world > 1:
@@ -465,9 +552,9 @@ def main():
             vis = os.environ.get("CUDA_VISIBLE_DEVICES")
             devs = vis.split(",") if vis else [str(q) for q in range(world)]
             os.environ["CUDA_VISIBLE_DEVICES"] = devs[local % len(devs)]
-    if args.workload == "batch":
+    if args.workload in ("batch", "surrogate"):
         if rank == 0:
-            print(json.dumps(run_batch(args)))
+            print(json.dumps(run_batch(args) if args.workload == "batch" else run_surrogate(args)))
         return
     res = run_gpu(args, rank, world)
     if rank == 0:

@@ -191,9 +191,29 @@ class Surrogate:
         return {"fallback": int(st3[0]), "max_steps": int(st3[1]), "failed": int(st3[2]), "ms": float(ms2[0]),
                 "ms_mlp": float(ms2[1]), "dT_pred": dTp}
 
+    def chem_step_device(self, mech, n, T, rho, Y, dt, gate, partner=None):
+        """chem_step on arrays already on the device (torch CUDA tensors:
+        T, rho, dt (n), Y (n, 9) row-major), updated in place; the caller's
+        work on them must be complete.  Returns the same dictionary without
+        dT_pred."""
+        kncf = np.ascontiguousarray(np.array(load_species("h2air9")["kncf"], dtype=np.int32))
+        g9 = np.ascontiguousarray(np.array(gate, dtype=np.float64))
+        st3 = np.zeros(3, dtype=np.int32)
+        ms2 = np.zeros(2, dtype=np.float32)
+        rc = self.lib.izem_gpu_psr_batch_mlp(self.h, partner.h if partner is not None else None, C.byref(mech), n,
+                                             T.data_ptr(), rho.data_ptr(), Y.data_ptr(), dt.data_ptr(), 1,
+                                             g9.ctypes.data, kncf.ctypes.data, kncf.shape[1], None,
+                                             st3.ctypes.data, ms2.ctypes.data)
+        if rc:
+            raise IzemError(rc, "izem_gpu_psr_batch_mlp")
+        return {"fallback": int(st3[0]), "max_steps": int(st3[1]), "failed": int(st3[2]), "ms": float(ms2[0]),
+                "ms_mlp": float(ms2[1])}
+
 
 # Tmin, Tmax, dtmin, dtmax, tol_el, tol_T_abs [K], tol_T_rel, tol_ens_abs [K], tol_ens_rel
 DEFAULT_GATE = (800.0, 2400.0, 1e-8, 1e-6, 2e-3, 2.0, 0.003, 1.0, 0.002)
+# tighter energy-consistency and agreement tolerances: more cells go to BDF
+STRICT_GATE = (800.0, 2400.0, 1e-8, 1e-6, 2e-3, 0.5, 0.001, 0.2, 0.0003)
 
 
 def train_ensemble(mech, n=1 << 22, seed=31, epochs=30, batch=4096, lr=1e-3, members=2, log=None):
