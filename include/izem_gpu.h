@@ -290,6 +290,15 @@ int  izem_gpu_set_surrogate(izem_ctx* ctx, izem_mlp* m, izem_mlp* m2, const doub
 int  izem_gpu_chem_surrogate_stats(izem_ctx* ctx, long long* cells, int* fallback, float* ms_total,
                                    float* ms_network);
 
+/* Autotuning (no counterpart in the reference): times the candidate thread
+ * blocks (64, 128, 256) of the face-flux and viscous point kernels on the
+ * context's current state, and -- when a mechanism is set and chem_dt > 0
+ * -- of the persistent chemistry kernel on a copy of the reaction window
+ * for a half step chem_dt (code units); keeps the fastest of each.  Results
+ * do not depend on the choice.  report (may be NULL) receives the timings
+ * as JSON.  Call after the state is uploaded, before the timed steps. */
+int  izem_gpu_autotune(izem_ctx* ctx, double chem_dt, char* report, int report_len);
+
 /* Device timing of the calls above on the context's stream (CUDA events). */
 int  izem_gpu_timer_start(izem_ctx* ctx);
 int  izem_gpu_timer_stop(izem_ctx* ctx, float* ms);

@@ -1134,7 +1134,7 @@ __global__ void k_chem_scatter(ChemField f, const double* T, const double* Y, Ch
 }
 
 template <int KK>
-__global__ void __launch_bounds__(128) k_psr_field(ChemField f, unsigned* counter, ChemStats* stats) {
+__global__ void __launch_bounds__(256) k_psr_field(ChemField f, unsigned* counter, ChemStats* stats) {
   constexpr int N = KK + 1;
   const long long ncell = (long long)f.wx * f.wy * f.wz;
   const long long nc = f.ncell;
@@ -1171,7 +1171,7 @@ __global__ void __launch_bounds__(128) k_psr_field(ChemField f, unsigned* counte
 }
 
 template <int KK>
-__global__ void __launch_bounds__(128) k_psr_batch(int n, double* T, const double* rho, double* Y, const double* dt,
+__global__ void __launch_bounds__(256) k_psr_batch(int n, double* T, const double* rho, double* Y, const double* dt,
                                                    int* istate, int* nsteps, unsigned* counter, ChemStats* stats) {
   constexpr int N = KK + 1;
   auto load = [&](unsigned q, double& rh, double* z, double& tf) {
@@ -1302,7 +1302,7 @@ __global__ void k_decode_gate(int n, const float* out, const float* out2, int ld
 }
 
 template <int KK>
-__global__ void __launch_bounds__(128) k_psr_list(const int* list, const unsigned* count, double* T, const double* rho,
+__global__ void __launch_bounds__(256) k_psr_list(const int* list, const unsigned* count, double* T, const double* rho,
                                                   double* Y, const double* dt, unsigned* counter, ChemStats* stats) {
   constexpr int N = KK + 1;
   auto load = [&](unsigned w, double& rh, double* z, double& tf) {
@@ -1323,11 +1323,17 @@ __global__ void __launch_bounds__(128) k_psr_list(const int* list, const unsigne
   rc_drive<KK>(*count, counter, load, store);
 }
 
+// Threads per block of the persistent chemistry kernels: 128 until an
+// autotuning pass (izem_gpu_autotune) measures the candidates on the
+// caller's reactors and keeps the fastest (the same for every context of
+// the process).
+int g_chem_tpb = 128;
+
 int chem_grid(int* blocks) {
   int dev = 0, sms = 0, per = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return -1;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return -1;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_psr_batch<9>, 128, 0) != cudaSuccess) return -1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_psr_batch<9>, g_chem_tpb, 0) != cudaSuccess) return -1;
   *blocks = sms * (per > 0 ? per : 1);
   return 0;
 }
@@ -1335,6 +1341,9 @@ int chem_grid(int* blocks) {
 }  // namespace
 
 // ---------------------------------------------------------- host side -------
+void chem_set_block(int tpb) { g_chem_tpb = tpb; }
+int chem_block() { return g_chem_tpb; }
+
 cudaError_t chem_upload_mech(const izem_mech* m) {
   cudaError_t e = cudaMemcpyToSymbol(c_mech_dev, m, sizeof(izem_mech));
   if (e != cudaSuccess) return e;
@@ -1351,7 +1360,7 @@ cudaError_t chem_launch_field(const ChemField& f, unsigned* d_counter, ChemStats
   cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(unsigned), s);
   if (e != cudaSuccess) return e;
   if (kk != 9) return cudaErrorInvalidValue;
-  k_psr_field<9><<<blocks, 128, 0, s>>>(f, d_counter, d_stats);
+  k_psr_field<9><<<blocks, g_chem_tpb, 0, s>>>(f, d_counter, d_stats);
   return cudaGetLastError();
 }
 
@@ -1362,7 +1371,7 @@ cudaError_t chem_launch_batch(int n, double* T, const double* rho, double* Y, co
   cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(unsigned), s);
   if (e != cudaSuccess) return e;
   if (kk != 9) return cudaErrorInvalidValue;
-  k_psr_batch<9><<<blocks, 128, 0, s>>>(n, T, rho, Y, dt, istate, nsteps, d_counter, d_stats);
+  k_psr_batch<9><<<blocks, g_chem_tpb, 0, s>>>(n, T, rho, Y, dt, istate, nsteps, d_counter, d_stats);
   return cudaGetLastError();
 }
 
@@ -1400,6 +1409,6 @@ cudaError_t chem_launch_list(const int* list, const unsigned* count, double* T, 
   if (chem_grid(&blocks)) return cudaErrorUnknown;
   cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(unsigned), s);
   if (e != cudaSuccess) return e;
-  k_psr_list<9><<<blocks, 128, 0, s>>>(list, count, T, rho, Y, dt, d_counter, d_stats);
+  k_psr_list<9><<<blocks, g_chem_tpb, 0, s>>>(list, count, T, rho, Y, dt, d_counter, d_stats);
   return cudaGetLastError();
 }

@@ -23,6 +23,9 @@ struct ChemStats {
 };
 
 cudaError_t chem_upload_mech(const izem_mech* m);
+// threads per block of the persistent chemistry kernels (set by the autotuner)
+void chem_set_block(int tpb);
+int chem_block();
 cudaError_t chem_launch_field(const ChemField& f, unsigned* d_counter, ChemStats* d_stats, cudaStream_t s, int kk);
 cudaError_t chem_launch_batch(int n, double* T, const double* rho, double* Y, const double* dt, int* istate,
                               int* nsteps, unsigned* d_counter, ChemStats* d_stats, cudaStream_t s, int kk);

@@ -37,6 +37,8 @@ struct izem_ctx {
   std::vector<double> kt_ms;
   std::vector<std::vector<std::pair<cudaEvent_t, cudaEvent_t>>> kt_pending;
   bool have_eg = false;   // EGLIB linking data uploaded (izem_gpu_set_eglib)
+  // threads per block chosen by izem_gpu_autotune (face fluxes, viscous point kernel)
+  int tb_euler = 128, tb_visc = 128;
   // chemistry
   bool have_mech = false;
   izem_mech mech;

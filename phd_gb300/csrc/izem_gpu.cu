@@ -150,9 +150,9 @@ int enq_euler(izem_ctx* c, int d) {
   int rc;
   const char* names[3] = {"euler_face_x", "euler_face_y", "euler_face_z"};
   rc = launch(c, names[d], [&] {
-    if (d == 0) k_euler_face<NRV, 0><<<grid_for(nf), kThreads, 0, c->stream>>>(g, c->cfg.weno_avg, c->cfg.weno5_linear_fix, c->v, c->prim, c->sensor, c->fhat, nf);
-    if (d == 1) k_euler_face<NRV, 1><<<grid_for(nf), kThreads, 0, c->stream>>>(g, c->cfg.weno_avg, c->cfg.weno5_linear_fix, c->v, c->prim, c->sensor, c->fhat, nf);
-    if (d == 2) k_euler_face<NRV, 2><<<grid_for(nf), kThreads, 0, c->stream>>>(g, c->cfg.weno_avg, c->cfg.weno5_linear_fix, c->v, c->prim, c->sensor, c->fhat, nf);
+    if (d == 0) k_euler_face<NRV, 0><<<grid_for(nf, c->tb_euler), c->tb_euler, 0, c->stream>>>(g, c->cfg.weno_avg, c->cfg.weno5_linear_fix, c->v, c->prim, c->sensor, c->fhat, nf);
+    if (d == 1) k_euler_face<NRV, 1><<<grid_for(nf, c->tb_euler), c->tb_euler, 0, c->stream>>>(g, c->cfg.weno_avg, c->cfg.weno5_linear_fix, c->v, c->prim, c->sensor, c->fhat, nf);
+    if (d == 2) k_euler_face<NRV, 2><<<grid_for(nf, c->tb_euler), c->tb_euler, 0, c->stream>>>(g, c->cfg.weno_avg, c->cfg.weno5_linear_fix, c->v, c->prim, c->sensor, c->fhat, nf);
   });
   if (rc) return rc;
   return launch(c, "flux_diff", [&] {
@@ -180,12 +180,12 @@ int enq_visc(izem_ctx* c) {
   if (eg) {
     const long long ns_all = slab_count(g);
     if ((rc = launch(c, "visc_point_eg", [&] {
-           k_visc_point_eg<NRV><<<(unsigned)((ns_all + 127) / 128), 128, 0, c->stream>>>(g, c->v, c->T, c->W_i, c->ha, c->Xa,
+           k_visc_point_eg<NRV><<<grid_for(ns_all, c->tb_visc), c->tb_visc, 0, c->stream>>>(g, c->v, c->T, c->W_i, c->ha, c->Xa,
                                                                                          c->prim, c->fd, c->tau, c->qv);
          })))
       return rc;
   } else if ((rc = launch(c, "visc_point", [&] {
-         k_visc_point<NRV><<<grid_for(slab_count(g)), kThreads, 0, c->stream>>>(g, c->v, c->T, c->W_i, c->ha, c->Xa, c->fd, c->tau, c->qv);
+         k_visc_point<NRV><<<grid_for(slab_count(g), c->tb_visc), c->tb_visc, 0, c->stream>>>(g, c->v, c->T, c->W_i, c->ha, c->Xa, c->fd, c->tau, c->qv);
        })))
     return rc;
   return launch(c, "visc_div", [&] { k_visc_div<NRV><<<grid_for(g.nint), kThreads, 0, c->stream>>>(g, mt, c->tau, c->qv, c->fd, c->f); });
@@ -302,6 +302,64 @@ int do_visc(izem_ctx* c) {
   int rc = enq_prim<NRV>(c);
   if (rc) return rc;
   return enq_visc<NRV>(c);
+}
+
+
+// ---------------------------------------------------------- autotuning -------
+// Times each candidate launch configuration on the context's current state
+// with CUDA events and keeps the fastest.  Block size changes only how the
+// points are grouped, never a point's arithmetic, so every candidate gives
+// identical results.
+constexpr int kTuneCand[3] = {64, 128, 256};
+
+template <class F>
+float tune_time(izem_ctx* c, int reps, F body) {
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  body();   // untimed first pass
+  cudaEventRecord(a, c->stream);
+  for (int r = 0; r < reps; ++r) body();
+  cudaEventRecord(b, c->stream);
+  float ms = -1.f;
+  if (cudaEventSynchronize(b) == cudaSuccess) cudaEventElapsedTime(&ms, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  return ms < 0.f ? 1e30f : ms / reps;
+}
+
+void tune_report(std::string& rep, const char* name, const float* ms, int chosen) {
+  char buf[256];
+  std::snprintf(buf, sizeof(buf), "%s\"%s\": {\"64\": %.4f, \"128\": %.4f, \"256\": %.4f, \"chosen\": %d}",
+                rep.size() > 1 ? ", " : "", name, ms[0], ms[1], ms[2], chosen);
+  rep += buf;
+}
+
+template <int NRV>
+int tune_flow(izem_ctx* c, std::string* rep) {
+  int rc = enq_prim<NRV>(c);
+  if (rc) return rc;
+  float ms[3];
+  int best = 1;
+  for (int q = 0; q < 3; ++q) {
+    c->tb_euler = kTuneCand[q];
+    ms[q] = tune_time(c, 2, [&] { for (int d = 0; d < 3; ++d) (void)enq_euler<NRV>(c, d); });
+    if (ms[q] < ms[best]) best = q;
+  }
+  c->tb_euler = kTuneCand[best];
+  tune_report(*rep, "euler_face", ms, c->tb_euler);
+  if (c->cfg.vis) {
+    best = 1;
+    for (int q = 0; q < 3; ++q) {
+      c->tb_visc = kTuneCand[q];
+      ms[q] = tune_time(c, 2, [&] { (void)enq_visc<NRV>(c); });
+      if (ms[q] < ms[best]) best = q;
+    }
+    c->tb_visc = kTuneCand[best];
+    tune_report(*rep, c->cfg.eglib ? "visc_point_eg" : "visc_point", ms, c->tb_visc);
+  }
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? IZEM_OK : ctx_fail(c, IZEM_ERR_CUDA, "autotune", e);
 }
 
 // ================================================================ C ABI =====
@@ -753,6 +811,65 @@ int izem_gpu_psr_batch(const izem_mech* mech, int n, double* T, const double* rh
   cudaFree(counter);
   cudaFree(st);
   cudaStreamDestroy(s);
+  return rc;
+}
+
+int izem_gpu_autotune(izem_ctx* c, double chem_dt, char* report, int report_len) {
+  if (!c) return IZEM_ERR_ARG;
+  if (!c->grid_set) return ctx_fail(c, IZEM_ERR_STATE, "grid not set", cudaSuccess);
+  if (c->cfg.vis && c->cfg.eglib && !c->have_eg)
+    return ctx_fail(c, IZEM_ERR_STATE, "EGLIB transport requested (cfg.eglib) but izem_gpu_set_eglib not called", cudaSuccess);
+  // the captured RK3 graph holds the old launch configurations
+  if (c->graph_exec) { cudaGraphExecDestroy(c->graph_exec); c->graph_exec = nullptr; }
+  if (c->graph) { cudaGraphDestroy(c->graph); c->graph = nullptr; }
+  const bool kt = c->kt_enabled;
+  c->kt_enabled = false;
+  std::string rep = "{";
+  int rc = IZEM_DISPATCH(c, tune_flow, c, &rep);
+  if (rc == IZEM_OK && c->have_mech && chem_dt > 0.0) {
+    // the persistent chemistry kernel on a copy of this context's reaction window
+    const Geo& g = c->g;
+    ChemField f{};
+    f.v = c->v; f.T = c->T; f.ncell = g.ncell; f.gx = g.g[0]; f.gy = g.g[1]; f.ng = g.ng;
+    const int ng = g.ng;
+    f.ix = ng + 1; f.iy = ng + 1; f.iz = ng + 1;
+    const int fx = std::min(g.n[0], g.n[0] - ng - 1), fy = std::min(g.n[1], g.n[1] - ng - 1);
+    const int fz = std::min(g.n[1], g.n[2] - ng - 1);
+    f.wx = fx - f.ix + 1; f.wy = fy - f.iy + 1; f.wz = fz - f.iz + 1;
+    f.t_ref = c->adi.t_ref; f.tref_i = 1.0 / c->adi.t_ref;
+    f.rho_cgs = c->adi.rho_ref * 1.0e-3; f.dt_phys = chem_dt * c->adi.time_ref;
+    const long long n = (f.wx > 0 && f.wy > 0 && f.wz > 0) ? (long long)f.wx * f.wy * f.wz : 0;
+    if (n > 0 && n <= INT32_MAX) {
+      double *T = nullptr, *rho = nullptr, *Y = nullptr, *dt = nullptr, *T0 = nullptr, *Y0 = nullptr;
+      cudaError_t e = cudaSuccess;
+      if ((e = cudaMalloc(&T, n * 8)) || (e = cudaMalloc(&rho, n * 8)) || (e = cudaMalloc(&Y, n * 72)) ||
+          (e = cudaMalloc(&dt, n * 8)) || (e = cudaMalloc(&T0, n * 8)) || (e = cudaMalloc(&Y0, n * 72))) {
+        rc = ctx_fail(c, IZEM_ERR_NOMEM, "autotune buffers", e);
+      } else {
+        chem_launch_gather(f, T0, rho, Y0, dt, c->stream);
+        float ms[3];
+        int best = 1;
+        for (int q = 0; q < 3; ++q) {
+          chem_set_block(kTuneCand[q]);
+          auto body = [&] {
+            cudaMemcpyAsync(T, T0, n * 8, cudaMemcpyDeviceToDevice, c->stream);
+            cudaMemcpyAsync(Y, Y0, n * 72, cudaMemcpyDeviceToDevice, c->stream);
+            (void)chem_launch_batch((int)n, T, rho, Y, dt, nullptr, nullptr, c->d_counter,
+                                    (ChemStats*)c->d_chem_stats, c->stream, 9);
+          };
+          ms[q] = tune_time(c, 1, body);
+          if (ms[q] < ms[best]) best = q;
+        }
+        chem_set_block(kTuneCand[best]);
+        tune_report(rep, "chem_psr", ms, kTuneCand[best]);
+      }
+      cudaFree(T); cudaFree(rho); cudaFree(Y); cudaFree(dt); cudaFree(T0); cudaFree(Y0);
+    }
+  }
+  rep += "}";
+  c->kt_enabled = kt;
+  if (report && report_len > 0) std::snprintf(report, report_len, "%s", rep.c_str());
+  if (rc == IZEM_OK) CK(cudaStreamSynchronize(c->stream));
   return rc;
 }
 

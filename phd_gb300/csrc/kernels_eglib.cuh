@@ -435,7 +435,7 @@ __global__ void k_grad_p(Geo g, Metrics mt, const double* __restrict__ prim, dou
 // interior points and the ghost slabs of periodic faces.  Writes tau (6),
 // q (3) and overwrites the species gradients of fd with rho Y_k V_k.
 template <int NRV>
-__global__ void __launch_bounds__(128) k_visc_point_eg(Geo g, const double* __restrict__ v,
+__global__ void __launch_bounds__(256) k_visc_point_eg(Geo g, const double* __restrict__ v,
                                                        const double* __restrict__ T, const double* __restrict__ W_i,
                                                        const double* __restrict__ ha, const double* __restrict__ Xa,
                                                        const double* __restrict__ prim, double* __restrict__ fd,

@@ -141,7 +141,7 @@ __device__ __forceinline__ double weno5_nl(const double* vp, const double* vm) {
 // up to rounding.  Linear (sensor-off) faces accumulate the WENO5 stencil
 // while streaming over the 6 stencil points; sensed faces keep the 6 values.
 template <int NRV, int D>
-__global__ void __launch_bounds__(128) k_euler_face(Geo g, int weno_avg, int linfix,
+__global__ void __launch_bounds__(256) k_euler_face(Geo g, int weno_avg, int linfix,
                                                     const double* __restrict__ v,
                                                     const double* __restrict__ prim,
                                                     const uint8_t* __restrict__ sensor,

@@ -237,6 +237,14 @@ struct izem_mlp {
   __nv_bfloat16* blob[NL] = {};
   bool blob_dirty = true;
   int* d_err = nullptr;
+  // error-gate scratch of izem_gpu_psr_batch_mlp (kept across calls)
+  int* g_kncf = nullptr;
+  int* g_list = nullptr;
+  int g_list_cap = 0;
+  unsigned* g_count = nullptr;
+  int g_count_cap = 0;
+  unsigned* g_counter = nullptr;
+  ChemStats* g_stats = nullptr;
 };
 
 #include "mlp_tc.cuh"
@@ -406,6 +414,7 @@ void izem_mlp_destroy(izem_mlp* m) {
   cudaFree(m->ib[0]); cudaFree(m->ib[1]); cudaFree(m->iout); cudaFree(m->d_norm);
   for (int l = 0; l < NL; ++l) cudaFree(m->blob[l]);
   cudaFree(m->d_err);
+  cudaFree(m->g_kncf); cudaFree(m->g_list); cudaFree(m->g_count); cudaFree(m->g_counter); cudaFree(m->g_stats);
   cudaStreamDestroy(m->s);
   delete m;
 }
@@ -573,29 +582,41 @@ int izem_gpu_psr_batch_mlp(izem_mlp* m, izem_mlp* m2, const izem_mech* mech, int
                            double* Y, const double* dt, int device_ptrs, const double* gate9, const int* kncf, int nele,
                            double* dT_pred, int* stats3, float* ms2) {
   if (!m || !mech || n <= 0 || !T || !rho || !Y || !dt || !gate9 || !kncf || mech->kk != 9) return IZEM_ERR_ARG;
+  if (nele <= 0 || nele > 8) return IZEM_ERR_ARG;
   const int CH = 1 << 20;
   const int chunk = n < CH ? n : CH;
+  const int nch = (n + chunk - 1) / chunk;
   cudaStream_t s = m->s;
   if (mlp_infer_ensure(m, chunk) != cudaSuccess) return IZEM_ERR_NOMEM;
   if (m2 && mlp_infer_ensure(m2, chunk) != cudaSuccess) return IZEM_ERR_NOMEM;
-  if (m2 && !m2->d_norm && cudaMalloc(&m2->d_norm, sizeof(m2->norm)) != cudaSuccess) return IZEM_ERR_NOMEM;
-  if (m2) cudaMemcpyAsync(m2->d_norm, m2->norm, sizeof(m2->norm), cudaMemcpyHostToDevice, s);
-  if (chem_upload_mech(mech) != cudaSuccess) return IZEM_ERR_CUDA;
-  int* d_kncf = nullptr;
-  int* d_list = nullptr;
-  unsigned *d_count = nullptr, *d_counter = nullptr;
-  ChemStats* d_st = nullptr;
-  double *dT = nullptr, *drho = nullptr, *dY = nullptr, *ddt = nullptr, *ddTp = nullptr;
-  const size_t kk = mech->kk;
-  int rc = IZEM_OK;
   if (!m->d_norm && cudaMalloc(&m->d_norm, sizeof(m->norm)) != cudaSuccess) return IZEM_ERR_NOMEM;
-  cudaMemcpyAsync(m->d_norm, m->norm, sizeof(m->norm), cudaMemcpyHostToDevice, s);
-  if (cudaMalloc(&d_kncf, kk * nele * sizeof(int)) || cudaMalloc(&d_list, (size_t)chunk * sizeof(int)) ||
-      cudaMalloc(&d_count, sizeof(unsigned)) || cudaMalloc(&d_counter, sizeof(unsigned)) ||
-      cudaMalloc(&d_st, sizeof(ChemStats)))
+  if (m2 && !m2->d_norm && cudaMalloc(&m2->d_norm, sizeof(m2->norm)) != cudaSuccess) return IZEM_ERR_NOMEM;
+  // gate scratch kept in the handle: element counts, fallback list, per-chunk counts
+  if (!m->g_kncf && cudaMalloc(&m->g_kncf, IZEM_NSMAX * 8 * sizeof(int)) != cudaSuccess) return IZEM_ERR_NOMEM;
+  if (!m->g_counter && (cudaMalloc(&m->g_counter, sizeof(unsigned)) != cudaSuccess ||
+                        cudaMalloc(&m->g_stats, sizeof(ChemStats)) != cudaSuccess))
     return IZEM_ERR_NOMEM;
-  cudaMemcpyAsync(d_kncf, kncf, kk * nele * sizeof(int), cudaMemcpyHostToDevice, s);
-  cudaMemsetAsync(d_st, 0, sizeof(ChemStats), s);
+  if (chunk > m->g_list_cap) {
+    cudaFree(m->g_list);
+    m->g_list = nullptr;
+    if (cudaMalloc(&m->g_list, (size_t)chunk * sizeof(int)) != cudaSuccess) return IZEM_ERR_NOMEM;
+    m->g_list_cap = chunk;
+  }
+  if (nch > m->g_count_cap) {
+    cudaFree(m->g_count);
+    m->g_count = nullptr;
+    if (cudaMalloc(&m->g_count, (size_t)nch * sizeof(unsigned)) != cudaSuccess) return IZEM_ERR_NOMEM;
+    m->g_count_cap = nch;
+  }
+  if (chem_upload_mech(mech) != cudaSuccess) return IZEM_ERR_CUDA;
+  cudaMemcpyAsync(m->d_norm, m->norm, sizeof(m->norm), cudaMemcpyHostToDevice, s);
+  if (m2) cudaMemcpyAsync(m2->d_norm, m2->norm, sizeof(m2->norm), cudaMemcpyHostToDevice, s);
+  const size_t kk = mech->kk;
+  cudaMemcpyAsync(m->g_kncf, kncf, kk * nele * sizeof(int), cudaMemcpyHostToDevice, s);
+  cudaMemsetAsync(m->g_stats, 0, sizeof(ChemStats), s);
+  cudaMemsetAsync(m->g_count, 0, (size_t)nch * sizeof(unsigned), s);
+  double *dT = nullptr, *drho = nullptr, *dY = nullptr, *ddt = nullptr, *ddTp = nullptr;
+  int rc = IZEM_OK;
   if (device_ptrs) {
     dT = T; drho = const_cast<double*>(rho); dY = Y; ddt = const_cast<double*>(dt); ddTp = dT_pred;
   } else {
@@ -607,37 +628,31 @@ int izem_gpu_psr_batch_mlp(izem_mlp* m, izem_mlp* m2, const izem_mech* mech, int
     cudaMemcpyAsync(dY, Y, n * kk * 8, cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(ddt, dt, n * 8, cudaMemcpyHostToDevice, s);
   }
-  cudaEvent_t e0, e1, a0, a1;
-  cudaEventCreate(&e0); cudaEventCreate(&e1); cudaEventCreate(&a0); cudaEventCreate(&a1);
-  float ms_mlp = 0.f;
-  unsigned nfb = 0;
-  cudaEventRecord(e0, s);
-  for (int c0 = 0; c0 < n && rc == IZEM_OK; c0 += chunk) {
+  std::vector<cudaEvent_t> ev(2 * nch + 2);
+  for (auto& e : ev) cudaEventCreate(&e);
+  cudaEventRecord(ev[0], s);
+  for (int ci = 0; ci < nch && rc == IZEM_OK; ++ci) {
+    const int c0 = ci * chunk;
     const int cn = (n - c0) < chunk ? (n - c0) : chunk;
-    cudaEventRecord(a0, s);
+    cudaEventRecord(ev[2 + 2 * ci], s);
     chem_launch_featurize(cn, dT + c0, drho + c0, dY + (size_t)c0 * kk, ddt + c0, m->d_norm, m->ib[0], INP, s);
     if (mlp_infer_tc(m, cn, m->ib[0], m->iout, s) != cudaSuccess) { rc = IZEM_ERR_CUDA; break; }
     if (m2) {
       chem_launch_featurize(cn, dT + c0, drho + c0, dY + (size_t)c0 * kk, ddt + c0, m2->d_norm, m2->ib[0], INP, s);
       if (mlp_infer_tc(m2, cn, m2->ib[0], m2->iout, s) != cudaSuccess) { rc = IZEM_ERR_CUDA; break; }
     }
-    cudaEventRecord(a1, s);
-    cudaMemsetAsync(d_count, 0, sizeof(unsigned), s);
+    cudaEventRecord(ev[3 + 2 * ci], s);
     chem_launch_decode_gate(cn, m->iout, m2 ? m2->iout : nullptr, OUTP, m->d_norm, m2 ? m2->d_norm : nullptr, dT + c0,
-                            drho + c0, dY + (size_t)c0 * kk, ddt + c0, gate9, d_kncf, nele, d_list, d_count,
-                            ddTp ? ddTp + c0 : nullptr, d_st, s);
-    chem_launch_list(d_list, d_count, dT + c0, drho + c0, dY + (size_t)c0 * kk, ddt + c0, d_counter, d_st, s);
-    unsigned hc = 0;
-    cudaMemcpyAsync(&hc, d_count, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
-    if (cudaStreamSynchronize(s) != cudaSuccess) { rc = IZEM_ERR_CUDA; break; }
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, a0, a1);
-    ms_mlp += ms;
-    nfb += hc;
+                            drho + c0, dY + (size_t)c0 * kk, ddt + c0, gate9, m->g_kncf, nele, m->g_list,
+                            m->g_count + ci, ddTp ? ddTp + c0 : nullptr, m->g_stats, s);
+    chem_launch_list(m->g_list, m->g_count + ci, dT + c0, drho + c0, dY + (size_t)c0 * kk, ddt + c0, m->g_counter,
+                     m->g_stats, s);
   }
-  cudaEventRecord(e1, s);
+  cudaEventRecord(ev[1], s);
   ChemStats hs{};
-  cudaMemcpyAsync(&hs, d_st, sizeof(ChemStats), cudaMemcpyDeviceToHost, s);
+  std::vector<unsigned> hc(nch, 0u);
+  cudaMemcpyAsync(&hs, m->g_stats, sizeof(ChemStats), cudaMemcpyDeviceToHost, s);
+  cudaMemcpyAsync(hc.data(), m->g_count, (size_t)nch * sizeof(unsigned), cudaMemcpyDeviceToHost, s);
   if (!device_ptrs) {
     cudaMemcpyAsync(T, dT, n * 8, cudaMemcpyDeviceToHost, s);
     cudaMemcpyAsync(Y, dY, n * kk * 8, cudaMemcpyDeviceToHost, s);
@@ -646,12 +661,17 @@ int izem_gpu_psr_batch_mlp(izem_mlp* m, izem_mlp* m2, const izem_mech* mech, int
   if (cudaStreamSynchronize(s) != cudaSuccess) rc = IZEM_ERR_CUDA;
   if (rc == IZEM_OK) rc = mlp_tc_status(m);
   if (rc == IZEM_OK && m2) rc = mlp_tc_status(m2);
-  float ms_tot = 0.f;
-  cudaEventElapsedTime(&ms_tot, e0, e1);
+  float ms_tot = 0.f, ms_mlp = 0.f;
+  cudaEventElapsedTime(&ms_tot, ev[0], ev[1]);
+  for (int ci = 0; ci < nch; ++ci) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, ev[2 + 2 * ci], ev[3 + 2 * ci]) == cudaSuccess) ms_mlp += ms;
+  }
+  unsigned nfb = 0;
+  for (unsigned c : hc) nfb += c;
   if (ms2) { ms2[0] = ms_tot; ms2[1] = ms_mlp; }
   if (stats3) { stats3[0] = (int)nfb; stats3[1] = hs.max_steps; stats3[2] = hs.failed; }
-  cudaEventDestroy(e0); cudaEventDestroy(e1); cudaEventDestroy(a0); cudaEventDestroy(a1);
-  cudaFree(d_kncf); cudaFree(d_list); cudaFree(d_count); cudaFree(d_counter); cudaFree(d_st);
+  for (auto& e : ev) cudaEventDestroy(e);
   if (!device_ptrs) { cudaFree(dT); cudaFree(drho); cudaFree(dY); cudaFree(ddt); if (ddTp) cudaFree(ddTp); }
   if (rc == IZEM_OK && hs.failed) rc = IZEM_ERR_CHEM;
   return rc;

@@ -12,9 +12,9 @@
 //     layout, so each layer's 128 KB arrives in shared memory by bulk copies
 //     (cp.async.bulk, completion counted on an mbarrier), the next layer's
 //     copy overlapping the current layer's epilogue;
-//   * the epilogue (bias + exact GELU, then BF16) is split over 8 warps:
+//   * the epilogue (bias + exact GELU, then BF16) is split over 16 warps:
 //     warp w reads TMEM lanes 32 (w % 4) .. + 31 (the rows it owns) and the
-//     columns of half w / 4.
+//     64 columns of quarter w / 4.
 // Every wait on an mbarrier is bounded; on a timeout the kernel records it
 // in *err, waits (bounded) for its own operations, frees its TMEM and
 // returns.
@@ -28,7 +28,7 @@ constexpr int TM = 128;             // rows per tile (MMA M)
 constexpr int KH = 256;             // hidden width
 constexpr int KIN = 16;             // padded input width
 constexpr int NOUT = 16;            // padded output width
-constexpr int THREADS = 256;
+constexpr int THREADS = 512;
 constexpr uint32_t TMEM_COLS = 256;
 // shared memory map (bytes)
 constexpr uint32_t SA = 0;                        // activations, 128 x 256 BF16 = 64 KB
@@ -167,13 +167,13 @@ __global__ void k_tc_blob(const __nv_bfloat16* __restrict__ W, int K, int N, __n
 
 // bias + exact GELU of one layer's 128 x 256 accumulator, written back as the
 // next layer's BF16 K-major operand; warp w owns rows 32 (w % 4) + lane and
-// columns 128 (w / 4) .. + 127
+// columns 64 (w / 4) .. + 63
 __device__ __forceinline__ void epilogue_hidden(uint8_t* sm, uint32_t tmem, int warp, int lane, const float* bias) {
   const int r = (warp & 3) * 32 + lane;
   const uint32_t lane_addr = tmem + ((uint32_t)((warp & 3) * 32) << 16);
 #pragma unroll 1
-  for (int c = 0; c < 4; ++c) {
-    const int col = (warp >> 2) * 128 + c * 32;
+  for (int c = 0; c < 2; ++c) {
+    const int col = (warp >> 2) * 64 + c * 32;
     uint32_t v[32];
     tmem_ld32(lane_addr + (uint32_t)col, v);
     tmem_wait_ld();

@@ -74,6 +74,7 @@ def load_library(path=None):
                                          C.c_void_p, C.c_void_p, C.c_int, C.POINTER(C.c_float)]),
         "izem_gpu_set_surrogate": (C.c_int, [P, P, P, _dp, C.POINTER(C.c_int), C.c_int]),
         "izem_gpu_set_eglib": (C.c_int, [P, C.POINTER(IzemEglib)]),
+        "izem_gpu_autotune": (C.c_int, [P, C.c_double, C.c_char_p, C.c_int]),
         "izem_gpu_chem_surrogate_stats": (C.c_int, [P, C.POINTER(C.c_longlong), C.POINTER(C.c_int),
                                                     C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     }
@@ -250,6 +251,16 @@ class IzemGPU:
         dtm = C.c_double(dtmin)
         self._check(self.lib.izem_gpu_timestep(self.h, float(DTmax), _ptr(dt4), C.byref(dtm)), "timestep")
         return dt4, dtm.value
+
+    def autotune(self, chem_dt=0.0):
+        """Choose the thread blocks of the face-flux, viscous point and (with
+        chem_dt > 0 and a mechanism set) chemistry kernels by timing the
+        candidates on the current state; returns the timings [ms] and
+        choices."""
+        import json
+        buf = C.create_string_buffer(2048)
+        self._check(self.lib.izem_gpu_autotune(self.h, float(chem_dt), buf, 2048), "autotune")
+        return json.loads(buf.value.decode())
 
     def set_eglib(self, link):
         """EGLIB linking data (phd_gb300.thd.eglib_link) for cfg.eglib = 1."""

@@ -163,3 +163,30 @@ def test_rk3_steps_eglib():
     err = W.normwise(interior(got["v"]), interior(st["v"]))
     assert np.all(err <= TOL), err
     assert np.max(np.abs(interior(got["T"]) - interior(st["T"]))) <= TOL * np.max(st["T"])
+
+
+def test_autotune_keeps_results():
+    """The autotuner only regroups points into thread blocks: the fluxes and
+    an RK3 step and a chemistry half step after tuning are bit-identical to
+    those before."""
+    cfg, thd, adi, dxi, st, info, orc = W.case("mix", 16, eglib=True)
+    W.perturb(st, 0.01, seed=5)
+    orc.update_primitives(st)
+    from phd_gb300.mech import h2_mechanism
+    ref = []
+    for tune in (False, True):
+        g = _eglib_gpu(cfg, thd, adi, dxi, W.copy(st))
+        g.set_mechanism(h2_mechanism())
+        if tune:
+            rep = g.autotune(chem_dt=0.5)
+            assert {"euler_face", "visc_point_eg", "chem_psr"} <= set(rep)
+            assert all(r["chosen"] in (64, 128, 256) for r in rep.values())
+        g.zero_flux()
+        g.euler_LLF_x(); g.euler_LLF_y(); g.euler_LLF_z()
+        g.viscflux_xyz()
+        fl = g.flux()
+        g.rk3(1e-3)
+        g.reaction_selec(0.5)
+        ref.append((fl, g.download()))
+    assert np.array_equal(ref[0][0], ref[1][0])
+    assert np.array_equal(ref[0][1]["v"], ref[1][1]["v"]) and np.array_equal(ref[0][1]["T"], ref[1][1]["T"])
