@@ -1229,11 +1229,11 @@ struct GateArgs {
 // predicted dT agrees with the temperature that conserves internal energy
 // (constant-volume reactor) for the predicted composition.  Accepted cells
 // take the energy-consistent temperature.  Rejected cells are appended to
-// `list` for the BDF integrator.
+// `list` as base + q (their index in the whole batch) for the BDF integrator.
 template <int KK>
 __global__ void k_decode_gate(int n, const float* out, const float* out2, int ldo, const float* norm, const float* norm2,
                               double* T, const double* rho, double* Y, const double* dt, GateArgs ga, const int* kncf,
-                              int nele, int* list, unsigned* count, double* dT_pred, ChemStats* stats) {
+                              int nele, int* list, int base, unsigned* count, double* dT_pred, ChemStats* stats) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= n) return;
   const int NI = KK + 3, NO = KK + 1;
@@ -1297,7 +1297,7 @@ __global__ void k_decode_gate(int n, const float* out, const float* out2, int ld
     for (int k = 0; k < KK; ++k) Y[(size_t)q * KK + k] = Yn[k];
   } else {
     const unsigned slot = atomicAdd(count, 1u);
-    list[slot] = q;
+    list[slot] = base + q;
   }
 }
 
@@ -1395,11 +1395,11 @@ cudaError_t chem_launch_featurize(int n, const double* T, const double* rho, con
 
 cudaError_t chem_launch_decode_gate(int n, const float* out, const float* out2, int ldo, const float* d_norm,
                                     const float* d_norm2, double* T, const double* rho, double* Y, const double* dt,
-                                    const double* gate9, const int* d_kncf, int nele, int* list, unsigned* count,
-                                    double* dT_pred, ChemStats* stats, cudaStream_t s) {
+                                    const double* gate9, const int* d_kncf, int nele, int* list, int base,
+                                    unsigned* count, double* dT_pred, ChemStats* stats, cudaStream_t s) {
   GateArgs ga{gate9[0], gate9[1], gate9[2], gate9[3], gate9[4], gate9[5], gate9[6], gate9[7], gate9[8]};
   k_decode_gate<9><<<(n + 127) / 128, 128, 0, s>>>(n, out, out2, ldo, d_norm, d_norm2, T, rho, Y, dt, ga, d_kncf, nele,
-                                                   list, count, dT_pred, stats);
+                                                   list, base, count, dT_pred, stats);
   return cudaGetLastError();
 }
 

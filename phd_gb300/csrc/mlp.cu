@@ -239,10 +239,9 @@ struct izem_mlp {
   int* d_err = nullptr;
   // error-gate scratch of izem_gpu_psr_batch_mlp (kept across calls)
   int* g_kncf = nullptr;
-  int* g_list = nullptr;
+  int* g_list = nullptr;        // rejected cells of the whole batch
   int g_list_cap = 0;
-  unsigned* g_count = nullptr;
-  int g_count_cap = 0;
+  unsigned* g_count = nullptr;   // their number
   unsigned* g_counter = nullptr;
   ChemStats* g_stats = nullptr;
 };
@@ -569,8 +568,10 @@ int izem_mlp_train(izem_mlp* m, long long n, const float* x, const float* t, int
 }
 
 // Surrogate chemistry on n independent reactors (same arrays as
-// izem_gpu_psr_batch): MLP inference in chunks, the error gate, and the BDF
-// integrator on every rejected cell.  gate9 = {Tmin, Tmax, dtmin, dtmax,
+// izem_gpu_psr_batch): MLP inference and the error gate in chunks of 2^20
+// rows, the rejected cells of all chunks collected in one list, then one
+// BDF launch over that list (one load-balanced pass, so the slowest stiff
+// cell is waited for once, not once per chunk).  gate9 = {Tmin, Tmax, dtmin, dtmax,
 // tol_el, tol_T_abs, tol_T_rel, tol_ens_abs, tol_ens_rel}; m2 (optional) is
 // a second, independently trained network: the prediction is the mean of
 // the two, and cells where their dT disagree are rejected;
@@ -594,19 +595,14 @@ int izem_gpu_psr_batch_mlp(izem_mlp* m, izem_mlp* m2, const izem_mech* mech, int
   // gate scratch kept in the handle: element counts, fallback list, per-chunk counts
   if (!m->g_kncf && cudaMalloc(&m->g_kncf, IZEM_NSMAX * 8 * sizeof(int)) != cudaSuccess) return IZEM_ERR_NOMEM;
   if (!m->g_counter && (cudaMalloc(&m->g_counter, sizeof(unsigned)) != cudaSuccess ||
+                        cudaMalloc(&m->g_count, sizeof(unsigned)) != cudaSuccess ||
                         cudaMalloc(&m->g_stats, sizeof(ChemStats)) != cudaSuccess))
     return IZEM_ERR_NOMEM;
-  if (chunk > m->g_list_cap) {
+  if (n > m->g_list_cap) {
     cudaFree(m->g_list);
     m->g_list = nullptr;
-    if (cudaMalloc(&m->g_list, (size_t)chunk * sizeof(int)) != cudaSuccess) return IZEM_ERR_NOMEM;
-    m->g_list_cap = chunk;
-  }
-  if (nch > m->g_count_cap) {
-    cudaFree(m->g_count);
-    m->g_count = nullptr;
-    if (cudaMalloc(&m->g_count, (size_t)nch * sizeof(unsigned)) != cudaSuccess) return IZEM_ERR_NOMEM;
-    m->g_count_cap = nch;
+    if (cudaMalloc(&m->g_list, (size_t)n * sizeof(int)) != cudaSuccess) return IZEM_ERR_NOMEM;
+    m->g_list_cap = n;
   }
   if (chem_upload_mech(mech) != cudaSuccess) return IZEM_ERR_CUDA;
   cudaMemcpyAsync(m->d_norm, m->norm, sizeof(m->norm), cudaMemcpyHostToDevice, s);
@@ -614,7 +610,7 @@ int izem_gpu_psr_batch_mlp(izem_mlp* m, izem_mlp* m2, const izem_mech* mech, int
   const size_t kk = mech->kk;
   cudaMemcpyAsync(m->g_kncf, kncf, kk * nele * sizeof(int), cudaMemcpyHostToDevice, s);
   cudaMemsetAsync(m->g_stats, 0, sizeof(ChemStats), s);
-  cudaMemsetAsync(m->g_count, 0, (size_t)nch * sizeof(unsigned), s);
+  cudaMemsetAsync(m->g_count, 0, sizeof(unsigned), s);
   double *dT = nullptr, *drho = nullptr, *dY = nullptr, *ddt = nullptr, *ddTp = nullptr;
   int rc = IZEM_OK;
   if (device_ptrs) {
@@ -643,16 +639,17 @@ int izem_gpu_psr_batch_mlp(izem_mlp* m, izem_mlp* m2, const izem_mech* mech, int
     }
     cudaEventRecord(ev[3 + 2 * ci], s);
     chem_launch_decode_gate(cn, m->iout, m2 ? m2->iout : nullptr, OUTP, m->d_norm, m2 ? m2->d_norm : nullptr, dT + c0,
-                            drho + c0, dY + (size_t)c0 * kk, ddt + c0, gate9, m->g_kncf, nele, m->g_list,
-                            m->g_count + ci, ddTp ? ddTp + c0 : nullptr, m->g_stats, s);
-    chem_launch_list(m->g_list, m->g_count + ci, dT + c0, drho + c0, dY + (size_t)c0 * kk, ddt + c0, m->g_counter,
-                     m->g_stats, s);
+                            drho + c0, dY + (size_t)c0 * kk, ddt + c0, gate9, m->g_kncf, nele, m->g_list, c0,
+                            m->g_count, ddTp ? ddTp + c0 : nullptr, m->g_stats, s);
   }
+  if (rc == IZEM_OK && chem_launch_list(m->g_list, m->g_count, dT, drho, dY, ddt, m->g_counter, m->g_stats, s) !=
+                           cudaSuccess)
+    rc = IZEM_ERR_CUDA;
   cudaEventRecord(ev[1], s);
   ChemStats hs{};
-  std::vector<unsigned> hc(nch, 0u);
+  unsigned nfb = 0;
   cudaMemcpyAsync(&hs, m->g_stats, sizeof(ChemStats), cudaMemcpyDeviceToHost, s);
-  cudaMemcpyAsync(hc.data(), m->g_count, (size_t)nch * sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+  cudaMemcpyAsync(&nfb, m->g_count, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
   if (!device_ptrs) {
     cudaMemcpyAsync(T, dT, n * 8, cudaMemcpyDeviceToHost, s);
     cudaMemcpyAsync(Y, dY, n * kk * 8, cudaMemcpyDeviceToHost, s);
@@ -667,8 +664,6 @@ int izem_gpu_psr_batch_mlp(izem_mlp* m, izem_mlp* m2, const izem_mech* mech, int
     float ms = 0.f;
     if (cudaEventElapsedTime(&ms, ev[2 + 2 * ci], ev[3 + 2 * ci]) == cudaSuccess) ms_mlp += ms;
   }
-  unsigned nfb = 0;
-  for (unsigned c : hc) nfb += c;
   if (ms2) { ms2[0] = ms_tot; ms2[1] = ms_mlp; }
   if (stats3) { stats3[0] = (int)nfb; stats3[1] = hs.max_steps; stats3[2] = hs.failed; }
   for (auto& e : ev) cudaEventDestroy(e);
