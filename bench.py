@@ -305,7 +305,7 @@ def run_mlp_chem(args, g, stp, ncell, world):
             "rms_dT_err_K": float(np.sqrt((err ** 2).mean())),
             "training": {"samples": int(len(X)), "networks": 2, "epochs": 30, "label_s": t_label,
                          "train_s": t_train},
-            "gate": list(gate), "clocks": clk.summary()}
+            "gate": gate_json(gate), "clocks": clk.summary()}
 
 
 def run_batch(args):
@@ -369,12 +369,15 @@ def run_surrogate(args):
     from phd_gb300 import ics
     from phd_gb300.izem import psr_batch_device
     from phd_gb300.mech import h2_mechanism
-    from phd_gb300.surrogate import DEFAULT_GATE, STRICT_GATE, train_ensemble
+    from phd_gb300.surrogate import DEFAULT_GATE, STRICT_GATE, calibrate_cap, train_ensemble
     gate = STRICT_GATE if args.gate == "strict" else DEFAULT_GATE
     mech = h2_mechanism()
     t0 = time.perf_counter()
     nets = train_ensemble(mech, n=args.train, seed=31, epochs=args.epochs)
     t_train = time.perf_counter() - t0
+    calib = None
+    if args.gate == "calibrated":   # the dT cap chosen on 2^20 held-out labelled reactors
+        gate, calib = calibrate_cap(nets, mech, DEFAULT_GATE)
     n = args.cells
     T = torch.empty(n, dtype=torch.float64, device="cuda:0")
     rho, dt = torch.empty_like(T), torch.empty_like(T)
@@ -437,7 +440,8 @@ def run_surrogate(args):
         "vs_baseline": None, "dtype": "bf16 network, f64 integrator", "data": "synthetic (seeded PCG64)",
         "config": {"workload": "independent H2/air reactors (batched-chemistry distribution)", "cells": n,
                    "training": {"samples": args.train, "epochs": args.epochs, "networks": 2, "seconds": t_train},
-                   "gate": {"name": args.gate, "values": list(gate)}, "l2": "inputs larger than L2"},
+                   "gate": {"name": args.gate, "values": gate_json(gate), "calibration": calib},
+                   "l2": "inputs larger than L2"},
         "bdf": {"value": n / (bdf_ms * 1e-3) / 1e6, "unit": "Mcells/s", "ms": bdf_ms},
         "speedup_vs_bdf": bdf_ms / ms,
         "fallback_frac": float(np.mean([r["fallback"] for r in runs])) / n,
@@ -447,9 +451,14 @@ def run_surrogate(args):
         "roofline": {"bound": "tensor", "kernel": "k_mlp_tc (two networks, with the feature kernel)",
                      "achieved": tflops, "peak": peak, "unit": "TFLOP/s", "frac": tflops / peak,
                      "traffic": None, "network_ms": ms_net},
-        # per 2^20-reactor chunk: 2 feature kernels, 2 tensor-core networks, the gate, the BDF fallback
-        "gpu_launches": args.steps * 6 * ((n + (1 << 20) - 1) >> 20), "clocks": clk.summary(),
+        # per 2^20-reactor chunk: 2 feature kernels, 2 tensor-core networks, the gate; one BDF fallback launch
+        "gpu_launches": args.steps * (5 * ((n + (1 << 20) - 1) >> 20) + 1), "clocks": clk.summary(),
     }
+
+
+def gate_json(gate):
+    """Gate values for the JSON line: an infinite dT cap (no cap) as null."""
+    return [float(x) if np.isfinite(x) else None for x in gate]
 
 
 def workload_note(chem, eg):
@@ -541,7 +550,9 @@ def main():
                     help="reactors of the batch (default 2^20) and surrogate (default 512*256*256) workloads")
     ap.add_argument("--train", type=int, default=1 << 22, help="training reactors of the surrogate workload")
     ap.add_argument("--epochs", type=int, default=24, help="training epochs of the surrogate workload")
-    ap.add_argument("--gate", default="default", choices=["default", "strict"], help="surrogate error gate")
+    ap.add_argument("--gate", default="calibrated", choices=["calibrated", "default", "strict"],
+                    help="surrogate error gate: the default tolerances with a dT cap calibrated on held-out "
+                         "reactors, the default tolerances alone, or tighter ones")
     ap.add_argument("--nx", type=int, default=256)
     ap.add_argument("--ny", type=int, default=256)
     ap.add_argument("--nz", type=int, default=128)

@@ -250,16 +250,17 @@ int  izem_mlp_grads(izem_mlp* m, int M, const float* x, const float* t, double* 
 int  izem_mlp_train(izem_mlp* m, long long n, const float* x, const float* t, int device_ptrs,
                     int epochs, int batch, float lr, unsigned seed, double* losses);
 /* Surrogate chemistry step on independent reactors with the per-cell error
- * gate (training envelope, element conservation of dY, internal-energy
- * consistency of dT, agreement with a second independently trained network
- * m2 when m2 is not NULL, the prediction then being the mean of the two);
- * rejected cells are integrated by the BDF method.
- * gate9 = {Tmin, Tmax, dtmin, dtmax, tol_el, tol_T_abs, tol_T_rel,
- * tol_ens_abs, tol_ens_rel}; kncf[kk][nele] element counts; stats3 =
+ * gate (training envelope, a cap on the predicted |dT|, element conservation
+ * of dY, internal-energy consistency of dT, agreement with a second
+ * independently trained network m2 when m2 is not NULL, the prediction then
+ * being the mean of the two); rejected cells are integrated by the BDF
+ * method (no counterpart in the reference).
+ * gate10 = {Tmin, Tmax, dtmin, dtmax, tol_el, tol_T_abs, tol_T_rel,
+ * tol_ens_abs, tol_ens_rel, dT_cap}; kncf[kk][nele] element counts; stats3 =
  * {fallback cells, max BDF steps, failed cells}; ms2 = {total ms, MLP ms}. */
 int  izem_gpu_psr_batch_mlp(izem_mlp* m, izem_mlp* m2, const izem_mech* mech, int n, double* T,
                             const double* rho, double* Y, const double* dt, int device_ptrs,
-                            const double* gate9, const int* kncf, int nele, double* dT_pred,
+                            const double* gate10, const int* kncf, int nele, double* dT_pred,
                             int* stats3, float* ms2);
 /* No counterpart in the reference.  Inference for callers that cannot
  * allocate device memory while they run -- a solver whose own arena (or a
@@ -280,12 +281,12 @@ int  izem_gpu_psr_batch_mlp(izem_mlp* m, izem_mlp* m2, const izem_mech* mech, in
 #define IZEM_MLP_NOALLOC_MAX_ROWS 4096
 int  izem_mlp_forward_noalloc(izem_mlp* m, int M, const float* d_x, float* d_y, void* stream);
 /* Surrogate used by izem_gpu_chem_step(..., IZEM_CHEM_MLP, ...): networks m
- * (and optional partner m2, see izem_gpu_psr_batch_mlp), gate9 and the
+ * (and optional partner m2, see izem_gpu_psr_batch_mlp), gate10 and the
  * element counts kncf[nrv][nele] (no counterpart in the reference).  The
  * handles stay owned by the caller.  izem_gpu_chem_surrogate_stats reports
  * the last such step: window cells, cells sent to the BDF method, total and
  * network-only milliseconds. */
-int  izem_gpu_set_surrogate(izem_ctx* ctx, izem_mlp* m, izem_mlp* m2, const double* gate9,
+int  izem_gpu_set_surrogate(izem_ctx* ctx, izem_mlp* m, izem_mlp* m2, const double* gate10,
                             const int* kncf, int nele);
 int  izem_gpu_chem_surrogate_stats(izem_ctx* ctx, long long* cells, int* fallback, float* ms_total,
                                    float* ms_network);

@@ -1221,10 +1221,13 @@ struct GateArgs {
   double tol_el;                     // relative element residual
   double tol_T_abs, tol_T_rel;       // energy-consistency of dT [K]
   double tol_ens_abs, tol_ens_rel;   // agreement of two independently trained networks on dT [K]
+  double dT_cap;                     // largest predicted |dT| accepted [K]
 };
 
 // Decode the surrogate output, gate it, and write accepted cells in place.
-// Gate: (1) state inside the training envelope; (2) element conservation of
+// Gate: (1) state inside the training envelope, and a predicted |dT| not
+// above the cap (igniting cells, where the network's error is largest, go
+// to the integrator); (2) element conservation of
 // the predicted dY (H, O, N, from the species composition); (3) the
 // predicted dT agrees with the temperature that conserves internal energy
 // (constant-volume reactor) for the predicted composition.  Accepted cells
@@ -1256,6 +1259,7 @@ __global__ void k_decode_gate(int n, const float* out, const float* out2, int ld
     if (fabs(dT2 - dTp) > ga.tol_ens_abs + ga.tol_ens_rel * fabs(dTp)) ok = false;
     dTp = 0.5 * (dTp + dT2);
   }
+  if (!(fabs(dTp) <= ga.dT_cap)) ok = false;
   if (dT_pred) dT_pred[q] = dTp;
   // element residuals
   for (int e = 0; e < nele && ok; ++e) {
@@ -1395,9 +1399,10 @@ cudaError_t chem_launch_featurize(int n, const double* T, const double* rho, con
 
 cudaError_t chem_launch_decode_gate(int n, const float* out, const float* out2, int ldo, const float* d_norm,
                                     const float* d_norm2, double* T, const double* rho, double* Y, const double* dt,
-                                    const double* gate9, const int* d_kncf, int nele, int* list, int base,
+                                    const double* gate10, const int* d_kncf, int nele, int* list, int base,
                                     unsigned* count, double* dT_pred, ChemStats* stats, cudaStream_t s) {
-  GateArgs ga{gate9[0], gate9[1], gate9[2], gate9[3], gate9[4], gate9[5], gate9[6], gate9[7], gate9[8]};
+  GateArgs ga{gate10[0], gate10[1], gate10[2], gate10[3], gate10[4],
+              gate10[5], gate10[6], gate10[7], gate10[8], gate10[9]};
   k_decode_gate<9><<<(n + 127) / 128, 128, 0, s>>>(n, out, out2, ldo, d_norm, d_norm2, T, rho, Y, dt, ga, d_kncf, nele,
                                                    list, base, count, dT_pred, stats);
   return cudaGetLastError();

@@ -48,7 +48,7 @@ struct izem_ctx {
   // learned surrogate for chemistry mode IZEM_CHEM_MLP
   izem_mlp* sur_m = nullptr;
   izem_mlp* sur_m2 = nullptr;
-  double sur_gate[9] = {};
+  double sur_gate[10] = {};
   std::vector<int> sur_kncf;
   int sur_nele = 0;
   long long sur_cap = 0;                  // reactor buffers for the window

@@ -667,11 +667,11 @@ int izem_gpu_set_mechanism(izem_ctx* c, const izem_mech* mech) {
   return IZEM_OK;
 }
 
-int izem_gpu_set_surrogate(izem_ctx* c, izem_mlp* m, izem_mlp* m2, const double* gate9, const int* kncf, int nele) {
-  if (!c || !m || !gate9 || !kncf || nele <= 0) return IZEM_ERR_ARG;
+int izem_gpu_set_surrogate(izem_ctx* c, izem_mlp* m, izem_mlp* m2, const double* gate10, const int* kncf, int nele) {
+  if (!c || !m || !gate10 || !kncf || nele <= 0) return IZEM_ERR_ARG;
   c->sur_m = m;
   c->sur_m2 = m2;
-  std::memcpy(c->sur_gate, gate9, sizeof(c->sur_gate));
+  std::memcpy(c->sur_gate, gate10, sizeof(c->sur_gate));
   c->sur_kncf.assign(kncf, kncf + (size_t)c->cfg.nrv * nele);
   c->sur_nele = nele;
   return IZEM_OK;

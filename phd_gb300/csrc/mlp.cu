@@ -571,8 +571,8 @@ int izem_mlp_train(izem_mlp* m, long long n, const float* x, const float* t, int
 // izem_gpu_psr_batch): MLP inference and the error gate in chunks of 2^20
 // rows, the rejected cells of all chunks collected in one list, then one
 // BDF launch over that list (one load-balanced pass, so the slowest stiff
-// cell is waited for once, not once per chunk).  gate9 = {Tmin, Tmax, dtmin, dtmax,
-// tol_el, tol_T_abs, tol_T_rel, tol_ens_abs, tol_ens_rel}; m2 (optional) is
+// cell is waited for once, not once per chunk).  gate10 = {Tmin, Tmax, dtmin, dtmax,
+// tol_el, tol_T_abs, tol_T_rel, tol_ens_abs, tol_ens_rel, dT_cap}; m2 (optional) is
 // a second, independently trained network: the prediction is the mean of
 // the two, and cells where their dT disagree are rejected;
 // kncf = element counts [kk][nele].
@@ -580,9 +580,9 @@ int izem_mlp_train(izem_mlp* m, long long n, const float* x, const float* t, int
 // network temperature increment.  stats3 = {fallback cells, max BDF steps,
 // failed}; ms2 = {total kernel ms, MLP-only ms}.
 int izem_gpu_psr_batch_mlp(izem_mlp* m, izem_mlp* m2, const izem_mech* mech, int n, double* T, const double* rho,
-                           double* Y, const double* dt, int device_ptrs, const double* gate9, const int* kncf, int nele,
+                           double* Y, const double* dt, int device_ptrs, const double* gate10, const int* kncf, int nele,
                            double* dT_pred, int* stats3, float* ms2) {
-  if (!m || !mech || n <= 0 || !T || !rho || !Y || !dt || !gate9 || !kncf || mech->kk != 9) return IZEM_ERR_ARG;
+  if (!m || !mech || n <= 0 || !T || !rho || !Y || !dt || !gate10 || !kncf || mech->kk != 9) return IZEM_ERR_ARG;
   if (nele <= 0 || nele > 8) return IZEM_ERR_ARG;
   const int CH = 1 << 20;
   const int chunk = n < CH ? n : CH;
@@ -639,7 +639,7 @@ int izem_gpu_psr_batch_mlp(izem_mlp* m, izem_mlp* m2, const izem_mech* mech, int
     }
     cudaEventRecord(ev[3 + 2 * ci], s);
     chem_launch_decode_gate(cn, m->iout, m2 ? m2->iout : nullptr, OUTP, m->d_norm, m2 ? m2->d_norm : nullptr, dT + c0,
-                            drho + c0, dY + (size_t)c0 * kk, ddt + c0, gate9, m->g_kncf, nele, m->g_list, c0,
+                            drho + c0, dY + (size_t)c0 * kk, ddt + c0, gate10, m->g_kncf, nele, m->g_list, c0,
                             m->g_count, ddTp ? ddTp + c0 : nullptr, m->g_stats, s);
   }
   if (rc == IZEM_OK && chem_launch_list(m->g_list, m->g_count, dT, drho, dY, ddt, m->g_counter, m->g_stats, s) !=

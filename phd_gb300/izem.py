@@ -275,13 +275,14 @@ class IzemGPU:
     def set_surrogate(self, net, partner=None, gate=None, kncf=None):
         """Learned chemistry for reaction_selec(mode=CHEM_MLP): a
         phd_gb300.surrogate.Surrogate (and optional partner network), the
-        error gate (9 numbers) and the element counts kncf[nrv][nele]."""
-        from .surrogate import DEFAULT_GATE
+        error gate (10 numbers, see surrogate.DEFAULT_GATE; 9 without the dT
+        cap) and the element counts kncf[nrv][nele]."""
+        from .surrogate import DEFAULT_GATE, gate10
         from .thd import load_species
         if kncf is None:
             kncf = load_species("h2air9")["kncf"]
         self._sur = (net, partner)
-        self._gate = np.ascontiguousarray(np.array(DEFAULT_GATE if gate is None else gate, dtype=np.float64))
+        self._gate = gate10(DEFAULT_GATE if gate is None else gate)
         self._kncf = np.ascontiguousarray(np.array(kncf, dtype=np.int32))
         self._check(self.lib.izem_gpu_set_surrogate(self.h, net.h, partner.h if partner is not None else None,
                                                     _ptr(self._gate), _ptr(self._kncf, C.POINTER(C.c_int)),

@@ -178,13 +178,13 @@ class Surrogate:
         are rejected.  Returns dict with fallback count, times and the raw
         predicted dT."""
         kncf = np.ascontiguousarray(np.array(load_species("h2air9")["kncf"], dtype=np.int32))
-        g7 = np.ascontiguousarray(np.array(gate, dtype=np.float64))
+        g10 = gate10(gate)
         dTp = np.zeros(len(T))
         st3 = np.zeros(3, dtype=np.int32)
         ms2 = np.zeros(2, dtype=np.float32)
         rc = self.lib.izem_gpu_psr_batch_mlp(self.h, partner.h if partner is not None else None, C.byref(mech),
                                              len(T), T.ctypes.data, rho.ctypes.data,
-                                             Y.ctypes.data, dt.ctypes.data, 0, g7.ctypes.data, kncf.ctypes.data,
+                                             Y.ctypes.data, dt.ctypes.data, 0, g10.ctypes.data, kncf.ctypes.data,
                                              kncf.shape[1], dTp.ctypes.data, st3.ctypes.data, ms2.ctypes.data)
         if rc:
             raise IzemError(rc, "izem_gpu_psr_batch_mlp")
@@ -197,12 +197,12 @@ class Surrogate:
         work on them must be complete.  Returns the same dictionary without
         dT_pred."""
         kncf = np.ascontiguousarray(np.array(load_species("h2air9")["kncf"], dtype=np.int32))
-        g9 = np.ascontiguousarray(np.array(gate, dtype=np.float64))
+        g10 = gate10(gate)
         st3 = np.zeros(3, dtype=np.int32)
         ms2 = np.zeros(2, dtype=np.float32)
         rc = self.lib.izem_gpu_psr_batch_mlp(self.h, partner.h if partner is not None else None, C.byref(mech), n,
                                              T.data_ptr(), rho.data_ptr(), Y.data_ptr(), dt.data_ptr(), 1,
-                                             g9.ctypes.data, kncf.ctypes.data, kncf.shape[1], None,
+                                             g10.ctypes.data, kncf.ctypes.data, kncf.shape[1], None,
                                              st3.ctypes.data, ms2.ctypes.data)
         if rc:
             raise IzemError(rc, "izem_gpu_psr_batch_mlp")
@@ -210,10 +210,60 @@ class Surrogate:
                 "ms_mlp": float(ms2[1])}
 
 
-# Tmin, Tmax, dtmin, dtmax, tol_el, tol_T_abs [K], tol_T_rel, tol_ens_abs [K], tol_ens_rel
-DEFAULT_GATE = (800.0, 2400.0, 1e-8, 1e-6, 2e-3, 2.0, 0.003, 1.0, 0.002)
+# Tmin, Tmax, dtmin, dtmax, tol_el, tol_T_abs [K], tol_T_rel, tol_ens_abs [K], tol_ens_rel,
+# dT_cap [K] (largest predicted |dT| accepted)
+DEFAULT_GATE = (800.0, 2400.0, 1e-8, 1e-6, 2e-3, 2.0, 0.003, 1.0, 0.002, float("inf"))
 # tighter energy-consistency and agreement tolerances: more cells go to BDF
-STRICT_GATE = (800.0, 2400.0, 1e-8, 1e-6, 2e-3, 0.5, 0.001, 0.2, 0.0003)
+STRICT_GATE = (800.0, 2400.0, 1e-8, 1e-6, 2e-3, 0.5, 0.001, 0.2, 0.0003, float("inf"))
+
+
+def gate10(gate):
+    """The error gate as the 10 doubles the library reads; a 9-value gate
+    (without the dT cap) is accepted and gets no cap."""
+    g = [float(x) for x in gate]
+    if len(g) == 9:
+        g.append(float("inf"))
+    if len(g) != 10:
+        raise ValueError("the error gate has 10 values (Tmin, Tmax, dtmin, dtmax, tol_el, tol_T_abs, tol_T_rel, "
+                         "tol_ens_abs, tol_ens_rel, dT_cap)")
+    return np.ascontiguousarray(np.array(g, dtype=np.float64))
+
+
+CAP_LADDER = (10.0, 20.0, 30.0, 50.0, 75.0, 100.0, 150.0, 200.0, 300.0, 400.0, 800.0)
+
+
+def calibrate_cap(nets, mech, gate=DEFAULT_GATE, n=1 << 20, seed=977, target=0.005, caps=CAP_LADDER):
+    """Choose the gate's cap on the predicted |dT| on held-out reactors: n
+    reactors of the batched-chemistry distribution (another seed than the
+    training and test sets) are labelled by the FP64 BDF integrator and run
+    through the gated step without a cap; the cap is the largest value of
+    `caps` for which every accepted cell whose predicted |dT| is at most the
+    cap has an error within target x the largest |dT| of the set.  Returns
+    (gate with that cap, per-cap table)."""
+    from .ics import batched_reactors
+    T, rho, Y, dt = batched_reactors(n, seed=seed)
+    Tb, Yb = T.copy(), Y.copy()
+    psr_batch(mech, Tb, rho.copy(), Yb, dt.copy())
+    ref = Tb - T
+    Ts, Ys = T.copy(), Y.copy()
+    g = list(gate10(gate))
+    g[9] = float("inf")
+    r = nets[0].chem_step(mech, Ts, rho.copy(), Ys, dt.copy(), g, partner=nets[1] if len(nets) > 1 else None)
+    err = np.abs((Ts - T) - ref)
+    acc = err > 0.0          # rejected cells repeat the BDF result exactly
+    pred = np.abs(r["dT_pred"])
+    scale = float(np.abs(ref).max())
+    table, best = [], None
+    for cap in sorted(caps):
+        keep = acc & (pred <= cap)
+        worst = float(err[keep].max()) if keep.any() else 0.0
+        table.append({"cap_K": cap, "max_err_K": worst, "rejected_by_cap_frac": float((acc & ~keep).sum()) / n})
+        if worst <= target * scale and (best is None or cap > best):
+            best = cap
+        elif worst > target * scale:
+            break
+    g[9] = float(best if best is not None else min(caps))
+    return tuple(g), {"cells": n, "seed": seed, "target_frac": target, "scale_K": scale, "table": table}
 
 
 def train_ensemble(mech, n=1 << 22, seed=31, epochs=30, batch=4096, lr=1e-3, members=2, log=None):
@@ -308,4 +358,5 @@ def flow_gate(X, Yt, dT_tol_frac=0.002):
     scale = float(np.abs(Yt[:, -1]).max())
     dt = np.exp(X[:, 11])
     a = dT_tol_frac * scale
-    return (float(X[:, 0].min()), float(X[:, 0].max()), float(dt.min()), float(dt.max()), 2e-3, a, 0.02, 0.5 * a, 0.005)
+    return (float(X[:, 0].min()), float(X[:, 0].max()), float(dt.min()), float(dt.max()), 2e-3, a, 0.02, 0.5 * a, 0.005,
+            float("inf"))

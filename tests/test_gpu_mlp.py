@@ -14,7 +14,7 @@ from oracle import mlp_oracle as mo
 from phd_gb300 import ics
 from phd_gb300.izem import psr_batch
 from phd_gb300.mech import h2_mechanism
-from phd_gb300.surrogate import DEFAULT_GATE, Surrogate, features, train_ensemble, training_set
+from phd_gb300.surrogate import DEFAULT_GATE, Surrogate, calibrate_cap, features, train_ensemble, training_set
 
 pytestmark = pytest.mark.gpu
 
@@ -80,6 +80,18 @@ def test_surrogate_gains_over_bdf_with_gate():
     assert frac_fb < 1.0
     print("surrogate: fallback %.3f, max err %.3g K (scale %.3g K), BDF %.1f ms, surrogate %.1f ms (MLP %.1f ms)"
           % (frac_fb, err.max(), scale, ms_bdf, r["ms"], r["ms_mlp"]))
+    # the same step with the dT cap calibrated on other held-out reactors:
+    # cells predicted above the cap get the BDF result bit for bit, the
+    # others the same surrogate result as without the cap
+    gcap, cal = calibrate_cap([s, s2], mech, DEFAULT_GATE, n=1 << 18)
+    Tc, Yc = T.copy(), Y.copy()
+    rc = s.chem_step(mech, Tc, rho.copy(), Yc, dt.copy(), gcap, partner=s2)
+    errc = np.abs((Tc - T) - dT_ref)
+    over = np.abs(rc["dT_pred"]) > gcap[9]
+    assert rc["failed"] == 0 and rc["fallback"] >= r["fallback"]
+    assert np.array_equal(Tc[over], Tb[over]) and np.array_equal(Yc[over], Yb[over])
+    assert np.all(errc <= err)
+    print("dT cap %.0f K: fallback %.3f, max err %.3g K" % (gcap[9], rc["fallback"] / len(T), errc.max()))
 
 
 def _small_flow():
