@@ -294,10 +294,12 @@ int  izem_gpu_chem_surrogate_stats(izem_ctx* ctx, long long* cells, int* fallbac
 /* Autotuning (no counterpart in the reference): times the candidate thread
  * blocks (64, 128, 256) of the face-flux and viscous point kernels on the
  * context's current state, and -- when a mechanism is set and chem_dt > 0
- * -- of the persistent chemistry kernel on a copy of the reaction window
- * for a half step chem_dt (code units); keeps the fastest of each.  Results
- * do not depend on the choice.  report (may be NULL) receives the timings
- * as JSON.  Call after the state is uploaded, before the timed steps. */
+ * -- the register-budget variants of the persistent chemistry kernels
+ * (128 threads, 8 to 4 resident blocks per SM) on a copy of the reaction
+ * window for a half step chem_dt (code units); keeps the fastest of each.
+ * Results do not depend on the choice.  report (may be NULL, at least 2048
+ * bytes otherwise) receives the timings as JSON.  Call after the state is
+ * uploaded, before the timed steps. */
 int  izem_gpu_autotune(izem_ctx* ctx, double chem_dt, char* report, int report_len);
 
 /* Device timing of the calls above on the context's stream (CUDA events). */

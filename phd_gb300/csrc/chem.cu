@@ -1133,8 +1133,15 @@ __global__ void k_chem_scatter(ChemField f, const double* T, const double* Y, Ch
   if (f.dT_out) f.dT_out[q] = T[q] - T0;
 }
 
-template <int KK>
-__global__ void __launch_bounds__(256) k_psr_field(ChemField f, unsigned* counter, ChemStats* stats) {
+// The persistent chemistry kernels come in variants that differ only in
+// the register budget the compiler is held to (128 threads per block, at
+// least MINB blocks resident per SM): fewer registers give more resident
+// warps to hide the FP64 and local-memory latency of the BDF state machine,
+// more registers fewer spills.  The arithmetic is the same in every variant.
+constexpr int kChemThreads = 128;
+
+template <int KK, int MINB>
+__global__ void __launch_bounds__(kChemThreads, MINB) k_psr_field(ChemField f, unsigned* counter, ChemStats* stats) {
   constexpr int N = KK + 1;
   const long long ncell = (long long)f.wx * f.wy * f.wz;
   const long long nc = f.ncell;
@@ -1170,9 +1177,10 @@ __global__ void __launch_bounds__(256) k_psr_field(ChemField f, unsigned* counte
   rc_drive<KK>((unsigned)ncell, counter, load, store);
 }
 
-template <int KK>
-__global__ void __launch_bounds__(256) k_psr_batch(int n, double* T, const double* rho, double* Y, const double* dt,
-                                                   int* istate, int* nsteps, unsigned* counter, ChemStats* stats) {
+template <int KK, int MINB>
+__global__ void __launch_bounds__(kChemThreads, MINB) k_psr_batch(int n, double* T, const double* rho, double* Y,
+                                                                  const double* dt, int* istate, int* nsteps,
+                                                                  unsigned* counter, ChemStats* stats) {
   constexpr int N = KK + 1;
   auto load = [&](unsigned q, double& rh, double* z, double& tf) {
     z[0] = T[q];
@@ -1305,9 +1313,10 @@ __global__ void k_decode_gate(int n, const float* out, const float* out2, int ld
   }
 }
 
-template <int KK>
-__global__ void __launch_bounds__(256) k_psr_list(const int* list, const unsigned* count, double* T, const double* rho,
-                                                  double* Y, const double* dt, unsigned* counter, ChemStats* stats) {
+template <int KK, int MINB>
+__global__ void __launch_bounds__(kChemThreads, MINB) k_psr_list(const int* list, const unsigned* count, double* T,
+                                                                 const double* rho, double* Y, const double* dt,
+                                                                 unsigned* counter, ChemStats* stats) {
   constexpr int N = KK + 1;
   auto load = [&](unsigned w, double& rh, double* z, double& tf) {
     const int q = list[w];
@@ -1327,17 +1336,35 @@ __global__ void __launch_bounds__(256) k_psr_list(const int* list, const unsigne
   rc_drive<KK>(*count, counter, load, store);
 }
 
-// Threads per block of the persistent chemistry kernels: 128 until an
-// autotuning pass (izem_gpu_autotune) measures the candidates on the
-// caller's reactors and keeps the fastest (the same for every context of
-// the process).
-int g_chem_tpb = 128;
+struct ChemVariant {
+  int min_blocks;
+  void (*field)(ChemField, unsigned*, ChemStats*);
+  void (*batch)(int, double*, const double*, double*, const double*, int*, int*, unsigned*, ChemStats*);
+  void (*list)(const int*, const unsigned*, double*, const double*, double*, const double*, unsigned*, ChemStats*);
+};
+
+template <int MINB>
+constexpr ChemVariant chem_variant_of() {
+  return ChemVariant{MINB, k_psr_field<9, MINB>, k_psr_batch<9, MINB>, k_psr_list<9, MINB>};
+}
+
+const ChemVariant kChemVariants[IZEM_CHEM_VARIANTS] = {chem_variant_of<8>(), chem_variant_of<7>(),
+                                                       chem_variant_of<6>(), chem_variant_of<5>(),
+                                                       chem_variant_of<4>()};
+
+// Variant of the persistent chemistry kernels in use: 7 blocks of 128
+// threads per SM until an autotuning pass (izem_gpu_autotune) times the
+// variants on the caller's reactors and keeps the fastest (the same for every
+// context of the process).
+int g_chem_variant = 1;
 
 int chem_grid(int* blocks) {
   int dev = 0, sms = 0, per = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return -1;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return -1;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_psr_batch<9>, g_chem_tpb, 0) != cudaSuccess) return -1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kChemVariants[g_chem_variant].batch, kChemThreads, 0) !=
+      cudaSuccess)
+    return -1;
   *blocks = sms * (per > 0 ? per : 1);
   return 0;
 }
@@ -1345,8 +1372,18 @@ int chem_grid(int* blocks) {
 }  // namespace
 
 // ---------------------------------------------------------- host side -------
-void chem_set_block(int tpb) { g_chem_tpb = tpb; }
-int chem_block() { return g_chem_tpb; }
+int chem_set_variant(int v) {
+  if (v < 0 || v >= IZEM_CHEM_VARIANTS) return -1;
+  g_chem_variant = v;
+  return 0;
+}
+int chem_variant() { return g_chem_variant; }
+int chem_variant_min_blocks(int v) { return (v >= 0 && v < IZEM_CHEM_VARIANTS) ? kChemVariants[v].min_blocks : 0; }
+int chem_variant_registers(int v) {
+  cudaFuncAttributes a{};
+  if (v < 0 || v >= IZEM_CHEM_VARIANTS || cudaFuncGetAttributes(&a, kChemVariants[v].batch) != cudaSuccess) return 0;
+  return a.numRegs;
+}
 
 cudaError_t chem_upload_mech(const izem_mech* m) {
   cudaError_t e = cudaMemcpyToSymbol(c_mech_dev, m, sizeof(izem_mech));
@@ -1364,7 +1401,7 @@ cudaError_t chem_launch_field(const ChemField& f, unsigned* d_counter, ChemStats
   cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(unsigned), s);
   if (e != cudaSuccess) return e;
   if (kk != 9) return cudaErrorInvalidValue;
-  k_psr_field<9><<<blocks, g_chem_tpb, 0, s>>>(f, d_counter, d_stats);
+  kChemVariants[g_chem_variant].field<<<blocks, kChemThreads, 0, s>>>(f, d_counter, d_stats);
   return cudaGetLastError();
 }
 
@@ -1375,7 +1412,8 @@ cudaError_t chem_launch_batch(int n, double* T, const double* rho, double* Y, co
   cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(unsigned), s);
   if (e != cudaSuccess) return e;
   if (kk != 9) return cudaErrorInvalidValue;
-  k_psr_batch<9><<<blocks, g_chem_tpb, 0, s>>>(n, T, rho, Y, dt, istate, nsteps, d_counter, d_stats);
+  kChemVariants[g_chem_variant].batch<<<blocks, kChemThreads, 0, s>>>(n, T, rho, Y, dt, istate, nsteps, d_counter,
+                                                                      d_stats);
   return cudaGetLastError();
 }
 
@@ -1414,6 +1452,6 @@ cudaError_t chem_launch_list(const int* list, const unsigned* count, double* T, 
   if (chem_grid(&blocks)) return cudaErrorUnknown;
   cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(unsigned), s);
   if (e != cudaSuccess) return e;
-  k_psr_list<9><<<blocks, g_chem_tpb, 0, s>>>(list, count, T, rho, Y, dt, d_counter, d_stats);
+  kChemVariants[g_chem_variant].list<<<blocks, kChemThreads, 0, s>>>(list, count, T, rho, Y, dt, d_counter, d_stats);
   return cudaGetLastError();
 }

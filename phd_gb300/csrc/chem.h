@@ -23,9 +23,14 @@ struct ChemStats {
 };
 
 cudaError_t chem_upload_mech(const izem_mech* m);
-// threads per block of the persistent chemistry kernels (set by the autotuner)
-void chem_set_block(int tpb);
-int chem_block();
+// Register-budget variants of the persistent chemistry kernels (128 threads
+// per block; variant v keeps at least 8 - v blocks resident per SM), chosen
+// by the autotuner.  chem_set_variant returns -1 for an unknown variant.
+#define IZEM_CHEM_VARIANTS 5
+int chem_set_variant(int v);
+int chem_variant();
+int chem_variant_min_blocks(int v);
+int chem_variant_registers(int v);
 cudaError_t chem_launch_field(const ChemField& f, unsigned* d_counter, ChemStats* d_stats, cudaStream_t s, int kk);
 cudaError_t chem_launch_batch(int n, double* T, const double* rho, double* Y, const double* dt, int* istate,
                               int* nsteps, unsigned* d_counter, ChemStats* d_stats, cudaStream_t s, int kk);

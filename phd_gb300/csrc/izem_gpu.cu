@@ -846,11 +846,13 @@ int izem_gpu_autotune(izem_ctx* c, double chem_dt, char* report, int report_len)
           (e = cudaMalloc(&dt, n * 8)) || (e = cudaMalloc(&T0, n * 8)) || (e = cudaMalloc(&Y0, n * 72))) {
         rc = ctx_fail(c, IZEM_ERR_NOMEM, "autotune buffers", e);
       } else {
+        // the register-budget variants of the persistent kernel (128 threads,
+        // 8 down to 4 resident blocks per SM)
         chem_launch_gather(f, T0, rho, Y0, dt, c->stream);
-        float ms[3];
-        int best = 1;
-        for (int q = 0; q < 3; ++q) {
-          chem_set_block(kTuneCand[q]);
+        float ms[IZEM_CHEM_VARIANTS];
+        int best = chem_variant();
+        for (int q = 0; q < IZEM_CHEM_VARIANTS; ++q) {
+          chem_set_variant(q);
           auto body = [&] {
             cudaMemcpyAsync(T, T0, n * 8, cudaMemcpyDeviceToDevice, c->stream);
             cudaMemcpyAsync(Y, Y0, n * 72, cudaMemcpyDeviceToDevice, c->stream);
@@ -860,8 +862,18 @@ int izem_gpu_autotune(izem_ctx* c, double chem_dt, char* report, int report_len)
           ms[q] = tune_time(c, 1, body);
           if (ms[q] < ms[best]) best = q;
         }
-        chem_set_block(kTuneCand[best]);
-        tune_report(rep, "chem_psr", ms, kTuneCand[best]);
+        chem_set_variant(best);
+        char buf[160];
+        std::snprintf(buf, sizeof(buf), "%s\"chem_psr\": {", rep.size() > 1 ? ", " : "");
+        rep += buf;
+        for (int q = 0; q < IZEM_CHEM_VARIANTS; ++q) {
+          std::snprintf(buf, sizeof(buf), "\"128x%d (%d regs)\": %.4f, ", chem_variant_min_blocks(q),
+                        chem_variant_registers(q), ms[q]);
+          rep += buf;
+        }
+        std::snprintf(buf, sizeof(buf), "\"chosen\": \"128x%d (%d regs)\"}", chem_variant_min_blocks(best),
+                      chem_variant_registers(best));
+        rep += buf;
       }
       cudaFree(T); cudaFree(rho); cudaFree(Y); cudaFree(dt); cudaFree(T0); cudaFree(Y0);
     }

@@ -253,10 +253,10 @@ class IzemGPU:
         return dt4, dtm.value
 
     def autotune(self, chem_dt=0.0):
-        """Choose the thread blocks of the face-flux, viscous point and (with
-        chem_dt > 0 and a mechanism set) chemistry kernels by timing the
-        candidates on the current state; returns the timings [ms] and
-        choices."""
+        """Choose the thread blocks of the face-flux and viscous point kernels
+        and (with chem_dt > 0 and a mechanism set) the register-budget
+        variant of the persistent chemistry kernels by timing the candidates
+        on the current state; returns the timings [ms] and choices."""
         import json
         buf = C.create_string_buffer(2048)
         self._check(self.lib.izem_gpu_autotune(self.h, float(chem_dt), buf, 2048), "autotune")
