@@ -301,6 +301,11 @@ int  izem_gpu_chem_surrogate_stats(izem_ctx* ctx, long long* cells, int* fallbac
  * bytes otherwise) receives the timings as JSON.  Call after the state is
  * uploaded, before the timed steps. */
 int  izem_gpu_autotune(izem_ctx* ctx, double chem_dt, char* report, int report_len);
+/* Pins the register-budget variant of the persistent chemistry kernels
+ * (0..4: 128 threads and 8 - v resident blocks per SM) for every context of
+ * the process, as izem_gpu_autotune would choose it (no counterpart in the
+ * reference); IZEM_ERR_ARG outside 0..4. */
+int  izem_gpu_set_chem_variant(int variant);
 
 /* Device timing of the calls above on the context's stream (CUDA events). */
 int  izem_gpu_timer_start(izem_ctx* ctx);

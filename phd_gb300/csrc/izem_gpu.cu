@@ -885,6 +885,8 @@ int izem_gpu_autotune(izem_ctx* c, double chem_dt, char* report, int report_len)
   return rc;
 }
 
+int izem_gpu_set_chem_variant(int variant) { return chem_set_variant(variant) == 0 ? IZEM_OK : IZEM_ERR_ARG; }
+
 int izem_gpu_timer_start(izem_ctx* c) {
   if (!c) return IZEM_ERR_ARG;
   CK(cudaEventRecord(c->t0, c->stream));

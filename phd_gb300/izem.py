@@ -75,6 +75,7 @@ def load_library(path=None):
         "izem_gpu_set_surrogate": (C.c_int, [P, P, P, _dp, C.POINTER(C.c_int), C.c_int]),
         "izem_gpu_set_eglib": (C.c_int, [P, C.POINTER(IzemEglib)]),
         "izem_gpu_autotune": (C.c_int, [P, C.c_double, C.c_char_p, C.c_int]),
+        "izem_gpu_set_chem_variant": (C.c_int, [C.c_int]),
         "izem_gpu_chem_surrogate_stats": (C.c_int, [P, C.POINTER(C.c_longlong), C.POINTER(C.c_int),
                                                     C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     }
@@ -261,6 +262,11 @@ class IzemGPU:
         buf = C.create_string_buffer(2048)
         self._check(self.lib.izem_gpu_autotune(self.h, float(chem_dt), buf, 2048), "autotune")
         return json.loads(buf.value.decode())
+
+    def set_chem_variant(self, v):
+        """Pin the register-budget variant (0..4) of the persistent chemistry
+        kernels, process-wide, without timing."""
+        self._check(self.lib.izem_gpu_set_chem_variant(int(v)), "set_chem_variant")
 
     def set_eglib(self, link):
         """EGLIB linking data (phd_gb300.thd.eglib_link) for cfg.eglib = 1."""

@@ -180,7 +180,8 @@ def test_autotune_keeps_results():
         if tune:
             rep = g.autotune(chem_dt=0.5)
             assert {"euler_face", "visc_point_eg", "chem_psr"} <= set(rep)
-            assert all(r["chosen"] in (64, 128, 256) for r in rep.values())
+            assert all(rep[k]["chosen"] in (64, 128, 256) for k in ("euler_face", "visc_point_eg"))
+            assert rep["chem_psr"]["chosen"].startswith("128x")
         g.zero_flux()
         g.euler_LLF_x(); g.euler_LLF_y(); g.euler_LLF_z()
         g.viscflux_xyz()
@@ -190,3 +191,18 @@ def test_autotune_keeps_results():
         ref.append((fl, g.download()))
     assert np.array_equal(ref[0][0], ref[1][0])
     assert np.array_equal(ref[0][1]["v"], ref[1][1]["v"]) and np.array_equal(ref[0][1]["T"], ref[1][1]["T"])
+    # every register-budget variant of the chemistry kernels gives the same bits
+    g = _eglib_gpu(cfg, thd, adi, dxi, W.copy(st))
+    g.set_mechanism(h2_mechanism())
+    st0 = g.download()
+    outs = []
+    for v in range(5):
+        g.set_chem_variant(v)
+        g.upload(**st0)
+        g.reaction_selec(0.5)
+        outs.append(g.download())
+    g.set_chem_variant(1)
+    with pytest.raises(Exception):
+        g.set_chem_variant(5)
+    for o in outs[1:]:
+        assert np.array_equal(o["v"], outs[0]["v"]) and np.array_equal(o["T"], outs[0]["T"])
