@@ -297,7 +297,11 @@ int  izem_gpu_chem_surrogate_stats(izem_ctx* ctx, long long* cells, int* fallbac
  * -- the register-budget variants of the persistent chemistry kernels
  * (128 threads, 8 to 4 resident blocks per SM) on a copy of the reaction
  * window for a half step chem_dt (code units); keeps the fastest of each.
- * Results do not depend on the choice.  report (may be NULL, at least 2048
+ * The flow kernels' results do not depend on the choice; the chemistry
+ * variants are separate compilations of the same source, whose results
+ * agree within the integrator's tolerance (the compiler may fuse a multiply
+ * and an add differently under another register limit).  report (may be
+ * NULL, at least 2048
  * bytes otherwise) receives the timings as JSON.  Call after the state is
  * uploaded, before the timed steps. */
 int  izem_gpu_autotune(izem_ctx* ctx, double chem_dt, char* report, int report_len);

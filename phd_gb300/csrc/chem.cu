@@ -1137,7 +1137,10 @@ __global__ void k_chem_scatter(ChemField f, const double* T, const double* Y, Ch
 // the register budget the compiler is held to (128 threads per block, at
 // least MINB blocks resident per SM): fewer registers give more resident
 // warps to hide the FP64 and local-memory latency of the BDF state machine,
-// more registers fewer spills.  The arithmetic is the same in every variant.
+// more registers fewer spills.  The source is the same in every variant;
+// the compiler may fuse a multiply and an add into an FMA differently under
+// another register limit, so the variants agree within the integrator's
+// tolerance rather than to the bit.
 constexpr int kChemThreads = 128;
 
 template <int KK, int MINB>

@@ -165,10 +165,30 @@ def test_rk3_steps_eglib():
     assert np.max(np.abs(interior(got["T"]) - interior(st["T"]))) <= TOL * np.max(st["T"])
 
 
+def _chem_close(a, b):
+    """Two chemistry half steps from the same state by two compilations of
+    the integrator (register-budget variants): ptxas may contract a plain
+    multiply and add into an FMA differently under different register
+    limits, so the results agree within the integrator's tolerance, with
+    the bounds of the GPU-against-oracle chemistry tests, not to the bit.
+    The conserved density, momentum and energy are not touched."""
+    rtol, atol = 1e-6, 1e-10
+    i = (slice(3, -3),) * 3
+    Ta, Tb = a["T"][i], b["T"][i]
+    assert np.all(np.abs(Ta - Tb) <= 100 * (rtol * np.abs(Tb) + atol))
+    va, vb = a["v"][i], b["v"][i]
+    assert np.array_equal(va[..., :5], vb[..., :5])
+    for q in range(5, va.shape[-1]):
+        ya, yb = va[..., q] / va[..., 0], vb[..., q] / vb[..., 0]
+        assert np.max(np.abs(ya - yb)) <= 1e-3 * np.abs(yb).max()
+
+
 def test_autotune_keeps_results():
-    """The autotuner only regroups points into thread blocks: the fluxes and
-    an RK3 step and a chemistry half step after tuning are bit-identical to
-    those before."""
+    """The autotuner regroups points into thread blocks for the flow kernels
+    and picks a register-budget variant of the chemistry kernels: the fluxes
+    and an RK3 step after tuning are bit-identical to those before, and a
+    chemistry half step agrees within the integrator's tolerance for every
+    variant."""
     cfg, thd, adi, dxi, st, info, orc = W.case("mix", 16, eglib=True)
     W.perturb(st, 0.01, seed=5)
     orc.update_primitives(st)
@@ -187,11 +207,13 @@ def test_autotune_keeps_results():
         g.viscflux_xyz()
         fl = g.flux()
         g.rk3(1e-3)
+        after_rk3 = g.download()
         g.reaction_selec(0.5)
-        ref.append((fl, g.download()))
+        ref.append((fl, after_rk3, g.download()))
     assert np.array_equal(ref[0][0], ref[1][0])
     assert np.array_equal(ref[0][1]["v"], ref[1][1]["v"]) and np.array_equal(ref[0][1]["T"], ref[1][1]["T"])
-    # every register-budget variant of the chemistry kernels gives the same bits
+    _chem_close(ref[1][2], ref[0][2])
+    # every register-budget variant from the same state
     g = _eglib_gpu(cfg, thd, adi, dxi, W.copy(st))
     g.set_mechanism(h2_mechanism())
     st0 = g.download()
@@ -204,5 +226,5 @@ def test_autotune_keeps_results():
     g.set_chem_variant(1)
     with pytest.raises(Exception):
         g.set_chem_variant(5)
-    for o in outs[1:]:
-        assert np.array_equal(o["v"], outs[0]["v"]) and np.array_equal(o["T"], outs[0]["T"])
+    for o in outs:
+        _chem_close(o, outs[1])
