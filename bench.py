@@ -113,6 +113,27 @@ def euler_face_bytes(cfg):
     return nf * (nv * 8 + 8 * 8 + 1 + nv * 8)
 
 
+def chem_window(cfg):
+    """Reactors of one chemistry half step: the reaction_dvode window skips
+    ng + 1 cells at every face, and its z bound uses ey
+    (module_reaction.f90:155-159)."""
+    ng = cfg.ng
+    wx = min(cfg.nx, cfg.nx - ng - 1) - ng
+    wy = min(cfg.ny, cfg.ny - ng - 1) - ng
+    wz = min(cfg.ny, cfg.nz - ng - 1) - ng
+    return max(wx, 0) * max(wy, 0) * max(wz, 0)
+
+
+# one window reactor: reads rho, rho*Y (9) and T, writes rho*Y (9) and T
+CHEM_BYTES_PER_REACTOR = 11 * 8 + 10 * 8
+# FP64 flops per BDF step of the persistent chemistry kernel (2 DFMA + DADD +
+# DMUL per thread, summed by ncu over one launch, / the BDF steps of that
+# launch): profiles/k_psr_field_mix64.md
+CHEM_FLOP_PER_BDF_STEP = None
+# DRAM bytes (read + write) per reactor of that launch: the per-thread BDF
+# state in local memory that the L2 does not hold
+CHEM_TRAFFIC_PER_REACTOR = None
+
 EULER_FLOP_PER_FACE = {2: 1400, 9: 2481}   # FP64 flops per face (sensor-off branch): ncu DFMA x2 + DADD + DMUL counts (profiles/euler_face_mix128.md)
 
 
@@ -124,10 +145,13 @@ class Stepper:
         self.g, self.chem, self.mode = g, chem, mode
         self.dtmin, self.DTmax = 1.0, 0.0
         self.log = []   # surrogate half steps: (dt, window cells, fallback cells, ms, network ms)
+        self.bdf_steps = []   # BDF steps summed over the window, per BDF half step
 
     def _chem(self, dt):
         d = self.g.reaction_selec(dt, mode=self.mode)
-        if self.mode == 1:
+        if self.mode == 0:
+            self.bdf_steps.append(self.g.chem_stats()["total_steps"])
+        else:
             s = self.g.surrogate_stats()
             self.log.append((dt, s["cells"], s["fallback"], s["ms"], s["ms_network"]))
         return d
@@ -173,6 +197,7 @@ def run_gpu(args, rank, world):
     g.synchronize()
     barrier(world)
     g.set_kernel_timing(True)
+    stp.bdf_steps.clear()
     with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
         g.timer_start()
         t0 = time.perf_counter()
@@ -180,6 +205,7 @@ def run_gpu(args, rank, world):
             stp.step()
         ms = g.timer_stop()
         wall = time.perf_counter() - t0
+    timed_bdf = list(stp.bdf_steps)
     kt = g.kernel_times()
     g.set_kernel_timing(False)
     ms = max_over_ranks(ms, world)
@@ -203,7 +229,21 @@ def run_gpu(args, rank, world):
     dom = max(kt.items(), key=lambda kv: kv[1][1])
     dom_name, (dom_n, dom_ms) = dom
     fx = kt.get("euler_face_x", (0, 0.0))
-    rl = None
+    rl = rl_chem = None
+    nre = chem_window(cfg) if chem else 0
+    if chem and kt.get("chem_psr", (0, 0.0))[0]:
+        n_l, ms_l = kt["chem_psr"]
+        avg_s = ms_l / n_l * 1e-3
+        byts = nre * CHEM_BYTES_PER_REACTOR
+        rl_chem = {"bound": "hbm", "kernel": "k_psr_field (persistent BDF chemistry, dominant)",
+                   "achieved": byts / avg_s / 1e9, "peak": hbm, "unit": "GB/s", "frac": byts / avg_s / 1e9 / hbm,
+                   "traffic": CHEM_TRAFFIC_PER_REACTOR * nre if CHEM_TRAFFIC_PER_REACTOR else None,
+                   "peak_source": hbm_src + " (MEASURED_PEAKS.json hbm_gbs)",
+                   "reactors_per_launch": nre, "bdf_steps_per_launch": timed_bdf}
+        if CHEM_FLOP_PER_BDF_STEP and timed_bdf:
+            gf = CHEM_FLOP_PER_BDF_STEP * sum(timed_bdf) / (ms_l * 1e-3) / 1e9
+            rl_chem["fp64"] = {"achieved": gf, "peak": FP64_PEAK_GFLOPS, "unit": "GFLOP/s",
+                               "frac": gf / FP64_PEAK_GFLOPS}
     if fx[0]:
         avg_s = fx[1] / fx[0] * 1e-3
         byts = euler_face_bytes(cfg)
@@ -231,7 +271,8 @@ def run_gpu(args, rank, world):
                    "autotuned_threads_per_block": {k: v["chosen"] for k, v in tuning.items()}},
         "e2e": {"value": e2e_value, "unit": "Mcell-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "steps": e2e_steps},
-        "roofline": rl,
+        "roofline": rl_chem if rl_chem else rl,
+        "roofline_euler_face": rl if rl_chem else None,
         "dominant_kernel": {"name": dom_name, "launches": dom_n, "ms": dom_ms},
         "kernel_ms": {k: round(v[1], 3) for k, v in sorted(kt.items(), key=lambda kv: -kv[1][1])},
         "gpu_launches": launches,
@@ -315,13 +356,14 @@ def run_batch(args):
     per step, arrays resident on the device; e2e adds the host copies."""
     import torch
     from phd_gb300 import ics
-    from phd_gb300.izem import psr_batch_device, psr_batch
+    from phd_gb300.izem import chem_autotune_device, psr_batch_device, psr_batch
     from phd_gb300.mech import h2_mechanism
     mech = h2_mechanism()
     n = args.cells
     T, rho, Y, dt = ics.batched_reactors(n)
     dev = {k: torch.from_numpy(a).to("cuda:0") for k, a in (("T", T), ("rho", rho), ("Y", Y), ("dt", dt))}
     T0, Y0 = dev["T"].clone(), dev["Y"].clone()
+    tuning = chem_autotune_device(mech, n, dev["T"], dev["rho"], dev["Y"], dev["dt"])
     ist = torch.zeros(n, dtype=torch.int32, device="cuda:0")
     nst = torch.zeros(n, dtype=torch.int32, device="cuda:0")
 
@@ -350,6 +392,7 @@ def run_batch(args):
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded PCG64 20261203)",
         "config": {"workload": "independent H2/air reactors", "cells": n, "mean_bdf_steps": steps_per_cell,
+                   "autotuned_kernel_variant": tuning,
                    "max_bdf_steps": int(nst.max().item()), "l2": "inputs larger than L2" if n * bytes_cell > 129e6
                    else "inputs smaller than L2 (%d B)" % (n * bytes_cell)},
         "e2e": {"value": n / e2e_s / 1e6, "unit": "Mcells/s", "h2d_bytes_per_step": n * 8 * 12,
@@ -367,7 +410,7 @@ def run_surrogate(args):
     against the BDF step on all of them.  Arrays resident on the device."""
     import torch
     from phd_gb300 import ics
-    from phd_gb300.izem import psr_batch_device
+    from phd_gb300.izem import chem_autotune_device, psr_batch_device
     from phd_gb300.mech import h2_mechanism
     from phd_gb300.surrogate import DEFAULT_GATE, STRICT_GATE, calibrate_cap, train_ensemble
     gate = STRICT_GATE if args.gate == "strict" else DEFAULT_GATE
@@ -397,6 +440,7 @@ def run_surrogate(args):
         Y.copy_(Y0)
         torch.cuda.synchronize()
 
+    tuning = chem_autotune_device(mech, n, T, rho, Y, dt)
     reset()
     psr_batch_device(mech, n, T, rho, Y, dt)   # warm-up, and the FP64 reference increments
     dT_ref_d = T - T0
@@ -441,6 +485,7 @@ def run_surrogate(args):
         "config": {"workload": "independent H2/air reactors (batched-chemistry distribution)", "cells": n,
                    "training": {"samples": args.train, "epochs": args.epochs, "networks": 2, "seconds": t_train},
                    "gate": {"name": args.gate, "values": gate_json(gate), "calibration": calib},
+                   "autotuned_kernel_variant": tuning,
                    "l2": "inputs larger than L2"},
         "bdf": {"value": n / (bdf_ms * 1e-3) / 1e6, "unit": "Mcells/s", "ms": bdf_ms},
         "speedup_vs_bdf": bdf_ms / ms,

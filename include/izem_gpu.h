@@ -310,6 +310,13 @@ int  izem_gpu_autotune(izem_ctx* ctx, double chem_dt, char* report, int report_l
  * the process, as izem_gpu_autotune would choose it (no counterpart in the
  * reference); IZEM_ERR_ARG outside 0..4. */
 int  izem_gpu_set_chem_variant(int variant);
+/* The same choice for independent reactors (no counterpart in the
+ * reference): times the five variants on the first min(n, 2^18) reactors of
+ * a batch laid out as for izem_gpu_psr_batch (copies; the caller's arrays
+ * are not changed) and keeps the fastest for the process.  report (may be
+ * NULL) receives the timings as JSON. */
+int  izem_gpu_chem_autotune(const izem_mech* mech, int n, const double* T, const double* rho, const double* Y,
+                            const double* dt, int device_ptrs, char* report, int report_len);
 
 /* Device timing of the calls above on the context's stream (CUDA events). */
 int  izem_gpu_timer_start(izem_ctx* ctx);

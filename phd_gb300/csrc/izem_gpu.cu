@@ -887,6 +887,70 @@ int izem_gpu_autotune(izem_ctx* c, double chem_dt, char* report, int report_len)
 
 int izem_gpu_set_chem_variant(int variant) { return chem_set_variant(variant) == 0 ? IZEM_OK : IZEM_ERR_ARG; }
 
+int izem_gpu_chem_autotune(const izem_mech* mech, int n, const double* T, const double* rho, const double* Y,
+                           const double* dt, int device_ptrs, char* report, int report_len) {
+  if (!mech || n <= 0 || !T || !rho || !Y || !dt || mech->kk != 9) return IZEM_ERR_ARG;
+  const int ns = n < (1 << 18) ? n : (1 << 18);   // the first 2^18 reactors are the sample
+  const cudaMemcpyKind kind = device_ptrs ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  cudaStream_t s = nullptr;
+  if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return IZEM_ERR_CUDA;
+  double *T0 = nullptr, *Y0 = nullptr, *r = nullptr, *d = nullptr, *Tw = nullptr, *Yw = nullptr;
+  unsigned* counter = nullptr;
+  ChemStats* st = nullptr;
+  cudaEvent_t a = nullptr, b = nullptr;
+  int rc = IZEM_OK;
+  float ms[IZEM_CHEM_VARIANTS];
+  int best = chem_variant();
+  do {
+    if (chem_upload_mech(mech) != cudaSuccess) { rc = IZEM_ERR_CUDA; break; }
+    if (cudaMalloc(&T0, ns * 8) || cudaMalloc(&Y0, (size_t)ns * 72) || cudaMalloc(&r, ns * 8) ||
+        cudaMalloc(&d, ns * 8) || cudaMalloc(&Tw, ns * 8) || cudaMalloc(&Yw, (size_t)ns * 72) ||
+        cudaMalloc(&counter, sizeof(unsigned)) || cudaMalloc(&st, sizeof(ChemStats))) { rc = IZEM_ERR_NOMEM; break; }
+    cudaMemcpyAsync(T0, T, ns * 8, kind, s);
+    cudaMemcpyAsync(Y0, Y, (size_t)ns * 72, kind, s);
+    cudaMemcpyAsync(r, rho, ns * 8, kind, s);
+    cudaMemcpyAsync(d, dt, ns * 8, kind, s);
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    for (int q = 0; q < IZEM_CHEM_VARIANTS && rc == IZEM_OK; ++q) {
+      chem_set_variant(q);
+      ms[q] = 1e30f;
+      for (int rep = 0; rep < 2; ++rep) {   // untimed first pass, then the timed one
+        cudaMemcpyAsync(Tw, T0, ns * 8, cudaMemcpyDeviceToDevice, s);
+        cudaMemcpyAsync(Yw, Y0, (size_t)ns * 72, cudaMemcpyDeviceToDevice, s);
+        cudaEventRecord(a, s);
+        if (chem_launch_batch(ns, Tw, r, Yw, d, nullptr, nullptr, counter, st, s, 9) != cudaSuccess) {
+          rc = IZEM_ERR_CUDA;
+          break;
+        }
+        cudaEventRecord(b, s);
+        if (cudaEventSynchronize(b) != cudaSuccess) { rc = IZEM_ERR_CUDA; break; }
+        if (rep == 1) cudaEventElapsedTime(&ms[q], a, b);
+      }
+      if (rc == IZEM_OK && ms[q] < ms[best]) best = q;
+    }
+  } while (0);
+  chem_set_variant(best);
+  if (rc == IZEM_OK && report && report_len > 0) {
+    std::string rep = "{\"sample\": " + std::to_string(ns);
+    char buf[96];
+    for (int q = 0; q < IZEM_CHEM_VARIANTS; ++q) {
+      std::snprintf(buf, sizeof(buf), ", \"128x%d (%d regs)\": %.4f", chem_variant_min_blocks(q),
+                    chem_variant_registers(q), ms[q]);
+      rep += buf;
+    }
+    std::snprintf(buf, sizeof(buf), ", \"chosen\": \"128x%d (%d regs)\"}", chem_variant_min_blocks(best),
+                  chem_variant_registers(best));
+    rep += buf;
+    std::snprintf(report, report_len, "%s", rep.c_str());
+  }
+  if (a) cudaEventDestroy(a);
+  if (b) cudaEventDestroy(b);
+  cudaFree(T0); cudaFree(Y0); cudaFree(r); cudaFree(d); cudaFree(Tw); cudaFree(Yw); cudaFree(counter); cudaFree(st);
+  cudaStreamDestroy(s);
+  return rc;
+}
+
 int izem_gpu_timer_start(izem_ctx* c) {
   if (!c) return IZEM_ERR_ARG;
   CK(cudaEventRecord(c->t0, c->stream));

@@ -76,6 +76,8 @@ def load_library(path=None):
         "izem_gpu_set_eglib": (C.c_int, [P, C.POINTER(IzemEglib)]),
         "izem_gpu_autotune": (C.c_int, [P, C.c_double, C.c_char_p, C.c_int]),
         "izem_gpu_set_chem_variant": (C.c_int, [C.c_int]),
+        "izem_gpu_chem_autotune": (C.c_int, [C.POINTER(IzemMech), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                             C.c_void_p, C.c_int, C.c_char_p, C.c_int]),
         "izem_gpu_chem_surrogate_stats": (C.c_int, [P, C.POINTER(C.c_longlong), C.POINTER(C.c_int),
                                                     C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     }
@@ -129,6 +131,21 @@ def psr_batch(mech, T, rho, Y, dt, device_ptrs=False):
     if rc:
         raise IzemError(rc, "izem_gpu_psr_batch")
     return istate, nsteps, ms.value
+
+
+def chem_autotune_device(mech, n, T, rho, Y, dt):
+    """Choose the register-budget variant of the persistent chemistry
+    kernels for independent reactors by timing each on the first
+    min(n, 2^18) of them (device arrays as for psr_batch_device, left
+    unchanged).  Returns the timings [ms] and the choice."""
+    import json
+    lib = load_library()
+    buf = C.create_string_buffer(1024)
+    rc = lib.izem_gpu_chem_autotune(C.byref(mech), n, T.data_ptr(), rho.data_ptr(), Y.data_ptr(), dt.data_ptr(), 1,
+                                    buf, 1024)
+    if rc:
+        raise IzemError(rc, "izem_gpu_chem_autotune")
+    return json.loads(buf.value.decode())
 
 
 def psr_batch_device(mech, n, T, rho, Y, dt, istate=None, nsteps=None):

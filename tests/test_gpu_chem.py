@@ -63,3 +63,26 @@ def test_field_chem_step_matches_oracle():
     assert abs(dtm_g - dtm_o) <= 100 * (RTOL * 3000 + ATOL)
     st_ = g.chem_stats()
     assert st_["failed"] == 0
+
+
+def test_chem_autotune_batch_leaves_inputs_and_keeps_results():
+    """The batch autotuner times the register-budget variants on copies of a
+    sample: the caller's arrays are unchanged, it reports every variant and
+    its choice, and a batch integrated afterwards stays within the bounds
+    above against the oracle."""
+    import torch
+    from phd_gb300.izem import chem_autotune_device
+    m = h2_mechanism()
+    T, rho, Y, dt = ics.batched_reactors(4096, seed=23)
+    dev = [torch.from_numpy(a).to("cuda:0") for a in (T, rho, Y, dt)]
+    rep = chem_autotune_device(m, len(T), *dev)
+    assert rep["sample"] == len(T) and rep["chosen"].startswith("128x")
+    assert sum(1 for k in rep if k.startswith("128x")) == 5
+    assert np.array_equal(dev[0].cpu().numpy(), T) and np.array_equal(dev[2].cpu().numpy(), Y)
+    To, Yo = T.copy(), Y.copy()
+    oracle.psr_cells(m, To, rho.copy(), Yo, dt.copy())
+    Tg, Yg = T.copy(), Y.copy()
+    psr_batch(m, Tg, rho.copy(), Yg, dt.copy())
+    rT = np.abs(Tg - To) / (RTOL * np.abs(To) + ATOL)
+    assert rT.max() <= 100 and np.percentile(rT, 99) <= 10
+    assert (np.abs(Yg - Yo) / np.abs(Yo).max(axis=0)).max() <= 1e-3
