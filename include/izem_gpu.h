@@ -311,7 +311,7 @@ int  izem_gpu_autotune(izem_ctx* ctx, double chem_dt, char* report, int report_l
  * reference); IZEM_ERR_ARG outside 0..4. */
 int  izem_gpu_set_chem_variant(int variant);
 /* The same choice for independent reactors (no counterpart in the
- * reference): times the five variants on the first min(n, 2^18) reactors of
+ * reference): times the five variants on the first min(n, 2^20) reactors of
  * a batch laid out as for izem_gpu_psr_batch (copies; the caller's arrays
  * are not changed) and keeps the fastest for the process.  report (may be
  * NULL) receives the timings as JSON. */

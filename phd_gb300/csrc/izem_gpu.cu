@@ -339,7 +339,7 @@ template <int NRV>
 int tune_flow(izem_ctx* c, std::string* rep) {
   int rc = enq_prim<NRV>(c);
   if (rc) return rc;
-  float ms[3];
+  float ms[3] = {1e30f, 1e30f, 1e30f};   // untimed candidates never win
   int best = 1;
   for (int q = 0; q < 3; ++q) {
     c->tb_euler = kTuneCand[q];
@@ -350,6 +350,7 @@ int tune_flow(izem_ctx* c, std::string* rep) {
   tune_report(*rep, "euler_face", ms, c->tb_euler);
   if (c->cfg.vis) {
     best = 1;
+    for (float& x : ms) x = 1e30f;
     for (int q = 0; q < 3; ++q) {
       c->tb_visc = kTuneCand[q];
       ms[q] = tune_time(c, 2, [&] { (void)enq_visc<NRV>(c); });
@@ -850,6 +851,7 @@ int izem_gpu_autotune(izem_ctx* c, double chem_dt, char* report, int report_len)
         // 8 down to 4 resident blocks per SM)
         chem_launch_gather(f, T0, rho, Y0, dt, c->stream);
         float ms[IZEM_CHEM_VARIANTS];
+        for (float& x : ms) x = 1e30f;   // untimed candidates never win
         int best = chem_variant();
         for (int q = 0; q < IZEM_CHEM_VARIANTS; ++q) {
           chem_set_variant(q);
@@ -890,7 +892,9 @@ int izem_gpu_set_chem_variant(int variant) { return chem_set_variant(variant) ==
 int izem_gpu_chem_autotune(const izem_mech* mech, int n, const double* T, const double* rho, const double* Y,
                            const double* dt, int device_ptrs, char* report, int report_len) {
   if (!mech || n <= 0 || !T || !rho || !Y || !dt || mech->kk != 9) return IZEM_ERR_ARG;
-  const int ns = n < (1 << 18) ? n : (1 << 18);   // the first 2^18 reactors are the sample
+  // the first 2^20 reactors are the sample: a smaller one is dominated by the
+  // tail of its slowest cells and ranks the variants differently
+  const int ns = n < (1 << 20) ? n : (1 << 20);
   const cudaMemcpyKind kind = device_ptrs ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
   cudaStream_t s = nullptr;
   if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return IZEM_ERR_CUDA;
@@ -900,6 +904,7 @@ int izem_gpu_chem_autotune(const izem_mech* mech, int n, const double* T, const 
   cudaEvent_t a = nullptr, b = nullptr;
   int rc = IZEM_OK;
   float ms[IZEM_CHEM_VARIANTS];
+  for (float& x : ms) x = 1e30f;   // untimed candidates never win
   int best = chem_variant();
   do {
     if (chem_upload_mech(mech) != cudaSuccess) { rc = IZEM_ERR_CUDA; break; }

@@ -136,7 +136,7 @@ def psr_batch(mech, T, rho, Y, dt, device_ptrs=False):
 def chem_autotune_device(mech, n, T, rho, Y, dt):
     """Choose the register-budget variant of the persistent chemistry
     kernels for independent reactors by timing each on the first
-    min(n, 2^18) of them (device arrays as for psr_batch_device, left
+    min(n, 2^20) of them (device arrays as for psr_batch_device, left
     unchanged).  Returns the timings [ms] and the choice."""
     import json
     lib = load_library()
