@@ -2,7 +2,8 @@
 
 Forward and backward of the 12 -> 4 x 256 (GELU) -> 10 network in float64
 numpy, with the inputs and weights rounded to BF16 exactly as the device
-kernels round them, and the exact erf-based GELU.  Used to check the
+kernels round them, and GELU in the same tanh form (evaluated exactly
+here, with the special-function tanh on the device).  Used to check the
 device's tensor-core forward, backward and parameter gradients.
 """
 import math
@@ -20,15 +21,20 @@ def bf16(x):
     return r.view(np.float32).astype(np.float64)
 
 
-_erf = np.vectorize(math.erf)
+# GELU in the tanh form of Hendrycks and Gimpel (2016), the form the
+# library's kernels evaluate: 0.5 z (1 + tanh(sqrt(2/pi) (z + 0.044715 z^3)))
+_C0 = math.sqrt(2.0 / math.pi)
+_C1 = _C0 * 0.044715
 
 
 def gelu(z):
-    return 0.5 * z * (1.0 + _erf(z / math.sqrt(2.0)))
+    return 0.5 * z * (1.0 + np.tanh(z * (_C0 + _C1 * z * z)))
 
 
 def gelu_grad(z):
-    return 0.5 * (1.0 + _erf(z / math.sqrt(2.0))) + z * np.exp(-0.5 * z * z) / math.sqrt(2.0 * math.pi)
+    z2 = z * z
+    t = np.tanh(z * (_C0 + _C1 * z2))
+    return 0.5 * (1.0 + t) + 0.5 * z * (1.0 - t * t) * (_C0 + 3.0 * _C1 * z2)
 
 
 def forward(W, b, x, rounding=True):

@@ -35,11 +35,29 @@ constexpr int BM = 128, BN = 128, BK = 32;
 
 enum Epi { EPI_STORE_F32 = 0, EPI_BIAS_GELU = 1, EPI_BIAS = 2, EPI_GELU_BWD = 3 };
 
-__device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.0f + erff(z * 0.70710678118654752f)); }
+// GELU in the tanh form of Hendrycks and Gimpel (2016),
+//   gelu(z) = 0.5 z (1 + tanh(u)),  u = sqrt(2/pi) (z + 0.044715 z^3),
+// with the tanh of the special-function unit (tanh.approx.f32, relative
+// error about 2^-11, below the BF16 rounding of the activations it feeds).
+// Training, inference and the oracle use this same form.
+constexpr float kGeluC0 = 0.7978845608028654f;    // sqrt(2/pi)
+constexpr float kGeluC1 = 0.0356774081363001f;    // sqrt(2/pi) * 0.044715
+__device__ __forceinline__ float tanh_sfu(float x) {
+  float y;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float gelu(float z) {
+  const float u = z * fmaf(kGeluC1, z * z, kGeluC0);
+  const float hz = 0.5f * z;
+  return fmaf(hz, tanh_sfu(u), hz);
+}
+// d gelu / dz = 0.5 (1 + t) + 0.5 z (1 - t^2) du/dz,  du/dz = sqrt(2/pi) (1 + 3 * 0.044715 z^2)
 __device__ __forceinline__ float gelu_grad(float z) {
-  const float cdf = 0.5f * (1.0f + erff(z * 0.70710678118654752f));
-  const float pdf = 0.39894228040143268f * __expf(-0.5f * z * z);
-  return cdf + z * pdf;
+  const float z2 = z * z;
+  const float t = tanh_sfu(z * fmaf(kGeluC1, z2, kGeluC0));
+  const float du = fmaf(3.0f * kGeluC1, z2, kGeluC0);
+  return fmaf(0.5f * z * du, fmaf(-t, t, 1.0f), 0.5f * (1.0f + t));
 }
 
 struct GemmArgs {

@@ -12,7 +12,7 @@
 //     layout, so each layer's 128 KB arrives in shared memory by bulk copies
 //     (cp.async.bulk, completion counted on an mbarrier), the next layer's
 //     copy overlapping the current layer's epilogue;
-//   * the epilogue (bias + exact GELU, then BF16) is split over 16 warps:
+//   * the epilogue (bias + GELU in its tanh form, then BF16) is split over 16 warps:
 //     warp w reads TMEM lanes 32 (w % 4) .. + 31 (the rows it owns) and the
 //     64 columns of quarter w / 4.
 // Every wait on an mbarrier is bounded; on a timeout the kernel records it
@@ -35,7 +35,8 @@ constexpr uint32_t SA = 0;                        // activations, 128 x 256 BF16
 constexpr uint32_t SB = SA + TM * KH * 2;         // hidden weights, 256 x 256 BF16 = 128 KB
 constexpr uint32_t SW0 = SB + KH * KH * 2;        // layer 0 weights, 256 x 16 = 8 KB
 constexpr uint32_t SW4 = SW0 + KH * KIN * 2;      // layer 4 weights, 16 x 256 = 8 KB
-constexpr uint32_t SBAR = SW4 + NOUT * KH * 2;    // two mbarriers (8 B each) + TMEM address
+constexpr uint32_t SBIAS = SW4 + NOUT * KH * 2;   // biases of the five layers, 4 x 256 + 16 FP32
+constexpr uint32_t SBAR = SBIAS + (4 * KH + NOUT) * 4;   // two mbarriers (8 B each) + TMEM address
 constexpr uint32_t SMEM_BYTES = SBAR + 64;
 constexpr int kWaitLimit = 1 << 24;              // non-blocking polls (about 1 s) before a wait gives up
 
@@ -165,9 +166,10 @@ __global__ void k_tc_blob(const __nv_bfloat16* __restrict__ W, int K, int N, __n
   blob[core_off(n, k, K) >> 1] = W[idx];
 }
 
-// bias + exact GELU of one layer's 128 x 256 accumulator, written back as the
+// bias + GELU of one layer's 128 x 256 accumulator, written back as the
 // next layer's BF16 K-major operand; warp w owns rows 32 (w % 4) + lane and
-// columns 64 (w / 4) .. + 63
+// columns 64 (w / 4) .. + 63; `bias` is the layer's 256 biases in shared
+// memory (the same address in every lane: broadcast loads)
 __device__ __forceinline__ void epilogue_hidden(uint8_t* sm, uint32_t tmem, int warp, int lane, const float* bias) {
   const int r = (warp & 3) * 32 + lane;
   const uint32_t lane_addr = tmem + ((uint32_t)((warp & 3) * 32) << 16);
@@ -178,12 +180,17 @@ __device__ __forceinline__ void epilogue_hidden(uint8_t* sm, uint32_t tmem, int 
     tmem_ld32(lane_addr + (uint32_t)col, v);
     tmem_wait_ld();
     uint32_t pk[16];
+    const float4* b4 = reinterpret_cast<const float4*>(bias + col);
 #pragma unroll
-    for (int j = 0; j < 16; ++j) {
-      const float f0 = gelu(__uint_as_float(v[2 * j]) + bias[col + 2 * j]);
-      const float f1 = gelu(__uint_as_float(v[2 * j + 1]) + bias[col + 2 * j + 1]);
-      __nv_bfloat162 h = __floats2bfloat162_rn(f0, f1);
-      pk[j] = *reinterpret_cast<uint32_t*>(&h);
+    for (int j = 0; j < 8; ++j) {
+      const float4 b = b4[j];
+      const float f0 = gelu(__uint_as_float(v[4 * j]) + b.x);
+      const float f1 = gelu(__uint_as_float(v[4 * j + 1]) + b.y);
+      const float f2 = gelu(__uint_as_float(v[4 * j + 2]) + b.z);
+      const float f3 = gelu(__uint_as_float(v[4 * j + 3]) + b.w);
+      __nv_bfloat162 h0 = __floats2bfloat162_rn(f0, f1), h1 = __floats2bfloat162_rn(f2, f3);
+      pk[2 * j] = *reinterpret_cast<uint32_t*>(&h0);
+      pk[2 * j + 1] = *reinterpret_cast<uint32_t*>(&h1);
     }
 #pragma unroll
     for (int q = 0; q < 4; ++q)
@@ -203,6 +210,11 @@ __global__ void __launch_bounds__(THREADS, 1) k_mlp_tc(TcArgs a) {
     fence_async_smem();
   }
   if (warp == 0) tmem_alloc(base + SBAR + 16, TMEM_COLS);
+  {   // biases of all layers, once per CTA
+    float* bs = reinterpret_cast<float*>(sm + SBIAS);
+    for (int q = tid; q < 4 * KH; q += THREADS) bs[q] = a.bias[q / KH][q % KH];
+    if (tid < NOUT) bs[4 * KH + tid] = a.bias[4][tid];
+  }
   tc_before_sync();
   __syncthreads();
   tc_after_sync();
@@ -248,7 +260,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_mlp_tc(TcArgs a) {
     if (!__syncthreads_and(mbar_wait(bar_mma, ph_mma))) { failed = 1; break; }
     ph_mma ^= 1;
     tc_after_sync();
-    epilogue_hidden(sm, tmem, warp, lane, a.bias[0]);
+    epilogue_hidden(sm, tmem, warp, lane, reinterpret_cast<const float*>(sm + SBIAS));
     fence_async_smem();
     tc_before_sync();
     __syncthreads();
@@ -270,7 +282,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_mlp_tc(TcArgs a) {
         for (int q = 0; q < 4; ++q)
           bulk_g2s(base + SB + q * 32768, reinterpret_cast<const uint8_t*>(a.blob[l + 1]) + q * 32768, 32768, bar_ld);
       }
-      epilogue_hidden(sm, tmem, warp, lane, a.bias[l]);
+      epilogue_hidden(sm, tmem, warp, lane, reinterpret_cast<const float*>(sm + SBIAS) + l * KH);
       fence_async_smem();
       tc_before_sync();
       __syncthreads();
