@@ -40,8 +40,11 @@ cudaError_t chem_launch_gather(const ChemField& f, double* T, double* rho, doubl
 cudaError_t chem_launch_scatter(const ChemField& f, const double* T, const double* Y, ChemStats* d_stats, cudaStream_t s);
 
 // learned-surrogate support (chem.cu)
+// inputs of one network, or of both networks of an ensemble (d_norm2 and
+// x2_bf16 null for one); rows of 16 BF16 values, 16-byte aligned
 cudaError_t chem_launch_featurize(int n, const double* T, const double* rho, const double* Y, const double* dt,
-                                  const float* d_norm, void* x_bf16, int ldx, cudaStream_t s);
+                                  const float* d_norm, void* x_bf16, const float* d_norm2, void* x2_bf16,
+                                  cudaStream_t s);
 cudaError_t chem_launch_decode_gate(int n, const float* out, const float* out2, int ldo, const float* d_norm,
                                     const float* d_norm2, double* T, const double* rho, double* Y, const double* dt,
                                     const double* gate10, const int* d_kncf, int nele, int* list, int base,

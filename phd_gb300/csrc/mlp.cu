@@ -649,12 +649,10 @@ int izem_gpu_psr_batch_mlp(izem_mlp* m, izem_mlp* m2, const izem_mech* mech, int
     const int c0 = ci * chunk;
     const int cn = (n - c0) < chunk ? (n - c0) : chunk;
     cudaEventRecord(ev[2 + 2 * ci], s);
-    chem_launch_featurize(cn, dT + c0, drho + c0, dY + (size_t)c0 * kk, ddt + c0, m->d_norm, m->ib[0], INP, s);
+    chem_launch_featurize(cn, dT + c0, drho + c0, dY + (size_t)c0 * kk, ddt + c0, m->d_norm, m->ib[0],
+                          m2 ? m2->d_norm : nullptr, m2 ? m2->ib[0] : nullptr, s);
     if (mlp_infer_tc(m, cn, m->ib[0], m->iout, s) != cudaSuccess) { rc = IZEM_ERR_CUDA; break; }
-    if (m2) {
-      chem_launch_featurize(cn, dT + c0, drho + c0, dY + (size_t)c0 * kk, ddt + c0, m2->d_norm, m2->ib[0], INP, s);
-      if (mlp_infer_tc(m2, cn, m2->ib[0], m2->iout, s) != cudaSuccess) { rc = IZEM_ERR_CUDA; break; }
-    }
+    if (m2 && mlp_infer_tc(m2, cn, m2->ib[0], m2->iout, s) != cudaSuccess) { rc = IZEM_ERR_CUDA; break; }
     cudaEventRecord(ev[3 + 2 * ci], s);
     chem_launch_decode_gate(cn, m->iout, m2 ? m2->iout : nullptr, OUTP, m->d_norm, m2 ? m2->d_norm : nullptr, dT + c0,
                             drho + c0, dY + (size_t)c0 * kk, ddt + c0, gate10, m->g_kncf, nele, m->g_list, c0,
