@@ -1206,28 +1206,27 @@ __global__ void __launch_bounds__(kChemThreads, MINB) k_psr_batch(int n, double*
 // ------------------------------------------------ surrogate support --------
 // Inputs of the learned surrogate: T [K], ln p [atm], ln(Y_k + 1e-10),
 // ln dt [s], normalised by the training means / standard deviations.
-// The features are rounded to BF16 (8 significant bits) after
-// normalisation, so the logarithms and the normalisation run in FP32; the
-// pressure (a sum over species) is formed in FP64.  One pass writes the
-// inputs of both networks of an ensemble (x2 may be null); rows are 16
-// BF16 values, written as two 16-byte stores.
+// The features are formed in FP64 as on the host that trains the networks,
+// so a device row rounds to the same BF16 values as the host's; one pass
+// writes the inputs of both networks of an ensemble (x2 may be null); rows
+// are 16 BF16 values, written as two 16-byte stores.
 template <int KK>
 __global__ void k_featurize(int n, const double* T, const double* rho, const double* Y, const double* dt,
                             const float* norm, __nv_bfloat16* x, const float* norm2, __nv_bfloat16* x2) {
   static_assert(KK + 3 <= 16, "one 16-wide input row");
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= n) return;
-  float f[16];
+  double f[16];
   const double Tq = T[q];
   double wmi = 0.0;
 #pragma unroll
-  for (int k = 0; k < KK; ++k) wmi += fmax(Y[(size_t)q * KK + k], 0.0) * c_fast.wt_inv[k];
+  for (int k = 0; k < KK; ++k) wmi += fmax(Y[(size_t)q * KK + k], 0.0) / c_mech.wt[k];
   const double p_atm = rho[q] * c_mech.ru * Tq * wmi / c_mech.patm;
-  f[0] = (float)Tq;
-  f[1] = logf((float)p_atm);
+  f[0] = Tq;
+  f[1] = log(p_atm);
 #pragma unroll
-  for (int k = 0; k < KK; ++k) f[2 + k] = logf((float)(fmax(Y[(size_t)q * KK + k], 0.0) + 1.0e-10));
-  f[KK + 2] = logf((float)dt[q]);
+  for (int k = 0; k < KK; ++k) f[2 + k] = log(fmax(Y[(size_t)q * KK + k], 0.0) + 1.0e-10);
+  f[KK + 2] = log(dt[q]);
   for (int net = 0; net < 2; ++net) {
     const float* nm = net ? norm2 : norm;
     __nv_bfloat16* out = net ? x2 : x;
@@ -1235,8 +1234,8 @@ __global__ void k_featurize(int n, const double* T, const double* rho, const dou
     uint32_t pk[8];
 #pragma unroll
     for (int c = 0; c < 16; c += 2) {
-      const float a = c < KK + 3 ? __fdividef(f[c] - nm[c], nm[KK + 3 + c]) : 0.f;
-      const float b = c + 1 < KK + 3 ? __fdividef(f[c + 1] - nm[c + 1], nm[KK + 3 + c + 1]) : 0.f;
+      const float a = c < KK + 3 ? (float)((f[c] - nm[c]) / nm[KK + 3 + c]) : 0.f;
+      const float b = c + 1 < KK + 3 ? (float)((f[c + 1] - nm[c + 1]) / nm[KK + 3 + c + 1]) : 0.f;
       __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
       pk[c / 2] = *reinterpret_cast<uint32_t*>(&h);
     }

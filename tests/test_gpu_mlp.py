@@ -58,6 +58,25 @@ def test_training_reduces_loss():
     assert losses[-1] < 0.2 * losses[0], losses
 
 
+def test_device_features_match_host_features():
+    """The gated step featurises the reactors on the device (FP32 logarithms,
+    normalisation, BF16 rows for the tensor-core network).  Its raw
+    temperature prediction equals izem_mlp_forward on the host's FP64
+    features normalised the same way, up to BF16 rounding of the inputs."""
+    mech = h2_mechanism()
+    X, Yt = training_set(mech, 1 << 12, seed=5)
+    s = Surrogate(seed=3)
+    s.fit_norm(X, Yt)
+    T, rho, Y, dt = ics.batched_reactors(4096, seed=41)
+    wt = np.array([mech.wt[k] for k in range(mech.kk)])
+    yh = s.forward(s.normalise(features(T, rho, Y, dt, wt)))
+    dT_host = yh[:, 9].astype(np.float64) * s.norm[2 * 12 + 10 + 9] + s.norm[2 * 12 + 9]
+    r = s.chem_step(mech, T.copy(), rho.copy(), Y.copy(), dt.copy(), DEFAULT_GATE)
+    d = np.abs(r["dT_pred"] - dT_host)
+    spread = np.std(dT_host)
+    assert np.median(d) <= 1e-3 * spread and d.max() <= 0.1 * spread, (np.median(d), d.max(), spread)
+
+
 def test_surrogate_gains_over_bdf_with_gate():
     """What the trained network gains over the method without it: the gated
     surrogate step, with its |dT| cap calibrated on other held-out reactors,
