@@ -31,6 +31,7 @@ def load():
     sig = {
         "or_create": (P, [C.POINTER(IzemCfg), C.POINTER(IzemThd), C.POINTER(IzemAdi), _dp, _dp, _dp]),
         "or_destroy": (None, [P]),
+        "or_set_sensor_xblocks": (C.c_int, [P, C.c_int]),
         "or_last_error": (C.c_int, [P, C.c_char_p, C.c_int]),
         "or_cp_scalar": (None, [P, C.c_double, _dp, _dp]),
         "or_ha_scalar": (None, [P, C.c_double, _dp]),
@@ -155,6 +156,11 @@ class Oracle:
     def set_eglib(self, link):
         self._eglib = link
         self._rc(self.lib.or_set_eglib(self.h, C.byref(link)), "set_eglib")
+
+    def set_sensor_xblocks(self, nblk):
+        """Emulate a run whose x direction was split into nblk MPI blocks:
+        the shock sensor does not compare points across block edges."""
+        self._rc(self.lib.or_set_sensor_xblocks(self.h, int(nblk)), "set_sensor_xblocks")
 
     def newton_warnings(self):
         return self.lib.or_last_error(self.h, None, 0)

@@ -10,9 +10,13 @@
 // reference's operation order so that results agree to rounding.  Build with
 // -ffp-contract=off so that no multiply-add is fused on either machine.
 //
-// Parity pinning: the chemistry restatement is cross-checked against an
-// independent DVODE (scipy's BDF integrator) on the same reactor equations;
-// the flow path is not yet pinned against stored outputs of the reference.
+// Parity pinning: the flow restatement reproduces the reference's own FP64
+// restart files of its 2-D WENO7 Sod run (testcases/sod) to about 5e-8 of
+// the field maxima after 647-777 steps (tests/test_sod_pin.py); that case
+// runs the ng = 4, ndim = 2 branches below and emulates the two effects of
+// the reference's two MPI blocks on the shock sensor.  The chemistry
+// restatement is cross-checked against an independent DVODE (scipy's BDF
+// integrator) on the same reactor equations.
 //
 // Layout: one block of nx*ny*nz interior points with ng ghost layers,
 // Fortran column-major, variable index slowest, exactly the reference's
@@ -59,6 +63,7 @@ struct Ctx {
   Block b;
   std::vector<double> dxi[3];   // indexed (i-1+ng), length n+2ng
   int newton_warn = 0;
+  int sensor_xblocks = 1;   // x-blocks of the reference's MPI run whose edges the sensor does not cross
   std::string err;
 };
 
@@ -374,8 +379,10 @@ int finalize_ic(Ctx& c, double* v, double* T, double* W_i, double* cp, double* h
 }
 
 // ------------------------------------------------------------ derivatives --
-// module_deriv.f90 coefficient tables (:25-66) for ng = 3
+// module_deriv.f90 coefficient tables (:25-66)
 const double alpha6[7] = {-1.0 / 60.0, 9.0 / 60.0, -45.0 / 60.0, 0.0, 45.0 / 60.0, -9.0 / 60.0, 1.0 / 60.0};
+const double alpha8[9] = {3.0 / 840.0,    -32.0 / 840.0, 168.0 / 840.0, -672.0 / 840.0, 0.0,
+                          672.0 / 840.0,  -168.0 / 840.0, 32.0 / 840.0, -3.0 / 840.0};
 const double alph4[5] = {1.0 / 12.0, -8.0 / 12.0, 0.0, 8.0 / 12.0, -1.0 / 12.0};
 const double alph4ol[5] = {-25.0 / 12.0, 48.0 / 12.0, -36.0 / 12.0, 16.0 / 12.0, -3.0 / 12.0};   // l = 0..4
 const double alph4ul[5] = {-3.0 / 12.0, -10.0 / 12.0, 18.0 / 12.0, -6.0 / 12.0, 1.0 / 12.0};    // l = -1..3
@@ -384,12 +391,18 @@ const double alph4or[5] = {-3.0 / 12.0, 16.0 / 12.0, -36.0 / 12.0, 48.0 / 12.0, 
 
 // dx/dy/dz, d?_fixed1, d?_fixed2 (module_deriv.f90:212-2354): the three
 // families share one arithmetic; `out_interior` selects the interior-sized
-// output of d?_fixed2.  Only interior points are written.
+// output of d?_fixed2.  Only interior points are written.  Interior and
+// inter-block points use the 6th-order (ng = 3) or 8th-order (ng = 4)
+// central stencil; next to a physical boundary the rows are 4th order and,
+// with ng = 4, the fourth row is 6th order.  In a 2-D run (ndim = 2) there
+// is no z derivative: the reference's 2-D routines (viscflux_xy) have no z
+// term, and a zero z derivative reproduces them.
 void deriv(const Ctx& c, int d, const double* in, double* out, bool out_interior) {
   const Block& b = c.b;
   const int n = b.n(d), ng = b.ng;
   const double* di = c.dxi[d].data();
   const bool lo_b = b.bnd[2 * d], hi_b = b.bnd[2 * d + 1];
+  const bool none = d == 2 && c.cfg.ndim == 2;
 #pragma omp parallel for collapse(2) schedule(static)
   for (int k = 1; k <= b.nz; ++k)
     for (int j = 1; j <= b.ny; ++j)
@@ -402,7 +415,9 @@ void deriv(const Ctx& c, int d, const double* in, double* out, bool out_interior
         };
         double dd = 0.0, res;
         double dis = di[s - 1 + ng];
-        if (lo_b && s == 1) {
+        if (none) {
+          res = 0.0;
+        } else if (lo_b && s == 1) {
           for (int l = 0; l <= 4; ++l) dd = dd + alph4ol[l] * at(l);
           res = dd * dis;
         } else if (lo_b && s == 2) {
@@ -410,6 +425,9 @@ void deriv(const Ctx& c, int d, const double* in, double* out, bool out_interior
           res = dd * dis;
         } else if (lo_b && s == 3) {
           for (int l = -2; l <= 2; ++l) dd = dd + alph4[l + 2] * at(l);
+          res = dd * dis;
+        } else if (ng == 4 && ((lo_b && s == 4) || (hi_b && s == n - 3))) {
+          for (int l = -3; l <= 3; ++l) dd = dd + alpha6[l + 3] * at(l);
           res = dd * dis;
         } else if (hi_b && s == n - 2) {
           for (int l = -2; l <= 2; ++l) dd = dd + alph4[l + 2] * at(l);
@@ -420,6 +438,9 @@ void deriv(const Ctx& c, int d, const double* in, double* out, bool out_interior
         } else if (hi_b && s == n) {
           for (int l = -4; l <= 0; ++l) dd = dd + alph4or[l + 4] * at(l);
           res = -dd * dis;
+        } else if (ng == 4) {
+          for (int l = -4; l <= 4; ++l) dd = dd + alpha8[l + 4] * at(l);
+          res = dd * dis;
         } else {
           for (int l = -3; l <= 3; ++l) dd = dd + alpha6[l + 3] * at(l);
           res = dd * dis;
@@ -431,14 +452,31 @@ void deriv(const Ctx& c, int d, const double* in, double* out, bool out_interior
 
 // ------------------------------------------------------------------ WENO ---
 struct Weno {
-  double cweno[5][3];  // cweno(-1:ng-1, 0:ng-1) stored at [r+1][j]
-  double dweno[3], dtweno[3];
-  double z1, z2, za, zb, zc, zd;
+  int ng;
+  double cweno[5][4];  // cweno(-1:ng-1, 0:ng-1) stored at [r+1][j]
+  double dweno[4], dtweno[4];
+  double z1, z2, za, zb, zc, zd, ze, zf, zg, zh, zi, zl, zm, zn, zo, zp, zq, zr, zs, zt, zu;
 };
 
-// wenopar (module_weno.f90:60-225), ng = 3 branch
-Weno wenopar() {
-  Weno w;
+// wenopar (module_weno.f90:60-225): ng = 4 (7th order) and ng = 3 (5th order)
+Weno wenopar(int ng) {
+  Weno w{};
+  w.ng = ng;
+  if (ng == 4) {
+    const double c[5][4] = {{25.0 / 12.0, -23.0 / 12.0, 13.0 / 12.0, -1.0 / 4.0},
+                            {1.0 / 4.0, 13.0 / 12.0, -5.0 / 12.0, 1.0 / 12.0},
+                            {-1.0 / 12.0, 7.0 / 12.0, 7.0 / 12.0, -1.0 / 12.0},
+                            {1.0 / 12.0, -5.0 / 12.0, 13.0 / 12.0, 1.0 / 4.0},
+                            {-1.0 / 4.0, 13.0 / 12.0, -23.0 / 12.0, 25.0 / 12.0}};
+    for (int r = 0; r < 5; ++r)
+      for (int j = 0; j < 4; ++j) w.cweno[r][j] = c[r][j];
+    w.dweno[0] = 4.0 / 35.0; w.dweno[1] = 18.0 / 35.0; w.dweno[2] = 12.0 / 35.0; w.dweno[3] = 1.0 / 35.0;
+    for (int r = 0; r < 4; ++r) w.dtweno[r] = w.dweno[3 - r];
+    w.za = 547.0; w.zb = -1854.0; w.zc = 4642.0; w.zd = -3882.0; w.ze = -17246.0; w.zf = 2107.0;
+    w.zg = 7043.0; w.zh = -9402.0; w.zi = 11003.0; w.zl = 7042.0; w.zm = 3443.0; w.zn = -5966.0;
+    w.zo = -2522.0; w.zp = 1602.0; w.zq = 2843.0; w.zr = 267.0; w.zs = 1922.0; w.zt = -494.0; w.zu = -1642.0;
+    return w;
+  }
   w.cweno[0][0] = 11.0 / 6.0; w.cweno[0][1] = -7.0 / 6.0; w.cweno[0][2] = 1.0 / 3.0;
   w.cweno[1][0] = 1.0 / 3.0;  w.cweno[1][1] = 5.0 / 6.0;  w.cweno[1][2] = -1.0 / 6.0;
   w.cweno[2][0] = -1.0 / 6.0; w.cweno[2][1] = 5.0 / 6.0;  w.cweno[2][2] = 1.0 / 3.0;
@@ -449,10 +487,19 @@ Weno wenopar() {
   return w;
 }
 
-// wenorec_nw (module_weno.f90:236-275), ng = 3.  vp/vm are 1-based arrays
-// of length 2ng.  `fix` selects the textbook upwind-biased stencil instead of
-// the reference's mirrored one.
-void wenorec_nw(const double* vp, const double* vm, double& vminus, double& vplus, bool fix) {
+// wenorec_nw (module_weno.f90:236-275).  vp/vm are 1-based arrays of length
+// 2ng.  For ng = 3, `fix` selects the textbook upwind-biased stencil
+// instead of the reference's mirrored one; the ng = 4 stencil is the
+// textbook 7th-order one in the reference already.
+void wenorec_nw(int ng, const double* vp, const double* vm, double& vminus, double& vplus, bool fix) {
+  if (ng == 4) {
+    const double denom = 1.0 / 420.0;
+    vminus = (-3.0 * vp[1] + 25.0 * vp[2] - 101.0 * vp[3] + 319.0 * vp[4] + 214.0 * vp[5] - 38.0 * vp[6] +
+              4.0 * vp[7]) * denom;
+    vplus = (-3.0 * vm[8] + 25.0 * vm[7] - 101.0 * vm[6] + 319.0 * vm[5] + 214.0 * vm[4] - 38.0 * vm[3] +
+             4.0 * vm[2]) * denom;
+    return;
+  }
   const double denom = 1.0 / 60.0;
   if (!fix) {
     vminus = (-3.0 * vp[1] + 27.0 * vp[2] + 47.0 * vp[3] - 13.0 * vp[4] + 2.0 * vp[5]) * denom;
@@ -463,16 +510,29 @@ void wenorec_nw(const double* vp, const double* vm, double& vminus, double& vplu
   }
 }
 
-// wenorec (module_weno.f90:286-527), ng = 3
+// wenorec (module_weno.f90:286-527): nonlinear reconstruction of the '-'
+// state from vp (stencil centre i = ng) and of the '+' state from vm
+// (centre i = ng + 1), 1-based arrays of length 2ng.
 void wenorec(const Weno& w, const double* vp, const double* vm, double& vminus, double& vplus) {
   const double eps_weno = 1.0e-10;
-  double vpr[3], vmr[3], beta[3], alfa[3], omega[3], sum;
-  int i = 3;
-  for (int r = 0; r < 3; ++r) {
-    vpr[r] = 0.0;
-    for (int j = 0; j < 3; ++j) vpr[r] = vpr[r] + w.cweno[r + 1][j] * vp[i - r + j];
-  }
+  const int ng = w.ng;
+  double vpr[4], vmr[4], beta[4], alfa[4], omega[4], sum;
   auto betas = [&](const double* q, int ii) {
+    if (ng == 4) {
+      beta[0] = q[ii] * (w.zf * q[ii] + w.zh * q[ii + 1] + w.zl * q[ii + 2] + w.zb * q[ii + 3]) +
+                q[ii + 1] * (w.zi * q[ii + 1] + w.ze * q[ii + 2] + w.zc * q[ii + 3]) +
+                q[ii + 2] * (w.zg * q[ii + 2] + w.zd * q[ii + 3]) + q[ii + 3] * (w.za * q[ii + 3]);
+      beta[1] = q[ii - 1] * (w.za * q[ii - 1] + w.zo * q[ii] + w.zs * q[ii + 1] + w.zt * q[ii + 2]) +
+                q[ii] * (w.zm * q[ii] + w.zn * q[ii + 1] + w.zp * q[ii + 2]) +
+                q[ii + 1] * (w.zq * q[ii + 1] + w.zu * q[ii + 2]) + q[ii + 2] * (w.zr * q[ii + 2]);
+      beta[2] = q[ii - 2] * (w.zr * q[ii - 2] + w.zu * q[ii - 1] + w.zp * q[ii] + w.zt * q[ii + 1]) +
+                q[ii - 1] * (w.zq * q[ii - 1] + w.zn * q[ii] + w.zs * q[ii + 1]) +
+                q[ii] * (w.zm * q[ii] + w.zo * q[ii + 1]) + q[ii + 1] * (w.za * q[ii + 1]);
+      beta[3] = q[ii - 3] * (w.za * q[ii - 3] + w.zd * q[ii - 2] + w.zc * q[ii - 1] + w.zb * q[ii]) +
+                q[ii - 2] * (w.zg * q[ii - 2] + w.ze * q[ii - 1] + w.zl * q[ii]) +
+                q[ii - 1] * (w.zi * q[ii - 1] + w.zh * q[ii]) + q[ii] * (w.zf * q[ii]);
+      return;
+    }
     double a = q[ii] + w.za * q[ii + 1] + q[ii + 2];
     double bq = w.zc * q[ii] + w.zb * q[ii + 1] + q[ii + 2];
     beta[0] = w.z1 * a * a + w.z2 * bq * bq;
@@ -483,32 +543,37 @@ void wenorec(const Weno& w, const double* vp, const double* vm, double& vminus, 
     bq = q[ii - 2] + w.zb * q[ii - 1] + w.zc * q[ii];
     beta[2] = w.z1 * a * a + w.z2 * bq * bq;
   };
+  int i = ng;
+  for (int r = 0; r < ng; ++r) {
+    vpr[r] = 0.0;
+    for (int j = 0; j < ng; ++j) vpr[r] = vpr[r] + w.cweno[r + 1][j] * vp[i - r + j];
+  }
   betas(vp, i);
   sum = 0.0;
-  for (int r = 0; r < 3; ++r) {
+  for (int r = 0; r < ng; ++r) {
     alfa[r] = w.dweno[r] / ((eps_weno + beta[r]) * (eps_weno + beta[r]));
     sum = sum + alfa[r];
   }
   sum = 1.0 / sum;
-  for (int r = 0; r < 3; ++r) omega[r] = alfa[r] * sum;
+  for (int r = 0; r < ng; ++r) omega[r] = alfa[r] * sum;
   vminus = 0.0;
-  for (int r = 0; r < 3; ++r) vminus = vminus + omega[r] * vpr[r];
+  for (int r = 0; r < ng; ++r) vminus = vminus + omega[r] * vpr[r];
 
-  i = 4;
-  for (int r = 0; r < 3; ++r) {
+  i = ng + 1;
+  for (int r = 0; r < ng; ++r) {
     vmr[r] = 0.0;
-    for (int j = 0; j < 3; ++j) vmr[r] = vmr[r] + w.cweno[r][j] * vm[i - r + j];
+    for (int j = 0; j < ng; ++j) vmr[r] = vmr[r] + w.cweno[r][j] * vm[i - r + j];
   }
   betas(vm, i);
   sum = 0.0;
-  for (int r = 0; r < 3; ++r) {
+  for (int r = 0; r < ng; ++r) {
     alfa[r] = w.dtweno[r] / ((eps_weno + beta[r]) * (eps_weno + beta[r]));
     sum = sum + alfa[r];
   }
   sum = 1.0 / sum;
-  for (int r = 0; r < 3; ++r) omega[r] = alfa[r] * sum;
+  for (int r = 0; r < ng; ++r) omega[r] = alfa[r] * sum;
   vplus = 0.0;
-  for (int r = 0; r < 3; ++r) vplus = vplus + omega[r] * vmr[r];
+  for (int r = 0; r < ng; ++r) vplus = vplus + omega[r] * vmr[r];
 }
 
 // euler_LLF_x/_y/_z (module_weno.f90:537-1044, 1055-1590, 1595-2125).
@@ -520,13 +585,16 @@ int euler_flux(Ctx& c, int d, const double* v, const double* T, const double* W_
   const izem_thd& t = c.thd;
   const int ng = b.ng, nv = b.nv, nrv = b.nrv, st_m1 = 2 * ng;
   const size_t nc = b.ncell;
-  const Weno w = wenopar();
+  const Weno w = wenopar(ng);
   const int n = b.n(d);
   const int t1 = d == 0 ? 1 : 0, t2 = d == 2 ? 1 : 2;  // tangential components
   const double* di = c.dxi[d].data();
   const bool fixlin = c.cfg.weno5_linear_fix != 0;
   int m1 = d == 0 ? b.ny : b.nx, m2 = d == 2 ? b.ny : b.nz;
   bool negp = false;
+  // MPI block of a point along the sweep (x only; ghosts belong to the edge blocks)
+  const int nxb = d == 0 ? std::max(c.sensor_xblocks, 1) : 1, bxs = n / nxb;
+  auto xblk = [&](int s) { return (std::min(std::max(s, 1), n) - 1) / bxs; };
 #pragma omp parallel for collapse(2) schedule(dynamic)
   for (int q2 = 1; q2 <= m2; ++q2)
     for (int q1 = 1; q1 <= m1; ++q1) {
@@ -538,7 +606,7 @@ int euler_flux(Ctx& c, int d, const double* v, const double* T, const double* W_
       const int len = n + 2 * ng;
       std::vector<double> rho_i(len), uu[3], P(len), gam(len), cs(len), ht(len), et(len), Ya(len * nrv);
       for (int a = 0; a < 3; ++a) uu[a].assign(len, 0.0);
-      std::vector<double> fhat((n + 1) * nv);
+      std::vector<double> fhat((n + 1) * nv), fhatR((n + 1) * nv);
       auto ix = [&](int s) { return s - 1 + ng; };
       for (int s = 1 - ng; s <= n + ng; ++s) {
         size_t p = cell(s);
@@ -564,9 +632,9 @@ int euler_flux(Ctx& c, int d, const double* v, const double* T, const double* W_
         ht[ix(s)] = h + 0.5 * (ux * ux + vy * vy + wz * wz);
         et[ix(s)] = v[4 * nc + p] * rho_i[ix(s)];
       }
-      double f_s[8][2 * IZEM_NSMAX + 6], L_s[8][2 * IZEM_NSMAX + 6];
+      double f_s[9][2 * IZEM_NSMAX + 6], L_s[9][2 * IZEM_NSMAX + 6];
       double el[IZEM_NSMAX + 5][IZEM_NSMAX + 5], er[IZEM_NSMAX + 5][IZEM_NSMAX + 5];
-      double gplus[8], gminus[8], ghat[IZEM_NSMAX + 5];
+      double gplus[9], gminus[9], ghat[IZEM_NSMAX + 5];
       for (int il = 0; il <= n; ++il) {
         int ir = il + 1;
         for (int st = 1; st <= st_m1; ++st) {
@@ -663,10 +731,22 @@ int euler_flux(Ctx& c, int d, const double* v, const double* T, const double* W_
         er[nv - 1][5] = -1.0 / psi_c[nrv - 1];
         wrk = -1.0 / psi_c[nrv - 1];
         for (int l = 1; l <= nrv - 1; ++l) er[nv - 1][l + 5] = wrk * psi_c[l - 1];
-        // characteristic LLF-WENO (module_weno.f90:953-989)
-        bool shk = false;
-        for (int s = il - ng + 1; s <= il + ng; ++s) shk = shk || (sensor[cell(s)] != 0);
-        shk = shk && c.cfg.weno_avg;
+        // characteristic LLF-WENO (module_weno.f90:953-989).  The sensor
+        // is evaluated on each MPI block's interior and never exchanged, so
+        // a block sees its neighbours' points as unflagged: a face is
+        // evaluated with the flags of the block that uses it, and a face on
+        // a block edge twice (left block's view into fhat, right block's
+        // view into fhatR).
+        const int vL = xblk(il), vR = xblk(ir);
+        bool shkL = false, shkR = false;
+        for (int s = il - ng + 1; s <= il + ng; ++s) {
+          if (!sensor[cell(s)]) continue;
+          if (xblk(s) == vL) shkL = true;
+          if (xblk(s) == vR) shkR = true;
+        }
+        for (int view = 0; view < (vL == vR ? 1 : 2); ++view) {
+        const bool shk = (view ? shkR : shkL) && c.cfg.weno_avg;
+        double* fout = view ? fhatR.data() : fhat.data();
         for (int m = 0; m < nv; ++m) {
           double eigenmax = -1.0;
           for (int st = 1; st <= st_m1; ++st) eigenmax = std::max(L_s[st][m], eigenmax);
@@ -683,18 +763,20 @@ int euler_flux(Ctx& c, int d, const double* v, const double* T, const double* W_
           }
           double gl, gr;
           if (shk) wenorec(w, gplus, gminus, gl, gr);
-          else wenorec_nw(gplus, gminus, gl, gr, fixlin);
+          else wenorec_nw(ng, gplus, gminus, gl, gr, fixlin);
           ghat[m] = gl + gr;
         }
         for (int m = 0; m < nv; ++m) {
           double fh = 0.0;
           for (int mm = 0; mm < nv; ++mm) fh = fh + er[m][mm] * ghat[mm];
-          fhat[il * nv + m] = fh;
+          fout[il * nv + m] = fh;
+        }
         }
       }
       for (int m = 0; m < nv; ++m)
         for (int s = 1; s <= n; ++s) {
-          double df = (fhat[s * nv + m] - fhat[(s - 1) * nv + m]) * di[s - 1 + ng];
+          const double* fleft = xblk(s - 1) == xblk(s) ? fhat.data() : fhatR.data();
+          double df = (fhat[s * nv + m] - fleft[(s - 1) * nv + m]) * di[s - 1 + ng];
           int i, j, k;
           if (d == 0) { i = s; j = q1; k = q2; }
           else if (d == 1) { i = q1; j = s; k = q2; }
@@ -728,9 +810,13 @@ void shock_sensor(const Ctx& c, const double* v, const double* T, const double* 
     double dpres = std::fabs(P[q] - P[p]) / std::min(P[p], P[q]);
     if (drho > mrw && dpres > mrw) sensor[p] = 1;
   };
+  // On each MPI block the x loop runs to ex - 1 with min(i+1, ex): a
+  // block's last point is never compared with the next block's first one.
+  const int bx = b.nx / std::max(c.sensor_xblocks, 1);
   for (int k = 1; k <= b.nz; ++k)
     for (int j = 1; j <= b.ny; ++j)
-      for (int i = 1; i <= b.nx - 1; ++i) test(b.id(i, j, k), b.id(std::min(i + 1, b.nx), j, k));
+      for (int i = 1; i <= b.nx - 1; ++i)
+        if (i % bx != 0) test(b.id(i, j, k), b.id(std::min(i + 1, b.nx), j, k));
   for (int k = 1; k <= b.nz; ++k)
     for (int i = 1; i <= b.nx; ++i)
       for (int j = 1; j <= b.ny - 1; ++j) test(b.id(i, j, k), b.id(i, std::min(j + 1, b.ny), k));
@@ -932,7 +1018,7 @@ int rk3(Ctx& c, double dt, double* v, double* T, double* W_i, double* cp, double
   for (int ik = 0; ik < 3; ++ik) {
     shock_sensor(c, v, T, W_i, sensor);
     int rc;
-    for (int d = 0; d < 3; ++d)
+    for (int d = 0; d < c.cfg.ndim; ++d)   // euler_LLF_z only when ndim == 3 (module_solver.f90:769-774)
       if ((rc = euler_flux(c, d, v, T, W_i, cp, ha, sensor, f.data()))) return rc;
     if (c.cfg.vis)
       if ((rc = visc_flux(c, v, T, W_i, cp, ha, f.data()))) return rc;
@@ -1059,7 +1145,9 @@ extern "C" {
 
 void* or_create(const izem_cfg* cfg, const izem_thd* thd, const izem_adi* adi, const double* dx_i,
                 const double* dy_i, const double* dz_i) {
-  if (!cfg || !thd || !adi || cfg->ng != 3 || cfg->nrv < 2 || cfg->nrv > IZEM_NSMAX) return nullptr;
+  if (!cfg || !thd || !adi || (cfg->ng != 3 && cfg->ng != 4) || (cfg->ndim != 2 && cfg->ndim != 3) ||
+      (cfg->ndim == 2 && cfg->nz != 1) || cfg->nrv < 2 || cfg->nrv > IZEM_NSMAX)
+    return nullptr;
   Ctx* c = new Ctx();
   c->cfg = *cfg;
   c->thd = *thd;
@@ -1079,6 +1167,15 @@ void* or_create(const izem_cfg* cfg, const izem_thd* thd, const izem_adi* adi, c
 }
 
 void or_destroy(void* h) { delete static_cast<Ctx*>(h); }
+
+// The reference's run decomposed x into nblk equal MPI blocks: the shock
+// sensor of each block stops at its own last point (module_tools.f90:2761-2770).
+int or_set_sensor_xblocks(void* h, int nblk) {
+  Ctx* c = static_cast<Ctx*>(h);
+  if (nblk < 1 || c->b.nx % nblk) return IZEM_ERR_ARG;
+  c->sensor_xblocks = nblk;
+  return IZEM_OK;
+}
 
 int or_last_error(void* h, char* buf, int n) {
   Ctx* c = static_cast<Ctx*>(h);
@@ -1169,16 +1266,25 @@ void or_ck_wdot(const izem_mech* mech, double rho, double T, const double* Y, do
   ck_wyr(*mech, rho, T, Y, wdot);
 }
 
-// dscalar + inversion (module_deriv.f90:80-205, module_tools.f90:374-426)
+// dscalar + inversion (module_deriv.f90:80-205, module_tools.f90:374-426):
+// central 6th order (ng = 3) or 8th order with 6th-order fourth rows (ng = 4)
 void or_metrics_dscalar(int n, int ng, const double* coord, double* d_i) {
-  (void)ng;
   std::vector<double> dv(n, 1.0);
   auto v = [&](int m) { return coord[m - 1]; };
-  for (int m = 1 + 3; m <= n - 3; ++m) {
+  for (int m = 1 + ng; m <= n - ng; ++m) {
     double dd = 0.0;
-    for (int l = -3; l <= 3; ++l) dd = dd + alpha6[l + 3] * v(m + l);
+    if (ng == 4)
+      for (int l = -4; l <= 4; ++l) dd = dd + alpha8[l + 4] * v(m + l);
+    else
+      for (int l = -3; l <= 3; ++l) dd = dd + alpha6[l + 3] * v(m + l);
     dv[m - 1] = dd * 1.0;
   }
+  if (ng == 4)
+    for (int m : {4, n - 3}) {
+      double dd = 0.0;
+      for (int l = -3; l <= 3; ++l) dd = dd + alpha6[l + 3] * v(m + l);
+      dv[m - 1] = dd * 1.0;
+    }
   { int m = 1; double dd = 0.0; for (int l = 0; l <= 4; ++l) dd = dd + alph4ol[l] * v(m + l); dv[m - 1] = dd * 1.0; }
   { int m = 2; double dd = 0.0; for (int l = -1; l <= 3; ++l) dd = dd + alph4ul[l + 1] * v(m + l); dv[m - 1] = dd * 1.0; }
   { int m = 3; double dd = 0.0; for (int l = -2; l <= 2; ++l) dd = dd + alph4[l + 2] * v(m + l); dv[m - 1] = dd * 1.0; }

@@ -15,7 +15,9 @@ Run from the repository root, where the reference tree is readable:
     python tests/golden/make_sod_fixtures.py /path/to/devel-izem/testcases/sod
 
 It writes tests/golden/sod_restart_000NN.npz (arrays rho, rhoU, rhoV, rhoW,
-rhoE, O2, N2 with shape (ntx, nty, ntz) in Fortran index order, and time).
+rhoE, O2, N2 with shape (ntx, nty, ntz) in Fortran index order, and time)
+and tests/golden/sod_grid.npz (the x, y, z coordinates of grid.dat, in
+metres, parsed as the reference's list-directed read parses them).
 """
 import os
 import struct
@@ -105,7 +107,23 @@ def read_h5(path):
     return out
 
 
+def read_grid(path):
+    """The X-, Y- and Z-DIRECTION coordinate lists of a grid.dat file."""
+    out, cur = {}, None
+    for line in open(path):
+        t = line.strip()
+        if t.endswith("-DIRECTION"):
+            cur = t[0].lower()
+            out[cur] = []
+        elif t == "END":
+            break
+        elif t and cur:
+            out[cur].append(float(t))
+    return {k: np.array(v, dtype=np.float64) for k, v in out.items()}
+
+
 def main(sod_dir):
+    np.savez_compressed(os.path.join(HERE, "sod_grid.npz"), **read_grid(os.path.join(sod_dir, "grid.dat")))
     for n in RESTARTS:
         f = read_h5(os.path.join(sod_dir, "restarts", "restart_%05d.h5" % n))
         arrays = {k.split("/")[1]: v for k, v in f.items() if k.startswith("consvar/")}
