@@ -216,14 +216,23 @@ class IzemGPU:
         self._check(self.lib.izem_gpu_upload_state(self.h, _ptr(v), _ptr(T), _ptr(W_i), _ptr(cp), _ptr(ha),
                                                    _ptr(ss, _u8p)), "upload_state")
 
-    def download(self):
+    def download(self, out=None):
+        """The ghosted state as Fortran-ordered host arrays.  `out` (a dict
+        like the one returned, e.g. in pinned memory) is filled in place
+        instead of allocating new arrays."""
         gx, gy, gz = self.shape
-        v = np.empty((gx, gy, gz, self.nv), order="F")
-        T = np.empty((gx, gy, gz), order="F")
-        W_i = np.empty((gx, gy, gz), order="F")
-        cp = np.empty((gx, gy, gz), order="F")
-        ha = np.empty((gx, gy, gz, self.cfg.nrv), order="F")
-        ss = np.empty((gx, gy, gz), dtype=np.uint8, order="F")
+        shapes = {"v": ((gx, gy, gz, self.nv), np.float64), "T": ((gx, gy, gz), np.float64),
+                  "W_i": ((gx, gy, gz), np.float64), "cp": ((gx, gy, gz), np.float64),
+                  "ha": ((gx, gy, gz, self.cfg.nrv), np.float64), "shock_sensor": ((gx, gy, gz), np.uint8)}
+        arr = {}
+        for k, (shp, dt) in shapes.items():
+            a = None if out is None else out.get(k)
+            if a is None:
+                a = np.empty(shp, dtype=dt, order="F")
+            elif a.shape != shp or a.dtype != dt or not a.flags.f_contiguous:
+                raise ValueError("download: out[%r] must be a Fortran-ordered %s array of shape %s" % (k, dt, shp))
+            arr[k] = a
+        v, T, W_i, cp, ha, ss = (arr[k] for k in ("v", "T", "W_i", "cp", "ha", "shock_sensor"))
         self._check(self.lib.izem_gpu_download_state(self.h, _ptr(v), _ptr(T), _ptr(W_i), _ptr(cp), _ptr(ha),
                                                      _ptr(ss, _u8p)), "download_state")
         return {"v": v, "T": T, "W_i": W_i, "cp": cp, "ha": ha, "shock_sensor": ss}
