@@ -220,50 +220,44 @@ inline ChemFast chem_fast_constants(const izem_mech& m) {
   return f;
 }
 
-// The constant-volume reactor right-hand side of ck_fun with the divisions
-// by T, by the molar masses and by the Troe temperatures replaced by
-// multiplications with reciprocals, and 10^x / log10 by exp / log: the same
-// CHEMKIN expressions (CKCVBS, CKHMS, CKRATT, CKRATX, CKWYR) with different
-// rounding (a few ulp per term) and about a sixth of the FP64 instructions
-// of the divisions.  The BDF kernels call this one; ck_fun above keeps the
-// reference's operation order for the host build that is compared with the
-// oracle bit for bit.
+// The temperature-only terms of ck_fun_fast: species c_v and h, the forward
+// and reverse rate constants, and the fall-off low-pressure rates and
+// log10 F_cent.  The finite-difference Jacobian perturbs one variable per
+// column, so its nine species columns share the temperature of the call
+// before them and can reuse these terms (rc_drive).
 template <int KK>
-HD void ck_fun_fast(double rho, const double* z, double* zp) {
-  constexpr double kLn10 = 2.302585092994045684, kInvLn10 = 0.4342944819032518277;
-  const double T = z[0];
-  const double* Y = z + 1;
+struct FunT {
+  double T;                                    // temperature the entries belong to
+  double rut;                                  // RU * T
+  double cvk[KK], h[KK];
+  double kf[IZEM_MAXREAC], kr[IZEM_MAXREAC];   // before third-body and fall-off factors
+  double klow[IZEM_MAXREAC], fclog[IZEM_MAXREAC];
+};
+
+template <int KK>
+HD void fun_tpart(double T, FunT<KK>& t) {
   const double Tinv = 1.0 / T;
   const double alogt = log(T);
   const double T2 = T * T, T3 = T * T2, T4 = T2 * T2;
-  const double rut = T * c_mech.ru;
-  double cv = 0.0, h[KK], C[KK], wdot[KK];
-  double ctot = 0.0;
+  t.T = T;
+  t.rut = T * c_mech.ru;
+  double smh[KK];
 #pragma unroll
   for (int k = 0; k < KK; ++k) {
     const double* a = c_mech.a[k][T > c_mech.tmid[k] ? 1 : 0];
     const double cps = a[0] + T * a[1] + T2 * a[2] + T3 * a[3] + T4 * a[4];
-    cv = cv + Y[k] * (c_fast.ru_wt[k] * (cps - 1.0));
+    t.cvk[k] = c_fast.ru_wt[k] * (cps - 1.0);
     const double hs = a[0] + (0.5 * T) * a[1] + (T2 * (1.0 / 3.0)) * a[2] + (0.25 * T3) * a[3] + (0.2 * T4) * a[4];
-    h[k] = rut * (hs + a[5] * Tinv) * c_fast.wt_inv[k];
-    C[k] = rho * Y[k] * c_fast.wt_inv[k];
-    ctot = ctot + C[k];
-    wdot[k] = 0.0;
-  }
-  double smh[KK];
-  if (c_need_eqk) {
-#pragma unroll
-    for (int k = 0; k < KK; ++k) {
-      const double* a = c_mech.a[k][T > c_mech.tmid[k] ? 1 : 0];
+    t.h[k] = t.rut * (hs + a[5] * Tinv) * c_fast.wt_inv[k];
+    if (c_need_eqk) {
       const double sv = (alogt - 1.0) * a[0] + (0.5 * T) * a[1] + (T2 * (1.0 / 6.0)) * a[2] +
                         (T3 * (1.0 / 12.0)) * a[3] + (T4 * 0.05) * a[4];
       smh[k] = sv + a[6] - a[5] * Tinv;
     }
   }
-  double rop[IZEM_MAXREAC];
   const int ii = c_mech.ii;
   for (int i = 0; i < ii; ++i) {
-    double rkft = c_mech.par[i][0] * exp(c_mech.par[i][1] * alogt - c_mech.par[i][2] * Tinv);
+    const double rkft = c_mech.par[i][0] * exp(c_mech.par[i][1] * alogt - c_mech.par[i][2] * Tinv);
     double rkrt = 0.0;
     const int rv = c_mech.rev[i];
     if (rv == 1) {
@@ -280,6 +274,40 @@ HD void ck_fun_fast(double rho, const double* z, double* zp) {
     } else if (rv == 2) {
       rkrt = c_mech.rpar[i][0] * exp(c_mech.rpar[i][1] * alogt - c_mech.rpar[i][2] * Tinv);
     }
+    t.kf[i] = rkft;
+    t.kr[i] = rkrt;
+    const int fo = c_mech.fall[i];
+    if (fo) {
+      t.klow[i] = c_mech.low[i][0] * exp(c_mech.low[i][1] * alogt - c_mech.low[i][2] * Tinv);
+      if (fo > 1) {
+        constexpr double kInvLn10 = 0.4342944819032518277;
+        const double ta = c_mech.troe[i][0];
+        double fcent = (1.0 - ta) * exp(-T * c_fast.troe_inv[i][0]) + ta * exp(-T * c_fast.troe_inv[i][1]);
+        if (fo == 4) fcent = fcent + exp(-c_mech.troe[i][3] * Tinv);
+        t.fclog[i] = log(fmax(fcent, 1.0e-300)) * kInvLn10;
+      }
+    }
+  }
+}
+
+// The composition-dependent rest of ck_fun_fast, from the temperature terms t.
+template <int KK>
+HD void fun_cpart(double rho, const double* z, const FunT<KK>& t, double* zp) {
+  constexpr double kLn10 = 2.302585092994045684, kInvLn10 = 0.4342944819032518277;
+  const double* Y = z + 1;
+  double cv = 0.0, C[KK], wdot[KK];
+  double ctot = 0.0;
+#pragma unroll
+  for (int k = 0; k < KK; ++k) {
+    cv = cv + Y[k] * t.cvk[k];
+    C[k] = rho * Y[k] * c_fast.wt_inv[k];
+    ctot = ctot + C[k];
+    wdot[k] = 0.0;
+  }
+  double rop[IZEM_MAXREAC];
+  const int ii = c_mech.ii;
+  for (int i = 0; i < ii; ++i) {
+    double rkft = t.kf[i], rkrt = t.kr[i];
     double ctb = 1.0;
     if (c_mech.thb[i]) {
       ctb = ctot;
@@ -288,16 +316,12 @@ HD void ck_fun_fast(double rho, const double* z, double* zp) {
     }
     const int fo = c_mech.fall[i];
     if (fo) {
-      const double rklow = c_mech.low[i][0] * exp(c_mech.low[i][1] * alogt - c_mech.low[i][2] * Tinv);
-      const double pr = rklow * ctb / rkft;
+      const double pr = t.klow[i] * ctb / rkft;
       ctb = 1.0;
       double pcor = pr / (1.0 + pr);
       if (fo > 1) {
         const double prlog = log(fmax(pr, 1.0e-300)) * kInvLn10;
-        const double ta = c_mech.troe[i][0];
-        double fcent = (1.0 - ta) * exp(-T * c_fast.troe_inv[i][0]) + ta * exp(-T * c_fast.troe_inv[i][1]);
-        if (fo == 4) fcent = fcent + exp(-c_mech.troe[i][3] * Tinv);
-        const double fclog = log(fmax(fcent, 1.0e-300)) * kInvLn10;
+        const double fclog = t.fclog[i];
         const double xn = 0.75 - 1.27 * fclog;
         const double cprlog = prlog - (0.4 + 0.67 * fclog);
         const double q = cprlog / (xn - 0.14 * cprlog);
@@ -334,9 +358,24 @@ HD void ck_fun_fast(double rho, const double* z, double* zp) {
 #pragma unroll
   for (int k = 0; k < KK; ++k) {
     zp[k + 1] = wdot[k] * c_mech.wt[k] * rho_i;
-    sum = sum + h[k] * wdot[k] * c_mech.wt[k] + (-rut) * wdot[k];
+    sum = sum + t.h[k] * wdot[k] * c_mech.wt[k] + (-t.rut) * wdot[k];
   }
   zp[0] = -sum / (rho * cv);
+}
+
+// The constant-volume reactor right-hand side of ck_fun with the divisions
+// by T, by the molar masses and by the Troe temperatures replaced by
+// multiplications with reciprocals, and 10^x / log10 by exp / log: the same
+// CHEMKIN expressions (CKCVBS, CKHMS, CKRATT, CKRATX, CKWYR) with different
+// rounding (a few ulp per term) and about a sixth of the FP64 instructions
+// of the divisions.  The BDF kernels call it in two parts (fun_tpart,
+// fun_cpart); ck_fun above keeps the reference's operation order for the
+// host build that is compared with the oracle bit for bit.
+template <int KK>
+HD void ck_fun_fast(double rho, const double* z, double* zp) {
+  FunT<KK> t;
+  fun_tpart<KK>(z[0], t);
+  fun_cpart<KK>(rho, z, t, zp);
 }
 
 // ------------------------------------------------------------- DVODE -------
@@ -938,7 +977,10 @@ HD bool rc_advance(Rc<N>& r) {
           break;
         }
         const double srur = 1.4901161193847656e-08;   // sqrt(UROUND)
-        const int j = r.jcol;
+        // columns are independent: the species columns (1..N-1) come first,
+        // at the temperature of the FUN call before the Jacobian, and the
+        // temperature column last (rc_drive reuses the temperature terms)
+        const int j = (r.jcol + 1) % N;
         r.yj = r.y[j];
         const double rj = fmax(srur * fabs(r.yj), r.r0 / r.ewt[j]);
         r.y[j] = r.y[j] + rj;
@@ -947,10 +989,10 @@ HD bool rc_advance(Rc<N>& r) {
         return true;
       }
       case ST_JAC_COL_F: {
-        const int j = r.jcol;
+        const int j = (r.jcol + 1) % N;
         for (int i = 0; i < N; ++i) r.wmjs[i + j * N] = (r.fo[i] - r.savf[i]) * r.rfac;
         r.y[j] = r.yj;
-        r.jcol = j + 1;
+        r.jcol = r.jcol + 1;
         r.pc = ST_JAC_COL;
         break;
       }
@@ -1048,6 +1090,8 @@ template <int KK, class Load, class Store>
 __device__ __forceinline__ void rc_drive(unsigned n, unsigned* counter, Load load, Store store) {
   constexpr int N = KK + 1;
   Rc<N> r;
+  FunT<KK> ft;   // temperature terms of this thread's last right-hand side
+  ft.T = -1.0;
   unsigned q = 0;
   bool active = false;
   long long nfun = 0;
@@ -1064,7 +1108,13 @@ __device__ __forceinline__ void rc_drive(unsigned n, unsigned* counter, Load loa
     bool need = rc_advance<N>(r);
     if (need && ++nfun > kMaxFun) { r.istate = -99; need = false; }
     if (need) {
-      ck_fun_fast<KK>(r.rho, r.y, r.fo);
+      // The temperature terms are recomputed unless every evaluating lane
+      // of the warp is at the temperature of its previous call (the
+      // species columns of a Jacobian): a per-lane choice would only make
+      // the warp wait for its slowest lane.  Reused terms are the bits the
+      // recomputation would give.
+      if (!__all_sync(__activemask(), r.y[0] == ft.T)) fun_tpart<KK>(r.y[0], ft);
+      fun_cpart<KK>(r.rho, r.y, ft, r.fo);
     } else {
       store(q, r);
       active = false;
