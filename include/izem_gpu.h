@@ -262,6 +262,11 @@ int  izem_gpu_psr_batch_mlp(izem_mlp* m, izem_mlp* m2, const izem_mech* mech, in
                             const double* rho, double* Y, const double* dt, int device_ptrs,
                             const double* gate10, const int* kncf, int nele, double* dT_pred,
                             int* stats3, float* ms2);
+/* The cells that the last izem_gpu_psr_batch_mlp call on m sent to the BDF
+ * integrator (no counterpart in the reference): their indices in that
+ * call's batch, in no particular order; up to cap of them are written to
+ * out (host memory), and *count receives their number. */
+int  izem_mlp_fallback_cells(izem_mlp* m, int* out, int cap, int* count);
 /* No counterpart in the reference.  Inference for callers that cannot
  * allocate device memory while they run -- a solver whose own arena (or a
  * framework's caching allocator) already holds the GPU's memory, or one that

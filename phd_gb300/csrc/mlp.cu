@@ -688,6 +688,22 @@ int izem_gpu_psr_batch_mlp(izem_mlp* m, izem_mlp* m2, const izem_mech* mech, int
   return rc;
 }
 
+
+// The cells the last izem_gpu_psr_batch_mlp call on m sent to the BDF
+// integrator, as indices into that call's batch, in no particular order:
+// up to cap of them are copied to out (host), *count receives their number.
+int izem_mlp_fallback_cells(izem_mlp* m, int* out, int cap, int* count) {
+  if (!m || !count || (cap > 0 && !out)) return IZEM_ERR_ARG;
+  unsigned nfb = 0;
+  if (m->g_count && cudaMemcpy(&nfb, m->g_count, sizeof(unsigned), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return IZEM_ERR_CUDA;
+  *count = (int)nfb;
+  const int ncopy = (int)nfb < cap ? (int)nfb : cap;
+  if (ncopy > 0 && cudaMemcpy(out, m->g_list, (size_t)ncopy * sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return IZEM_ERR_CUDA;
+  return IZEM_OK;
+}
+
 }  // extern "C"
 
 // ===================================================== no-alloc inference ===

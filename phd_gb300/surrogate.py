@@ -41,6 +41,7 @@ def _bind(lib):
         "izem_mlp_get_params": (C.c_int, [P, fpp, fpp]),
         "izem_mlp_set_norm": (C.c_int, [P, C.POINTER(C.c_float)]),
         "izem_mlp_forward": (C.c_int, [P, C.c_int, C.c_void_p, C.c_void_p]),
+        "izem_mlp_fallback_cells": (C.c_int, [P, C.c_void_p, C.c_int, C.POINTER(C.c_int)]),
         "izem_mlp_grads": (C.c_int, [P, C.c_int, C.c_void_p, C.c_void_p, C.POINTER(C.c_double), fpp, fpp]),
         "izem_mlp_train": (C.c_int, [P, C.c_longlong, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_float,
                                      C.c_uint, C.c_void_p]),
@@ -191,6 +192,19 @@ class Surrogate:
         return {"fallback": int(st3[0]), "max_steps": int(st3[1]), "failed": int(st3[2]), "ms": float(ms2[0]),
                 "ms_mlp": float(ms2[1]), "dT_pred": dTp}
 
+    def fallback_cells(self):
+        """Sorted indices of the cells the last chem_step / chem_step_device
+        on this network sent to the BDF integrator."""
+        cnt = C.c_int()
+        rc = self.lib.izem_mlp_fallback_cells(self.h, None, 0, C.byref(cnt))
+        if rc:
+            raise IzemError(rc, "izem_mlp_fallback_cells")
+        out = np.zeros(max(cnt.value, 1), dtype=np.int32)
+        rc = self.lib.izem_mlp_fallback_cells(self.h, out.ctypes.data, cnt.value, C.byref(cnt))
+        if rc:
+            raise IzemError(rc, "izem_mlp_fallback_cells")
+        return np.sort(out[:cnt.value])
+
     def chem_step_device(self, mech, n, T, rho, Y, dt, gate, partner=None):
         """chem_step on arrays already on the device (torch CUDA tensors:
         T, rho, dt (n), Y (n, 9) row-major), updated in place; the caller's
@@ -250,7 +264,8 @@ def calibrate_cap(nets, mech, gate=DEFAULT_GATE, n=1 << 20, seed=977, target=0.0
     g[9] = float("inf")
     r = nets[0].chem_step(mech, Ts, rho.copy(), Ys, dt.copy(), g, partner=nets[1] if len(nets) > 1 else None)
     err = np.abs((Ts - T) - ref)
-    acc = err > 0.0          # rejected cells repeat the BDF result exactly
+    acc = np.ones(n, dtype=bool)
+    acc[nets[0].fallback_cells()] = False
     pred = np.abs(r["dT_pred"])
     scale = float(np.abs(ref).max())
     table, best = [], None

@@ -82,9 +82,9 @@ def test_surrogate_gains_over_bdf_with_gate():
     surrogate step, with its |dT| cap calibrated on other held-out reactors,
     is faster than BDF on every cell, and with the fallback active its
     temperature increments stay within 1 % of the largest FP64 increment.
-    Without the cap, the same step accepts more cells: cells above the cap
-    get the BDF result bit for bit with it, and the others the same
-    surrogate result."""
+    Without the cap, the same step accepts more cells: with it, the cells
+    predicted above the cap go to the BDF integrator, and the others get the
+    same surrogate result."""
     mech = h2_mechanism()
     s, s2 = train_ensemble(mech, n=1 << 19, seed=31, epochs=24)
     gcap, cal = calibrate_cap([s, s2], mech, DEFAULT_GATE, n=1 << 18)
@@ -102,13 +102,23 @@ def test_surrogate_gains_over_bdf_with_gate():
     assert frac_fb < 1.0
     print("surrogate: dT cap %.0f K, fallback %.3f, max err %.3g K (scale %.3g K), BDF %.1f ms, surrogate %.1f ms "
           "(MLP %.1f ms)" % (gcap[9], frac_fb, errc.max(), scale, ms_bdf, rc["ms"], rc["ms_mlp"]))
+    fb_c = s.fallback_cells()
     Ts, Ys = T.copy(), Y.copy()
     r = s.chem_step(mech, Ts, rho.copy(), Ys, dt.copy(), DEFAULT_GATE, partner=s2)
     err = np.abs((Ts - T) - dT_ref)
-    over = np.abs(rc["dT_pred"]) > gcap[9]
-    assert r["failed"] == 0 and rc["fallback"] >= r["fallback"]
-    assert np.array_equal(Tc[over], Tb[over]) and np.array_equal(Yc[over], Yb[over])
-    assert np.all(errc <= err)
+    fb_u = s.fallback_cells()
+    assert r["failed"] == 0 and len(fb_c) == rc["fallback"] and len(fb_u) == r["fallback"]
+    # the cap only adds rejections: the cells predicted above it fall back,
+    # and the cells accepted with the cap get the same result without it
+    over = np.flatnonzero(np.abs(rc["dT_pred"]) > gcap[9])
+    assert np.all(np.isin(over, fb_c)) and np.all(np.isin(fb_u, fb_c))
+    acc_c = np.setdiff1d(np.arange(len(T)), fb_c)
+    assert np.array_equal(Tc[acc_c], Ts[acc_c]) and np.array_equal(Yc[acc_c], Ys[acc_c])
+    # fallback cells are integrated by the BDF kernel for rejected cells: the
+    # same integrator as BDF on every cell, within its tolerance (the
+    # bounds of tests/test_gpu_chem.py)
+    rT = np.abs(Tc[fb_c] - Tb[fb_c]) / (1e-6 * np.abs(Tb[fb_c]) + 1e-10)
+    assert rT.max() <= 100, rT.max()
     print("without the cap: fallback %.3f, max err %.3g K" % (r["fallback"] / len(T), err.max()))
 
 
@@ -128,8 +138,12 @@ def _small_flow():
 
 def test_flow_surrogate_with_every_cell_rejected_equals_bdf():
     """Chemistry mode CHEM_MLP with a gate that accepts nothing sends every
-    window cell through the gather, the BDF fallback list and the scatter:
-    the flow state must equal that of the BDF mode bit for bit."""
+    window cell through the gather, the BDF kernel for rejected cells and
+    the scatter: the flow state must equal that of the BDF mode.  The two
+    modes run the same integrator in two kernels, which the compiler may
+    contract differently, so temperatures and species agree within the
+    integrator's tolerance (the bounds of tests/test_gpu_chem.py) and the
+    density, momentum and energy, which chemistry does not touch, exactly."""
     g, dt = _small_flow()
     st0 = g.download()
     chem_dt = 2000.0 * dt   # long enough for visible chemistry in the mixing region
@@ -142,8 +156,12 @@ def test_flow_surrogate_with_every_cell_rejected_equals_bdf():
     got = g.download()
     st = g.surrogate_stats()
     assert st["fallback"] == st["cells"] > 0
-    assert d1 == d0
-    assert np.array_equal(got["v"], ref["v"]) and np.array_equal(got["T"], ref["T"])
+    assert abs(d1 - d0) <= 100 * (1e-6 * abs(d0) + 1e-10)
+    assert np.array_equal(got["v"][..., :5], ref["v"][..., :5])
+    assert np.all(np.abs(got["T"] - ref["T"]) <= 100 * (1e-6 * np.abs(ref["T"]) + 1e-10))
+    for q in range(5, got["v"].shape[-1]):
+        yg, yr = got["v"][..., q] / got["v"][..., 0], ref["v"][..., q] / ref["v"][..., 0]
+        assert np.abs(yg - yr).max() <= 1e-3 * max(np.abs(yr).max(), 1e-30)
 
 
 def test_flow_surrogate_error_within_gate():
