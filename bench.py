@@ -129,11 +129,11 @@ CHEM_BYTES_PER_REACTOR = 11 * 8 + 10 * 8
 # FP64 flops per BDF step of the persistent chemistry kernel (2 DFMA + DADD +
 # DMUL per thread, summed by ncu over one launch, / the BDF steps of that
 # launch): profiles/k_psr_field_mix64.md
-CHEM_FLOP_PER_BDF_STEP = 14451
+CHEM_FLOP_PER_BDF_STEP = 9793
 # DRAM bytes (read + write) per reactor of that launch, scaled by reactors to
 # other windows: the per-thread BDF state in local memory that the L2 does
 # not hold
-CHEM_TRAFFIC_PER_REACTOR = 15361
+CHEM_TRAFFIC_PER_REACTOR = 16115
 
 EULER_FLOP_PER_FACE = {2: 1400, 9: 2481}   # FP64 flops per face (sensor-off branch): ncu DFMA x2 + DADD + DMUL counts (profiles/euler_face_mix128.md)
 
