@@ -55,3 +55,33 @@ def test_host_metrics_match_oracle():
     rng = np.random.Generator(np.random.PCG64(1))
     x = np.cumsum(0.5 + rng.random(40))
     assert np.array_equal(metrics_dscalar(x), oracle.metrics_dscalar(x))
+
+
+def test_entry_points_reject_bad_arguments_before_any_device_call():
+    """Argument checks come before any CUDA call, so they hold on a machine
+    without a GPU: unsupported configurations, empty batches, unknown
+    chemistry variants and missing pointers return IZEM_ERR_ARG (1)."""
+    import numpy as np
+    import oracle
+    from phd_gb300 import ics
+    from phd_gb300.capi import IzemMech
+    from phd_gb300.izem import load_library
+    lib = load_library()
+    cfg, thd, adi, dxi, st, info = ics.tgv(8, lib_dscalar=oracle.metrics_dscalar)
+    h = C.c_void_p()
+    for field, bad in (("ng", 4), ("ndim", 2), ("nrv", 3)):
+        good = getattr(cfg, field)
+        setattr(cfg, field, bad)
+        assert lib.izem_gpu_init(C.byref(cfg), C.byref(thd), C.byref(adi), C.byref(h)) == 1, field
+        setattr(cfg, field, good)
+    mech = IzemMech()
+    mech.kk = 9
+    one = np.zeros(9)
+    p = one.ctypes.data_as(C.c_void_p)
+    assert lib.izem_gpu_psr_batch(C.byref(mech), 0, p, p, p, p, None, None, 0, None) == 1
+    mech.kk = 8
+    assert lib.izem_gpu_psr_batch(C.byref(mech), 1, p, p, p, p, None, None, 0, None) == 1
+    assert lib.izem_gpu_set_chem_variant(5) == 1 and lib.izem_gpu_set_chem_variant(-1) == 1
+    assert lib.izem_gpu_chem_autotune(C.byref(mech), 0, p, p, p, p, 0, None, 0) == 1
+    cnt = C.c_int()
+    assert lib.izem_mlp_fallback_cells(None, None, 0, C.byref(cnt)) == 1

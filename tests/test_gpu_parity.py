@@ -231,3 +231,39 @@ def test_autotune_keeps_results():
         g.set_chem_variant(5)
     for o in outs:
         _chem_close(o, outs[1])
+
+
+@pytest.mark.parametrize("name", ["tgv", "mix"])
+def test_timestep_matches_oracle(name):
+    """timestep (module_solver.f90:202-408): the convective criterion dt_4(1)
+    and dtmin of the GPU reduction equal the oracle's (a max over points of
+    the same products, so the same value)."""
+    cfg, thd, adi, dxi, st, info, orc = W.case(name, 12)
+    g = gpu_from(cfg, thd, adi, dxi, st)
+    dt4_g, dt_g = g.timestep()
+    dt4_o, dt_o = orc.timestep(st)
+    g.close()
+    assert dt_g == dt_o and dt4_g[0] == dt4_o[0], (dt_g, dt_o)
+
+
+def test_negative_pressure_is_reported_not_computed():
+    """A state with P <= 0 in one interior cell makes euler_LLF abort in the
+    reference (module_weno.f90:1027-1036); the GPU flux returns
+    IZEM_ERR_NEG_PRESSURE, as the oracle does, and the context stays usable."""
+    from phd_gb300.izem import IzemError
+    cfg, thd, adi, dxi, st, info, orc = W.case("tgv", 12)
+    bad = W.copy(st)
+    bad["T"][8, 8, 8] = -bad["T"][8, 8, 8]
+    g = gpu_from(cfg, thd, adi, dxi, bad)
+    with pytest.raises(IzemError) as e:
+        g.euler_LLF_x()
+    assert e.value.code == 3
+    import oracle
+    with pytest.raises(oracle.OracleError):
+        orc.euler_flux(bad, 0, np.zeros((12, 12, 12, cfg.nrv + 5), order="F"))
+    g.upload(**st)
+    g.zero_flux()
+    g.euler_LLF_x()
+    fl = g.flux()
+    g.close()
+    assert np.all(np.isfinite(fl))
