@@ -2,7 +2,7 @@
 //
 // This file restates, in C++17 and loop by loop, the Fortran routines of the
 // reference solver (saras13015/Phd, devel-izem/src) that the GPU library
-// replaces.  It is the checker for the CUDA path: only tests, the smoke check
+// replaces.  It is the oracle for the CUDA path: only tests, the smoke check
 // and the CPU-baseline leg of the benchmark may load it; the product never
 // links or calls it.  The reference cannot be compiled here (no Fortran
 // compiler, MPI or HDF5), so this restatement is the oracle.  Each function

@@ -10,7 +10,8 @@ import workloads as W
 from phd_gb300 import thd as T
 from phd_gb300.capi import IzemCfg, IzemThd, IzemAdi
 
-REF = "/root/reference/devel-izem/testcases"
+# the reference tree, where it is mounted (IZEM_REFERENCE_TESTCASES overrides)
+REF = os.environ.get("IZEM_REFERENCE_TESTCASES", "/root/reference/devel-izem/testcases")
 
 
 @pytest.mark.skipif(not os.path.isdir(REF), reason="reference tree not mounted")
