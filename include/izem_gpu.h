@@ -51,8 +51,8 @@ enum {
  * RHS reads (module_parameters.f90:35-56, module_input.f90:266-400,622-770). */
 typedef struct izem_cfg {
   int    nx, ny, nz;        /* interior points of this block: ex-sx+1, ...      */
-  int    ng;                /* ghost depth = (order_weno+1)/2; 3 = WENO5        */
-  int    ndim;              /* must be 3                                        */
+  int    ng;                /* ghost depth = (order_weno+1)/2: 3 WENO5, 4 WENO7 */
+  int    ndim;              /* 3, or 2 with nz = 1                              */
   int    nrv;               /* reactive species, 2..IZEM_NSMAX                  */
   int    bc[6];             /* IZEM_BC_* per face W,E,S,N,B,F                   */
   int    weno_avg;          /* [WENO] WEIGHTS: nonlinear weights where sensed   */
@@ -142,6 +142,9 @@ typedef struct izem_ctx izem_ctx;
 
 /* Create a context on the current CUDA device.  Allocates the device-resident
  * state (v, T, W_i, cp, ha, shock sensor) and the RK3 scratch (v0, f).
+ * Supported: ng = 3 (WENO5) in 3-D or 2-D, ng = 4 (WENO7) for two-species
+ * sets; ndim = 2 needs nz = 1 (no z sweep, no z derivatives); EGLIB
+ * transport in 3-D with ng = 3.  Other configurations return IZEM_ERR_ARG.
  * Replaces the allocations at module_solver.f90:736-739 and the per-call
  * temporaries of module_weno.f90:588-607, module_viscflux.f90:1708-1714. */
 int  izem_gpu_init(const izem_cfg* cfg, const izem_thd* thd, const izem_adi* adi,

@@ -17,6 +17,7 @@ struct Geo {
   long long nint;  // interior points
   int bnd[6];      // face is a physical (non-periodic) boundary
   int bc[6];
+  int ndim;        // 3, or 2 (nz = 1: no z sweep, no z derivatives)
 };
 
 __host__ __device__ inline long long gid(const Geo& g, int i, int j, int k) {

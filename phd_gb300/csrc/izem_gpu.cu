@@ -149,11 +149,23 @@ int enq_euler(izem_ctx* c, int d) {
   long long nf = (long long)(g.n[0] + (d == 0)) * (g.n[1] + (d == 1)) * (g.n[2] + (d == 2));
   int rc;
   const char* names[3] = {"euler_face_x", "euler_face_y", "euler_face_z"};
+#define IZEM_FACE(DD, NGV)                                                                                         \
+  k_euler_face<NRV, DD, NGV><<<grid_for(nf, c->tb_euler), c->tb_euler, 0, c->stream>>>(                                \
+      g, c->cfg.weno_avg, c->cfg.weno5_linear_fix, c->v, c->prim, c->sensor, c->fhat, nf)
   rc = launch(c, names[d], [&] {
-    if (d == 0) k_euler_face<NRV, 0><<<grid_for(nf, c->tb_euler), c->tb_euler, 0, c->stream>>>(g, c->cfg.weno_avg, c->cfg.weno5_linear_fix, c->v, c->prim, c->sensor, c->fhat, nf);
-    if (d == 1) k_euler_face<NRV, 1><<<grid_for(nf, c->tb_euler), c->tb_euler, 0, c->stream>>>(g, c->cfg.weno_avg, c->cfg.weno5_linear_fix, c->v, c->prim, c->sensor, c->fhat, nf);
-    if (d == 2) k_euler_face<NRV, 2><<<grid_for(nf, c->tb_euler), c->tb_euler, 0, c->stream>>>(g, c->cfg.weno_avg, c->cfg.weno5_linear_fix, c->v, c->prim, c->sensor, c->fhat, nf);
+    if (g.ng == 4) {   // WENO7, two-species sets only (checked at init)
+      if constexpr (NRV == 2) {
+        if (d == 0) IZEM_FACE(0, 4);
+        if (d == 1) IZEM_FACE(1, 4);
+        if (d == 2) IZEM_FACE(2, 4);
+      }
+    } else {
+      if (d == 0) IZEM_FACE(0, 3);
+      if (d == 1) IZEM_FACE(1, 3);
+      if (d == 2) IZEM_FACE(2, 3);
+    }
   });
+#undef IZEM_FACE
   if (rc) return rc;
   return launch(c, "flux_diff", [&] {
     if (d == 0) k_flux_diff<0><<<grid_for(g.nint), kThreads, 0, c->stream>>>(g, NV, c->fhat, nf, c->dxi[0], c->f, 0);
@@ -209,7 +221,7 @@ int enq_stage(izem_ctx* c, int stage) {
   if ((rc = launch(c, "sensor", [&] { k_sensor<<<grid_for(g.nint), kThreads, 0, c->stream>>>(g, c->cfg.max_rel_weight, c->v, c->T, c->W_i, c->sensor); })))
     return rc;
   if ((rc = enq_prim<NRV>(c))) return rc;
-  for (int d = 0; d < 3; ++d)
+  for (int d = 0; d < c->cfg.ndim; ++d)   // euler_LLF_z only in 3-D (module_solver.f90:769-774)
     if ((rc = enq_euler<NRV>(c, d))) return rc;
   if (c->cfg.vis)
     if ((rc = enq_visc<NRV>(c))) return rc;
@@ -343,7 +355,7 @@ int tune_flow(izem_ctx* c, std::string* rep) {
   int best = 1;
   for (int q = 0; q < 3; ++q) {
     c->tb_euler = kTuneCand[q];
-    ms[q] = tune_time(c, 2, [&] { for (int d = 0; d < 3; ++d) (void)enq_euler<NRV>(c, d); });
+    ms[q] = tune_time(c, 2, [&] { for (int d = 0; d < c->cfg.ndim; ++d) (void)enq_euler<NRV>(c, d); });
     if (ms[q] < ms[best]) best = q;
   }
   c->tb_euler = kTuneCand[best];
@@ -369,8 +381,13 @@ extern "C" {
 int izem_gpu_init(const izem_cfg* cfg, const izem_thd* thd, const izem_adi* adi, izem_ctx** out) {
   if (!cfg || !thd || !adi || !out) return IZEM_ERR_ARG;
   *out = nullptr;
-  if (cfg->ng != 3 || cfg->ndim != 3 || !(cfg->nrv == 2 || cfg->nrv == 9) || thd->nspc != cfg->nrv) return IZEM_ERR_ARG;
-  if (cfg->nx < 7 || cfg->ny < 7 || cfg->nz < 7) return IZEM_ERR_ARG;
+  // WENO5 (ng = 3) in 2-D or 3-D; WENO7 (ng = 4) for two-species sets;
+  // 2-D runs have nz = 1; EGLIB transport in 3-D WENO5 only
+  const bool ng_ok = cfg->ng == 3 || (cfg->ng == 4 && cfg->nrv == 2 && !cfg->eglib);
+  const bool dim_ok = cfg->ndim == 3 || (cfg->ndim == 2 && cfg->nz == 1 && !cfg->eglib);
+  if (!ng_ok || !dim_ok || !(cfg->nrv == 2 || cfg->nrv == 9) || thd->nspc != cfg->nrv) return IZEM_ERR_ARG;
+  const int nmin = 2 * cfg->ng + 1;
+  if (cfg->nx < nmin || cfg->ny < nmin || (cfg->ndim == 3 && cfg->nz < nmin)) return IZEM_ERR_ARG;
   for (int f = 0; f < 6; ++f)
     if (cfg->bc[f] != IZEM_BC_PERIODIC && cfg->bc[f] != IZEM_BC_EXTRAPOLATION) return IZEM_ERR_ARG;
   for (int d = 0; d < 3; ++d)
@@ -380,7 +397,7 @@ int izem_gpu_init(const izem_cfg* cfg, const izem_thd* thd, const izem_adi* adi,
   c->thd = *thd;
   c->adi = *adi;
   Geo& g = c->g;
-  g.n[0] = cfg->nx; g.n[1] = cfg->ny; g.n[2] = cfg->nz; g.ng = cfg->ng;
+  g.n[0] = cfg->nx; g.n[1] = cfg->ny; g.n[2] = cfg->nz; g.ng = cfg->ng; g.ndim = cfg->ndim;
   for (int d = 0; d < 3; ++d) g.g[d] = g.n[d] + 2 * g.ng;
   g.ncell = (long long)g.g[0] * g.g[1] * g.g[2];
   g.nint = (long long)g.n[0] * g.n[1] * g.n[2];
@@ -559,7 +576,7 @@ int izem_gpu_shock_sensor(izem_ctx* c) {
 }
 
 int izem_gpu_euler_flux(izem_ctx* c, int dir) {
-  if (!c || dir < 0 || dir > 2) return IZEM_ERR_ARG;
+  if (!c || dir < 0 || dir >= c->cfg.ndim) return IZEM_ERR_ARG;
   if (!c->grid_set) return ctx_fail(c, IZEM_ERR_STATE, "grid not set", cudaSuccess);
   int rc = IZEM_DISPATCH(c, do_euler, c, dir);
   if (rc) return rc;
@@ -1008,8 +1025,7 @@ int izem_abi_sizes(size_t* a, size_t* b, size_t* d) {
 }
 
 int izem_metrics_dscalar(int n, int ng, const double* coord, double* d_i) {
-  (void)ng;
-  if (n < 7 || !coord || !d_i) return IZEM_ERR_ARG;
+  if ((ng != 3 && ng != 4) || n < 2 * ng + 1 || !coord || !d_i) return IZEM_ERR_ARG;
   std::vector<double> dv(n, 1.0);
   const double a6[7] = {-1.0 / 60.0, 9.0 / 60.0, -45.0 / 60.0, 0.0, 45.0 / 60.0, -9.0 / 60.0, 1.0 / 60.0};
   const double a4[5] = {1.0 / 12.0, -8.0 / 12.0, 0.0, 8.0 / 12.0, -1.0 / 12.0};
@@ -1018,11 +1034,23 @@ int izem_metrics_dscalar(int n, int ng, const double* coord, double* d_i) {
   const double a4ur[5] = {1.0 / 12.0, -6.0 / 12.0, 18.0 / 12.0, -10.0 / 12.0, -3.0 / 12.0};
   const double a4or[5] = {-3.0 / 12.0, 16.0 / 12.0, -36.0 / 12.0, 48.0 / 12.0, -25.0 / 12.0};
   auto x = [&](int m) { return coord[m - 1]; };
-  for (int m = 4; m <= n - 3; ++m) {
+  // central rows: 6th order (ng = 3), or 8th order with 6th-order fourth rows (ng = 4)
+  const double a8[9] = {3.0 / 840.0, -32.0 / 840.0, 168.0 / 840.0, -672.0 / 840.0, 0.0,
+                        672.0 / 840.0, -168.0 / 840.0, 32.0 / 840.0, -3.0 / 840.0};
+  for (int m = 1 + ng; m <= n - ng; ++m) {
     double dd = 0.0;
-    for (int l = -3; l <= 3; ++l) dd = dd + a6[l + 3] * x(m + l);
+    if (ng == 4)
+      for (int l = -4; l <= 4; ++l) dd = dd + a8[l + 4] * x(m + l);
+    else
+      for (int l = -3; l <= 3; ++l) dd = dd + a6[l + 3] * x(m + l);
     dv[m - 1] = dd * 1.0;
   }
+  if (ng == 4)
+    for (int m : {4, n - 3}) {
+      double dd = 0.0;
+      for (int l = -3; l <= 3; ++l) dd = dd + a6[l + 3] * x(m + l);
+      dv[m - 1] = dd * 1.0;
+    }
   { double dd = 0.0; for (int l = 0; l <= 4; ++l) dd = dd + a4ol[l] * x(1 + l); dv[0] = dd * 1.0; }
   { double dd = 0.0; for (int l = -1; l <= 3; ++l) dd = dd + a4ul[l + 1] * x(2 + l); dv[1] = dd * 1.0; }
   { double dd = 0.0; for (int l = -2; l <= 2; ++l) dd = dd + a4[l + 2] * x(3 + l); dv[2] = dd * 1.0; }

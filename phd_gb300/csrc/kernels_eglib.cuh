@@ -427,7 +427,7 @@ __global__ void k_grad_p(Geo g, Metrics mt, const double* __restrict__ prim, dou
   for (int d = 0; d < 3; ++d) {
     const double di = mt.dxi[d][c[d] - 1 + g.ng];
     fd[(12 + 3 * NRV + d) * nc + p] =
-        deriv_at(prim + PR_P * nc, p, strides[d], c[d], g.n[d], g.bnd[2 * d], g.bnd[2 * d + 1], di);
+        deriv_at(prim + PR_P * nc, p, strides[d], c[d], g.n[d], g.bnd[2 * d], g.bnd[2 * d + 1], di, g.ng);
   }
 }
 

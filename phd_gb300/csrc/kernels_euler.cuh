@@ -133,14 +133,79 @@ __device__ __forceinline__ double weno5_nl(const double* vp, const double* vm) {
   return vminus + vplus;
 }
 
+// Nonlinear WENO7 reconstruction (wenorec, ng = 4, module_weno.f90:286-527):
+// vp/vm hold the 2ng = 8 stencil values (index 0 = point il-3).
+__device__ __forceinline__ double weno7_nl(const double* vp, const double* vm) {
+  const double eps = 1.0e-10;
+  const double za = 547.0, zb = -1854.0, zc = 4642.0, zd = -3882.0, ze = -17246.0, zf = 2107.0, zg = 7043.0,
+               zh = -9402.0, zi = 11003.0, zl = 7042.0, zm = 3443.0, zn = -5966.0, zo = -2522.0, zp = 1602.0,
+               zq = 2843.0, zr = 267.0, zs = 1922.0, zt = -494.0, zu = -1642.0;
+  // cweno(r, j), r = -1..3
+  const double cw[5][4] = {{25.0 / 12.0, -23.0 / 12.0, 13.0 / 12.0, -1.0 / 4.0},
+                           {1.0 / 4.0, 13.0 / 12.0, -5.0 / 12.0, 1.0 / 12.0},
+                           {-1.0 / 12.0, 7.0 / 12.0, 7.0 / 12.0, -1.0 / 12.0},
+                           {1.0 / 12.0, -5.0 / 12.0, 13.0 / 12.0, 1.0 / 4.0},
+                           {-1.0 / 4.0, 13.0 / 12.0, -23.0 / 12.0, 25.0 / 12.0}};
+  const double dw[4] = {4.0 / 35.0, 18.0 / 35.0, 12.0 / 35.0, 1.0 / 35.0};
+  auto betas = [&](const double* q, int i, double* be) {   // q 0-based, centre i
+    be[0] = q[i] * (zf * q[i] + zh * q[i + 1] + zl * q[i + 2] + zb * q[i + 3]) +
+            q[i + 1] * (zi * q[i + 1] + ze * q[i + 2] + zc * q[i + 3]) + q[i + 2] * (zg * q[i + 2] + zd * q[i + 3]) +
+            q[i + 3] * (za * q[i + 3]);
+    be[1] = q[i - 1] * (za * q[i - 1] + zo * q[i] + zs * q[i + 1] + zt * q[i + 2]) +
+            q[i] * (zm * q[i] + zn * q[i + 1] + zp * q[i + 2]) + q[i + 1] * (zq * q[i + 1] + zu * q[i + 2]) +
+            q[i + 2] * (zr * q[i + 2]);
+    be[2] = q[i - 2] * (zr * q[i - 2] + zu * q[i - 1] + zp * q[i] + zt * q[i + 1]) +
+            q[i - 1] * (zq * q[i - 1] + zn * q[i] + zs * q[i + 1]) + q[i] * (zm * q[i] + zo * q[i + 1]) +
+            q[i + 1] * (za * q[i + 1]);
+    be[3] = q[i - 3] * (za * q[i - 3] + zd * q[i - 2] + zc * q[i - 1] + zb * q[i]) +
+            q[i - 2] * (zg * q[i - 2] + ze * q[i - 1] + zl * q[i]) + q[i - 1] * (zi * q[i - 1] + zh * q[i]) +
+            q[i] * (zf * q[i]);
+  };
+  double be[4], al[4], s, vminus = 0.0, vplus = 0.0;
+  // '-' state at i+1/2: centre vp[3], cweno(r, j) on vp[3 - r + j]
+  betas(vp, 3, be);
+  s = 0.0;
+#pragma unroll
+  for (int r = 0; r < 4; ++r) { al[r] = dw[r] / ((eps + be[r]) * (eps + be[r])); s = s + al[r]; }
+  s = 1.0 / s;
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    double q = 0.0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) q = q + cw[r + 1][j] * vp[3 - r + j];
+    vminus = vminus + (al[r] * s) * q;
+  }
+  // '+' state at i+1/2: centre vm[4], cweno(r-1, j) on vm[4 - r + j], weights reversed
+  betas(vm, 4, be);
+  s = 0.0;
+#pragma unroll
+  for (int r = 0; r < 4; ++r) { al[r] = dw[3 - r] / ((eps + be[r]) * (eps + be[r])); s = s + al[r]; }
+  s = 1.0 / s;
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    double q = 0.0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) q = q + cw[r][j] * vm[4 - r + j];
+    vplus = vplus + (al[r] * s) * q;
+  }
+  return vminus + vplus;
+}
+
+template <int NG>
+__device__ __forceinline__ double weno_nl(const double* vp, const double* vm) {
+  if constexpr (NG == 4) return weno7_nl(vp, vm);
+  else return weno5_nl(vp, vm);
+}
+
 // K2: one thread per cell face along axis D.  Characteristic projections use
 // the structure of the left eigenvectors (module_weno.f90:775-874): the three
 // acoustic/entropy rows are dense over (rho, m, rho e_t) plus a rank-one
 // species term psi.w; the shear rows have two entries; the species rows are
 // Y_s (a.w) + w_s.  The result equals the reference's dense nv x nv product
 // up to rounding.  Linear (sensor-off) faces accumulate the WENO5 stencil
-// while streaming over the 6 stencil points; sensed faces keep the 6 values.
-template <int NRV, int D>
+// while streaming over the 2NG stencil points; sensed faces keep the 2NG
+// values.  NG = 3 is WENO5, NG = 4 WENO7 (module_weno.f90, ng branches).
+template <int NRV, int D, int NG>
 __global__ void __launch_bounds__(256) k_euler_face(Geo g, int weno_avg, int linfix,
                                                     const double* __restrict__ v,
                                                     const double* __restrict__ prim,
@@ -168,7 +233,7 @@ __global__ void __launch_bounds__(256) k_euler_face(Geo g, int weno_avg, int lin
   const long long stride = D == 0 ? 1LL : (D == 1 ? (long long)g.g[0] : (long long)g.g[0] * g.g[1]);
   const long long pl = gid(g, c[0], c[1], c[2]);   // cell il
   const long long pr = pl + stride;                  // cell il+1
-  const long long p0 = pl - 2 * stride;              // stencil point il-2
+  const long long p0 = pl - (NG - 1) * stride;       // stencil point il-ng+1
 
   // ---- Roe average compatible with the EOS (module_weno.f90:726-761)
   const double rho_i_l = prim[PR_RHOI * nc + pl], rho_i_r = prim[PR_RHOI * nc + pr];
@@ -217,7 +282,7 @@ __global__ void __launch_bounds__(256) k_euler_face(Geo g, int weno_avg, int lin
   double lm0 = -1.0, lm1 = -1.0, lm2 = -1.0;
   bool shk = false;
 #pragma unroll
-  for (int st = 0; st < 6; ++st) {
+  for (int st = 0; st < 2 * NG; ++st) {
     const long long ps = p0 + st * stride;
     const double u_s = prim[(PR_U + D) * nc + ps], c_s = prim[PR_CS * nc + ps];
     lm0 = fmax(fabs(u_s - c_s), lm0);
@@ -229,17 +294,21 @@ __global__ void __launch_bounds__(256) k_euler_face(Geo g, int weno_avg, int lin
 
   double gh[NV];
   if (!shk) {
-    // linear WENO5 (wenorec_nw): accumulate while streaming over the stencil
+    // linear reconstruction (wenorec_nw): accumulate while streaming over the stencil
     double am[NV], ap[NV];
 #pragma unroll
     for (int m = 0; m < NV; ++m) { am[m] = 0.0; ap[m] = 0.0; }
-    // reference (mirrored) coefficients on points 0..4 ('-') and 1..5 ('+')
-    const double cmr[6] = {-3.0, 27.0, 47.0, -13.0, 2.0, 0.0};
-    const double cpr[6] = {0.0, 2.0, -13.0, 47.0, 27.0, -3.0};
-    const double cmf[6] = {2.0, -13.0, 47.0, 27.0, -3.0, 0.0};
-    const double cpf[6] = {0.0, -3.0, 27.0, 47.0, -13.0, 2.0};
+    // WENO5: the reference's (mirrored) coefficients on points 0..4 ('-') and
+    // 1..5 ('+'), or the textbook ones (linfix); WENO7: the 7th-order
+    // stencil on points 0..6 and 1..7
+    const double cmr[8] = {-3.0, 27.0, 47.0, -13.0, 2.0, 0.0, 0.0, 0.0};
+    const double cpr[8] = {0.0, 2.0, -13.0, 47.0, 27.0, -3.0, 0.0, 0.0};
+    const double cmf[8] = {2.0, -13.0, 47.0, 27.0, -3.0, 0.0, 0.0, 0.0};
+    const double cpf[8] = {0.0, -3.0, 27.0, 47.0, -13.0, 2.0, 0.0, 0.0};
+    const double cm7[8] = {-3.0, 25.0, -101.0, 319.0, 214.0, -38.0, 4.0, 0.0};
+    const double cp7[8] = {0.0, 4.0, -38.0, 214.0, 319.0, -101.0, 25.0, -3.0};
 #pragma unroll
-    for (int st = 0; st < 6; ++st) {
+    for (int st = 0; st < 2 * NG; ++st) {
       const long long ps = p0 + st * stride;
       double w[NV], f[NV];
 #pragma unroll
@@ -251,8 +320,8 @@ __global__ void __launch_bounds__(256) k_euler_face(Geo g, int weno_avg, int lin
       f[4] = u_s * (w[4] + P_s);
 #pragma unroll
       for (int l = IZEM_NIV; l < NV; ++l) f[l] = w[l] * u_s;
-      const double ccm = linfix ? cmf[st] : cmr[st];
-      const double ccp = linfix ? cpf[st] : cpr[st];
+      const double ccm = NG == 4 ? cm7[st] : (linfix ? cmf[st] : cmr[st]);
+      const double ccp = NG == 4 ? cp7[st] : (linfix ? cpf[st] : cpr[st]);
       // project w and f
       double sw = 0.0, sf = 0.0;
 #pragma unroll
@@ -287,12 +356,15 @@ __global__ void __launch_bounds__(256) k_euler_face(Geo g, int weno_avg, int lin
       }
     }
 #pragma unroll
-    for (int m = 0; m < NV; ++m) gh[m] = am[m] * (1.0 / 60.0) + ap[m] * (1.0 / 60.0);
+    for (int m = 0; m < NV; ++m) {
+      constexpr double den = NG == 4 ? 1.0 / 420.0 : 1.0 / 60.0;
+      gh[m] = am[m] * den + ap[m] * den;
+    }
   } else {
-    // nonlinear WENO5 (wenorec): keep the 6 stencil values of every field
-    double gpl[NV][6], gmi[NV][6];
+    // nonlinear reconstruction (wenorec): keep the 2NG stencil values of every field
+    double gpl[NV][2 * NG], gmi[NV][2 * NG];
 #pragma unroll 1
-    for (int st = 0; st < 6; ++st) {
+    for (int st = 0; st < 2 * NG; ++st) {
       const long long ps = p0 + st * stride;
       double w[NV], f[NV];
 #pragma unroll
@@ -336,7 +408,7 @@ __global__ void __launch_bounds__(256) k_euler_face(Geo g, int weno_avg, int lin
       }
     }
 #pragma unroll 1
-    for (int m = 0; m < NV; ++m) gh[m] = weno5_nl(gpl[m], gmi[m]);
+    for (int m = 0; m < NV; ++m) gh[m] = weno_nl<NG>(gpl[m], gmi[m]);
   }
 
   // ---- fhat = R ghat (module_weno.f90:881-989)

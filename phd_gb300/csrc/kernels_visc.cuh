@@ -7,9 +7,11 @@
 #include "common.cuh"
 #include "kernels_euler.cuh"
 
-// module_deriv.f90:25-66 (ng = 3)
+// module_deriv.f90:25-66 and dx (:212-478): 4th-order rows next to a
+// physical boundary; then, with ng = 4, one 6th-order row and the 8th-order
+// central stencil, with ng = 3 the 6th-order central stencil.
 __device__ __forceinline__ double deriv_at(const double* __restrict__ a, long long p, long long stride, int s, int n,
-                                           int lo_b, int hi_b, double di) {
+                                           int lo_b, int hi_b, double di, int ng) {
   if (lo_b && s <= 3) {
     if (s == 1) {
       double dd = (-25.0 / 12.0) * a[p] + (48.0 / 12.0) * a[p + stride] + (-36.0 / 12.0) * a[p + 2 * stride] +
@@ -40,6 +42,12 @@ __device__ __forceinline__ double deriv_at(const double* __restrict__ a, long lo
       return -dd * di;
     }
   }
+  if (ng == 4 && !((lo_b && s == 4) || (hi_b && s == n - 3))) {
+    double dd = (3.0 / 840.0) * a[p - 4 * stride] + (-32.0 / 840.0) * a[p - 3 * stride] +
+                (168.0 / 840.0) * a[p - 2 * stride] + (-672.0 / 840.0) * a[p - stride] + (672.0 / 840.0) * a[p + stride] +
+                (-168.0 / 840.0) * a[p + 2 * stride] + (32.0 / 840.0) * a[p + 3 * stride] + (-3.0 / 840.0) * a[p + 4 * stride];
+    return dd * di;
+  }
   double dd = (-1.0 / 60.0) * a[p - 3 * stride] + (9.0 / 60.0) * a[p - 2 * stride] + (-45.0 / 60.0) * a[p - stride] +
               (45.0 / 60.0) * a[p + stride] + (-9.0 / 60.0) * a[p + 2 * stride] + (1.0 / 60.0) * a[p + 3 * stride];
   return dd * di;
@@ -69,11 +77,13 @@ __global__ void k_grad(Geo g, Metrics mt, const double* __restrict__ prim, const
   for (int d = 0; d < 3; ++d) {
     const double di = mt.dxi[d][c[d] - 1 + g.ng];
     const int lo = g.bnd[2 * d], hi = g.bnd[2 * d + 1];
+    const bool none = d == 2 && g.ndim == 2;   // a 2-D run has no z derivative
 #pragma unroll
-    for (int s = 0; s < 4; ++s) fd[(3 * s + d) * nc + p] = deriv_at(src[s], p, strides[d], c[d], g.n[d], lo, hi, di);
+    for (int s = 0; s < 4; ++s)
+      fd[(3 * s + d) * nc + p] = none ? 0.0 : deriv_at(src[s], p, strides[d], c[d], g.n[d], lo, hi, di, g.ng);
 #pragma unroll
     for (int l = 0; l < NRV; ++l)
-      fd[(12 + 3 * l + d) * nc + p] = deriv_at(Xa + l * nc, p, strides[d], c[d], g.n[d], lo, hi, di);
+      fd[(12 + 3 * l + d) * nc + p] = none ? 0.0 : deriv_at(Xa + l * nc, p, strides[d], c[d], g.n[d], lo, hi, di, g.ng);
   }
 }
 
@@ -231,9 +241,9 @@ __global__ void k_visc_div(Geo g, Metrics mt, const double* __restrict__ tau, co
     hi[d] = g.bnd[2 * d + 1];
   }
   auto div3 = [&](const double* ax, const double* ay, const double* az) {
-    const double wx = deriv_at(ax, p, st[0], c[0], g.n[0], lo[0], hi[0], di[0]);
-    const double wy = deriv_at(ay, p, st[1], c[1], g.n[1], lo[1], hi[1], di[1]);
-    const double wz = deriv_at(az, p, st[2], c[2], g.n[2], lo[2], hi[2], di[2]);
+    const double wx = deriv_at(ax, p, st[0], c[0], g.n[0], lo[0], hi[0], di[0], g.ng);
+    const double wy = deriv_at(ay, p, st[1], c[1], g.n[1], lo[1], hi[1], di[1], g.ng);
+    const double wz = g.ndim == 2 ? 0.0 : deriv_at(az, p, st[2], c[2], g.n[2], lo[2], hi[2], di[2], g.ng);
     return wx + wy + wz;
   };
   const long long ni = g.nint;

@@ -34,9 +34,11 @@ def golden(n):
     return np.load(os.path.join(HERE, "golden", "sod_restart_%05d.npz" % n))
 
 
-def sod_case():
-    """Configuration, species data, references, metrics and the ghosted
-    initial state (closed by finalize_ic) of the reference's Sod run."""
+def sod_case(xblocks=NX_BLOCKS):
+    """Configuration, species data, references, oracle, the ghosted initial
+    state (closed by finalize_ic) and the metrics (dx_i, dy_i, dz_i) of the
+    reference's Sod run.  xblocks: the MPI x-blocks whose effect on the
+    shock sensor the oracle emulates (1 for a single block)."""
     a = constants()
     sp = load_species("o2n2")
     thd = thd_init(sp, a)
@@ -57,7 +59,7 @@ def sod_case():
     dz = np.full(nz + 2 * NG, 1.0) * L      # no z metric in 2-D: dz_i = 1 * L_ref
     grid = (dxi(xm), dxi(ym), dz)
     orc = oracle.Oracle(cfg, thd, adi_struct(a), *grid)
-    orc.set_sensor_xblocks(NX_BLOCKS)
+    orc.set_sensor_xblocks(xblocks)
 
     # ini_sod: mole fractions 0.233 / 0.767 turned into mass fractions by
     # X_to_Y (module_thermodynamics.f90:45-68); (P, rho) = (1, 1) left of
@@ -100,7 +102,7 @@ def sod_case():
     st = {"v": v, "T": T, "W_i": np.zeros(shp, order="F"), "cp": np.zeros(shp, order="F"),
           "ha": np.zeros(shp + (nrv,), order="F"), "shock_sensor": np.zeros(shp, dtype=np.uint8, order="F")}
     orc.finalize_ic(st)
-    return cfg, thd, a, orc, st
+    return cfg, thd, a, orc, st, grid
 
 
 def stat_times(a, n):

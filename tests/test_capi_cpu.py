@@ -46,7 +46,8 @@ def test_struct_layout_matches_header():
     assert [x.value for x in s] == [C.sizeof(IzemCfg), C.sizeof(IzemThd), C.sizeof(IzemAdi)]
 
 
-def test_host_metrics_match_oracle():
+@pytest.mark.parametrize("ng", [3, 4])
+def test_host_metrics_match_oracle(ng):
     import numpy as np
     import oracle
     from phd_gb300.izem import metrics_dscalar
@@ -54,7 +55,7 @@ def test_host_metrics_match_oracle():
     build_gpu()
     rng = np.random.Generator(np.random.PCG64(1))
     x = np.cumsum(0.5 + rng.random(40))
-    assert np.array_equal(metrics_dscalar(x), oracle.metrics_dscalar(x))
+    assert np.array_equal(metrics_dscalar(x, ng), oracle.metrics_dscalar(x, ng))
 
 
 def test_entry_points_reject_bad_arguments_before_any_device_call():
@@ -69,7 +70,7 @@ def test_entry_points_reject_bad_arguments_before_any_device_call():
     lib = load_library()
     cfg, thd, adi, dxi, st, info = ics.tgv(8, lib_dscalar=oracle.metrics_dscalar)
     h = C.c_void_p()
-    for field, bad in (("ng", 4), ("ndim", 2), ("nrv", 3)):
+    for field, bad in (("ng", 5), ("ndim", 2), ("nrv", 3)):
         good = getattr(cfg, field)
         setattr(cfg, field, bad)
         assert lib.izem_gpu_init(C.byref(cfg), C.byref(thd), C.byref(adi), C.byref(h)) == 1, field

@@ -1,0 +1,72 @@
+"""The GPU path on the reference's own Sod configuration (2-D, WENO7,
+fitted viscous fluxes, extrapolation and periodic boundaries; the case of
+tests/sod_case.py) against the oracle on one block.  The oracle with the
+reference's two-block sensor reproduces the reference's restart files
+(tests/test_sod_pin.py); here the GPU's WENO7 fluxes, 2-D viscous terms,
+Newton, boundaries, time step and RK3 must agree with the oracle to 1e-12
+relative per conserved variable, as the WENO5 3-D path does
+(tests/test_gpu_parity.py)."""
+import numpy as np
+import pytest
+
+import sod_case as S
+import workloads as W
+from phd_gb300.izem import IzemGPU
+from phd_gb300.thd import adi_struct
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-12
+
+
+def _gpu(cfg, thd, a, grid, st):
+    g = IzemGPU(cfg, thd, adi_struct(a))
+    g.set_grid(*grid)
+    g.upload(**st)
+    return g
+
+
+def _interior(x):
+    ng = S.NG
+    return x[ng:-ng, ng:-ng, ng:-ng]
+
+
+def test_sod_fluxes_match_oracle():
+    """x and y WENO7 fluxes (with the sensor set by one sensor pass, so both
+    the nonlinear and the linear reconstructions occur) and the 2-D viscous
+    fluxes at the initial discontinuity."""
+    cfg, thd, a, orc, st, grid = S.sod_case(xblocks=1)
+    g = _gpu(cfg, thd, a, grid, st)
+    orc.shock_sensor(st)
+    g.shock_sensor()
+    got_s = g.download()["shock_sensor"]
+    assert np.array_equal(_interior(got_s), _interior(st["shock_sensor"]))
+    assert _interior(st["shock_sensor"]).any()
+    nv = 5 + cfg.nrv
+    fl = np.zeros((cfg.nx, cfg.ny, cfg.nz, nv), order="F")
+    orc.euler_flux(st, 0, fl)
+    orc.euler_flux(st, 1, fl)
+    orc.visc_flux(st, fl)
+    g.zero_flux()
+    g.euler_LLF_x()
+    g.euler_LLF_y()
+    g.viscflux_xyz()
+    err = W.normwise(g.flux(), fl)
+    g.close()
+    assert np.all(err <= TOL), err
+
+
+def test_sod_steps_match_oracle():
+    """Twenty full time steps (time step, RK3 with the sticky sensor,
+    primitives, extrapolation and periodic halos) from the initial state."""
+    cfg, thd, a, orc, st, grid = S.sod_case(xblocks=1)
+    g = _gpu(cfg, thd, a, grid, st)
+    for _ in range(20):
+        _, dt_o = orc.timestep(st)
+        _, dt_g = g.timestep()
+        assert abs(dt_g - dt_o) <= 1e-14 * dt_o
+        orc.rk3(st, dt_o)
+        g.rk3(dt_o)
+    got = g.download()
+    g.close()
+    err = W.normwise(_interior(got["v"]), _interior(st["v"]))
+    assert np.all(err <= TOL), err

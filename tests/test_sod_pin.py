@@ -28,7 +28,7 @@ NAMES = ["rho", "rhoU", "rhoV", "rhoW", "rhoE", "O2", "N2"]
 
 @pytest.fixture(scope="module")
 def sod_run():
-    cfg, thd, a, orc, st = S.sod_case()
+    cfg, thd, a, orc, st, _ = S.sod_case()
     return S.run_to_stats(orc, st, a, 3)
 
 
