@@ -318,6 +318,15 @@ int  izem_gpu_autotune(izem_ctx* ctx, double chem_dt, char* report, int report_l
  * the process, as izem_gpu_autotune would choose it (no counterpart in the
  * reference); IZEM_ERR_ARG outside 0..4. */
 int  izem_gpu_set_chem_variant(int variant);
+/* Reproduce a run of the reference decomposed into nblk equal MPI blocks
+ * along x (its NUMPROCX) on this single context: the reference never
+ * exchanges the shock sensor, so each block tests only its own points
+ * (module_tools.f90:2761-2770) and picks nonlinear weights from its own
+ * flags (module_weno.f90:973), and the face on a block edge is computed
+ * twice, once as each neighbouring block sees it.  nblk = 1 (the default)
+ * is one block.  No counterpart as an entry point in the reference;
+ * IZEM_ERR_ARG unless nblk divides nx into blocks of at least ng points. */
+int  izem_gpu_set_sensor_xblocks(izem_ctx* ctx, int nblk);
 /* The same choice for independent reactors (no counterpart in the
  * reference): times the five variants on the first min(n, 2^20) reactors of
  * a batch laid out as for izem_gpu_psr_batch (copies; the caller's arrays

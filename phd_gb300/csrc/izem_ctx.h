@@ -39,6 +39,11 @@ struct izem_ctx {
   bool have_eg = false;   // EGLIB linking data uploaded (izem_gpu_set_eglib)
   // threads per block chosen by izem_gpu_autotune (face fluxes, viscous point kernel)
   int tb_euler = 128, tb_visc = 128;
+  // sensor x-blocks (izem_gpu_set_sensor_xblocks): block size in x (nx for
+  // one block) and the block-edge faces as seen by the right block
+  int sensor_bx = 0;
+  double* fhat_edge = nullptr;
+  long long nedge = 0;
   // chemistry
   bool have_mech = false;
   izem_mech mech;

@@ -151,7 +151,7 @@ int enq_euler(izem_ctx* c, int d) {
   const char* names[3] = {"euler_face_x", "euler_face_y", "euler_face_z"};
 #define IZEM_FACE(DD, NGV)                                                                                         \
   k_euler_face<NRV, DD, NGV><<<grid_for(nf, c->tb_euler), c->tb_euler, 0, c->stream>>>(                                \
-      g, c->cfg.weno_avg, c->cfg.weno5_linear_fix, c->v, c->prim, c->sensor, c->fhat, nf)
+      g, c->cfg.weno_avg, c->cfg.weno5_linear_fix, c->v, c->prim, c->sensor, c->fhat, nf, c->sensor_bx, 0)
   rc = launch(c, names[d], [&] {
     if (g.ng == 4) {   // WENO7, two-species sets only (checked at init)
       if constexpr (NRV == 2) {
@@ -167,10 +167,25 @@ int enq_euler(izem_ctx* c, int d) {
   });
 #undef IZEM_FACE
   if (rc) return rc;
+  if (d == 0 && c->sensor_bx < g.n[0]) {   // block-edge faces as seen by the right block
+    rc = launch(c, "euler_face_edge", [&] {
+#define IZEM_EDGE(NGV)                                                                                            \
+  k_euler_face<NRV, 0, NGV><<<grid_for(c->nedge, c->tb_euler), c->tb_euler, 0, c->stream>>>(                      \
+      g, c->cfg.weno_avg, c->cfg.weno5_linear_fix, c->v, c->prim, c->sensor, c->fhat_edge, c->nedge, c->sensor_bx, 1)
+      if (g.ng == 4) {
+        if constexpr (NRV == 2) IZEM_EDGE(4);
+      } else {
+        IZEM_EDGE(3);
+      }
+#undef IZEM_EDGE
+    });
+  }
+  if (rc) return rc;
   return launch(c, "flux_diff", [&] {
-    if (d == 0) k_flux_diff<0><<<grid_for(g.nint), kThreads, 0, c->stream>>>(g, NV, c->fhat, nf, c->dxi[0], c->f, 0);
-    if (d == 1) k_flux_diff<1><<<grid_for(g.nint), kThreads, 0, c->stream>>>(g, NV, c->fhat, nf, c->dxi[1], c->f, 1);
-    if (d == 2) k_flux_diff<2><<<grid_for(g.nint), kThreads, 0, c->stream>>>(g, NV, c->fhat, nf, c->dxi[2], c->f, 1);
+    const int bx = c->sensor_bx;
+    if (d == 0) k_flux_diff<0><<<grid_for(g.nint), kThreads, 0, c->stream>>>(g, NV, c->fhat, nf, c->dxi[0], c->f, 0, bx, c->fhat_edge, c->nedge);
+    if (d == 1) k_flux_diff<1><<<grid_for(g.nint), kThreads, 0, c->stream>>>(g, NV, c->fhat, nf, c->dxi[1], c->f, 1, bx, c->fhat_edge, c->nedge);
+    if (d == 2) k_flux_diff<2><<<grid_for(g.nint), kThreads, 0, c->stream>>>(g, NV, c->fhat, nf, c->dxi[2], c->f, 1, bx, c->fhat_edge, c->nedge);
   });
 }
 
@@ -218,7 +233,7 @@ template <int NRV>
 int enq_stage(izem_ctx* c, int stage) {
   const Geo& g = c->g;
   int rc;
-  if ((rc = launch(c, "sensor", [&] { k_sensor<<<grid_for(g.nint), kThreads, 0, c->stream>>>(g, c->cfg.max_rel_weight, c->v, c->T, c->W_i, c->sensor); })))
+  if ((rc = launch(c, "sensor", [&] { k_sensor<<<grid_for(g.nint), kThreads, 0, c->stream>>>(g, c->cfg.max_rel_weight, c->v, c->T, c->W_i, c->sensor, c->sensor_bx); })))
     return rc;
   if ((rc = enq_prim<NRV>(c))) return rc;
   for (int d = 0; d < c->cfg.ndim; ++d)   // euler_LLF_z only in 3-D (module_solver.f90:769-774)
@@ -299,7 +314,7 @@ int do_timestep(izem_ctx* c) {
 template <int NRV>
 int do_sensor(izem_ctx* c) {
   const Geo& g = c->g;
-  return launch(c, "sensor", [&] { k_sensor<<<grid_for(g.nint), kThreads, 0, c->stream>>>(g, c->cfg.max_rel_weight, c->v, c->T, c->W_i, c->sensor); });
+  return launch(c, "sensor", [&] { k_sensor<<<grid_for(g.nint), kThreads, 0, c->stream>>>(g, c->cfg.max_rel_weight, c->v, c->T, c->W_i, c->sensor, c->sensor_bx); });
 }
 
 template <int NRV>
@@ -398,6 +413,7 @@ int izem_gpu_init(const izem_cfg* cfg, const izem_thd* thd, const izem_adi* adi,
   c->adi = *adi;
   Geo& g = c->g;
   g.n[0] = cfg->nx; g.n[1] = cfg->ny; g.n[2] = cfg->nz; g.ng = cfg->ng; g.ndim = cfg->ndim;
+  c->sensor_bx = cfg->nx;   // one block
   for (int d = 0; d < 3; ++d) g.g[d] = g.n[d] + 2 * g.ng;
   g.ncell = (long long)g.g[0] * g.g[1] * g.g[2];
   g.nint = (long long)g.n[0] * g.n[1] * g.n[2];
@@ -499,6 +515,7 @@ void izem_gpu_destroy(izem_ctx* c) {
   if (c->graph) cudaGraphDestroy(c->graph);
   for (double* p : c->allocs) cudaFree(p);
   if (c->sensor) cudaFree(c->sensor);
+  if (c->fhat_edge) cudaFree(c->fhat_edge);
   if (c->d_status) cudaFree(c->d_status);
   if (c->d_counter) cudaFree(c->d_counter);
   if (c->d_chem_stats) cudaFree(c->d_chem_stats);
@@ -902,6 +919,17 @@ int izem_gpu_autotune(izem_ctx* c, double chem_dt, char* report, int report_len)
   if (report && report_len > 0) std::snprintf(report, report_len, "%s", rep.c_str());
   if (rc == IZEM_OK) CK(cudaStreamSynchronize(c->stream));
   return rc;
+}
+
+int izem_gpu_set_sensor_xblocks(izem_ctx* c, int nblk) {
+  if (!c || nblk < 1 || c->cfg.nx % nblk != 0 || c->cfg.nx / nblk < c->cfg.ng) return IZEM_ERR_ARG;
+  if (c->graph_exec) { cudaGraphExecDestroy(c->graph_exec); c->graph_exec = nullptr; }
+  if (c->graph) { cudaGraphDestroy(c->graph); c->graph = nullptr; }
+  if (c->fhat_edge) { CK(cudaFree(c->fhat_edge)); c->fhat_edge = nullptr; }
+  c->sensor_bx = c->cfg.nx / nblk;
+  c->nedge = (long long)(nblk - 1) * c->cfg.ny * c->cfg.nz;
+  if (c->nedge > 0) CK(cudaMalloc(&c->fhat_edge, (size_t)c->nv * c->nedge * sizeof(double)));
+  return IZEM_OK;
 }
 
 int izem_gpu_set_chem_variant(int variant) { return chem_set_variant(variant) == 0 ? IZEM_OK : IZEM_ERR_ARG; }

@@ -205,19 +205,35 @@ __device__ __forceinline__ double weno_nl(const double* vp, const double* vm) {
 // up to rounding.  Linear (sensor-off) faces accumulate the WENO5 stencil
 // while streaming over the 2NG stencil points; sensed faces keep the 2NG
 // values.  NG = 3 is WENO5, NG = 4 WENO7 (module_weno.f90, ng branches).
+//
+// Sensor blocks (x sweep only): with bx < n[0] the x direction is read as
+// n[0] / bx blocks of bx points, as in a run decomposed into MPI blocks whose
+// shock sensor is never exchanged (module_weno.f90:973 reads the block's own
+// flags; its ghosts stay unflagged).  A face then sees only the flags of the
+// block that uses it.  With edge = 0 the kernel writes every face as seen by
+// its left cell's block; with edge = 1 it runs over the faces on block edges
+// only (nfaces = (n[0]/bx - 1) n[1] n[2]) and writes them as seen by the
+// right block into fhat.
 template <int NRV, int D, int NG>
 __global__ void __launch_bounds__(256) k_euler_face(Geo g, int weno_avg, int linfix,
                                                     const double* __restrict__ v,
                                                     const double* __restrict__ prim,
                                                     const uint8_t* __restrict__ sensor,
-                                                    double* __restrict__ fhat, long long nfaces) {
+                                                    double* __restrict__ fhat, long long nfaces, int bx, int edge) {
   constexpr int NV = IZEM_NIV + NRV;
   constexpr int T1 = D == 0 ? 1 : 0;
   constexpr int T2 = D == 2 ? 1 : 2;
   long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (idx >= nfaces) return;
   int c[3];
-  {
+  if (D == 0 && edge) {
+    const int ne = g.n[0] / bx - 1;
+    long long r = idx;
+    c[0] = ((int)(r % ne) + 1) * bx;   // face between the last cell of a block and the next
+    r /= ne;
+    c[1] = (int)(r % g.n[1]) + 1;
+    c[2] = (int)(r / g.n[1]) + 1;
+  } else {
     long long r = idx;
     int e0 = D == 0 ? g.n[0] + 1 : g.n[0];
     int e1 = D == 1 ? g.n[1] + 1 : g.n[1];
@@ -281,6 +297,10 @@ __global__ void __launch_bounds__(256) k_euler_face(Geo g, int weno_avg, int lin
   // ---- stencil eigenvalue maxima (LLF) and shock flag
   double lm0 = -1.0, lm1 = -1.0, lm2 = -1.0;
   bool shk = false;
+  // the block whose flags count (x sweep with sensor blocks only)
+  const bool blocks = D == 0 && bx < g.n[0];
+  auto xblock = [&](int s) { return (min(max(s, 1), g.n[0]) - 1) / bx; };
+  const int view = blocks ? xblock(edge ? c[0] + 1 : c[0]) : 0;
 #pragma unroll
   for (int st = 0; st < 2 * NG; ++st) {
     const long long ps = p0 + st * stride;
@@ -288,7 +308,8 @@ __global__ void __launch_bounds__(256) k_euler_face(Geo g, int weno_avg, int lin
     lm0 = fmax(fabs(u_s - c_s), lm0);
     lm1 = fmax(fabs(u_s), lm1);
     lm2 = fmax(fabs(u_s + c_s), lm2);
-    shk = shk || (sensor[ps] != 0);
+    const bool counts = !blocks || xblock(c[0] - NG + 1 + st) == view;
+    shk = shk || (counts && sensor[ps] != 0);
   }
   shk = shk && (weno_avg != 0);
 
@@ -433,9 +454,13 @@ __global__ void __launch_bounds__(256) k_euler_face(Geo g, int weno_avg, int lin
 
 // fl(i) = (fhat(i) - fhat(i-1)) * dx_i(i); the x sweep overwrites, y and z
 // accumulate (module_weno.f90:995-1020, 1534-1558).
+// With sensor blocks (bx < n[0], x sweep) the first cell of every block but
+// the first takes its left face from fhat_edge, the block-edge faces as seen
+// by that block (k_euler_face with edge = 1).
 template <int D>
 __global__ void k_flux_diff(Geo g, int nv, const double* __restrict__ fhat, long long nfaces,
-                            const double* __restrict__ dxi, double* __restrict__ fl, int accumulate) {
+                            const double* __restrict__ dxi, double* __restrict__ fl, int accumulate, int bx,
+                            const double* __restrict__ fhat_edge, long long nedge) {
   long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (idx >= g.nint) return;
   int i = (int)(idx % g.n[0]) + 1;
@@ -449,8 +474,16 @@ __global__ void k_flux_diff(Geo g, int nv, const double* __restrict__ fhat, long
   else if (D == 1) { s = j; fr = (long long)(i - 1) + (long long)g.n[0] * (j + (long long)(g.n[1] + 1) * (k - 1)); fl_ = fr - g.n[0]; }
   else { s = k; fr = (long long)(i - 1) + (long long)g.n[0] * ((j - 1) + (long long)g.n[1] * k); fl_ = fr - (long long)g.n[0] * g.n[1]; }
   const double di = dxi[s - 1 + g.ng];
+  const double* fleft = fhat;
+  long long nleft = nfaces;
+  if (D == 0 && bx < g.n[0] && i > 1 && (i - 1) % bx == 0) {
+    const int ne = g.n[0] / bx - 1;
+    fleft = fhat_edge;
+    nleft = nedge;
+    fl_ = (long long)((i - 1) / bx - 1) + (long long)ne * ((j - 1) + (long long)g.n[1] * (k - 1));
+  }
   for (int m = 0; m < nv; ++m) {
-    double df = (fhat[m * nfaces + fr] - fhat[m * nfaces + fl_]) * di;
+    double df = (fhat[m * nfaces + fr] - fleft[m * nleft + fl_]) * di;
     long long o = (long long)m * g.nint + idx;
     fl[o] = accumulate ? fl[o] + df : df;
   }
@@ -458,8 +491,10 @@ __global__ void k_flux_diff(Geo g, int nv, const double* __restrict__ fhat, long
 
 // K3: Adams-Shariff sensor, sticky (only ever sets).  Interior neighbour tests
 // along +x, +y, +z (module_tools.f90:2756-2812).
+// With x blocks of bx points (bx < n[0]) a block's last point is not
+// compared with the next block's first (each MPI block loops to its own ex).
 __global__ void k_sensor(Geo g, double mrw, const double* __restrict__ v, const double* __restrict__ T,
-                         const double* __restrict__ W_i, uint8_t* __restrict__ sensor) {
+                         const double* __restrict__ W_i, uint8_t* __restrict__ sensor, int bx) {
   long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (idx >= g.nint) return;
   int c[3];
@@ -475,7 +510,7 @@ __global__ void k_sensor(Geo g, double mrw, const double* __restrict__ v, const 
   const long long strides[3] = {1LL, (long long)g.g[0], (long long)g.g[0] * g.g[1]};
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
-    if (c[d] <= g.n[d] - 1) {
+    if (c[d] <= g.n[d] - 1 && !(d == 0 && c[0] % bx == 0)) {
       const long long q = p + strides[d];
       const double rq = v[q];
       const double rho_iq = 1.0 / rq;

@@ -76,6 +76,7 @@ def load_library(path=None):
         "izem_gpu_set_eglib": (C.c_int, [P, C.POINTER(IzemEglib)]),
         "izem_gpu_autotune": (C.c_int, [P, C.c_double, C.c_char_p, C.c_int]),
         "izem_gpu_set_chem_variant": (C.c_int, [C.c_int]),
+        "izem_gpu_set_sensor_xblocks": (C.c_int, [P, C.c_int]),
         "izem_gpu_chem_autotune": (C.c_int, [C.POINTER(IzemMech), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                                              C.c_void_p, C.c_int, C.c_char_p, C.c_int]),
         "izem_gpu_chem_surrogate_stats": (C.c_int, [P, C.POINTER(C.c_longlong), C.POINTER(C.c_int),
@@ -288,6 +289,11 @@ class IzemGPU:
         buf = C.create_string_buffer(2048)
         self._check(self.lib.izem_gpu_autotune(self.h, float(chem_dt), buf, 2048), "autotune")
         return json.loads(buf.value.decode())
+
+    def set_sensor_xblocks(self, nblk):
+        """Reproduce a reference run decomposed into nblk MPI blocks along x:
+        the shock sensor is not shared between blocks (izem_gpu_set_sensor_xblocks)."""
+        self._check(self.lib.izem_gpu_set_sensor_xblocks(self.h, int(nblk)), "set_sensor_xblocks")
 
     def set_chem_variant(self, v):
         """Pin the register-budget variant (0..4) of the persistent chemistry
