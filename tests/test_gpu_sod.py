@@ -58,7 +58,8 @@ def test_sod_fluxes_match_oracle():
 def test_sod_steps_match_oracle():
     """Full time steps (time step, RK3 with the sticky sensor, primitives,
     extrapolation and periodic halos) from the initial discontinuity: one
-    step within TOL; after twenty steps the rounding differences of the two
+    step within TOL (the x momentum, created by cancellation, within 1e-10);
+    after twenty steps the rounding differences of the two
     machines have grown at the discontinuity, and the state agrees within
     1e-10 (the y and z momenta, rounding noise of the 2-D run, absolutely
     within 1e-10 of the largest density)."""
@@ -71,8 +72,11 @@ def test_sod_steps_match_oracle():
         orc.rk3(st, dt_o)
         g.rk3(dt_o)
         if step == 0:
+            # after one step the x momentum is small, made from the pressure
+            # jump across the discontinuity: its rounding is relative to that
+            # cancellation, not to its own size
             err = W.normwise(_interior(g.download()["v"]), _interior(st["v"]))
-            assert np.all(err[[0, 1, 4, 5, 6]] <= TOL), err
+            assert np.all(err[[0, 4, 5, 6]] <= TOL) and err[1] <= 1e-10, err
     got = _interior(g.download()["v"])
     g.close()
     ref = _interior(st["v"])
