@@ -315,10 +315,13 @@ __global__ void __launch_bounds__(256) k_euler_face(Geo g, int weno_avg, int lin
 
   double gh[NV];
   if (!shk) {
-    // linear reconstruction (wenorec_nw): accumulate while streaming over the stencil
-    double am[NV], ap[NV];
-#pragma unroll
-    for (int m = 0; m < NV; ++m) { am[m] = 0.0; ap[m] = 0.0; }
+    // linear reconstruction (wenorec_nw).  The LLF speed of each field is
+    // the same at every stencil point and the projection L is linear, so
+    //   sum_st c_st (L f_st +/- lam L w_st) / 2 = (L F +/- lam L W) / 2
+    // with F = sum_st c_st f_st and W = sum_st c_st w_st: the raw stencil
+    // sums are accumulated while streaming over the points and projected
+    // once each (the reference projects every point, module_weno.f90:953-989;
+    // the two agree to rounding).
     // WENO5: the reference's (mirrored) coefficients on points 0..4 ('-') and
     // 1..5 ('+'), or the textbook ones (linfix); WENO7: the 7th-order
     // stencil on points 0..6 and 1..7
@@ -328,6 +331,9 @@ __global__ void __launch_bounds__(256) k_euler_face(Geo g, int weno_avg, int lin
     const double cpf[8] = {0.0, -3.0, 27.0, 47.0, -13.0, 2.0, 0.0, 0.0};
     const double cm7[8] = {-3.0, 25.0, -101.0, 319.0, 214.0, -38.0, 4.0, 0.0};
     const double cp7[8] = {0.0, 4.0, -38.0, 214.0, 319.0, -101.0, 25.0, -3.0};
+    double Wm[NV], Fm[NV], Wp[NV], Fp[NV];
+#pragma unroll
+    for (int m = 0; m < NV; ++m) { Wm[m] = 0.0; Fm[m] = 0.0; Wp[m] = 0.0; Fp[m] = 0.0; }
 #pragma unroll
     for (int st = 0; st < 2 * NG; ++st) {
       const long long ps = p0 + st * stride;
@@ -343,43 +349,41 @@ __global__ void __launch_bounds__(256) k_euler_face(Geo g, int weno_avg, int lin
       for (int l = IZEM_NIV; l < NV; ++l) f[l] = w[l] * u_s;
       const double ccm = NG == 4 ? cm7[st] : (linfix ? cmf[st] : cmr[st]);
       const double ccp = NG == 4 ? cp7[st] : (linfix ? cpf[st] : cpr[st]);
-      // project w and f
-      double sw = 0.0, sf = 0.0;
-#pragma unroll
-      for (int l = 0; l < NRV; ++l) { sw = sw + psi[l] * w[IZEM_NIV + l]; sf = sf + psi[l] * f[IZEM_NIV + l]; }
-      const double Gw = -b1 * w[0] + B1 * w[1] + B2 * w[2] + B3 * w[3] - b2 * w[4] - b2 * sw;
-      const double Gf = -b1 * f[0] + B1 * f[1] + B2 * f[2] + B3 * f[3] - b2 * f[4] - b2 * sf;
-      double pw[NV], pf[NV];
-      pw[0] = A0 * w[0] + An * w[1 + D] + At1 * w[1 + T1] + At2 * w[1 + T2] + hb2 * w[4] + hb2 * sw;
-      pf[0] = A0 * f[0] + An * f[1 + D] + At1 * f[1 + T1] + At2 * f[1 + T2] + hb2 * f[4] + hb2 * sf;
-      pw[1] = w[0] + Gw;
-      pf[1] = f[0] + Gf;
-      pw[2] = C0 * w[0] + Cn * w[1 + D] + At1 * w[1 + T1] + At2 * w[1 + T2] + hb2 * w[4] + hb2 * sw;
-      pf[2] = C0 * f[0] + Cn * f[1 + D] + At1 * f[1 + T1] + At2 * f[1 + T2] + hb2 * f[4] + hb2 * sf;
-      pw[3] = -uc[T1] * w[0] + w[1 + T1];
-      pf[3] = -uc[T1] * f[0] + f[1 + T1];
-      pw[4] = -uc[T2] * w[0] + w[1 + T2];
-      pf[4] = -uc[T2] * f[0] + f[1 + T2];
-      pw[5] = E0 * w[0] + E1 * w[1] + E2 * w[2] + E3 * w[3] + opx * w[4] + xi * sw;
-      pf[5] = E0 * f[0] + E1 * f[1] + E2 * f[2] + E3 * f[3] + opx * f[4] + xi * sf;
-#pragma unroll
-      for (int s = 0; s < NRV - 1; ++s) {
-        pw[6 + s] = Yc[s] * Gw + w[IZEM_NIV + s];
-        pf[6 + s] = Yc[s] * Gf + f[IZEM_NIV + s];
-      }
 #pragma unroll
       for (int m = 0; m < NV; ++m) {
-        const double lam = m == 0 ? lm0 : (m == 2 ? lm2 : lm1);
-        const double gp = 0.5 * (pf[m] + lam * pw[m]);
-        const double gmn = pf[m] - gp;
-        am[m] = am[m] + ccm * gp;
-        ap[m] = ap[m] + ccp * gmn;
+        Wm[m] = Wm[m] + ccm * w[m];
+        Fm[m] = Fm[m] + ccm * f[m];
+        Wp[m] = Wp[m] + ccp * w[m];
+        Fp[m] = Fp[m] + ccp * f[m];
       }
     }
+    // the structured left-eigenvector product of the nonlinear branch, on one vector
+    auto project = [&](const double* w, double* pw) {
+      double sw = 0.0;
+#pragma unroll
+      for (int l = 0; l < NRV; ++l) sw = sw + psi[l] * w[IZEM_NIV + l];
+      const double Gw = -b1 * w[0] + B1 * w[1] + B2 * w[2] + B3 * w[3] - b2 * w[4] - b2 * sw;
+      pw[0] = A0 * w[0] + An * w[1 + D] + At1 * w[1 + T1] + At2 * w[1 + T2] + hb2 * w[4] + hb2 * sw;
+      pw[1] = w[0] + Gw;
+      pw[2] = C0 * w[0] + Cn * w[1 + D] + At1 * w[1 + T1] + At2 * w[1 + T2] + hb2 * w[4] + hb2 * sw;
+      pw[3] = -uc[T1] * w[0] + w[1 + T1];
+      pw[4] = -uc[T2] * w[0] + w[1 + T2];
+      pw[5] = E0 * w[0] + E1 * w[1] + E2 * w[2] + E3 * w[3] + opx * w[4] + xi * sw;
+#pragma unroll
+      for (int s = 0; s < NRV - 1; ++s) pw[6 + s] = Yc[s] * Gw + w[IZEM_NIV + s];
+    };
+    double pWm[NV], pFm[NV], pWp[NV], pFp[NV];
+    project(Wm, pWm);
+    project(Fm, pFm);
+    project(Wp, pWp);
+    project(Fp, pFp);
+    constexpr double den = NG == 4 ? 1.0 / 420.0 : 1.0 / 60.0;
 #pragma unroll
     for (int m = 0; m < NV; ++m) {
-      constexpr double den = NG == 4 ? 1.0 / 420.0 : 1.0 / 60.0;
-      gh[m] = am[m] * den + ap[m] * den;
+      const double lam = m == 0 ? lm0 : (m == 2 ? lm2 : lm1);
+      const double am = 0.5 * (pFm[m] + lam * pWm[m]);   // sum c gplus
+      const double ap = 0.5 * (pFp[m] - lam * pWp[m]);   // sum c gminus
+      gh[m] = am * den + ap * den;
     }
   } else {
     // nonlinear reconstruction (wenorec): keep the 2NG stencil values of every field
