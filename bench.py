@@ -135,7 +135,9 @@ CHEM_FLOP_PER_BDF_STEP = 9793
 # not hold
 CHEM_TRAFFIC_PER_REACTOR = 16115
 
-EULER_FLOP_PER_FACE = {2: 1400, 9: 2481}   # FP64 flops per face (sensor-off branch): ncu DFMA x2 + DADD + DMUL counts (profiles/euler_face_mix128.md)
+# FP64 flops per face of k_euler_face (2 DFMA + DADD + DMUL per thread, summed
+# by ncu over one launch, / faces): profiles/euler_face_mix128.md (9 species)
+EULER_FLOP_PER_FACE = {9: 1869}
 
 
 class Stepper:
@@ -257,12 +259,13 @@ def run_gpu(args, rank, world):
         avg_s = fx[1] / fx[0] * 1e-3
         byts = euler_face_bytes(cfg)
         nf = (cfg.nx + 1) * cfg.ny * cfg.nz
-        flops = nf * EULER_FLOP_PER_FACE.get(cfg.nrv, 2000)
         rl = {"bound": "hbm", "kernel": "k_euler_face (x sweep)", "achieved": byts / avg_s / 1e9, "peak": hbm,
               "unit": "GB/s", "frac": byts / avg_s / 1e9 / hbm, "traffic": TRAFFIC_PER_LAUNCH.get(args.workload),
-              "peak_source": hbm_src + " (MEASURED_PEAKS.json hbm_gbs)",
-              "fp64": {"achieved": flops / avg_s / 1e9, "peak": FP64_PEAK_GFLOPS, "unit": "GFLOP/s",
-                       "frac": flops / avg_s / 1e9 / FP64_PEAK_GFLOPS}}
+              "peak_source": hbm_src + " (MEASURED_PEAKS.json hbm_gbs)"}
+        if cfg.nrv in EULER_FLOP_PER_FACE:
+            flops = nf * EULER_FLOP_PER_FACE[cfg.nrv]
+            rl["fp64"] = {"achieved": flops / avg_s / 1e9, "peak": FP64_PEAK_GFLOPS, "unit": "GFLOP/s",
+                          "frac": flops / avg_s / 1e9 / FP64_PEAK_GFLOPS}
     launches = sum(n for n, _ in kt.values())
     mlp = run_mlp_chem(args, g, stp, ncell, world) if chem and not args.no_mlp else None
     res = {
