@@ -4,8 +4,9 @@ Workload (one "step" = one full time step of the reference driver,
 izem.f90:242-389: timestep, then the three SSP-RK3 stages, plus the two
 Strang chemistry half-steps when chemistry is on): the temporal H2/air mixing
 layer on 256 x 256 x 128 cells, 9 species, WENO5 characteristic fluxes,
-mixture-averaged viscous and diffusive fluxes, Newton temperature, seeded
-synthetic initial field (numpy PCG64 seed 20261203).
+EGLIB viscous and diffusive fluxes (--transport fitted: the mixture-averaged
+fits), Newton temperature, Strang BDF chemistry, seeded synthetic initial
+field (numpy PCG64 seed 20261203).
 
 Printed JSON (one line, rank 0):
   value       device throughput, inputs resident in HBM
@@ -227,11 +228,16 @@ def run_gpu(args, rank, world):
     pinned_out = {k: pin(a) for k, a in host.items()}   # results read back into pinned memory
     h2d = sum(a.nbytes for a in pinned.values())
     g.synchronize()
+    t_copy = 0.0
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
+        ta = time.perf_counter()
         g.upload(**pinned)
+        tb = time.perf_counter()
         stp.step()
+        tc = time.perf_counter()
         out = g.download(out=pinned_out)
+        t_copy += (tb - ta) + (time.perf_counter() - tc)
     e2e_s = time.perf_counter() - t0
     d2h = sum(a.nbytes for a in out.values())
     e2e_value = world * ncell * e2e_steps / e2e_s / 1e6
@@ -282,7 +288,8 @@ def run_gpu(args, rank, world):
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "autotuned_threads_per_block": {k: v["chosen"] for k, v in tuning.items()}},
         "e2e": {"value": e2e_value, "unit": "Mcell-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "steps": e2e_steps},
+                "steps": e2e_steps, "ms_per_step": e2e_s * 1e3 / e2e_steps,
+                "copy_ms_per_step": t_copy * 1e3 / e2e_steps},
         "roofline": rl_chem if rl_chem else rl,
         "roofline_euler_face": rl if rl_chem else None,
         "dominant_kernel": {"name": dom_name, "launches": dom_n, "ms": dom_ms},

@@ -204,7 +204,10 @@ int  izem_gpu_rk3(izem_ctx* ctx, double dt, double time0);
 
 /* timestep (module_solver.f90:202-408): dt_4 and dtmin (non-dimensional).
  * dtmin is in/out: its input value is the previous step's dtmin (used by the
- * chemical criterion), DTmax the previous chemistry's max |dT|. */
+ * chemical criterion), DTmax the previous chemistry's max |dT|.  With
+ * cfg.vis and cfg.vis_dt, dt_4[1] and dt_4[2] are the Fourier criteria of
+ * mass and thermal diffusion (:294-367) from the mixture-averaged fits, as
+ * the reference uses them even under EGLIB; otherwise they stay 1. */
 int  izem_gpu_timestep(izem_ctx* ctx, double DTmax, double dt_4[4], double* dtmin);
 
 /* Mechanism for the chemistry steps (the chem.bin data; see izem_mech). */

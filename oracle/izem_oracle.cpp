@@ -1057,6 +1057,43 @@ void timestep(const Ctx& c, double DTmax, const double* v, const double* T, cons
         dtc = std::max(std::max(std::max(dtc, ax), ay), az);
       }
   dt4[0] = c.cfg.cfl / dtc;
+  if (c.cfg.vis && c.cfg.vis_dt) {
+    // Fourier criteria (module_solver.f90:294-367) from the simple transport
+    // fits (prim_vis_vars_wo_mu, module_thermodynamics.f90:1243-1420) even
+    // under EGLIB, with the filter width of filter_width (module_tools.f90:
+    // 2328-2378).  Without LES mu_SGS is zero, so its terms add exactly 0.
+    const int nrv = b.nrv;
+    const size_t nc = b.ncell, np = (size_t)b.nx * b.ny * b.nz;
+    std::vector<double> dm(nrv * np), d2(np), rct(np);
+    const double third = 1.0 / 3.0;
+    for (int k = 1; k <= b.nz; ++k)
+      for (int j = 1; j <= b.ny; ++j)
+        for (int i = 1; i <= b.nx; ++i) {
+          const size_t p = b.id(i, j, k), q = (size_t)(i - 1) + (size_t)b.nx * ((j - 1) + (size_t)b.ny * (k - 1));
+          double X[IZEM_NSMAX], d[IZEM_NSMAX], mu, ct;
+          for (int l = 0; l < nrv; ++l) X[l] = v[(NIV + l) * nc + p] / (v[p] * W_i[p] * t.Wc[l]);
+          prim_vis_point(c, v[p], T[p], W_i[p], X, d, &mu, &ct);
+          for (int l = 0; l < nrv; ++l) dm[l * np + q] = d[l];
+          const double dx = c.dxi[0][i - 1 + b.ng], dy = c.dxi[1][j - 1 + b.ng], dz = c.dxi[2][k - 1 + b.ng];
+          const double delta = c.cfg.ndim == 2 ? 1.0 / std::sqrt(dx * dy) : 1.0 / std::pow(dx * dy * dz, third);
+          d2[q] = delta * delta;
+          rct[q] = d2[q] * v[p] / (ct / cp[p]);
+        }
+    // the species of the largest diffusivity: first in (l, k, j, i) order
+    int ldmax = 0;
+    double diffmax = dm[0];
+    for (int l = 0; l < nrv; ++l)
+      for (size_t q = 0; q < np; ++q)
+        if (diffmax < dm[l * np + q]) { ldmax = l; diffmax = dm[l * np + q]; }
+    double m2 = d2[0] / dm[ldmax * np], m3 = rct[0];
+    for (size_t q = 0; q < np; ++q) {
+      m2 = std::min(m2, d2[q] / dm[ldmax * np + q]);
+      m3 = std::min(m3, rct[q]);
+    }
+    const double rvd0_i = c.adi.sc / c.adi.sqgmr, rlamcp0_i = c.adi.pr / c.adi.sqgmr;
+    dt4[1] = rvd0_i * c.cfg.fo * m2;
+    dt4[2] = rlamcp0_i * c.cfg.fo * m3;
+  }
   if (c.cfg.reaction) {
     dt4[3] = *dtmin * c.cfg.cpr / DTmax;
     dt4[3] = std::min(dt4[3], 1.0);

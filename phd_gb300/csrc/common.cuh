@@ -61,6 +61,11 @@ struct DevStatus {
   int newton_nan;
   int newton_unconverged;
   unsigned long long dtc_bits;       // timestep: max (|u|+c)/dx (bit pattern)
+  // timestep, Fourier criteria (bit patterns of positive doubles): per
+  // species max of D_k and min of delta^2 / D_k, and min of delta^2 rho cp / lambda
+  unsigned long long fo_dmax_bits[IZEM_NSMAX];
+  unsigned long long fo_dmin_bits[IZEM_NSMAX];
+  unsigned long long fo_ctmin_bits;
   int timeout;
   int chem_fail;
 };

@@ -306,8 +306,12 @@ int do_timestep(izem_ctx* c) {
   const Geo& g = c->g;
   Metrics mt;
   for (int d = 0; d < 3; ++d) mt.dxi[d] = c->dxi[d];
-  return launch(c, "timestep", [&] {
+  int rc = launch(c, "timestep", [&] {
     k_dtc<NRV><<<grid_for(g.nint), kThreads, 0, c->stream>>>(g, mt, c->v, c->T, c->W_i, c->cp, c->d_status);
+  });
+  if (rc || !(c->cfg.vis && c->cfg.vis_dt)) return rc;
+  return launch(c, "timestep_fourier", [&] {
+    k_dtv<NRV><<<grid_for(g.nint), kThreads, 0, c->stream>>>(g, mt, c->v, c->T, c->W_i, c->cp, c->d_status);
   });
 }
 
@@ -658,6 +662,13 @@ int izem_gpu_rk3(izem_ctx* c, double dt, double time0) {
 int izem_gpu_timestep(izem_ctx* c, double DTmax, double dt_4[4], double* dtmin) {
   if (!c || !dt_4 || !dtmin) return IZEM_ERR_ARG;
   CK(cudaMemsetAsync(&c->d_status->dtc_bits, 0, sizeof(unsigned long long), c->stream));
+  const bool fourier = c->cfg.vis && c->cfg.vis_dt;
+  if (fourier) {
+    // max slots from 0; min slots from bytes 0x7f (1.4e306, above any criterion)
+    CK(cudaMemsetAsync(c->d_status->fo_dmax_bits, 0, sizeof(c->d_status->fo_dmax_bits), c->stream));
+    CK(cudaMemsetAsync(c->d_status->fo_dmin_bits, 0x7f, sizeof(c->d_status->fo_dmin_bits), c->stream));
+    CK(cudaMemsetAsync(&c->d_status->fo_ctmin_bits, 0x7f, sizeof(unsigned long long), c->stream));
+  }
   int rc = IZEM_DISPATCH(c, do_timestep, c);
   if (rc) return rc;
   rc = read_status(c);
@@ -667,6 +678,19 @@ int izem_gpu_timestep(izem_ctx* c, double DTmax, double dt_4[4], double* dtmin) 
   double dtc = std::fmax(1.0, m);
   for (int q = 0; q < 4; ++q) dt_4[q] = 1.0;
   dt_4[0] = c->cfg.cfl / dtc;
+  if (fourier) {
+    // the species of the largest D_k: the first that reaches the maximum, as
+    // the reference's scan in (l, k, j, i) order with a strict comparison
+    const DevStatus& s = *c->h_status;
+    auto dbl = [](unsigned long long b) { double x; std::memcpy(&x, &b, sizeof(double)); return x; };
+    int ldmax = 0;
+    double dmax = dbl(s.fo_dmax_bits[0]);
+    for (int l = 1; l < c->cfg.nrv; ++l)
+      if (dmax < dbl(s.fo_dmax_bits[l])) { ldmax = l; dmax = dbl(s.fo_dmax_bits[l]); }
+    const double rvd0_i = c->adi.sc / c->adi.sqgmr, rlamcp0_i = c->adi.pr / c->adi.sqgmr;
+    dt_4[1] = rvd0_i * c->cfg.fo * dbl(s.fo_dmin_bits[ldmax]);
+    dt_4[2] = rlamcp0_i * c->cfg.fo * dbl(s.fo_ctmin_bits);
+  }
   if (c->cfg.reaction) {
     dt_4[3] = *dtmin * c->cfg.cpr / DTmax;
     dt_4[3] = std::fmin(dt_4[3], 1.0);

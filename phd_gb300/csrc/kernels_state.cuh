@@ -251,3 +251,95 @@ __global__ void k_dtc(Geo g, Metrics mt, const double* __restrict__ v, const dou
   for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
   if ((threadIdx.x & 31) == 0) atomic_max_nonneg(&st->dtc_bits, m);
 }
+
+__device__ inline void atomic_min_pos(unsigned long long* addr, double v) {
+  atomicMin(addr, (unsigned long long)__double_as_longlong(v));
+}
+
+// Fourier time-step criteria (module_solver.f90:294-367) at the interior
+// points: the mixture-averaged D_k and lambda of prim_vis_vars_wo_mu
+// (module_thermodynamics.f90:1243-1420, the simple fits even under EGLIB)
+// with X_k of molefrac (:1669-1698), and delta^2 of filter_width
+// (module_tools.f90:2328-2378).  Per species the max of D_k and the min of
+// delta^2 / D_k, and the min of delta^2 rho / (lambda / cp), reduced into the
+// status word; the host picks the species of the largest D_k.  The LES terms
+// of the reference (mu_SGS = 0 without LES) add exactly zero and are left out.
+template <int NRV>
+__global__ void k_dtv(Geo g, Metrics mt, const double* __restrict__ v, const double* __restrict__ T,
+                      const double* __restrict__ W_i, const double* __restrict__ cp, DevStatus* st) {
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const double big = __longlong_as_double(0x7ff0000000000000LL);   // +inf: identity of min
+  double dmx[NRV], dmn[NRV], rct = big;
+#pragma unroll
+  for (int l = 0; l < NRV; ++l) { dmx[l] = 0.0; dmn[l] = big; }
+  if (idx < g.nint) {
+    int c[3];
+    c[0] = (int)(idx % g.n[0]) + 1;
+    long long r = idx / g.n[0];
+    c[1] = (int)(r % g.n[1]) + 1;
+    c[2] = (int)(r / g.n[1]) + 1;
+    const long long nc = g.ncell;
+    const long long p = gid(g, c[0], c[1], c[2]);
+    const double rho = v[p], Tp = T[p], Wi = W_i[p];
+    double X[NRV];
+#pragma unroll
+    for (int l = 0; l < NRV; ++l) X[l] = v[(IZEM_NIV + l) * nc + p] / (rho * Wi * c_thd.Wc[l]);
+    const double lt1 = log(Tp * c_thd.tinf);
+    const double lt2 = lt1 * lt1, lt3 = lt2 * lt1;
+    const double P = rho * Tp * Wi;
+    const double epsm12 = 1.0e-12;
+    double dm[NRV], wk1[NRV], xe[NRV], aw[NRV];
+#pragma unroll
+    for (int l = 0; l < NRV; ++l) {
+      xe[l] = X[l] + epsm12;
+      aw[l] = xe[l] * c_thd.Wc[l] * Wi;
+      dm[l] = 0.0;
+      wk1[l] = 0.0;
+    }
+    // D_kl symmetric: one exponential per pair, sums over l in ascending order
+#pragma unroll
+    for (int m = 0; m < NRV; ++m)
+#pragma unroll
+      for (int l = m + 1; l < NRV; ++l) {
+        const double* cf = c_thd.cofd[m][l];
+        const double e = 1.0 / exp(0.0 + cf[0] * 1.0 + cf[1] * lt1 + cf[2] * lt2 + cf[3] * lt3);
+        dm[m] = dm[m] + xe[l] * e;
+        dm[l] = dm[l] + xe[m] * e;
+        wk1[m] = wk1[m] + aw[l];
+        wk1[l] = wk1[l] + aw[m];
+      }
+    double ct = 0.0, w1 = 0.0;
+#pragma unroll
+    for (int l = 0; l < NRV; ++l) {
+      const double* cl = c_thd.coflam[l];
+      const double c1 = exp(0.0 + cl[0] * 1.0 + cl[1] * lt1 + cl[2] * lt2 + cl[3] * lt3);
+      ct = ct + X[l] / c1;
+      w1 = w1 + X[l] * c1;
+    }
+    ct = c_thd.Kl * (1.0 / ct + w1);
+    const double dx = mt.dxi[0][c[0] - 1 + g.ng], dy = mt.dxi[1][c[1] - 1 + g.ng], dz = mt.dxi[2][c[2] - 1 + g.ng];
+    const double delta = g.ndim == 2 ? 1.0 / sqrt(dx * dy) : 1.0 / pow(dx * dy * dz, 1.0 / 3.0);
+    const double d2 = delta * delta;
+#pragma unroll
+    for (int l = 0; l < NRV; ++l) {
+      dmx[l] = wk1[l] * c_thd.Kd[l] / (dm[l] * P);
+      dmn[l] = d2 / dmx[l];
+    }
+    rct = d2 * rho / (ct / cp[p]);
+  }
+#pragma unroll
+  for (int l = 0; l < NRV; ++l)
+    for (int o = 16; o > 0; o >>= 1) {
+      dmx[l] = fmax(dmx[l], __shfl_down_sync(0xffffffffu, dmx[l], o));
+      dmn[l] = fmin(dmn[l], __shfl_down_sync(0xffffffffu, dmn[l], o));
+    }
+  for (int o = 16; o > 0; o >>= 1) rct = fmin(rct, __shfl_down_sync(0xffffffffu, rct, o));
+  if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+    for (int l = 0; l < NRV; ++l) {
+      atomic_max_nonneg(&st->fo_dmax_bits[l], dmx[l]);
+      atomic_min_pos(&st->fo_dmin_bits[l], dmn[l]);
+    }
+    atomic_min_pos(&st->fo_ctmin_bits, rct);
+  }
+}

@@ -246,6 +246,24 @@ def test_timestep_matches_oracle(name):
     assert dt_g == dt_o and dt4_g[0] == dt4_o[0], (dt_g, dt_o)
 
 
+@pytest.mark.parametrize("name", ["tgv", "mix"])
+def test_fourier_timestep_matches_oracle(name):
+    """With VIS_DT the Fourier criteria dt_4(2), dt_4(3) (module_solver.f90:
+    294-367): per-species max and min reductions on the device, the species
+    of the largest D_k picked on the host.  The transport fits go through
+    exp and the filter width through a cube root, so they agree with the
+    oracle to rounding (1e-13 relative); dt_4(1) is bitwise."""
+    cfg, thd, adi, dxi, st, info, orc = W.case(name, 12, vis_dt=True)
+    g = gpu_from(cfg, thd, adi, dxi, st)
+    dt4_g, dt_g = g.timestep()
+    dt4_o, dt_o = orc.timestep(st)
+    g.close()
+    assert dt4_g[0] == dt4_o[0] and dt4_g[3] == dt4_o[3]
+    for q in (1, 2):
+        assert dt4_o[q] != 1.0 and abs(dt4_g[q] - dt4_o[q]) <= 1e-13 * dt4_o[q], (q, dt4_g, dt4_o)
+    assert abs(dt_g - dt_o) <= 1e-13 * dt_o
+
+
 def test_negative_pressure_is_reported_not_computed():
     """A state with P <= 0 in one interior cell makes euler_LLF abort in the
     reference (module_weno.f90:1027-1036); the GPU flux returns

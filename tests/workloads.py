@@ -12,10 +12,11 @@ def _copy(state):
     return {k: np.array(v, order="F", copy=True) for k, v in state.items()}
 
 
-def case(name, n=12, seed=ics.SEED, eglib=False):
+def case(name, n=12, seed=ics.SEED, eglib=False, vis_dt=False):
     """Returns cfg, thd, adi, dxi, finalized state (oracle-closed), info.
     eglib: EGLIB precision-1 transport (cfg.eglib = 1, linking data set on
-    the oracle; the caller sets it on the GPU context)."""
+    the oracle; the caller sets it on the GPU context).  vis_dt: the Fourier
+    criteria of the time step (cfg.vis_dt = 1)."""
     if name == "tgv":
         cfg, thd, adi, dxi, st, info = ics.tgv(n, lib_dscalar=oracle.metrics_dscalar)
     elif name == "mix":
@@ -26,6 +27,8 @@ def case(name, n=12, seed=ics.SEED, eglib=False):
         raise KeyError(name)
     if eglib:
         cfg.eglib = 1
+    if vis_dt:
+        cfg.vis_dt = 1
     orc = oracle.Oracle(cfg, thd, adi, *dxi)
     if eglib:
         orc.set_eglib(eglib_link(load_species("h2air9" if name == "mix" else "o2n2")))
