@@ -225,6 +225,20 @@ int  izem_gpu_set_mechanism(izem_ctx* ctx, const izem_mech* mech);
  * reference).  DTmax receives max |dT| [K]. */
 enum { IZEM_CHEM_BDF = 0, IZEM_CHEM_MLP = 1 };
 int  izem_gpu_chem_step(izem_ctx* ctx, double dt, int mode, double* DTmax);
+
+/* [REACTING] DVODESIMP with Y1F, Y0O, INDEX_H2, INDEX_N2 (module_reaction.f90:
+ * 173-251): with enable != 0, mode IZEM_CHEM_BDF integrates only the window
+ * cells whose initial production rates move some mass fraction by more than
+ * 1e-12 in dt (psr_simp_chemkin: CKWYR x molar mass x dt / rho) and whose H2
+ * and N2 both differ by more than 1e-6 from the pure fuel Y_fuel and from the
+ * pure oxidiser Y_oxidizer (arrays of nrv mass fractions); the other cells
+ * keep their state and do not enter DTmax, and the integrated cells clip the
+ * closing species to [0, 1] as that branch does.  index_h2 and index_n2 are
+ * 0-based species indices (the deck's INDEX_* minus 1).  enable = 0 restores
+ * the integration of every cell.  The reference calls psr_simp_chemkin with
+ * four of its five arguments; this is the routine's stated semantics. */
+int  izem_gpu_set_chem_skip(izem_ctx* ctx, int enable, const double* Y_fuel, const double* Y_oxidizer,
+                            int index_h2, int index_n2);
 /* Statistics of the last chemistry step: cells whose integration failed
  * (ISTATE <= -2), largest and summed BDF step counts. */
 int  izem_gpu_chem_stats(izem_ctx* ctx, int* failed, int* max_steps, unsigned long long* total_steps);

@@ -32,6 +32,7 @@ def load():
         "or_create": (P, [C.POINTER(IzemCfg), C.POINTER(IzemThd), C.POINTER(IzemAdi), _dp, _dp, _dp]),
         "or_destroy": (None, [P]),
         "or_set_sensor_xblocks": (C.c_int, [P, C.c_int]),
+        "or_set_chem_skip": (C.c_int, [P, C.c_int, _dp, _dp, C.c_int, C.c_int]),
         "or_last_error": (C.c_int, [P, C.c_char_p, C.c_int]),
         "or_cp_scalar": (None, [P, C.c_double, _dp, _dp]),
         "or_ha_scalar": (None, [P, C.c_double, _dp]),
@@ -161,6 +162,16 @@ class Oracle:
         """Emulate a run whose x direction was split into nblk MPI blocks:
         the shock sensor does not compare points across block edges."""
         self._rc(self.lib.or_set_sensor_xblocks(self.h, int(nblk)), "set_sensor_xblocks")
+
+    def set_chem_skip(self, y_fuel=None, y_oxidizer=None, index_h2=0, index_n2=0, enable=True):
+        """dvodesimp: integrate only the cells that the skip test selects
+        (pure fuel / oxidiser compositions, 0-based H2 and N2 indices)."""
+        if not enable:
+            self._rc(self.lib.or_set_chem_skip(self.h, 0, None, None, 0, 0), "set_chem_skip")
+            return
+        yf = np.ascontiguousarray(y_fuel, dtype=np.float64)
+        yo = np.ascontiguousarray(y_oxidizer, dtype=np.float64)
+        self._rc(self.lib.or_set_chem_skip(self.h, 1, _p(yf), _p(yo), int(index_h2), int(index_n2)), "set_chem_skip")
 
     def newton_warnings(self):
         return self.lib.or_last_error(self.h, None, 0)

@@ -64,6 +64,11 @@ struct Ctx {
   std::vector<double> dxi[3];   // indexed (i-1+ng), length n+2ng
   int newton_warn = 0;
   int sensor_xblocks = 1;   // x-blocks of the reference's MPI run whose edges the sensor does not cross
+  // dvodesimp (module_reaction.f90:173-251): pure fuel Y1f and oxidiser Y0o,
+  // H2 and N2 species indices (0-based)
+  bool dvodesimp = false;
+  double y1f[IZEM_NSMAX] = {}, y0o[IZEM_NSMAX] = {};
+  int index_h2 = 0, index_n2 = 0;
   std::string err;
 };
 
@@ -1104,9 +1109,15 @@ void timestep(const Ctx& c, double DTmax, const double* v, const double* T, cons
 
 #include "chem_oracle.inc"
 
-// reaction_dvode (module_reaction.f90:102-321, dvodesimp = F) followed by
-// the rest of reaction_selec (:83-86): upd_prim_var_woT on the interior,
-// comm_cons, upd_boundaries, upd_prim_var_ghost.
+// reaction_dvode (module_reaction.f90:102-321) followed by the rest of
+// reaction_selec (:83-86): upd_prim_var_woT on the interior, comm_cons,
+// upd_boundaries, upd_prim_var_ghost.  With dvodesimp a cell is integrated
+// only if psr_simp_chemkin's increments (CKWYR rates x molar mass x dt /
+// rho, psr_simp_chemkin.f:31-42; the reference passes it four of its five
+// arguments, so its stated semantics are restated) move some species by more
+// than 1e-12 and its H2 and N2 both differ from the pure fuel and from the
+// pure oxidiser by more than 1e-6 (:185-215); that branch also clips the
+// closing species (:233-240).
 int chem_step(Ctx& c, const izem_mech& mech, double dt, double* v, double* T, double* W_i, double* cp, double* ha,
               double* DTmax_out, int* max_steps) {
   const Block& b = c.b;
@@ -1132,6 +1143,18 @@ int chem_step(Ctx& c, const izem_mech& mech, double dt, double* v, double* T, do
         const double rho_phys = rho0 * rho_cgs;
         const double T0_phys = T[p] * a.t_ref;
         z[0] = T0_phys;
+        if (c.dvodesimp) {
+          double wdot[IZEM_NSMAX];
+          ck_wyr(mech, rho_phys, T0_phys, z + 1, wdot);
+          const double myc = dt_phys / rho_phys;
+          bool call_w = false;
+          for (int l = 0; l < nrv; ++l)
+            if (std::fabs(wdot[l] * mech.wt[l] * myc) > 1.0e-12) call_w = true;
+          const double yh = z[1 + c.index_h2], yn = z[1 + c.index_n2];
+          const bool call_f = std::fabs(yh - c.y1f[c.index_h2]) > 1.0e-6 && std::fabs(yn - c.y1f[c.index_n2]) > 1.0e-6;
+          const bool call_o = std::fabs(yh - c.y0o[c.index_h2]) > 1.0e-6 && std::fabs(yn - c.y0o[c.index_n2]) > 1.0e-6;
+          if (!(call_w && call_f && call_o)) continue;
+        }
         int nst = 0;
         const int istate = reaction_v(mech, rho_phys, z, dt_phys, &nst);
         if (istate <= -2) fail += 1;
@@ -1145,7 +1168,8 @@ int chem_step(Ctx& c, const izem_mech& mech, double dt, double* v, double* T, do
           v[(NIV + l) * b.ncell + p] = rho0 * Ya;
           sumY = sumY + Ya;
         }
-        v[(NIV + nrv - 1) * b.ncell + p] = rho0 * (1.0 - sumY);
+        const double ylast = c.dvodesimp ? std::min(std::max(1.0 - sumY, 0.0), 1.0) : 1.0 - sumY;
+        v[(NIV + nrv - 1) * b.ncell + p] = rho0 * ylast;
       }
   *DTmax_out = DTmax;
   if (max_steps) *max_steps = mxs;
@@ -1207,6 +1231,22 @@ void or_destroy(void* h) { delete static_cast<Ctx*>(h); }
 
 // The reference's run decomposed x into nblk equal MPI blocks: the shock
 // sensor of each block stops at its own last point (module_tools.f90:2761-2770).
+int or_set_chem_skip(void* h, int enable, const double* y1f, const double* y0o, int index_h2, int index_n2) {
+  Ctx* c = static_cast<Ctx*>(h);
+  const int nrv = c->b.nrv;
+  if (!enable) {
+    c->dvodesimp = false;
+    return IZEM_OK;
+  }
+  if (!y1f || !y0o || index_h2 < 0 || index_h2 >= nrv || index_n2 < 0 || index_n2 >= nrv || index_h2 == index_n2)
+    return IZEM_ERR_ARG;
+  for (int l = 0; l < nrv; ++l) { c->y1f[l] = y1f[l]; c->y0o[l] = y0o[l]; }
+  c->index_h2 = index_h2;
+  c->index_n2 = index_n2;
+  c->dvodesimp = true;
+  return IZEM_OK;
+}
+
 int or_set_sensor_xblocks(void* h, int nblk) {
   Ctx* c = static_cast<Ctx*>(h);
   if (nblk < 1 || c->b.nx % nblk) return IZEM_ERR_ARG;

@@ -1183,6 +1183,60 @@ __global__ void k_chem_scatter(ChemField f, const double* T, const double* Y, Ch
   if (f.dT_out) f.dT_out[q] = T[q] - T0;
 }
 
+// The dvodesimp selection of reaction_dvode (module_reaction.f90:173-215):
+// a gathered reactor goes to the integrator only if some species would move
+// by more than 1e-12 in dt at its initial production rates (psr_simp_chemkin:
+// CKWYR rates x molar mass x dt / rho, psr_simp_chemkin.f:31-42) and it is
+// neither the pure fuel nor the pure oxidiser (H2 and N2 both off by more
+// than 1e-6).  The selected reactors are appended to list.
+template <int KK>
+__global__ void k_chem_select(int n, const double* T, const double* rho, const double* Y, const double* dt,
+                              ChemSkip sk, int* list, unsigned* count) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  double y[KK], w[KK];
+#pragma unroll
+  for (int l = 0; l < KK; ++l) y[l] = Y[(long long)q * KK + l];
+  ck_wyr<KK>(rho[q], T[q], y, w);
+  const double myc = dt[q] / rho[q];
+  bool call_w = false;
+#pragma unroll
+  for (int l = 0; l < KK; ++l)
+    if (fabs(w[l] * c_mech.wt[l] * myc) > 1.0e-12) call_w = true;
+  const double yh = y[sk.ih2], yn = y[sk.in2];
+  const bool call_f = fabs(yh - sk.yf_h2) > 1.0e-6 && fabs(yn - sk.yf_n2) > 1.0e-6;
+  const bool call_o = fabs(yh - sk.yo_h2) > 1.0e-6 && fabs(yn - sk.yo_n2) > 1.0e-6;
+  if (call_w && call_f && call_o) list[atomicAdd(count, 1u)] = q;
+}
+
+// Selected reactors -> window with the dvodesimp branch's post-processing
+// (module_reaction.f90:219-245): as k_chem_scatter, except that the closing
+// species is clipped to [0, 1] as well.  Cells not in the list keep their
+// state and do not enter max |dT|.
+template <int KK>
+__global__ void k_chem_scatter_list(ChemField f, const int* list, const unsigned* count, const double* T,
+                                    const double* Y, ChemStats* stats) {
+  const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= *count) return;
+  const int q = list[t];
+  const long long p = window_point(f, (unsigned)q);
+  const long long nc = f.ncell;
+  const double rho0 = f.v[p];
+  const double T0 = f.T[p] * f.t_ref;
+  f.T[p] = T[q] * f.tref_i;
+  const double dT = fabs(T[q] - T0);
+  atomicMax(&stats->dtmax_bits, (unsigned long long)__double_as_longlong(dT));
+  double sumY = 0.0;
+#pragma unroll
+  for (int l = 0; l < KK - 1; ++l) {
+    const double Ya = fmin(fmax(Y[(long long)q * KK + l], 0.0), 1.0);
+    f.v[(5 + l) * nc + p] = rho0 * Ya;
+    sumY = sumY + Ya;
+  }
+  const double Yl = fmin(fmax(1.0 - sumY, 0.0), 1.0);
+  f.v[(5 + KK - 1) * nc + p] = rho0 * Yl;
+}
+
 // The persistent chemistry kernels come in variants that differ only in
 // the register budget the compiler is held to (128 threads per block, at
 // least MINB blocks resident per SM): fewer registers give more resident
@@ -1491,6 +1545,20 @@ cudaError_t chem_launch_batch(int n, double* T, const double* rho, double* Y, co
 cudaError_t chem_launch_gather(const ChemField& f, double* T, double* rho, double* Y, double* dt, cudaStream_t s) {
   const long long n = (long long)f.wx * f.wy * f.wz;
   k_chem_gather<9><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(f, T, rho, Y, dt);
+  return cudaGetLastError();
+}
+
+cudaError_t chem_launch_select(int n, const double* T, const double* rho, const double* Y, const double* dt,
+                               const ChemSkip& sk, int* list, unsigned* count, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_chem_select<9><<<(n + 127) / 128, 128, 0, s>>>(n, T, rho, Y, dt, sk, list, count);
+  return cudaGetLastError();
+}
+
+cudaError_t chem_launch_scatter_list(const ChemField& f, int n, const int* list, const unsigned* count,
+                                     const double* T, const double* Y, ChemStats* d_stats, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_chem_scatter_list<9><<<(n + 255) / 256, 256, 0, s>>>(f, list, count, T, Y, d_stats);
   return cudaGetLastError();
 }
 

@@ -38,6 +38,18 @@ cudaError_t chem_launch_batch(int n, double* T, const double* rho, double* Y, co
 // chemistry window <-> independent reactors (physical units)
 cudaError_t chem_launch_gather(const ChemField& f, double* T, double* rho, double* Y, double* dt, cudaStream_t s);
 cudaError_t chem_launch_scatter(const ChemField& f, const double* T, const double* Y, ChemStats* d_stats, cudaStream_t s);
+// dvodesimp (module_reaction.f90:173-251): the pure-stream compositions of
+// H2 and N2 and their species indices (0-based)
+struct ChemSkip {
+  double yf_h2, yf_n2, yo_h2, yo_n2;
+  int ih2, in2;
+};
+// gathered reactors that the skip test sends to the integrator -> list, count
+cudaError_t chem_launch_select(int n, const double* T, const double* rho, const double* Y, const double* dt,
+                               const ChemSkip& sk, int* list, unsigned* count, cudaStream_t s);
+// listed reactors -> window (the skip branch's clipping); n bounds *count
+cudaError_t chem_launch_scatter_list(const ChemField& f, int n, const int* list, const unsigned* count,
+                                     const double* T, const double* Y, ChemStats* d_stats, cudaStream_t s);
 
 // learned-surrogate support (chem.cu)
 // inputs of one network, or of both networks of an ensemble (d_norm2 and

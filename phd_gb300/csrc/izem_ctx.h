@@ -61,6 +61,13 @@ struct izem_ctx {
   int sur_stats[3] = {};                  // fallback cells, max BDF steps, failed
   float sur_ms[2] = {};                   // total, network
   long long sur_cells = 0;
+  // dvodesimp skip test for chemistry mode IZEM_CHEM_BDF (izem_gpu_set_chem_skip)
+  bool skip_on = false;
+  double skip_y[4] = {};                  // fuel H2, fuel N2, oxidiser H2, oxidiser N2
+  int skip_ih2 = 0, skip_in2 = 0;
+  int* b_list = nullptr;                  // selected reactors (sur_cap entries)
+  unsigned* d_list_count = nullptr;
+  long long list_cap = 0;
   int newton_warn = 0;
   std::string err;
 };

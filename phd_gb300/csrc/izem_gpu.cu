@@ -525,6 +525,7 @@ void izem_gpu_destroy(izem_ctx* c) {
   if (c->d_chem_stats) cudaFree(c->d_chem_stats);
   if (c->h_chem_stats) cudaFreeHost(c->h_chem_stats);
   cudaFree(c->b_T); cudaFree(c->b_rho); cudaFree(c->b_Y); cudaFree(c->b_dt);
+  cudaFree(c->b_list); cudaFree(c->d_list_count);
   if (c->h_status) cudaFreeHost(c->h_status);
   if (c->h_dt) cudaFreeHost(c->h_dt);
   for (auto& v : c->kt_pending)
@@ -745,6 +746,22 @@ int izem_gpu_chem_surrogate_stats(izem_ctx* c, long long* cells, int* fallback, 
   return IZEM_OK;
 }
 
+// The rest of reaction_selec after the reactors (module_reaction.f90:83-86):
+// upd_prim_var_woT, halo, boundaries, ghost primitives; then the statistics.
+static int chem_finish(izem_ctx* c, int mode, int sur_rc, double* DTmax) {
+  int rc = IZEM_DISPATCH(c, do_chem_after, c);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(c->h_chem_stats, c->d_chem_stats, sizeof(ChemStats), cudaMemcpyDeviceToHost, c->stream));
+  rc = read_status(c);
+  if (rc) return rc;
+  ChemStats& cs = *(ChemStats*)c->h_chem_stats;
+  if (mode == IZEM_CHEM_MLP) { cs.failed = c->sur_stats[2]; cs.max_steps = c->sur_stats[1]; }
+  std::memcpy(DTmax, &cs.dtmax_bits, sizeof(double));
+  if (cs.failed || sur_rc == IZEM_ERR_CHEM)
+    return ctx_fail(c, IZEM_ERR_CHEM, "stiff integration failed (ISTATE <= -2) on some cells", cudaSuccess);
+  return IZEM_OK;
+}
+
 int izem_gpu_chem_step(izem_ctx* c, double dt, int mode, double* DTmax) {
   if (!c || !DTmax) return IZEM_ERR_ARG;
   if (!c->have_mech) return ctx_fail(c, IZEM_ERR_STATE, "no mechanism set", cudaSuccess);
@@ -771,7 +788,8 @@ int izem_gpu_chem_step(izem_ctx* c, double dt, int mode, double* DTmax) {
   f.dt_phys = dt * c->adi.time_ref;
   CK(cudaMemsetAsync(c->d_chem_stats, 0, sizeof(ChemStats), c->stream));
   int sur_rc = IZEM_OK;
-  if (f.wx > 0 && f.wy > 0 && f.wz > 0 && mode == IZEM_CHEM_BDF) {
+  const bool skip = mode == IZEM_CHEM_BDF && c->skip_on;
+  if (f.wx > 0 && f.wy > 0 && f.wz > 0 && mode == IZEM_CHEM_BDF && !skip) {
     int rc = launch(c, "chem_psr", [&] { (void)chem_launch_field(f, c->d_counter, (ChemStats*)c->d_chem_stats, c->stream, 9); });
     if (rc) return rc;
   } else if (f.wx > 0 && f.wy > 0 && f.wz > 0) {
@@ -789,6 +807,33 @@ int izem_gpu_chem_step(izem_ctx* c, double dt, int mode, double* DTmax) {
     }
     int rc = launch(c, "chem_gather", [&] { (void)chem_launch_gather(f, c->b_T, c->b_rho, c->b_Y, c->b_dt, c->stream); });
     if (rc) return rc;
+    if (skip) {
+      // dvodesimp: select, integrate the selected reactors, write them back
+      if (n > c->list_cap) {
+        cudaFree(c->b_list);
+        c->b_list = nullptr;
+        CK(cudaMalloc(&c->b_list, n * sizeof(int)));
+        c->list_cap = n;
+      }
+      if (!c->d_list_count) CK(cudaMalloc(&c->d_list_count, sizeof(unsigned)));
+      CK(cudaMemsetAsync(c->d_list_count, 0, sizeof(unsigned), c->stream));
+      ChemSkip sk{c->skip_y[0], c->skip_y[1], c->skip_y[2], c->skip_y[3], c->skip_ih2, c->skip_in2};
+      rc = launch(c, "chem_select", [&] {
+        (void)chem_launch_select((int)n, c->b_T, c->b_rho, c->b_Y, c->b_dt, sk, c->b_list, c->d_list_count, c->stream);
+      });
+      if (rc) return rc;
+      rc = launch(c, "chem_psr", [&] {
+        (void)chem_launch_list(c->b_list, c->d_list_count, c->b_T, c->b_rho, c->b_Y, c->b_dt, c->d_counter,
+                               (ChemStats*)c->d_chem_stats, c->stream);
+      });
+      if (rc) return rc;
+      rc = launch(c, "chem_scatter", [&] {
+        (void)chem_launch_scatter_list(f, (int)n, c->b_list, c->d_list_count, c->b_T, c->b_Y,
+                                       (ChemStats*)c->d_chem_stats, c->stream);
+      });
+      if (rc) return rc;
+      return chem_finish(c, mode, sur_rc, DTmax);
+    }
     CK(cudaStreamSynchronize(c->stream));
     sur_rc = izem_gpu_psr_batch_mlp(c->sur_m, c->sur_m2, &c->mech, (int)n, c->b_T, c->b_rho, c->b_Y, c->b_dt, 1,
                                     c->sur_gate, c->sur_kncf.data(), c->sur_nele, nullptr, c->sur_stats, c->sur_ms);
@@ -798,16 +843,27 @@ int izem_gpu_chem_step(izem_ctx* c, double dt, int mode, double* DTmax) {
     rc = launch(c, "chem_scatter", [&] { (void)chem_launch_scatter(f, c->b_T, c->b_Y, (ChemStats*)c->d_chem_stats, c->stream); });
     if (rc) return rc;
   }
-  int rc = IZEM_DISPATCH(c, do_chem_after, c);
-  if (rc) return rc;
-  CK(cudaMemcpyAsync(c->h_chem_stats, c->d_chem_stats, sizeof(ChemStats), cudaMemcpyDeviceToHost, c->stream));
-  rc = read_status(c);
-  if (rc) return rc;
-  ChemStats& cs = *(ChemStats*)c->h_chem_stats;
-  if (mode == IZEM_CHEM_MLP) { cs.failed = c->sur_stats[2]; cs.max_steps = c->sur_stats[1]; }
-  std::memcpy(DTmax, &cs.dtmax_bits, sizeof(double));
-  if (cs.failed || sur_rc == IZEM_ERR_CHEM)
-    return ctx_fail(c, IZEM_ERR_CHEM, "stiff integration failed (ISTATE <= -2) on some cells", cudaSuccess);
+  return chem_finish(c, mode, sur_rc, DTmax);
+}
+
+int izem_gpu_set_chem_skip(izem_ctx* c, int enable, const double* Y_fuel, const double* Y_oxidizer, int index_h2,
+                           int index_n2) {
+  if (!c) return IZEM_ERR_ARG;
+  if (!enable) {
+    c->skip_on = false;
+    return IZEM_OK;
+  }
+  const int nrv = c->cfg.nrv;
+  if (!Y_fuel || !Y_oxidizer || index_h2 < 0 || index_h2 >= nrv || index_n2 < 0 || index_n2 >= nrv ||
+      index_h2 == index_n2)
+    return IZEM_ERR_ARG;
+  c->skip_y[0] = Y_fuel[index_h2];
+  c->skip_y[1] = Y_fuel[index_n2];
+  c->skip_y[2] = Y_oxidizer[index_h2];
+  c->skip_y[3] = Y_oxidizer[index_n2];
+  c->skip_ih2 = index_h2;
+  c->skip_in2 = index_n2;
+  c->skip_on = true;
   return IZEM_OK;
 }
 

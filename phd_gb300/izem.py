@@ -77,6 +77,7 @@ def load_library(path=None):
         "izem_gpu_autotune": (C.c_int, [P, C.c_double, C.c_char_p, C.c_int]),
         "izem_gpu_set_chem_variant": (C.c_int, [C.c_int]),
         "izem_gpu_set_sensor_xblocks": (C.c_int, [P, C.c_int]),
+        "izem_gpu_set_chem_skip": (C.c_int, [P, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_int]),
         "izem_gpu_chem_autotune": (C.c_int, [C.POINTER(IzemMech), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                                              C.c_void_p, C.c_int, C.c_char_p, C.c_int]),
         "izem_gpu_chem_surrogate_stats": (C.c_int, [P, C.POINTER(C.c_longlong), C.POINTER(C.c_int),
@@ -294,6 +295,19 @@ class IzemGPU:
         """Reproduce a reference run decomposed into nblk MPI blocks along x:
         the shock sensor is not shared between blocks (izem_gpu_set_sensor_xblocks)."""
         self._check(self.lib.izem_gpu_set_sensor_xblocks(self.h, int(nblk)), "set_sensor_xblocks")
+
+    def set_chem_skip(self, y_fuel=None, y_oxidizer=None, index_h2=0, index_n2=0, enable=True):
+        """[REACTING] DVODESIMP (izem_gpu_set_chem_skip): chemistry mode 0
+        integrates only the cells the skip test selects; y_fuel and
+        y_oxidizer are the pure-stream mass fractions, index_h2 and index_n2
+        0-based species indices.  enable=False integrates every cell again."""
+        if not enable:
+            self._check(self.lib.izem_gpu_set_chem_skip(self.h, 0, None, None, 0, 0), "set_chem_skip")
+            return
+        yf = np.ascontiguousarray(y_fuel, dtype=np.float64)
+        yo = np.ascontiguousarray(y_oxidizer, dtype=np.float64)
+        self._check(self.lib.izem_gpu_set_chem_skip(self.h, 1, yf.ctypes.data, yo.ctypes.data, int(index_h2),
+                                                    int(index_n2)), "set_chem_skip")
 
     def set_chem_variant(self, v):
         """Pin the register-budget variant (0..4) of the persistent chemistry

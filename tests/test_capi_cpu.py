@@ -86,3 +86,4 @@ def test_entry_points_reject_bad_arguments_before_any_device_call():
     assert lib.izem_gpu_chem_autotune(C.byref(mech), 0, p, p, p, p, 0, None, 0) == 1
     cnt = C.c_int()
     assert lib.izem_mlp_fallback_cells(None, None, 0, C.byref(cnt)) == 1
+    assert lib.izem_gpu_set_chem_skip(None, 1, p, p, 0, 8) == 1

@@ -122,3 +122,45 @@ def test_device_rhs_with_reciprocals_matches_reference_order(tmp_path):
     assert np.array_equal(zf[:, scale == 0], zr[:, scale == 0])   # components that stay exactly zero
     err = (np.abs(zf - zr) / np.where(scale == 0, 1.0, scale)).max(axis=0)
     assert np.all(err < 1e-12), err
+
+
+def _window(cfg):
+    """reaction_dvode's window (module_reaction.f90:155-159) as slices of the
+    ghosted arrays; its z bound uses ey."""
+    ng = cfg.ng
+    hi = (min(cfg.nx, cfg.nx - ng - 1), min(cfg.ny, cfg.ny - ng - 1), min(cfg.ny, cfg.nz - ng - 1))
+    return tuple(slice(2 * ng, ng + h) for h in hi)
+
+
+def test_dvodesimp_skips_pure_streams_and_keeps_the_rest():
+    """dvodesimp (module_reaction.f90:173-251): window cells in the pure fuel
+    or oxidiser streams (H2 or N2 within 1e-6 of the stream's) keep v and T
+    to the bit; the others get the full path's result, with the closing
+    species clipped; max |dT| comes from the integrated cells only."""
+    import workloads as W
+    m = h2_mechanism()
+    cfg, thd, adi, dxi, st, orc, (yf, yo, ih2, in2) = W.mixing_layer_with_streams()
+    st0 = W.copy(st)
+    full = W.copy(st)
+    dtm_full = orc.chem_step(full, m, 0.5)
+    orc.set_chem_skip(yf, yo, ih2, in2)
+    skip = W.copy(st)
+    dtm_skip = orc.chem_step(skip, m, 0.5)
+    w = _window(cfg)
+    v0 = st0["v"][w]
+    Y = v0[..., 5:] / v0[..., :1]
+    pure = ~((np.abs(Y[..., ih2] - yf[ih2]) > 1e-6) & (np.abs(Y[..., in2] - yf[in2]) > 1e-6)
+             & (np.abs(Y[..., ih2] - yo[ih2]) > 1e-6) & (np.abs(Y[..., in2] - yo[in2]) > 1e-6))
+    moved = np.any(skip["v"][w] != v0, axis=-1) | (skip["T"][w] != st0["T"][w])
+    assert 0 < pure.sum() < pure.size and not np.any(moved & pure)
+    called = ~np.all(skip["v"][w][..., 5:] == v0[..., 5:], axis=-1) | (skip["T"][w] != st0["T"][w])
+    assert called.sum() > 0
+    assert np.array_equal(skip["T"][w][called], full["T"][w][called])
+    assert np.array_equal(skip["v"][w][called][:, :13], full["v"][w][called][:, :13])
+    assert np.allclose(skip["v"][w][called][:, 13], full["v"][w][called][:, 13], rtol=1e-15, atol=0)
+    T_ref = adi.t_ref
+    dT = np.abs(skip["T"][w] - st0["T"][w]) * T_ref
+    assert dtm_skip <= dtm_full and abs(dtm_skip - dT.max()) <= 1e-9 * max(dT.max(), 1e-30)
+    orc.set_chem_skip(enable=False)
+    again = W.copy(st)
+    assert orc.chem_step(again, m, 0.5) == dtm_full and np.array_equal(again["v"], full["v"])

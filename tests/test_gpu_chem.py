@@ -87,3 +87,40 @@ def test_chem_autotune_batch_leaves_inputs_and_keeps_results():
     rT = np.abs(Tg - To) / (RTOL * np.abs(To) + ATOL)
     assert rT.max() <= 100 and np.percentile(rT, 99) <= 10
     assert (np.abs(Yg - Yo) / np.abs(Yo).max(axis=0)).max() <= 1e-3
+
+
+def test_dvodesimp_matches_oracle():
+    """dvodesimp (module_reaction.f90:173-251) on the device: the same cells
+    are left alone as by the oracle (v and T unchanged to the bit), the
+    integrated ones agree within the bounds above, and max |dT| comes from
+    them; disabling the skip restores the integration of every cell."""
+    m = h2_mechanism()
+    cfg, thd, adi, dxi, st, orc, (yf, yo, ih2, in2) = W.mixing_layer_with_streams()
+    st0 = W.copy(st)
+    orc.set_chem_skip(yf, yo, ih2, in2)
+    dtm_o = orc.chem_step(st, m, 0.5)
+    g = IzemGPU(cfg, thd, adi)
+    g.set_grid(*dxi)
+    g.upload(**st0)
+    g.set_mechanism(m)
+    g.set_chem_skip(yf, yo, ih2, in2)
+    dtm_g = g.reaction_selec(0.5)
+    got = g.download()
+    i = (slice(3, -3),) * 3
+    same_o = np.all(st["v"][i] == st0["v"][i], axis=-1) & (st["T"][i] == st0["T"][i])
+    same_g = np.all(got["v"][i] == st0["v"][i], axis=-1) & (got["T"][i] == st0["T"][i])
+    assert np.array_equal(same_g, same_o) and 0 < same_o.sum() < same_o.size
+    T_o, T_g = st["T"][i], got["T"][i]
+    assert np.all(np.abs(T_g - T_o) <= 100 * (RTOL * np.abs(T_o) + ATOL))
+    for q in range(5, 14):
+        yo_, yg_ = st["v"][i][..., q] / st["v"][i][..., 0], got["v"][i][..., q] / got["v"][i][..., 0]
+        assert np.all(np.abs(yg_ - yo_) <= 1e-3 * np.abs(yo_).max() + ATOL)
+    assert abs(dtm_g - dtm_o) <= 100 * (RTOL * 3000 + ATOL)
+    assert g.chem_stats()["failed"] == 0
+    g.set_chem_skip(enable=False)
+    g.upload(**st0)
+    g.reaction_selec(0.5)
+    allc = g.download()
+    g.close()
+    assert np.sum(~(np.all(allc["v"][i] == st0["v"][i], axis=-1) & (allc["T"][i] == st0["T"][i]))) >= \
+        np.sum(~same_o)

@@ -63,3 +63,21 @@ def normwise(a, b, floor=1e-6):
     den = np.maximum(den, floor * den.max())
     den = np.where(den == 0, 1.0, den)
     return num / den
+
+
+def mixing_layer_with_streams(nx=12, ny=24, nz=8):
+    """A mixing layer whose y extent (12 mm, 24 points) reaches the pure fuel
+    and oxidiser streams: the chemistry window holds cells that the
+    dvodesimp skip test leaves alone.  Returns cfg, thd, adi, dxi, state,
+    oracle and the skip data (pure-stream mass fractions, H2 and N2
+    indices)."""
+    cfg, thd, adi, dxi, st, info = ics.mixing_layer(nx, ny, nz, Lx=nx * 47e-6, Ly=12e-3, Lz=nz * 47e-6,
+                                                     lib_dscalar=oracle.metrics_dscalar)
+    cfg.reaction = 1
+    orc = oracle.Oracle(cfg, thd, adi, *dxi)
+    orc.finalize_ic(st)
+    names = load_species("h2air9")["names"]
+    ih2, in2 = names.index("H2"), names.index("N2")
+    yf = np.zeros(9); yf[ih2] = 0.5; yf[in2] = 0.5
+    yo = np.zeros(9); yo[names.index("O2")] = 0.233; yo[in2] = 0.767
+    return cfg, thd, adi, dxi, st, orc, (yf, yo, ih2, in2)
