@@ -239,6 +239,18 @@ int  izem_gpu_chem_step(izem_ctx* ctx, double dt, int mode, double* DTmax);
  * four of its five arguments; this is the routine's stated semantics. */
 int  izem_gpu_set_chem_skip(izem_ctx* ctx, int enable, const double* Y_fuel, const double* Y_oxidizer,
                             int index_h2, int index_n2);
+
+/* [IFLES] LES = T with MU_SGS_MODEL = SMAGORINSKY under EGLIB: the viscous
+ * fluxes of viscflux_eg_LES_xyz (module_eg_lib.f90:2687-3352) with
+ * mu_SGS_smagorinsky (module_SGS_models.f90:176-304), MU_SGS_FACTOR,
+ * SC_SGS, PR_SGS and the shock-detector threshold PERCENT_WEIGHT_SGS
+ * (shock_det_slv, module_tools.f90:1945-2085).  TAU_ISO_SGS_SWITCH = F (the
+ * deck default): the isotropic SGS tensor is not built.  Needs cfg.vis,
+ * cfg.eglib and ndim = 3; enable = 0 restores the laminar fluxes.  The time
+ * step is unchanged: the reference's mu_SGS array seen by timestep stays 0
+ * under EGLIB. */
+int  izem_gpu_set_les(izem_ctx* ctx, int enable, double mu_sgs_factor, double sc_sgs, double pr_sgs,
+                      double percent_weight_sgs);
 /* Statistics of the last chemistry step: cells whose integration failed
  * (ISTATE <= -2), largest and summed BDF step counts. */
 int  izem_gpu_chem_stats(izem_ctx* ctx, int* failed, int* max_steps, unsigned long long* total_steps);

@@ -33,6 +33,7 @@ def load():
         "or_destroy": (None, [P]),
         "or_set_sensor_xblocks": (C.c_int, [P, C.c_int]),
         "or_set_chem_skip": (C.c_int, [P, C.c_int, _dp, _dp, C.c_int, C.c_int]),
+        "or_set_les": (C.c_int, [P, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double]),
         "or_last_error": (C.c_int, [P, C.c_char_p, C.c_int]),
         "or_cp_scalar": (None, [P, C.c_double, _dp, _dp]),
         "or_ha_scalar": (None, [P, C.c_double, _dp]),
@@ -162,6 +163,11 @@ class Oracle:
         """Emulate a run whose x direction was split into nblk MPI blocks:
         the shock sensor does not compare points across block edges."""
         self._rc(self.lib.or_set_sensor_xblocks(self.h, int(nblk)), "set_sensor_xblocks")
+
+    def set_les(self, mu_sgs_factor=0.18, sc_sgs=0.7, pr_sgs=0.7, percent_weight_sgs=70.0, enable=True):
+        """LES with the Smagorinsky closure under EGLIB (viscflux_eg_LES_xyz)."""
+        self._rc(self.lib.or_set_les(self.h, int(bool(enable)), float(mu_sgs_factor), float(sc_sgs), float(pr_sgs),
+                                     float(percent_weight_sgs)), "set_les")
 
     def set_chem_skip(self, y_fuel=None, y_oxidizer=None, index_h2=0, index_n2=0, enable=True):
         """dvodesimp: integrate only the cells that the skip test selects

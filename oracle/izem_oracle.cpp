@@ -66,6 +66,10 @@ struct Ctx {
   int sensor_xblocks = 1;   // x-blocks of the reference's MPI run whose edges the sensor does not cross
   // dvodesimp (module_reaction.f90:173-251): pure fuel Y1f and oxidiser Y0o,
   // H2 and N2 species indices (0-based)
+  // LES with the Smagorinsky closure under EGLIB (or_set_les): MU_SGS_FACTOR,
+  // SC_SGS, PR_SGS, PERCENT_WEIGHT_SGS
+  bool les = false;
+  double les_factor = 0.0, les_sc_sgs = 1.0, les_pr_sgs = 1.0, les_pw = 0.0;
   bool dvodesimp = false;
   double y1f[IZEM_NSMAX] = {}, y0o[IZEM_NSMAX] = {};
   int index_h2 = 0, index_n2 = 0;
@@ -1004,7 +1008,7 @@ int visc_flux(Ctx& c, const double* v, const double* T, const double* W_i, const
               double* fl) {
   if (c.cfg.eglib) {
     if (!c.eg) { c.err = "EGLIB transport requested but no linking data set"; return IZEM_ERR_STATE; }
-    return visc_flux_eg(c, *c.eg, v, T, W_i, ha, fl);
+    return visc_flux_eg(c, *c.eg, v, T, W_i, cp, ha, fl);
   }
   return visc_flux_fit(c, v, T, W_i, cp, ha, fl);
 }
@@ -1231,6 +1235,23 @@ void or_destroy(void* h) { delete static_cast<Ctx*>(h); }
 
 // The reference's run decomposed x into nblk equal MPI blocks: the shock
 // sensor of each block stops at its own last point (module_tools.f90:2761-2770).
+int or_set_les(void* h, int enable, double mu_sgs_factor, double sc_sgs, double pr_sgs, double percent_weight_sgs) {
+  Ctx* c = static_cast<Ctx*>(h);
+  if (!enable) {
+    c->les = false;
+    return IZEM_OK;
+  }
+  if (!c->cfg.vis || !c->cfg.eglib || c->cfg.ndim != 3 || !(mu_sgs_factor >= 0.0) || !(sc_sgs > 0.0) ||
+      !(pr_sgs > 0.0) || !(percent_weight_sgs >= 0.0))
+    return IZEM_ERR_ARG;
+  c->les_factor = mu_sgs_factor;
+  c->les_sc_sgs = sc_sgs;
+  c->les_pr_sgs = pr_sgs;
+  c->les_pw = percent_weight_sgs;
+  c->les = true;
+  return IZEM_OK;
+}
+
 int or_set_chem_skip(void* h, int enable, const double* y1f, const double* y0o, int index_h2, int index_n2) {
   Ctx* c = static_cast<Ctx*>(h);
   const int nrv = c->b.nrv;

@@ -68,6 +68,10 @@ struct izem_ctx {
   int* b_list = nullptr;                  // selected reactors (sur_cap entries)
   unsigned* d_list_count = nullptr;
   long long list_cap = 0;
+  // LES closure (izem_gpu_set_les)
+  bool les_on = false;
+  double les_cs2 = 0.0, les_sc_sgs_i = 0.0, les_pr_sgs_i = 0.0, les_pw = 0.0;
+  double* les = nullptr;                  // 4 ghosted components (W_i gradient, criterion)
   int newton_warn = 0;
   std::string err;
 };

@@ -201,10 +201,32 @@ int enq_visc(izem_ctx* c) {
     return rc;
   if (eg && (rc = launch(c, "visc_grad_p", [&] { k_grad_p<NRV><<<grid_for(g.nint), kThreads, 0, c->stream>>>(g, mt, c->prim, c->fd); })))
     return rc;
+  const bool les = eg && c->les_on;
+  if (les && (rc = launch(c, "les_prep", [&] {
+                k_les_prep<<<grid_for(g.nint), kThreads, 0, c->stream>>>(g, mt, c->v, c->T, c->W_i, c->les_pw, c->les);
+              })))
+    return rc;
   long long ns = slab_count(g) - g.nint;
   if ((rc = launch(c, "visc_wrap", [&] { k_wrap_periodic<<<grid_for(ns), kThreads, 0, c->stream>>>(g, nderiv, c->fd); })))
     return rc;
-  if (eg) {
+  if (les && (rc = launch(c, "les_wrap", [&] { k_wrap_periodic<<<grid_for(ns), kThreads, 0, c->stream>>>(g, 4, c->les); })))
+    return rc;
+  if (les) {
+    SgsArgs sa;
+    sa.les = c->les;
+    sa.cp = c->cp;
+    for (int d = 0; d < 3; ++d) sa.dxi[d] = c->dxi[d];
+    sa.cs2 = c->les_cs2;
+    sa.sc = c->adi.sc;
+    sa.sc_sgs_i = c->les_sc_sgs_i;
+    sa.pr_sgs_i = c->les_pr_sgs_i;
+    const long long ns_all = slab_count(g);
+    if ((rc = launch(c, "visc_point_eg", [&] {
+           k_visc_point_eg<NRV, true><<<grid_for(ns_all, c->tb_visc), c->tb_visc, 0, c->stream>>>(
+               g, c->v, c->T, c->W_i, c->ha, c->Xa, c->prim, c->fd, c->tau, c->qv, sa);
+         })))
+      return rc;
+  } else if (eg) {
     const long long ns_all = slab_count(g);
     if ((rc = launch(c, "visc_point_eg", [&] {
            k_visc_point_eg<NRV><<<grid_for(ns_all, c->tb_visc), c->tb_visc, 0, c->stream>>>(g, c->v, c->T, c->W_i, c->ha, c->Xa,
@@ -525,7 +547,7 @@ void izem_gpu_destroy(izem_ctx* c) {
   if (c->d_chem_stats) cudaFree(c->d_chem_stats);
   if (c->h_chem_stats) cudaFreeHost(c->h_chem_stats);
   cudaFree(c->b_T); cudaFree(c->b_rho); cudaFree(c->b_Y); cudaFree(c->b_dt);
-  cudaFree(c->b_list); cudaFree(c->d_list_count);
+  cudaFree(c->b_list); cudaFree(c->d_list_count); cudaFree(c->les);
   if (c->h_status) cudaFreeHost(c->h_status);
   if (c->h_dt) cudaFreeHost(c->h_dt);
   for (auto& v : c->kt_pending)
@@ -1009,6 +1031,34 @@ int izem_gpu_set_sensor_xblocks(izem_ctx* c, int nblk) {
   c->sensor_bx = c->cfg.nx / nblk;
   c->nedge = (long long)(nblk - 1) * c->cfg.ny * c->cfg.nz;
   if (c->nedge > 0) CK(cudaMalloc(&c->fhat_edge, (size_t)c->nv * c->nedge * sizeof(double)));
+  return IZEM_OK;
+}
+
+int izem_gpu_set_les(izem_ctx* c, int enable, double mu_sgs_factor, double sc_sgs, double pr_sgs,
+                     double percent_weight_sgs) {
+  if (!c) return IZEM_ERR_ARG;
+  // the captured RK3 graph holds the other viscous kernel
+  if (c->graph_exec) { cudaGraphExecDestroy(c->graph_exec); c->graph_exec = nullptr; }
+  if (c->graph) { cudaGraphDestroy(c->graph); c->graph = nullptr; }
+  if (!enable) {
+    c->les_on = false;
+    return IZEM_OK;
+  }
+  if (!c->cfg.vis || !c->cfg.eglib || c->cfg.ndim != 3)
+    return ctx_fail(c, IZEM_ERR_ARG, "LES closure needs VIS, EGLIB and a 3-D block", cudaSuccess);
+  if (!(mu_sgs_factor >= 0.0) || !(sc_sgs > 0.0) || !(pr_sgs > 0.0) || !(percent_weight_sgs >= 0.0))
+    return ctx_fail(c, IZEM_ERR_ARG, "LES parameters out of range", cudaSuccess);
+  if (!c->les) {
+    CK(cudaMalloc(&c->les, 4 * (size_t)c->g.ncell * sizeof(double)));
+    CK(cudaMemset(c->les, 0, 4 * (size_t)c->g.ncell * sizeof(double)));
+  }
+  double cs2 = mu_sgs_factor;
+  cs2 = cs2 * cs2 / c->adi.sqgmr;
+  c->les_cs2 = cs2;
+  c->les_sc_sgs_i = 1.0 / sc_sgs;
+  c->les_pr_sgs_i = 1.0 / pr_sgs;
+  c->les_pw = percent_weight_sgs;
+  c->les_on = true;
   return IZEM_OK;
 }
 

@@ -431,15 +431,76 @@ __global__ void k_grad_p(Geo g, Metrics mt, const double* __restrict__ prim, dou
   }
 }
 
+// Smagorinsky closure of viscflux_eg_LES_xyz (module_eg_lib.f90:2687-3352)
+// with mu_SGS_smagorinsky (module_SGS_models.f90:176-304); the isotropic SGS
+// tensor is off (TAU_ISO_SGS_SWITCH = F), so its terms add exactly zero.
+struct SgsArgs {
+  const double* les;     // 4 ghosted components: dW_i/dx, dW_i/dy, dW_i/dz, shock-detector criterion
+  const double* cp;      // ghosted cp (code units)
+  const double* dxi[3];  // inverse spacings, ghosted index
+  double cs2;            // MU_SGS_FACTOR^2 / sqgmr
+  double sc;             // Sc of the reference scales
+  double sc_sgs_i, pr_sgs_i;   // 1 / SC_SGS, 1 / PR_SGS
+};
+
+// The W_i gradients of viscflux_eg_LES_xyz (dx_fixed1 etc., module_eg_lib.f90:
+// 2866-2871) and the criterion of shock_det_slv (module_tools.f90:1945-2085)
+// at the interior points: 0 where, on the 2 ng-point stencil of the point's
+// x or y face, the relative density jump and the relative pressure jump of
+// some neighbour pair both exceed PERCENT_WEIGHT_SGS, else 1.  The
+// reference's z pass writes with the y pass's final j_l and the final k, a
+// ghost corner that no later step reads, so only the x and y passes shape
+// the criterion.  3-D only.
+__global__ void k_les_prep(Geo g, Metrics mt, const double* __restrict__ v, const double* __restrict__ T,
+                           const double* __restrict__ W_i, double pw, double* __restrict__ les) {
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= g.nint) return;
+  int c[3];
+  c[0] = (int)(idx % g.n[0]) + 1;
+  long long r = idx / g.n[0];
+  c[1] = (int)(r % g.n[1]) + 1;
+  c[2] = (int)(r / g.n[1]) + 1;
+  const long long nc = g.ncell;
+  const long long p = gid(g, c[0], c[1], c[2]);
+  const long long strides[3] = {1LL, (long long)g.g[0], (long long)g.g[0] * g.g[1]};
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const double di = mt.dxi[d][c[d] - 1 + g.ng];
+    les[d * nc + p] = deriv_at(W_i, p, strides[d], c[d], g.n[d], g.bnd[2 * d], g.bnd[2 * d + 1], di, g.ng);
+  }
+  double crit = 1.0;
+  for (int d = 0; d < 2; ++d)
+    for (int st = 1; st <= 2 * g.ng; ++st) {
+      const int s = c[d] + st - g.ng;           // i_s, from c - ng + 1 to c + ng
+      const int sp = min(s + 1, g.n[d]);        // min(i_s + 1, ex)
+      const long long pa = p + (long long)(s - c[d]) * strides[d];
+      const long long pb = p + (long long)(sp - c[d]) * strides[d];
+      const double drho = fabs(v[pb] - v[pa]) / fmin(v[pb], v[pa]);
+      const double pp = v[pb] * T[pb] * W_i[pb];
+      const double pm = v[pa] * T[pa] * W_i[pa];
+      const double dpres = fabs(pp - pm) / fmin(pp, pm);
+      if (drho > pw && dpres > pw) crit = 0.0;
+    }
+  les[3 * nc + p] = crit;
+}
+
 // egvars + the stresses, rho Y_k V_k and heat flux of viscflux_eg_xyz at
 // interior points and the ghost slabs of periodic faces.  Writes tau (6),
-// q (3) and overwrites the species gradients of fd with rho Y_k V_k.
-template <int NRV>
+// q (3) and overwrites the species gradients of fd with rho Y_k V_k.  With
+// LES the terms of viscflux_eg_LES_xyz (module_eg_lib.f90:3017-3239): the
+// divergence gets the stresses scaled by 1 + mu_SGS / mu, the species
+// fluxes the SGS diffusion and W_i-gradient terms, the heat flux the SGS
+// conductivity mu_SGS cp / Pr_SGS; the work term keeps the molecular
+// stresses.  The reference reuses its temperature-gradient scalar wrk1 for
+// the SGS factor of each species, so the x thermal-diffusion term of species
+// l >= 2 uses the SGS factor of species l - 1; that is reproduced.
+template <int NRV, bool LES = false>
 __global__ void __launch_bounds__(256) k_visc_point_eg(Geo g, const double* __restrict__ v,
                                                        const double* __restrict__ T, const double* __restrict__ W_i,
                                                        const double* __restrict__ ha, const double* __restrict__ Xa,
                                                        const double* __restrict__ prim, double* __restrict__ fd,
-                                                       double* __restrict__ tau, double* __restrict__ qv) {
+                                                       double* __restrict__ tau, double* __restrict__ qv,
+                                                       SgsArgs sa = SgsArgs{}) {
   long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   int i, j, k, dom;
   if (!slab_point(g, idx, i, j, k, dom)) return;
@@ -472,16 +533,28 @@ __global__ void __launch_bounds__(256) k_visc_point_eg(Geo g, const double* __re
   const double syy = bulk + twothirds * rmu * (F(5) + F(5) - (F(1) + F(9)));
   const double syz = rmu * (F(8) + F(6));
   const double szz = bulk + twothirds * rmu * (F(9) + F(9) - (F(1) + F(5)));
+  double mu_sgs = 0.0;
+  if constexpr (LES) {
+    const double dxv = sa.dxi[0][i - 1 + g.ng], dyv = sa.dxi[1][j - 1 + g.ng], dzv = sa.dxi[2][k - 1 + g.ng];
+    const double delta = 1.0 / pow(dxv * dyv * dzv, 1.0 / 3.0);
+    const double s11 = F(1), s12 = 0.5 * (F(2) + F(4)), s13 = 0.5 * (F(3) + F(7));
+    const double s22 = F(5), s23 = 0.5 * (F(6) + F(8)), s33 = F(9);
+    double sb = s11 * s11 + s12 * s12 + s13 * s13 + s12 * s12 + s22 * s22 + s23 * s23 + s13 * s13 + s23 * s23 +
+                s33 * s33;
+    sb = sqrt(sb + sb);
+    mu_sgs = rho * sa.cs2 * (delta * delta) * sb * sa.les[3 * nc + p];
+  }
   const double Ps = 1.0 / prim[PR_P * nc + p];
   const double Ts = 1.0 / Tp;
   const double w1 = F(10) * Ts, w2 = F(11) * Ts, w3 = F(12) * Ts;
   const double w4 = fd[(12 + 3 * NRV) * nc + p] * Ps;
   const double w5 = fd[(13 + 3 * NRV) * nc + p] * Ps;
   const double w6 = fd[(14 + 3 * NRV) * nc + p] * Ps;
-  double dx[NRV], dy[NRV], dz[NRV], xt[NRV];
+  double dx[NRV], dy[NRV], dz[NRV], xt[NRV], xa[NRV];
 #pragma unroll
   for (int l = 0; l < NRV; ++l) {
     const double X = Xa[l * nc + p];
+    xa[l] = X;
     const double xy = X - v[(IZEM_NIV + l) * nc + p] * rho_i;
     dx[l] = F(13 + 3 * l) + xy * w4;
     dy[l] = F(14 + 3 * l) + xy * w5;
@@ -491,19 +564,31 @@ __global__ void __launch_bounds__(256) k_visc_point_eg(Geo g, const double* __re
   const double rvd0 = c_thd.rvd0;
   const double uxs = v[nc + p] * rho_i, vys = v[2 * nc + p] * rho_i, wzs = v[3 * nc + p] * rho_i;
   double sx = 0.0, sy = 0.0, sz = 0.0;
+  const double dm_sgs = mu_sgs * rho_i * sa.sc_sgs_i;
+  double w1c = w1;   // the reference's wrk1
 #pragma unroll
   for (int l = 0; l < NRV; ++l) {
     double jx = 0.0, jy = 0.0, jz = 0.0;
 #pragma unroll
     for (int m = 0; m < NRV; ++m) {
       const double r = rd[l * NRV + m] * c_eg.rd_adim;
-      jx = jx + r * (dx[m] + xt[m] * w1);
+      jx = jx + r * (dx[m] + xt[m] * (LES ? w1c : w1));
       jy = jy + r * (dy[m] + xt[m] * w2);
       jz = jz + r * (dz[m] + xt[m] * w3);
     }
-    jx = -rvd0 * jx;
-    jy = -rvd0 * jy;
-    jz = -rvd0 * jz;
+    if constexpr (LES) {
+      const double wk = rho * dm_sgs * sa.sc * c_thd.Wc[l];
+      const double fw = 1.0 + wk * Wi;
+      const double wx = wk * xa[l];
+      jx = -rvd0 * (jx * fw + wx * sa.les[p]);
+      jy = -rvd0 * (jy * fw + wx * sa.les[nc + p]);
+      jz = -rvd0 * (jz * fw + wx * sa.les[2 * nc + p]);
+      w1c = wk;
+    } else {
+      jx = -rvd0 * jx;
+      jy = -rvd0 * jy;
+      jz = -rvd0 * jz;
+    }
     fd[(long long)(12 + 3 * l) * nc + p] = jx;
     fd[(long long)(13 + 3 * l) * nc + p] = jy;
     fd[(long long)(14 + 3 * l) * nc + p] = jz;
@@ -512,9 +597,18 @@ __global__ void __launch_bounds__(256) k_visc_point_eg(Geo g, const double* __re
     sy = sy + jy * h;
     sz = sz + jz * h;
   }
-  const double wl = -c_thd.rlam0 * ct;
-  tau[0 * nc + p] = sxx; tau[1 * nc + p] = sxy; tau[2 * nc + p] = sxz;
-  tau[3 * nc + p] = syy; tau[4 * nc + p] = syz; tau[5 * nc + p] = szz;
+  double wl;
+  if constexpr (LES) {
+    const double ct_sgs = mu_sgs * sa.cp[p] * sa.pr_sgs_i;
+    wl = -c_thd.rlam0 * (ct + ct_sgs);
+    const double fs = 1.0 + -c_thd.sqgmr * mu_sgs / rmu;
+    tau[0 * nc + p] = bulk + (sxx - bulk) * fs; tau[1 * nc + p] = sxy * fs; tau[2 * nc + p] = sxz * fs;
+    tau[3 * nc + p] = bulk + (syy - bulk) * fs; tau[4 * nc + p] = syz * fs; tau[5 * nc + p] = bulk + (szz - bulk) * fs;
+  } else {
+    wl = -c_thd.rlam0 * ct;
+    tau[0 * nc + p] = sxx; tau[1 * nc + p] = sxy; tau[2 * nc + p] = sxz;
+    tau[3 * nc + p] = syy; tau[4 * nc + p] = syz; tau[5 * nc + p] = szz;
+  }
   qv[0 * nc + p] = sx + wl * F(10) + uxs * sxx + vys * sxy + wzs * sxz;
   qv[1 * nc + p] = sy + wl * F(11) + uxs * sxy + vys * syy + wzs * syz;
   qv[2 * nc + p] = sz + wl * F(12) + uxs * sxz + vys * syz + wzs * szz;

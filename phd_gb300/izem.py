@@ -78,6 +78,7 @@ def load_library(path=None):
         "izem_gpu_set_chem_variant": (C.c_int, [C.c_int]),
         "izem_gpu_set_sensor_xblocks": (C.c_int, [P, C.c_int]),
         "izem_gpu_set_chem_skip": (C.c_int, [P, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_int]),
+        "izem_gpu_set_les": (C.c_int, [P, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double]),
         "izem_gpu_chem_autotune": (C.c_int, [C.POINTER(IzemMech), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                                              C.c_void_p, C.c_int, C.c_char_p, C.c_int]),
         "izem_gpu_chem_surrogate_stats": (C.c_int, [P, C.POINTER(C.c_longlong), C.POINTER(C.c_int),
@@ -295,6 +296,12 @@ class IzemGPU:
         """Reproduce a reference run decomposed into nblk MPI blocks along x:
         the shock sensor is not shared between blocks (izem_gpu_set_sensor_xblocks)."""
         self._check(self.lib.izem_gpu_set_sensor_xblocks(self.h, int(nblk)), "set_sensor_xblocks")
+
+    def set_les(self, mu_sgs_factor=0.18, sc_sgs=0.7, pr_sgs=0.7, percent_weight_sgs=70.0, enable=True):
+        """[IFLES] LES = T, MU_SGS_MODEL = SMAGORINSKY under EGLIB
+        (izem_gpu_set_les); the deck defaults are the keyword defaults."""
+        self._check(self.lib.izem_gpu_set_les(self.h, int(bool(enable)), float(mu_sgs_factor), float(sc_sgs),
+                                              float(pr_sgs), float(percent_weight_sgs)), "set_les")
 
     def set_chem_skip(self, y_fuel=None, y_oxidizer=None, index_h2=0, index_n2=0, enable=True):
         """[REACTING] DVODESIMP (izem_gpu_set_chem_skip): chemistry mode 0

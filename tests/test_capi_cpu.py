@@ -87,3 +87,5 @@ def test_entry_points_reject_bad_arguments_before_any_device_call():
     cnt = C.c_int()
     assert lib.izem_mlp_fallback_cells(None, None, 0, C.byref(cnt)) == 1
     assert lib.izem_gpu_set_chem_skip(None, 1, p, p, 0, 8) == 1
+    lib.izem_gpu_set_les.argtypes = [C.c_void_p, C.c_int] + [C.c_double] * 4
+    assert lib.izem_gpu_set_les(None, 1, 0.18, 0.7, 0.7, 70.0) == 1

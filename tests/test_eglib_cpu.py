@@ -109,3 +109,36 @@ def test_eglib_species_fluxes_sum_to_zero():
     orc0.visc_flux(st0, fl0)
     rel = np.abs(fl[..., 1:4] - fl0[..., 1:4]).max() / np.abs(fl0[..., 1:4]).max()
     assert rel < 0.1, rel
+
+
+def _les_flux(factor=None, pw=70.0):
+    cfg, thd, adi, dxi, st, info, orc = W.case("mix", 12, eglib=True)
+    W.perturb(st, 0.01, seed=5)
+    orc.update_primitives(st)
+    if factor is not None:
+        orc.set_les(mu_sgs_factor=factor, percent_weight_sgs=pw)
+    fl = np.zeros((cfg.nx, cfg.ny, cfg.nz, 5 + cfg.nrv), order="F")
+    orc.visc_flux(st, fl)
+    return fl
+
+
+def test_les_closure_in_the_oracle():
+    """viscflux_eg_LES_xyz with the Smagorinsky viscosity (module_eg_lib.f90:
+    2687-3352):
+    * MU_SGS_FACTOR = 0: the momentum fluxes equal the laminar ones to the
+      bit (the stresses are scaled by 1 + 0); the species and energy fluxes
+      still differ, through the reference's reuse of its temperature-gradient
+      scalar for the SGS factor in the x thermal-diffusion term of species
+      l >= 2;
+    * a shock-detector threshold below every relative jump of the perturbed
+      field zeroes mu_SGS everywhere: the same fluxes as MU_SGS_FACTOR = 0;
+    * the deck defaults (0.18, threshold 70: no point detected) change the
+      momentum fluxes by the SGS stresses."""
+    lam = _les_flux()
+    zero = _les_flux(0.0)
+    assert np.array_equal(zero[..., 1:4], lam[..., 1:4])
+    assert not np.array_equal(zero[..., 5:], lam[..., 5:])
+    assert np.array_equal(_les_flux(0.18, pw=1e-14), zero)
+    smag = _les_flux(0.18)
+    rel = np.abs(smag[..., 1:4] - lam[..., 1:4]).max() / np.abs(lam[..., 1:4]).max()
+    assert np.isfinite(smag).all() and rel > 1e-6, rel

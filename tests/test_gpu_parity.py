@@ -148,6 +148,49 @@ def test_visc_flux_eglib():
     assert np.all(err <= TOL), err
 
 
+@pytest.mark.parametrize("pw", [70.0, 0.02])
+def test_visc_flux_eglib_les(pw):
+    """viscflux_eg_LES_xyz: EGLIB fluxes with the Smagorinsky SGS viscosity
+    (MU_SGS_FACTOR 0.18, SC_SGS = PR_SGS = 0.7), the shock-detector threshold
+    at the deck default (no point detected) and low enough to detect some
+    points of the perturbed field."""
+    cfg, thd, adi, dxi, st, info, orc = W.case("mix", 12, eglib=True)
+    W.perturb(st, 0.01, seed=5)
+    orc.update_primitives(st)
+    orc.set_les(0.18, 0.7, 0.7, pw)
+    g = _eglib_gpu(cfg, thd, adi, dxi, st)
+    g.set_les(0.18, 0.7, 0.7, pw)
+    fl = np.zeros((cfg.nx, cfg.ny, cfg.nz, 5 + cfg.nrv), order="F")
+    orc.visc_flux(st, fl)
+    g.zero_flux()
+    g.viscflux_xyz()
+    err = W.normwise(g.flux(), fl)
+    g.close()
+    assert np.all(err <= TOL), err
+
+
+def test_rk3_steps_eglib_les():
+    """Two SSP-RK3 steps with the LES closure (the RK3 graph is captured with
+    the LES kernels), against the oracle.  MU_SGS_FACTOR 0.05: with the deck
+    default 0.18 the SGS viscosity of this 47-micron block is some 20 times
+    the laminar one in the code's units, and the convective time step (the
+    reference's timestep sees mu_SGS = 0 under EGLIB) is unstable for it."""
+    cfg, thd, adi, dxi, st, info, orc = W.case("mix", 12, eglib=True)
+    W.perturb(st, 0.02, seed=3)
+    orc.update_primitives(st)
+    orc.set_les(mu_sgs_factor=0.05)
+    g = _eglib_gpu(cfg, thd, adi, dxi, st)
+    g.set_les(mu_sgs_factor=0.05)
+    for step in range(2):
+        dt4, dt = orc.timestep(st)
+        orc.rk3(st, dt)
+        g.rk3(dt)
+    got = g.download()
+    g.close()
+    err = W.normwise(interior(got["v"]), interior(st["v"]))
+    assert np.all(err <= TOL), err
+
+
 def test_rk3_steps_eglib():
     cfg, thd, adi, dxi, st, info, orc = W.case("mix", 12, eglib=True)
     W.perturb(st, 0.02, seed=3)
