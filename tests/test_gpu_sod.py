@@ -128,3 +128,75 @@ def test_gpu_reproduces_reference_restarts():
             else:
                 tol = 1e-6 if name == "rhoU" else 5e-7
                 assert err <= tol * np.abs(ref[name]).max(), (n, name, err / np.abs(ref[name]).max())
+
+
+def test_gpu_resumes_reference_restart(tmp_path):
+    """Restart 1 of the reference's Sod run written in its HDF5 layout, read
+    back (phd_gb300/restart.py), uploaded with a cleared temperature and
+    closed on the device (izem_gpu_finalize_ic, the closure of
+    read_restart_hdf5):
+    * with the Adams-Shariff flags of the run that wrote it (the reference
+      never clears a flag and does not store them), the resumed GPU run
+      reproduces restart 2 at the pin tolerances;
+    * with cleared flags, as the reference's own resume starts, it agrees
+      with the oracle resumed the same way, within the same bounds."""
+    from phd_gb300 import restart as R
+    names7 = ["rho", "rhoU", "rhoV", "rhoW", "rhoE", "O2", "N2"]
+    cfg, thd, a, orc, st, grid = S.sod_case(xblocks=S.NX_BLOCKS)
+    S.run_to_stats(orc, st, a, 1)
+    flags = st["shock_sensor"].copy()
+    g1 = S.golden(1)
+    p = str(tmp_path / "restart_00001.h5")
+    R.write_restart(p, names7, [g1[n] for n in names7], float(g1["time"][0]))
+    names, arrs, t1 = R.read_restart(p)
+    ref = S.golden(2)
+    t2 = float(ref["time"][0])
+    out = []
+    for carried in (True, False):
+        st2 = R.state_from_restart(names, arrs, S.NG, species=["O2", "N2"])
+        if carried:
+            st2["shock_sensor"][...] = flags
+        g = _gpu(cfg, thd, a, grid, st2)
+        g.set_sensor_xblocks(S.NX_BLOCKS)
+        g.finalize_ic()
+        time = t1
+        while True:
+            _, dt = g.timestep()
+            last = time + dt > t2 and time - dt < t2
+            if last:
+                dt = t2 - time
+            g.rk3(dt)
+            time = time + dt
+            if last:
+                break
+        out.append(_interior(g.download()["v"]))
+        g.close()
+    rho_max = np.abs(ref["rho"]).max()
+    for q, name in enumerate(names7):
+        err = np.abs(out[0][..., q] - ref[name]).max()
+        if name in ("rhoV", "rhoW"):
+            assert err <= 1e-10 * rho_max, (name, err)
+        else:
+            tol = 1e-6 if name == "rhoU" else 5e-7
+            assert err <= tol * np.abs(ref[name]).max(), (name, err / np.abs(ref[name]).max())
+    _, _, _, orc2, _, _ = S.sod_case(xblocks=S.NX_BLOCKS)
+    st3 = R.state_from_restart(names, arrs, S.NG, species=["O2", "N2"])
+    orc2.finalize_ic(st3)
+    time = t1
+    while True:
+        _, dt = orc2.timestep(st3)
+        last = time + dt > t2 and time - dt < t2
+        if last:
+            dt = t2 - time
+        orc2.rk3(st3, dt)
+        time = time + dt
+        if last:
+            break
+    vo = _interior(st3["v"])
+    for q, name in enumerate(names7):
+        err = np.abs(out[1][..., q] - vo[..., q]).max()
+        if name in ("rhoV", "rhoW"):
+            assert err <= 1e-10 * rho_max, (name, err)
+        else:
+            tol = 1e-6 if name == "rhoU" else 5e-7
+            assert err <= tol * np.abs(vo[..., q]).max(), (name, err / np.abs(vo[..., q]).max())

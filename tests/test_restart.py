@@ -1,0 +1,126 @@
+"""Restart files in the reference's HDF5 layout (phd_gb300/restart.py;
+save_restart_hdf5 / read_restart_hdf5, module_io.f90:56-197).
+
+* The reader returns the reference's own Sod restart files as the committed
+  fixtures hold them (where the reference tree is mounted).
+* Written files read back bit for bit, group members beyond one symbol node
+  included, and carry the same dataset header messages as the reference's.
+* Resuming: read_restart_hdf5 fills the interior and closes the state; the
+  Adams-Shariff flags are not in the file.  The reference sets a flag and
+  never clears it (module_tools.f90:2733-2814, shock_sensor initialised once
+  in izem.f90:238), so a resumed run starts without the flags of the run
+  that wrote the file.  Given those flags, a run resumed from restart 1
+  reproduces restart 2 at the pin tolerances of tests/test_sod_pin.py.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import sod_case as S
+from phd_gb300 import restart as R
+
+REF = os.environ.get("IZEM_REFERENCE_TESTCASES", "/root/reference/devel-izem/testcases")
+SOD_RESTARTS = os.path.join(REF, "sod", "restarts")
+NAMES = ["rho", "rhoU", "rhoV", "rhoW", "rhoE", "O2", "N2"]
+
+
+def _golden_arrays(n):
+    g = S.golden(n)
+    return [g[k] for k in NAMES], float(g["time"][0])
+
+
+@pytest.mark.skipif(not os.path.isdir(SOD_RESTARTS), reason="reference tree not mounted")
+@pytest.mark.parametrize("n", [1, 2, 3])
+def test_reads_reference_restart_files(n):
+    names, arrays, time = R.read_restart(os.path.join(SOD_RESTARTS, "restart_%05d.h5" % n))
+    g = S.golden(n)
+    assert sorted(names) == sorted(NAMES) and time == float(g["time"][0])
+    for name, a in zip(names, arrays):
+        assert a.shape == (400, 11, 1) and np.array_equal(a, g[name]), name
+
+
+def test_write_read_round_trip(tmp_path):
+    rng = np.random.Generator(np.random.PCG64(3))
+    names = list(R.NIV_NAMES) + ["Y%02d" % k for k in range(12)]      # 17 members: three symbol nodes
+    arrays = [np.asfortranarray(rng.standard_normal((5, 4, 3))) for _ in names]
+    p = str(tmp_path / "r.h5")
+    R.write_restart(p, names, arrays, 2.5)
+    got_names, got, time = R.read_restart(p)
+    assert got_names == names and time == 2.5
+    assert all(np.array_equal(a, b) for a, b in zip(got, arrays))
+
+
+@pytest.mark.skipif(not os.path.isdir(SOD_RESTARTS), reason="reference tree not mounted")
+def test_written_headers_match_reference_file(tmp_path):
+    """The dataspace, datatype, fill-value and layout messages of a written
+    dataset have the reference file's types, sizes and (but for the data
+    address) bytes; the group structure holds the same names."""
+    arrays, time = _golden_arrays(1)
+    p = str(tmp_path / "r1.h5")
+    R.write_restart(p, NAMES, arrays, time)
+    heads = []
+    for path in (os.path.join(SOD_RESTARTS, "restart_00001.h5"), p):
+        d = open(path, "rb").read()
+        root = 56
+        groups = R._group(d, R._u(d, root + 24, 8), R._u(d, root + 32, 8))
+        gb, gh = np.frombuffer(groups["consvar"][2], dtype="<u8")
+        members = R._group(d, int(gb), int(gh))
+        msgs = {t: bytes(d[q:q + s]) for t, q, s in R._messages(d, members["N2"][0]) if t in (1, 3, 5, 8)}
+        msgs[8] = msgs[8][:2] + msgs[8][10:]          # layout: version, class and size; not the address
+        heads.append((sorted(groups), sorted(members), msgs))
+    assert heads[0] == heads[1]
+
+
+def test_state_round_trip():
+    arrays, time = _golden_arrays(2)
+    st = R.state_from_restart(NAMES, arrays, S.NG, species=["O2", "N2"])
+    assert st["v"].shape == (400 + 8, 11 + 8, 1 + 8, 7) and not st["T"].any()
+    names, back = R.restart_from_state(st["v"], S.NG, ["O2", "N2"])
+    assert names == NAMES and all(np.array_equal(a, b) for a, b in zip(back, arrays))
+
+
+def _resume_to(orc, st, t0, t1):
+    """The main loop from time t0 to the statistics time t1 (timestep, the
+    step that would pass t1 clipped onto it, rk3)."""
+    time = t0
+    while True:
+        _, dt = orc.timestep(st)
+        last = time + dt > t1 and time - dt < t1
+        if last:
+            dt = t1 - time
+        orc.rk3(st, dt)
+        time = time + dt
+        if last:
+            return time
+
+
+def test_oracle_resumes_reference_restart(tmp_path):
+    """Restart 1 written and read back, closed as read_restart_hdf5 closes
+    it, resumed with the sensor flags of the run that wrote it: restart 2 at
+    the pin tolerances.  Resumed with cleared flags, as the reference's own
+    resume starts, the result moves away from restart 2 near the waves."""
+    cfg, thd, a, orc, st, grid = S.sod_case()
+    S.run_to_stats(orc, st, a, 1)
+    flags = st["shock_sensor"].copy()
+    arrays, t1 = _golden_arrays(1)
+    p = str(tmp_path / "restart_00001.h5")
+    R.write_restart(p, NAMES, arrays, t1)
+    names, arrs, time = R.read_restart(p)
+    ref = S.golden(2)
+    t2 = float(ref["time"][0])
+    errs = []
+    for carried in (True, False):
+        _, _, _, orc2, _, _ = S.sod_case()
+        st2 = R.state_from_restart(names, arrs, S.NG, species=["O2", "N2"])
+        orc2.finalize_ic(st2)
+        if carried:
+            st2["shock_sensor"][...] = flags
+        assert _resume_to(orc2, st2, time, t2) == t2
+        vi = st2["v"][S.NG:-S.NG, S.NG:-S.NG, S.NG:-S.NG]
+        errs.append({n: np.abs(vi[..., q] - ref[n]).max() / max(np.abs(ref[n]).max(), 1e-300)
+                     for q, n in enumerate(NAMES)})
+    for n in ("rho", "rhoE", "O2", "N2"):
+        assert errs[0][n] <= 5e-7, (n, errs[0][n])
+    assert errs[0]["rhoU"] <= 1e-6
+    assert errs[1]["rho"] > 100 * errs[0]["rho"]
