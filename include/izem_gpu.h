@@ -28,8 +28,12 @@ extern "C" {
 #define IZEM_NSMAX 10      /* maximum reactive species (9-species H2/air set) */
 #define IZEM_NPOLY 4       /* transport fit order (tranfit.out: Npoly = 4)    */
 
-/* Boundary kinds of the faces W,E,S,N,B,F (module_parameters: bc(1:6)). */
-enum { IZEM_BC_PERIODIC = 0, IZEM_BC_EXTRAPOLATION = 1 };
+/* Boundary kinds of the faces W,E,S,N,B,F (module_parameters: bc(1:6),
+ * module_BCs.f90): periodic (comm_cons), bc_extrapolation
+ * (:327-412), bc_inflowjet on the W face only (:1646-1791) and bc_nscbc_out
+ * on the E face only (:2331-2516); the last two are Dirichlet faces closed by
+ * upd_prim_var_dirichlet (:297-314) and need izem_gpu_set_coords. */
+enum { IZEM_BC_PERIODIC = 0, IZEM_BC_EXTRAPOLATION = 1, IZEM_BC_INFLOWJET = 2, IZEM_BC_NSCBC_OUT = 3 };
 enum { IZEM_FACE_W = 0, IZEM_FACE_E, IZEM_FACE_S, IZEM_FACE_N, IZEM_FACE_B, IZEM_FACE_F };
 
 /* Status codes. */
@@ -239,6 +243,15 @@ int  izem_gpu_chem_step(izem_ctx* ctx, double dt, int mode, double* DTmax);
  * four of its five arguments; this is the routine's stated semantics. */
 int  izem_gpu_set_chem_skip(izem_ctx* ctx, int enable, const double* Y_fuel, const double* Y_oxidizer,
                             int index_h2, int index_n2);
+
+/* Coordinates of the interior points in code units (x, y, z: nx, ny, nz
+ * values; the reference's x/L_ref arrays) and the domain length in x, Lx
+ * (module_tools.f90:319,489), for the jet faces IZEM_BC_INFLOWJET (radius
+ * sqrt(y^2 + z^2)) and IZEM_BC_NSCBC_OUT (Lx).  Required before
+ * izem_gpu_rk3 when a jet face is set; the time0 argument of izem_gpu_rk3
+ * then gives the stage times timek = time0 + dt tk3 (module_solver.f90:756).
+ * The chemistry step is built for periodic and extrapolation faces only. */
+int  izem_gpu_set_coords(izem_ctx* ctx, const double* x, const double* y, const double* z, double lx);
 
 /* [IFLES] LES = T with MU_SGS_MODEL = SMAGORINSKY under EGLIB: the viscous
  * fluxes of viscflux_eg_LES_xyz (module_eg_lib.f90:2687-3352) with

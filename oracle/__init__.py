@@ -44,7 +44,8 @@ def load():
         "or_force_sumY": (C.c_int, [P, C.c_int, _dp]),
         "or_update_primitives": (C.c_int, [P, _dp, _dp, _dp, _dp, _dp]),
         "or_finalize_ic": (C.c_int, [P, _dp, _dp, _dp, _dp, _dp]),
-        "or_rk3": (C.c_int, [P, C.c_double, _dp, _dp, _dp, _dp, _dp, _u8p]),
+        "or_rk3": (C.c_int, [P, C.c_double, C.c_double, _dp, _dp, _dp, _dp, _dp, _u8p]),
+        "or_set_coords": (C.c_int, [P, _dp, _dp, _dp, C.c_double]),
         "or_timestep": (C.c_int, [P, C.c_double, _dp, _dp, _dp, _dp, _dp, _dp]),
         "or_metrics_dscalar": (None, [C.c_int, C.c_int, _dp, _dp]),
         "or_chem_step": (C.c_int, [P, C.POINTER(IzemMech), C.c_double, _dp, _dp, _dp, _dp, _dp, _dp,
@@ -223,10 +224,17 @@ class Oracle:
         v, T, W_i, cp, ha = self._arrs(s)
         self._rc(self.lib.or_finalize_ic(self.h, _p(v), _p(T), _p(W_i), _p(cp), _p(ha)), "finalize_ic")
 
-    def rk3(self, s, dt):
+    def rk3(self, s, dt, time0=0.0):
         v, T, W_i, cp, ha = self._arrs(s)
-        self._rc(self.lib.or_rk3(self.h, float(dt), _p(v), _p(T), _p(W_i), _p(cp), _p(ha),
+        self._rc(self.lib.or_rk3(self.h, float(dt), float(time0), _p(v), _p(T), _p(W_i), _p(cp), _p(ha),
                                  _p(s["shock_sensor"], _u8p)), "rk3")
+
+    def set_coords(self, x, y, z, lx):
+        """Coordinates of the interior points (code units) and the domain
+        length in x, for the jet boundaries."""
+        xs = [np.ascontiguousarray(a, dtype=np.float64) for a in (x, y, z)]
+        self._keep_coords = xs
+        self._rc(self.lib.or_set_coords(self.h, *[_p(a) for a in xs], float(lx)), "set_coords")
 
     def chem_step(self, s, mech, dt):
         v, T, W_i, cp, ha = self._arrs(s)

@@ -70,6 +70,10 @@ struct Ctx {
   // SC_SGS, PR_SGS, PERCENT_WEIGHT_SGS
   bool les = false;
   double les_factor = 0.0, les_sc_sgs = 1.0, les_pr_sgs = 1.0, les_pw = 0.0;
+  // coordinates of the interior points (code units) and the domain length
+  // in x (Lx, module_tools.f90:319,489) for the jet boundaries
+  std::vector<double> crd[3];
+  double lx = 0.0;
   bool dvodesimp = false;
   double y1f[IZEM_NSMAX] = {}, y0o[IZEM_NSMAX] = {};
   int index_h2 = 0, index_n2 = 0;
@@ -88,6 +92,12 @@ void domain_select(const Block& b, int id, int& i0, int& i1, int& j0, int& j1, i
     case 1: i0 = b.nx + 1; i1 = b.nx + b.ng; break;
     case 2: j0 = b.ny + 1; j1 = b.ny + b.ng; break;
     case 3: k0 = b.nz + 1; k1 = b.nz + b.ng; break;
+    case -10: i1 = 1; break;          // Dirichlet planes (module_parallel.f90:1944-2000)
+    case 10: i0 = b.nx; break;
+    case -20: j1 = 1; break;
+    case 20: j0 = b.ny; break;
+    case -30: k1 = 1; break;
+    case 30: k0 = b.nz; break;
     default: break;
   }
 }
@@ -354,17 +364,204 @@ void bc_extrapolation(const Block& b, int face, double* v) {
 }
 
 const int kFaceDomain[6] = {-1, 1, -2, 2, -3, 3};
+const int kDirichletDomain[6] = {-10, 10, -20, 20, -30, 30};
+
+bool is_dirichlet(int bc) { return bc == IZEM_BC_INFLOWJET || bc == IZEM_BC_NSCBC_OUT; }
+
+// Wmix_i_scalar (module_thermodynamics.f90:739-756)
+double wmix_i_scalar(const izem_thd& t, int nrv, const double* Ya) {
+  double w = 0.0;
+  for (int l = 0; l < nrv; ++l) w = w + Ya[l] * t.Wc_i[l];
+  return w;
+}
+
+// bc_inflowjet (module_BCs.f90:1646-1791), W face: the underexpanded jet of
+// a 1 mm nozzle (nozzle pressure ratio 15, 1000 K, Mach 1.01 at the exit)
+// into 300 K air at 20 m/s, tanh profiles in the radius sqrt(y^2 + z^2),
+// the nozzle state ramped in with (t / 0.1 ms)^3.  Written at the ghost
+// points and the first interior plane.  The reference computes the exit
+// sound speed from a mass-fraction array of which only the entries below
+// are set; the others are taken as 0.  Species sets of 2, 3 or 9 species.
+void bc_inflowjet(const Ctx& c, double time, double* v) {
+  const Block& b = c.b;
+  const izem_adi& a = c.adi;
+  const izem_thd& t = c.thd;
+  const int nrv = b.nrv;
+  const size_t nc = b.ncell;
+  const double NPR = 15.0;
+  const double hbuse = 0.0010 / a.l_ref, tmaxy = 0.0001 / a.time_ref;
+  const double u_2 = 20.0 / a.u_ref;
+  double T_1 = 1000.0 / a.t_ref;
+  const double T_2 = 300.0 / a.t_ref;
+  double P_1 = 101325.0 * NPR / a.p_ref;
+  const double P_2 = 101325.0 / a.p_ref;
+  double Ya_1 = 1.0;
+  const double Ya_2 = 0.0;
+  const double delt = 1.0 / (0.04 * hbuse), y0 = hbuse / 2.0;
+  const double vy = 0.0, wz = 0.0;
+  if (time <= tmaxy) {
+    P_1 = (P_2 - (P_2 - P_1) * (time / tmaxy) * (time / tmaxy) * (time / tmaxy));
+    Ya_1 = (Ya_2 - (Ya_2 - Ya_1) * (time / tmaxy) * (time / tmaxy) * (time / tmaxy));
+    T_1 = (T_2 - (T_2 - T_1) * (time / tmaxy) * (time / tmaxy) * (time / tmaxy));
+  }
+  double Ya[IZEM_NSMAX] = {};
+  if (nrv == 2) { Ya[0] = 0.233; Ya[1] = 0.767; }
+  else if (nrv == 3) { Ya[0] = Ya_1; Ya[1] = 0.0; Ya[2] = 1.0 - Ya_1; }
+  else { Ya[1] = Ya_1; Ya[3] = 0.0; Ya[8] = 1.0 - Ya_1; }
+  double Ws_i = wmix_i_scalar(t, nrv, Ya);
+  const double cps = cp_scalar(t, T_1, Ya);
+  double gamma = t.gam2 * Ws_i / cps;
+  gamma = 1.0 / (1.0 - gamma);
+  const double cs = std::sqrt(gamma * Ws_i * T_1);
+  const double u_1 = 1.01 * cs;
+  for (int k = 1; k <= b.nz; ++k)
+    for (int j = 1; j <= b.ny; ++j)
+      for (int i = 1 - b.ng; i <= 1; ++i) {
+        const double y = c.crd[1][j - 1], z = c.crd[2][k - 1];
+        const double rrr = std::sqrt(y * y + z * z);
+        const double th = std::tanh((rrr - y0) * delt);
+        const double ux = 0.5 * ((u_1 + u_2) - (u_1 - u_2) * th);
+        const double T = 0.5 * ((T_1 + T_2) - (T_1 - T_2) * th);
+        const double P = 0.5 * ((P_1 + P_2) - (P_1 - P_2) * th);
+        for (int l = 0; l < nrv; ++l) Ya[l] = 0.0;
+        if (nrv == 2) {
+          Ya[0] = 0.233;
+          Ya[1] = 1.0 - Ya[0];
+        } else if (nrv == 3) {
+          Ya[0] = 0.5 * ((Ya_1 + 0.0) - (Ya_1 - 0.0) * th);
+          Ya[1] = 0.5 * ((0.0 + 0.233) - (0.0 - 0.233) * th);
+          Ya[2] = 0.5 * ((1.0 - Ya_1 + 0.767) - (1.0 - Ya_1 - 0.767) * th);
+        } else {
+          Ya[1] = 0.5 * ((Ya_1 + 0.0) - (Ya_1 - 0.0) * th);
+          Ya[3] = 0.5 * ((0.0 + 0.233) - (0.0 - 0.233) * th);
+          Ya[8] = 0.5 * ((1.0 - Ya_1 + 0.767) - (1.0 - Ya_1 - 0.767) * th);
+        }
+        Ws_i = wmix_i_scalar(t, nrv, Ya);
+        const double rho = P / (T * Ws_i);
+        double has[IZEM_NSMAX];
+        ha_scalar(t, T, has);
+        double hm = 0.0;
+        for (int l = 0; l < nrv; ++l) hm = hm + has[l] * Ya[l];
+        const size_t p = b.id(i, j, k);
+        v[p] = rho;
+        v[nc + p] = rho * ux;
+        v[2 * nc + p] = rho * vy;
+        v[3 * nc + p] = rho * wz;
+        v[4 * nc + p] = rho * hm - P + 0.5 * rho * (ux * ux + vy * vy + wz * wz);
+        for (int l = 0; l < nrv; ++l) v[(NIV + l) * nc + p] = rho * Ya[l];
+      }
+}
+
+// bc_nscbc_out (module_BCs.f90:2331-2516), E face: characteristic outflow
+// with 4th-order one-sided derivatives at the last interior point, the
+// incoming wave relaxed toward 94232.25 Pa (sigma 0.28, the domain length
+// Lx); the same updated state, advanced by dt, at the last interior plane
+// and the ghost points.
+void bc_nscbc_out(const Ctx& c, double dtime, const double* T, const double* W_i, const double* cp, double* v) {
+  const Block& b = c.b;
+  const izem_adi& a = c.adi;
+  const izem_thd& t = c.thd;
+  const int nrv = b.nrv;
+  const size_t nc = b.ncell;
+  const double Pinf = 94232.25 / a.p_ref, sigma1 = 0.28, Lx = c.lx;
+  static const double a4or[5] = {-3.0 / 12.0, 16.0 / 12.0, -36.0 / 12.0, 48.0 / 12.0, -25.0 / 12.0};   // m = -4..0
+  const int ex = b.nx;
+  const double dxe = c.dxi[0][ex - 1 + b.ng];
+  for (int k = 1; k <= b.nz; ++k)
+    for (int j = 1; j <= b.ny; ++j) {
+      double Machm = 0.0;
+      size_t p = b.id(ex, j, k);
+      double rho = v[p], rho_i = 1.0 / rho;
+      double ux = v[nc + p] * rho_i, vy = v[2 * nc + p] * rho_i, wz = v[3 * nc + p] * rho_i;
+      double Pres = v[p] * T[p] * W_i[p];
+      double gam = t.gam2 * W_i[p] / cp[p];
+      gam = 1.0 / (1.0 - gam);
+      double cs = std::sqrt(gam * Pres * rho_i);
+      const double Mach = std::sqrt(ux * ux + vy * vy + wz * wz) / cs;
+      Machm = std::max(Machm, Mach);
+      double drho = 0.0, dux = 0.0, dvy = 0.0, dwz = 0.0, dPres = 0.0;
+      double Ya[IZEM_NSMAX], dYa[IZEM_NSMAX] = {};
+      for (int m = -4; m <= 0; ++m) {
+        const size_t q = b.id(ex + m, j, k);
+        rho = v[q];
+        rho_i = 1.0 / rho;
+        ux = v[nc + q] * rho_i;
+        vy = v[2 * nc + q] * rho_i;
+        wz = v[3 * nc + q] * rho_i;
+        Pres = v[q] * T[q] * W_i[q];
+        for (int l = 0; l < nrv; ++l) Ya[l] = v[(NIV + l) * nc + q] * rho_i;
+        const double w = a4or[m + 4];
+        drho = drho + w * rho;
+        dux = dux + w * ux;
+        dvy = dvy + w * vy;
+        dwz = dwz + w * wz;
+        dPres = dPres + w * Pres;
+        for (int l = 0; l < nrv; ++l) dYa[l] = dYa[l] + w * Ya[l];
+      }
+      drho = -drho * dxe;
+      dux = -dux * dxe;
+      dvy = -dvy * dxe;
+      dwz = -dwz * dxe;
+      dPres = -dPres * dxe;
+      for (int l = 0; l < nrv; ++l) dYa[l] = -dYa[l] * dxe;
+      double L1 = 0.0, L2 = 0.0, L3 = 0.0, L4 = 0.0, L5 = 0.0, L5_Ya[IZEM_NSMAX] = {};
+      gam = t.gam2 * W_i[p] / cp[p];
+      gam = 1.0 / (1.0 - gam);
+      cs = std::sqrt(gam * Pres * rho_i);
+      if (ux - cs < 0.0) L1 = sigma1 * (1.0 - Machm * Machm) * cs / Lx * (Pres - Pinf);
+      else L1 = (ux - cs) * (dPres - rho * cs * dux);
+      if (ux + cs > 0.0) L5 = (ux + cs) * (dPres + rho * cs * dux);
+      else L5 = (ux + cs) * (2.0 * dPres - L1 / (ux - cs));
+      if (ux > 0.0) {
+        L2 = ux * (cs * cs * drho - dPres);
+        L3 = ux * dvy;
+        L4 = ux * dwz;
+        for (int l = 0; l < nrv; ++l) L5_Ya[l] = ux * dYa[l];
+      } else {
+        L2 = ux * cs * cs * drho - 0.5 * ux * (L5 / (ux + cs) + L1 / (ux - cs));
+      }
+      const double d2 = 0.5 * (L5 + L1);
+      const double d1 = (L2 + d2) / (cs * cs);
+      const double d3 = 0.5 * (L5 - L1) / (cs * rho);
+      const double d4 = L3, d5 = L4;
+      double has[IZEM_NSMAX];
+      ha_scalar(t, T[p], has);
+      double hm = 0.0;
+      for (int l = 0; l < nrv; ++l) hm = hm + has[l] * Ya[l];
+      const double kin = ux * ux + vy * vy + wz * wz;
+      for (int i = ex; i <= ex + b.ng; ++i) {
+        const size_t o = b.id(i, j, k);
+        v[o] = rho - d1 * dtime;
+        v[nc + o] = (rho * ux) - (ux * d1 + rho * d3) * dtime;
+        v[2 * nc + o] = (rho * vy) - (vy * d1 + rho * d4) * dtime;
+        v[3 * nc + o] = (rho * wz) - (wz * d1 + rho * d5) * dtime;
+        v[4 * nc + o] = (rho * hm - Pres + 0.5 * rho * kin) -
+                        (0.5 * kin * d1 + rho * (ux * d3 + vy * d4 + wz * d5) + d2 / (gam - 1.0)) * dtime;
+        for (int l = 0; l < nrv; ++l) v[(NIV + l) * nc + o] = (rho * Ya[l]) - (Ya[l] * d1 + rho * L5_Ya[l]) * dtime;
+      }
+    }
+}
 
 // upd_prim_var_domain + comm_cons + upd_boundaries + upd_prim_var_ghost
 // (module_solver.f90:839-845, module_BCs.f90:41-296)
-int update_primitives(Ctx& c, double* v, double* T, double* W_i, double* cp, double* ha) {
+// time: the stage time given to upd_boundaries; dt: the step.
+int update_primitives(Ctx& c, double* v, double* T, double* W_i, double* cp, double* ha, double time = 0.0,
+                      double dt = 0.0) {
   const Block& b = c.b;
   if (c.cfg.forcesum) force_sumY(c, 0, v);
   int rc = prim_inv_var(c, 0, false, v, W_i, T, cp, ha);
   if (rc) return rc;
   comm_periodic(b, b.nv, v, b.ncell);
-  for (int f = 0; f < 6; ++f)
-    if (b.bnd[f] && b.bc[f] == IZEM_BC_EXTRAPOLATION) bc_extrapolation(b, f, v);
+  for (int f = 0; f < 6; ++f) {
+    if (!b.bnd[f]) continue;
+    if (b.bc[f] == IZEM_BC_EXTRAPOLATION) bc_extrapolation(b, f, v);
+    else if (b.bc[f] == IZEM_BC_INFLOWJET) bc_inflowjet(c, time, v);
+    else if (b.bc[f] == IZEM_BC_NSCBC_OUT) bc_nscbc_out(c, dt, T, W_i, cp, v);
+    if (is_dirichlet(b.bc[f])) {   // upd_prim_var_dirichlet
+      if (c.cfg.forcesum) force_sumY(c, kDirichletDomain[f], v);
+      if ((rc = prim_inv_var(c, kDirichletDomain[f], false, v, W_i, T, cp, ha))) return rc;
+    }
+  }
   for (int f = 0; f < 6; ++f) {
     if (c.cfg.forcesum) force_sumY(c, kFaceDomain[f], v);
     rc = prim_inv_var(c, kFaceDomain[f], false, v, W_i, T, cp, ha);
@@ -1014,8 +1211,14 @@ int visc_flux(Ctx& c, const double* v, const double* T, const double* W_i, const
 }
 
 // rk3 (module_solver.f90:694-856)
-int rk3(Ctx& c, double dt, double* v, double* T, double* W_i, double* cp, double* ha, uint8_t* sensor) {
+int rk3(Ctx& c, double dt, double time0, double* v, double* T, double* W_i, double* cp, double* ha,
+        uint8_t* sensor) {
   const Block& b = c.b;
+  if ((is_dirichlet(b.bc[0]) || is_dirichlet(b.bc[1])) && c.crd[0].empty()) {
+    c.err = "jet boundaries need the coordinates (or_set_coords)";
+    return IZEM_ERR_STATE;
+  }
+  const double tk3[3] = {0.0, 0.5, 1.0};   // stage times (module_solver.f90:727,756)
   const double bk3[3] = {0.00, 0.75, 1.00 / 3.00};
   const double ck3[3] = {1.00, 0.25, 2.00 / 3.00};
   const size_t ni = b.nint, nc = b.ncell;
@@ -1038,7 +1241,7 @@ int rk3(Ctx& c, double dt, double* v, double* T, double* W_i, double* cp, double
             size_t p = l * nc + b.id(i, j, k), q = l * ni + b.fid(i, j, k);
             v[p] = v0[q] * bk3[ik] + ck3[ik] * (v[p] - dt * f[q]);
           }
-    if ((rc = update_primitives(c, v, T, W_i, cp, ha))) return rc;
+    if ((rc = update_primitives(c, v, T, W_i, cp, ha, time0 + dt * tk3[ik], dt))) return rc;
   }
   return IZEM_OK;
 }
@@ -1213,6 +1416,12 @@ void* or_create(const izem_cfg* cfg, const izem_thd* thd, const izem_adi* adi, c
   if (!cfg || !thd || !adi || (cfg->ng != 3 && cfg->ng != 4) || (cfg->ndim != 2 && cfg->ndim != 3) ||
       (cfg->ndim == 2 && cfg->nz != 1) || cfg->nrv < 2 || cfg->nrv > IZEM_NSMAX)
     return nullptr;
+  for (int f = 0; f < 6; ++f) {
+    const int bc = cfg->bc[f];
+    if (bc < IZEM_BC_PERIODIC || bc > IZEM_BC_NSCBC_OUT) return nullptr;
+    if ((bc == IZEM_BC_INFLOWJET && f != 0) || (bc == IZEM_BC_NSCBC_OUT && f != 1)) return nullptr;
+  }
+  if (cfg->bc[0] == IZEM_BC_INFLOWJET && cfg->nrv != 2 && cfg->nrv != 3 && cfg->nrv != 9) return nullptr;
   Ctx* c = new Ctx();
   c->cfg = *cfg;
   c->thd = *thd;
@@ -1233,8 +1442,16 @@ void* or_create(const izem_cfg* cfg, const izem_thd* thd, const izem_adi* adi, c
 
 void or_destroy(void* h) { delete static_cast<Ctx*>(h); }
 
-// The reference's run decomposed x into nblk equal MPI blocks: the shock
-// sensor of each block stops at its own last point (module_tools.f90:2761-2770).
+// Coordinates of the interior points (code units) and Lx, for the jet boundaries.
+int or_set_coords(void* h, const double* x, const double* y, const double* z, double lx) {
+  Ctx* c = static_cast<Ctx*>(h);
+  if (!x || !y || !z) return IZEM_ERR_ARG;
+  const double* src[3] = {x, y, z};
+  for (int d = 0; d < 3; ++d) c->crd[d].assign(src[d], src[d] + c->b.n(d));
+  c->lx = lx;
+  return IZEM_OK;
+}
+
 int or_set_les(void* h, int enable, double mu_sgs_factor, double sc_sgs, double pr_sgs, double percent_weight_sgs) {
   Ctx* c = static_cast<Ctx*>(h);
   if (!enable) {
@@ -1268,6 +1485,8 @@ int or_set_chem_skip(void* h, int enable, const double* y1f, const double* y0o, 
   return IZEM_OK;
 }
 
+// The reference's run decomposed x into nblk equal MPI blocks: the shock
+// sensor of each block stops at its own last point (module_tools.f90:2761-2770).
 int or_set_sensor_xblocks(void* h, int nblk) {
   Ctx* c = static_cast<Ctx*>(h);
   if (nblk < 1 || c->b.nx % nblk) return IZEM_ERR_ARG;
@@ -1327,8 +1546,9 @@ int or_update_primitives(void* h, double* v, double* T, double* W_i, double* cp,
 int or_finalize_ic(void* h, double* v, double* T, double* W_i, double* cp, double* ha) {
   return finalize_ic(*static_cast<Ctx*>(h), v, T, W_i, cp, ha);
 }
-int or_rk3(void* h, double dt, double* v, double* T, double* W_i, double* cp, double* ha, uint8_t* sensor) {
-  return rk3(*static_cast<Ctx*>(h), dt, v, T, W_i, cp, ha, sensor);
+int or_rk3(void* h, double dt, double time0, double* v, double* T, double* W_i, double* cp, double* ha,
+           uint8_t* sensor) {
+  return rk3(*static_cast<Ctx*>(h), dt, time0, v, T, W_i, cp, ha, sensor);
 }
 int or_timestep(void* h, double DTmax, const double* v, const double* T, const double* W_i, const double* cp,
                 double* dt4, double* dtmin) {
@@ -1338,7 +1558,12 @@ int or_timestep(void* h, double DTmax, const double* v, const double* T, const d
 
 int or_chem_step(void* h, const izem_mech* mech, double dt, double* v, double* T, double* W_i, double* cp, double* ha,
                  double* DTmax, int* max_steps) {
-  return chem_step(*static_cast<Ctx*>(h), *mech, dt, v, T, W_i, cp, ha, DTmax, max_steps);
+  Ctx* c = static_cast<Ctx*>(h);
+  if (is_dirichlet(c->b.bc[0]) || is_dirichlet(c->b.bc[1])) {
+    c->err = "the chemistry step is built for periodic and extrapolation faces only";
+    return IZEM_ERR_STATE;
+  }
+  return chem_step(*c, *mech, dt, v, T, W_i, cp, ha, DTmax, max_steps);
 }
 
 // Independent constant-volume reactors (PSR_CHEMKIN per cell): T [K],

@@ -10,6 +10,8 @@ NPOLY = 4
 
 BC_PERIODIC = 0
 BC_EXTRAPOLATION = 1
+BC_INFLOWJET = 2
+BC_NSCBC_OUT = 3
 
 OK = 0
 ERR_ARG = 1

@@ -53,9 +53,11 @@ static __constant__ DevThd c_thd;
 
 // Device status word shared by all kernels of a context.
 struct DevStatus {
-  unsigned long long maxdf_bits[8];  // per sub-domain max dT^2 (bit pattern of a non-negative double)
-  int it[8];
-  int done[8];
+  // per sub-domain (0 interior, 1-6 ghost faces, 7-8 the Dirichlet planes
+  // of the W and E faces) max dT^2 (bit pattern of a non-negative double)
+  unsigned long long maxdf_bits[10];
+  int it[10];
+  int done[10];
   int neg_pressure;
   int neg_temperature;
   int newton_nan;

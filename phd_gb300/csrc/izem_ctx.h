@@ -68,6 +68,11 @@ struct izem_ctx {
   int* b_list = nullptr;                  // selected reactors (sur_cap entries)
   unsigned* d_list_count = nullptr;
   long long list_cap = 0;
+  // jet faces (izem_gpu_set_coords): interior y, z coordinates and the
+  // constants of bc_inflowjet / bc_nscbc_out
+  bool have_coords = false;
+  double *d_y = nullptr, *d_z = nullptr;
+  JetArgs jet{};
   // LES closure (izem_gpu_set_les)
   bool les_on = false;
   double les_cs2 = 0.0, les_sc_sgs_i = 0.0, les_pr_sgs_i = 0.0, les_pw = 0.0;

@@ -114,15 +114,17 @@ int read_status(izem_ctx* c) {
 }
 
 // ------------------------------------------------------- stage building -----
+// ghost: 0 the interior (sub-domain 0), 1 the ghost slabs (1-6), 2 the
+// Dirichlet planes of jet faces (7-8)
 template <int NRV>
 int enq_newton(izem_ctx* c, int ghost, double eps, int itmax, int niter, int check_negT) {
   const Geo& g = c->g;
-  int d0 = ghost ? 1 : 0, d1 = ghost ? 6 : 0;
-  long long n = ghost ? slab_count(g) - g.nint : g.nint;
+  int d0 = ghost == 2 ? 7 : (ghost ? 1 : 0), d1 = ghost == 2 ? 8 : (ghost ? 6 : 0);
+  long long n = ghost == 2 ? 2LL * g.n[1] * g.n[2] : (ghost ? slab_count(g) - g.nint : g.nint);
   int rc;
   if ((rc = launch(c, "newton_reset", [&] { k_newton_reset<<<1, 8, 0, c->stream>>>(c->d_status, d0, d1); }))) return rc;
   for (int it = 0; it < niter; ++it) {
-    if ((rc = launch(c, ghost ? "newton_iter_ghost" : "newton_iter", [&] {
+    if ((rc = launch(c, ghost == 2 ? "newton_iter_plane" : (ghost ? "newton_iter_ghost" : "newton_iter"), [&] {
            k_newton_iter<NRV><<<grid_for(n), kThreads, 0, c->stream>>>(g, ghost, c->v, c->T, c->cp, c->ha, c->d_status, check_negT);
          })))
       return rc;
@@ -240,13 +242,54 @@ int enq_visc(izem_ctx* c) {
   return launch(c, "visc_div", [&] { k_visc_div<NRV><<<grid_for(g.nint), kThreads, 0, c->stream>>>(g, mt, c->tau, c->qv, c->fd, c->f); });
 }
 
+static bool jet_face(int bc) { return bc == IZEM_BC_INFLOWJET || bc == IZEM_BC_NSCBC_OUT; }
+
+// upd_prim_var_domain's Newton, comm_cons, upd_boundaries, upd_prim_var_ghost
+// (module_solver.f90:840-847).  stage: the RK stage whose time goes to the
+// jet faces (timek = time0 + dt tk3(stage)), -1 for time 0 and dt 0.
 template <int NRV>
-int enq_update_primitives_after(izem_ctx* c) {
+int enq_update_primitives_after(izem_ctx* c, int stage = -1) {
   const Geo& g = c->g;
   int rc;
   if ((rc = enq_newton<NRV>(c, 0, 1.0e-5, 200, kNewtonIters, 1))) return rc;
   long long ns = slab_count(g) - g.nint;
-  if ((rc = launch(c, "halo", [&] { k_halo<NRV><<<grid_for(ns), kThreads, 0, c->stream>>>(g, 0, c->cfg.forcesum, c->v, c->W_i); })))
+  const bool jet = jet_face(g.bc[0]) || jet_face(g.bc[1]);
+  if (!jet) {
+    if ((rc = launch(c, "halo", [&] { k_halo<NRV><<<grid_for(ns), kThreads, 0, c->stream>>>(g, 0, c->cfg.forcesum, c->v, c->W_i); })))
+      return rc;
+    return enq_newton<NRV>(c, 1, 1.0e-5, 200, kNewtonIters, 1);
+  }
+  // faces in the reference's order: periodic copies first (comm_cons), then
+  // W and E (the jet faces, closed on their boundary planes), then the
+  // extrapolated faces
+  int per = 0, ext = 0, dir = 0;
+  for (int f = 0; f < 6; ++f) {
+    if (g.bc[f] == IZEM_BC_PERIODIC) per |= 1 << f;
+    else if (g.bc[f] == IZEM_BC_EXTRAPOLATION) ext |= 1 << f;
+    else dir |= 1 << f;
+  }
+  const double tk3[3] = {0.0, 0.5, 1.0};
+  JetArgs ja = c->jet;
+  ja.tdt = stage >= 0 ? c->d_dt : c->d_dt + 2;
+  ja.tk = stage >= 0 ? tk3[stage] : 0.0;
+  const long long np = (long long)g.n[1] * g.n[2];
+  if (per && (rc = launch(c, "halo", [&] { k_halo<NRV><<<grid_for(ns), kThreads, 0, c->stream>>>(g, 0, c->cfg.forcesum, c->v, c->W_i, per); })))
+    return rc;
+  if (g.bc[0] == IZEM_BC_INFLOWJET &&
+      (rc = launch(c, "bc_inflowjet", [&] { k_bc_inflowjet<NRV><<<grid_for(np), kThreads, 0, c->stream>>>(g, ja, c->v); })))
+    return rc;
+  if (g.bc[1] == IZEM_BC_NSCBC_OUT && (rc = launch(c, "bc_nscbc_out", [&] {
+                                         k_bc_nscbc_out<NRV><<<grid_for(np), kThreads, 0, c->stream>>>(g, ja, c->T, c->W_i, c->cp, c->v);
+                                       })))
+    return rc;
+  if ((rc = launch(c, "dirichlet_prep", [&] {
+         k_dirichlet_prep<NRV><<<grid_for(2 * np), kThreads, 0, c->stream>>>(g, c->cfg.forcesum, c->v, c->W_i);
+       })))
+    return rc;
+  if ((rc = enq_newton<NRV>(c, 2, 1.0e-5, 200, kNewtonIters, 1))) return rc;
+  if (ext && (rc = launch(c, "halo", [&] { k_halo<NRV><<<grid_for(ns), kThreads, 0, c->stream>>>(g, 0, c->cfg.forcesum, c->v, c->W_i, ext); })))
+    return rc;
+  if ((rc = launch(c, "halo", [&] { k_halo<NRV><<<grid_for(ns), kThreads, 0, c->stream>>>(g, 2, c->cfg.forcesum, c->v, c->W_i, dir); })))
     return rc;
   return enq_newton<NRV>(c, 1, 1.0e-5, 200, kNewtonIters, 1);
 }
@@ -266,7 +309,7 @@ int enq_stage(izem_ctx* c, int stage) {
          k_rk_update<NRV><<<grid_for(g.nint), kThreads, 0, c->stream>>>(g, stage, c->cfg.forcesum, c->d_dt, c->v, c->v0, c->f, c->W_i);
        })))
     return rc;
-  return enq_update_primitives_after<NRV>(c);
+  return enq_update_primitives_after<NRV>(c, stage);
 }
 
 // ------------------------------------------------------ NRV dispatch --------
@@ -429,8 +472,13 @@ int izem_gpu_init(const izem_cfg* cfg, const izem_thd* thd, const izem_adi* adi,
   if (!ng_ok || !dim_ok || !(cfg->nrv == 2 || cfg->nrv == 9) || thd->nspc != cfg->nrv) return IZEM_ERR_ARG;
   const int nmin = 2 * cfg->ng + 1;
   if (cfg->nx < nmin || cfg->ny < nmin || (cfg->ndim == 3 && cfg->nz < nmin)) return IZEM_ERR_ARG;
-  for (int f = 0; f < 6; ++f)
-    if (cfg->bc[f] != IZEM_BC_PERIODIC && cfg->bc[f] != IZEM_BC_EXTRAPOLATION) return IZEM_ERR_ARG;
+  for (int f = 0; f < 6; ++f) {
+    const int bc = cfg->bc[f];
+    if (bc < IZEM_BC_PERIODIC || bc > IZEM_BC_NSCBC_OUT) return IZEM_ERR_ARG;
+    // bc_inflowjet declares the W face only, bc_nscbc_out the E face only
+    if ((bc == IZEM_BC_INFLOWJET && f != IZEM_FACE_W) || (bc == IZEM_BC_NSCBC_OUT && f != IZEM_FACE_E))
+      return IZEM_ERR_ARG;
+  }
   for (int d = 0; d < 3; ++d)
     if ((cfg->bc[2 * d] == IZEM_BC_PERIODIC) != (cfg->bc[2 * d + 1] == IZEM_BC_PERIODIC)) return IZEM_ERR_ARG;
   izem_ctx* c = new izem_ctx();
@@ -511,7 +559,7 @@ int ctx_alloc(izem_ctx* c) {
       (e = alloc(&c->ha, nrv * nc)) || (e = alloc(&c->v0, nv * ni)) || (e = alloc(&c->f, nv * ni)) ||
       (e = alloc(&c->prim, PR_N * nc)) || (e = alloc(&c->Xa, nrv * nc)) || (e = alloc(&c->fhat, nv * maxf)) ||
       (e = alloc(&c->fd, (15 + 3 * nrv) * nc)) || (e = alloc(&c->tau, 6 * nc)) || (e = alloc(&c->qv, 3 * nc)) ||
-      (e = alloc(&c->d_dt, 1)))
+      (e = alloc(&c->d_dt, 4)))
     return ctx_fail(c, e == cudaErrorMemoryAllocation ? IZEM_ERR_NOMEM : IZEM_ERR_CUDA, "device allocation", e);
   for (int d = 0; d < 3; ++d)
     if ((e = alloc(&c->dxi[d], g.g[d]))) return ctx_fail(c, IZEM_ERR_CUDA, "device allocation", e);
@@ -520,7 +568,8 @@ int ctx_alloc(izem_ctx* c) {
   CK(cudaMalloc(&c->d_status, sizeof(DevStatus)));
   CK(cudaMemset(c->d_status, 0, sizeof(DevStatus)));
   CK(cudaMallocHost(&c->h_status, sizeof(DevStatus)));
-  CK(cudaMallocHost(&c->h_dt, sizeof(double)));
+  CK(cudaMallocHost(&c->h_dt, 2 * sizeof(double)));
+  CK(cudaMemset(c->d_dt, 0, 4 * sizeof(double)));   // dt, time0 of the step; zeros for calls outside rk3
   // zero the arrays whose ghost corners are never written
   CK(cudaMemset(c->v, 0, nv * nc * sizeof(double)));
   CK(cudaMemset(c->fd, 0, (15 + 3 * nrv) * nc * sizeof(double)));
@@ -547,7 +596,7 @@ void izem_gpu_destroy(izem_ctx* c) {
   if (c->d_chem_stats) cudaFree(c->d_chem_stats);
   if (c->h_chem_stats) cudaFreeHost(c->h_chem_stats);
   cudaFree(c->b_T); cudaFree(c->b_rho); cudaFree(c->b_Y); cudaFree(c->b_dt);
-  cudaFree(c->b_list); cudaFree(c->d_list_count); cudaFree(c->les);
+  cudaFree(c->b_list); cudaFree(c->d_list_count); cudaFree(c->les); cudaFree(c->d_y); cudaFree(c->d_z);
   if (c->h_status) cudaFreeHost(c->h_status);
   if (c->h_dt) cudaFreeHost(c->h_dt);
   for (auto& v : c->kt_pending)
@@ -652,13 +701,15 @@ int izem_gpu_finalize_ic(izem_ctx* c) {
 }
 
 int izem_gpu_rk3(izem_ctx* c, double dt, double time0) {
-  (void)time0;
   if (!c) return IZEM_ERR_ARG;
   if (!c->grid_set) return ctx_fail(c, IZEM_ERR_STATE, "grid not set", cudaSuccess);
+  if ((jet_face(c->cfg.bc[0]) || jet_face(c->cfg.bc[1])) && !c->have_coords)
+    return ctx_fail(c, IZEM_ERR_STATE, "jet faces need izem_gpu_set_coords", cudaSuccess);
   if (c->cfg.vis && c->cfg.eglib && !c->have_eg)
     return ctx_fail(c, IZEM_ERR_STATE, "EGLIB transport requested (cfg.eglib) but izem_gpu_set_eglib not called", cudaSuccess);
-  *c->h_dt = dt;
-  CK(cudaMemcpyAsync(c->d_dt, c->h_dt, sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  c->h_dt[0] = dt;
+  c->h_dt[1] = time0;
+  CK(cudaMemcpyAsync(c->d_dt, c->h_dt, 2 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   int rc;
   if (c->kt_enabled) {
     // timed mode: direct launches, each bracketed by events
@@ -786,6 +837,9 @@ static int chem_finish(izem_ctx* c, int mode, int sur_rc, double* DTmax) {
 
 int izem_gpu_chem_step(izem_ctx* c, double dt, int mode, double* DTmax) {
   if (!c || !DTmax) return IZEM_ERR_ARG;
+  if (jet_face(c->cfg.bc[0]) || jet_face(c->cfg.bc[1]))
+    return ctx_fail(c, IZEM_ERR_STATE, "the chemistry step is built for periodic and extrapolation faces only",
+                    cudaSuccess);
   if (!c->have_mech) return ctx_fail(c, IZEM_ERR_STATE, "no mechanism set", cudaSuccess);
   if (mode != IZEM_CHEM_BDF && mode != IZEM_CHEM_MLP) return ctx_fail(c, IZEM_ERR_ARG, "unknown chemistry mode", cudaSuccess);
   if (mode == IZEM_CHEM_MLP && !c->sur_m) return ctx_fail(c, IZEM_ERR_STATE, "no surrogate set", cudaSuccess);
@@ -1031,6 +1085,35 @@ int izem_gpu_set_sensor_xblocks(izem_ctx* c, int nblk) {
   c->sensor_bx = c->cfg.nx / nblk;
   c->nedge = (long long)(nblk - 1) * c->cfg.ny * c->cfg.nz;
   if (c->nedge > 0) CK(cudaMalloc(&c->fhat_edge, (size_t)c->nv * c->nedge * sizeof(double)));
+  return IZEM_OK;
+}
+
+int izem_gpu_set_coords(izem_ctx* c, const double* x, const double* y, const double* z, double lx) {
+  if (!c || !x || !y || !z) return IZEM_ERR_ARG;
+  (void)x;
+  if (!c->d_y) {
+    CK(cudaMalloc(&c->d_y, c->g.n[1] * sizeof(double)));
+    CK(cudaMalloc(&c->d_z, c->g.n[2] * sizeof(double)));
+  }
+  CK(cudaMemcpy(c->d_y, y, c->g.n[1] * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(c->d_z, z, c->g.n[2] * sizeof(double), cudaMemcpyHostToDevice));
+  const izem_adi& a = c->adi;
+  JetArgs& j = c->jet;
+  j.y = c->d_y;
+  j.z = c->d_z;
+  j.lx = lx;
+  j.dxi0 = c->dxi[0];
+  // bc_inflowjet's constants (module_BCs.f90:1680-1700) and bc_nscbc_out's
+  // far-field pressure (:2390), in code units as the routines divide them
+  j.hbuse = 0.0010 / a.l_ref;
+  j.tmaxy = 0.0001 / a.time_ref;
+  j.u2 = 20.0 / a.u_ref;
+  j.T1 = 1000.0 / a.t_ref;
+  j.T2 = 300.0 / a.t_ref;
+  j.P1 = 101325.0 * 15.0 / a.p_ref;
+  j.P2 = 101325.0 / a.p_ref;
+  j.pinf = 94232.25 / a.p_ref;
+  c->have_coords = true;
   return IZEM_OK;
 }
 

@@ -125,8 +125,11 @@ __global__ void k_prim_woT(Geo g, const double* __restrict__ v, const double* __
 // extrapolation, then force_sumY and W_i on the ghost point.
 // mode 0: periodic faces wrap, boundary faces extrapolate (comm_cons +
 // upd_boundaries); mode 1: every face extrapolates (upd_extrapolation).
+// mask: the faces (bit f) this launch treats; mode 2: no copy, only the
+// force_sumY and W_i of ghost points that a Dirichlet face kernel wrote.
 template <int NRV>
-__global__ void k_halo(Geo g, int mode, int forcesum, double* __restrict__ v, double* __restrict__ W_i) {
+__global__ void k_halo(Geo g, int mode, int forcesum, double* __restrict__ v, double* __restrict__ W_i,
+                       int mask = 0x3f) {
   constexpr int NV = IZEM_NIV + NRV;
   long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   const long long ntot = slab_count(g) - g.nint;
@@ -134,13 +137,16 @@ __global__ void k_halo(Geo g, int mode, int forcesum, double* __restrict__ v, do
   int i, j, k, dom;
   if (!slab_point(g, idx + g.nint, i, j, k, dom)) return;
   const int f = dom - 1, d = f >> 1;
+  if (!((mask >> f) & 1)) return;
   int c[3] = {i, j, k};
   if (mode == 0 && g.bc[f] == IZEM_BC_PERIODIC) c[d] = (f & 1) ? c[d] - g.n[d] : c[d] + g.n[d];
   else c[d] = (f & 1) ? g.n[d] : 1;
   const long long nc = g.ncell;
   const long long p = gid(g, i, j, k), q = gid(g, c[0], c[1], c[2]);
+  if (mode != 2) {
 #pragma unroll
-  for (int l = 0; l < NV; ++l) v[l * nc + p] = v[l * nc + q];
+    for (int l = 0; l < NV; ++l) v[l * nc + p] = v[l * nc + q];
+  }
   if (forcesum) force_sumY_cell<NRV>(v, nc, p);
   W_i[p] = wmix_cell<NRV>(v, nc, p);
 }
@@ -153,7 +159,18 @@ __global__ void k_newton_iter(Geo g, int ghost, const double* __restrict__ v, do
                               double* __restrict__ cp, double* __restrict__ ha, DevStatus* st, int check_negT) {
   long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   int i, j, k, dom;
-  if (ghost) {
+  if (ghost == 2) {
+    // the Dirichlet planes i = 1 (sub-domain 7) and i = nx (8) of jet faces
+    const long long np = (long long)g.n[1] * g.n[2];
+    if (idx >= 2 * np) return;
+    const int face = (int)(idx / np);
+    if (g.bc[face] != IZEM_BC_INFLOWJET && g.bc[face] != IZEM_BC_NSCBC_OUT) return;
+    const long long r = idx - face * np;
+    i = face ? g.n[0] : 1;
+    j = (int)(r % g.n[1]) + 1;
+    k = (int)(r / g.n[1]) + 1;
+    dom = 7 + face;
+  } else if (ghost) {
     const long long ntot = slab_count(g) - g.nint;
     if (idx >= ntot) return;
     if (!slab_point(g, idx + g.nint, i, j, k, dom)) return;
@@ -342,4 +359,208 @@ __global__ void k_dtv(Geo g, Metrics mt, const double* __restrict__ v, const dou
     }
     atomic_min_pos(&st->fo_ctmin_bits, rct);
   }
+}
+
+// Jet boundaries (module_BCs.f90).  The step start time and the step are
+// read from device memory (tdt[0] = dt, tdt[1] = time0), so that the
+// captured RK3 graph sees each step's values; tk is the stage fraction of
+// timek = time0 + dt tk3(ik) (module_solver.f90:756).
+struct JetArgs {
+  const double* y;      // interior coordinates (code units), ny
+  const double* z;      // nz
+  const double* tdt;    // device: dt, time0
+  double tk;
+  double lx;            // domain length in x (code units)
+  double hbuse, tmaxy, u2, T1, T2, P1, P2, pinf;   // the routines' constants in code units
+  const double* dxi0;   // x metrics, ghosted index
+};
+
+// bc_inflowjet (module_BCs.f90:1646-1791), W face: one thread per (j, k)
+// writes the ghost points and the first interior plane.  The exit sound
+// speed uses a mass-fraction array whose unset entries are taken as 0.
+template <int NRV>
+__global__ void k_bc_inflowjet(Geo g, JetArgs ja, double* __restrict__ v) {
+  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= (long long)g.n[1] * g.n[2]) return;
+  const int j = (int)(idx % g.n[1]) + 1, k = (int)(idx / g.n[1]) + 1;
+  const double time = ja.tdt[1] + ja.tdt[0] * ja.tk;
+  double T_1 = ja.T1, P_1 = ja.P1, Ya_1 = 1.0;
+  const double T_2 = ja.T2, P_2 = ja.P2, Ya_2 = 0.0, u_2 = ja.u2;
+  if (time <= ja.tmaxy) {
+    P_1 = (P_2 - (P_2 - P_1) * (time / ja.tmaxy) * (time / ja.tmaxy) * (time / ja.tmaxy));
+    Ya_1 = (Ya_2 - (Ya_2 - Ya_1) * (time / ja.tmaxy) * (time / ja.tmaxy) * (time / ja.tmaxy));
+    T_1 = (T_2 - (T_2 - T_1) * (time / ja.tmaxy) * (time / ja.tmaxy) * (time / ja.tmaxy));
+  }
+  double Ya[NRV];
+#pragma unroll
+  for (int l = 0; l < NRV; ++l) Ya[l] = 0.0;
+  if constexpr (NRV == 2) { Ya[0] = 0.233; Ya[1] = 0.767; }
+  else if constexpr (NRV == 3) { Ya[0] = Ya_1; Ya[1] = 0.0; Ya[2] = 1.0 - Ya_1; }
+  else if constexpr (NRV == 9) { Ya[1] = Ya_1; Ya[3] = 0.0; Ya[8] = 1.0 - Ya_1; }
+  double Ws_i = 0.0;
+#pragma unroll
+  for (int l = 0; l < NRV; ++l) Ws_i = Ws_i + Ya[l] * c_thd.Wc_i[l];
+  const double cps = th_cp_mix<NRV>(T_1, Ya);
+  double gamma = c_thd.gam2 * Ws_i / cps;
+  gamma = 1.0 / (1.0 - gamma);
+  const double cs = sqrt(gamma * Ws_i * T_1);
+  const double u_1 = 1.01 * cs;
+  const double delt = 1.0 / (0.04 * ja.hbuse), y0 = ja.hbuse / 2.0;
+  const double yy = ja.y[j - 1], zz = ja.z[k - 1];
+  const double rrr = sqrt(yy * yy + zz * zz);
+  const double th = tanh((rrr - y0) * delt);
+  const double ux = 0.5 * ((u_1 + u_2) - (u_1 - u_2) * th);
+  const double T = 0.5 * ((T_1 + T_2) - (T_1 - T_2) * th);
+  const double P = 0.5 * ((P_1 + P_2) - (P_1 - P_2) * th);
+  const double vy = 0.0, wz = 0.0;
+#pragma unroll
+  for (int l = 0; l < NRV; ++l) Ya[l] = 0.0;
+  if constexpr (NRV == 2) {
+    Ya[0] = 0.233;
+    Ya[1] = 1.0 - Ya[0];
+  } else if constexpr (NRV == 3) {
+    Ya[0] = 0.5 * ((Ya_1 + 0.0) - (Ya_1 - 0.0) * th);
+    Ya[1] = 0.5 * ((0.0 + 0.233) - (0.0 - 0.233) * th);
+    Ya[2] = 0.5 * ((1.0 - Ya_1 + 0.767) - (1.0 - Ya_1 - 0.767) * th);
+  } else if constexpr (NRV == 9) {
+    Ya[1] = 0.5 * ((Ya_1 + 0.0) - (Ya_1 - 0.0) * th);
+    Ya[3] = 0.5 * ((0.0 + 0.233) - (0.0 - 0.233) * th);
+    Ya[8] = 0.5 * ((1.0 - Ya_1 + 0.767) - (1.0 - Ya_1 - 0.767) * th);
+  }
+  Ws_i = 0.0;
+#pragma unroll
+  for (int l = 0; l < NRV; ++l) Ws_i = Ws_i + Ya[l] * c_thd.Wc_i[l];
+  const double rho = P / (T * Ws_i);
+  double hm = 0.0;
+#pragma unroll
+  for (int l = 0; l < NRV; ++l) {
+    double cpk;
+    hm = hm + th_species(l, T, &cpk) * Ya[l];
+  }
+  const long long nc = g.ncell;
+  for (int i = 1 - g.ng; i <= 1; ++i) {
+    const long long p = gid(g, i, j, k);
+    v[p] = rho;
+    v[nc + p] = rho * ux;
+    v[2 * nc + p] = rho * vy;
+    v[3 * nc + p] = rho * wz;
+    v[4 * nc + p] = rho * hm - P + 0.5 * rho * (ux * ux + vy * vy + wz * wz);
+#pragma unroll
+    for (int l = 0; l < NRV; ++l) v[(IZEM_NIV + l) * nc + p] = rho * Ya[l];
+  }
+}
+
+// bc_nscbc_out (module_BCs.f90:2331-2516), E face: one thread per (j, k);
+// 4th-order one-sided derivatives at the last interior point, the incoming
+// wave relaxed toward the far-field pressure, the state advanced by dt
+// written at the last interior plane and the ghost points.
+template <int NRV>
+__global__ void k_bc_nscbc_out(Geo g, JetArgs ja, const double* __restrict__ T, const double* __restrict__ W_i,
+                               const double* __restrict__ cp, double* __restrict__ v) {
+  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= (long long)g.n[1] * g.n[2]) return;
+  const int j = (int)(idx % g.n[1]) + 1, k = (int)(idx / g.n[1]) + 1;
+  const double a4or[5] = {-3.0 / 12.0, 16.0 / 12.0, -36.0 / 12.0, 48.0 / 12.0, -25.0 / 12.0};   // m = -4..0
+  const double dtime = ja.tdt[0], sigma1 = 0.28, Pinf = ja.pinf, Lx = ja.lx;
+  const int ex = g.n[0];
+  const double dxe = ja.dxi0[ex - 1 + g.ng];
+  const long long nc = g.ncell;
+  const long long p = gid(g, ex, j, k);
+  double Machm = 0.0;
+  double rho = v[p], rho_i = 1.0 / rho;
+  double ux = v[nc + p] * rho_i, vy = v[2 * nc + p] * rho_i, wz = v[3 * nc + p] * rho_i;
+  double Pres = v[p] * T[p] * W_i[p];
+  double gam = c_thd.gam2 * W_i[p] / cp[p];
+  gam = 1.0 / (1.0 - gam);
+  double cs = sqrt(gam * Pres * rho_i);
+  const double Mach = sqrt(ux * ux + vy * vy + wz * wz) / cs;
+  Machm = fmax(Machm, Mach);
+  double drho = 0.0, dux = 0.0, dvy = 0.0, dwz = 0.0, dPres = 0.0;
+  double Ya[NRV], dYa[NRV];
+#pragma unroll
+  for (int l = 0; l < NRV; ++l) dYa[l] = 0.0;
+#pragma unroll
+  for (int m = -4; m <= 0; ++m) {
+    const long long q = gid(g, ex + m, j, k);
+    rho = v[q];
+    rho_i = 1.0 / rho;
+    ux = v[nc + q] * rho_i;
+    vy = v[2 * nc + q] * rho_i;
+    wz = v[3 * nc + q] * rho_i;
+    Pres = v[q] * T[q] * W_i[q];
+#pragma unroll
+    for (int l = 0; l < NRV; ++l) Ya[l] = v[(IZEM_NIV + l) * nc + q] * rho_i;
+    const double w = a4or[m + 4];
+    drho = drho + w * rho;
+    dux = dux + w * ux;
+    dvy = dvy + w * vy;
+    dwz = dwz + w * wz;
+    dPres = dPres + w * Pres;
+#pragma unroll
+    for (int l = 0; l < NRV; ++l) dYa[l] = dYa[l] + w * Ya[l];
+  }
+  drho = -drho * dxe;
+  dux = -dux * dxe;
+  dvy = -dvy * dxe;
+  dwz = -dwz * dxe;
+  dPres = -dPres * dxe;
+#pragma unroll
+  for (int l = 0; l < NRV; ++l) dYa[l] = -dYa[l] * dxe;
+  double L1 = 0.0, L2 = 0.0, L3 = 0.0, L4 = 0.0, L5 = 0.0, L5_Ya[NRV];
+#pragma unroll
+  for (int l = 0; l < NRV; ++l) L5_Ya[l] = 0.0;
+  gam = c_thd.gam2 * W_i[p] / cp[p];
+  gam = 1.0 / (1.0 - gam);
+  cs = sqrt(gam * Pres * rho_i);
+  if (ux - cs < 0.0) L1 = sigma1 * (1.0 - Machm * Machm) * cs / Lx * (Pres - Pinf);
+  else L1 = (ux - cs) * (dPres - rho * cs * dux);
+  if (ux + cs > 0.0) L5 = (ux + cs) * (dPres + rho * cs * dux);
+  else L5 = (ux + cs) * (2.0 * dPres - L1 / (ux - cs));
+  if (ux > 0.0) {
+    L2 = ux * (cs * cs * drho - dPres);
+    L3 = ux * dvy;
+    L4 = ux * dwz;
+#pragma unroll
+    for (int l = 0; l < NRV; ++l) L5_Ya[l] = ux * dYa[l];
+  } else {
+    L2 = ux * cs * cs * drho - 0.5 * ux * (L5 / (ux + cs) + L1 / (ux - cs));
+  }
+  const double d2 = 0.5 * (L5 + L1);
+  const double d1 = (L2 + d2) / (cs * cs);
+  const double d3 = 0.5 * (L5 - L1) / (cs * rho);
+  const double d4 = L3, d5 = L4;
+  double hm = 0.0;
+#pragma unroll
+  for (int l = 0; l < NRV; ++l) {
+    double cpk;
+    hm = hm + th_species(l, T[p], &cpk) * Ya[l];
+  }
+  const double kin = ux * ux + vy * vy + wz * wz;
+  for (int i = ex; i <= ex + g.ng; ++i) {
+    const long long o = gid(g, i, j, k);
+    v[o] = rho - d1 * dtime;
+    v[nc + o] = (rho * ux) - (ux * d1 + rho * d3) * dtime;
+    v[2 * nc + o] = (rho * vy) - (vy * d1 + rho * d4) * dtime;
+    v[3 * nc + o] = (rho * wz) - (wz * d1 + rho * d5) * dtime;
+    v[4 * nc + o] = (rho * hm - Pres + 0.5 * rho * kin) -
+                    (0.5 * kin * d1 + rho * (ux * d3 + vy * d4 + wz * d5) + d2 / (gam - 1.0)) * dtime;
+#pragma unroll
+    for (int l = 0; l < NRV; ++l)
+      v[(IZEM_NIV + l) * nc + o] = (rho * Ya[l]) - (Ya[l] * d1 + rho * L5_Ya[l]) * dtime;
+  }
+}
+
+// upd_prim_var_dirichlet's force_sumY and W_i on the Dirichlet planes i = 1
+// and i = nx of jet faces (before their Newton solve).
+template <int NRV>
+__global__ void k_dirichlet_prep(Geo g, int forcesum, double* __restrict__ v, double* __restrict__ W_i) {
+  const long long np = (long long)g.n[1] * g.n[2];
+  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= 2 * np) return;
+  const int face = (int)(idx / np);
+  if (g.bc[face] != IZEM_BC_INFLOWJET && g.bc[face] != IZEM_BC_NSCBC_OUT) return;
+  const long long r = idx - face * np;
+  const long long p = gid(g, face ? g.n[0] : 1, (int)(r % g.n[1]) + 1, (int)(r / g.n[1]) + 1);
+  if (forcesum) force_sumY_cell<NRV>(v, g.ncell, p);
+  W_i[p] = wmix_cell<NRV>(v, g.ncell, p);
 }

@@ -196,3 +196,39 @@ def batched_reactors(n, seed=SEED):
     Wmix = 1.0 / (Y / W).sum(axis=1)
     rho = p * Wmix * 1e-3 / (8.314510 * T) * 1e-3    # kg/m^3 -> g/cm^3
     return np.ascontiguousarray(T), np.ascontiguousarray(rho), np.ascontiguousarray(Y), np.ascontiguousarray(dt)
+
+
+def jet(nx=24, ny=16, nz=16, species="o2n2", Lx=4e-3, Lr=1.5e-3, uco=20.0, lib_dscalar=None):
+    """Box for the reference's jet boundaries: bc_inflowjet on the W face
+    (the 1 mm nozzle centred on y = z = 0), bc_nscbc_out on the E face,
+    y and z extrapolation; initially air (the 21/79-ish O2/N2 mass
+    fractions 0.233/0.767 of the species set) at 300 K, 1 atm, moving at
+    uco in x.  Returns cfg, thd, adi, dxi, state, info; info["coords"]
+    holds the interior coordinates in code units and info["lx"] the domain
+    length Lx = (x_last - x_first) / L_ref (module_tools.f90:319,489)."""
+    from .capi import BC_INFLOWJET, BC_NSCBC_OUT
+    a = constants()
+    sp = load_species(species)
+    thd = thd_init(sp, a)
+    names = sp["names"]
+    x = np.arange(nx) * (Lx / (nx - 1))
+    y = -Lr + np.arange(ny) * (2 * Lr / (ny - 1))
+    z = -Lr + np.arange(nz) * (2 * Lr / (nz - 1))
+    Xg, Yg, Zg = np.meshgrid(x, y, z, indexing="ij")
+    Ya = np.zeros(len(names))
+    Ya[names.index("O2")] = 0.233
+    Ya[names.index("N2")] = 0.767
+    Ys = np.broadcast_to(Ya, Xg.shape + (len(names),)).copy()
+    T = np.full(Xg.shape, 300.0)
+    Wmix_i = np.einsum("...k,k->...", Ys, 1.0 / (np.array(sp["W_gmol"]) * 1e-3))
+    rho = 101325.0 / (a["r_ref"] * Wmix_i * T)
+    u = np.full(Xg.shape, uco)
+    zero = np.zeros(Xg.shape)
+    state = _state_from_primitives(thd, a, rho, u, zero, zero, T, Ys, 3)
+    bc = (BC_INFLOWJET, BC_NSCBC_OUT, BC_EXTRAPOLATION, BC_EXTRAPOLATION, BC_EXTRAPOLATION, BC_EXTRAPOLATION)
+    cfg = make_cfg(nx, ny, nz, len(names), bc=bc)
+    dxi = [grid_dxi(c, 3, a, lib_dscalar) for c in (x, y, z)]
+    L = a["l_ref"]
+    info = {"name": "jet box %dx%dx%d (%s)" % (nx, ny, nz, species),
+            "coords": (x / L, y / L, z / L), "lx": (x[-1] - x[0]) / L, "time_ref": a["time_ref"]}
+    return cfg, thd, adi_struct(a), dxi, state, info

@@ -79,6 +79,7 @@ def load_library(path=None):
         "izem_gpu_set_sensor_xblocks": (C.c_int, [P, C.c_int]),
         "izem_gpu_set_chem_skip": (C.c_int, [P, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_int]),
         "izem_gpu_set_les": (C.c_int, [P, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double]),
+        "izem_gpu_set_coords": (C.c_int, [P, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double]),
         "izem_gpu_chem_autotune": (C.c_int, [C.POINTER(IzemMech), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                                              C.c_void_p, C.c_int, C.c_char_p, C.c_int]),
         "izem_gpu_chem_surrogate_stats": (C.c_int, [P, C.POINTER(C.c_longlong), C.POINTER(C.c_int),
@@ -296,6 +297,12 @@ class IzemGPU:
         """Reproduce a reference run decomposed into nblk MPI blocks along x:
         the shock sensor is not shared between blocks (izem_gpu_set_sensor_xblocks)."""
         self._check(self.lib.izem_gpu_set_sensor_xblocks(self.h, int(nblk)), "set_sensor_xblocks")
+
+    def set_coords(self, x, y, z, lx):
+        """Interior coordinates (code units) and Lx for the jet faces
+        (izem_gpu_set_coords)."""
+        xs = [np.ascontiguousarray(a, dtype=np.float64) for a in (x, y, z)]
+        self._check(self.lib.izem_gpu_set_coords(self.h, *[a.ctypes.data for a in xs], float(lx)), "set_coords")
 
     def set_les(self, mu_sgs_factor=0.18, sc_sgs=0.7, pr_sgs=0.7, percent_weight_sgs=70.0, enable=True):
         """[IFLES] LES = T, MU_SGS_MODEL = SMAGORINSKY under EGLIB

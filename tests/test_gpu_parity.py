@@ -328,3 +328,33 @@ def test_negative_pressure_is_reported_not_computed():
     fl = g.flux()
     g.close()
     assert np.all(np.isfinite(fl))
+
+
+@pytest.mark.parametrize("species", ["o2n2", "h2air9"])
+def test_rk3_steps_jet_faces(species):
+    """The jet faces (bc_inflowjet W, bc_nscbc_out E, closed by
+    upd_prim_var_dirichlet) inside the captured RK3 graph: three steps as
+    the nozzle ramps in from t = 0, then a short step past the 0.1 ms ramp
+    (the full nozzle state), against the oracle on the same state."""
+    from phd_gb300 import ics
+    import oracle
+    cfg, thd, adi, dxi, st, info = ics.jet(species=species, lib_dscalar=oracle.metrics_dscalar)
+    orc = oracle.Oracle(cfg, thd, adi, *dxi)
+    orc.finalize_ic(st)
+    orc.set_coords(*info["coords"], info["lx"])
+    g = gpu_from(cfg, thd, adi, dxi, st)
+    g.set_coords(*info["coords"], info["lx"])
+    t = 0.0
+    for step in range(4):
+        dt4, dt = orc.timestep(st)
+        if step == 3:
+            t, dt = 2e-4 / info["time_ref"], 0.01 * dt
+        orc.rk3(st, dt, t)
+        g.rk3(dt, t)
+        t = t + dt
+    got = g.download()
+    g.close()
+    ng = cfg.ng
+    err = W.normwise(got["v"][:ng + cfg.nx + ng, ng:-ng, ng:-ng], st["v"][:ng + cfg.nx + ng, ng:-ng, ng:-ng])
+    assert np.all(err <= TOL), err
+    assert np.max(np.abs(interior(got["T"]) - interior(st["T"]))) <= TOL * np.max(st["T"])
