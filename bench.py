@@ -180,6 +180,8 @@ def run_gpu(args, rank, world):
     cfg.reaction = 1 if chem else 0
     eg = args.workload == "mix" and args.transport == "eglib"
     cfg.eglib = 1 if eg else 0
+    if args.vis_dt:
+        cfg.vis_dt = 1
     g = IzemGPU(cfg, thd, adi)
     if eg:
         from phd_gb300.thd import eglib_link, load_species
@@ -189,6 +191,20 @@ def run_gpu(args, rank, world):
     g.finalize_ic()
     if chem:
         g.set_mechanism(h2_mechanism())
+    options = {}
+    if args.les is not None:
+        g.set_les(mu_sgs_factor=args.les)
+        options["les"] = "Smagorinsky under EGLIB, MU_SGS_FACTOR %g" % args.les
+    if args.dvodesimp and chem:
+        from phd_gb300.thd import load_species
+        names = load_species("h2air9")["names"]
+        ih2, in2 = names.index("H2"), names.index("N2")
+        yf = np.zeros(9); yf[ih2] = 0.5; yf[in2] = 0.5                               # the fuel stream
+        yo = np.zeros(9); yo[names.index("O2")] = 0.233; yo[in2] = 0.767             # the air stream
+        g.set_chem_skip(yf, yo, ih2, in2)
+        options["dvodesimp"] = "chemistry skipped in the pure streams and where rates are negligible"
+    if args.vis_dt:
+        options["vis_dt"] = "Fourier time-step criteria"
     stp = Stepper(g, chem)
     ncell = cfg.nx * cfg.ny * cfg.nz
     # warm-up, then the thread blocks of the dominant kernels chosen by timing
@@ -286,7 +302,8 @@ def run_gpu(args, rank, world):
                                  if chem else "off"),
                    "l2": "inputs larger than L2 (state %.2f GB)" % (host["v"].nbytes / 1e9),
                    "parallelism": "replicas" if world > 1 else "single GPU",
-                   "autotuned_threads_per_block": {k: v["chosen"] for k, v in tuning.items()}},
+                   "autotuned_threads_per_block": {k: v["chosen"] for k, v in tuning.items()},
+                   **({"options": options} if options else {})},
         "e2e": {"value": e2e_value, "unit": "Mcell-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "steps": e2e_steps, "ms_per_step": e2e_s * 1e3 / e2e_steps,
                 "copy_ms_per_step": t_copy * 1e3 / e2e_steps},
@@ -625,6 +642,10 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-chem", action="store_true", help="mixing layer without the chemistry half-steps")
     ap.add_argument("--no-mlp", action="store_true", help="skip the learned-chemistry leg of the reacting step")
+    ap.add_argument("--les", type=float, default=None,
+                    help="mixing layer with the Smagorinsky closure (EGLIB) at this MU_SGS_FACTOR")
+    ap.add_argument("--dvodesimp", action="store_true", help="mixing layer with the dvodesimp chemistry skip")
+    ap.add_argument("--vis-dt", action="store_true", help="mixing layer with the Fourier time-step criteria")
     ap.add_argument("--transport", default="eglib", choices=["eglib", "fitted"],
                     help="viscous transport of the mixing layer (EGLIB precision 1 or the tranfit fits)")
     args = ap.parse_args()
