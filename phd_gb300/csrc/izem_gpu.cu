@@ -688,6 +688,8 @@ int izem_gpu_visc_flux(izem_ctx* c) {
 
 int izem_gpu_update_primitives(izem_ctx* c) {
   if (!c) return IZEM_ERR_ARG;
+  if ((jet_face(c->cfg.bc[0]) || jet_face(c->cfg.bc[1])) && !c->have_coords)
+    return ctx_fail(c, IZEM_ERR_STATE, "jet faces need izem_gpu_set_coords", cudaSuccess);
   int rc = IZEM_DISPATCH(c, do_update_primitives, c);
   if (rc) return rc;
   return read_status(c);
