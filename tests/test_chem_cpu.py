@@ -1,6 +1,8 @@
 """Chemistry oracle checks on the CPU: the CHEMKIN-format mechanism, the
 restated DVODE against the real DVODE shipped in scipy (same algorithm,
 MF = 22, same tolerances), element conservation of the reactor."""
+import os
+
 import numpy as np
 import pytest
 
@@ -164,3 +166,22 @@ def test_dvodesimp_skips_pure_streams_and_keeps_the_rest():
     orc.set_chem_skip(enable=False)
     again = W.copy(st)
     assert orc.chem_step(again, m, 0.5) == dtm_full and np.array_equal(again["v"], full["v"])
+
+
+@pytest.mark.skipif(not os.path.isdir(os.environ.get("IZEM_REFERENCE_TESTCASES", "/root/reference/devel-izem/testcases")),
+                    reason="reference tree not mounted")
+def test_mechanism_species_match_reference_interpreter_output():
+    """The species, their order and molecular weights of the shipped
+    mechanism are those of the reference's CHEMKIN interpreter listing for
+    the 9-species case (testcases/shockedshearlayer/chem.out)."""
+    ref = os.environ.get("IZEM_REFERENCE_TESTCASES", "/root/reference/devel-izem/testcases")
+    rows = []
+    for line in open(os.path.join(ref, "shockedshearlayer", "chem.out")):
+        t = line.split()
+        if len(t) >= 8 and t[0].endswith(".") and t[0][:-1].isdigit() and t[2] == "G":
+            rows.append((t[1], float(t[4])))
+    m = h2_mechanism()
+    names = load_species("h2air9")["names"]
+    assert [n for n, _ in rows] == names
+    for k, (_, w) in enumerate(rows):
+        assert abs(m.wt[k] - w) <= 5e-6 * w, (names[k], m.wt[k], w)
