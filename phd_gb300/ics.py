@@ -201,9 +201,8 @@ def batched_reactors(n, seed=SEED):
 def jet(nx=24, ny=16, nz=16, species="o2n2", Lx=4e-3, Lr=1.5e-3, uco=20.0, lib_dscalar=None):
     """Box for the reference's jet boundaries: bc_inflowjet on the W face
     (the 1 mm nozzle centred on y = z = 0), bc_nscbc_out on the E face,
-    y and z extrapolation; initially air (the 21/79-ish O2/N2 mass
-    fractions 0.233/0.767 of the species set) at 300 K, 1 atm, moving at
-    uco in x.  Returns cfg, thd, adi, dxi, state, info; info["coords"]
+    y and z extrapolation; initially air (O2/N2 mass fractions 0.233/0.767,
+    the other species 0) at 300 K and 1 atm, moving at uco in x.  Returns cfg, thd, adi, dxi, state, info; info["coords"]
     holds the interior coordinates in code units and info["lx"] the domain
     length Lx = (x_last - x_first) / L_ref (module_tools.f90:319,489)."""
     from .capi import BC_INFLOWJET, BC_NSCBC_OUT
