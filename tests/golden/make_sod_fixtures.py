@@ -26,7 +26,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 from phd_gb300.restart import read_h5  # noqa: E402
-RESTARTS = (1, 2, 3)
+RESTARTS = (1, 2, 3, 10)
 
 
 def read_grid(path):
