@@ -15,8 +15,10 @@ Run from the repository root, where the reference tree is readable:
 
 It writes tests/golden/sod_restart_000NN.npz (arrays rho, rhoU, rhoV, rhoW,
 rhoE, O2, N2 with shape (ntx, nty, ntz) in Fortran index order, and time)
-and tests/golden/sod_grid.npz (the x, y, z coordinates of grid.dat, in
-metres, parsed as the reference's list-directed read parses them).
+tests/golden/sod_grid.npz (the x, y, z coordinates of grid.dat, in
+metres, parsed as the reference's list-directed read parses them) and
+tests/golden/sod_plot_000NN.npz (temperature, pressure, density and x
+velocity of the post-processor's FP32 plot files, dimensional).
 """
 import os
 import sys
@@ -27,6 +29,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 from phd_gb300.restart import read_h5  # noqa: E402
 RESTARTS = (1, 2, 3, 10)
+PLOTS = (1, 3)
 
 
 def read_grid(path):
@@ -44,6 +47,38 @@ def read_grid(path):
     return {k: np.array(v, dtype=np.float64) for k, v in out.items()}
 
 
+def read_vtr(path):
+    """(piece extent, {name: FP64 array}) of a VTK RectilinearGrid piece in
+    raw appended big-endian FP32 (each block prefixed by its byte count), as
+    the reference's post-processor writes plots/plotNNNNN_BBBBB.vtr."""
+    import re
+    d = open(path, "rb").read()
+    head = d[:d.index(b"<AppendedData")].decode()
+    arrs = re.findall(r'Name="([^"]+)" NumberOfComponents="1" format="appended" offset="(\d+)"', head)
+    ext = [int(x) for x in re.search(r'Piece Extent="([^"]+)"', head).group(1).split()]
+    start = d.index(b"_", d.index(b"<AppendedData")) + 1
+    out = {}
+    for name, off in arrs:
+        o = start + int(off)
+        n = int.from_bytes(d[o:o + 4], "big")
+        out[name] = np.frombuffer(d[o + 4:o + 4 + n], dtype=">f4").astype(np.float64)
+    return ext, out
+
+
+def plot_fields(sod_dir, n):
+    """The two x-blocks of plot n merged on the 400 x 11 grid (the blocks
+    share the point at x index 200)."""
+    fields = {}
+    for piece in (0, 1):
+        ext, d = read_vtr(os.path.join(sod_dir, "plots", "plot%05d_%05d.vtr" % (n, piece)))
+        nxp, nyp = ext[1] - ext[0] + 1, ext[3] - ext[2] + 1
+        for name, key in (("Temperature", "T"), ("Pressure", "P"), ("Density", "rho"), ("Velocity-X", "u")):
+            a = d[name].reshape(nyp, nxp).T
+            f = fields.setdefault(key, np.zeros((400, nyp)))
+            f[ext[0] - 1:ext[1]] = a
+    return fields
+
+
 def main(sod_dir):
     np.savez_compressed(os.path.join(HERE, "sod_grid.npz"), **read_grid(os.path.join(sod_dir, "grid.dat")))
     for n in RESTARTS:
@@ -51,6 +86,8 @@ def main(sod_dir):
         arrays = {k.split("/")[1]: v for k, v in f.items() if k.startswith("consvar/")}
         arrays["time"] = np.asarray(f["simulation/time"]).reshape(-1)[:1]
         np.savez_compressed(os.path.join(HERE, "sod_restart_%05d.npz" % n), **arrays)
+        if n in PLOTS:
+            np.savez_compressed(os.path.join(HERE, "sod_plot_%05d.npz" % n), **plot_fields(sod_dir, n))
         print(n, {k: v.shape for k, v in arrays.items()}, float(arrays["time"][0]))
 
 

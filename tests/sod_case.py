@@ -34,6 +34,12 @@ def golden(n):
     return np.load(os.path.join(HERE, "golden", "sod_restart_%05d.npz" % n))
 
 
+def golden_plot(n):
+    """Temperature [K], pressure [Pa], density [kg/m^3] and x velocity [m/s]
+    of the reference's plot file n (FP32), shape (ntx, nty)."""
+    return np.load(os.path.join(HERE, "golden", "sod_plot_%05d.npz" % n))
+
+
 def sod_case(xblocks=NX_BLOCKS):
     """Configuration, species data, references, oracle, the ghosted initial
     state (closed by finalize_ic) and the metrics (dx_i, dy_i, dz_i) of the
@@ -114,11 +120,11 @@ def stat_times(a, n):
     return [x / a["time_ref"] for x in t]
 
 
-def run_to_stats(orc, st, a, nstats):
+def run_to_stats(orc, st, a, nstats, extra=False):
     """The main loop of izem.f90:240-330 without chemistry: timestep, the
     step that would pass the next statistics time clipped onto it, rk3.
     Returns [(time, steps, copy of v)] at each of the first nstats
-    statistics times."""
+    statistics times; with extra, copies of T and W_i follow v."""
     timing = stat_times(a, nstats)
     time, nb, ite, out = 0.0, 0, 0, []
     while nb < nstats:
@@ -132,5 +138,6 @@ def run_to_stats(orc, st, a, nstats):
         time = time + dtmin
         if write:
             nb += 1
-            out.append((time, ite, st["v"].copy()))
+            keep = (st["v"].copy(), st["T"].copy(), st["W_i"].copy()) if extra else (st["v"].copy(),)
+            out.append((time, ite) + keep)
     return out

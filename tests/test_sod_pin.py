@@ -30,14 +30,14 @@ PINNED = [1, 2, 3, 10]      # restart files held as fixtures (tests/golden/make_
 @pytest.fixture(scope="module")
 def sod_run():
     cfg, thd, a, orc, st, _ = S.sod_case()
-    return S.run_to_stats(orc, st, a, 10)
+    return a, S.run_to_stats(orc, st, a, 10, extra=True)
 
 
 def test_sod_stat_times_match_reference_exactly(sod_run):
     """The CFL step sequence and the clipping onto the statistics times land
     on the reference's stored times bit for bit."""
     for n in PINNED:
-        time, steps, _ = sod_run[n - 1]
+        time, steps = sod_run[1][n - 1][:2]
         assert time == float(S.golden(n)["time"][0]), (n, time, steps)
 
 
@@ -48,7 +48,7 @@ def test_sod_state_matches_reference_restart(sod_run, n):
     magnitude, the x momentum within 1e-6 of its largest magnitude; the y and
     z momenta (rounding noise of the 2-D run, 1e-13 of the density) within
     1e-10 of the largest density."""
-    _, _, v = sod_run[n - 1]
+    v = sod_run[1][n - 1][2]
     g = S.golden(n)
     ng = S.NG
     vi = v[ng:-ng, ng:-ng, ng:-ng]
@@ -61,3 +61,21 @@ def test_sod_state_matches_reference_restart(sod_run, n):
         else:
             tol = 1e-6 if name == "rhoU" else 5e-7
             assert err <= tol * np.abs(ref).max(), (name, err / np.abs(ref).max())
+
+
+@pytest.mark.parametrize("n", [1, 3])
+def test_sod_temperature_and_pressure_match_reference_plots(sod_run, n):
+    """The temperature of the Newton solve, the pressure rho T W_i, the
+    density and the x velocity at statistics time n against the reference
+    post-processor's FP32 plot files (dimensional): within 3e-7 of each
+    field's largest magnitude (FP32 rounding plus the 5e-8 of the pin)."""
+    a, run = sod_run
+    _, _, v, T, W_i = run[n - 1]
+    ng = S.NG
+    sl = (slice(ng, -ng), slice(ng, -ng), ng)
+    ours = {"T": T[sl] * a["t_ref"], "P": (v[sl + (0,)] * T[sl] * W_i[sl]) * a["p_ref"],
+            "rho": v[sl + (0,)] * a["rho_ref"], "u": (v[sl + (1,)] / v[sl + (0,)]) * a["u_ref"]}
+    ref = S.golden_plot(n)
+    for k, x in ours.items():
+        err = np.abs(x - ref[k]).max() / np.abs(ref[k]).max()
+        assert err <= 3e-7, (k, err)
