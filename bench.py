@@ -35,7 +35,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 HBM_FALLBACK_GBS = 6800.0
-FP64_PEAK_GFLOPS = 1194.4   # measured FP64 FMA rate of this GB300 pool (profiles/fp64_peak_probe.md)
+FP64_PEAK_GFLOPS = 1194.4   # FP64 FMA rate measured on a GB300 by a dependent-FMA probe kernel
 
 
 def measured_peaks():
@@ -129,7 +129,7 @@ def chem_window(cfg):
 CHEM_BYTES_PER_REACTOR = 11 * 8 + 10 * 8
 # FP64 flops per BDF step of the persistent chemistry kernel (2 DFMA + DADD +
 # DMUL per thread, summed by ncu over one launch, / the BDF steps of that
-# launch): profiles/k_psr_field_mix64.md
+# launch, ncu capture of the 64x64x32 mixing-layer window)
 CHEM_FLOP_PER_BDF_STEP = 9793
 # DRAM bytes (read + write) per reactor of that launch, scaled by reactors to
 # other windows: the per-thread BDF state in local memory that the L2 does
@@ -137,39 +137,32 @@ CHEM_FLOP_PER_BDF_STEP = 9793
 CHEM_TRAFFIC_PER_REACTOR = 16115
 
 # FP64 flops per face of k_euler_face (2 DFMA + DADD + DMUL per thread, summed
-# by ncu over one launch, / faces): profiles/euler_face_mix128.md (9 species)
+# by ncu over one launch of the 9-species mixing layer, / faces)
 EULER_FLOP_PER_FACE = {9: 1869}
 
 
-class Stepper:
-    """One time step of the reference driver (izem.f90:252-283): timestep,
-    then with chemistry the Strang sequence chem(dt/2), rk3(dt), chem(dt/2)."""
+def make_stepper(g, chem, mode=0):
+    """The driver's step (phd_gb300.izem.TimeLoop) with per-half-step
+    chemistry statistics for the JSON line."""
+    from phd_gb300.izem import TimeLoop
 
-    def __init__(self, g, chem, mode=0):
-        self.g, self.chem, self.mode = g, chem, mode
-        self.dtmin, self.DTmax = 1.0, 0.0
-        self.log = []   # surrogate half steps: (dt, window cells, fallback cells, ms, network ms)
-        self.bdf_steps = []   # BDF steps summed over the window, per BDF half step
+    class Stepper(TimeLoop):
+        def __init__(self):
+            super().__init__(g, chem, chem_mode=mode)
+            self.g = g
+            self.log = []   # surrogate half steps: (dt, window cells, fallback cells, ms, network ms)
+            self.bdf_steps = []   # BDF steps summed over the window, per BDF half step
 
-    def _chem(self, dt):
-        d = self.g.reaction_selec(dt, mode=self.mode)
-        if self.mode == 0:
-            self.bdf_steps.append(self.g.chem_stats()["total_steps"])
-        else:
-            s = self.g.surrogate_stats()
-            self.log.append((dt, s["cells"], s["fallback"], s["ms"], s["ms_network"]))
-        return d
+        def chem(self, dt):
+            d = super().chem(dt)
+            if self.mode == 0:
+                self.bdf_steps.append(self.g.chem_stats()["total_steps"])
+            else:
+                s = self.g.surrogate_stats()
+                self.log.append((dt, s["cells"], s["fallback"], s["ms"], s["ms_network"]))
+            return d
 
-    def step(self):
-        g = self.g
-        _, dt = g.timestep(DTmax=self.DTmax, dtmin=self.dtmin)
-        if self.chem:
-            self._chem(0.5 * dt)
-        g.rk3(dt)
-        if self.chem:
-            self.DTmax = self._chem(0.5 * dt)
-        self.dtmin = dt
-        return dt
+    return Stepper()
 
 
 def run_gpu(args, rank, world):
@@ -205,7 +198,7 @@ def run_gpu(args, rank, world):
         options["dvodesimp"] = "chemistry skipped in the pure streams and where rates are negligible"
     if args.vis_dt:
         options["vis_dt"] = "Fourier time-step criteria"
-    stp = Stepper(g, chem)
+    stp = make_stepper(g, chem)
     ncell = cfg.nx * cfg.ny * cfg.nz
     # warm-up, then the thread blocks of the dominant kernels chosen by timing
     # them on this state (the CUDA graph of RK3 is captured afterwards)
@@ -215,6 +208,7 @@ def run_gpu(args, rank, world):
     tuning = g.autotune(chem_dt=0.5 * dt_tune if chem else 0.0)
     stp.step()
     g.synchronize()
+    g.newton_stats(reset=True)
     barrier(world)
     # timed steps without per-kernel events: `value`
     with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
@@ -233,6 +227,7 @@ def run_gpu(args, rank, world):
         stp.step()
     ms_instr = g.timer_stop()
     timed_bdf = list(stp.bdf_steps)
+    newton_it, newton_unconv = g.newton_stats()
     kt = g.kernel_times()
     g.set_kernel_timing(False)
     ms = max_over_ranks(ms, world)
@@ -311,6 +306,9 @@ def run_gpu(args, rank, world):
         "roofline_euler_face": rl if rl_chem else None,
         "dominant_kernel": {"name": dom_name, "launches": dom_n, "ms": dom_ms},
         "instrumented_ms_per_step": ms_instr / args.steps,
+        "newton": {"max_iterations": newton_it, "unconverged_solves": newton_unconv, "itmax": 200,
+                   "note": "prim_inv_var solves of the timed steps; each iterates until the reference's "
+                           "stopping test holds or itmax"},
         "kernel_ms": {k: round(v[1], 3) for k, v in sorted(kt.items(), key=lambda kv: -kv[1][1])},
         "gpu_launches": launches,
         "clocks": clk.summary(),
@@ -356,7 +354,7 @@ def run_mlp_chem(args, g, stp, ncell, world):
     g.upload(**st0)
     err = np.abs(dgot - dref)
     scale = float(np.abs(dref).max())
-    mstp = Stepper(g, True, mode=1)
+    mstp = make_stepper(g, True, mode=1)
     mstp.dtmin, mstp.DTmax = stp.dtmin, stp.DTmax
     mstp.step()
     g.synchronize()
@@ -562,7 +560,8 @@ def pin(a):
 
 def cpu_baseline(args, steps=2):
     """The oracle (C++ restatement of the reference, OpenMP) on a 64x64x32
-    sub-block of the same workload, all host threads."""
+    block of the same workload (the full layer's grid spacing), all host
+    threads, stepped as the reference driver steps (TimeLoop's sequence)."""
     import oracle
     from phd_gb300 import ics
     nx, ny, nz = 64, 64, 32
@@ -570,9 +569,10 @@ def cpu_baseline(args, steps=2):
         cfg, thd, adi, dxi, st, info = ics.tgv(48, lib_dscalar=oracle.metrics_dscalar)
         nx = ny = nz = 48
     else:
-        cfg, thd, adi, dxi, st, info = ics.mixing_layer(nx, ny, nz, Lx=nx * 47e-6, Ly=ny * 47e-6, Lz=nz * 47e-6,
-                                                        lib_dscalar=oracle.metrics_dscalar)
+        cfg, thd, adi, dxi, st, info = ics.mixing_layer_block(nx, ny, nz, lib_dscalar=oracle.metrics_dscalar)
     eg = args.workload == "mix" and args.transport == "eglib"
+    chem = args.workload == "mix" and not args.no_chem
+    cfg.reaction = 1 if chem else 0
     if eg:
         from phd_gb300.thd import eglib_link, load_species
         cfg.eglib = 1
@@ -580,19 +580,21 @@ def cpu_baseline(args, steps=2):
     if eg:
         orc.set_eglib(eglib_link(load_species("h2air9")))
     orc.finalize_ic(st)
-    chem = args.workload == "mix" and not args.no_chem
     mech = None
     if chem:
         from phd_gb300.mech import h2_mechanism
         mech = h2_mechanism()
 
+    loop = {"dtmin": 1.0, "DTmax": 0.0}
+
     def step():
-        _, dt = orc.timestep(st)
+        _, dt = orc.timestep(st, DTmax=loop["DTmax"], dtmin=loop["dtmin"])
         if chem:
             orc.chem_step(st, mech, 0.5 * dt)
         orc.rk3(st, dt)
         if chem:
-            orc.chem_step(st, mech, 0.5 * dt)
+            loop["DTmax"] = orc.chem_step(st, mech, 0.5 * dt)
+        loop["dtmin"] = dt
 
     step()   # warm
     t0 = time.perf_counter()

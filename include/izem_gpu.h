@@ -156,6 +156,15 @@ int  izem_gpu_init(const izem_cfg* cfg, const izem_thd* thd, const izem_adi* adi
 void izem_gpu_destroy(izem_ctx* ctx);
 int  izem_gpu_last_error(izem_ctx* ctx, char* buf, int n);
 
+/* Newton temperature solves (prim_inv_var, module_thermodynamics.f90:79-186):
+ * the most iterations any sub-domain needed, and the number of solves that
+ * reached itmax without meeting the stopping test (the reference's
+ * "WARNING: failure in temperatures convergence", :161), counted since the
+ * context was created or since the last call with reset != 0.  Every solve
+ * iterates until the reference's test holds or itmax (200; 100 for the
+ * initial-condition closure) iterations have run. */
+int  izem_gpu_newton_stats(izem_ctx* ctx, int* max_iters, int* unconverged, int reset);
+
 /* Inverted metrics dx_i(sx-ng:ex+ng) etc. (module_tools.f90:223-452, already
  * multiplied by L_ref as in adimensionalize, module_tools.f90:185-187). */
 int  izem_gpu_set_grid(izem_ctx* ctx, const double* dx_i, const double* dy_i,
@@ -316,10 +325,15 @@ int  izem_mlp_fallback_cells(izem_mlp* m, int* out, int cap, int* count);
  * allocate device memory while they run -- a solver whose own arena (or a
  * framework's caching allocator) already holds the GPU's memory, or one that
  * calls the surrogate inside its time-step loop, where cudaMalloc/cudaFree
- * would synchronise the whole device.  Same result as izem_mlp_forward, but
+ * would synchronise the whole device.  It evaluates the same network as
+ * izem_mlp_forward, with the warp-level BF16 GEMM kernels that training
+ * uses instead of the tensor-core inference kernel, so the two agree to
+ * BF16 rounding (within 1e-2 of the largest output), not bit for bit.
  * d_x (M x 12) and d_y (M x 10) are FP32 device arrays, the work is queued
  * on `stream` (a cudaStream_t; NULL is the default stream) and the call
- * returns without waiting.  No memory is allocated or freed: the
+ * returns without waiting.  The device that was current when the handle
+ * was created must be current for the call (its weights live there);
+ * otherwise the call returns IZEM_ERR_ARG.  No memory is allocated or freed: the
  * activations use one fixed device array of about 4.3 MiB per GPU, which
  * every GPU that loads the library holds until the process exits, so M is
  * at most IZEM_MLP_NOALLOC_MAX_ROWS (larger M returns IZEM_ERR_TOO_LARGE;

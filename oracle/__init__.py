@@ -35,6 +35,7 @@ def load():
         "or_set_chem_skip": (C.c_int, [P, C.c_int, _dp, _dp, C.c_int, C.c_int]),
         "or_set_les": (C.c_int, [P, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double]),
         "or_last_error": (C.c_int, [P, C.c_char_p, C.c_int]),
+        "or_newton_it_max": (C.c_int, [P]),
         "or_cp_scalar": (None, [P, C.c_double, _dp, _dp]),
         "or_ha_scalar": (None, [P, C.c_double, _dp]),
         "or_shock_sensor": (C.c_int, [P, _dp, _dp, _dp, _u8p]),
@@ -182,6 +183,10 @@ class Oracle:
 
     def newton_warnings(self):
         return self.lib.or_last_error(self.h, None, 0)
+
+    def newton_it_max(self):
+        """Most Newton iterations any prim_inv_var call of this context ran."""
+        return self.lib.or_newton_it_max(self.h)
 
     def cp_scalar(self, T, Y):
         Y = np.ascontiguousarray(Y, dtype=np.float64)

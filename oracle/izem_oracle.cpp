@@ -63,6 +63,7 @@ struct Ctx {
   Block b;
   std::vector<double> dxi[3];   // indexed (i-1+ng), length n+2ng
   int newton_warn = 0;
+  int newton_it_max = 0;   // most iterations of any prim_inv_var call (test readout)
   int sensor_xblocks = 1;   // x-blocks of the reference's MPI run whose edges the sensor does not cross
   // dvodesimp (module_reaction.f90:173-251): pure fuel Y1f and oxidiser Y0o,
   // H2 and N2 species indices (0-based)
@@ -275,6 +276,7 @@ int prim_inv_var(Ctx& c, int dom, bool err_mach, double* v, double* W_i, double*
     if (error < eps) break;
   }
   if (it > itmax) c.newton_warn++;
+  c.newton_it_max = std::max(c.newton_it_max, std::min(it, itmax));
   if (!err_mach && error != error) {
     c.err = "Newton error is a NaN";
     return IZEM_ERR_NAN;
@@ -1499,6 +1501,8 @@ int or_last_error(void* h, char* buf, int n) {
   if (buf && n > 0) { std::snprintf(buf, n, "%s", c->err.c_str()); }
   return c->newton_warn;
 }
+
+int or_newton_it_max(void* h) { return static_cast<Ctx*>(h)->newton_it_max; }
 
 void or_cp_scalar(void* h, double T, const double* Y, double* cp) { *cp = cp_scalar(static_cast<Ctx*>(h)->thd, T, Y); }
 void or_ha_scalar(void* h, double T, double* ha) { ha_scalar(static_cast<Ctx*>(h)->thd, T, ha); }

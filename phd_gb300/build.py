@@ -65,7 +65,8 @@ def build_gpu(force=False, verbose=False):
 
 
 def build_oracle(force=False):
-    srcs = sorted(glob.glob(os.path.join(ORACLE_DIR, "*.cpp")) + [os.path.join(ROOT, "include", "izem_gpu.h")])
+    srcs = sorted(glob.glob(os.path.join(ORACLE_DIR, "*.cpp")) + glob.glob(os.path.join(ORACLE_DIR, "*.inc")) +
+                  [os.path.join(ROOT, "include", "izem_gpu.h")])
     if not force and not _stale(ORACLE_LIB, srcs):
         return ORACLE_LIB
     os.makedirs(os.path.dirname(ORACLE_LIB), exist_ok=True)

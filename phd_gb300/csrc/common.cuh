@@ -62,6 +62,7 @@ struct DevStatus {
   int neg_temperature;
   int newton_nan;
   int newton_unconverged;
+  int newton_it_max;                 // most iterations any sub-domain used since the host last read it
   unsigned long long dtc_bits;       // timestep: max (|u|+c)/dx (bit pattern)
   // timestep, Fourier criteria (bit patterns of positive doubles): per
   // species max of D_k and min of delta^2 / D_k, and min of delta^2 rho cp / lambda

@@ -25,10 +25,16 @@ struct izem_ctx {
   double* h_dt = nullptr;
   std::vector<double*> allocs;
   bool grid_set = false;
-  // CUDA graph of one RK3 step
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t graph_exec = nullptr;
+  // CUDA graphs captured once and replayed: one RK3 step, the primitives
+  // update, the initial-condition closure and the tail of a chemistry half
+  // step.  Their Newton solves are conditional WHILE nodes.
+  enum { GR_RK3, GR_PRIM, GR_IC, GR_CHEM_AFTER, GR_N };
+  cudaGraph_t graph[GR_N] = {};
+  cudaGraphExec_t graph_exec[GR_N] = {};
   bool capturing = false;
+  cudaStream_t side = nullptr;            // captures the bodies of conditional nodes
+  int* h_done = nullptr;                  // pinned: stop flags read by direct-launch Newton loops
+  int newton_it_max = 0;                  // most Newton iterations of any sub-domain since the last izem_gpu_newton_stats reset
   // timing
   cudaEvent_t t0 = nullptr, t1 = nullptr;
   bool kt_enabled = false;

@@ -26,7 +26,7 @@
 namespace {
 
 constexpr int kThreads = 128;
-constexpr int kNewtonIters = 12;   // Newton iterations captured per sub-domain and stage
+constexpr int kNewtonChunk = 4;    // direct-launch Newton: iterations between two host reads of the stop flags
 
 unsigned grid_for(long long n, int threads = kThreads) { return (unsigned)((n + threads - 1) / threads); }
 
@@ -105,6 +105,8 @@ int read_status(izem_ctx* c) {
   else if (s.timeout) rc = ctx_fail(c, IZEM_ERR_TIMEOUT, "bounded device wait gave up", cudaSuccess);
   else if (s.chem_fail) rc = ctx_fail(c, IZEM_ERR_CHEM, "stiff chemistry integration failed on some cells", cudaSuccess);
   c->newton_warn += s.newton_unconverged;
+  c->newton_it_max = std::max(c->newton_it_max, s.newton_it_max);
+  if (s.newton_it_max) CK(cudaMemsetAsync(&c->d_status->newton_it_max, 0, sizeof(int), c->stream));
   if (rc != IZEM_OK || s.newton_unconverged) {
     // clear sticky flags so that the context stays usable
     CK(cudaMemsetAsync(c->d_status, 0, sizeof(DevStatus), c->stream));
@@ -113,25 +115,117 @@ int read_status(izem_ctx* c) {
   return rc;
 }
 
+// Runs the work that `enqueue` launches.  With kernel timing off it is
+// captured once into graph slot `slot` and the graph is replayed on later
+// calls; with kernel timing on the launches go out directly, each bracketed
+// by events.  Both forms launch the same kernels with the same arguments.
+template <class F>
+int run_graph(izem_ctx* c, int slot, F enqueue) {
+  if (c->kt_enabled) return enqueue();
+  if (!c->graph_exec[slot]) {
+    c->capturing = true;
+    CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = enqueue();
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
+    c->capturing = false;
+    if (rc) { if (graph) cudaGraphDestroy(graph); return rc; }
+    if (e != cudaSuccess) return ctx_fail(c, IZEM_ERR_CUDA, "cudaStreamEndCapture", e);
+    c->graph[slot] = graph;
+    e = cudaGraphInstantiate(&c->graph_exec[slot], graph, 0);
+    if (e != cudaSuccess) {
+      c->graph_exec[slot] = nullptr;
+      cudaGraphDestroy(graph);
+      c->graph[slot] = nullptr;
+      return ctx_fail(c, IZEM_ERR_CUDA, "cudaGraphInstantiate", e);
+    }
+  }
+  CK(cudaGraphLaunch(c->graph_exec[slot], c->stream));
+  return IZEM_OK;
+}
+
+// Drops every captured graph; the next call of each entry point captures
+// again (after a change of launch shapes, kernel variants or options).
+void drop_graphs(izem_ctx* c) {
+  for (int q = 0; q < izem_ctx::GR_N; ++q) {
+    if (c->graph_exec[q]) cudaGraphExecDestroy(c->graph_exec[q]);
+    if (c->graph[q]) cudaGraphDestroy(c->graph[q]);
+    c->graph_exec[q] = nullptr;
+    c->graph[q] = nullptr;
+  }
+}
+
 // ------------------------------------------------------- stage building -----
-// ghost: 0 the interior (sub-domain 0), 1 the ghost slabs (1-6), 2 the
-// Dirichlet planes of jet faces (7-8)
+// prim_inv_var's Newton loop (module_thermodynamics.f90:79-186) on one kind
+// of sub-domain; every sub-domain stops on its own test, after at most itmax
+// iterations.  ghost: 0 the interior (sub-domain 0), 1 the ghost slabs (1-6),
+// 2 the Dirichlet planes of jet faces (7-8).
+//
+// Captured into a graph, the loop is a conditional WHILE node whose body is
+// one iteration and the stopping test; the test launch clears the condition
+// when every sub-domain has stopped, so the graph runs exactly the
+// iterations the reference runs.  Launched directly (kernel timing), the
+// host runs the iterations in chunks and reads the stop flags between them;
+// iterations after a sub-domain has stopped leave it untouched, so both
+// forms give the same bits.
 template <int NRV>
-int enq_newton(izem_ctx* c, int ghost, double eps, int itmax, int niter, int check_negT) {
+int enq_newton(izem_ctx* c, int ghost, double eps, int itmax, int check_negT) {
   const Geo& g = c->g;
-  int d0 = ghost == 2 ? 7 : (ghost ? 1 : 0), d1 = ghost == 2 ? 8 : (ghost ? 6 : 0);
-  long long n = ghost == 2 ? 2LL * g.n[1] * g.n[2] : (ghost ? slab_count(g) - g.nint : g.nint);
+  const int d0 = ghost == 2 ? 7 : (ghost ? 1 : 0), d1 = ghost == 2 ? 8 : (ghost ? 6 : 0);
+  const long long n = ghost == 2 ? 2LL * g.n[1] * g.n[2] : (ghost ? slab_count(g) - g.nint : g.nint);
+  const char* iname = ghost == 2 ? "newton_iter_plane" : (ghost ? "newton_iter_ghost" : "newton_iter");
   int rc;
   if ((rc = launch(c, "newton_reset", [&] { k_newton_reset<<<1, 8, 0, c->stream>>>(c->d_status, d0, d1); }))) return rc;
-  for (int it = 0; it < niter; ++it) {
-    if ((rc = launch(c, ghost == 2 ? "newton_iter_plane" : (ghost ? "newton_iter_ghost" : "newton_iter"), [&] {
-           k_newton_iter<NRV><<<grid_for(n), kThreads, 0, c->stream>>>(g, ghost, c->v, c->T, c->cp, c->ha, c->d_status, check_negT);
-         })))
-      return rc;
-    if ((rc = launch(c, "newton_check", [&] { k_newton_check<<<1, 1, 0, c->stream>>>(c->d_status, d0, d1, eps, itmax); })))
-      return rc;
+  auto iterate = [&](cudaGraphConditionalHandle cond, int use_cond) -> int {
+    int r = launch(c, iname, [&] {
+      k_newton_iter<NRV><<<grid_for(n), kThreads, 0, c->stream>>>(g, ghost, c->v, c->T, c->cp, c->ha, c->d_status, check_negT);
+    });
+    if (r) return r;
+    return launch(c, "newton_check", [&] {
+      k_newton_check<<<1, 32, 0, c->stream>>>(c->d_status, d0, d1, eps, itmax, cond, use_cond);
+    });
+  };
+  if (c->capturing) {
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t graph = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t ndeps = 0;
+    CK(cudaStreamGetCaptureInfo(c->stream, &cs, nullptr, &graph, &deps, nullptr, &ndeps));
+    cudaGraphConditionalHandle cond;
+    // the condition is 1 at every launch of the graph: the loop body runs at
+    // least once, as the reference's first iteration always does
+    CK(cudaGraphConditionalHandleCreate(&cond, graph, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams np{};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = cond;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t node;
+    CK(cudaGraphAddNode(&node, graph, deps, nullptr, ndeps, &np));
+    CK(cudaStreamUpdateCaptureDependencies(c->stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+    cudaStream_t main = c->stream;
+    cudaError_t e = cudaStreamBeginCaptureToGraph(c->side, np.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                                  cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return ctx_fail(c, IZEM_ERR_CUDA, "cudaStreamBeginCaptureToGraph", e);
+    c->stream = c->side;   // the body's launches go to the side stream
+    rc = iterate(cond, 1);
+    c->stream = main;
+    cudaGraph_t body = nullptr;
+    e = cudaStreamEndCapture(c->side, &body);
+    if (rc) return rc;
+    if (e != cudaSuccess) return ctx_fail(c, IZEM_ERR_CUDA, "cudaStreamEndCapture (Newton loop body)", e);
+    return IZEM_OK;
   }
-  return launch(c, "newton_final", [&] { k_newton_final<<<1, 1, 0, c->stream>>>(c->d_status, d0, d1); });
+  for (int it = 0; it < itmax; it += kNewtonChunk) {
+    for (int q = 0; q < kNewtonChunk && it + q < itmax; ++q)
+      if ((rc = iterate(0, 0))) return rc;
+    CK(cudaMemcpyAsync(c->h_done, c->d_status->done + d0, (d1 - d0 + 1) * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    bool all = true;
+    for (int d = 0; d <= d1 - d0; ++d) all = all && c->h_done[d] != 0;
+    if (all) break;
+  }
+  return IZEM_OK;
 }
 
 template <int NRV>
@@ -251,13 +345,13 @@ template <int NRV>
 int enq_update_primitives_after(izem_ctx* c, int stage = -1) {
   const Geo& g = c->g;
   int rc;
-  if ((rc = enq_newton<NRV>(c, 0, 1.0e-5, 200, kNewtonIters, 1))) return rc;
+  if ((rc = enq_newton<NRV>(c, 0, 1.0e-5, 200, 1))) return rc;
   long long ns = slab_count(g) - g.nint;
   const bool jet = jet_face(g.bc[0]) || jet_face(g.bc[1]);
   if (!jet) {
     if ((rc = launch(c, "halo", [&] { k_halo<NRV><<<grid_for(ns), kThreads, 0, c->stream>>>(g, 0, c->cfg.forcesum, c->v, c->W_i); })))
       return rc;
-    return enq_newton<NRV>(c, 1, 1.0e-5, 200, kNewtonIters, 1);
+    return enq_newton<NRV>(c, 1, 1.0e-5, 200, 1);
   }
   // faces in the reference's order: periodic copies first (comm_cons), then
   // W and E (the jet faces, closed on their boundary planes), then the
@@ -286,12 +380,12 @@ int enq_update_primitives_after(izem_ctx* c, int stage = -1) {
          k_dirichlet_prep<NRV><<<grid_for(2 * np), kThreads, 0, c->stream>>>(g, c->cfg.forcesum, c->v, c->W_i);
        })))
     return rc;
-  if ((rc = enq_newton<NRV>(c, 2, 1.0e-5, 200, kNewtonIters, 1))) return rc;
+  if ((rc = enq_newton<NRV>(c, 2, 1.0e-5, 200, 1))) return rc;
   if (ext && (rc = launch(c, "halo", [&] { k_halo<NRV><<<grid_for(ns), kThreads, 0, c->stream>>>(g, 0, c->cfg.forcesum, c->v, c->W_i, ext); })))
     return rc;
   if ((rc = launch(c, "halo", [&] { k_halo<NRV><<<grid_for(ns), kThreads, 0, c->stream>>>(g, 2, c->cfg.forcesum, c->v, c->W_i, dir); })))
     return rc;
-  return enq_newton<NRV>(c, 1, 1.0e-5, 200, kNewtonIters, 1);
+  return enq_newton<NRV>(c, 1, 1.0e-5, 200, 1);
 }
 
 template <int NRV>
@@ -333,10 +427,10 @@ int do_finalize_ic(izem_ctx* c) {
   int rc;
   if ((rc = launch(c, "wmix", [&] { k_wmix_interior<NRV><<<grid_for(g.nint), kThreads, 0, c->stream>>>(g, c->v, c->W_i); })))
     return rc;
-  if ((rc = enq_newton<NRV>(c, 0, 1.0e-10, 100, 100, 0))) return rc;
+  if ((rc = enq_newton<NRV>(c, 0, 1.0e-10, 100, 0))) return rc;
   long long ns = slab_count(g) - g.nint;
   if ((rc = launch(c, "halo", [&] { k_halo<NRV><<<grid_for(ns), kThreads, 0, c->stream>>>(g, 1, 0, c->v, c->W_i); }))) return rc;
-  return enq_newton<NRV>(c, 1, 1.0e-10, 100, 100, 0);
+  return enq_newton<NRV>(c, 1, 1.0e-10, 100, 0);
 }
 
 template <int NRV>
@@ -363,7 +457,7 @@ int do_chem_after(izem_ctx* c) {
   long long ns = slab_count(g) - g.nint;
   if ((rc = launch(c, "halo", [&] { k_halo<NRV><<<grid_for(ns), kThreads, 0, c->stream>>>(g, 0, c->cfg.forcesum, c->v, c->W_i); })))
     return rc;
-  return enq_newton<NRV>(c, 1, 1.0e-5, 200, kNewtonIters, 1);
+  return enq_newton<NRV>(c, 1, 1.0e-5, 200, 1);
 }
 
 template <int NRV>
@@ -542,6 +636,8 @@ int ctx_alloc(izem_ctx* c) {
   const Geo& g = c->g;
   const int nv = c->nv, nrv = c->cfg.nrv;
   CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  CK(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
+  CK(cudaMallocHost(&c->h_done, 16 * sizeof(int)));
   CK(cudaMemcpyToSymbol(c_thd, &c->devthd, sizeof(DevThd)));
   auto alloc = [&](double** p, size_t n) -> cudaError_t {
     cudaError_t e = cudaMalloc(p, n * sizeof(double));
@@ -586,8 +682,7 @@ extern "C" {
 void izem_gpu_destroy(izem_ctx* c) {
   if (!c) return;
   if (c->stream) cudaStreamSynchronize(c->stream);
-  if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
-  if (c->graph) cudaGraphDestroy(c->graph);
+  drop_graphs(c);
   for (double* p : c->allocs) cudaFree(p);
   if (c->sensor) cudaFree(c->sensor);
   if (c->fhat_edge) cudaFree(c->fhat_edge);
@@ -603,8 +698,21 @@ void izem_gpu_destroy(izem_ctx* c) {
     for (auto& pr : v) { cudaEventDestroy(pr.first); cudaEventDestroy(pr.second); }
   if (c->t0) cudaEventDestroy(c->t0);
   if (c->t1) cudaEventDestroy(c->t1);
+  if (c->h_done) cudaFreeHost(c->h_done);
+  if (c->side) cudaStreamDestroy(c->side);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
+}
+
+int izem_gpu_newton_stats(izem_ctx* c, int* max_iters, int* unconverged, int reset) {
+  if (!c) return IZEM_ERR_ARG;
+  if (max_iters) *max_iters = c->newton_it_max;
+  if (unconverged) *unconverged = c->newton_warn;
+  if (reset) {
+    c->newton_it_max = 0;
+    c->newton_warn = 0;
+  }
+  return IZEM_OK;
 }
 
 int izem_gpu_last_error(izem_ctx* c, char* buf, int n) {
@@ -690,14 +798,14 @@ int izem_gpu_update_primitives(izem_ctx* c) {
   if (!c) return IZEM_ERR_ARG;
   if ((jet_face(c->cfg.bc[0]) || jet_face(c->cfg.bc[1])) && !c->have_coords)
     return ctx_fail(c, IZEM_ERR_STATE, "jet faces need izem_gpu_set_coords", cudaSuccess);
-  int rc = IZEM_DISPATCH(c, do_update_primitives, c);
+  int rc = run_graph(c, izem_ctx::GR_PRIM, [&] { return IZEM_DISPATCH(c, do_update_primitives, c); });
   if (rc) return rc;
   return read_status(c);
 }
 
 int izem_gpu_finalize_ic(izem_ctx* c) {
   if (!c) return IZEM_ERR_ARG;
-  int rc = IZEM_DISPATCH(c, do_finalize_ic, c);
+  int rc = run_graph(c, izem_ctx::GR_IC, [&] { return IZEM_DISPATCH(c, do_finalize_ic, c); });
   if (rc) return rc;
   return read_status(c);
 }
@@ -712,26 +820,8 @@ int izem_gpu_rk3(izem_ctx* c, double dt, double time0) {
   c->h_dt[0] = dt;
   c->h_dt[1] = time0;
   CK(cudaMemcpyAsync(c->d_dt, c->h_dt, 2 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-  int rc;
-  if (c->kt_enabled) {
-    // timed mode: direct launches, each bracketed by events
-    rc = IZEM_DISPATCH(c, do_rk3_enqueue, c);
-    if (rc) return rc;
-  } else {
-    if (!c->graph_exec) {
-      c->capturing = true;
-      CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-      rc = IZEM_DISPATCH(c, do_rk3_enqueue, c);
-      cudaGraph_t graph = nullptr;
-      cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
-      c->capturing = false;
-      if (rc) { if (graph) cudaGraphDestroy(graph); return rc; }
-      if (e != cudaSuccess) return ctx_fail(c, IZEM_ERR_CUDA, "cudaStreamEndCapture", e);
-      c->graph = graph;
-      CK(cudaGraphInstantiate(&c->graph_exec, c->graph, 0));
-    }
-    CK(cudaGraphLaunch(c->graph_exec, c->stream));
-  }
+  int rc = run_graph(c, izem_ctx::GR_RK3, [&] { return IZEM_DISPATCH(c, do_rk3_enqueue, c); });
+  if (rc) return rc;
   return read_status(c);
 }
 
@@ -824,7 +914,7 @@ int izem_gpu_chem_surrogate_stats(izem_ctx* c, long long* cells, int* fallback, 
 // The rest of reaction_selec after the reactors (module_reaction.f90:83-86):
 // upd_prim_var_woT, halo, boundaries, ghost primitives; then the statistics.
 static int chem_finish(izem_ctx* c, int mode, int sur_rc, double* DTmax) {
-  int rc = IZEM_DISPATCH(c, do_chem_after, c);
+  int rc = run_graph(c, izem_ctx::GR_CHEM_AFTER, [&] { return IZEM_DISPATCH(c, do_chem_after, c); });
   if (rc) return rc;
   CK(cudaMemcpyAsync(c->h_chem_stats, c->d_chem_stats, sizeof(ChemStats), cudaMemcpyDeviceToHost, c->stream));
   rc = read_status(c);
@@ -1013,8 +1103,7 @@ int izem_gpu_autotune(izem_ctx* c, double chem_dt, char* report, int report_len)
   if (c->cfg.vis && c->cfg.eglib && !c->have_eg)
     return ctx_fail(c, IZEM_ERR_STATE, "EGLIB transport requested (cfg.eglib) but izem_gpu_set_eglib not called", cudaSuccess);
   // the captured RK3 graph holds the old launch configurations
-  if (c->graph_exec) { cudaGraphExecDestroy(c->graph_exec); c->graph_exec = nullptr; }
-  if (c->graph) { cudaGraphDestroy(c->graph); c->graph = nullptr; }
+  drop_graphs(c);
   const bool kt = c->kt_enabled;
   c->kt_enabled = false;
   std::string rep = "{";
@@ -1081,8 +1170,7 @@ int izem_gpu_autotune(izem_ctx* c, double chem_dt, char* report, int report_len)
 
 int izem_gpu_set_sensor_xblocks(izem_ctx* c, int nblk) {
   if (!c || nblk < 1 || c->cfg.nx % nblk != 0 || c->cfg.nx / nblk < c->cfg.ng) return IZEM_ERR_ARG;
-  if (c->graph_exec) { cudaGraphExecDestroy(c->graph_exec); c->graph_exec = nullptr; }
-  if (c->graph) { cudaGraphDestroy(c->graph); c->graph = nullptr; }
+  drop_graphs(c);
   if (c->fhat_edge) { CK(cudaFree(c->fhat_edge)); c->fhat_edge = nullptr; }
   c->sensor_bx = c->cfg.nx / nblk;
   c->nedge = (long long)(nblk - 1) * c->cfg.ny * c->cfg.nz;
@@ -1093,6 +1181,7 @@ int izem_gpu_set_sensor_xblocks(izem_ctx* c, int nblk) {
 int izem_gpu_set_coords(izem_ctx* c, const double* x, const double* y, const double* z, double lx) {
   if (!c || !x || !y || !z) return IZEM_ERR_ARG;
   (void)x;
+  drop_graphs(c);   // captured graphs hold the jet constants by value
   if (!c->d_y) {
     CK(cudaMalloc(&c->d_y, c->g.n[1] * sizeof(double)));
     CK(cudaMalloc(&c->d_z, c->g.n[2] * sizeof(double)));
@@ -1123,8 +1212,7 @@ int izem_gpu_set_les(izem_ctx* c, int enable, double mu_sgs_factor, double sc_sg
                      double percent_weight_sgs) {
   if (!c) return IZEM_ERR_ARG;
   // the captured RK3 graph holds the other viscous kernel
-  if (c->graph_exec) { cudaGraphExecDestroy(c->graph_exec); c->graph_exec = nullptr; }
-  if (c->graph) { cudaGraphDestroy(c->graph); c->graph = nullptr; }
+  drop_graphs(c);
   if (!enable) {
     c->les_on = false;
     return IZEM_OK;

@@ -214,9 +214,18 @@ __global__ void k_newton_iter(Geo g, int ghost, const double* __restrict__ v, do
   else atomic_max_nonneg(&st->maxdf_bits[dom], df2);
 }
 
-// Stopping test of prim_inv_var for sub-domains [d0, d1].
-__global__ void k_newton_check(DevStatus* st, int d0, int d1, double eps, int itmax) {
+// Stopping test of prim_inv_var (module_thermodynamics.f90:110-115,161-162)
+// for sub-domains [d0, d1]: a sub-domain stops when its largest correction
+// is below eps, or after itmax iterations with a convergence warning, as the
+// reference's `it > itmax` exit.  Inside a captured graph (use_cond) the
+// launch also sets the condition of the enclosing WHILE node: the loop runs
+// while any sub-domain is still iterating.  Every iteration moves each live
+// sub-domain one step closer to itmax, so the loop ends after at most itmax
+// passes.
+__global__ void k_newton_check(DevStatus* st, int d0, int d1, double eps, int itmax,
+                               cudaGraphConditionalHandle cond, int use_cond) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  unsigned live = 0;
   for (int d = d0; d <= d1; ++d) {
     if (st->done[d]) continue;
     st->it[d] += 1;
@@ -224,19 +233,15 @@ __global__ void k_newton_check(DevStatus* st, int d0, int d1, double eps, int it
     st->maxdf_bits[d] = 0ULL;
     if (err < eps) st->done[d] = 1;
     else if (st->it[d] >= itmax) { st->done[d] = 1; st->newton_unconverged += 1; }
+    if (st->done[d]) st->newton_it_max = max(st->newton_it_max, st->it[d]);
+    else live = 1;
   }
+  if (use_cond) cudaGraphSetConditional(cond, live);
 }
 
 __global__ void k_newton_reset(DevStatus* st, int d0, int d1) {
   int d = d0 + threadIdx.x;
   if (d <= d1) { st->done[d] = 0; st->it[d] = 0; st->maxdf_bits[d] = 0ULL; }
-}
-
-// After the captured iterations: any sub-domain still running is reported.
-__global__ void k_newton_final(DevStatus* st, int d0, int d1) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  for (int d = d0; d <= d1; ++d)
-    if (!st->done[d]) st->newton_unconverged += 1;
 }
 
 // Convective time-step criterion: max over the interior of (|u_d|+c) dx_i.

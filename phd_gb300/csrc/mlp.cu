@@ -244,6 +244,7 @@ struct izem_mlp {
   float* out = nullptr;              // network output FP32 (M x OUTP)
   double* d_loss = nullptr;
   int step = 0;
+  int device = 0;                    // device current at izem_mlp_create; holds every buffer
   cudaStream_t s = nullptr;
   // inference buffers: BF16 features (rows x 16) and FP32 output (rows x 16)
   long long icap = 0;
@@ -399,22 +400,29 @@ extern "C" {
 int izem_mlp_create(izem_mlp** out) {
   if (!out) return IZEM_ERR_ARG;
   izem_mlp* m = new izem_mlp();
-  if (cudaStreamCreateWithFlags(&m->s, cudaStreamNonBlocking) != cudaSuccess) { delete m; return IZEM_ERR_CUDA; }
-  for (int l = 0; l < NL; ++l) {
-    const size_t nw = (size_t)LIN[l] * LOUT[l], nb = LOUT[l];
-    if (cudaMalloc(&m->W[l], nw * 4) || cudaMalloc(&m->b[l], nb * 4) || cudaMalloc(&m->Wb[l], nw * 2) ||
-        cudaMalloc(&m->mW[l], nw * 4) || cudaMalloc(&m->vW[l], nw * 4) || cudaMalloc(&m->mb[l], nb * 4) ||
-        cudaMalloc(&m->vb[l], nb * 4) || cudaMalloc(&m->gW[l], nw * 4) || cudaMalloc(&m->gb[l], nb * 4)) {
-      return IZEM_ERR_NOMEM;
-    }
-    cudaMemset(m->mW[l], 0, nw * 4); cudaMemset(m->vW[l], 0, nw * 4);
-    cudaMemset(m->mb[l], 0, nb * 4); cudaMemset(m->vb[l], 0, nb * 4);
+  if (cudaGetDevice(&m->device) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&m->s, cudaStreamNonBlocking) != cudaSuccess) {
+    delete m;
+    return IZEM_ERR_CUDA;
   }
-  if (cudaMalloc(&m->d_loss, sizeof(double)) != cudaSuccess) return IZEM_ERR_NOMEM;
-  for (int l = 0; l < NL; ++l)
-    if (cudaMalloc(&m->blob[l], (size_t)LIN[l] * LOUT[l] * 2) != cudaSuccess) return IZEM_ERR_NOMEM;
-  if (cudaMalloc(&m->d_err, sizeof(int)) != cudaSuccess || cudaMemset(m->d_err, 0, sizeof(int)) != cudaSuccess)
+  bool ok = true;
+  for (int l = 0; l < NL && ok; ++l) {
+    const size_t nw = (size_t)LIN[l] * LOUT[l], nb = LOUT[l];
+    ok = !(cudaMalloc(&m->W[l], nw * 4) || cudaMalloc(&m->b[l], nb * 4) || cudaMalloc(&m->Wb[l], nw * 2) ||
+           cudaMalloc(&m->mW[l], nw * 4) || cudaMalloc(&m->vW[l], nw * 4) || cudaMalloc(&m->mb[l], nb * 4) ||
+           cudaMalloc(&m->vb[l], nb * 4) || cudaMalloc(&m->gW[l], nw * 4) || cudaMalloc(&m->gb[l], nb * 4));
+    if (ok) {
+      cudaMemset(m->mW[l], 0, nw * 4); cudaMemset(m->vW[l], 0, nw * 4);
+      cudaMemset(m->mb[l], 0, nb * 4); cudaMemset(m->vb[l], 0, nb * 4);
+    }
+  }
+  ok = ok && cudaMalloc(&m->d_loss, sizeof(double)) == cudaSuccess;
+  for (int l = 0; l < NL && ok; ++l) ok = cudaMalloc(&m->blob[l], (size_t)LIN[l] * LOUT[l] * 2) == cudaSuccess;
+  ok = ok && cudaMalloc(&m->d_err, sizeof(int)) == cudaSuccess && cudaMemset(m->d_err, 0, sizeof(int)) == cudaSuccess;
+  if (!ok) {
+    izem_mlp_destroy(m);   // frees what was allocated (cudaFree of a null pointer is a no-op)
     return IZEM_ERR_NOMEM;
+  }
   *out = m;
   return IZEM_OK;
 }
@@ -477,11 +485,15 @@ int izem_mlp_forward(izem_mlp* m, int M, const float* x, float* y) {
     for (int c = 0; c < IN; ++c) xp[(size_t)r * INP + c] = x[(size_t)r * IN + c];
   float* dx = nullptr;
   if (cudaMalloc(&dx, xp.size() * 4) != cudaSuccess) return IZEM_ERR_NOMEM;
-  cudaMemcpy(dx, xp.data(), xp.size() * 4, cudaMemcpyHostToDevice);
+  if (cudaMemcpy(dx, xp.data(), xp.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess) {
+    cudaFree(dx);
+    return IZEM_ERR_CUDA;
+  }
   k_f32_to_bf16<<<g1(xp.size()), 256, 0, m->s>>>(dx, m->ib[0], (long long)xp.size());
-  int rc = mlp_infer_tc(m, M, m->ib[0], m->iout, m->s) == cudaSuccess ? IZEM_OK : IZEM_ERR_CUDA;
+  int rc = cudaGetLastError() == cudaSuccess ? IZEM_OK : IZEM_ERR_CUDA;
+  if (rc == IZEM_OK && mlp_infer_tc(m, M, m->ib[0], m->iout, m->s) != cudaSuccess) rc = IZEM_ERR_CUDA;
   std::vector<float> o((size_t)M * OUTP);
-  cudaMemcpyAsync(o.data(), m->iout, o.size() * 4, cudaMemcpyDeviceToHost, m->s);
+  if (cudaMemcpyAsync(o.data(), m->iout, o.size() * 4, cudaMemcpyDeviceToHost, m->s) != cudaSuccess) rc = IZEM_ERR_CUDA;
   if (cudaStreamSynchronize(m->s) != cudaSuccess) rc = IZEM_ERR_CUDA;
   if (rc == IZEM_OK) rc = mlp_tc_status(m);
   cudaFree(dx);
@@ -501,10 +513,17 @@ int izem_mlp_grads(izem_mlp* m, int M, const float* x, const float* t, double* l
   for (int r = 0; r < M; ++r)
     for (int c = 0; c < IN; ++c) xp[(size_t)r * INP + c] = x[(size_t)r * IN + c];
   float *dx = nullptr, *dt = nullptr;
-  cudaMalloc(&dx, xp.size() * 4);
-  cudaMalloc(&dt, (size_t)M * OUT * 4);
-  cudaMemcpy(dx, xp.data(), xp.size() * 4, cudaMemcpyHostToDevice);
-  cudaMemcpy(dt, t, (size_t)M * OUT * 4, cudaMemcpyHostToDevice);
+  if (cudaMalloc(&dx, xp.size() * 4) != cudaSuccess) return IZEM_ERR_NOMEM;
+  if (cudaMalloc(&dt, (size_t)M * OUT * 4) != cudaSuccess) {
+    cudaFree(dx);
+    return IZEM_ERR_NOMEM;
+  }
+  if (cudaMemcpy(dx, xp.data(), xp.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(dt, t, (size_t)M * OUT * 4, cudaMemcpyHostToDevice) != cudaSuccess) {
+    cudaFree(dx);
+    cudaFree(dt);
+    return IZEM_ERR_CUDA;
+  }
   k_f32_to_bf16<<<g1(xp.size()), 256, 0, m->s>>>(dx, m->act[0], (long long)xp.size());
   int rc = IZEM_OK;
   if (mlp_forward(m, M) != cudaSuccess) rc = IZEM_ERR_CUDA;
@@ -634,13 +653,16 @@ int izem_gpu_psr_batch_mlp(izem_mlp* m, izem_mlp* m2, const izem_mech* mech, int
   if (device_ptrs) {
     dT = T; drho = const_cast<double*>(rho); dY = Y; ddt = const_cast<double*>(dt); ddTp = dT_pred;
   } else {
-    if (cudaMalloc(&dT, n * 8) || cudaMalloc(&drho, n * 8) || cudaMalloc(&dY, n * kk * 8) || cudaMalloc(&ddt, n * 8) ||
-        (dT_pred && cudaMalloc(&ddTp, n * 8)))
+    const size_t n8 = (size_t)n * 8;
+    if (cudaMalloc(&dT, n8) || cudaMalloc(&drho, n8) || cudaMalloc(&dY, n8 * kk) || cudaMalloc(&ddt, n8) ||
+        (dT_pred && cudaMalloc(&ddTp, n8))) {
+      // cudaFree(nullptr) is a no-op: release whatever the chain allocated
+      cudaFree(dT); cudaFree(drho); cudaFree(dY); cudaFree(ddt); cudaFree(ddTp);
       return IZEM_ERR_NOMEM;
-    cudaMemcpyAsync(dT, T, n * 8, cudaMemcpyHostToDevice, s);
-    cudaMemcpyAsync(drho, rho, n * 8, cudaMemcpyHostToDevice, s);
-    cudaMemcpyAsync(dY, Y, n * kk * 8, cudaMemcpyHostToDevice, s);
-    cudaMemcpyAsync(ddt, dt, n * 8, cudaMemcpyHostToDevice, s);
+    }
+    if (cudaMemcpyAsync(dT, T, n8, cudaMemcpyHostToDevice, s) || cudaMemcpyAsync(drho, rho, n8, cudaMemcpyHostToDevice, s) ||
+        cudaMemcpyAsync(dY, Y, n8 * kk, cudaMemcpyHostToDevice, s) || cudaMemcpyAsync(ddt, dt, n8, cudaMemcpyHostToDevice, s))
+      rc = IZEM_ERR_CUDA;
   }
   std::vector<cudaEvent_t> ev(2 * nch + 2);
   for (auto& e : ev) cudaEventCreate(&e);
@@ -667,9 +689,9 @@ int izem_gpu_psr_batch_mlp(izem_mlp* m, izem_mlp* m2, const izem_mech* mech, int
   cudaMemcpyAsync(&hs, m->g_stats, sizeof(ChemStats), cudaMemcpyDeviceToHost, s);
   cudaMemcpyAsync(&nfb, m->g_count, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
   if (!device_ptrs) {
-    cudaMemcpyAsync(T, dT, n * 8, cudaMemcpyDeviceToHost, s);
-    cudaMemcpyAsync(Y, dY, n * kk * 8, cudaMemcpyDeviceToHost, s);
-    if (dT_pred) cudaMemcpyAsync(dT_pred, ddTp, n * 8, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(T, dT, (size_t)n * 8, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(Y, dY, (size_t)n * kk * 8, cudaMemcpyDeviceToHost, s);
+    if (dT_pred) cudaMemcpyAsync(dT_pred, ddTp, (size_t)n * 8, cudaMemcpyDeviceToHost, s);
   }
   if (cudaStreamSynchronize(s) != cudaSuccess) rc = IZEM_ERR_CUDA;
   if (rc == IZEM_OK) rc = mlp_tc_status(m);
@@ -770,6 +792,13 @@ __global__ void k_na_unpack(const float* __restrict__ o, int M, float* __restric
 extern "C" int izem_mlp_forward_noalloc(izem_mlp* m, int M, const float* d_x, float* d_y, void* stream) {
   if (!m || !d_x || !d_y || M <= 0) return IZEM_ERR_ARG;
   if (M > NA_ROWS) return IZEM_ERR_TOO_LARGE;
+  // the weights live on the device the handle was created on; the scratch
+  // array is taken from the current device, so the two must be the same
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess) return IZEM_ERR_CUDA;
+  if (dev != m->device) return IZEM_ERR_ARG;
+  // an error left by an earlier, unrelated launch is not this call's
+  (void)cudaGetLastError();
   unsigned char* base = nullptr;
   if (noalloc_scratch(&base) != cudaSuccess) return IZEM_ERR_CUDA;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -777,6 +806,7 @@ extern "C" int izem_mlp_forward_noalloc(izem_mlp* m, int M, const float* d_x, fl
                            reinterpret_cast<__nv_bfloat16*>(base + NA_ACT_BYTES)};
   float* out = reinterpret_cast<float*>(base + 2 * NA_ACT_BYTES);
   k_na_pack<<<g1((long long)M * INP), 256, 0, s>>>(d_x, M, buf[0]);
+  if (cudaGetLastError() != cudaSuccess) return IZEM_ERR_CUDA;
   int cur = 0;
   for (int l = 0; l < NL; ++l) {
     GemmArgs a{};

@@ -81,7 +81,9 @@ def air2():
 
 
 if __name__ == "__main__":
-    REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) < 2:
+        sys.exit("usage: make_species_data.py <root of the reference checkout (holds devel-izem/)>")
+    REF = sys.argv[1]
     tc = os.path.join(REF, "devel-izem", "testcases")
     sets = {
         "h2air9": build(os.path.join(tc, "shockedshearlayer", "tranfit.out"), os.path.join(tc, "sod", "therm.dat"),

@@ -167,6 +167,14 @@ def mixing_layer(nx=256, ny=256, nz=128, Lx=12e-3, Ly=12e-3, Lz=6e-3, seed=SEED,
     return cfg, thd, adi_struct(a), dxi, state, info
 
 
+def mixing_layer_block(nx=64, ny=64, nz=32, seed=SEED, lib_dscalar=None):
+    """A smaller block of the 256 x 256 x 128 mixing layer with its grid
+    spacing (12 mm / 256 in x, 12 mm / 255 in y, 6 mm / 128 in z), centred
+    on the layer in y, with the same faces, profiles and seeded noise law."""
+    return mixing_layer(nx, ny, nz, Lx=nx * 12e-3 / 256, Ly=(ny - 1) * 12e-3 / 255, Lz=nz * 6e-3 / 128, seed=seed,
+                        lib_dscalar=lib_dscalar)
+
+
 def batched_reactors(n, seed=SEED):
     """Independent H2/air reactors: T ~ U[800, 2400] K, p ~ U[1, 10] atm,
     equivalence ratio ~ U[0.3, 3], progress c ~ U[0, 1] blending the unburnt

@@ -48,6 +48,7 @@ def load_library(path=None):
         "izem_gpu_init": (C.c_int, [C.POINTER(IzemCfg), C.POINTER(IzemThd), C.POINTER(IzemAdi), C.POINTER(P)]),
         "izem_gpu_destroy": (None, [P]),
         "izem_gpu_last_error": (C.c_int, [P, C.c_char_p, C.c_int]),
+        "izem_gpu_newton_stats": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int]),
         "izem_gpu_set_grid": (C.c_int, [P, _dp, _dp, _dp]),
         "izem_gpu_upload_state": (C.c_int, [P, _dp, _dp, _dp, _dp, _dp, _u8p]),
         "izem_gpu_download_state": (C.c_int, [P, _dp, _dp, _dp, _dp, _dp, _u8p]),
@@ -202,6 +203,14 @@ class IzemGPU:
 
     def newton_warnings(self):
         return self.lib.izem_gpu_last_error(self.h, None, 0)
+
+    def newton_stats(self, reset=False):
+        """(most Newton iterations of any sub-domain, solves that reached itmax)
+        since the context was made or since the last reset."""
+        it, unc = C.c_int(0), C.c_int(0)
+        self._check(self.lib.izem_gpu_newton_stats(self.h, C.byref(it), C.byref(unc), int(bool(reset))),
+                    "newton_stats")
+        return it.value, unc.value
 
     # ---- state ----------------------------------------------------------
     def set_grid(self, dx_i, dy_i, dz_i):
@@ -403,3 +412,48 @@ class IzemGPU:
 
     def synchronize(self):
         self._check(self.lib.izem_gpu_synchronize(self.h), "synchronize")
+
+
+CHEM_BDF, CHEM_MLP = 0, 1
+
+
+class TimeLoop:
+    """One pass of the reference driver's main loop (izem.f90:252-281) over
+    a device context:
+
+    * ``timestep`` with the previous step's dtmin and the chemistry's DTmax
+      (the CPR criterion dt_4(4) reads both);
+    * with chemistry, the Strang sequence ``reaction_selec(dtmin/2)``,
+      ``rk3(dtmin)`` from the current time, time += dtmin,
+      ``reaction_selec(dtmin/2)``, whose DTmax feeds the next time step;
+    * without chemistry, ``rk3(dtmin)`` and time += dtmin.
+
+    The clipping of dtmin onto statistics times (:256-263) belongs to the
+    caller, who may pass ``dt`` to impose a step.  ``chem`` is the hook that
+    runs a chemistry half step and returns DTmax; subclasses wrap it to log
+    per-half-step statistics."""
+
+    def __init__(self, solver, reaction, chem_mode=CHEM_BDF, time=0.0):
+        self.s = solver
+        self.reaction = bool(reaction)
+        self.mode = chem_mode
+        self.time = float(time)
+        self.dtmin = 1.0
+        self.DTmax = 0.0
+        self.dt4 = None
+
+    def chem(self, dt):
+        return self.s.reaction_selec(dt, mode=self.mode)
+
+    def step(self, dt=None):
+        self.dt4, dtmin = self.s.timestep(DTmax=self.DTmax, dtmin=self.dtmin)
+        if dt is not None:
+            dtmin = float(dt)
+        if self.reaction:
+            self.chem(0.5 * dtmin)
+        self.s.rk3(dtmin, self.time)
+        self.time += dtmin
+        if self.reaction:
+            self.DTmax = self.chem(0.5 * dtmin)
+        self.dtmin = dtmin
+        return dtmin

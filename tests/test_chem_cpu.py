@@ -7,6 +7,7 @@ import numpy as np
 import pytest
 
 import oracle
+import refdata
 from phd_gb300 import ics
 from phd_gb300.mech import h2_mechanism
 from phd_gb300.thd import load_species
@@ -168,15 +169,13 @@ def test_dvodesimp_skips_pure_streams_and_keeps_the_rest():
     assert orc.chem_step(again, m, 0.5) == dtm_full and np.array_equal(again["v"], full["v"])
 
 
-@pytest.mark.skipif(not os.path.isdir(os.environ.get("IZEM_REFERENCE_TESTCASES", "/root/reference/devel-izem/testcases")),
-                    reason="reference tree not mounted")
+@refdata.needs_reference
 def test_mechanism_species_match_reference_interpreter_output():
     """The species, their order and molecular weights of the shipped
     mechanism are those of the reference's CHEMKIN interpreter listing for
     the 9-species case (testcases/shockedshearlayer/chem.out)."""
-    ref = os.environ.get("IZEM_REFERENCE_TESTCASES", "/root/reference/devel-izem/testcases")
     rows = []
-    for line in open(os.path.join(ref, "shockedshearlayer", "chem.out")):
+    for line in open(refdata.path("shockedshearlayer", "chem.out")):
         t = line.split()
         if len(t) >= 8 and t[0].endswith(".") and t[0][:-1].isdigit() and t[2] == "G":
             rows.append((t[1], float(t[4])))

@@ -358,3 +358,70 @@ def test_rk3_steps_jet_faces(species):
     err = W.normwise(got["v"][:ng + cfg.nx + ng, ng:-ng, ng:-ng], st["v"][:ng + cfg.nx + ng, ng:-ng, ng:-ng])
     assert np.all(err <= TOL), err
     assert np.max(np.abs(interior(got["T"]) - interior(st["T"]))) <= TOL * np.max(st["T"])
+
+
+def _hot_spot(st, fac=40.0):
+    """Raise the internal energy of a 3x3x3 block of interior cells by
+    `fac`, keeping density, momentum and the temperature guess: the Newton
+    solve then starts far below a temperature (about 20,000 K) that lies
+    above the species fits' Tmax, where the reference's linear
+    extrapolation of h with a growing cp makes Newton converge linearly
+    (26 iterations in the oracle, more than any fixed small count)."""
+    v = st["v"]
+    sl = (slice(5, 8), slice(5, 8), slice(5, 8))
+    rho = v[sl + (0,)]
+    ek = 0.5 * (v[sl + (1,)] ** 2 + v[sl + (2,)] ** 2 + v[sl + (3,)] ** 2) / rho
+    v[sl + (4,)] = ek + (v[sl + (4,)] - ek) * fac
+    return st
+
+
+@pytest.mark.parametrize("timed", [False, True])
+def test_newton_runs_to_the_reference_limit(timed):
+    """prim_inv_var (module_thermodynamics.f90:79-186) iterates until its
+    stopping test holds or 200 iterations have run.  A state that needs 26
+    iterations gives the oracle's T, cp, h and conserved variables to
+    1e-12, both from the captured graph (a conditional WHILE node) and
+    from direct launches with kernel timing; the library reports the
+    iteration count and no unconverged solve."""
+    cfg, thd, adi, dxi, st, info, orc = W.case("mix", 12)
+    _hot_spot(st)
+    g = gpu_from(cfg, thd, adi, dxi, st)
+    if timed:
+        g.set_kernel_timing(True)
+    ref = W.copy(st)
+    orc.update_primitives(ref)
+    assert orc.newton_it_max() > 12
+    g.update_primitives()
+    got = g.download()
+    it_max, unconverged = g.newton_stats(reset=True)
+    g.close()
+    assert it_max == orc.newton_it_max() and unconverged == 0, (it_max, orc.newton_it_max(), unconverged)
+    for k in ("T", "cp"):
+        err = np.abs(got[k] - ref[k]).max() / np.abs(ref[k]).max()
+        assert err <= TOL, (k, err)
+    assert np.all(W.normwise(got["ha"], ref["ha"]) <= TOL)
+    assert np.all(W.normwise(got["v"], ref["v"]) <= TOL)
+
+
+def test_rk3_newton_beyond_a_dozen_iterations():
+    """A block heated 20-fold (about 11,000 K, above the species fits'
+    Tmax) and closed by update_primitives, then one RK3 step: the blast
+    changes its temperature within a stage, and Newton, linear in that
+    range, needs 64 iterations in the oracle.  The graph-captured step
+    matches the oracle's to 1e-12 per conserved variable."""
+    cfg, thd, adi, dxi, st, info, orc = W.case("mix", 12)
+    _hot_spot(st, 20.0)
+    orc.update_primitives(st)
+    g = gpu_from(cfg, thd, adi, dxi, st)
+    dt4, dt = orc.timestep(st)
+    orc.rk3(st, dt)
+    assert orc.newton_it_max() > 12
+    g.rk3(dt)
+    got = g.download()
+    it_max, unconverged = g.newton_stats()
+    g.close()
+    assert it_max == orc.newton_it_max() and unconverged == 0, (it_max, orc.newton_it_max(), unconverged)
+    err = W.normwise(interior(got["v"]), interior(st["v"]))
+    assert np.all(err <= TOL), err
+    errT = np.abs(interior(got["T"]) - interior(st["T"])).max() / np.abs(interior(st["T"])).max()
+    assert errT <= TOL, errT

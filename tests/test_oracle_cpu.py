@@ -10,15 +10,14 @@ import workloads as W
 from phd_gb300 import thd as T
 from phd_gb300.capi import IzemCfg, IzemThd, IzemAdi
 
-# the reference tree, where it is mounted (IZEM_REFERENCE_TESTCASES overrides)
-REF = os.environ.get("IZEM_REFERENCE_TESTCASES", "/root/reference/devel-izem/testcases")
+import refdata
 
 
-@pytest.mark.skipif(not os.path.isdir(REF), reason="reference tree not mounted")
+@refdata.needs_reference
 @pytest.mark.parametrize("setname,tranfit", [("h2air9", "shockedshearlayer/tranfit.out"), ("o2n2", "sod/tranfit.out")])
 def test_shipped_species_match_reference_files(setname, tranfit):
-    tf = T.read_tranfit(os.path.join(REF, tranfit))
-    th = T.read_therm(os.path.join(REF, "sod/therm.dat"), tf["names"])
+    tf = T.read_tranfit(refdata.path(tranfit))
+    th = T.read_therm(refdata.path("sod", "therm.dat"), tf["names"])
     sp = T.load_species(setname)
     assert sp["names"] == tf["names"]
     assert sp["cofd"] == tf["cofd"] and sp["coflam"] == tf["coflam"] and sp["cofeta"] == tf["cofeta"]

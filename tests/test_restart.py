@@ -2,7 +2,8 @@
 save_restart_hdf5 / read_restart_hdf5, module_io.f90:56-197).
 
 * The reader returns the reference's own Sod restart files as the committed
-  fixtures hold them (where the reference tree is mounted).
+  fixtures hold them (where IZEM_REFERENCE_TESTCASES names the reference's
+  test cases).
 * Written files read back bit for bit, group members beyond one symbol node
   included, and carry the same dataset header messages as the reference's.
 * Resuming: read_restart_hdf5 fills the interior and closes the state; the
@@ -20,8 +21,9 @@ import pytest
 import sod_case as S
 from phd_gb300 import restart as R
 
-REF = os.environ.get("IZEM_REFERENCE_TESTCASES", "/root/reference/devel-izem/testcases")
-SOD_RESTARTS = os.path.join(REF, "sod", "restarts")
+import refdata
+
+SOD_RESTARTS = refdata.path("sod", "restarts")
 NAMES = ["rho", "rhoU", "rhoV", "rhoW", "rhoE", "O2", "N2"]
 
 
@@ -30,7 +32,7 @@ def _golden_arrays(n):
     return [g[k] for k in NAMES], float(g["time"][0])
 
 
-@pytest.mark.skipif(not os.path.isdir(SOD_RESTARTS), reason="reference tree not mounted")
+@refdata.needs_reference
 @pytest.mark.parametrize("n", [1, 2, 3])
 def test_reads_reference_restart_files(n):
     names, arrays, time = R.read_restart(os.path.join(SOD_RESTARTS, "restart_%05d.h5" % n))
@@ -51,7 +53,7 @@ def test_write_read_round_trip(tmp_path):
     assert all(np.array_equal(a, b) for a, b in zip(got, arrays))
 
 
-@pytest.mark.skipif(not os.path.isdir(SOD_RESTARTS), reason="reference tree not mounted")
+@refdata.needs_reference
 def test_written_headers_match_reference_file(tmp_path):
     """The dataspace, datatype, fill-value and layout messages of a written
     dataset have the reference file's types, sizes and (but for the data

@@ -81,3 +81,43 @@ def mixing_layer_with_streams(nx=12, ny=24, nz=8):
     yf = np.zeros(9); yf[ih2] = 0.5; yf[in2] = 0.5
     yo = np.zeros(9); yo[names.index("O2")] = 0.233; yo[in2] = 0.767
     return cfg, thd, adi, dxi, st, orc, (yf, yo, ih2, in2)
+
+
+RTOL, ATOL = 1e-6, 1e-10   # the reference's DVODE tolerances (module_reaction.f90, ITOL = 1)
+
+
+def tol_units(got, ref):
+    """|got - ref| in units of the integrator's tolerance RTOL |ref| + ATOL."""
+    return np.abs(np.asarray(got) - np.asarray(ref)) / (RTOL * np.abs(np.asarray(ref)) + ATOL)
+
+
+def chem_error_stats(got, ref, ng=3, nrv=9):
+    """Per-cell error of a chemistry-carrying state against the oracle's, in
+    units of the integrator's tolerance: temperature and every species mass
+    fraction (the DVODE unknowns z = [T, Y_1..Y_K], chemkin reaction_v.f),
+    summarised as median, 99th percentile and max over the interior."""
+    i = (slice(ng, -ng),) * 3
+    rT = tol_units(got["T"][i], ref["T"][i]).ravel()
+    vg, vr = got["v"][i], ref["v"][i]
+    rY = np.stack([tol_units(vg[..., 5 + q] / vg[..., 0], vr[..., 5 + q] / vr[..., 0]).ravel()
+                   for q in range(nrv)], axis=1).max(axis=1)
+    out = {}
+    for nm, r in (("T", rT), ("Y", rY)):
+        out[nm] = {"median": float(np.median(r)), "p99": float(np.percentile(r, 99)), "max": float(r.max())}
+    return out
+
+
+def oracle_step(orc, st, mech, loop):
+    """The reference driver's step (izem.f90:252-281) on the oracle, in the
+    order of phd_gb300.izem.TimeLoop: timestep with the previous dtmin and
+    DTmax, then chem(dt/2), rk3(dt), chem(dt/2) when mech is given.
+    loop: dict with dtmin, DTmax and time, updated in place.  Returns dt."""
+    _, dt = orc.timestep(st, DTmax=loop["DTmax"], dtmin=loop["dtmin"])
+    if mech is not None:
+        orc.chem_step(st, mech, 0.5 * dt)
+    orc.rk3(st, dt, loop["time"])
+    loop["time"] += dt
+    if mech is not None:
+        loop["DTmax"] = orc.chem_step(st, mech, 0.5 * dt)
+    loop["dtmin"] = dt
+    return dt
