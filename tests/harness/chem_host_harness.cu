@@ -32,3 +32,24 @@ extern "C" void host_fun_pair(const izem_mech* m, int n, const double* rho, cons
     ck_fun_fast<9>(rho[q], z + 10 * q, zp_fast + 10 * q);
   }
 }
+
+// The integrator as the GPU kernels run it -- the right-hand side with
+// reciprocals (ck_fun_fast) -- on the host, without fused multiply-adds and
+// with the host's libm: what the reciprocal form alone changes against the
+// oracle, apart from CUDA's exp/log and FMA contraction.
+extern "C" void host_psr_fast(const izem_mech* m, int n, double* T, const double* rho, double* Y, const double* dt,
+                              int* nst_out) {
+  c_mech_host = *m;
+  c_fast_host = chem_fast_constants(*m);
+  for (int q = 0; q < n; ++q) {
+    Rc<10> r;
+    double z[10];
+    z[0] = T[q];
+    for (int k = 0; k < 9; ++k) z[1 + k] = Y[q * 9 + k];
+    rc_start<10>(r, rho[q], z, dt[q]);
+    while (rc_advance<10>(r)) ck_fun_fast<9>(r.rho, r.y, r.fo);
+    nst_out[q] = r.nsteps;
+    T[q] = r.y[0];
+    for (int k = 0; k < 9; ++k) Y[q * 9 + k] = r.y[1 + k];
+  }
+}

@@ -69,62 +69,85 @@ def test_chem_step_field_on_cpu():
     assert dtm >= 0.0
 
 
-def test_device_integrator_reproduces_oracle_bitwise(tmp_path):
-    """The GPU BDF code, compiled for the host without FMA contraction, gives
-    the oracle's results bit for bit: the device port is the same algorithm
-    in the same operation order."""
+@pytest.fixture(scope="module")
+def host_chem(tmp_path_factory):
+    """The GPU chemistry source (chem.cu) compiled for the host with FMA
+    contraction off (tests/harness/chem_host_harness.cu)."""
     import ctypes as C
-    import os
     import shutil
     import subprocess
     nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
     if not os.path.exists(nvcc):
         pytest.skip("nvcc not available")
     here = os.path.dirname(os.path.abspath(__file__))
-    so = str(tmp_path / "libchemhost.so")
+    so = str(tmp_path_factory.mktemp("chemhost") / "libchemhost.so")
     subprocess.check_call([nvcc, "-std=c++17", "-O2", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
                            "-shared", "-gencode", "arch=compute_103a,code=sm_103a", "-o", so,
                            os.path.join(here, "harness", "chem_host_harness.cu")])
-    lib = C.CDLL(so)
-    P = lambda a: a.ctypes.data_as(C.c_void_p)
+    return C.CDLL(so)
+
+
+def _P(a):
+    import ctypes as C
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def test_device_integrator_reproduces_oracle_bitwise(host_chem):
+    """The GPU BDF code, compiled for the host without FMA contraction, gives
+    the oracle's results bit for bit: the device port is the same algorithm
+    in the same operation order."""
+    import ctypes as C
     m = h2_mechanism()
     T, rho, Y, dt = ics.batched_reactors(512, seed=21)
     To, Yo = T.copy(), Y.copy()
     oracle.psr_cells(m, To, rho.copy(), Yo, dt.copy())
     Th, Yh = T.copy(), Y.copy()
     ns = np.zeros(len(T), np.int32)
-    lib.host_psr(C.byref(m), len(T), P(Th), P(rho), P(Yh), P(dt), P(ns))
+    host_chem.host_psr(C.byref(m), len(T), _P(Th), _P(rho), _P(Yh), _P(dt), _P(ns))
     assert np.array_equal(Th, To) and np.array_equal(Yh, Yo)
 
 
-def test_device_rhs_with_reciprocals_matches_reference_order(tmp_path):
+def test_device_rhs_with_reciprocals_matches_reference_order(host_chem):
     """The BDF kernels evaluate the reactor right-hand side with the
     divisions replaced by reciprocal multiplications (ck_fun_fast); on the
     host it agrees with the reference-order form to a few ulp of each
     term: 1e-12 relative to the largest rate of each component."""
     import ctypes as C
-    import os
-    import shutil
-    import subprocess
-    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
-    if not os.path.exists(nvcc):
-        pytest.skip("nvcc not available")
-    here = os.path.dirname(os.path.abspath(__file__))
-    so = str(tmp_path / "libchemhost2.so")
-    subprocess.check_call([nvcc, "-std=c++17", "-O2", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
-                           "-shared", "-gencode", "arch=compute_103a,code=sm_103a", "-o", so,
-                           os.path.join(here, "harness", "chem_host_harness.cu")])
-    lib = C.CDLL(so)
-    P = lambda a: a.ctypes.data_as(C.c_void_p)
     m = h2_mechanism()
     T, rho, Y, dt = ics.batched_reactors(4096, seed=23)
     z = np.ascontiguousarray(np.concatenate([T[:, None], Y], axis=1))
     zr, zf = np.zeros_like(z), np.zeros_like(z)
-    lib.host_fun_pair(C.byref(m), len(T), P(rho), P(z), P(zr), P(zf))
+    host_chem.host_fun_pair(C.byref(m), len(T), _P(rho), _P(z), _P(zr), _P(zf))
     scale = np.abs(zr).max(axis=0)
     assert np.array_equal(zf[:, scale == 0], zr[:, scale == 0])   # components that stay exactly zero
     err = (np.abs(zf - zr) / np.where(scale == 0, 1.0, scale)).max(axis=0)
     assert np.all(err < 1e-12), err
+
+
+def test_reciprocal_form_alone_against_the_oracle(host_chem):
+    """The integrator with the device right-hand side (ck_fun_fast), on the
+    host with the host's libm and no FMA contraction, against the oracle on
+    the 2048 batched reactors of the GPU batch test.  The reciprocal form
+    alone perturbs the last bits of the rates; in igniting cells that
+    changes adaptive step decisions (about 6 % of the cells take another
+    number of steps), and those cells differ by the integrator's own global
+    error.  The bounds are those of workloads.reactor_error_bounds, which
+    the GPU batch meets as well: the GPU's remaining difference from the
+    oracle is of this kind, not an error of CUDA's exp/log or of FMA
+    contraction."""
+    import ctypes as C
+    import workloads as W
+    m = h2_mechanism()
+    T, rho, Y, dt = ics.batched_reactors(2048, seed=21)
+    To, Yo = T.copy(), Y.copy()
+    oracle.psr_cells(m, To, rho.copy(), Yo, dt.copy())
+    Th, Yh = T.copy(), Y.copy()
+    ns = np.zeros(len(T), np.int32)
+    host_chem.host_psr_fast(C.byref(m), len(T), _P(Th), _P(rho), _P(Yh), _P(dt), _P(ns))
+    st, msg, ok = W.reactor_error_bounds(Th, Yh, To, Yo)
+    print(msg)
+    assert ok, msg
+    assert st["T"]["max"] > 0   # the reciprocal form does change results
 
 
 def _window(cfg):

@@ -7,11 +7,15 @@ On the GPU, fused multiply-adds and CUDA's exp/log perturb the last bits;
 for ignition-delay cells the radical pool starts below ATOL = 1e-10 and
 grows exponentially, so those perturbations change the adaptive step
 sequence and the two results differ by the integrator's own global error.
-Bounds, with tol(y) = RTOL |y| + ATOL (RTOL = 1e-6):
-  * temperature, every cell:   |dT| <= 100 tol(T)   (1e-4 relative)
-  * temperature, 99 % of cells: |dT| <= 10 tol(T)
-  * species, every cell:       |dY_k| <= 1e-3 max_cells |Y_k|
-  * median cell: relative T difference below 1e-10 (rounding level)"""
+Bounds (workloads.reactor_error_bounds), with tol(y) = RTOL |y| + ATOL
+(RTOL = 1e-6) per cell:
+  * temperature: median < 1e-3, 99th percentile <= 10, max <= 200 tol(T)
+  * species (largest over k per cell): median < 1e-2, 90th percentile
+    <= 10 tol(Y_k); every cell |dY_k| <= 1e-3 max_cells |Y_k|
+  * batch median cell: relative T difference below 1e-10 (rounding level)
+The same bounds hold for the device right-hand side compiled for the host
+without FMA and with the host's libm (tests/test_chem_cpu.py): the
+reciprocal form alone produces differences of this size."""
 import numpy as np
 import pytest
 
@@ -33,11 +37,9 @@ def test_psr_batch_matches_oracle():
     Tg, Yg = T.copy(), Y.copy()
     ist_g, ns_g, ms = psr_batch(m, Tg, rho.copy(), Yg, dt.copy())
     assert np.all(ist_g == 2) and np.all(ist_o == 2)
-    rT = np.abs(Tg - To) / (RTOL * np.abs(To) + ATOL)
-    rYn = (np.abs(Yg - Yo) / np.abs(Yo).max(axis=0)).max()
-    msg = "T: max %.3g p99 %.3g (units of tol); Y: max normwise %.3g" % (rT.max(), np.percentile(rT, 99), rYn)
-    assert rT.max() <= 100 and np.percentile(rT, 99) <= 10, msg
-    assert rYn <= 1e-3, msg
+    st, msg, ok = W.reactor_error_bounds(Tg, Yg, To, Yo)
+    print(msg)
+    assert ok, msg
     assert np.median(np.abs(Tg - To) / To) < 1e-10, msg
 
 
@@ -53,13 +55,12 @@ def test_field_chem_step_matches_oracle():
     dtm_g = g.reaction_selec(dt)
     got = g.download()
     i = (slice(3, -3),) * 3
-    T_o, T_g = st["T"][i], got["T"][i]
-    assert np.all(np.abs(T_g - T_o) <= 100 * (RTOL * np.abs(T_o) + ATOL))
     v_o, v_g = st["v"][i], got["v"][i]
-    for q in range(5, 14):
-        yo = v_o[..., q] / v_o[..., 0]
-        yg = v_g[..., q] / v_g[..., 0]
-        assert np.all(np.abs(yg - yo) <= 1e-3 * np.abs(yo).max() + ATOL)
+    Yo = np.stack([v_o[..., q] / v_o[..., 0] for q in range(5, 14)], axis=-1).reshape(-1, 9)
+    Yg = np.stack([v_g[..., q] / v_g[..., 0] for q in range(5, 14)], axis=-1).reshape(-1, 9)
+    s_, msg, ok = W.reactor_error_bounds(got["T"][i].ravel(), Yg, st["T"][i].ravel(), Yo)
+    print(msg)
+    assert ok, msg
     assert abs(dtm_g - dtm_o) <= 100 * (RTOL * 3000 + ATOL)
     st_ = g.chem_stats()
     assert st_["failed"] == 0

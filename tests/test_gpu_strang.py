@@ -16,11 +16,12 @@ Bounds, written here:
     as in the other parity tests;
   * with chemistry, in units of the integrator's tolerance
     tol(y) = RTOL |y| + ATOL (RTOL = 1e-6, ATOL = 1e-10) per cell, for T and
-    for every species mass fraction: max <= 100, 99th percentile <= 10,
-    median <= 0.1.  The two DVODE runs agree to rounding except where
-    last-bit differences of exp/log change an adaptive step decision; such
-    cells differ by the integrator's own error, a few tol units;
-    sum_k Y_k = 1 within 1e-13.
+    for every species mass fraction: max <= 1e-4.  In this pre-ignition
+    window every reactor takes the same three BDF steps on both sides, no
+    adaptive step decision differs, and the two DVODE runs agree to
+    rounding (measured: T 1.2e-9, species 4e-7 tol units, i.e. about 1e-15
+    relative in T); a changed step decision would show as about one tol
+    unit.  sum_k Y_k = 1 within 1e-13.
 """
 import numpy as np
 import pytest
@@ -88,4 +89,4 @@ def test_driver_step_on_the_mixing_layer_block(chem):
     msg = "tol units: T %s, Y %s" % (s["T"], s["Y"])
     print(msg)
     for k in ("T", "Y"):
-        assert s[k]["max"] <= 100 and s[k]["p99"] <= 10 and s[k]["median"] <= 0.1, msg
+        assert s[k]["max"] <= 1e-4, msg

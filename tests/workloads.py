@@ -121,3 +121,25 @@ def oracle_step(orc, st, mech, loop):
         loop["DTmax"] = orc.chem_step(st, mech, 0.5 * dt)
     loop["dtmin"] = dt
     return dt
+
+
+def reactor_error_bounds(Tg, Yg, To, Yo):
+    """Errors of an integrated reactor batch against the oracle's, in the
+    integrator's tolerance units per cell (T, and the largest over the
+    species), plus the species error relative to each species' largest
+    value.  Returns (stats dict, message, ok) for the bounds that any
+    last-bit perturbation of the right-hand side meets on the batched
+    ignition reactors (the reciprocal form alone, on the host, reaches
+    T max 97 and species p99 74): T median < 1e-3, p99 <= 10, max <= 200;
+    species median < 1e-2, p90 <= 10; species relative to their largest
+    value <= 1e-3."""
+    rT = tol_units(Tg, To).ravel()
+    rY = tol_units(Yg, Yo).reshape(len(rT), -1).max(axis=1)
+    yn = float((np.abs(Yg - Yo) / np.maximum(np.abs(Yo).max(axis=0), 1e-300)).max())
+    st = {"T": {"median": float(np.median(rT)), "p99": float(np.percentile(rT, 99)), "max": float(rT.max())},
+          "Y": {"median": float(np.median(rY)), "p90": float(np.percentile(rY, 90)), "p99": float(np.percentile(rY, 99)),
+                "max": float(rY.max())},
+          "Y_rel_to_max": yn}
+    ok = (st["T"]["median"] < 1e-3 and st["T"]["p99"] <= 10 and st["T"]["max"] <= 200 and
+          st["Y"]["median"] < 1e-2 and st["Y"]["p90"] <= 10 and yn <= 1e-3)
+    return st, "tol units: %s" % st, ok
