@@ -295,6 +295,8 @@ def run_gpu(args, rank, world):
                    "transport": "EGLIB precision 1 (EGSE2, EGSLCT2, EGSDR1)" if eg else "fitted mixture-averaged (tranfit)",
                    "chemistry": ("Strang: 2 x BDF (DVODE MF=22) half-steps per step, 9 species / 12 reactions"
                                  if chem else "off"),
+                   "chem_rhs": (("generated for the mechanism" if g.lib.izem_gpu_chem_generated() else
+                                 "mechanism tables") if chem else None),
                    "l2": "inputs larger than L2 (state %.2f GB)" % (host["v"].nbytes / 1e9),
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "autotuned_threads_per_block": {k: v["chosen"] for k, v in tuning.items()},

@@ -374,6 +374,18 @@ int  izem_gpu_autotune(izem_ctx* ctx, double chem_dt, char* report, int report_l
  * the process, as izem_gpu_autotune would choose it (no counterpart in the
  * reference); IZEM_ERR_ARG outside 0..4. */
 int  izem_gpu_set_chem_variant(int variant);
+/* 1 when the chemistry kernels evaluate the reactor right-hand side from
+ * code generated for the mechanism last passed to izem_gpu_set_mechanism
+ * (the shipped H2/air mechanism; the same operations in the same order as
+ * the table-driven form, with the tables as literals), 0 when they walk the
+ * mechanism's tables (any other mechanism).  No counterpart in the
+ * reference. */
+int  izem_gpu_chem_generated(void);
+/* allow = 0 makes the chemistry kernels walk the mechanism's tables even
+ * for the shipped mechanism (to compare the two forms); allow = 1 (the
+ * default) uses the generated form whenever it applies.  Takes effect at
+ * the next izem_gpu_set_mechanism / izem_gpu_psr_batch. */
+int  izem_gpu_allow_chem_generated(int allow);
 /* Reproduce a run of the reference decomposed into nblk equal MPI blocks
  * along x (its NUMPROCX) on this single context: the reference never
  * exchanges the shock sensor, so each block tests only its own points

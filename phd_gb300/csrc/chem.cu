@@ -26,6 +26,21 @@
 #include "../../include/izem_gpu.h"
 #include "chem.h"
 
+// This source builds two translation units, compiled in parallel:
+// IZEM_CHEM_UNIT 0 (chem.cu) holds the host side and the kernels that walk
+// the uploaded mechanism's tables; 1 (chem_generated.cu) the kernels with
+// the right-hand side generated for the shipped mechanism.
+#ifndef IZEM_CHEM_UNIT
+#define IZEM_CHEM_UNIT 0
+#endif
+
+// The persistent kernels of one register-budget variant and right-hand-side form.
+struct ChemKernelSet {
+  void (*field)(ChemField, unsigned*, ChemStats*);
+  void (*batch)(int, double*, const double*, double*, const double*, int*, int*, unsigned*, ChemStats*);
+  void (*list)(const int*, const unsigned*, double*, const double*, double*, const double*, unsigned*, ChemStats*);
+};
+
 namespace {
 
 __constant__ izem_mech c_mech_dev;
@@ -377,6 +392,30 @@ HD void ck_fun_fast(double rho, const double* z, double* zp) {
   fun_tpart<KK>(z[0], t);
   fun_cpart<KK>(rho, z, t, zp);
 }
+
+#include "chem_gen.cuh"
+
+// Right-hand-side policies of the BDF driver: the generic form, which walks
+// the uploaded mechanism's tables, and the generated form of the mechanism
+// the library was built with (chem_gen.cuh, phd_gb300/mechgen.py), which
+// performs the same operations in the same order with the tables as
+// literals.  chem_upload_mech picks the generated form when the uploaded
+// mechanism is that one.
+template <int KK>
+struct RhsTables {
+  using Terms = FunT<KK>;
+  static HD __forceinline__ void tpart(double T, Terms& t) { fun_tpart<KK>(T, t); }
+  static HD __forceinline__ void cpart(double rho, const double* z, const Terms& t, double* zp) {
+    fun_cpart<KK>(rho, z, t, zp);
+  }
+};
+struct RhsGenerated {
+  using Terms = chem_gen::FunT;
+  static HD __forceinline__ void tpart(double T, Terms& t) { chem_gen::tpart(T, t); }
+  static HD __forceinline__ void cpart(double rho, const double* z, const Terms& t, double* zp) {
+    chem_gen::cpart(rho, z, t, zp);
+  }
+};
 
 // ------------------------------------------------------------- DVODE -------
 template <int N>
@@ -1086,11 +1125,11 @@ HD int reaction_v(double rho, double* z, double tf, int* nsteps) {
 // kMaxFun caps the FUN rounds of one cell above that bound.
 constexpr long long kMaxFun = 1LL << 25;
 
-template <int KK, class Load, class Store>
+template <int KK, class Rhs, class Load, class Store>
 __device__ __forceinline__ void rc_drive(unsigned n, unsigned* counter, Load load, Store store) {
   constexpr int N = KK + 1;
   Rc<N> r;
-  FunT<KK> ft;   // temperature terms of this thread's last right-hand side
+  typename Rhs::Terms ft;   // temperature terms of this thread's last right-hand side
   ft.T = -1.0;
   unsigned q = 0;
   bool active = false;
@@ -1113,8 +1152,8 @@ __device__ __forceinline__ void rc_drive(unsigned n, unsigned* counter, Load loa
       // species columns of a Jacobian): a per-lane choice would only make
       // the warp wait for its slowest lane.  Reused terms are the bits the
       // recomputation would give.
-      if (!__all_sync(__activemask(), r.y[0] == ft.T)) fun_tpart<KK>(r.y[0], ft);
-      fun_cpart<KK>(r.rho, r.y, ft, r.fo);
+      if (!__all_sync(__activemask(), r.y[0] == ft.T)) Rhs::tpart(r.y[0], ft);
+      Rhs::cpart(r.rho, r.y, ft, r.fo);
     } else {
       store(q, r);
       active = false;
@@ -1247,7 +1286,7 @@ __global__ void k_chem_scatter_list(ChemField f, const int* list, const unsigned
 // tolerance rather than to the bit.
 constexpr int kChemThreads = 128;
 
-template <int KK, int MINB>
+template <int KK, int MINB, class Rhs>
 __global__ void __launch_bounds__(kChemThreads, MINB) k_psr_field(ChemField f, unsigned* counter, ChemStats* stats) {
   constexpr int N = KK + 1;
   const long long ncell = (long long)f.wx * f.wy * f.wz;
@@ -1281,10 +1320,10 @@ __global__ void __launch_bounds__(kChemThreads, MINB) k_psr_field(ChemField f, u
     f.v[(5 + KK - 1) * nc + p] = rho0 * (1.0 - sumY);
     if (f.dT_out) f.dT_out[q] = r.y[0] - T0;
   };
-  rc_drive<KK>((unsigned)ncell, counter, load, store);
+  rc_drive<KK, Rhs>((unsigned)ncell, counter, load, store);
 }
 
-template <int KK, int MINB>
+template <int KK, int MINB, class Rhs>
 __global__ void __launch_bounds__(kChemThreads, MINB) k_psr_batch(int n, double* T, const double* rho, double* Y,
                                                                   const double* dt, int* istate, int* nsteps,
                                                                   unsigned* counter, ChemStats* stats) {
@@ -1304,7 +1343,7 @@ __global__ void __launch_bounds__(kChemThreads, MINB) k_psr_batch(int n, double*
     if (istate) istate[q] = r.istate;
     if (nsteps) nsteps[q] = r.nsteps;
   };
-  rc_drive<KK>((unsigned)n, counter, load, store);
+  rc_drive<KK, Rhs>((unsigned)n, counter, load, store);
 }
 
 // ------------------------------------------------ surrogate support --------
@@ -1438,7 +1477,7 @@ __global__ void k_decode_gate(int n, const float* out, const float* out2, int ld
   }
 }
 
-template <int KK, int MINB>
+template <int KK, int MINB, class Rhs>
 __global__ void __launch_bounds__(kChemThreads, MINB) k_psr_list(const int* list, const unsigned* count, double* T,
                                                                  const double* rho, double* Y, const double* dt,
                                                                  unsigned* counter, ChemStats* stats) {
@@ -1458,36 +1497,50 @@ __global__ void __launch_bounds__(kChemThreads, MINB) k_psr_list(const int* list
 #pragma unroll
     for (int l = 0; l < KK; ++l) Y[(size_t)q * KK + l] = r.y[1 + l];
   };
-  rc_drive<KK>(*count, counter, load, store);
+  rc_drive<KK, Rhs>(*count, counter, load, store);
 }
 
-struct ChemVariant {
-  int min_blocks;
-  void (*field)(ChemField, unsigned*, ChemStats*);
-  void (*batch)(int, double*, const double*, double*, const double*, int*, int*, unsigned*, ChemStats*);
-  void (*list)(const int*, const unsigned*, double*, const double*, double*, const double*, unsigned*, ChemStats*);
-};
-
-template <int MINB>
-constexpr ChemVariant chem_variant_of() {
-  return ChemVariant{MINB, k_psr_field<9, MINB>, k_psr_batch<9, MINB>, k_psr_list<9, MINB>};
+// The three persistent kernels of one register-budget variant with one
+// right-hand-side form.
+template <int MINB, class Rhs>
+constexpr ChemKernelSet chem_set_of() {
+  return ChemKernelSet{k_psr_field<9, MINB, Rhs>, k_psr_batch<9, MINB, Rhs>, k_psr_list<9, MINB, Rhs>};
 }
 
-const ChemVariant kChemVariants[IZEM_CHEM_VARIANTS] = {chem_variant_of<8>(), chem_variant_of<7>(),
-                                                       chem_variant_of<6>(), chem_variant_of<5>(),
-                                                       chem_variant_of<4>()};
+}  // namespace
+
+#ifndef IZEM_CHEM_HOST_TEST
+#if IZEM_CHEM_UNIT == 1
+// This unit (chem_generated.cu): the kernels with the generated right-hand side.
+extern const ChemKernelSet kChemGenSets[IZEM_CHEM_VARIANTS] = {
+    chem_set_of<8, RhsGenerated>(), chem_set_of<7, RhsGenerated>(), chem_set_of<6, RhsGenerated>(),
+    chem_set_of<5, RhsGenerated>(), chem_set_of<4, RhsGenerated>()};
+#else
+extern const ChemKernelSet kChemGenSets[IZEM_CHEM_VARIANTS];
+
+namespace {
+
+constexpr int kChemMinBlocks[IZEM_CHEM_VARIANTS] = {8, 7, 6, 5, 4};
+const ChemKernelSet kChemTabSets[IZEM_CHEM_VARIANTS] = {
+    chem_set_of<8, RhsTables<9>>(), chem_set_of<7, RhsTables<9>>(), chem_set_of<6, RhsTables<9>>(),
+    chem_set_of<5, RhsTables<9>>(), chem_set_of<4, RhsTables<9>>()};
 
 // Variant of the persistent chemistry kernels in use: 7 blocks of 128
 // threads per SM until an autotuning pass (izem_gpu_autotune) times the
 // variants on the caller's reactors and keeps the fastest (the same for every
 // context of the process).
 int g_chem_variant = 1;
+// 1 when the uploaded mechanism is the one chem_gen.cuh was generated from
+int g_chem_gen = 0;
+bool g_chem_gen_allowed = true;
+
+const ChemKernelSet& chem_kernels(int v) { return g_chem_gen ? kChemGenSets[v] : kChemTabSets[v]; }
 
 int chem_grid(int* blocks) {
   int dev = 0, sms = 0, per = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return -1;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return -1;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kChemVariants[g_chem_variant].batch, kChemThreads, 0) !=
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, chem_kernels(g_chem_variant).batch, kChemThreads, 0) !=
       cudaSuccess)
     return -1;
   *blocks = sms * (per > 0 ? per : 1);
@@ -1503,10 +1556,12 @@ int chem_set_variant(int v) {
   return 0;
 }
 int chem_variant() { return g_chem_variant; }
-int chem_variant_min_blocks(int v) { return (v >= 0 && v < IZEM_CHEM_VARIANTS) ? kChemVariants[v].min_blocks : 0; }
+int chem_generated_rhs() { return g_chem_gen; }
+void chem_allow_generated(bool allow) { g_chem_gen_allowed = allow; }
+int chem_variant_min_blocks(int v) { return (v >= 0 && v < IZEM_CHEM_VARIANTS) ? kChemMinBlocks[v] : 0; }
 int chem_variant_registers(int v) {
   cudaFuncAttributes a{};
-  if (v < 0 || v >= IZEM_CHEM_VARIANTS || cudaFuncGetAttributes(&a, kChemVariants[v].batch) != cudaSuccess) return 0;
+  if (v < 0 || v >= IZEM_CHEM_VARIANTS || cudaFuncGetAttributes(&a, chem_kernels(v).batch) != cudaSuccess) return 0;
   return a.numRegs;
 }
 
@@ -1517,6 +1572,7 @@ cudaError_t chem_upload_mech(const izem_mech* m) {
   if ((e = cudaMemcpyToSymbol(c_fast_dev, &f, sizeof(ChemFast))) != cudaSuccess) return e;
   int need = 0;
   for (int i = 0; i < m->ii; ++i) need |= (m->rev[i] == 1);
+  g_chem_gen = (g_chem_gen_allowed && chem_gen::matches(*m)) ? 1 : 0;
   return cudaMemcpyToSymbol(c_need_eqk_dev, &need, sizeof(int));
 }
 
@@ -1526,7 +1582,7 @@ cudaError_t chem_launch_field(const ChemField& f, unsigned* d_counter, ChemStats
   cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(unsigned), s);
   if (e != cudaSuccess) return e;
   if (kk != 9) return cudaErrorInvalidValue;
-  kChemVariants[g_chem_variant].field<<<blocks, kChemThreads, 0, s>>>(f, d_counter, d_stats);
+  chem_kernels(g_chem_variant).field<<<blocks, kChemThreads, 0, s>>>(f, d_counter, d_stats);
   return cudaGetLastError();
 }
 
@@ -1537,7 +1593,7 @@ cudaError_t chem_launch_batch(int n, double* T, const double* rho, double* Y, co
   cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(unsigned), s);
   if (e != cudaSuccess) return e;
   if (kk != 9) return cudaErrorInvalidValue;
-  kChemVariants[g_chem_variant].batch<<<blocks, kChemThreads, 0, s>>>(n, T, rho, Y, dt, istate, nsteps, d_counter,
+  chem_kernels(g_chem_variant).batch<<<blocks, kChemThreads, 0, s>>>(n, T, rho, Y, dt, istate, nsteps, d_counter,
                                                                       d_stats);
   return cudaGetLastError();
 }
@@ -1593,6 +1649,8 @@ cudaError_t chem_launch_list(const int* list, const unsigned* count, double* T, 
   if (chem_grid(&blocks)) return cudaErrorUnknown;
   cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(unsigned), s);
   if (e != cudaSuccess) return e;
-  kChemVariants[g_chem_variant].list<<<blocks, kChemThreads, 0, s>>>(list, count, T, rho, Y, dt, d_counter, d_stats);
+  chem_kernels(g_chem_variant).list<<<blocks, kChemThreads, 0, s>>>(list, count, T, rho, Y, dt, d_counter, d_stats);
   return cudaGetLastError();
 }
+#endif  // IZEM_CHEM_UNIT
+#endif  // IZEM_CHEM_HOST_TEST

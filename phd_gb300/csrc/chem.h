@@ -29,6 +29,11 @@ cudaError_t chem_upload_mech(const izem_mech* m);
 #define IZEM_CHEM_VARIANTS 5
 int chem_set_variant(int v);
 int chem_variant();
+// 1 when the kernels use the right-hand side generated for the uploaded
+// mechanism (chem_gen.cuh), 0 when they walk its tables
+int chem_generated_rhs();
+// false: walk the tables even for the shipped mechanism (from the next upload)
+void chem_allow_generated(bool allow);
 int chem_variant_min_blocks(int v);
 int chem_variant_registers(int v);
 cudaError_t chem_launch_field(const ChemField& f, unsigned* d_counter, ChemStats* d_stats, cudaStream_t s, int kk);

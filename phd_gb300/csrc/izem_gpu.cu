@@ -1237,6 +1237,13 @@ int izem_gpu_set_les(izem_ctx* c, int enable, double mu_sgs_factor, double sc_sg
 
 int izem_gpu_set_chem_variant(int variant) { return chem_set_variant(variant) == 0 ? IZEM_OK : IZEM_ERR_ARG; }
 
+int izem_gpu_chem_generated(void) { return chem_generated_rhs(); }
+
+int izem_gpu_allow_chem_generated(int allow) {
+  chem_allow_generated(allow != 0);
+  return IZEM_OK;
+}
+
 int izem_gpu_chem_autotune(const izem_mech* mech, int n, const double* T, const double* rho, const double* Y,
                            const double* dt, int device_ptrs, char* report, int report_len) {
   if (!mech || n <= 0 || !T || !rho || !Y || !dt || mech->kk != 9) return IZEM_ERR_ARG;

@@ -77,6 +77,8 @@ def load_library(path=None):
         "izem_gpu_set_eglib": (C.c_int, [P, C.POINTER(IzemEglib)]),
         "izem_gpu_autotune": (C.c_int, [P, C.c_double, C.c_char_p, C.c_int]),
         "izem_gpu_set_chem_variant": (C.c_int, [C.c_int]),
+        "izem_gpu_chem_generated": (C.c_int, []),
+        "izem_gpu_allow_chem_generated": (C.c_int, [C.c_int]),
         "izem_gpu_set_sensor_xblocks": (C.c_int, [P, C.c_int]),
         "izem_gpu_set_chem_skip": (C.c_int, [P, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_int]),
         "izem_gpu_set_les": (C.c_int, [P, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double]),

@@ -53,3 +53,18 @@ extern "C" void host_psr_fast(const izem_mech* m, int n, double* T, const double
     for (int k = 0; k < 9; ++k) Y[q * 9 + k] = r.y[1 + k];
   }
 }
+
+// The right-hand side generated for the shipped mechanism (chem_gen.cuh)
+// next to the generic device form (ck_fun_fast), both on the host.
+extern "C" void host_fun_gen_pair(const izem_mech* m, int n, const double* rho, const double* z, double* zp_tab,
+                                  double* zp_gen, int* matches) {
+  c_mech_host = *m;
+  c_fast_host = chem_fast_constants(*m);
+  *matches = chem_gen::matches(*m) ? 1 : 0;
+  for (int q = 0; q < n; ++q) {
+    ck_fun_fast<9>(rho[q], z + 10 * q, zp_tab + 10 * q);
+    chem_gen::FunT t;
+    chem_gen::tpart(z[10 * q], t);
+    chem_gen::cpart(rho[q], z + 10 * q, t, zp_gen + 10 * q);
+  }
+}

@@ -125,3 +125,31 @@ def test_dvodesimp_matches_oracle():
     g.close()
     assert np.sum(~(np.all(allc["v"][i] == st0["v"][i], axis=-1) & (allc["T"][i] == st0["T"][i]))) >= \
         np.sum(~same_o)
+
+
+def test_generated_and_table_forms_agree():
+    """The shipped mechanism runs on the right-hand side generated for it
+    (phd_gb300/mechgen.py); the table-walking form gives the same results
+    within the bounds above (the two compilations may fuse multiply-adds
+    differently; on the host they agree bit for bit), and takes over when
+    the generated form is not allowed."""
+    from phd_gb300.izem import load_library
+    lib = load_library()
+    m = h2_mechanism()
+    T, rho, Y, dt = ics.batched_reactors(2048, seed=21)
+    out = []
+    try:
+        for allow in (1, 0):
+            lib.izem_gpu_allow_chem_generated(allow)
+            Tg, Yg = T.copy(), Y.copy()
+            ist, ns, ms = psr_batch(m, Tg, rho.copy(), Yg, dt.copy())
+            assert lib.izem_gpu_chem_generated() == allow and np.all(ist == 2)
+            out.append((Tg, Yg))
+    finally:
+        lib.izem_gpu_allow_chem_generated(1)
+    st, msg, ok = W.reactor_error_bounds(out[0][0], out[0][1], out[1][0], out[1][1])
+    assert ok, msg
+    To, Yo = T.copy(), Y.copy()
+    oracle.psr_cells(m, To, rho.copy(), Yo, dt.copy())
+    st, msg, ok = W.reactor_error_bounds(out[0][0], out[0][1], To, Yo)
+    assert ok, msg
