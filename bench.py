@@ -127,14 +127,15 @@ def chem_window(cfg):
 
 # one window reactor: reads rho, rho*Y (9) and T, writes rho*Y (9) and T
 CHEM_BYTES_PER_REACTOR = 11 * 8 + 10 * 8
-# FP64 flops per BDF step of the persistent chemistry kernel (2 DFMA + DADD +
-# DMUL per thread, summed by ncu over one launch, / the BDF steps of that
-# launch, ncu capture of the 64x64x32 mixing-layer window)
-CHEM_FLOP_PER_BDF_STEP = 9793
+# FP64 flops per BDF step of the persistent chemistry kernel with the
+# generated right-hand side (2 DFMA + DADD + DMUL per thread, summed by ncu
+# over one launch on the 64x64x32 mixing-layer window, 81,225 reactors and
+# 243,675 BDF steps, / those steps)
+CHEM_FLOP_PER_BDF_STEP = 6712
 # DRAM bytes (read + write) per reactor of that launch, scaled by reactors to
 # other windows: the per-thread BDF state in local memory that the L2 does
 # not hold
-CHEM_TRAFFIC_PER_REACTOR = 16115
+CHEM_TRAFFIC_PER_REACTOR = 11071
 
 # FP64 flops per face of k_euler_face (2 DFMA + DADD + DMUL per thread, summed
 # by ncu over one launch of the 9-species mixing layer, / faces)
@@ -205,7 +206,10 @@ def run_gpu(args, rank, world):
     for _ in range(args.warmup):
         stp.step()
     _, dt_tune = g.timestep(DTmax=stp.DTmax, dtmin=stp.dtmin)
-    tuning = g.autotune(chem_dt=0.5 * dt_tune if chem else 0.0)
+    tuning = g.autotune(chem_dt=0.5 * dt_tune if chem and args.chem_variant is None else 0.0)
+    if chem and args.chem_variant is not None:
+        g.set_chem_variant(args.chem_variant)
+        tuning["chem_psr"] = {"chosen": "variant %d (pinned)" % args.chem_variant}
     stp.step()
     g.synchronize()
     g.newton_stats(reset=True)
@@ -650,6 +654,8 @@ def main():
                     help="mixing layer with the Smagorinsky closure (EGLIB) at this MU_SGS_FACTOR")
     ap.add_argument("--dvodesimp", action="store_true", help="mixing layer with the dvodesimp chemistry skip")
     ap.add_argument("--vis-dt", action="store_true", help="mixing layer with the Fourier time-step criteria")
+    ap.add_argument("--chem-variant", type=int, default=None,
+                    help="pin the register-budget variant of the chemistry kernels (0..4) instead of autotuning it")
     ap.add_argument("--transport", default="eglib", choices=["eglib", "fitted"],
                     help="viscous transport of the mixing layer (EGLIB precision 1 or the tranfit fits)")
     args = ap.parse_args()
