@@ -325,16 +325,16 @@ int  izem_mlp_fallback_cells(izem_mlp* m, int* out, int cap, int* count);
  * allocate device memory while they run -- a solver whose own arena (or a
  * framework's caching allocator) already holds the GPU's memory, or one that
  * calls the surrogate inside its time-step loop, where cudaMalloc/cudaFree
- * would synchronise the whole device.  It evaluates the same network as
- * izem_mlp_forward, with the warp-level BF16 GEMM kernels that training
- * uses instead of the tensor-core inference kernel, so the two agree to
- * BF16 rounding (within 1e-2 of the largest output), not bit for bit.
+ * would synchronise the whole device.  It runs the tensor-core inference
+ * kernel of izem_mlp_forward on the same BF16 inputs, so the two give the
+ * same outputs bit for bit.
  * d_x (M x 12) and d_y (M x 10) are FP32 device arrays, the work is queued
  * on `stream` (a cudaStream_t; NULL is the default stream) and the call
  * returns without waiting.  The device that was current when the handle
  * was created must be current for the call (its weights live there);
- * otherwise the call returns IZEM_ERR_ARG.  No memory is allocated or freed: the
- * activations use one fixed device array of about 4.3 MiB per GPU, which
+ * otherwise the call returns IZEM_ERR_ARG.  No memory is allocated or freed:
+ * the kernel's BF16 inputs and FP32 outputs use one fixed device array of
+ * 384 KiB per GPU, which
  * every GPU that loads the library holds until the process exits, so M is
  * at most IZEM_MLP_NOALLOC_MAX_ROWS (larger M returns IZEM_ERR_TOO_LARGE;
  * split the batch).  The first call on a device looks up that array's

@@ -8,8 +8,10 @@
 // Inputs  : T [K], ln p [atm], ln(Y_k + 1e-10) (9 species), ln dt [s]
 // Outputs : dY_k (9 species), dT [K] over dt, in normalised units.
 //
-// GEMMs use mma.sync.m16n8k16 (BF16 x BF16 -> FP32) from shared-memory
-// tiles; epilogues fuse bias, GELU and its derivative.
+// Every GEMM runs on the 5th-generation tensor cores (tcgen05.mma, BF16 x
+// BF16 -> FP32 in tensor memory): inference in one fused persistent kernel
+// (mlp_tc.cuh), training in pipelined GEMM kernels whose epilogues fuse
+// bias, GELU and its derivative (mlp_train_tc.cuh).
 #include <cstdio>
 #include <cstring>
 #include <cmath>
@@ -25,15 +27,6 @@ namespace {
 constexpr int IN = 12, INP = 16, OUT = 10, OUTP = 16, H = 256, NL = 5;
 constexpr int LIN[NL] = {INP, H, H, H, H};
 constexpr int LOUT[NL] = {H, H, H, H, OUTP};
-
-// ---------------------------------------------------------------- GEMM ------
-// C[M,N] (+)= op(A)[M,K] * op(B)[K,N].  A is given row-major [M][K] (TA = 0)
-// or as [K][M] (TA = 1); B is given as [K][N] (TB = 0) or [N][K] (TB = 1).
-// Tiles are staged in shared memory K-contiguous for both operands, so the
-// mma fragments are plain 32-bit shared loads.
-constexpr int BM = 128, BN = 128, BK = 32;
-
-enum Epi { EPI_STORE_F32 = 0, EPI_BIAS_GELU = 1, EPI_BIAS = 2, EPI_GELU_BWD = 3 };
 
 // GELU in the tanh form of Hendrycks and Gimpel (2016),
 //   gelu(z) = 0.5 z (1 + tanh(u)),  u = sqrt(2/pi) (z + 0.044715 z^3),
@@ -60,166 +53,10 @@ __device__ __forceinline__ float gelu_grad(float z) {
   return fmaf(0.5f * z * du, fmaf(-t, t, 1.0f), 0.5f * (1.0f + t));
 }
 
-struct GemmArgs {
-  const __nv_bfloat16* A;
-  const __nv_bfloat16* B;
-  int M, N, K;
-  int lda, ldb;          // leading dimensions of the stored matrices
-  const float* bias;     // [N]
-  float* Cf;             // fp32 output (pre-activation or gradient), ld = ldc
-  __nv_bfloat16* Cb;     // bf16 output (activation), ld = ldc
-  const float* Zin;      // pre-activation for EPI_GELU_BWD, ld = ldc
-  int ldc;
-};
-
-template <int TA, int TB, int EPI>
-__global__ void __launch_bounds__(256) k_gemm(GemmArgs g) {
-  __shared__ __align__(16) __nv_bfloat16 As[BM][BK + 8];
-  __shared__ __align__(16) __nv_bfloat16 Bs[BN][BK + 8];
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int wm = warp >> 2, wn = warp & 3;   // 2 x 4 warps, warp tile 64 x 32
-  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
-  float acc[4][4][4];
-#pragma unroll
-  for (int a = 0; a < 4; ++a)
-#pragma unroll
-    for (int b = 0; b < 4; ++b)
-#pragma unroll
-      for (int c = 0; c < 4; ++c) acc[a][b][c] = 0.f;
-  const __nv_bfloat16 zero = __float2bfloat16(0.f);
-  for (int k0 = 0; k0 < g.K; k0 += BK) {
-    // stage A tile (BM x BK) and B tile (BN x BK), bounds-checked
-    for (int e = tid; e < BM * BK; e += 256) {
-      int mm, kk;
-      if (TA == 0) { mm = e / BK; kk = e % BK; } else { kk = e / BM; mm = e % BM; }
-      const int gm = m0 + mm, gk = k0 + kk;
-      __nv_bfloat16 val = zero;
-      if (gm < g.M && gk < g.K) val = TA == 0 ? g.A[(size_t)gm * g.lda + gk] : g.A[(size_t)gk * g.lda + gm];
-      As[mm][kk] = val;
-    }
-    for (int e = tid; e < BN * BK; e += 256) {
-      int nn, kk;
-      if (TB == 1) { nn = e / BK; kk = e % BK; } else { kk = e / BN; nn = e % BN; }
-      const int gn = n0 + nn, gk = k0 + kk;
-      __nv_bfloat16 val = zero;
-      if (gn < g.N && gk < g.K) val = TB == 1 ? g.B[(size_t)gn * g.ldb + gk] : g.B[(size_t)gk * g.ldb + gn];
-      Bs[nn][kk] = val;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int ks = 0; ks < BK; ks += 16) {
-      const int gid = lane >> 2, tig = lane & 3;
-      unsigned afr[4][4], bfr[4][2];
-#pragma unroll
-      for (int fm = 0; fm < 4; ++fm) {
-        const int r = wm * 64 + fm * 16 + gid;
-        const int c = ks + tig * 2;
-        afr[fm][0] = *reinterpret_cast<const unsigned*>(&As[r][c]);
-        afr[fm][1] = *reinterpret_cast<const unsigned*>(&As[r + 8][c]);
-        afr[fm][2] = *reinterpret_cast<const unsigned*>(&As[r][c + 8]);
-        afr[fm][3] = *reinterpret_cast<const unsigned*>(&As[r + 8][c + 8]);
-      }
-#pragma unroll
-      for (int fn = 0; fn < 4; ++fn) {
-        const int n = wn * 32 + fn * 8 + gid;
-        const int c = ks + tig * 2;
-        bfr[fn][0] = *reinterpret_cast<const unsigned*>(&Bs[n][c]);
-        bfr[fn][1] = *reinterpret_cast<const unsigned*>(&Bs[n][c + 8]);
-      }
-#pragma unroll
-      for (int fm = 0; fm < 4; ++fm)
-#pragma unroll
-        for (int fn = 0; fn < 4; ++fn) {
-          float* d = acc[fm][fn];
-          asm volatile(
-              "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-              "{%0,%1,%2,%3};\n"
-              : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-              : "r"(afr[fm][0]), "r"(afr[fm][1]), "r"(afr[fm][2]), "r"(afr[fm][3]), "r"(bfr[fn][0]), "r"(bfr[fn][1]));
-        }
-    }
-    __syncthreads();
-  }
-  // epilogue
-  const int gid = lane >> 2, tig = lane & 3;
-#pragma unroll
-  for (int fm = 0; fm < 4; ++fm)
-#pragma unroll
-    for (int fn = 0; fn < 4; ++fn)
-#pragma unroll
-      for (int h = 0; h < 4; ++h) {
-        const int r = m0 + wm * 64 + fm * 16 + gid + (h >= 2 ? 8 : 0);
-        const int cc = n0 + wn * 32 + fn * 8 + tig * 2 + (h & 1);
-        if (r >= g.M || cc >= g.N) continue;
-        float val = acc[fm][fn][h];
-        const size_t o = (size_t)r * g.ldc + cc;
-        if (EPI == EPI_STORE_F32) {
-          g.Cf[o] = val;
-        } else if (EPI == EPI_BIAS) {
-          g.Cf[o] = val + g.bias[cc];
-        } else if (EPI == EPI_BIAS_GELU) {
-          const float z = val + g.bias[cc];
-          if (g.Cf) g.Cf[o] = z;
-          g.Cb[o] = __float2bfloat16(gelu(z));
-        } else {   // EPI_GELU_BWD: dZ = dA * gelu'(Z), stored as bf16 and fp32
-          const float dz = val * gelu_grad(g.Zin[o]);
-          if (g.Cf) g.Cf[o] = dz;
-          g.Cb[o] = __float2bfloat16(dz);
-        }
-      }
-}
-
-template <int TA, int TB, int EPI>
-cudaError_t gemm(const GemmArgs& a, cudaStream_t s) {
-  dim3 grid((a.N + BN - 1) / BN, (a.M + BM - 1) / BM);
-  k_gemm<TA, TB, EPI><<<grid, 256, 0, s>>>(a);
-  return cudaGetLastError();
-}
-
 // ------------------------------------------------------- small kernels ------
 __global__ void k_f32_to_bf16(const float* x, __nv_bfloat16* y, long long n) {
   long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (i < n) y[i] = __float2bfloat16(x[i]);
-}
-
-// loss gradient for MSE on normalised outputs (first OUT columns)
-__global__ void k_mse_grad(const float* out, const float* tgt, int M, float* dout_f, __nv_bfloat16* dout_b,
-                           double* loss) {
-  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (i >= (long long)M * OUTP) return;
-  const int c = (int)(i % OUTP);
-  const long long r = i / OUTP;
-  float d = 0.f;
-  if (c < OUT) {
-    d = out[i] - tgt[r * OUT + c];
-    atomicAdd(loss, (double)(d * d));
-  }
-  const float gval = c < OUT ? 2.f * d / (float)(M * OUT) : 0.f;
-  dout_f[i] = gval;
-  dout_b[i] = __float2bfloat16(gval);
-}
-
-// column sums (bias gradient): db[n] = sum_m dZ[m][n]
-__global__ void k_colsum(const float* dz, int M, int N, float* db) {
-  const int n = blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= N) return;
-  float s = 0.f;
-  for (int m = 0; m < M; ++m) s += dz[(size_t)m * N + n];
-  db[n] = s;
-}
-
-__global__ void k_adam(float* w, const float* gw, float* mw, float* vw, long long n, float lr, float b1, float b2,
-                       float eps, float c1, float c2, __nv_bfloat16* wb) {
-  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const float gr = gw[i];
-  const float m = b1 * mw[i] + (1.f - b1) * gr;
-  const float v = b2 * vw[i] + (1.f - b2) * gr * gr;
-  mw[i] = m;
-  vw[i] = v;
-  const float wn = w[i] - lr * (m / c1) / (sqrtf(v / c2) + eps);
-  w[i] = wn;
-  if (wb) wb[i] = __float2bfloat16(wn);
 }
 
 unsigned g1(long long n) { return (unsigned)((n + 255) / 256); }
@@ -235,13 +72,20 @@ struct izem_mlp {
   float *mW[NL] = {}, *vW[NL] = {}, *mb[NL] = {}, *vb[NL] = {};
   float *gW[NL] = {}, *gb[NL] = {};
   float norm[2 * IN + 2 * OUT] = {};   // in_mean, in_std, out_mean, out_std
-  // work buffers for a batch of up to cap rows
+  // training buffers for batches of up to cap rows (a multiple of 128),
+  // operands in the K-slab layout of mlp_train_tc.cuh
   int cap = 0;
-  __nv_bfloat16* act[NL + 1] = {};   // act[0] = input (M x INP), act[l+1] = output of layer l
-  float* z[NL] = {};                 // pre-activations (FP32)
-  float* dzf = nullptr;              // FP32 gradient scratch (M x H)
-  __nv_bfloat16* dzb[2] = {};        // BF16 gradients (ping-pong)
-  float* out = nullptr;              // network output FP32 (M x OUTP)
+  uint8_t *xa = nullptr, *xt = nullptr;          // inputs: cap x 16; transposed 128 x cap
+  uint8_t *acta[NL - 1] = {}, *actt[NL - 1] = {};   // hidden activations: cap x 256; 256 x cap
+  float* z[NL - 1] = {};                         // hidden pre-activations (FP32, cap x 256)
+  float* out = nullptr;                          // network output (FP32, cap x 16)
+  float* gout = nullptr;                         // output gradient (FP32, cap x 16) ...
+  uint8_t *goa = nullptr, *got = nullptr;        // ... as K-slabs: cap x 16; 16 x cap
+  float* dzf = nullptr;                          // hidden gradient (FP32, cap x 256) ...
+  uint8_t *dza[2] = {}, *dzt = nullptr;          // ... as K-slabs: cap x 256 (two); 256 x cap
+  float* part = nullptr;                         // split-K partial weight gradients
+  int splits = 0, split_chunks = 0;              // K split of the weight-gradient GEMMs
+  uint8_t *wt[NL] = {}, *wn[NL] = {};            // BF16 weights as K-slabs: W^T (forward), W (backward)
   double* d_loss = nullptr;
   int step = 0;
   int device = 0;                    // device current at izem_mlp_create; holds every buffer
@@ -266,79 +110,164 @@ struct izem_mlp {
 };
 
 #include "mlp_tc.cuh"
+#include "mlp_train_tc.cuh"
 
 namespace {
 
+// Training buffers for batches of up to `rows` rows (rounded up to 128).
 cudaError_t mlp_ensure(izem_mlp* m, int rows) {
+  rows = (rows + 127) / 128 * 128;
   if (rows <= m->cap) return cudaSuccess;
-  for (int l = 0; l <= NL; ++l) if (m->act[l]) cudaFree(m->act[l]);
-  for (int l = 0; l < NL; ++l) if (m->z[l]) cudaFree(m->z[l]);
-  if (m->dzf) cudaFree(m->dzf);
-  for (int q = 0; q < 2; ++q) if (m->dzb[q]) cudaFree(m->dzb[q]);
-  if (m->out) cudaFree(m->out);
-  cudaError_t e;
+  cudaFree(m->xa); cudaFree(m->xt); cudaFree(m->out); cudaFree(m->gout); cudaFree(m->goa); cudaFree(m->got);
+  cudaFree(m->dzf); cudaFree(m->dza[0]); cudaFree(m->dza[1]); cudaFree(m->dzt); cudaFree(m->part);
+  for (int l = 0; l < NL - 1; ++l) { cudaFree(m->acta[l]); cudaFree(m->actt[l]); cudaFree(m->z[l]); }
+  m->cap = 0;
   const size_t M = rows;
-  if ((e = cudaMalloc(&m->act[0], M * INP * sizeof(__nv_bfloat16)))) return e;
-  for (int l = 0; l < NL; ++l) {
-    if ((e = cudaMalloc(&m->act[l + 1], M * LOUT[l] * sizeof(__nv_bfloat16)))) return e;
-    if ((e = cudaMalloc(&m->z[l], M * LOUT[l] * sizeof(float)))) return e;
-  }
-  if ((e = cudaMalloc(&m->dzf, M * H * sizeof(float)))) return e;
-  for (int q = 0; q < 2; ++q)
-    if ((e = cudaMalloc(&m->dzb[q], M * H * sizeof(__nv_bfloat16)))) return e;
-  if ((e = cudaMalloc(&m->out, M * OUTP * sizeof(float)))) return e;
+  // the weight-gradient GEMMs split the batch (K = rows, chunks of 64) over
+  // up to 32 CTAs per output tile
+  const int nchunks = rows / mlptt::KCMAX;
+  m->split_chunks = nchunks / 32 > 1 ? nchunks / 32 : 1;
+  m->splits = (nchunks + m->split_chunks - 1) / m->split_chunks;
+  cudaError_t e;
+  if ((e = cudaMalloc(&m->xa, M * 16 * 2)) || (e = cudaMalloc(&m->xt, 128 * M * 2)) ||
+      (e = cudaMemset(m->xt, 0, 128 * M * 2)) || (e = cudaMalloc(&m->out, M * 16 * 4)) ||
+      (e = cudaMalloc(&m->gout, M * 16 * 4)) || (e = cudaMalloc(&m->goa, M * 16 * 2)) ||
+      (e = cudaMalloc(&m->got, M * 16 * 2)) || (e = cudaMalloc(&m->dzf, M * H * 4)) ||
+      (e = cudaMalloc(&m->dza[0], M * H * 2)) || (e = cudaMalloc(&m->dza[1], M * H * 2)) ||
+      (e = cudaMalloc(&m->dzt, M * H * 2)) || (e = cudaMalloc(&m->part, (size_t)m->splits * H * H * 4)))
+    return e;
+  for (int l = 0; l < NL - 1; ++l)
+    if ((e = cudaMalloc(&m->acta[l], M * H * 2)) || (e = cudaMalloc(&m->actt[l], M * H * 2)) ||
+        (e = cudaMalloc(&m->z[l], M * H * 4)))
+      return e;
   m->cap = rows;
   return cudaSuccess;
 }
 
-// forward pass for M rows whose normalised inputs (bf16, M x INP) are in
-// act[0]; the final layer writes FP32 outputs into m->out (and z[4]).
+template <int NT, int MODE>
+cudaError_t tg_launch(const mlptt::TgArgs& a, int mt, int nt, int splits, cudaStream_t s) {
+  static bool attr = false;
+  cudaError_t e;
+  if (!attr) {
+    if ((e = cudaFuncSetAttribute(mlptt::k_tgemm<NT, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)mlptt::tg_smem_bytes(NT))) != cudaSuccess)
+      return e;
+    attr = true;
+  }
+  mlptt::k_tgemm<NT, MODE><<<dim3(mt, nt, splits), mlptt::GT_THREADS, mlptt::tg_smem_bytes(NT), s>>>(a);
+  return cudaGetLastError();
+}
+
+// Forward pass of M rows (a multiple of 128) whose inputs are in m->xa:
+// hidden pre-activations and activations of every layer kept for the
+// backward pass, FP32 outputs in m->out.
 cudaError_t mlp_forward(izem_mlp* m, int M) {
   cudaError_t e;
   for (int l = 0; l < NL; ++l) {
-    GemmArgs a{};
-    a.A = m->act[l];
-    a.B = m->Wb[l];
-    a.M = M; a.N = LOUT[l]; a.K = LIN[l];
-    a.lda = LIN[l]; a.ldb = LOUT[l]; a.ldc = LOUT[l];
+    mlptt::TgArgs a{};
+    a.A = l == 0 ? m->xa : m->acta[l - 1];
+    a.RA = M;
+    a.B = m->wt[l];
+    a.RB = LOUT[l];
+    a.K = LIN[l];
+    a.chunks = LIN[l] / mlptt::kslab_kc(LIN[l]);
+    a.N = LOUT[l];
     a.bias = m->b[l];
+    a.err = m->d_err;
     if (l < NL - 1) {
-      a.Cf = m->z[l];
-      a.Cb = m->act[l + 1];
-      if ((e = gemm<0, 0, EPI_BIAS_GELU>(a, m->s))) return e;
+      a.outf = m->z[l];
+      a.oa = m->acta[l];
+      a.ot = m->actt[l];
+      a.oaR = M;
+      a.otK = M;
+      e = tg_launch<128, mlptt::TG_FWD_GELU>(a, M / 128, H / 128, 1, m->s);
     } else {
-      a.Cf = m->out;
-      if ((e = gemm<0, 0, EPI_BIAS>(a, m->s))) return e;
+      a.outf = m->out;
+      e = tg_launch<OUTP, mlptt::TG_FWD_OUT>(a, M / 128, 1, 1, m->s);
     }
+    if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
 }
 
-// backward pass from dL/dout (FP32 in m->dzf laid out M x OUTP, BF16 copy in
-// dzb[0]) to parameter gradients gW/gb.
+// Backward pass of M rows from the output gradient in m->gout / m->goa /
+// m->got to the parameter gradients gW, gb.
 cudaError_t mlp_backward(izem_mlp* m, int M) {
   cudaError_t e;
-  int cur = 0;
+  const uint8_t* gA = m->goa;   // this layer's output gradient as an A operand
+  int nxt = 0;
   for (int l = NL - 1; l >= 0; --l) {
-    // gW[l] = act[l]^T (LIN x M) * dZ (M x LOUT)
-    GemmArgs gw{};
-    gw.A = m->act[l]; gw.lda = LIN[l];
-    gw.B = m->dzb[cur]; gw.ldb = LOUT[l];
-    gw.M = LIN[l]; gw.N = LOUT[l]; gw.K = M;
-    gw.Cf = m->gW[l]; gw.ldc = LOUT[l];
-    if ((e = gemm<1, 0, EPI_STORE_F32>(gw, m->s))) return e;
-    k_colsum<<<(LOUT[l] + 127) / 128, 128, 0, m->s>>>(m->dzf, M, LOUT[l], m->gb[l]);
+    // gW_l = act_l^T dZ_l: K = the batch, split over CTAs, partials added in order
+    mlptt::TgArgs w{};
+    w.A = l == 0 ? m->xt : m->actt[l - 1];
+    w.RA = l == 0 ? 128 : H;
+    w.B = l == NL - 1 ? m->got : m->dzt;
+    w.RB = LOUT[l];
+    w.K = M;
+    w.chunks = m->split_chunks;
+    w.N = LOUT[l];
+    w.outf = m->part;
+    w.err = m->d_err;
+    const int splits = (M / mlptt::KCMAX + w.chunks - 1) / w.chunks;
+    if (l == NL - 1) e = tg_launch<OUTP, mlptt::TG_WGRAD>(w, w.RA / 128, 1, splits, m->s);
+    else e = tg_launch<H, mlptt::TG_WGRAD>(w, w.RA / 128, 1, splits, m->s);
+    if (e != cudaSuccess) return e;
+    const int nw = LIN[l] * LOUT[l];
+    mlptt::k_tg_reduce<<<(nw + 255) / 256, 256, 0, m->s>>>(m->part, splits, w.RA, LIN[l], LOUT[l], m->gW[l]);
+    mlptt::k_tg_colsum<<<LOUT[l], 256, 0, m->s>>>(l == NL - 1 ? m->gout : m->dzf, M, LOUT[l], m->gb[l]);
     if (l == 0) break;
-    // dA[l-1] = dZ (M x LOUT) * W^T (LOUT x LIN), then * gelu'(z[l-1])
-    GemmArgs gx{};
-    gx.A = m->dzb[cur]; gx.lda = LOUT[l];
-    gx.B = m->Wb[l]; gx.ldb = LOUT[l];   // W stored [LIN][LOUT] = [K... ]: as B^T we read [N=LIN][K=LOUT]
-    gx.M = M; gx.N = LIN[l]; gx.K = LOUT[l];
-    gx.Zin = m->z[l - 1];
-    gx.Cf = m->dzf; gx.Cb = m->dzb[1 - cur]; gx.ldc = LIN[l];
-    if ((e = gemm<0, 1, EPI_GELU_BWD>(gx, m->s))) return e;
-    cur = 1 - cur;
+    // dZ_{l-1} = (dZ_l W_l^T) gelu'(z_{l-1})
+    mlptt::TgArgs d{};
+    d.A = gA;
+    d.RA = M;
+    d.B = m->wn[l];
+    d.RB = LIN[l];
+    d.K = LOUT[l];
+    d.chunks = LOUT[l] / mlptt::kslab_kc(LOUT[l]);
+    d.N = H;
+    d.zin = m->z[l - 1];
+    d.outf = m->dzf;
+    d.oa = m->dza[nxt];
+    d.ot = m->dzt;
+    d.oaR = M;
+    d.otK = M;
+    d.err = m->d_err;
+    if ((e = tg_launch<128, mlptt::TG_BWD_GELU>(d, M / 128, H / 128, 1, m->s)) != cudaSuccess) return e;
+    gA = m->dza[nxt];
+    nxt ^= 1;
   }
+  return cudaGetLastError();
+}
+
+// Adam on one parameter array; for weights (lin x lout, wt != nullptr) it
+// also writes the BF16 copies the GEMMs read (row-major, W^T and W K-slabs).
+__global__ void k_adam(float* w, const float* gw, float* mw, float* vw, int n, float lr, float b1, float b2, float eps,
+                       float c1, float c2, int lout, int lin, __nv_bfloat16* wb, uint8_t* wt, uint8_t* wn) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float gr = gw[i];
+  const float m = b1 * mw[i] + (1.f - b1) * gr;
+  const float v = b2 * vw[i] + (1.f - b2) * gr * gr;
+  mw[i] = m;
+  vw[i] = v;
+  const float wv = w[i] - lr * (m / c1) / (sqrtf(v / c2) + eps);
+  w[i] = wv;
+  if (wt) {
+    const int r = i / lout, c = i % lout;
+    const __nv_bfloat16 b = __float2bfloat16(wv);
+    wb[i] = b;
+    *reinterpret_cast<__nv_bfloat16*>(wt + mlptt::kslab_off(c, r, lout, lin)) = b;
+    *reinterpret_cast<__nv_bfloat16*>(wn + mlptt::kslab_off(r, c, lin, lout)) = b;
+  }
+}
+
+// The BF16 copies of every weight array after W changed outside Adam.
+cudaError_t mlp_weight_copies(izem_mlp* m) {
+  for (int l = 0; l < NL; ++l) {
+    const int nw = LIN[l] * LOUT[l];
+    mlptt::k_tg_weights<<<(nw + 255) / 256, 256, 0, m->s>>>(m->W[l], LIN[l], LOUT[l], m->Wb[l], m->wt[l], m->wn[l]);
+  }
+  m->blob_dirty = true;
   return cudaGetLastError();
 }
 
@@ -417,7 +346,10 @@ int izem_mlp_create(izem_mlp** out) {
     }
   }
   ok = ok && cudaMalloc(&m->d_loss, sizeof(double)) == cudaSuccess;
-  for (int l = 0; l < NL && ok; ++l) ok = cudaMalloc(&m->blob[l], (size_t)LIN[l] * LOUT[l] * 2) == cudaSuccess;
+  for (int l = 0; l < NL && ok; ++l)
+    ok = cudaMalloc(&m->blob[l], (size_t)LIN[l] * LOUT[l] * 2) == cudaSuccess &&
+         cudaMalloc(&m->wt[l], (size_t)LIN[l] * LOUT[l] * 2) == cudaSuccess &&
+         cudaMalloc(&m->wn[l], (size_t)LIN[l] * LOUT[l] * 2) == cudaSuccess;
   ok = ok && cudaMalloc(&m->d_err, sizeof(int)) == cudaSuccess && cudaMemset(m->d_err, 0, sizeof(int)) == cudaSuccess;
   if (!ok) {
     izem_mlp_destroy(m);   // frees what was allocated (cudaFree of a null pointer is a no-op)
@@ -432,10 +364,13 @@ void izem_mlp_destroy(izem_mlp* m) {
   cudaStreamSynchronize(m->s);
   for (int l = 0; l < NL; ++l) {
     cudaFree(m->W[l]); cudaFree(m->b[l]); cudaFree(m->Wb[l]); cudaFree(m->mW[l]); cudaFree(m->vW[l]);
-    cudaFree(m->mb[l]); cudaFree(m->vb[l]); cudaFree(m->gW[l]); cudaFree(m->gb[l]); cudaFree(m->z[l]);
+    cudaFree(m->mb[l]); cudaFree(m->vb[l]); cudaFree(m->gW[l]); cudaFree(m->gb[l]);
+    cudaFree(m->wt[l]); cudaFree(m->wn[l]);
   }
-  for (int l = 0; l <= NL; ++l) cudaFree(m->act[l]);
-  cudaFree(m->dzf); cudaFree(m->dzb[0]); cudaFree(m->dzb[1]); cudaFree(m->out); cudaFree(m->d_loss);
+  for (int l = 0; l < NL - 1; ++l) { cudaFree(m->acta[l]); cudaFree(m->actt[l]); cudaFree(m->z[l]); }
+  cudaFree(m->xa); cudaFree(m->xt); cudaFree(m->out); cudaFree(m->gout); cudaFree(m->goa); cudaFree(m->got);
+  cudaFree(m->dzf); cudaFree(m->dza[0]); cudaFree(m->dza[1]); cudaFree(m->dzt); cudaFree(m->part);
+  cudaFree(m->d_loss);
   cudaFree(m->ib[0]); cudaFree(m->ib[1]); cudaFree(m->iout); cudaFree(m->d_norm);
   for (int l = 0; l < NL; ++l) cudaFree(m->blob[l]);
   cudaFree(m->d_err);
@@ -454,8 +389,8 @@ int izem_mlp_set_params(izem_mlp* m, const float* const* W, const float* const* 
     const size_t nw = (size_t)LIN[l] * LOUT[l];
     if (cudaMemcpy(m->W[l], W[l], nw * 4, cudaMemcpyHostToDevice) != cudaSuccess) return IZEM_ERR_CUDA;
     if (cudaMemcpy(m->b[l], b[l], LOUT[l] * 4, cudaMemcpyHostToDevice) != cudaSuccess) return IZEM_ERR_CUDA;
-    k_f32_to_bf16<<<g1(nw), 256, 0, m->s>>>(m->W[l], m->Wb[l], nw);
   }
+  if (mlp_weight_copies(m) != cudaSuccess) return IZEM_ERR_CUDA;
   return cudaStreamSynchronize(m->s) == cudaSuccess ? IZEM_OK : IZEM_ERR_CUDA;
 }
 
@@ -507,36 +442,38 @@ int izem_mlp_forward(izem_mlp* m, int M, const float* x, float* y) {
 // parameters.  Used to check the backward kernels against the FP64 oracle.
 int izem_mlp_grads(izem_mlp* m, int M, const float* x, const float* t, double* loss, float* const* gW,
                    float* const* gb) {
-  if (!m || M <= 0 || !x || !t) return IZEM_ERR_ARG;
+  if (!m || M <= 0 || !x || !t || !loss || !gW || !gb) return IZEM_ERR_ARG;
   if (mlp_ensure(m, M) != cudaSuccess) return IZEM_ERR_NOMEM;
-  std::vector<float> xp((size_t)M * INP, 0.f);
-  for (int r = 0; r < M; ++r)
-    for (int c = 0; c < IN; ++c) xp[(size_t)r * INP + c] = x[(size_t)r * IN + c];
+  const int Mp = (M + 127) / 128 * 128;
   float *dx = nullptr, *dt = nullptr;
-  if (cudaMalloc(&dx, xp.size() * 4) != cudaSuccess) return IZEM_ERR_NOMEM;
+  if (cudaMalloc(&dx, (size_t)M * IN * 4) != cudaSuccess) return IZEM_ERR_NOMEM;
   if (cudaMalloc(&dt, (size_t)M * OUT * 4) != cudaSuccess) {
     cudaFree(dx);
     return IZEM_ERR_NOMEM;
   }
-  if (cudaMemcpy(dx, xp.data(), xp.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
-      cudaMemcpy(dt, t, (size_t)M * OUT * 4, cudaMemcpyHostToDevice) != cudaSuccess) {
-    cudaFree(dx);
-    cudaFree(dt);
-    return IZEM_ERR_CUDA;
-  }
-  k_f32_to_bf16<<<g1(xp.size()), 256, 0, m->s>>>(dx, m->act[0], (long long)xp.size());
   int rc = IZEM_OK;
-  if (mlp_forward(m, M) != cudaSuccess) rc = IZEM_ERR_CUDA;
-  cudaMemsetAsync(m->d_loss, 0, sizeof(double), m->s);
-  k_mse_grad<<<g1((long long)M * OUTP), 256, 0, m->s>>>(m->out, dt, M, m->dzf, m->dzb[0], m->d_loss);
-  if (rc == IZEM_OK && mlp_backward(m, M) != cudaSuccess) rc = IZEM_ERR_CUDA;
-  cudaMemcpyAsync(loss, m->d_loss, sizeof(double), cudaMemcpyDeviceToHost, m->s);
-  for (int l = 0; l < NL; ++l) {
-    cudaMemcpyAsync(gW[l], m->gW[l], (size_t)LIN[l] * LOUT[l] * 4, cudaMemcpyDeviceToHost, m->s);
-    cudaMemcpyAsync(gb[l], m->gb[l], LOUT[l] * 4, cudaMemcpyDeviceToHost, m->s);
+  if (cudaMemcpy(dx, x, (size_t)M * IN * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(dt, t, (size_t)M * OUT * 4, cudaMemcpyHostToDevice) != cudaSuccess)
+    rc = IZEM_ERR_CUDA;
+  if (rc == IZEM_OK) {
+    mlptt::k_tg_pack_input<<<(Mp * 16 + 255) / 256, 256, 0, m->s>>>(dx, Mp, M, m->xa, m->xt);
+    if (cudaGetLastError() != cudaSuccess || mlp_forward(m, Mp) != cudaSuccess) rc = IZEM_ERR_CUDA;
+  }
+  if (rc == IZEM_OK) {
+    cudaMemsetAsync(m->d_loss, 0, sizeof(double), m->s);
+    mlptt::k_tg_mse<<<(Mp * 16 + 255) / 256, 256, 0, m->s>>>(m->out, dt, Mp, M, m->gout, m->goa, m->got, m->d_loss);
+    if (cudaGetLastError() != cudaSuccess || mlp_backward(m, Mp) != cudaSuccess) rc = IZEM_ERR_CUDA;
+  }
+  if (rc == IZEM_OK) {
+    if (cudaMemcpyAsync(loss, m->d_loss, sizeof(double), cudaMemcpyDeviceToHost, m->s) != cudaSuccess) rc = IZEM_ERR_CUDA;
+    for (int l = 0; l < NL && rc == IZEM_OK; ++l)
+      if (cudaMemcpyAsync(gW[l], m->gW[l], (size_t)LIN[l] * LOUT[l] * 4, cudaMemcpyDeviceToHost, m->s) != cudaSuccess ||
+          cudaMemcpyAsync(gb[l], m->gb[l], LOUT[l] * 4, cudaMemcpyDeviceToHost, m->s) != cudaSuccess)
+        rc = IZEM_ERR_CUDA;
   }
   if (cudaStreamSynchronize(m->s) != cudaSuccess) rc = IZEM_ERR_CUDA;
-  *loss = *loss / ((double)M * OUT);
+  if (rc == IZEM_OK) rc = mlp_tc_status(m);
+  if (rc == IZEM_OK) *loss = *loss / ((double)M * OUT);
   cudaFree(dx);
   cudaFree(dt);
   return rc;
@@ -550,22 +487,26 @@ int izem_mlp_train(izem_mlp* m, long long n, const float* x, const float* t, int
                    float lr, unsigned seed, double* losses) {
   if (!m || n < batch || !x || !t || epochs <= 0 || batch <= 0) return IZEM_ERR_ARG;
   if (mlp_ensure(m, batch) != cudaSuccess) return IZEM_ERR_NOMEM;
-  float *dx = nullptr, *dt = nullptr, *bx = nullptr, *bt = nullptr;
+  const int Mp = (batch + 127) / 128 * 128;
+  float *dx = nullptr, *dt = nullptr;
   int rc = IZEM_OK;
   if (device_ptrs) {
     dx = const_cast<float*>(x);
     dt = const_cast<float*>(t);
   } else {
-    if (cudaMalloc(&dx, n * IN * 4) || cudaMalloc(&dt, n * OUT * 4)) return IZEM_ERR_NOMEM;
-    cudaMemcpy(dx, x, n * IN * 4, cudaMemcpyHostToDevice);
-    cudaMemcpy(dt, t, n * OUT * 4, cudaMemcpyHostToDevice);
+    if (cudaMalloc(&dx, (size_t)n * IN * 4) != cudaSuccess) return IZEM_ERR_NOMEM;
+    if (cudaMalloc(&dt, (size_t)n * OUT * 4) != cudaSuccess) {
+      cudaFree(dx);
+      return IZEM_ERR_NOMEM;
+    }
+    if (cudaMemcpy(dx, x, (size_t)n * IN * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(dt, t, (size_t)n * OUT * 4, cudaMemcpyHostToDevice) != cudaSuccess)
+      rc = IZEM_ERR_CUDA;
   }
-  if (cudaMalloc(&bx, (size_t)batch * INP * 4) || cudaMalloc(&bt, (size_t)batch * OUT * 4)) return IZEM_ERR_NOMEM;
-  cudaMemset(bx, 0, (size_t)batch * INP * 4);
   const long long nb = n / batch;
   std::vector<long long> perm(nb);
   unsigned long long st = seed ? seed : 1ULL;
-  for (int ep = 0; ep < epochs; ++ep) {
+  for (int ep = 0; ep < epochs && rc == IZEM_OK; ++ep) {
     for (long long q = 0; q < nb; ++q) perm[q] = q;
     for (long long q = nb - 1; q > 0; --q) {   // Fisher-Yates on batch indices (xorshift)
       st ^= st << 13; st ^= st >> 7; st ^= st << 17;
@@ -575,31 +516,31 @@ int izem_mlp_train(izem_mlp* m, long long n, const float* x, const float* t, int
     cudaMemsetAsync(m->d_loss, 0, sizeof(double), m->s);
     for (long long q = 0; q < nb; ++q) {
       const long long r0 = perm[q] * batch;
-      cudaMemcpy2DAsync(bx, INP * 4, dx + r0 * IN, IN * 4, IN * 4, batch, cudaMemcpyDeviceToDevice, m->s);
-      cudaMemcpyAsync(bt, dt + r0 * OUT, (size_t)batch * OUT * 4, cudaMemcpyDeviceToDevice, m->s);
-      k_f32_to_bf16<<<g1((long long)batch * INP), 256, 0, m->s>>>(bx, m->act[0], (long long)batch * INP);
-      if (mlp_forward(m, batch) != cudaSuccess) { rc = IZEM_ERR_CUDA; break; }
-      k_mse_grad<<<g1((long long)batch * OUTP), 256, 0, m->s>>>(m->out, bt, batch, m->dzf, m->dzb[0], m->d_loss);
-      if (mlp_backward(m, batch) != cudaSuccess) { rc = IZEM_ERR_CUDA; break; }
+      mlptt::k_tg_pack_input<<<(Mp * 16 + 255) / 256, 256, 0, m->s>>>(dx + r0 * IN, Mp, batch, m->xa, m->xt);
+      if (mlp_forward(m, Mp) != cudaSuccess) { rc = IZEM_ERR_CUDA; break; }
+      mlptt::k_tg_mse<<<(Mp * 16 + 255) / 256, 256, 0, m->s>>>(m->out, dt + r0 * OUT, Mp, batch, m->gout, m->goa,
+                                                                 m->got, m->d_loss);
+      if (mlp_backward(m, Mp) != cudaSuccess) { rc = IZEM_ERR_CUDA; break; }
       m->step += 1;
-      m->blob_dirty = true;
       const float b1 = 0.9f, b2 = 0.999f;
       const float c1 = 1.f - powf(b1, (float)m->step), c2 = 1.f - powf(b2, (float)m->step);
       for (int l = 0; l < NL; ++l) {
-        const long long nw = (long long)LIN[l] * LOUT[l];
-        k_adam<<<g1(nw), 256, 0, m->s>>>(m->W[l], m->gW[l], m->mW[l], m->vW[l], nw, lr, b1, b2, 1e-8f, c1, c2, m->Wb[l]);
-        k_adam<<<g1(LOUT[l]), 256, 0, m->s>>>(m->b[l], m->gb[l], m->mb[l], m->vb[l], LOUT[l], lr, b1, b2, 1e-8f, c1, c2,
-                                             nullptr);
+        const int nw = LIN[l] * LOUT[l];
+        k_adam<<<(nw + 255) / 256, 256, 0, m->s>>>(m->W[l], m->gW[l], m->mW[l], m->vW[l], nw, lr, b1, b2, 1e-8f, c1, c2,
+                                                   LOUT[l], LIN[l], m->Wb[l], m->wt[l], m->wn[l]);
+        k_adam<<<(LOUT[l] + 255) / 256, 256, 0, m->s>>>(m->b[l], m->gb[l], m->mb[l], m->vb[l], LOUT[l], lr, b1, b2,
+                                                        1e-8f, c1, c2, 0, 0, nullptr, nullptr, nullptr);
       }
+      m->blob_dirty = true;
     }
+    if (rc != IZEM_OK) break;
     double lsum = 0.0;
     cudaMemcpyAsync(&lsum, m->d_loss, sizeof(double), cudaMemcpyDeviceToHost, m->s);
     if (cudaStreamSynchronize(m->s) != cudaSuccess) { rc = IZEM_ERR_CUDA; break; }
+    if (mlp_tc_status(m) != IZEM_OK) { rc = IZEM_ERR_TIMEOUT; break; }
     if (losses) losses[ep] = lsum / ((double)nb * batch * OUT);
-    if (rc) break;
   }
-  cudaFree(bx);
-  cudaFree(bt);
+  if (cudaStreamSynchronize(m->s) != cudaSuccess && rc == IZEM_OK) rc = IZEM_ERR_CUDA;
   if (!device_ptrs) { cudaFree(dx); cudaFree(dt); }
   return rc;
 }
@@ -743,9 +684,9 @@ int izem_mlp_fallback_cells(izem_mlp* m, int* out, int cap, int* count) {
 namespace {
 
 constexpr int NA_ROWS = IZEM_MLP_NOALLOC_MAX_ROWS;
-constexpr size_t NA_ACT_BYTES = (size_t)NA_ROWS * H * sizeof(__nv_bfloat16);   // one activation buffer
-constexpr size_t NA_OUT_BYTES = (size_t)NA_ROWS * OUTP * sizeof(float);
-constexpr size_t NA_BYTES = 2 * NA_ACT_BYTES + NA_OUT_BYTES;                    // 4 MiB + 256 KiB
+constexpr size_t NA_IN_BYTES = (size_t)NA_ROWS * INP * sizeof(__nv_bfloat16);   // BF16 input rows
+constexpr size_t NA_OUT_BYTES = (size_t)NA_ROWS * OUTP * sizeof(float);         // FP32 output rows
+constexpr size_t NA_BYTES = NA_IN_BYTES + NA_OUT_BYTES;                          // 384 KiB
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NA_BYTES];
 
@@ -802,30 +743,13 @@ extern "C" int izem_mlp_forward_noalloc(izem_mlp* m, int M, const float* d_x, fl
   unsigned char* base = nullptr;
   if (noalloc_scratch(&base) != cudaSuccess) return IZEM_ERR_CUDA;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  __nv_bfloat16* buf[2] = {reinterpret_cast<__nv_bfloat16*>(base),
-                           reinterpret_cast<__nv_bfloat16*>(base + NA_ACT_BYTES)};
-  float* out = reinterpret_cast<float*>(base + 2 * NA_ACT_BYTES);
-  k_na_pack<<<g1((long long)M * INP), 256, 0, s>>>(d_x, M, buf[0]);
+  __nv_bfloat16* in = reinterpret_cast<__nv_bfloat16*>(base);
+  float* out = reinterpret_cast<float*>(base + NA_IN_BYTES);
+  k_na_pack<<<g1((long long)M * INP), 256, 0, s>>>(d_x, M, in);
   if (cudaGetLastError() != cudaSuccess) return IZEM_ERR_CUDA;
-  int cur = 0;
-  for (int l = 0; l < NL; ++l) {
-    GemmArgs a{};
-    a.A = buf[cur];
-    a.B = m->Wb[l];
-    a.M = M; a.N = LOUT[l]; a.K = LIN[l];
-    a.lda = LIN[l]; a.ldb = LOUT[l]; a.ldc = LOUT[l];
-    a.bias = m->b[l];
-    cudaError_t e;
-    if (l < NL - 1) {
-      a.Cb = buf[1 - cur];
-      e = gemm<0, 0, EPI_BIAS_GELU>(a, s);
-      cur = 1 - cur;
-    } else {
-      a.Cf = out;
-      e = gemm<0, 0, EPI_BIAS>(a, s);
-    }
-    if (e != cudaSuccess) return IZEM_ERR_CUDA;
-  }
+  // the tensor-core inference kernel of izem_mlp_forward; its weight
+  // operands and timeout flag live in the handle (allocated at creation)
+  if (mlp_infer_tc(m, M, in, out, s) != cudaSuccess) return IZEM_ERR_CUDA;
   k_na_unpack<<<g1((long long)M * OUT), 256, 0, s>>>(out, M, d_y);
   return cudaGetLastError() == cudaSuccess ? IZEM_OK : IZEM_ERR_CUDA;
 }
