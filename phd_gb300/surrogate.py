@@ -335,21 +335,42 @@ def window_reactors(g, dt):
             np.full(n, dt * adi.time_ref))
 
 
-def flow_training_set(g, mech, dt, n_max=1 << 20, spread=0.5, seed=5):
-    """Samples drawn from a flow block as the surrogate will meet them: its
-    window reactors with the half step scaled by 10**U[-spread, spread],
-    labelled by the FP64 BDF integrator.  Returns raw features and targets."""
+def flow_reactors(g, mech, dt, n_max=1 << 20, spread=0.5, seed=5, age=0.0):
+    """Reactors drawn from a flow block as the surrogate will meet them: its
+    window reactors with the half step scaled by 10**U[-spread, spread].
+    With age > 0, three quarters of them are first advanced by the FP64 BDF
+    integrator over U[0, age] half steps, so that the set also holds the
+    compositions the window reaches in later steps (the radical pool grows
+    during the induction).  Returns T [K], rho [g/cm^3], Y (n, 9), dt [s]."""
     T, rho, Y, dtp = window_reactors(g, dt)
     rng = np.random.Generator(np.random.PCG64(seed))
     idx = rng.choice(len(T), size=min(n_max, len(T)), replace=False) if len(T) > n_max else np.arange(len(T))
     T, rho, Y, dtp = T[idx].copy(), rho[idx].copy(), np.ascontiguousarray(Y[idx]), dtp[idx].copy()
+    if age > 0.0:
+        a = rng.uniform(0.0, age, len(T))
+        old = np.flatnonzero(rng.uniform(size=len(T)) >= 0.25)
+        if len(old):
+            Ta, Ya = T[old].copy(), np.ascontiguousarray(Y[old])
+            psr_batch(mech, Ta, rho[old].copy(), Ya, dtp[old] * a[old])
+            T[old], Y[old] = Ta, Ya
     dtp = dtp * 10.0 ** rng.uniform(-spread, spread, len(T))
+    return T, rho, Y, dtp
+
+
+def label(mech, T, rho, Y, dt):
+    """FP64 BDF labels of reactors: raw features and targets (dY_k, dT)."""
     wt = np.array([mech.wt[k] for k in range(mech.kk)])
-    X = features(T, rho, Y, dtp, wt)
+    X = features(T, rho, Y, dt, wt)
     T1, Y1 = T.copy(), Y.copy()
-    psr_batch(mech, T1, rho.copy(), Y1, dtp.copy())
+    psr_batch(mech, T1, rho.copy(), Y1, dt.copy())
     Yt = np.concatenate([Y1 - Y, (T1 - T)[:, None]], axis=1)
     return X, Yt
+
+
+def flow_training_set(g, mech, dt, n_max=1 << 20, spread=0.5, seed=5, age=0.0):
+    """flow_reactors labelled by the FP64 BDF integrator: raw features and
+    targets."""
+    return label(mech, *flow_reactors(g, mech, dt, n_max=n_max, spread=spread, seed=seed, age=age))
 
 
 def train_on(X, Yt, members=2, seed=31, epochs=24, batch=4096, lr=1e-3):
@@ -369,9 +390,42 @@ def train_on(X, Yt, members=2, seed=31, epochs=24, batch=4096, lr=1e-3):
 def flow_gate(X, Yt, dT_tol_frac=0.002):
     """Gate for a flow-trained surrogate: the envelope of its training
     temperatures and steps, element tolerance 2e-3, and temperature
-    tolerances scaled to the largest trained increment."""
+    tolerances scaled by f = dT_tol_frac: energy consistency within
+    f x (largest trained increment) + 5 f |dT|, agreement of the two
+    networks within f/2 x that increment + 2.5 f |dT|."""
     scale = float(np.abs(Yt[:, -1]).max())
     dt = np.exp(X[:, 11])
-    a = dT_tol_frac * scale
-    return (float(X[:, 0].min()), float(X[:, 0].max()), float(dt.min()), float(dt.max()), 2e-3, a, 0.02, 0.5 * a, 0.005,
-            float("inf"))
+    f = dT_tol_frac
+    a = f * scale
+    return (float(X[:, 0].min()), float(X[:, 0].max()), float(dt.min()), float(dt.max()), 2e-3, a, 5.0 * f, 0.5 * a,
+            2.5 * f, float("inf"))
+
+
+FLOW_TOL_LADDER = (0.00025, 0.0005, 0.001, 0.002, 0.004, 0.008)
+
+
+def calibrate_flow_gate(nets, mech, X, Yt, held, target=0.005, ladder=FLOW_TOL_LADDER):
+    """Choose the flow gate's tolerance scale on held-out reactors (another
+    draw from the same block, labelled by BDF): the largest f of `ladder`
+    for which every accepted held-out cell's |dT| error is within
+    target x the largest held-out |dT|.  held: (T, rho, Y, dt) raw
+    reactors.  Returns (gate, table)."""
+    T, rho, Y, dt = held
+    Tb, Yb = T.copy(), Y.copy()
+    psr_batch(mech, Tb, rho.copy(), Yb, dt.copy())
+    ref = Tb - T
+    scale = float(np.abs(ref).max())
+    table, best = [], None
+    for f in ladder:
+        gate = flow_gate(X, Yt, f)
+        Ts, Ys = T.copy(), Y.copy()
+        r = nets[0].chem_step(mech, Ts, rho.copy(), Ys, dt.copy(), gate, partner=nets[1] if len(nets) > 1 else None)
+        err = float(np.abs((Ts - T) - ref).max())
+        table.append({"f": f, "max_err_frac": err / scale if scale > 0 else None,
+                      "fallback_frac": r["fallback"] / len(T)})
+        if err <= target * scale:
+            best = f
+        else:
+            break
+    return flow_gate(X, Yt, best if best is not None else ladder[0]), {"cells": len(T), "scale_K": scale,
+                                                                        "target_frac": target, "table": table}
