@@ -391,9 +391,12 @@ int  izem_gpu_allow_chem_generated(int allow);
  * exchanges the shock sensor, so each block tests only its own points
  * (module_tools.f90:2761-2770) and picks nonlinear weights from its own
  * flags (module_weno.f90:973), and the face on a block edge is computed
- * twice, once as each neighbouring block sees it.  nblk = 1 (the default)
- * is one block.  No counterpart as an entry point in the reference;
- * IZEM_ERR_ARG unless nblk divides nx into blocks of at least ng points. */
+ * twice, once as each neighbouring block sees it.  Each rank also runs the
+ * Newton loop of prim_inv_var (module_thermodynamics.f90:79-186) and its
+ * stopping test on its own points: the interior and the y / z ghost slabs
+ * stop per x-block.  nblk = 1 (the default) is one block.  No counterpart
+ * as an entry point in the reference; IZEM_ERR_ARG unless nblk (at most 8)
+ * divides nx into blocks of at least ng points. */
 int  izem_gpu_set_sensor_xblocks(izem_ctx* ctx, int nblk);
 /* The same choice for independent reactors (no counterpart in the
  * reference): times the five variants on the first min(n, 2^20) reactors of

@@ -32,6 +32,7 @@ def load():
         "or_create": (P, [C.POINTER(IzemCfg), C.POINTER(IzemThd), C.POINTER(IzemAdi), _dp, _dp, _dp]),
         "or_destroy": (None, [P]),
         "or_set_sensor_xblocks": (C.c_int, [P, C.c_int]),
+        "or_set_newton_xblocks": (C.c_int, [P, C.c_int]),
         "or_set_chem_skip": (C.c_int, [P, C.c_int, _dp, _dp, C.c_int, C.c_int]),
         "or_set_les": (C.c_int, [P, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double]),
         "or_last_error": (C.c_int, [P, C.c_char_p, C.c_int]),
@@ -160,6 +161,11 @@ class Oracle:
     def set_eglib(self, link):
         self._eglib = link
         self._rc(self.lib.or_set_eglib(self.h, C.byref(link)), "set_eglib")
+
+    def set_newton_xblocks(self, nblk):
+        """Test-only: each of nblk x-blocks runs its own Newton loop and
+        stopping test (prim_inv_var per rank of an x-decomposition)."""
+        self._rc(self.lib.or_set_newton_xblocks(self.h, int(nblk)), "set_newton_xblocks")
 
     def set_sensor_xblocks(self, nblk):
         """Emulate a run whose x direction was split into nblk MPI blocks:

@@ -65,6 +65,7 @@ struct Ctx {
   int newton_warn = 0;
   int newton_it_max = 0;   // most iterations of any prim_inv_var call (test readout)
   int sensor_xblocks = 1;   // x-blocks of the reference's MPI run whose edges the sensor does not cross
+  int newton_xblocks = 1;   // x-blocks whose Newton loops stop on their own test
   // dvodesimp (module_reaction.f90:173-251): pure fuel Y1f and oxidiser Y0o,
   // H2 and N2 species indices (0-based)
   // LES with the Smagorinsky closure under EGLIB (or_set_les): MU_SGS_FACTOR,
@@ -238,13 +239,11 @@ double newton_cell(const izem_thd& t, const Block& b, const double* v, size_t p,
 // prim_inv_var (module_thermodynamics.f90:79-186) / prim_inv_var_err_mach
 // (:201-260) on one sub-domain: a global Newton loop whose stopping test is
 // the maximum temperature correction over the whole sub-domain.
-int prim_inv_var(Ctx& c, int dom, bool err_mach, double* v, double* W_i, double* T, double* cp, double* ha) {
+int prim_inv_var_region(Ctx& c, bool err_mach, int i0, int i1, int j0, int j1, int k0, int k1, double* v, double* T,
+                        double* cp, double* ha) {
   const Block& b = c.b;
   const int itmax = err_mach ? 100 : 200;
   const double eps = err_mach ? 1.0e-10 : 1.0e-5;
-  int i0, i1, j0, j1, k0, k1;
-  domain_select(b, dom, i0, i1, j0, j1, k0, k1);
-  wmix_i(c, dom, v, W_i);
   int it = 0;
   double error = 0.0;
   bool negT = false;
@@ -282,6 +281,28 @@ int prim_inv_var(Ctx& c, int dom, bool err_mach, double* v, double* W_i, double*
     return IZEM_ERR_NAN;
   }
   return IZEM_OK;
+}
+
+int prim_inv_var(Ctx& c, int dom, bool err_mach, double* v, double* W_i, double* T, double* cp, double* ha) {
+  const Block& b = c.b;
+  int i0, i1, j0, j1, k0, k1;
+  domain_select(b, dom, i0, i1, j0, j1, k0, k1);
+  wmix_i(c, dom, v, W_i);
+  // the reference's ranks each run the loop, and its stopping test, on
+  // their own points (test-only emulation of an x-decomposition: the
+  // interior and the ghost slabs that span x split into x-blocks)
+  const int nxb = std::max(c.newton_xblocks, 1);
+  if (nxb > 1 && i0 >= 1 && i1 <= b.nx) {
+    const int bx = b.nx / nxb;
+    for (int q = 0; q < nxb; ++q) {
+      const int lo = std::max(i0, 1 + q * bx), hi = std::min(i1, (q + 1) * bx);
+      if (lo > hi) continue;
+      int rc = prim_inv_var_region(c, err_mach, lo, hi, j0, j1, k0, k1, v, T, cp, ha);
+      if (rc) return rc;
+    }
+    return IZEM_OK;
+  }
+  return prim_inv_var_region(c, err_mach, i0, i1, j0, j1, k0, k1, v, T, cp, ha);
 }
 
 // force_sumY (module_thermodynamics.f90:1709-1860), npv = nvv = 0 branch
@@ -1493,6 +1514,13 @@ int or_set_sensor_xblocks(void* h, int nblk) {
   Ctx* c = static_cast<Ctx*>(h);
   if (nblk < 1 || c->b.nx % nblk) return IZEM_ERR_ARG;
   c->sensor_xblocks = nblk;
+  return IZEM_OK;
+}
+
+int or_set_newton_xblocks(void* h, int nblk) {
+  Ctx* c = static_cast<Ctx*>(h);
+  if (nblk < 1 || c->b.nx % nblk) return IZEM_ERR_ARG;
+  c->newton_xblocks = nblk;
   return IZEM_OK;
 }
 

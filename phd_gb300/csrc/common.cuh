@@ -52,12 +52,17 @@ struct DevThd {
 static __constant__ DevThd c_thd;
 
 // Device status word shared by all kernels of a context.
+// Newton stopping slots: sub-domain d (0 interior, 1-6 ghost faces, 7-8 the
+// Dirichlet planes of the W and E faces) of x-block b is slot d + 10 b; one
+// x-block unless the reference's x-decomposition is emulated.
+constexpr int kNewtonXBlocksMax = 8;
+constexpr int kNewtonSlots = 10 * kNewtonXBlocksMax;
+
 struct DevStatus {
-  // per sub-domain (0 interior, 1-6 ghost faces, 7-8 the Dirichlet planes
-  // of the W and E faces) max dT^2 (bit pattern of a non-negative double)
-  unsigned long long maxdf_bits[10];
-  int it[10];
-  int done[10];
+  // per slot max dT^2 (bit pattern of a non-negative double), iterations, stop flag
+  unsigned long long maxdf_bits[kNewtonSlots];
+  int it[kNewtonSlots];
+  int done[kNewtonSlots];
   int neg_pressure;
   int neg_temperature;
   int newton_nan;

@@ -48,6 +48,7 @@ struct izem_ctx {
   // sensor x-blocks (izem_gpu_set_sensor_xblocks): block size in x (nx for
   // one block) and the block-edge faces as seen by the right block
   int sensor_bx = 0;
+  int newton_bx = 0;   // x-block size of the Newton stopping test (nx: one block)
   double* fhat_edge = nullptr;
   long long nedge = 0;
   // chemistry

@@ -175,14 +175,17 @@ int enq_newton(izem_ctx* c, int ghost, double eps, int itmax, int check_negT) {
   const long long n = ghost == 2 ? 2LL * g.n[1] * g.n[2] : (ghost ? slab_count(g) - g.nint : g.nint);
   const char* iname = ghost == 2 ? "newton_iter_plane" : (ghost ? "newton_iter_ghost" : "newton_iter");
   int rc;
-  if ((rc = launch(c, "newton_reset", [&] { k_newton_reset<<<1, 8, 0, c->stream>>>(c->d_status, d0, d1); }))) return rc;
+  const int nxb = g.n[0] / c->newton_bx, bx = c->newton_bx;
+  if ((rc = launch(c, "newton_reset", [&] { k_newton_reset<<<1, 16 * kNewtonXBlocksMax, 0, c->stream>>>(c->d_status, d0, d1, nxb); })))
+    return rc;
   auto iterate = [&](cudaGraphConditionalHandle cond, int use_cond) -> int {
     int r = launch(c, iname, [&] {
-      k_newton_iter<NRV><<<grid_for(n), kThreads, 0, c->stream>>>(g, ghost, c->v, c->T, c->cp, c->ha, c->d_status, check_negT);
+      k_newton_iter<NRV><<<grid_for(n), kThreads, 0, c->stream>>>(g, ghost, c->v, c->T, c->cp, c->ha, c->d_status, check_negT,
+                                                                  bx);
     });
     if (r) return r;
     return launch(c, "newton_check", [&] {
-      k_newton_check<<<1, 32, 0, c->stream>>>(c->d_status, d0, d1, eps, itmax, cond, use_cond);
+      k_newton_check<<<1, 32, 0, c->stream>>>(c->d_status, d0, d1, nxb, eps, itmax, cond, use_cond);
     });
   };
   if (c->capturing) {
@@ -219,10 +222,11 @@ int enq_newton(izem_ctx* c, int ghost, double eps, int itmax, int check_negT) {
   for (int it = 0; it < itmax; it += kNewtonChunk) {
     for (int q = 0; q < kNewtonChunk && it + q < itmax; ++q)
       if ((rc = iterate(0, 0))) return rc;
-    CK(cudaMemcpyAsync(c->h_done, c->d_status->done + d0, (d1 - d0 + 1) * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(c->h_done, c->d_status->done, kNewtonSlots * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     bool all = true;
-    for (int d = 0; d <= d1 - d0; ++d) all = all && c->h_done[d] != 0;
+    for (int b = 0; b < nxb; ++b)
+      for (int d = d0; d <= d1; ++d) all = all && c->h_done[d + 10 * b] != 0;
     if (all) break;
   }
   return IZEM_OK;
@@ -582,6 +586,7 @@ int izem_gpu_init(const izem_cfg* cfg, const izem_thd* thd, const izem_adi* adi,
   Geo& g = c->g;
   g.n[0] = cfg->nx; g.n[1] = cfg->ny; g.n[2] = cfg->nz; g.ng = cfg->ng; g.ndim = cfg->ndim;
   c->sensor_bx = cfg->nx;   // one block
+  c->newton_bx = cfg->nx;
   for (int d = 0; d < 3; ++d) g.g[d] = g.n[d] + 2 * g.ng;
   g.ncell = (long long)g.g[0] * g.g[1] * g.g[2];
   g.nint = (long long)g.n[0] * g.n[1] * g.n[2];
@@ -637,7 +642,7 @@ int ctx_alloc(izem_ctx* c) {
   const int nv = c->nv, nrv = c->cfg.nrv;
   CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
   CK(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
-  CK(cudaMallocHost(&c->h_done, 16 * sizeof(int)));
+  CK(cudaMallocHost(&c->h_done, kNewtonSlots * sizeof(int)));
   CK(cudaMemcpyToSymbol(c_thd, &c->devthd, sizeof(DevThd)));
   auto alloc = [&](double** p, size_t n) -> cudaError_t {
     cudaError_t e = cudaMalloc(p, n * sizeof(double));
@@ -1169,10 +1174,12 @@ int izem_gpu_autotune(izem_ctx* c, double chem_dt, char* report, int report_len)
 }
 
 int izem_gpu_set_sensor_xblocks(izem_ctx* c, int nblk) {
-  if (!c || nblk < 1 || c->cfg.nx % nblk != 0 || c->cfg.nx / nblk < c->cfg.ng) return IZEM_ERR_ARG;
+  if (!c || nblk < 1 || nblk > kNewtonXBlocksMax || c->cfg.nx % nblk != 0 || c->cfg.nx / nblk < c->cfg.ng)
+    return IZEM_ERR_ARG;
   drop_graphs(c);
   if (c->fhat_edge) { CK(cudaFree(c->fhat_edge)); c->fhat_edge = nullptr; }
   c->sensor_bx = c->cfg.nx / nblk;
+  c->newton_bx = c->cfg.nx / nblk;
   c->nedge = (long long)(nblk - 1) * c->cfg.ny * c->cfg.nz;
   if (c->nedge > 0) CK(cudaMalloc(&c->fhat_edge, (size_t)c->nv * c->nedge * sizeof(double)));
   return IZEM_OK;

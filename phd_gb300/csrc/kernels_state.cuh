@@ -156,7 +156,8 @@ __global__ void k_halo(Geo g, int mode, int forcesum, double* __restrict__ v, do
 // sub-domain stops on its own maximum correction.
 template <int NRV>
 __global__ void k_newton_iter(Geo g, int ghost, const double* __restrict__ v, double* __restrict__ T,
-                              double* __restrict__ cp, double* __restrict__ ha, DevStatus* st, int check_negT) {
+                              double* __restrict__ cp, double* __restrict__ ha, DevStatus* st, int check_negT,
+                              int bx) {
   long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   int i, j, k, dom;
   if (ghost == 2) {
@@ -182,6 +183,9 @@ __global__ void k_newton_iter(Geo g, int ghost, const double* __restrict__ v, do
     k = (int)(r / g.n[1]) + 1;
     dom = 0;
   }
+  // the interior and the y / z ghost slabs span x: with an emulated
+  // x-decomposition (bx < nx) each x-block of them stops on its own test
+  if (bx < g.n[0] && (dom == 0 || (dom >= 3 && dom <= 6))) dom += 10 * ((i - 1) / bx);
   if (st->done[dom]) return;
   const long long nc = g.ncell;
   const long long p = gid(g, i, j, k);
@@ -222,26 +226,35 @@ __global__ void k_newton_iter(Geo g, int ghost, const double* __restrict__ v, do
 // while any sub-domain is still iterating.  Every iteration moves each live
 // sub-domain one step closer to itmax, so the loop ends after at most itmax
 // passes.
-__global__ void k_newton_check(DevStatus* st, int d0, int d1, double eps, int itmax,
+__global__ void k_newton_check(DevStatus* st, int d0, int d1, int nxb, double eps, int itmax,
                                cudaGraphConditionalHandle cond, int use_cond) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   unsigned live = 0;
-  for (int d = d0; d <= d1; ++d) {
-    if (st->done[d]) continue;
-    st->it[d] += 1;
-    const double err = sqrt(__longlong_as_double((long long)st->maxdf_bits[d]));
-    st->maxdf_bits[d] = 0ULL;
-    if (err < eps) st->done[d] = 1;
-    else if (st->it[d] >= itmax) { st->done[d] = 1; st->newton_unconverged += 1; }
-    if (st->done[d]) st->newton_it_max = max(st->newton_it_max, st->it[d]);
-    else live = 1;
-  }
+  for (int b = 0; b < nxb; ++b)
+    for (int d = d0 + 10 * b; d <= d1 + 10 * b; ++d) {
+      if (st->done[d]) continue;
+      st->it[d] += 1;
+      const double err = sqrt(__longlong_as_double((long long)st->maxdf_bits[d]));
+      st->maxdf_bits[d] = 0ULL;
+      if (err < eps) st->done[d] = 1;
+      else if (st->it[d] >= itmax) { st->done[d] = 1; st->newton_unconverged += 1; }
+      if (st->done[d]) st->newton_it_max = max(st->newton_it_max, st->it[d]);
+      else live = 1;
+    }
   if (use_cond) cudaGraphSetConditional(cond, live);
 }
 
-__global__ void k_newton_reset(DevStatus* st, int d0, int d1) {
-  int d = d0 + threadIdx.x;
-  if (d <= d1) { st->done[d] = 0; st->it[d] = 0; st->maxdf_bits[d] = 0ULL; }
+// Slots of sub-domains [d0, d1] of every x-block start iterating; the slots
+// of x-blocks b > 0 of a sub-domain that does not span x receive no points
+// and stop on their first test.
+__global__ void k_newton_reset(DevStatus* st, int d0, int d1, int nxb) {
+  const int b = threadIdx.x / 16, d = d0 + threadIdx.x % 16;
+  if (b < nxb && d <= d1) {
+    const int q = d + 10 * b;
+    st->done[q] = 0;
+    st->it[q] = 0;
+    st->maxdf_bits[q] = 0ULL;
+  }
 }
 
 // Convective time-step criterion: max over the interior of (|u_d|+c) dx_i.

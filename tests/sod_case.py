@@ -43,8 +43,9 @@ def golden_plot(n):
 def sod_case(xblocks=NX_BLOCKS):
     """Configuration, species data, references, oracle, the ghosted initial
     state (closed by finalize_ic) and the metrics (dx_i, dy_i, dz_i) of the
-    reference's Sod run.  xblocks: the MPI x-blocks whose effect on the
-    shock sensor the oracle emulates (1 for a single block)."""
+    reference's Sod run.  xblocks: the MPI x-blocks of the reference's run,
+    whose effects on the shock sensor and on the Newton stopping test the
+    oracle emulates (1 for a single block)."""
     a = constants()
     sp = load_species("o2n2")
     thd = thd_init(sp, a)
@@ -66,6 +67,7 @@ def sod_case(xblocks=NX_BLOCKS):
     grid = (dxi(xm), dxi(ym), dz)
     orc = oracle.Oracle(cfg, thd, adi_struct(a), *grid)
     orc.set_sensor_xblocks(xblocks)
+    orc.set_newton_xblocks(xblocks)
 
     # ini_sod: mole fractions 0.233 / 0.767 turned into mass fractions by
     # X_to_Y (module_thermodynamics.f90:45-68); (P, rho) = (1, 1) left of

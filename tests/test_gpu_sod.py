@@ -95,9 +95,10 @@ def test_gpu_reproduces_reference_restarts():
     condition through the main loop's time stepping and reproduces the
     reference's own FP64 restart files at the first three statistics
     times, within the bounds of the oracle's pin (tests/test_sod_pin.py):
-    density, energy and species within 5e-7 of their largest magnitude, x
-    momentum within 1e-6, y and z momenta within 1e-10 of the largest
-    density."""
+    density, energy, species and x momentum within 2e-9 of their largest
+    magnitude, y and z momenta within 1e-10 of the largest density.  The
+    x-blocks also stop their Newton loops on their own tests, as the
+    reference's ranks do."""
     cfg, thd, a, orc, st, grid = S.sod_case(xblocks=S.NX_BLOCKS)
     g = _gpu(cfg, thd, a, grid, st)
     g.set_sensor_xblocks(S.NX_BLOCKS)
@@ -126,8 +127,7 @@ def test_gpu_reproduces_reference_restarts():
             if name in ("rhoV", "rhoW"):
                 assert err <= 1e-10 * rho_max, (n, name, err)
             else:
-                tol = 1e-6 if name == "rhoU" else 5e-7
-                assert err <= tol * np.abs(ref[name]).max(), (n, name, err / np.abs(ref[name]).max())
+                assert err <= 2e-9 * np.abs(ref[name]).max(), (n, name, err / np.abs(ref[name]).max())
 
 
 def test_gpu_resumes_reference_restart(tmp_path):
@@ -137,9 +137,9 @@ def test_gpu_resumes_reference_restart(tmp_path):
     read_restart_hdf5):
     * with the Adams-Shariff flags of the run that wrote it (the reference
       never clears a flag and does not store them), the resumed GPU run
-      reproduces restart 2 at the pin tolerances;
+      reproduces restart 2 within 5e-10 of each field's largest magnitude;
     * with cleared flags, as the reference's own resume starts, it agrees
-      with the oracle resumed the same way, within the same bounds."""
+      with the oracle resumed the same way, within the same bound."""
     from phd_gb300 import restart as R
     names7 = ["rho", "rhoU", "rhoV", "rhoW", "rhoE", "O2", "N2"]
     cfg, thd, a, orc, st, grid = S.sod_case(xblocks=S.NX_BLOCKS)
@@ -177,8 +177,7 @@ def test_gpu_resumes_reference_restart(tmp_path):
         if name in ("rhoV", "rhoW"):
             assert err <= 1e-10 * rho_max, (name, err)
         else:
-            tol = 1e-6 if name == "rhoU" else 5e-7
-            assert err <= tol * np.abs(ref[name]).max(), (name, err / np.abs(ref[name]).max())
+            assert err <= 5e-10 * np.abs(ref[name]).max(), (name, err / np.abs(ref[name]).max())
     _, _, _, orc2, _, _ = S.sod_case(xblocks=S.NX_BLOCKS)
     st3 = R.state_from_restart(names, arrs, S.NG, species=["O2", "N2"])
     orc2.finalize_ic(st3)
@@ -198,5 +197,4 @@ def test_gpu_resumes_reference_restart(tmp_path):
         if name in ("rhoV", "rhoW"):
             assert err <= 1e-10 * rho_max, (name, err)
         else:
-            tol = 1e-6 if name == "rhoU" else 5e-7
-            assert err <= tol * np.abs(vo[..., q]).max(), (name, err / np.abs(vo[..., q]).max())
+            assert err <= 5e-10 * np.abs(vo[..., q]).max(), (name, err / np.abs(vo[..., q]).max())
