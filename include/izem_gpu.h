@@ -231,13 +231,15 @@ int  izem_gpu_set_mechanism(izem_ctx* ctx, const izem_mech* mech);
  * window (ng+1 cells are skipped at every global face, as in the reference),
  * each integrated as a constant-volume reactor by the BDF method (DVODE
  * MF=22, RTOL 1e-6, ATOL 1e-10, <= 20 restarts) in a persistent
- * work-stealing kernel; then upd_prim_var_woT, halo fill and the ghost
- * Newton solve.  mode IZEM_CHEM_BDF: the BDF method on every cell;
- * IZEM_CHEM_MLP: the learned surrogate set by izem_gpu_set_surrogate with its
- * error gate, rejected cells by the BDF method (no counterpart in the
- * reference).  DTmax receives max |dT| [K]. */
+ * work-stealing kernel; then upd_prim_var_woT, comm_cons, upd_boundaries
+ * (given `time` and dt, as reaction_selec passes them: the jet faces read
+ * them) and the ghost Newton solve.  mode IZEM_CHEM_BDF: the BDF method on
+ * every cell; IZEM_CHEM_MLP: the learned surrogate set by
+ * izem_gpu_set_surrogate with its error gate, rejected cells by the BDF
+ * method (no counterpart in the reference).  DTmax receives max |dT| [K].
+ * Blocks with jet faces need izem_gpu_set_coords first. */
 enum { IZEM_CHEM_BDF = 0, IZEM_CHEM_MLP = 1 };
-int  izem_gpu_chem_step(izem_ctx* ctx, double dt, int mode, double* DTmax);
+int  izem_gpu_chem_step(izem_ctx* ctx, double dt, double time, int mode, double* DTmax);
 
 /* [REACTING] DVODESIMP with Y1F, Y0O, INDEX_H2, INDEX_N2 (module_reaction.f90:
  * 173-251): with enable != 0, mode IZEM_CHEM_BDF integrates only the window
@@ -258,9 +260,38 @@ int  izem_gpu_set_chem_skip(izem_ctx* ctx, int enable, const double* Y_fuel, con
  * (module_tools.f90:319,489), for the jet faces IZEM_BC_INFLOWJET (radius
  * sqrt(y^2 + z^2)) and IZEM_BC_NSCBC_OUT (Lx).  Required before
  * izem_gpu_rk3 when a jet face is set; the time0 argument of izem_gpu_rk3
- * then gives the stage times timek = time0 + dt tk3 (module_solver.f90:756).
- * The chemistry step is built for periodic and extrapolation faces only. */
+ * then gives the stage times timek = time0 + dt tk3 (module_solver.f90:756),
+ * and the time argument of izem_gpu_chem_step the chemistry tail's time. */
 int  izem_gpu_set_coords(izem_ctx* ctx, const double* x, const double* y, const double* z, double lx);
+
+/* Parameters of the jet faces.  izem_jet_reference fills the constants that
+ * bc_inflowjet (module_BCs.f90:1680-1700) and bc_nscbc_out (:2390) hard-code,
+ * which izem_gpu_set_coords installs: a round sonic nozzle of 1 mm with
+ * pure fuel at 1000 K and 15 atm into 300 K air at 1 atm and 20 m/s, ramped
+ * in as (t / 0.1 ms)^3, and the outflow relaxed toward 94232.25 Pa.  Other
+ * values run the same profile formulas with another nozzle (no counterpart
+ * in the reference): a planar slot (tanh profile in |y|), a given jet
+ * velocity, a fuel/N2 jet, no ramp, and seeded velocity fluctuations
+ * u' = turb u_jet (1 - tanh) / 2 r with r uniform in [-1, 1), a hash of the
+ * seed, the face point and the stage time's 1 ns interval, on all three
+ * components. */
+typedef struct izem_jet {
+  double width;            /* [m] nozzle diameter, or slot width (planar)        */
+  double ramp;             /* [s] ramp time of the nozzle state; 0: none         */
+  double T_jet, T_co;      /* [K] nozzle and coflow temperatures                 */
+  double p_jet, p_co;      /* [Pa] nozzle and coflow pressures                   */
+  double u_jet;            /* [m/s] jet velocity; 0: 1.01 x its sound speed       */
+  double u_co;             /* [m/s] coflow velocity                              */
+  double y_fuel;           /* H2 mass fraction of the jet (the rest N2)          */
+  double p_far;            /* [Pa] far-field pressure of the outflow             */
+  double turb;             /* relative amplitude of the fluctuations; 0: none    */
+  int    planar;           /* 0: round jet, 1: planar slot                       */
+  int    reserved;
+  unsigned long long seed; /* seed of the fluctuations                           */
+} izem_jet;
+void izem_jet_reference(izem_jet* p);
+/* Installs p for the jet faces of ctx (after izem_gpu_set_coords). */
+int  izem_gpu_set_jet(izem_ctx* ctx, const izem_jet* p);
 
 /* [IFLES] LES = T with MU_SGS_MODEL = SMAGORINSKY under EGLIB: the viscous
  * fluxes of viscflux_eg_LES_xyz (module_eg_lib.f90:2687-3352) with
@@ -316,6 +347,18 @@ int  izem_gpu_psr_batch_mlp(izem_mlp* m, izem_mlp* m2, const izem_mech* mech, in
                             const double* rho, double* Y, const double* dt, int device_ptrs,
                             const double* gate10, const int* kncf, int nele, double* dT_pred,
                             int* stats3, float* ms2);
+/* Target form of a network (no counterpart in the reference): residual = 1
+ * when it was trained on the chemistry increment minus the explicit one,
+ * dt f(y0) with f the reactor right-hand side at the start state; the gated
+ * step then adds dt f(y0) back before its tests.  Both networks of an
+ * ensemble must have the same form.  Default 0. */
+int  izem_mlp_set_residual(izem_mlp* m, int residual);
+/* The constant-volume reactor right-hand side dz/dt, z = [T, Y_1..Y_9]
+ * (FUN of REACTION_V, chemkin/reaction_v.f), at n states: T [K], rho
+ * [g/cm^3], Y (n x 9) -> zdot (n x 10).  Device arrays when device_ptrs,
+ * host arrays otherwise. */
+int  izem_gpu_reactor_rhs(const izem_mech* mech, int n, const double* T, const double* rho, const double* Y,
+                          double* zdot, int device_ptrs);
 /* The cells that the last izem_gpu_psr_batch_mlp call on m sent to the BDF
  * integrator (no counterpart in the reference): their indices in that
  * call's batch, in no particular order; up to cap of them are written to

@@ -48,9 +48,10 @@ def load():
         "or_finalize_ic": (C.c_int, [P, _dp, _dp, _dp, _dp, _dp]),
         "or_rk3": (C.c_int, [P, C.c_double, C.c_double, _dp, _dp, _dp, _dp, _dp, _u8p]),
         "or_set_coords": (C.c_int, [P, _dp, _dp, _dp, C.c_double]),
+        "or_set_jet": (C.c_int, [P, C.c_void_p]),
         "or_timestep": (C.c_int, [P, C.c_double, _dp, _dp, _dp, _dp, _dp, _dp]),
         "or_metrics_dscalar": (None, [C.c_int, C.c_int, _dp, _dp]),
-        "or_chem_step": (C.c_int, [P, C.POINTER(IzemMech), C.c_double, _dp, _dp, _dp, _dp, _dp, _dp,
+        "or_chem_step": (C.c_int, [P, C.POINTER(IzemMech), C.c_double, C.c_double, _dp, _dp, _dp, _dp, _dp, _dp,
                                    C.POINTER(C.c_int)]),
         "or_psr_cells": (None, [C.POINTER(IzemMech), C.c_int, _dp, _dp, _dp, _dp, C.POINTER(C.c_int),
                                 C.POINTER(C.c_int)]),
@@ -247,12 +248,19 @@ class Oracle:
         self._keep_coords = xs
         self._rc(self.lib.or_set_coords(self.h, *[_p(a) for a in xs], float(lx)), "set_coords")
 
-    def chem_step(self, s, mech, dt):
+    def set_jet(self, jet):
+        """Jet-face parameters (phd_gb300.capi.IzemJet)."""
+        self._jet = jet
+        self._rc(self.lib.or_set_jet(self.h, C.addressof(jet)), "set_jet")
+
+    def chem_step(self, s, mech, dt, time=0.0):
+        """reaction_selec over a half step dt at the given time (the jet
+        faces' boundary closure reads both); returns DTmax [K]."""
         v, T, W_i, cp, ha = self._arrs(s)
         dtm = C.c_double()
         mx = C.c_int()
-        self._rc(self.lib.or_chem_step(self.h, C.byref(mech), float(dt), _p(v), _p(T), _p(W_i), _p(cp), _p(ha),
-                                       C.byref(dtm), C.byref(mx)), "chem_step")
+        self._rc(self.lib.or_chem_step(self.h, C.byref(mech), float(dt), float(time), _p(v), _p(T), _p(W_i), _p(cp),
+                                       _p(ha), C.byref(dtm), C.byref(mx)), "chem_step")
         return dtm.value
 
     def timestep(self, s, DTmax=0.0, dtmin=1.0):

@@ -76,6 +76,9 @@ struct Ctx {
   // in x (Lx, module_tools.f90:319,489) for the jet boundaries
   std::vector<double> crd[3];
   double lx = 0.0;
+  // parameters of the jet faces: the constants of bc_inflowjet
+  // (module_BCs.f90:1680-1700) and bc_nscbc_out (:2390) unless overridden
+  izem_jet jet{0.0010, 0.0001, 1000.0, 300.0, 101325.0 * 15.0, 101325.0, 0.0, 20.0, 1.0, 94232.25, 0.0, 0, 0, 0ULL};
   bool dvodesimp = false;
   double y1f[IZEM_NSMAX] = {}, y0o[IZEM_NSMAX] = {};
   int index_h2 = 0, index_n2 = 0;
@@ -405,24 +408,42 @@ double wmix_i_scalar(const izem_thd& t, int nrv, const double* Ya) {
 // points and the first interior plane.  The reference computes the exit
 // sound speed from a mass-fraction array of which only the entries below
 // are set; the others are taken as 0.  Species sets of 2, 3 or 9 species.
+// Seeded fluctuation of a jet inflow point: uniform in [-1, 1) from a hash
+// (splitmix64 finaliser, Steele, Lea and Flood 2014) of the seed, the face
+// point, the velocity component and the time interval n (stage time in 1 ns
+// units, rounded down).
+double jet_noise(unsigned long long seed, int j, int k, int comp, long long n) {
+  unsigned long long x = seed ^ ((unsigned long long)(unsigned)j << 40) ^ ((unsigned long long)(unsigned)k << 20) ^
+                         ((unsigned long long)comp * 0x9E3779B97F4A7C15ULL) ^ ((unsigned long long)n * 0xD1B54A32D192ED03ULL);
+  for (int r = 0; r < 2; ++r) {
+    x += 0x9E3779B97F4A7C15ULL;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBULL;
+    x = x ^ (x >> 31);
+  }
+  return (double)(x >> 11) * (1.0 / 9007199254740992.0) * 2.0 - 1.0;
+}
+
+// bc_inflowjet with the context's jet parameters (the reference's constants
+// by default): round or planar profile, a given or sonic jet velocity, the
+// ramp, and the seeded fluctuations when turb > 0.
 void bc_inflowjet(const Ctx& c, double time, double* v) {
   const Block& b = c.b;
   const izem_adi& a = c.adi;
   const izem_thd& t = c.thd;
+  const izem_jet& jp = c.jet;
   const int nrv = b.nrv;
   const size_t nc = b.ncell;
-  const double NPR = 15.0;
-  const double hbuse = 0.0010 / a.l_ref, tmaxy = 0.0001 / a.time_ref;
-  const double u_2 = 20.0 / a.u_ref;
-  double T_1 = 1000.0 / a.t_ref;
-  const double T_2 = 300.0 / a.t_ref;
-  double P_1 = 101325.0 * NPR / a.p_ref;
-  const double P_2 = 101325.0 / a.p_ref;
-  double Ya_1 = 1.0;
+  const double hbuse = jp.width / a.l_ref, tmaxy = jp.ramp / a.time_ref;
+  const double u_2 = jp.u_co / a.u_ref;
+  double T_1 = jp.T_jet / a.t_ref;
+  const double T_2 = jp.T_co / a.t_ref;
+  double P_1 = jp.p_jet / a.p_ref;
+  const double P_2 = jp.p_co / a.p_ref;
+  double Ya_1 = jp.y_fuel;
   const double Ya_2 = 0.0;
   const double delt = 1.0 / (0.04 * hbuse), y0 = hbuse / 2.0;
-  const double vy = 0.0, wz = 0.0;
-  if (time <= tmaxy) {
+  if (tmaxy > 0.0 && time <= tmaxy) {
     P_1 = (P_2 - (P_2 - P_1) * (time / tmaxy) * (time / tmaxy) * (time / tmaxy));
     Ya_1 = (Ya_2 - (Ya_2 - Ya_1) * (time / tmaxy) * (time / tmaxy) * (time / tmaxy));
     T_1 = (T_2 - (T_2 - T_1) * (time / tmaxy) * (time / tmaxy) * (time / tmaxy));
@@ -436,14 +457,23 @@ void bc_inflowjet(const Ctx& c, double time, double* v) {
   double gamma = t.gam2 * Ws_i / cps;
   gamma = 1.0 / (1.0 - gamma);
   const double cs = std::sqrt(gamma * Ws_i * T_1);
-  const double u_1 = 1.01 * cs;
+  const double u1p = jp.u_jet / a.u_ref;
+  const double u_1 = u1p > 0.0 ? u1p : 1.01 * cs;
   for (int k = 1; k <= b.nz; ++k)
     for (int j = 1; j <= b.ny; ++j)
       for (int i = 1 - b.ng; i <= 1; ++i) {
         const double y = c.crd[1][j - 1], z = c.crd[2][k - 1];
-        const double rrr = std::sqrt(y * y + z * z);
+        const double rrr = jp.planar ? std::fabs(y) : std::sqrt(y * y + z * z);
         const double th = std::tanh((rrr - y0) * delt);
-        const double ux = 0.5 * ((u_1 + u_2) - (u_1 - u_2) * th);
+        double ux = 0.5 * ((u_1 + u_2) - (u_1 - u_2) * th);
+        double vy = 0.0, wz = 0.0;
+        if (jp.turb > 0.0) {
+          const double am = jp.turb * u_1 * (0.5 * (1.0 - th));
+          const long long n = (long long)std::floor(time * (a.time_ref / 1.0e-9));
+          ux = ux + am * jet_noise(jp.seed, j, k, 0, n);
+          vy = am * jet_noise(jp.seed, j, k, 1, n);
+          wz = am * jet_noise(jp.seed, j, k, 2, n);
+        }
         const double T = 0.5 * ((T_1 + T_2) - (T_1 - T_2) * th);
         const double P = 0.5 * ((P_1 + P_2) - (P_1 - P_2) * th);
         for (int l = 0; l < nrv; ++l) Ya[l] = 0.0;
@@ -486,7 +516,7 @@ void bc_nscbc_out(const Ctx& c, double dtime, const double* T, const double* W_i
   const izem_thd& t = c.thd;
   const int nrv = b.nrv;
   const size_t nc = b.ncell;
-  const double Pinf = 94232.25 / a.p_ref, sigma1 = 0.28, Lx = c.lx;
+  const double Pinf = c.jet.p_far / a.p_ref, sigma1 = 0.28, Lx = c.lx;
   static const double a4or[5] = {-3.0 / 12.0, 16.0 / 12.0, -36.0 / 12.0, 48.0 / 12.0, -25.0 / 12.0};   // m = -4..0
   const int ex = b.nx;
   const double dxe = c.dxi[0][ex - 1 + b.ng];
@@ -565,15 +595,12 @@ void bc_nscbc_out(const Ctx& c, double dtime, const double* T, const double* W_i
     }
 }
 
-// upd_prim_var_domain + comm_cons + upd_boundaries + upd_prim_var_ghost
-// (module_solver.f90:839-845, module_BCs.f90:41-296)
-// time: the stage time given to upd_boundaries; dt: the step.
-int update_primitives(Ctx& c, double* v, double* T, double* W_i, double* cp, double* ha, double time = 0.0,
-                      double dt = 0.0) {
+// comm_cons + upd_boundaries + upd_prim_var_ghost (module_BCs.f90:41-296):
+// the closure of the ghost points after the interior changed.  time and dt
+// are what upd_boundaries is given (the jet faces read them).
+int update_boundaries(Ctx& c, double* v, double* T, double* W_i, double* cp, double* ha, double time, double dt) {
   const Block& b = c.b;
-  if (c.cfg.forcesum) force_sumY(c, 0, v);
-  int rc = prim_inv_var(c, 0, false, v, W_i, T, cp, ha);
-  if (rc) return rc;
+  int rc = IZEM_OK;
   comm_periodic(b, b.nv, v, b.ncell);
   for (int f = 0; f < 6; ++f) {
     if (!b.bnd[f]) continue;
@@ -591,6 +618,16 @@ int update_primitives(Ctx& c, double* v, double* T, double* W_i, double* cp, dou
     if (rc) return rc;
   }
   return IZEM_OK;
+}
+
+// upd_prim_var_domain, then the ghost closure (module_solver.f90:839-845)
+// time: the stage time given to upd_boundaries; dt: the step.
+int update_primitives(Ctx& c, double* v, double* T, double* W_i, double* cp, double* ha, double time = 0.0,
+                      double dt = 0.0) {
+  if (c.cfg.forcesum) force_sumY(c, 0, v);
+  int rc = prim_inv_var(c, 0, false, v, W_i, T, cp, ha);
+  if (rc) return rc;
+  return update_boundaries(c, v, T, W_i, cp, ha, time, dt);
 }
 
 // closure of the initial conditions (module_ICs.f90:2874-2879)
@@ -1348,8 +1385,13 @@ void timestep(const Ctx& c, double DTmax, const double* v, const double* T, cons
 // than 1e-12 and its H2 and N2 both differ from the pure fuel and from the
 // pure oxidiser by more than 1e-6 (:185-215); that branch also clips the
 // closing species (:233-240).
-int chem_step(Ctx& c, const izem_mech& mech, double dt, double* v, double* T, double* W_i, double* cp, double* ha,
-              double* DTmax_out, int* max_steps) {
+int update_boundaries(Ctx& c, double* v, double* T, double* W_i, double* cp, double* ha, double time, double dt);
+
+// reaction_selec (module_reaction.f90:47-100): the reactors of the window,
+// then upd_prim_var_woT, comm_cons, upd_boundaries (given time and the half
+// step dt) and upd_prim_var_ghost.
+int chem_step(Ctx& c, const izem_mech& mech, double dt, double time, double* v, double* T, double* W_i, double* cp,
+              double* ha, double* DTmax_out, int* max_steps) {
   const Block& b = c.b;
   const izem_adi& a = c.adi;
   const double dt_phys = dt * a.time_ref;
@@ -1414,14 +1456,8 @@ int chem_step(Ctx& c, const izem_mech& mech, double dt, double* v, double* T, do
         cp[p] = cpp;
         for (int is = 0; is < nrv; ++is) ha[is * b.ncell + p] = hak[is];
       }
-  comm_periodic(b, b.nv, v, b.ncell);
-  for (int f = 0; f < 6; ++f)
-    if (b.bnd[f] && b.bc[f] == IZEM_BC_EXTRAPOLATION) bc_extrapolation(b, f, v);
-  for (int f = 0; f < 6; ++f) {
-    if (c.cfg.forcesum) force_sumY(c, kFaceDomain[f], v);
-    int rc = prim_inv_var(c, kFaceDomain[f], false, v, W_i, T, cp, ha);
-    if (rc) return rc;
-  }
+  int rc = update_boundaries(c, v, T, W_i, cp, ha, time, dt);
+  if (rc) return rc;
   if (fail) {
     c.err = "DVODE failed (ISTATE <= -2) on some cells";
     return IZEM_ERR_CHEM;
@@ -1524,6 +1560,12 @@ int or_set_newton_xblocks(void* h, int nblk) {
   return IZEM_OK;
 }
 
+int or_set_jet(void* h, const izem_jet* p) {
+  if (!h || !p) return IZEM_ERR_ARG;
+  static_cast<Ctx*>(h)->jet = *p;
+  return IZEM_OK;
+}
+
 int or_last_error(void* h, char* buf, int n) {
   Ctx* c = static_cast<Ctx*>(h);
   if (buf && n > 0) { std::snprintf(buf, n, "%s", c->err.c_str()); }
@@ -1588,14 +1630,14 @@ int or_timestep(void* h, double DTmax, const double* v, const double* T, const d
   return 0;
 }
 
-int or_chem_step(void* h, const izem_mech* mech, double dt, double* v, double* T, double* W_i, double* cp, double* ha,
-                 double* DTmax, int* max_steps) {
+int or_chem_step(void* h, const izem_mech* mech, double dt, double time, double* v, double* T, double* W_i,
+                 double* cp, double* ha, double* DTmax, int* max_steps) {
   Ctx* c = static_cast<Ctx*>(h);
-  if (is_dirichlet(c->b.bc[0]) || is_dirichlet(c->b.bc[1])) {
-    c->err = "the chemistry step is built for periodic and extrapolation faces only";
+  if ((is_dirichlet(c->b.bc[0]) || is_dirichlet(c->b.bc[1])) && c->crd[0].empty()) {
+    c->err = "jet boundaries need the coordinates (or_set_coords)";
     return IZEM_ERR_STATE;
   }
-  return chem_step(*c, *mech, dt, v, T, W_i, cp, ha, DTmax, max_steps);
+  return chem_step(*c, *mech, dt, time, v, T, W_i, cp, ha, DTmax, max_steps);
 }
 
 // Independent constant-volume reactors (PSR_CHEMKIN per cell): T [K],

@@ -101,3 +101,17 @@ class IzemAdi(C.Structure):
         "gamma_inf", "re", "pr", "le", "ma", "sc", "sqgmr", "ggmopr",
         "t_ref", "l_ref", "r_ref", "w_ref", "cp_ref", "mu_ref", "c_inf", "u_ref", "time_ref",
         "rho_ref", "p_ref", "lbda_ref", "d_ref")]
+
+
+class IzemJet(C.Structure):
+    """izem_jet: parameters of the jet faces (SI units)."""
+    _fields_ = [(n, C.c_double) for n in ("width", "ramp", "T_jet", "T_co", "p_jet", "p_co", "u_jet", "u_co",
+                                          "y_fuel", "p_far", "turb")] + \
+               [("planar", C.c_int), ("reserved", C.c_int), ("seed", C.c_ulonglong)]
+
+
+def jet_reference():
+    """The constants that bc_inflowjet and bc_nscbc_out hard-code
+    (module_BCs.f90:1680-1700, 2390)."""
+    return IzemJet(width=1e-3, ramp=1e-4, T_jet=1000.0, T_co=300.0, p_jet=101325.0 * 15.0, p_co=101325.0,
+                   u_jet=0.0, u_co=20.0, y_fuel=1.0, p_far=94232.25, turb=0.0, planar=0, reserved=0, seed=0)

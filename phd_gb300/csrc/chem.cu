@@ -1394,6 +1394,7 @@ struct GateArgs {
   double tol_T_abs, tol_T_rel;       // energy-consistency of dT [K]
   double tol_ens_abs, tol_ens_rel;   // agreement of two independently trained networks on dT [K]
   double dT_cap;                     // largest predicted |dT| accepted [K]
+  int residual;                      // the networks predict the increment minus dt f(y0)
 };
 
 // Decode the surrogate output, gate it, and write accepted cells in place.
@@ -1430,6 +1431,18 @@ __global__ void k_decode_gate(int n, const float* out, const float* out2, int ld
     const double dT2 = (double)out2[(size_t)q * ldo + KK] * so2[KK] + mo2[KK];
     if (fabs(dT2 - dTp) > ga.tol_ens_abs + ga.tol_ens_rel * fabs(dTp)) ok = false;
     dTp = 0.5 * (dTp + dT2);
+  }
+  if (ga.residual) {
+    // networks trained on the increment minus the explicit one: add
+    // dt f(y0), the reactor right-hand side at the start state
+    double z0[KK + 1], f0[KK + 1];
+    z0[0] = T0;
+#pragma unroll
+    for (int k = 0; k < KK; ++k) z0[1 + k] = Y[(size_t)q * KK + k];
+    ck_fun_fast<KK>(rho[q], z0, f0);
+#pragma unroll
+    for (int k = 0; k < KK; ++k) dY[k] = dY[k] + dt[q] * f0[1 + k];
+    dTp = dTp + dt[q] * f0[0];
   }
   if (!(fabs(dTp) <= ga.dT_cap)) ok = false;
   if (dT_pred) dT_pred[q] = dTp;
@@ -1475,6 +1488,22 @@ __global__ void k_decode_gate(int n, const float* out, const float* out2, int ld
     const unsigned slot = atomicAdd(count, 1u);
     list[slot] = base + q;
   }
+}
+
+// The reactor right-hand side dz/dt, z = [T, Y_1..Y_K] (FUN of REACTION_V,
+// the device form ck_fun_fast), at n states; zdot is n x (KK + 1).
+template <int KK>
+__global__ void k_reactor_rhs(int n, const double* __restrict__ T, const double* __restrict__ rho,
+                              const double* __restrict__ Y, double* __restrict__ zdot) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  double z[KK + 1], f[KK + 1];
+  z[0] = T[q];
+#pragma unroll
+  for (int k = 0; k < KK; ++k) z[1 + k] = Y[(size_t)q * KK + k];
+  ck_fun_fast<KK>(rho[q], z, f);
+#pragma unroll
+  for (int c = 0; c <= KK; ++c) zdot[(size_t)q * (KK + 1) + c] = f[c];
 }
 
 template <int KK, int MINB, class Rhs>
@@ -1635,11 +1664,18 @@ cudaError_t chem_launch_featurize(int n, const double* T, const double* rho, con
 cudaError_t chem_launch_decode_gate(int n, const float* out, const float* out2, int ldo, const float* d_norm,
                                     const float* d_norm2, double* T, const double* rho, double* Y, const double* dt,
                                     const double* gate10, const int* d_kncf, int nele, int* list, int base,
-                                    unsigned* count, double* dT_pred, ChemStats* stats, cudaStream_t s) {
+                                    unsigned* count, double* dT_pred, ChemStats* stats, int residual,
+                                    cudaStream_t s) {
   GateArgs ga{gate10[0], gate10[1], gate10[2], gate10[3], gate10[4],
-              gate10[5], gate10[6], gate10[7], gate10[8], gate10[9]};
+              gate10[5], gate10[6], gate10[7], gate10[8], gate10[9], residual};
   k_decode_gate<9><<<(n + 127) / 128, 128, 0, s>>>(n, out, out2, ldo, d_norm, d_norm2, T, rho, Y, dt, ga, d_kncf, nele,
                                                    list, base, count, dT_pred, stats);
+  return cudaGetLastError();
+}
+
+cudaError_t chem_launch_rhs(int n, const double* T, const double* rho, const double* Y, double* zdot, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_reactor_rhs<9><<<(n + 127) / 128, 128, 0, s>>>(n, T, rho, Y, zdot);
   return cudaGetLastError();
 }
 

@@ -65,6 +65,9 @@ cudaError_t chem_launch_featurize(int n, const double* T, const double* rho, con
 cudaError_t chem_launch_decode_gate(int n, const float* out, const float* out2, int ldo, const float* d_norm,
                                     const float* d_norm2, double* T, const double* rho, double* Y, const double* dt,
                                     const double* gate10, const int* d_kncf, int nele, int* list, int base,
-                                    unsigned* count, double* dT_pred, ChemStats* stats, cudaStream_t s);
+                                    unsigned* count, double* dT_pred, ChemStats* stats, int residual,
+                                    cudaStream_t s);
+// the reactor right-hand side dz/dt (z = [T, Y]) at n states: zdot n x 10
+cudaError_t chem_launch_rhs(int n, const double* T, const double* rho, const double* Y, double* zdot, cudaStream_t s);
 cudaError_t chem_launch_list(const int* list, const unsigned* count, double* T, const double* rho, double* Y,
                              const double* dt, unsigned* d_counter, ChemStats* d_stats, cudaStream_t s);

@@ -81,3 +81,20 @@ struct DevStatus {
 __device__ inline void atomic_max_nonneg(unsigned long long* addr, double v) {
   atomicMax(addr, (unsigned long long)__double_as_longlong(v));
 }
+
+// Seeded fluctuation of the jet inflow: uniform in [-1, 1) from a hash
+// (splitmix64 finaliser, Steele, Lea and Flood 2014) of the seed, the face
+// point (j, k), the velocity component and the time interval n (the stage
+// time in units of a fixed quantum, rounded down: runs whose times differ
+// in the last bits draw the same values).
+__host__ __device__ inline double jet_noise(unsigned long long seed, int j, int k, int comp, long long n) {
+  unsigned long long x = seed ^ ((unsigned long long)(unsigned)j << 40) ^ ((unsigned long long)(unsigned)k << 20) ^
+                         ((unsigned long long)comp * 0x9E3779B97F4A7C15ULL) ^ ((unsigned long long)n * 0xD1B54A32D192ED03ULL);
+  for (int r = 0; r < 2; ++r) {
+    x += 0x9E3779B97F4A7C15ULL;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBULL;
+    x = x ^ (x >> 31);
+  }
+  return (double)(x >> 11) * (1.0 / 9007199254740992.0) * 2.0 - 1.0;
+}

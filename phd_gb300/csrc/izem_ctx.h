@@ -80,6 +80,7 @@ struct izem_ctx {
   bool have_coords = false;
   double *d_y = nullptr, *d_z = nullptr;
   JetArgs jet{};
+  izem_jet jet_par{};                     // the jet faces' parameters (izem_gpu_set_jet)
   // LES closure (izem_gpu_set_les)
   bool les_on = false;
   double les_cs2 = 0.0, les_sc_sgs_i = 0.0, les_pr_sgs_i = 0.0, les_pw = 0.0;

@@ -144,6 +144,28 @@ int run_graph(izem_ctx* c, int slot, F enqueue) {
   return IZEM_OK;
 }
 
+// The jet faces' constants in code units, as bc_inflowjet and bc_nscbc_out
+// divide them, from the context's parameters.
+void jet_args(izem_ctx* c) {
+  const izem_adi& a = c->adi;
+  const izem_jet& p = c->jet_par;
+  JetArgs& j = c->jet;
+  j.hbuse = p.width / a.l_ref;
+  j.tmaxy = p.ramp / a.time_ref;
+  j.u2 = p.u_co / a.u_ref;
+  j.T1 = p.T_jet / a.t_ref;
+  j.T2 = p.T_co / a.t_ref;
+  j.P1 = p.p_jet / a.p_ref;
+  j.P2 = p.p_co / a.p_ref;
+  j.pinf = p.p_far / a.p_ref;
+  j.u1 = p.u_jet / a.u_ref;
+  j.ya1 = p.y_fuel;
+  j.turb = p.turb;
+  j.tq_i = a.time_ref / 1.0e-9;   // fluctuations drawn anew every 1 ns
+  j.seed = p.seed;
+  j.planar = p.planar;
+}
+
 // Drops every captured graph; the next call of each entry point captures
 // again (after a change of launch shapes, kernel variants or options).
 void drop_graphs(izem_ctx* c) {
@@ -342,14 +364,14 @@ int enq_visc(izem_ctx* c) {
 
 static bool jet_face(int bc) { return bc == IZEM_BC_INFLOWJET || bc == IZEM_BC_NSCBC_OUT; }
 
-// upd_prim_var_domain's Newton, comm_cons, upd_boundaries, upd_prim_var_ghost
-// (module_solver.f90:840-847).  stage: the RK stage whose time goes to the
-// jet faces (timek = time0 + dt tk3(stage)), -1 for time 0 and dt 0.
+// comm_cons, upd_boundaries, upd_prim_var_ghost (module_BCs.f90:41-296):
+// the ghost closure after the interior changed.  The jet faces read the
+// step and time from device memory: tdt[0] = dt, tdt[1] = time0, and the
+// time they are given is time0 + tk dt.
 template <int NRV>
-int enq_update_primitives_after(izem_ctx* c, int stage = -1) {
+int enq_boundaries(izem_ctx* c, const double* tdt, double tk) {
   const Geo& g = c->g;
   int rc;
-  if ((rc = enq_newton<NRV>(c, 0, 1.0e-5, 200, 1))) return rc;
   long long ns = slab_count(g) - g.nint;
   const bool jet = jet_face(g.bc[0]) || jet_face(g.bc[1]);
   if (!jet) {
@@ -366,10 +388,9 @@ int enq_update_primitives_after(izem_ctx* c, int stage = -1) {
     else if (g.bc[f] == IZEM_BC_EXTRAPOLATION) ext |= 1 << f;
     else dir |= 1 << f;
   }
-  const double tk3[3] = {0.0, 0.5, 1.0};
   JetArgs ja = c->jet;
-  ja.tdt = stage >= 0 ? c->d_dt : c->d_dt + 2;
-  ja.tk = stage >= 0 ? tk3[stage] : 0.0;
+  ja.tdt = tdt;
+  ja.tk = tk;
   const long long np = (long long)g.n[1] * g.n[2];
   if (per && (rc = launch(c, "halo", [&] { k_halo<NRV><<<grid_for(ns), kThreads, 0, c->stream>>>(g, 0, c->cfg.forcesum, c->v, c->W_i, per); })))
     return rc;
@@ -390,6 +411,17 @@ int enq_update_primitives_after(izem_ctx* c, int stage = -1) {
   if ((rc = launch(c, "halo", [&] { k_halo<NRV><<<grid_for(ns), kThreads, 0, c->stream>>>(g, 2, c->cfg.forcesum, c->v, c->W_i, dir); })))
     return rc;
   return enq_newton<NRV>(c, 1, 1.0e-5, 200, 1);
+}
+
+// upd_prim_var_domain's Newton, then the ghost closure (module_solver.f90:
+// 840-847).  stage: the RK stage whose time goes to the jet faces (timek =
+// time0 + dt tk3(stage)), -1 for time 0 and dt 0.
+template <int NRV>
+int enq_update_primitives_after(izem_ctx* c, int stage = -1) {
+  int rc;
+  if ((rc = enq_newton<NRV>(c, 0, 1.0e-5, 200, 1))) return rc;
+  const double tk3[3] = {0.0, 0.5, 1.0};
+  return enq_boundaries<NRV>(c, stage >= 0 ? c->d_dt : c->d_dt + 2, stage >= 0 ? tk3[stage] : 0.0);
 }
 
 template <int NRV>
@@ -449,7 +481,8 @@ int do_update_primitives(izem_ctx* c) {
   return enq_update_primitives_after<NRV>(c);
 }
 
-// reaction_selec tail (module_reaction.f90:83-86)
+// reaction_selec tail (module_reaction.f90:83-86): upd_prim_var_woT, then
+// the ghost closure given the half step and the time (d_dt[4], d_dt[5]).
 template <int NRV>
 int do_chem_after(izem_ctx* c) {
   const Geo& g = c->g;
@@ -458,10 +491,7 @@ int do_chem_after(izem_ctx* c) {
          k_prim_woT<NRV><<<grid_for(g.nint), kThreads, 0, c->stream>>>(g, c->v, c->T, c->W_i, c->cp, c->ha);
        })))
     return rc;
-  long long ns = slab_count(g) - g.nint;
-  if ((rc = launch(c, "halo", [&] { k_halo<NRV><<<grid_for(ns), kThreads, 0, c->stream>>>(g, 0, c->cfg.forcesum, c->v, c->W_i); })))
-    return rc;
-  return enq_newton<NRV>(c, 1, 1.0e-5, 200, 1);
+  return enq_boundaries<NRV>(c, c->d_dt + 4, 0.0);
 }
 
 template <int NRV>
@@ -660,7 +690,7 @@ int ctx_alloc(izem_ctx* c) {
       (e = alloc(&c->ha, nrv * nc)) || (e = alloc(&c->v0, nv * ni)) || (e = alloc(&c->f, nv * ni)) ||
       (e = alloc(&c->prim, PR_N * nc)) || (e = alloc(&c->Xa, nrv * nc)) || (e = alloc(&c->fhat, nv * maxf)) ||
       (e = alloc(&c->fd, (15 + 3 * nrv) * nc)) || (e = alloc(&c->tau, 6 * nc)) || (e = alloc(&c->qv, 3 * nc)) ||
-      (e = alloc(&c->d_dt, 4)))
+      (e = alloc(&c->d_dt, 6)))
     return ctx_fail(c, e == cudaErrorMemoryAllocation ? IZEM_ERR_NOMEM : IZEM_ERR_CUDA, "device allocation", e);
   for (int d = 0; d < 3; ++d)
     if ((e = alloc(&c->dxi[d], g.g[d]))) return ctx_fail(c, IZEM_ERR_CUDA, "device allocation", e);
@@ -669,8 +699,10 @@ int ctx_alloc(izem_ctx* c) {
   CK(cudaMalloc(&c->d_status, sizeof(DevStatus)));
   CK(cudaMemset(c->d_status, 0, sizeof(DevStatus)));
   CK(cudaMallocHost(&c->h_status, sizeof(DevStatus)));
-  CK(cudaMallocHost(&c->h_dt, 2 * sizeof(double)));
-  CK(cudaMemset(c->d_dt, 0, 4 * sizeof(double)));   // dt, time0 of the step; zeros for calls outside rk3
+  CK(cudaMallocHost(&c->h_dt, 4 * sizeof(double)));
+  // dt, time0 of the RK3 step; zeros for calls outside rk3; the half step
+  // and time of the last chemistry step
+  CK(cudaMemset(c->d_dt, 0, 6 * sizeof(double)));
   // zero the arrays whose ghost corners are never written
   CK(cudaMemset(c->v, 0, nv * nc * sizeof(double)));
   CK(cudaMemset(c->fd, 0, (15 + 3 * nrv) * nc * sizeof(double)));
@@ -707,6 +739,23 @@ void izem_gpu_destroy(izem_ctx* c) {
   if (c->side) cudaStreamDestroy(c->side);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
+}
+
+void izem_jet_reference(izem_jet* p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof(*p));
+  // bc_inflowjet's constants (module_BCs.f90:1680-1700) and bc_nscbc_out's
+  // far-field pressure (:2390)
+  p->width = 0.0010;
+  p->ramp = 0.0001;
+  p->T_jet = 1000.0;
+  p->T_co = 300.0;
+  p->p_jet = 101325.0 * 15.0;
+  p->p_co = 101325.0;
+  p->u_jet = 0.0;
+  p->u_co = 20.0;
+  p->y_fuel = 1.0;
+  p->p_far = 94232.25;
 }
 
 int izem_gpu_newton_stats(izem_ctx* c, int* max_iters, int* unconverged, int reset) {
@@ -932,11 +981,10 @@ static int chem_finish(izem_ctx* c, int mode, int sur_rc, double* DTmax) {
   return IZEM_OK;
 }
 
-int izem_gpu_chem_step(izem_ctx* c, double dt, int mode, double* DTmax) {
+int izem_gpu_chem_step(izem_ctx* c, double dt, double time, int mode, double* DTmax) {
   if (!c || !DTmax) return IZEM_ERR_ARG;
-  if (jet_face(c->cfg.bc[0]) || jet_face(c->cfg.bc[1]))
-    return ctx_fail(c, IZEM_ERR_STATE, "the chemistry step is built for periodic and extrapolation faces only",
-                    cudaSuccess);
+  if ((jet_face(c->cfg.bc[0]) || jet_face(c->cfg.bc[1])) && !c->have_coords)
+    return ctx_fail(c, IZEM_ERR_STATE, "jet faces need izem_gpu_set_coords", cudaSuccess);
   if (!c->have_mech) return ctx_fail(c, IZEM_ERR_STATE, "no mechanism set", cudaSuccess);
   if (mode != IZEM_CHEM_BDF && mode != IZEM_CHEM_MLP) return ctx_fail(c, IZEM_ERR_ARG, "unknown chemistry mode", cudaSuccess);
   if (mode == IZEM_CHEM_MLP && !c->sur_m) return ctx_fail(c, IZEM_ERR_STATE, "no surrogate set", cudaSuccess);
@@ -959,6 +1007,10 @@ int izem_gpu_chem_step(izem_ctx* c, double dt, int mode, double* DTmax) {
   f.tref_i = 1.0 / c->adi.t_ref;
   f.rho_cgs = c->adi.rho_ref * 1.0e-3;
   f.dt_phys = dt * c->adi.time_ref;
+  // the half step and the time that the boundary closure of the tail reads
+  c->h_dt[2] = dt;
+  c->h_dt[3] = time;
+  CK(cudaMemcpyAsync(c->d_dt + 4, c->h_dt + 2, 2 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   CK(cudaMemsetAsync(c->d_chem_stats, 0, sizeof(ChemStats), c->stream));
   int sur_rc = IZEM_OK;
   const bool skip = mode == IZEM_CHEM_BDF && c->skip_on;
@@ -1195,23 +1247,27 @@ int izem_gpu_set_coords(izem_ctx* c, const double* x, const double* y, const dou
   }
   CK(cudaMemcpy(c->d_y, y, c->g.n[1] * sizeof(double), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(c->d_z, z, c->g.n[2] * sizeof(double), cudaMemcpyHostToDevice));
-  const izem_adi& a = c->adi;
   JetArgs& j = c->jet;
   j.y = c->d_y;
   j.z = c->d_z;
   j.lx = lx;
   j.dxi0 = c->dxi[0];
-  // bc_inflowjet's constants (module_BCs.f90:1680-1700) and bc_nscbc_out's
-  // far-field pressure (:2390), in code units as the routines divide them
-  j.hbuse = 0.0010 / a.l_ref;
-  j.tmaxy = 0.0001 / a.time_ref;
-  j.u2 = 20.0 / a.u_ref;
-  j.T1 = 1000.0 / a.t_ref;
-  j.T2 = 300.0 / a.t_ref;
-  j.P1 = 101325.0 * 15.0 / a.p_ref;
-  j.P2 = 101325.0 / a.p_ref;
-  j.pinf = 94232.25 / a.p_ref;
+  izem_jet_reference(&c->jet_par);
+  jet_args(c);
   c->have_coords = true;
+  return IZEM_OK;
+}
+
+int izem_gpu_set_jet(izem_ctx* c, const izem_jet* p) {
+  if (!c || !p) return IZEM_ERR_ARG;
+  if (!c->have_coords) return ctx_fail(c, IZEM_ERR_STATE, "izem_gpu_set_jet needs izem_gpu_set_coords first", cudaSuccess);
+  if (!(p->width > 0.0) || !(p->ramp >= 0.0) || !(p->T_jet > 0.0) || !(p->T_co > 0.0) || !(p->p_jet > 0.0) ||
+      !(p->p_co > 0.0) || !(p->u_jet >= 0.0) || !(p->y_fuel >= 0.0 && p->y_fuel <= 1.0) || !(p->p_far > 0.0) ||
+      !(p->turb >= 0.0))
+    return ctx_fail(c, IZEM_ERR_ARG, "jet parameters out of range", cudaSuccess);
+  drop_graphs(c);   // captured graphs hold the jet constants by value
+  c->jet_par = *p;
+  jet_args(c);
   return IZEM_OK;
 }
 

@@ -390,6 +390,12 @@ struct JetArgs {
   double tk;
   double lx;            // domain length in x (code units)
   double hbuse, tmaxy, u2, T1, T2, P1, P2, pinf;   // the routines' constants in code units
+  double u1;            // jet velocity (code units); 0: 1.01 x the jet's sound speed
+  double ya1;           // fuel mass fraction of the jet
+  double turb;          // relative amplitude of the seeded fluctuations
+  double tq_i;          // 1 / the time quantum of the fluctuations (code units)
+  unsigned long long seed;
+  int planar;           // tanh profile in |y| instead of sqrt(y^2 + z^2)
   const double* dxi0;   // x metrics, ghosted index
 };
 
@@ -402,9 +408,9 @@ __global__ void k_bc_inflowjet(Geo g, JetArgs ja, double* __restrict__ v) {
   if (idx >= (long long)g.n[1] * g.n[2]) return;
   const int j = (int)(idx % g.n[1]) + 1, k = (int)(idx / g.n[1]) + 1;
   const double time = ja.tdt[1] + ja.tdt[0] * ja.tk;
-  double T_1 = ja.T1, P_1 = ja.P1, Ya_1 = 1.0;
+  double T_1 = ja.T1, P_1 = ja.P1, Ya_1 = ja.ya1;
   const double T_2 = ja.T2, P_2 = ja.P2, Ya_2 = 0.0, u_2 = ja.u2;
-  if (time <= ja.tmaxy) {
+  if (ja.tmaxy > 0.0 && time <= ja.tmaxy) {
     P_1 = (P_2 - (P_2 - P_1) * (time / ja.tmaxy) * (time / ja.tmaxy) * (time / ja.tmaxy));
     Ya_1 = (Ya_2 - (Ya_2 - Ya_1) * (time / ja.tmaxy) * (time / ja.tmaxy) * (time / ja.tmaxy));
     T_1 = (T_2 - (T_2 - T_1) * (time / ja.tmaxy) * (time / ja.tmaxy) * (time / ja.tmaxy));
@@ -422,15 +428,22 @@ __global__ void k_bc_inflowjet(Geo g, JetArgs ja, double* __restrict__ v) {
   double gamma = c_thd.gam2 * Ws_i / cps;
   gamma = 1.0 / (1.0 - gamma);
   const double cs = sqrt(gamma * Ws_i * T_1);
-  const double u_1 = 1.01 * cs;
+  const double u_1 = ja.u1 > 0.0 ? ja.u1 : 1.01 * cs;
   const double delt = 1.0 / (0.04 * ja.hbuse), y0 = ja.hbuse / 2.0;
   const double yy = ja.y[j - 1], zz = ja.z[k - 1];
-  const double rrr = sqrt(yy * yy + zz * zz);
+  const double rrr = ja.planar ? fabs(yy) : sqrt(yy * yy + zz * zz);
   const double th = tanh((rrr - y0) * delt);
-  const double ux = 0.5 * ((u_1 + u_2) - (u_1 - u_2) * th);
+  double ux = 0.5 * ((u_1 + u_2) - (u_1 - u_2) * th);
   const double T = 0.5 * ((T_1 + T_2) - (T_1 - T_2) * th);
   const double P = 0.5 * ((P_1 + P_2) - (P_1 - P_2) * th);
-  const double vy = 0.0, wz = 0.0;
+  double vy = 0.0, wz = 0.0;
+  if (ja.turb > 0.0) {
+    const double a = ja.turb * u_1 * (0.5 * (1.0 - th));
+    const long long n = (long long)floor(time * ja.tq_i);
+    ux = ux + a * jet_noise(ja.seed, j, k, 0, n);
+    vy = a * jet_noise(ja.seed, j, k, 1, n);
+    wz = a * jet_noise(ja.seed, j, k, 2, n);
+  }
 #pragma unroll
   for (int l = 0; l < NRV; ++l) Ya[l] = 0.0;
   if constexpr (NRV == 2) {

@@ -88,6 +88,7 @@ struct izem_mlp {
   uint8_t *wt[NL] = {}, *wn[NL] = {};            // BF16 weights as K-slabs: W^T (forward), W (backward)
   double* d_loss = nullptr;
   int step = 0;
+  int residual = 0;                  // trained on the increment minus dt f(y0) (izem_mlp_set_residual)
   int device = 0;                    // device current at izem_mlp_create; holds every buffer
   cudaStream_t s = nullptr;
   // inference buffers: BF16 features (rows x 16) and FP32 output (rows x 16)
@@ -404,6 +405,35 @@ int izem_mlp_get_params(izem_mlp* m, float* const* W, float* const* b) {
   return IZEM_OK;
 }
 
+int izem_mlp_set_residual(izem_mlp* m, int residual) {
+  if (!m) return IZEM_ERR_ARG;
+  m->residual = residual != 0;
+  return IZEM_OK;
+}
+
+int izem_gpu_reactor_rhs(const izem_mech* mech, int n, const double* T, const double* rho, const double* Y,
+                         double* zdot, int device_ptrs) {
+  if (!mech || n <= 0 || !T || !rho || !Y || !zdot || mech->kk != 9) return IZEM_ERR_ARG;
+  (void)cudaGetLastError();
+  if (chem_upload_mech(mech) != cudaSuccess) return IZEM_ERR_CUDA;
+  if (device_ptrs) {
+    if (chem_launch_rhs(n, T, rho, Y, zdot, 0) != cudaSuccess) return IZEM_ERR_CUDA;
+    return cudaStreamSynchronize(0) == cudaSuccess ? IZEM_OK : IZEM_ERR_CUDA;
+  }
+  const size_t n8 = (size_t)n * 8;
+  double *dT = nullptr, *dr = nullptr, *dY = nullptr, *dz = nullptr;
+  int rc = IZEM_OK;
+  if (cudaMalloc(&dT, n8) || cudaMalloc(&dr, n8) || cudaMalloc(&dY, 9 * n8) || cudaMalloc(&dz, 10 * n8)) {
+    rc = IZEM_ERR_NOMEM;
+  } else if (cudaMemcpy(dT, T, n8, cudaMemcpyHostToDevice) || cudaMemcpy(dr, rho, n8, cudaMemcpyHostToDevice) ||
+             cudaMemcpy(dY, Y, 9 * n8, cudaMemcpyHostToDevice) || chem_launch_rhs(n, dT, dr, dY, dz, 0) ||
+             cudaMemcpy(zdot, dz, 10 * n8, cudaMemcpyDeviceToHost)) {
+    rc = IZEM_ERR_CUDA;
+  }
+  cudaFree(dT); cudaFree(dr); cudaFree(dY); cudaFree(dz);
+  return rc;
+}
+
 int izem_mlp_set_norm(izem_mlp* m, const float* norm) {
   if (!m || !norm) return IZEM_ERR_ARG;
   std::memcpy(m->norm, norm, sizeof(m->norm));
@@ -562,6 +592,7 @@ int izem_gpu_psr_batch_mlp(izem_mlp* m, izem_mlp* m2, const izem_mech* mech, int
                            double* dT_pred, int* stats3, float* ms2) {
   if (!m || !mech || n <= 0 || !T || !rho || !Y || !dt || !gate10 || !kncf || mech->kk != 9) return IZEM_ERR_ARG;
   if (nele <= 0 || nele > 8) return IZEM_ERR_ARG;
+  if (m2 && m2->residual != m->residual) return IZEM_ERR_ARG;   // one target form per ensemble
   const int CH = 1 << 20;
   const int chunk = n < CH ? n : CH;
   const int nch = (n + chunk - 1) / chunk;
@@ -619,7 +650,7 @@ int izem_gpu_psr_batch_mlp(izem_mlp* m, izem_mlp* m2, const izem_mech* mech, int
     cudaEventRecord(ev[3 + 2 * ci], s);
     chem_launch_decode_gate(cn, m->iout, m2 ? m2->iout : nullptr, OUTP, m->d_norm, m2 ? m2->d_norm : nullptr, dT + c0,
                             drho + c0, dY + (size_t)c0 * kk, ddt + c0, gate10, m->g_kncf, nele, m->g_list, c0,
-                            m->g_count, ddTp ? ddTp + c0 : nullptr, m->g_stats, s);
+                            m->g_count, ddTp ? ddTp + c0 : nullptr, m->g_stats, m->residual, s);
   }
   if (rc == IZEM_OK && chem_launch_list(m->g_list, m->g_count, dT, drho, dY, ddt, m->g_counter, m->g_stats, s) !=
                            cudaSuccess)

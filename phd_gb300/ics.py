@@ -175,6 +175,96 @@ def mixing_layer_block(nx=64, ny=64, nz=32, seed=SEED, lib_dscalar=None):
                         lib_dscalar=lib_dscalar)
 
 
+def jet_les(nx=512, ny=512, nz=256, dx=47e-6, width=2e-3, u_jet=300.0, u_co=10.0, T_jet=1000.0, T_co=1200.0,
+            y_fuel=0.5, turb=0.02, seed=SEED, lib_dscalar=None):
+    """Reacting planar H2/air jet: a slot of `width` (2 mm) in y issuing
+    H2/N2 (y_fuel H2 by mass, the rest N2) at u_jet (300 m/s) and T_jet into
+    air (O2/N2 0.233/0.767) at T_co (1200 K) and u_co (10 m/s), 1 atm; the
+    9-species set.  Uniform spacing dx; x from the nozzle plane, y centred
+    on the slot, z periodic.  Faces: the jet inflow on W (planar profile,
+    no ramp, seeded fluctuations of relative amplitude turb), the
+    characteristic outflow on E, extrapolation in y, periodic in z.  The
+    initial field carries the inflow profile through the domain (the tanh
+    profile of the inflow in |y|) with seeded velocity fluctuations of the
+    same amplitude (numpy PCG64(seed)).  Returns cfg, thd, adi, dxi, state,
+    info; info["coords"], info["lx"] and info["jet"] (capi.IzemJet) set up
+    the jet faces."""
+    from .capi import BC_INFLOWJET, BC_NSCBC_OUT, IzemJet
+    a = constants()
+    sp = load_species("h2air9")
+    thd = thd_init(sp, a)
+    names = sp["names"]
+    ih2, io2, in2 = names.index("H2"), names.index("O2"), names.index("N2")
+    x = np.arange(nx) * dx
+    y = (np.arange(ny) - 0.5 * (ny - 1)) * dx
+    z = np.arange(nz) * dx
+    ng = 3
+    # profiles across the slot (they depend on y only)
+    th = np.tanh((np.abs(y) - 0.5 * width) / (0.04 * width))
+    Ys = np.zeros((ny, len(names)))
+    Ys[:, ih2] = 0.5 * (y_fuel - y_fuel * th)
+    Ys[:, io2] = 0.5 * (0.233 + 0.233 * th)
+    Ys[:, in2] = 0.5 * ((1.0 - y_fuel + 0.767) - (1.0 - y_fuel - 0.767) * th)
+    T_y = 0.5 * ((T_jet + T_co) - (T_jet - T_co) * th)
+    u_y = 0.5 * ((u_jet + u_co) - (u_jet - u_co) * th)
+    Wmix_i = np.einsum("yk,k->y", Ys, 1.0 / (np.array(sp["W_gmol"]) * 1e-3))
+    rho_y = 101325.0 / (a["r_ref"] * Wmix_i * T_y)
+    # code units (as _state_from_primitives converts them)
+    rho_c = rho_y / a["rho_ref"]
+    T_c = T_y / a["t_ref"]
+    W_i = np.zeros_like(T_c)
+    for k in range(len(names)):
+        W_i += Ys[:, k] * thd.Wc_i[k]
+    P_c = rho_c * T_c * W_i
+    hm = np.einsum("yk,yk->y", ha_code(thd, T_c), Ys)
+    # seeded velocity fluctuations in the jet, drawn over the interior
+    rng = np.random.Generator(np.random.PCG64(seed))
+    amp = (turb * u_jet * 0.5 * (1.0 - th))[None, :, None]
+    shp = (nx, ny, nz)
+    u = (u_y[None, :, None] + amp * rng.uniform(-1.0, 1.0, shp)) / a["u_ref"]
+    v = (amp * rng.uniform(-1.0, 1.0, shp)) / a["u_ref"]
+    w = (amp * rng.uniform(-1.0, 1.0, shp)) / a["u_ref"]
+    # ghosted state, ghosts by zero-gradient extension of the interior
+    gsh = (nx + 2 * ng, ny + 2 * ng, nz + 2 * ng)
+    jy = np.clip(np.arange(ny + 2 * ng) - ng, 0, ny - 1)   # ghosted y -> interior y
+
+    def ext(a3):
+        out = np.empty(gsh, order="F")
+        out[ng:ng + nx, ng:ng + ny, ng:ng + nz] = a3
+        out[:ng] = out[ng:ng + 1]
+        out[ng + nx:] = out[ng + nx - 1:ng + nx]
+        out[:, :ng] = out[:, ng:ng + 1]
+        out[:, ng + ny:] = out[:, ng + ny - 1:ng + ny]
+        out[:, :, :ng] = out[:, :, ng:ng + 1]
+        out[:, :, ng + nz:] = out[:, :, ng + nz - 1:ng + nz]
+        return out
+
+    vg = np.empty(gsh + (5 + len(names),), order="F")
+    rho3 = rho_c[None, :, None]
+    vg[..., 0] = rho_c[jy][None, :, None]
+    vg[..., 1] = ext(rho3 * u)
+    vg[..., 2] = ext(rho3 * v)
+    vg[..., 3] = ext(rho3 * w)
+    vg[..., 4] = ext(rho3 * hm[None, :, None] - P_c[None, :, None] + 0.5 * rho3 * (u * u + v * v + w * w))
+    for k in range(len(names)):
+        vg[..., 5 + k] = (rho_c * Ys[:, k])[jy][None, :, None]
+    del u, v, w
+    Tg = np.empty(gsh, order="F")
+    Tg[...] = T_c[jy][None, :, None]
+    state = {"v": vg, "T": Tg, "W_i": np.zeros(gsh, order="F"), "cp": np.zeros(gsh, order="F"),
+             "ha": np.zeros(gsh + (len(names),), order="F"), "shock_sensor": np.zeros(gsh, dtype=np.uint8, order="F")}
+    bc = (BC_INFLOWJET, BC_NSCBC_OUT, BC_EXTRAPOLATION, BC_EXTRAPOLATION, BC_PERIODIC, BC_PERIODIC)
+    cfg = make_cfg(nx, ny, nz, len(names), bc=bc)
+    dxi = [grid_dxi(c, 3, a, lib_dscalar) for c in (x, y, z)]
+    L = a["l_ref"]
+    jet = IzemJet(width=width, ramp=0.0, T_jet=T_jet, T_co=T_co, p_jet=101325.0, p_co=101325.0, u_jet=u_jet,
+                  u_co=u_co, y_fuel=y_fuel, p_far=101325.0, turb=turb, planar=1, reserved=0, seed=seed)
+    info = {"name": "reacting planar H2/air jet %dx%dx%d" % (nx, ny, nz), "seed": seed,
+            "coords": (x / L, y / L, z / L), "lx": (x[-1] - x[0]) / L, "time_ref": a["time_ref"], "jet": jet,
+            "width_m": width, "dx_m": dx}
+    return cfg, thd, adi_struct(a), dxi, state, info
+
+
 def batched_reactors(n, seed=SEED):
     """Independent H2/air reactors: T ~ U[800, 2400] K, p ~ U[1, 10] atm,
     equivalence ratio ~ U[0.3, 3], progress c ~ U[0, 1] blending the unburnt

@@ -19,7 +19,7 @@ import os
 import numpy as np
 
 from . import capi
-from .capi import IzemAdi, IzemCfg, IzemEglib, IzemMech, IzemThd
+from .capi import IzemAdi, IzemCfg, IzemEglib, IzemJet, IzemMech, IzemThd
 
 _LIB = None
 LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "libizem_gpu.so")
@@ -69,7 +69,7 @@ def load_library(path=None):
         "izem_gpu_synchronize": (C.c_int, [P]),
         "izem_metrics_dscalar": (C.c_int, [C.c_int, C.c_int, _dp, _dp]),
         "izem_gpu_set_mechanism": (C.c_int, [P, C.POINTER(IzemMech)]),
-        "izem_gpu_chem_step": (C.c_int, [P, C.c_double, C.c_int, _dp]),
+        "izem_gpu_chem_step": (C.c_int, [P, C.c_double, C.c_double, C.c_int, _dp]),
         "izem_gpu_chem_stats": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_ulonglong)]),
         "izem_gpu_psr_batch": (C.c_int, [C.POINTER(IzemMech), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                          C.c_void_p, C.c_void_p, C.c_int, C.POINTER(C.c_float)]),
@@ -83,6 +83,8 @@ def load_library(path=None):
         "izem_gpu_set_chem_skip": (C.c_int, [P, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_int]),
         "izem_gpu_set_les": (C.c_int, [P, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double]),
         "izem_gpu_set_coords": (C.c_int, [P, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double]),
+        "izem_gpu_set_jet": (C.c_int, [P, C.POINTER(IzemJet)]),
+        "izem_jet_reference": (None, [C.POINTER(IzemJet)]),
         "izem_gpu_chem_autotune": (C.c_int, [C.POINTER(IzemMech), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                                              C.c_void_p, C.c_int, C.c_char_p, C.c_int]),
         "izem_gpu_chem_surrogate_stats": (C.c_int, [P, C.POINTER(C.c_longlong), C.POINTER(C.c_int),
@@ -315,6 +317,11 @@ class IzemGPU:
         xs = [np.ascontiguousarray(a, dtype=np.float64) for a in (x, y, z)]
         self._check(self.lib.izem_gpu_set_coords(self.h, *[a.ctypes.data for a in xs], float(lx)), "set_coords")
 
+    def set_jet(self, jet):
+        """Jet-face parameters (capi.IzemJet; after set_coords)."""
+        self._jet = jet
+        self._check(self.lib.izem_gpu_set_jet(self.h, C.byref(jet)), "set_jet")
+
     def set_les(self, mu_sgs_factor=0.18, sc_sgs=0.7, pr_sgs=0.7, percent_weight_sgs=70.0, enable=True):
         """[IFLES] LES = T, MU_SGS_MODEL = SMAGORINSKY under EGLIB
         (izem_gpu_set_les); the deck defaults are the keyword defaults."""
@@ -373,13 +380,15 @@ class IzemGPU:
                     "chem_surrogate_stats")
         return {"cells": n.value, "fallback": fb.value, "ms": a.value, "ms_network": b.value}
 
-    def reaction_selec(self, dt, mode=0):
-        """One Strang chemistry half step of length dt (code units); returns
+    def reaction_selec(self, dt, mode=0, time=0.0):
+        """One Strang chemistry half step of length dt (code units) at the
+        given time (the jet faces' boundary closure reads both); returns
         DTmax [K] (module_reaction.f90:47-100).  mode CHEM_BDF (0) integrates
         every cell with the BDF method, CHEM_MLP (1) uses the surrogate set by
         set_surrogate with BDF fallback."""
         d = C.c_double()
-        self._check(self.lib.izem_gpu_chem_step(self.h, float(dt), int(mode), C.byref(d)), "chem_step")
+        self._check(self.lib.izem_gpu_chem_step(self.h, float(dt), float(time), int(mode), C.byref(d)),
+                    "chem_step")
         return d.value
 
     def chem_stats(self):
@@ -445,7 +454,7 @@ class TimeLoop:
         self.dt4 = None
 
     def chem(self, dt):
-        return self.s.reaction_selec(dt, mode=self.mode)
+        return self.s.reaction_selec(dt, mode=self.mode, time=self.time)
 
     def step(self, dt=None):
         self.dt4, dtmin = self.s.timestep(DTmax=self.DTmax, dtmin=self.dtmin)

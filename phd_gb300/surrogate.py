@@ -40,6 +40,9 @@ def _bind(lib):
         "izem_mlp_set_params": (C.c_int, [P, fpp, fpp]),
         "izem_mlp_get_params": (C.c_int, [P, fpp, fpp]),
         "izem_mlp_set_norm": (C.c_int, [P, C.POINTER(C.c_float)]),
+        "izem_mlp_set_residual": (C.c_int, [P, C.c_int]),
+        "izem_gpu_reactor_rhs": (C.c_int, [C.POINTER(IzemMech), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                           C.c_void_p, C.c_int]),
         "izem_mlp_forward": (C.c_int, [P, C.c_int, C.c_void_p, C.c_void_p]),
         "izem_mlp_fallback_cells": (C.c_int, [P, C.c_void_p, C.c_int, C.POINTER(C.c_int)]),
         "izem_mlp_grads": (C.c_int, [P, C.c_int, C.c_void_p, C.c_void_p, C.POINTER(C.c_double), fpp, fpp]),
@@ -93,6 +96,7 @@ class Surrogate:
         if rc:
             raise IzemError(rc, "izem_mlp_create")
         self.h = h
+        self.residual = False
         W, b = he_init(seed)
         self.set_params(W, b)
         self.norm = np.concatenate([np.zeros(IN), np.ones(IN), np.zeros(OUT), np.ones(OUT)]).astype(np.float32)
@@ -125,6 +129,14 @@ class Surrogate:
         if rc:
             raise IzemError(rc, "izem_mlp_get_params")
         return W, b
+
+    def set_residual(self, residual):
+        """The network predicts the increment minus dt f(y0) (see
+        explicit_increment); the gated step adds dt f(y0) back."""
+        self.residual = bool(residual)
+        rc = self.lib.izem_mlp_set_residual(self.h, int(self.residual))
+        if rc:
+            raise IzemError(rc, "izem_mlp_set_residual")
 
     def set_norm(self, norm):
         self.norm = np.ascontiguousarray(norm, dtype=np.float32)
@@ -357,14 +369,30 @@ def flow_reactors(g, mech, dt, n_max=1 << 20, spread=0.5, seed=5, age=0.0):
     return T, rho, Y, dtp
 
 
-def label(mech, T, rho, Y, dt):
-    """FP64 BDF labels of reactors: raw features and targets (dY_k, dT)."""
+def explicit_increment(mech, T, rho, Y, dt):
+    """dt f(y0) in the target order (dY_1..dY_9, dT): the reactor
+    right-hand side at the start state (izem_gpu_reactor_rhs) times dt."""
+    lib = _bind(load_library())
+    T = np.ascontiguousarray(T, dtype=np.float64)
+    rho = np.ascontiguousarray(rho, dtype=np.float64)
+    Y = np.ascontiguousarray(Y, dtype=np.float64)
+    z = np.zeros((len(T), mech.kk + 1))
+    rc = lib.izem_gpu_reactor_rhs(C.byref(mech), len(T), T.ctypes.data, rho.ctypes.data, Y.ctypes.data, z.ctypes.data, 0)
+    if rc:
+        raise IzemError(rc, "izem_gpu_reactor_rhs")
+    return np.concatenate([z[:, 1:], z[:, :1]], axis=1) * np.asarray(dt)[:, None]
+
+
+def label(mech, T, rho, Y, dt, explicit=False):
+    """FP64 BDF labels of reactors: raw features and targets (dY_k, dT);
+    with explicit, also dt f(y0) (explicit_increment)."""
     wt = np.array([mech.wt[k] for k in range(mech.kk)])
     X = features(T, rho, Y, dt, wt)
+    E = explicit_increment(mech, T, rho, Y, dt) if explicit else None
     T1, Y1 = T.copy(), Y.copy()
     psr_batch(mech, T1, rho.copy(), Y1, dt.copy())
     Yt = np.concatenate([Y1 - Y, (T1 - T)[:, None]], axis=1)
-    return X, Yt
+    return (X, Yt, E) if explicit else (X, Yt)
 
 
 def flow_training_set(g, mech, dt, n_max=1 << 20, spread=0.5, seed=5, age=0.0):
@@ -373,14 +401,18 @@ def flow_training_set(g, mech, dt, n_max=1 << 20, spread=0.5, seed=5, age=0.0):
     return label(mech, *flow_reactors(g, mech, dt, n_max=n_max, spread=spread, seed=seed, age=age))
 
 
-def train_on(X, Yt, members=2, seed=31, epochs=24, batch=4096, lr=1e-3):
+def train_on(X, Yt, members=2, seed=31, epochs=24, batch=4096, lr=1e-3, E=None):
     """Train `members` networks on raw features/targets (different
-    initialisations and shuffles, step-decayed learning rate)."""
+    initialisations and shuffles, step-decayed learning rate).  With E (the
+    explicit increments dt f(y0)), the networks learn Yt - E and are marked
+    residual: the gated step adds dt f(y0) back."""
     nets = []
+    tgt = Yt if E is None else Yt - E
     for q in range(members):
         s = Surrogate(seed=seed + 1000 * (q + 1))
-        s.fit_norm(X, Yt)
-        xn, tn = s.normalise(X, Yt)
+        s.set_residual(E is not None)
+        s.fit_norm(X, tgt)
+        xn, tn = s.normalise(X, tgt)
         for stage, f in enumerate((1.0, 0.3, 0.1)):
             s.train(xn, tn, epochs=max(1, epochs // 3), batch=batch, lr=lr * f, seed=seed + 17 * q + stage)
         nets.append(s)

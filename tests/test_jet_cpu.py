@@ -79,9 +79,64 @@ def test_nscbc_outflow_writes_one_state_and_steps_stay_finite():
     assert np.isfinite(st["v"]).all() and (st["T"][ng:-ng, ng:-ng, ng:-ng] > 0).all()
 
 
-def test_jet_faces_reject_chemistry_and_need_coordinates():
-    cfg, thd, adi, dxi, st, info = ics.jet(lib_dscalar=oracle.metrics_dscalar)
+def test_jet_faces_need_coordinates():
+    """rk3 and the chemistry step refuse a block with jet faces until the
+    coordinates are set."""
+    from phd_gb300.mech import h2_mechanism
+    cfg, thd, adi, dxi, st, info = ics.jet(species="h2air9", lib_dscalar=oracle.metrics_dscalar)
     orc = oracle.Oracle(cfg, thd, adi, *dxi)
     orc.finalize_ic(st)
     with pytest.raises(oracle.OracleError):
         orc.rk3(st, 0.1, 0.0)
+    with pytest.raises(oracle.OracleError):
+        orc.chem_step(st, h2_mechanism(), 0.1, 0.0)
+
+
+def test_planar_jet_inflow_with_the_workload_parameters():
+    """With the reacting-jet workload's parameters (planar 2 mm slot, H2/N2
+    0.5/0.5 at 300 m/s and 1000 K into air at 1200 K and 10 m/s, 1 atm, no
+    ramp) and no fluctuations, the W ghosts hold the tanh profiles in |y|,
+    restated here; with 2 % fluctuations the velocities move by at most 2 %
+    of the jet velocity times the core weight, and two runs draw the same
+    values."""
+    from phd_gb300 import capi
+    cfg, thd, adi, dxi, st0, info = ics.jet_les(12, 64, 8, lib_dscalar=oracle.metrics_dscalar)
+    ng, nrv = cfg.ng, cfg.nrv
+    y = info["coords"][1]
+    jet = info["jet"]
+    runs = []
+    for turb in (0.0, 0.02, 0.02):
+        orc = oracle.Oracle(cfg, thd, adi, *dxi)
+        orc.set_coords(*info["coords"], info["lx"])
+        j = capi.IzemJet(**{f: getattr(jet, f) for f, _ in capi.IzemJet._fields_})
+        j.turb = turb
+        orc.set_jet(j)
+        st = {k: v.copy(order="F") for k, v in st0.items()}
+        orc.finalize_ic(st)
+        _, dt = orc.timestep(st)
+        orc.rk3(st, 0.01 * dt, 0.0)
+        runs.append(st["v"][:ng + 1, ng:-ng, ng:-ng].copy())
+    hb = 2e-3 / adi.l_ref
+    delt, y0 = 1.0 / (0.04 * hb), hb / 2.0
+    T1, T2 = 1000.0 / adi.t_ref, 1200.0 / adi.t_ref
+    P = 101325.0 / adi.p_ref
+    u1, u2 = 300.0 / adi.u_ref, 10.0 / adi.u_ref
+    Wc_i = np.array(thd.Wc_i[:nrv])
+    for jj in (0, 20, 32, 63):
+        th = np.tanh((abs(y[jj]) - y0) * delt)
+        ux = 0.5 * ((u1 + u2) - (u1 - u2) * th)
+        T = 0.5 * ((T1 + T2) - (T1 - T2) * th)
+        Y = np.zeros(nrv)
+        Y[1] = 0.5 * (0.5 - 0.5 * th)
+        Y[3] = 0.5 * (0.233 + 0.233 * th)
+        Y[8] = 0.5 * ((0.5 + 0.767) - (0.5 - 0.767) * th)
+        rho = P / (T * (Y @ Wc_i))
+        want = np.concatenate([[rho, rho * ux, 0.0, 0.0], rho * Y])
+        got = runs[0][:, jj, :][..., [0, 1, 2, 3] + list(range(5, 5 + nrv))]
+        assert np.allclose(got, np.broadcast_to(want, got.shape), rtol=1e-12, atol=1e-14 * rho), (jj, got[0, 0] - want)
+        amp = 0.02 * u1 * 0.5 * (1.0 - th)
+        for c in (1, 2, 3):
+            d = runs[1][:, jj, :, c] / runs[1][:, jj, :, 0] - runs[0][:, jj, :, c] / runs[0][:, jj, :, 0]
+            assert np.all(np.abs(d) <= amp * (1 + 1e-9) + 1e-15)
+    assert np.array_equal(runs[1], runs[2])
+    assert not np.array_equal(runs[0], runs[1])

@@ -114,11 +114,11 @@ def oracle_step(orc, st, mech, loop):
     loop: dict with dtmin, DTmax and time, updated in place.  Returns dt."""
     _, dt = orc.timestep(st, DTmax=loop["DTmax"], dtmin=loop["dtmin"])
     if mech is not None:
-        orc.chem_step(st, mech, 0.5 * dt)
+        orc.chem_step(st, mech, 0.5 * dt, loop["time"])
     orc.rk3(st, dt, loop["time"])
     loop["time"] += dt
     if mech is not None:
-        loop["DTmax"] = orc.chem_step(st, mech, 0.5 * dt)
+        loop["DTmax"] = orc.chem_step(st, mech, 0.5 * dt, loop["time"])
     loop["dtmin"] = dt
     return dt
 
