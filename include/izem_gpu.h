@@ -32,8 +32,20 @@ extern "C" {
  * module_BCs.f90): periodic (comm_cons), bc_extrapolation
  * (:327-412), bc_inflowjet on the W face only (:1646-1791) and bc_nscbc_out
  * on the E face only (:2331-2516); the last two are Dirichlet faces closed by
- * upd_prim_var_dirichlet (:297-314) and need izem_gpu_set_coords. */
-enum { IZEM_BC_PERIODIC = 0, IZEM_BC_EXTRAPOLATION = 1, IZEM_BC_INFLOWJET = 2, IZEM_BC_NSCBC_OUT = 3 };
+ * upd_prim_var_dirichlet (:297-314) and need izem_gpu_set_coords.
+ * IZEM_BC_NOREFLECTION (NOREFLECTION, any face): the ghost points hold the
+ * boundary point's state times 10 (bc_noreflection, :426-512), the Euler
+ * sweep across the face drops its flux difference at the boundary points
+ * (module_weno.f90:620-623, 1002, 1018 and the y, z counterparts), and
+ * every stage adds the one-sided characteristic term of bc_noreflectionweno
+ * (module_weno.f90:2129-4498) after the viscous fluxes. */
+enum {
+  IZEM_BC_PERIODIC = 0,
+  IZEM_BC_EXTRAPOLATION = 1,
+  IZEM_BC_INFLOWJET = 2,
+  IZEM_BC_NSCBC_OUT = 3,
+  IZEM_BC_NOREFLECTION = 4
+};
 enum { IZEM_FACE_W = 0, IZEM_FACE_E, IZEM_FACE_S, IZEM_FACE_N, IZEM_FACE_B, IZEM_FACE_F };
 
 /* Status codes. */
@@ -195,6 +207,16 @@ int  izem_gpu_euler_flux(izem_ctx* ctx, int dir);
  * viscflux_eg_xyz (module_eg_lib.f90:2140-2676, EGLIB precision 1):
  * accumulates into f. */
 int  izem_gpu_visc_flux(izem_ctx* ctx);
+
+/* NR_boundaries (module_BCs.f90:185-212): for each face of kind
+ * IZEM_BC_NOREFLECTION in the order W,E,S,N,B,F, bc_noreflectionweno
+ * (module_weno.f90:2129-4498) adds to f at the face's boundary points
+ * R diag(lambda-) L (dv/dn), with L, R the characteristic vectors at the
+ * point's own state, lambda- the eigenvalues leaving the domain (min(.,0) on
+ * W, S, B; max(.,0) on E, N, F) and dv/dn the one-sided derivative over
+ * 2ng-1 points (wenopar's cnr weights, :199-217).  No-op without such
+ * faces. */
+int  izem_gpu_nr_flux(izem_ctx* ctx);
 
 /* EGLIB linking data for cfg.eglib = 1 (init_eglib + EGINI,
  * module_eg_lib.f90:44-96, eglib/EGini.f:58-301); call once after

@@ -42,6 +42,7 @@ def load():
         "or_shock_sensor": (C.c_int, [P, _dp, _dp, _dp, _u8p]),
         "or_euler_flux": (C.c_int, [P, C.c_int, _dp, _dp, _dp, _dp, _dp, _u8p, _dp]),
         "or_visc_flux": (C.c_int, [P, _dp, _dp, _dp, _dp, _dp, _dp]),
+        "or_nr_flux": (C.c_int, [P, _dp, _dp, _dp, _dp, _dp, _dp]),
         "or_prim_inv_var": (C.c_int, [P, C.c_int, C.c_int, _dp, _dp, _dp, _dp, _dp]),
         "or_force_sumY": (C.c_int, [P, C.c_int, _dp]),
         "or_update_primitives": (C.c_int, [P, _dp, _dp, _dp, _dp, _dp]),
@@ -222,6 +223,12 @@ class Oracle:
     def visc_flux(self, s, fl):
         v, T, W_i, cp, ha = self._arrs(s)
         self._rc(self.lib.or_visc_flux(self.h, _p(v), _p(T), _p(W_i), _p(cp), _p(ha), _p(fl)), "visc_flux")
+
+    def nr_flux(self, s, fl):
+        """NR_boundaries: adds bc_noreflectionweno's term of every
+        non-reflecting face to fl."""
+        v, T, W_i, cp, ha = self._arrs(s)
+        self._rc(self.lib.or_nr_flux(self.h, _p(v), _p(T), _p(W_i), _p(cp), _p(ha), _p(fl)), "nr_flux")
 
     def prim_inv_var(self, s, domain_id, err_mach=False):
         v, T, W_i, cp, ha = self._arrs(s)

@@ -389,6 +389,38 @@ void bc_extrapolation(const Block& b, int face, double* v) {
   }
 }
 
+// bc_noreflection (module_BCs.f90:426-512): the ghost points of a
+// non-reflecting face take the boundary point's conserved variables times
+// 10 (the reference's "garbage" factor); the same loops as bc_extrapolation.
+void bc_noreflection(const Block& b, int face, double* v) {
+  const double garbage = 10.0;
+  for (int l = 0; l < b.nv; ++l) {
+    double* q = v + l * b.ncell;
+    if (face == 0 || face == 1) {
+      for (int k = 1; k <= b.nz; ++k)
+        for (int j = 1; j <= b.ny; ++j)
+          for (int g = 1; g <= b.ng; ++g) {
+            if (face == 0) q[b.id(1 - g, j, k)] = q[b.id(1, j, k)] * garbage;
+            else q[b.id(b.nx + g, j, k)] = q[b.id(b.nx, j, k)] * garbage;
+          }
+    } else if (face == 2 || face == 3) {
+      for (int k = 1; k <= b.nz; ++k)
+        for (int g = 1; g <= b.ng; ++g)
+          for (int i = 1; i <= b.nx; ++i) {
+            if (face == 2) q[b.id(i, 1 - g, k)] = q[b.id(i, 1, k)] * garbage;
+            else q[b.id(i, b.ny + g, k)] = q[b.id(i, b.ny, k)] * garbage;
+          }
+    } else {
+      for (int g = 1; g <= b.ng; ++g)
+        for (int j = 1; j <= b.ny; ++j)
+          for (int i = 1; i <= b.nx; ++i) {
+            if (face == 4) q[b.id(i, j, 1 - g)] = q[b.id(i, j, 1)] * garbage;
+            else q[b.id(i, j, b.nz + g)] = q[b.id(i, j, b.nz)] * garbage;
+          }
+    }
+  }
+}
+
 const int kFaceDomain[6] = {-1, 1, -2, 2, -3, 3};
 const int kDirichletDomain[6] = {-10, 10, -20, 20, -30, 30};
 
@@ -605,6 +637,7 @@ int update_boundaries(Ctx& c, double* v, double* T, double* W_i, double* cp, dou
   for (int f = 0; f < 6; ++f) {
     if (!b.bnd[f]) continue;
     if (b.bc[f] == IZEM_BC_EXTRAPOLATION) bc_extrapolation(b, f, v);
+    else if (b.bc[f] == IZEM_BC_NOREFLECTION) bc_noreflection(b, f, v);
     else if (b.bc[f] == IZEM_BC_INFLOWJET) bc_inflowjet(c, time, v);
     else if (b.bc[f] == IZEM_BC_NSCBC_OUT) bc_nscbc_out(c, dt, T, W_i, cp, v);
     if (is_dirichlet(b.bc[f])) {   // upd_prim_var_dirichlet
@@ -842,6 +875,77 @@ void wenorec(const Weno& w, const double* vp, const double* vm, double& vminus, 
   for (int r = 0; r < ng; ++r) vplus = vplus + omega[r] * vmr[r];
 }
 
+// The left and right characteristic vectors of the flux Jacobian along
+// axis d at one state: euler_LLF_x/_y/_z build them at the Roe state
+// (module_weno.f90:775-951), bc_noreflectionweno at a boundary point's own
+// state (:2224-2418, and the same blocks for the other faces).
+struct CharState {
+  double uc[3];
+  const double* Yc;
+  const double* psi_c;
+  double ht_c, q, cs_c, cs_c_i, b1, b2, xi;
+};
+
+void char_vectors(int d, int nv, int nrv, const CharState& cs, double el[][IZEM_NSMAX + 5],
+                  double er[][IZEM_NSMAX + 5]) {
+  const int t1 = d == 0 ? 1 : 0, t2 = d == 2 ? 1 : 2;
+  const double* uc = cs.uc;
+  const double* Yc = cs.Yc;
+  const double* psi_c = cs.psi_c;
+  const double ht_c = cs.ht_c, q = cs.q, cs_c = cs.cs_c, cs_c_i = cs.cs_c_i, b1 = cs.b1, b2 = cs.b2, xi = cs.xi;
+  const double un = uc[d];
+  double wrk;
+  // left eigenvectors (module_weno.f90:775-874)
+  for (int a = 0; a < nv; ++a)
+    for (int e = 0; e < nv; ++e) el[a][e] = 0.0;
+  el[0][0] = 0.5 * (b1 + un * cs_c_i);
+  el[2][0] = 0.5 * (b1 - un * cs_c_i);
+  for (int a = 0; a < 3; ++a) {
+    if (a == d) {
+      el[0][1 + a] = -0.5 * (b2 * un + cs_c_i);
+      el[2][1 + a] = -0.5 * (b2 * un - cs_c_i);
+    } else {
+      el[0][1 + a] = -0.5 * (b2 * uc[a]);
+      el[2][1 + a] = -0.5 * (b2 * uc[a]);
+    }
+    el[1][1 + a] = b2 * uc[a];
+  }
+  el[0][4] = 0.5 * b2; el[2][4] = 0.5 * b2;
+  el[1][0] = 1.0 - b1; el[1][4] = -b2;
+  el[3][0] = -uc[t1]; el[3][1 + t1] = 1.0;
+  el[4][0] = -uc[t2]; el[4][1 + t2] = 1.0;
+  wrk = 0.5 * b2;
+  for (int l = NIV; l < nv; ++l) el[0][l] = wrk * psi_c[l - NIV];
+  for (int l = NIV; l < nv; ++l) el[1][l] = -el[0][l] - el[0][l];
+  for (int l = NIV; l < nv; ++l) el[2][l] = el[0][l];
+  el[5][0] = (1 + xi) * q;
+  for (int a = 0; a < 3; ++a) el[5][1 + a] = -(1 + xi) * uc[a];
+  el[5][4] = (1 + xi);
+  for (int l = NIV; l < nv; ++l) el[5][l] = xi * psi_c[l - NIV];
+  for (int l = 6; l < nv; ++l) {
+    double Y = Yc[l - 6];
+    el[l][0] = -b1 * Y;
+    for (int a = 0; a < 3; ++a) el[l][1 + a] = b2 * uc[a] * Y;
+    el[l][4] = -b2 * Y;
+  }
+  for (int s1 = 1; s1 <= nrv - 1; ++s1)
+    for (int s2 = 1; s2 <= nrv; ++s2) el[s1 + 5][s2 + 4] = -b2 * Yc[s1 - 1] * psi_c[s2 - 1];
+  for (int l = 1; l <= nrv - 1; ++l) el[l + 5][l + 4] = el[l + 5][l + 4] + 1.0;
+  // right eigenvectors (module_weno.f90:881-951)
+  for (int a = 0; a < nv; ++a)
+    for (int e = 0; e < nv; ++e) er[a][e] = 0.0;
+  er[0][0] = 1.0; er[0][1] = 1.0; er[0][2] = 1.0;
+  er[1 + d][0] = un - cs_c; er[1 + d][1] = un; er[1 + d][2] = un + cs_c;
+  er[1 + t1][0] = uc[t1]; er[1 + t1][1] = uc[t1]; er[1 + t1][2] = uc[t1]; er[1 + t1][3] = 1.0;
+  er[1 + t2][0] = uc[t2]; er[1 + t2][1] = uc[t2]; er[1 + t2][2] = uc[t2]; er[1 + t2][4] = 1.0;
+  er[4][0] = ht_c - un * cs_c; er[4][1] = q; er[4][2] = ht_c + un * cs_c; er[4][3] = uc[t1]; er[4][4] = uc[t2];
+  for (int l = NIV; l < nv; ++l) { er[l][0] = Yc[l - NIV]; er[l][2] = Yc[l - NIV]; }
+  for (int l = NIV + 1; l <= nv; ++l) er[l - 2][l - 1] = 1.0;
+  er[nv - 1][5] = -1.0 / psi_c[nrv - 1];
+  wrk = -1.0 / psi_c[nrv - 1];
+  for (int l = 1; l <= nrv - 1; ++l) er[nv - 1][l + 5] = wrk * psi_c[l - 1];
+}
+
 // euler_LLF_x/_y/_z (module_weno.f90:537-1044, 1055-1590, 1595-2125).
 // The three routines differ only in the sweep axis d and in which velocity
 // components are normal / tangential; they are restated once over d.
@@ -948,55 +1052,11 @@ int euler_flux(Ctx& c, int d, const double* v, const double* T, const double* W_
         double b1 = b2 * q;
         double xi = b1 - b2 * ht_c;
         double un = uc[d];
-        // left eigenvectors (module_weno.f90:775-874)
-        for (int a = 0; a < nv; ++a)
-          for (int e = 0; e < nv; ++e) el[a][e] = 0.0;
-        el[0][0] = 0.5 * (b1 + un * cs_c_i);
-        el[2][0] = 0.5 * (b1 - un * cs_c_i);
-        for (int a = 0; a < 3; ++a) {
-          if (a == d) {
-            el[0][1 + a] = -0.5 * (b2 * un + cs_c_i);
-            el[2][1 + a] = -0.5 * (b2 * un - cs_c_i);
-          } else {
-            el[0][1 + a] = -0.5 * (b2 * uc[a]);
-            el[2][1 + a] = -0.5 * (b2 * uc[a]);
-          }
-          el[1][1 + a] = b2 * uc[a];
-        }
-        el[0][4] = 0.5 * b2; el[2][4] = 0.5 * b2;
-        el[1][0] = 1.0 - b1; el[1][4] = -b2;
-        el[3][0] = -uc[t1]; el[3][1 + t1] = 1.0;
-        el[4][0] = -uc[t2]; el[4][1 + t2] = 1.0;
-        wrk = 0.5 * b2;
-        for (int l = NIV; l < nv; ++l) el[0][l] = wrk * psi_c[l - NIV];
-        for (int l = NIV; l < nv; ++l) el[1][l] = -el[0][l] - el[0][l];
-        for (int l = NIV; l < nv; ++l) el[2][l] = el[0][l];
-        el[5][0] = (1 + xi) * q;
-        for (int a = 0; a < 3; ++a) el[5][1 + a] = -(1 + xi) * uc[a];
-        el[5][4] = (1 + xi);
-        for (int l = NIV; l < nv; ++l) el[5][l] = xi * psi_c[l - NIV];
-        for (int l = 6; l < nv; ++l) {
-          double Y = Yc[l - 6];
-          el[l][0] = -b1 * Y;
-          for (int a = 0; a < 3; ++a) el[l][1 + a] = b2 * uc[a] * Y;
-          el[l][4] = -b2 * Y;
-        }
-        for (int s1 = 1; s1 <= nrv - 1; ++s1)
-          for (int s2 = 1; s2 <= nrv; ++s2) el[s1 + 5][s2 + 4] = -b2 * Yc[s1 - 1] * psi_c[s2 - 1];
-        for (int l = 1; l <= nrv - 1; ++l) el[l + 5][l + 4] = el[l + 5][l + 4] + 1.0;
-        // right eigenvectors (module_weno.f90:881-951)
-        for (int a = 0; a < nv; ++a)
-          for (int e = 0; e < nv; ++e) er[a][e] = 0.0;
-        er[0][0] = 1.0; er[0][1] = 1.0; er[0][2] = 1.0;
-        er[1 + d][0] = un - cs_c; er[1 + d][1] = un; er[1 + d][2] = un + cs_c;
-        er[1 + t1][0] = uc[t1]; er[1 + t1][1] = uc[t1]; er[1 + t1][2] = uc[t1]; er[1 + t1][3] = 1.0;
-        er[1 + t2][0] = uc[t2]; er[1 + t2][1] = uc[t2]; er[1 + t2][2] = uc[t2]; er[1 + t2][4] = 1.0;
-        er[4][0] = ht_c - un * cs_c; er[4][1] = q; er[4][2] = ht_c + un * cs_c; er[4][3] = uc[t1]; er[4][4] = uc[t2];
-        for (int l = NIV; l < nv; ++l) { er[l][0] = Yc[l - NIV]; er[l][2] = Yc[l - NIV]; }
-        for (int l = NIV + 1; l <= nv; ++l) er[l - 2][l - 1] = 1.0;
-        er[nv - 1][5] = -1.0 / psi_c[nrv - 1];
-        wrk = -1.0 / psi_c[nrv - 1];
-        for (int l = 1; l <= nrv - 1; ++l) er[nv - 1][l + 5] = wrk * psi_c[l - 1];
+        CharState chs;
+        for (int a = 0; a < 3; ++a) chs.uc[a] = uc[a];
+        chs.Yc = Yc; chs.psi_c = psi_c;
+        chs.ht_c = ht_c; chs.q = q; chs.cs_c = cs_c; chs.cs_c_i = cs_c_i; chs.b1 = b1; chs.b2 = b2; chs.xi = xi;
+        char_vectors(d, nv, nrv, chs, el, er);
         // characteristic LLF-WENO (module_weno.f90:953-989).  The sensor
         // is evaluated on each MPI block's interior and never exchanged, so
         // a block sees its neighbours' points as unflagged: a face is
@@ -1048,8 +1108,13 @@ int euler_flux(Ctx& c, int d, const double* v, const double* T, const double* W_
           else if (d == 1) { i = q1; j = s; k = q2; }
           else { i = q1; j = q2; k = s; }
           size_t f = (size_t)m * b.nint + b.fid(i, j, k);
-          if (d == 0) fl[f] = df * 1.0;
-          else fl[f] = fl[f] + df * 1.0;
+          // fl_W / fl_E (and S, N, B, F): 0 at the boundary points of a
+          // non-reflecting face (module_weno.f90:620-623, 1002, 1018)
+          double flag = 1.0;
+          if ((s == 1 && b.bc[2 * d] == IZEM_BC_NOREFLECTION) || (s == n && b.bc[2 * d + 1] == IZEM_BC_NOREFLECTION))
+            flag = 0.0;
+          if (d == 0) fl[f] = df * flag;
+          else fl[f] = fl[f] + df * flag;
         }
     }
   if (negp) {
@@ -1270,6 +1335,104 @@ int visc_flux(Ctx& c, const double* v, const double* T, const double* W_i, const
   return visc_flux_fit(c, v, T, W_i, cp, ha, fl);
 }
 
+// bc_noreflectionweno (module_weno.f90:2129-4498), one face: at every
+// boundary point, the characteristic vectors at the point's own state, the
+// eigenvalues of the waves leaving the domain (min(., 0) on the low faces,
+// max(., 0) on the high ones), the one-sided derivative of the conserved
+// variables over 2ng-1 points with wenopar's cnr weights (:199-217), and
+// fl += R diag(L_s) L dw * dx_i.  The six face blocks of the reference
+// differ only in the axis, the side and the sign; they are restated once.
+void bc_noreflectionweno(Ctx& c, int face, const double* v, const double* T, const double* W_i, const double* cp,
+                         const double* ha, double* fl) {
+  const Block& b = c.b;
+  const izem_thd& t = c.thd;
+  const int ng = b.ng, nv = b.nv, nrv = b.nrv, d = face / 2, hi = face & 1;
+  const size_t nc = b.ncell;
+  // cnr: for ng = 4 the 7-point one-sided first derivative; for ng = 3 the
+  // reference keeps its first five weights (their sum is -31/30, not 0)
+  const double cnr[7] = {-49.0 / 20.0, 6.0, -15.0 / 2.0, 20.0 / 3.0, -15.0 / 4.0, 6.0 / 5.0, -1.0 / 6.0};
+  const int st_m2 = ng + ng - 1;
+  const int sc = hi ? b.n(d) : 1;
+  const double* di = c.dxi[d].data();
+  const int m1 = d == 0 ? b.ny : b.nx, m2 = d == 2 ? b.ny : b.nz;
+  for (int q2 = 1; q2 <= m2; ++q2)
+    for (int q1 = 1; q1 <= m1; ++q1) {
+      auto cell = [&](int s) {
+        if (d == 0) return b.id(s, q1, q2);
+        if (d == 1) return b.id(q1, s, q2);
+        return b.id(q1, q2, s);
+      };
+      const size_t p = cell(sc);
+      const double rho_i = 1.0 / v[p];
+      double uc[3];
+      uc[0] = v[nc + p] * rho_i;
+      const double P = v[p] * T[p] * W_i[p];
+      double gam_c = t.gam2 * W_i[p] / cp[p];
+      gam_c = 1.0 / (1.0 - gam_c);
+      const double cs_c = std::sqrt(gam_c * P * rho_i);
+      uc[1] = v[2 * nc + p] * rho_i;
+      uc[2] = v[3 * nc + p] * rho_i;
+      double Y_c[IZEM_NSMAX], psi_c[IZEM_NSMAX];
+      for (int l = 0; l < nrv; ++l) Y_c[l] = v[(NIV + l) * nc + p] * rho_i;
+      double ht_c = 0.0;
+      double wrk = (gam_c / (gam_c - 1.0)) * T[p];
+      for (int l = 0; l < nrv; ++l) {
+        ht_c = ht_c + ha[l * nc + p] * Y_c[l];
+        psi_c[l] = -ha[l * nc + p];
+        psi_c[l] = psi_c[l] + wrk * t.Wc_i[l];
+      }
+      const double cs_c_i = 1.0 / cs_c, cs_c_2 = cs_c * cs_c;
+      const double q = 0.5 * (uc[0] * uc[0] + uc[1] * uc[1] + uc[2] * uc[2]);
+      ht_c = ht_c + q;
+      const double b2 = (gam_c - 1.0) / cs_c_2;
+      const double b1 = b2 * q;
+      const double xi = b1 - b2 * ht_c;
+      double el[IZEM_NSMAX + 5][IZEM_NSMAX + 5], er[IZEM_NSMAX + 5][IZEM_NSMAX + 5];
+      CharState chs;
+      for (int a = 0; a < 3; ++a) chs.uc[a] = uc[a];
+      chs.Yc = Y_c; chs.psi_c = psi_c;
+      chs.ht_c = ht_c; chs.q = q; chs.cs_c = cs_c; chs.cs_c_i = cs_c_i; chs.b1 = b1; chs.b2 = b2; chs.xi = xi;
+      char_vectors(d, nv, nrv, chs, el, er);
+      const double un = uc[d];
+      auto side = [&](double x) { return hi ? std::max(x, 0.0) : std::min(x, 0.0); };
+      double L_s[IZEM_NSMAX + 5], dw[IZEM_NSMAX + 5], dwc[IZEM_NSMAX + 5];
+      L_s[0] = side(un - cs_c);
+      L_s[1] = side(un);
+      L_s[2] = side(un + cs_c);
+      L_s[3] = side(un);
+      L_s[4] = side(un);
+      for (int m = NIV; m < nv; ++m) L_s[m] = side(un);
+      for (int m = 0; m < nv; ++m) {
+        dw[m] = 0.0;
+        for (int st = 1; st <= st_m2; ++st) {
+          if (hi) dw[m] = dw[m] - cnr[st - 1] * v[m * nc + cell(sc - st + 1)];
+          else dw[m] = dw[m] + cnr[st - 1] * v[m * nc + cell(sc + st - 1)];
+        }
+      }
+      for (int m = 0; m < nv; ++m) {
+        dwc[m] = 0.0;
+        for (int mm = 0; mm < nv; ++mm) dwc[m] = dwc[m] + el[m][mm] * dw[mm];
+      }
+      int i, j, k;
+      if (d == 0) { i = sc; j = q1; k = q2; }
+      else if (d == 1) { i = q1; j = sc; k = q2; }
+      else { i = q1; j = q2; k = sc; }
+      for (int m = 0; m < nv; ++m) {
+        double df = 0.0;
+        for (int mm = 0; mm < nv; ++mm) df = df + er[m][mm] * L_s[mm] * dwc[mm];
+        size_t f = (size_t)m * b.nint + b.fid(i, j, k);
+        fl[f] = fl[f] + df * di[sc - 1 + ng];
+      }
+    }
+}
+
+// NR_boundaries (module_BCs.f90:185-212): every non-reflecting face, W to F
+void nr_boundaries(Ctx& c, const double* v, const double* T, const double* W_i, const double* cp, const double* ha,
+                   double* fl) {
+  for (int f = 0; f < 2 * c.cfg.ndim; ++f)
+    if (c.b.bc[f] == IZEM_BC_NOREFLECTION) bc_noreflectionweno(c, f, v, T, W_i, cp, ha, fl);
+}
+
 // rk3 (module_solver.f90:694-856)
 int rk3(Ctx& c, double dt, double time0, double* v, double* T, double* W_i, double* cp, double* ha,
         uint8_t* sensor) {
@@ -1294,6 +1457,7 @@ int rk3(Ctx& c, double dt, double time0, double* v, double* T, double* W_i, doub
       if ((rc = euler_flux(c, d, v, T, W_i, cp, ha, sensor, f.data()))) return rc;
     if (c.cfg.vis)
       if ((rc = visc_flux(c, v, T, W_i, cp, ha, f.data()))) return rc;
+    nr_boundaries(c, v, T, W_i, cp, ha, f.data());   // module_solver.f90:824
     for (int l = 0; l < b.nv; ++l)
       for (int k = 1; k <= b.nz; ++k)
         for (int j = 1; j <= b.ny; ++j)
@@ -1477,7 +1641,7 @@ void* or_create(const izem_cfg* cfg, const izem_thd* thd, const izem_adi* adi, c
     return nullptr;
   for (int f = 0; f < 6; ++f) {
     const int bc = cfg->bc[f];
-    if (bc < IZEM_BC_PERIODIC || bc > IZEM_BC_NSCBC_OUT) return nullptr;
+    if (bc < IZEM_BC_PERIODIC || bc > IZEM_BC_NOREFLECTION) return nullptr;
     if ((bc == IZEM_BC_INFLOWJET && f != 0) || (bc == IZEM_BC_NSCBC_OUT && f != 1)) return nullptr;
   }
   if (cfg->bc[0] == IZEM_BC_INFLOWJET && cfg->nrv != 2 && cfg->nrv != 3 && cfg->nrv != 9) return nullptr;
@@ -1585,6 +1749,12 @@ int or_euler_flux(void* h, int dir, const double* v, const double* T, const doub
                   const double* ha, const uint8_t* sensor, double* fl) {
   return euler_flux(*static_cast<Ctx*>(h), dir, v, T, W_i, cp, ha, sensor, fl);
 }
+int or_nr_flux(void* h, const double* v, const double* T, const double* W_i, const double* cp, const double* ha,
+               double* fl) {
+  nr_boundaries(*static_cast<Ctx*>(h), v, T, W_i, cp, ha, fl);
+  return IZEM_OK;
+}
+
 int or_visc_flux(void* h, const double* v, const double* T, const double* W_i, const double* cp,
                  const double* ha, double* fl) {
   return visc_flux(*static_cast<Ctx*>(h), v, T, W_i, cp, ha, fl);

@@ -12,6 +12,7 @@ BC_PERIODIC = 0
 BC_EXTRAPOLATION = 1
 BC_INFLOWJET = 2
 BC_NSCBC_OUT = 3
+BC_NOREFLECTION = 4
 
 OK = 0
 ERR_ARG = 1

@@ -362,6 +362,36 @@ int enq_visc(izem_ctx* c) {
   return launch(c, "visc_div", [&] { k_visc_div<NRV><<<grid_for(g.nint), kThreads, 0, c->stream>>>(g, mt, c->tau, c->qv, c->fd, c->f); });
 }
 
+// NR_boundaries (module_BCs.f90:185-212): bc_noreflectionweno on every
+// non-reflecting face, W to F, after the viscous fluxes (module_solver.f90:824)
+template <int NRV>
+int enq_nr(izem_ctx* c) {
+  const Geo& g = c->g;
+  int rc = IZEM_OK;
+  for (int f = 0; f < 2 * g.ndim && !rc; ++f) {
+    if (g.bc[f] != IZEM_BC_NOREFLECTION) continue;
+    const int d = f >> 1, hi = f & 1;
+    const long long np = (long long)(d == 0 ? g.n[1] : g.n[0]) * (d == 2 ? g.n[1] : g.n[2]);
+    rc = launch(c, "bc_nr", [&] {
+#define IZEM_NR(DD, NGV)                                                                                           \
+  k_bc_nr<NRV, DD, NGV><<<grid_for(np), kThreads, 0, c->stream>>>(g, hi, c->v, c->T, c->W_i, c->cp, c->ha, c->dxi[DD], c->f)
+      if (g.ng == 4) {
+        if constexpr (NRV == 2) {
+          if (d == 0) IZEM_NR(0, 4);
+          if (d == 1) IZEM_NR(1, 4);
+          if (d == 2) IZEM_NR(2, 4);
+        }
+      } else {
+        if (d == 0) IZEM_NR(0, 3);
+        if (d == 1) IZEM_NR(1, 3);
+        if (d == 2) IZEM_NR(2, 3);
+      }
+#undef IZEM_NR
+    });
+  }
+  return rc;
+}
+
 static bool jet_face(int bc) { return bc == IZEM_BC_INFLOWJET || bc == IZEM_BC_NSCBC_OUT; }
 
 // comm_cons, upd_boundaries, upd_prim_var_ghost (module_BCs.f90:41-296):
@@ -385,7 +415,7 @@ int enq_boundaries(izem_ctx* c, const double* tdt, double tk) {
   int per = 0, ext = 0, dir = 0;
   for (int f = 0; f < 6; ++f) {
     if (g.bc[f] == IZEM_BC_PERIODIC) per |= 1 << f;
-    else if (g.bc[f] == IZEM_BC_EXTRAPOLATION) ext |= 1 << f;
+    else if (g.bc[f] == IZEM_BC_EXTRAPOLATION || g.bc[f] == IZEM_BC_NOREFLECTION) ext |= 1 << f;
     else dir |= 1 << f;
   }
   JetArgs ja = c->jet;
@@ -435,6 +465,7 @@ int enq_stage(izem_ctx* c, int stage) {
     if ((rc = enq_euler<NRV>(c, d))) return rc;
   if (c->cfg.vis)
     if ((rc = enq_visc<NRV>(c))) return rc;
+  if ((rc = enq_nr<NRV>(c))) return rc;
   if ((rc = launch(c, "rk_update", [&] {
          k_rk_update<NRV><<<grid_for(g.nint), kThreads, 0, c->stream>>>(g, stage, c->cfg.forcesum, c->d_dt, c->v, c->v0, c->f, c->W_i);
        })))
@@ -528,6 +559,11 @@ int do_visc(izem_ctx* c) {
   return enq_visc<NRV>(c);
 }
 
+template <int NRV>
+int do_nr(izem_ctx* c) {
+  return enq_nr<NRV>(c);
+}
+
 
 // ---------------------------------------------------------- autotuning -------
 // Times each candidate launch configuration on the context's current state
@@ -602,7 +638,7 @@ int izem_gpu_init(const izem_cfg* cfg, const izem_thd* thd, const izem_adi* adi,
   if (cfg->nx < nmin || cfg->ny < nmin || (cfg->ndim == 3 && cfg->nz < nmin)) return IZEM_ERR_ARG;
   for (int f = 0; f < 6; ++f) {
     const int bc = cfg->bc[f];
-    if (bc < IZEM_BC_PERIODIC || bc > IZEM_BC_NSCBC_OUT) return IZEM_ERR_ARG;
+    if (bc < IZEM_BC_PERIODIC || bc > IZEM_BC_NOREFLECTION) return IZEM_ERR_ARG;
     // bc_inflowjet declares the W face only, bc_nscbc_out the E face only
     if ((bc == IZEM_BC_INFLOWJET && f != IZEM_FACE_W) || (bc == IZEM_BC_NSCBC_OUT && f != IZEM_FACE_E))
       return IZEM_ERR_ARG;
@@ -844,6 +880,14 @@ int izem_gpu_visc_flux(izem_ctx* c) {
   if (!c) return IZEM_ERR_ARG;
   if (!c->grid_set) return ctx_fail(c, IZEM_ERR_STATE, "grid not set", cudaSuccess);
   int rc = IZEM_DISPATCH(c, do_visc, c);
+  if (rc) return rc;
+  return read_status(c);
+}
+
+int izem_gpu_nr_flux(izem_ctx* c) {
+  if (!c) return IZEM_ERR_ARG;
+  if (!c->grid_set) return ctx_fail(c, IZEM_ERR_STATE, "grid not set", cudaSuccess);
+  int rc = IZEM_DISPATCH(c, do_nr, c);
   if (rc) return rc;
   return read_status(c);
 }

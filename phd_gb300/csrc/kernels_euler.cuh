@@ -486,11 +486,136 @@ __global__ void k_flux_diff(Geo g, int nv, const double* __restrict__ fhat, long
     nleft = nedge;
     fl_ = (long long)((i - 1) / bx - 1) + (long long)ne * ((j - 1) + (long long)g.n[1] * (k - 1));
   }
+  // fl_W / fl_E (and S, N, B, F): the boundary points of a non-reflecting
+  // face take 0 times their flux difference (module_weno.f90:620-623, 1002,
+  // 1018); bc_noreflectionweno supplies their normal term
+  const double flag = ((s == 1 && g.bc[2 * D] == IZEM_BC_NOREFLECTION) ||
+                       (s == g.n[D] && g.bc[2 * D + 1] == IZEM_BC_NOREFLECTION))
+                          ? 0.0
+                          : 1.0;
   for (int m = 0; m < nv; ++m) {
     double df = (fhat[m * nfaces + fr] - fleft[m * nleft + fl_]) * di;
     long long o = (long long)m * g.nint + idx;
-    fl[o] = accumulate ? fl[o] + df : df;
+    fl[o] = accumulate ? fl[o] + df * flag : df * flag;
   }
+}
+
+// bc_noreflectionweno (module_weno.f90:2129-4498), one face per launch, one
+// thread per boundary point.  At the point's own state: the characteristic
+// vectors of the flux Jacobian along the face normal D (the structure of
+// k_euler_face's projections), the eigenvalues of the waves leaving the
+// domain (min(., 0) on the low face, max(., 0) on the high one), and the
+// one-sided derivative of the conserved variables over 2NG-1 points with
+// wenopar's cnr weights (:199-217; for NG = 3 the reference keeps the first
+// five of the 7-point set).  fl += R diag(L_s) L dw * dx_i.
+template <int NRV, int D, int NG>
+__global__ void k_bc_nr(Geo g, int hi, const double* __restrict__ v, const double* __restrict__ T,
+                        const double* __restrict__ W_i, const double* __restrict__ cp,
+                        const double* __restrict__ ha, const double* __restrict__ dxi, double* __restrict__ fl) {
+  constexpr int NV = IZEM_NIV + NRV;
+  constexpr int T1 = D == 0 ? 1 : 0;
+  constexpr int T2 = D == 2 ? 1 : 2;
+  const int m1 = D == 0 ? g.n[1] : g.n[0], m2 = D == 2 ? g.n[1] : g.n[2];
+  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= (long long)m1 * m2) return;
+  const int q1 = (int)(idx % m1) + 1, q2 = (int)(idx / m1) + 1;
+  const int sc = hi ? g.n[D] : 1;
+  int c[3];
+  c[D] = sc;
+  c[D == 0 ? 1 : 0] = q1;
+  c[D == 2 ? 1 : 2] = q2;
+  const long long nc = g.ncell;
+  const long long stride = D == 0 ? 1LL : (D == 1 ? (long long)g.g[0] : (long long)g.g[0] * g.g[1]);
+  const long long p = gid(g, c[0], c[1], c[2]);
+  const double rho_i = 1.0 / v[p];
+  double uc[3];
+  uc[0] = v[nc + p] * rho_i;
+  uc[1] = v[2 * nc + p] * rho_i;
+  uc[2] = v[3 * nc + p] * rho_i;
+  const double P = v[p] * T[p] * W_i[p];
+  double gam_c = c_thd.gam2 * W_i[p] / cp[p];
+  gam_c = 1.0 / (1.0 - gam_c);
+  const double cs_c = sqrt(gam_c * P * rho_i);
+  double Yc[NRV], psi[NRV];
+  double ht_c = 0.0;
+  {
+    const double wrk = (gam_c / (gam_c - 1.0)) * T[p];
+#pragma unroll
+    for (int l = 0; l < NRV; ++l) {
+      Yc[l] = v[(IZEM_NIV + l) * nc + p] * rho_i;
+      const double h = ha[l * nc + p];
+      ht_c = ht_c + h * Yc[l];
+      psi[l] = -h + wrk * c_thd.Wc_i[l];
+    }
+  }
+  const double cs_c_i = 1.0 / cs_c;
+  const double q = 0.5 * (uc[0] * uc[0] + uc[1] * uc[1] + uc[2] * uc[2]);
+  ht_c = ht_c + q;
+  const double b2 = (gam_c - 1.0) / (cs_c * cs_c);
+  const double b1 = b2 * q;
+  const double xi = b1 - b2 * ht_c;
+  const double un = uc[D];
+  // one-sided derivative (times the spacing) into the domain
+  const double cnr[7] = {-49.0 / 20.0, 6.0, -15.0 / 2.0, 20.0 / 3.0, -15.0 / 4.0, 6.0 / 5.0, -1.0 / 6.0};
+  const double sgn = hi ? -1.0 : 1.0;
+  double w[NV];
+#pragma unroll
+  for (int m = 0; m < NV; ++m) w[m] = 0.0;
+#pragma unroll
+  for (int st = 0; st < 2 * NG - 1; ++st) {
+    const long long ps = hi ? p - st * stride : p + st * stride;
+    const double cw = sgn * cnr[st];
+#pragma unroll
+    for (int m = 0; m < NV; ++m) w[m] = w[m] + cw * v[m * nc + ps];
+  }
+  // L w (module_weno.f90:2224-2332 and the other faces' copies)
+  double sw = 0.0;
+#pragma unroll
+  for (int l = 0; l < NRV; ++l) sw = sw + psi[l] * w[IZEM_NIV + l];
+  const double hb2 = 0.5 * b2;
+  const double Gw = -b1 * w[0] + b2 * uc[0] * w[1] + b2 * uc[1] * w[2] + b2 * uc[2] * w[3] - b2 * w[4] - b2 * sw;
+  double pw[NV];
+  pw[0] = 0.5 * (b1 + un * cs_c_i) * w[0] - 0.5 * (b2 * un + cs_c_i) * w[1 + D] - 0.5 * (b2 * uc[T1]) * w[1 + T1] -
+          0.5 * (b2 * uc[T2]) * w[1 + T2] + hb2 * w[4] + hb2 * sw;
+  pw[1] = w[0] + Gw;
+  pw[2] = 0.5 * (b1 - un * cs_c_i) * w[0] - 0.5 * (b2 * un - cs_c_i) * w[1 + D] - 0.5 * (b2 * uc[T1]) * w[1 + T1] -
+          0.5 * (b2 * uc[T2]) * w[1 + T2] + hb2 * w[4] + hb2 * sw;
+  pw[3] = -uc[T1] * w[0] + w[1 + T1];
+  pw[4] = -uc[T2] * w[0] + w[1 + T2];
+  {
+    const double opx = 1.0 + xi;
+    pw[5] = opx * q * w[0] - opx * uc[0] * w[1] - opx * uc[1] * w[2] - opx * uc[2] * w[3] + opx * w[4] + xi * sw;
+  }
+#pragma unroll
+  for (int s = 0; s < NRV - 1; ++s) pw[6 + s] = Yc[s] * Gw + w[IZEM_NIV + s];
+  // the waves leaving the domain
+  auto side = [&](double x) { return hi ? fmax(x, 0.0) : fmin(x, 0.0); };
+  double gh[NV];
+  gh[0] = side(un - cs_c) * pw[0];
+  gh[2] = side(un + cs_c) * pw[2];
+#pragma unroll
+  for (int m = 0; m < NV; ++m)
+    if (m != 0 && m != 2) gh[m] = side(un) * pw[m];
+  // R gh (module_weno.f90:2334-2418)
+  double fh[NV];
+  fh[0] = gh[0] + gh[1] + gh[2];
+  fh[1 + D] = (un - cs_c) * gh[0] + un * gh[1] + (un + cs_c) * gh[2];
+  fh[1 + T1] = uc[T1] * gh[0] + uc[T1] * gh[1] + uc[T1] * gh[2] + gh[3];
+  fh[1 + T2] = uc[T2] * gh[0] + uc[T2] * gh[1] + uc[T2] * gh[2] + gh[4];
+  fh[4] = (ht_c - un * cs_c) * gh[0] + q * gh[1] + (ht_c + un * cs_c) * gh[2] + uc[T1] * gh[3] + uc[T2] * gh[4] + gh[5];
+#pragma unroll
+  for (int s = 0; s < NRV - 1; ++s) fh[IZEM_NIV + s] = Yc[s] * gh[0] + Yc[s] * gh[2] + gh[6 + s];
+  {
+    const double wrk = -1.0 / psi[NRV - 1];
+    double acc = Yc[NRV - 1] * gh[0] + Yc[NRV - 1] * gh[2] + wrk * gh[5];
+#pragma unroll
+    for (int s = 0; s < NRV - 1; ++s) acc = acc + (wrk * psi[s]) * gh[6 + s];
+    fh[NV - 1] = acc;
+  }
+  const double di = dxi[sc - 1 + g.ng];
+  const long long o = fidx(g, c[0], c[1], c[2]);
+#pragma unroll
+  for (int m = 0; m < NV; ++m) fl[(long long)m * g.nint + o] += fh[m] * di;
 }
 
 // K3: Adams-Shariff sensor, sticky (only ever sets).  Interior neighbour tests

@@ -121,8 +121,9 @@ __global__ void k_prim_woT(Geo g, const double* __restrict__ v, const double* __
   cp[p] = cpm;
 }
 
-// Ghost slabs: fill v from the periodic partner or by zero-gradient
-// extrapolation, then force_sumY and W_i on the ghost point.
+// Ghost slabs: fill v from the periodic partner, by zero-gradient
+// extrapolation, or (non-reflecting faces) with the boundary state times 10,
+// then force_sumY and W_i on the ghost point.
 // mode 0: periodic faces wrap, boundary faces extrapolate (comm_cons +
 // upd_boundaries); mode 1: every face extrapolates (upd_extrapolation).
 // mask: the faces (bit f) this launch treats; mode 2: no copy, only the
@@ -143,7 +144,11 @@ __global__ void k_halo(Geo g, int mode, int forcesum, double* __restrict__ v, do
   else c[d] = (f & 1) ? g.n[d] : 1;
   const long long nc = g.ncell;
   const long long p = gid(g, i, j, k), q = gid(g, c[0], c[1], c[2]);
-  if (mode != 2) {
+  if (mode == 0 && g.bc[f] == IZEM_BC_NOREFLECTION) {
+    // bc_noreflection (module_BCs.f90:426-512): the boundary state times 10
+#pragma unroll
+    for (int l = 0; l < NV; ++l) v[l * nc + p] = v[l * nc + q] * 10.0;
+  } else if (mode != 2) {
 #pragma unroll
     for (int l = 0; l < NV; ++l) v[l * nc + p] = v[l * nc + q];
   }

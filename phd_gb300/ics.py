@@ -329,3 +329,57 @@ def jet(nx=24, ny=16, nz=16, species="o2n2", Lx=4e-3, Lr=1.5e-3, uco=20.0, lib_d
     info = {"name": "jet box %dx%dx%d (%s)" % (nx, ny, nz, species),
             "coords": (x / L, y / L, z / L), "lx": (x[-1] - x[0]) / L, "time_ref": a["time_ref"]}
     return cfg, thd, adi_struct(a), dxi, state, info
+
+
+def acoustic_pulse(nx=16, ny=12, nz=8, species="o2n2", L=1e-3, amp=0.05, u0=30.0, w0=10.0, blob=0.0, faces="xy",
+                   ng=3, lib_dscalar=None):
+    """Box with non-reflecting faces (NOREFLECTION: bc_noreflection and
+    bc_noreflectionweno) for the waves that leave it: air (O2/N2 mass
+    fractions 0.233/0.767) at 300 K and 1 atm moving at u0 in x and w0 in z, with a
+    Gaussian pressure pulse of relative amplitude amp and width L/6 at the
+    centre of the x-y section (isothermal: the density follows the
+    pressure).  blob > 0 (nine-species sets) adds an H2 mass fraction
+    blob * exp(-r^2/s^2) at the same place, taken from N2.  faces: the
+    axes whose two faces are non-reflecting ("x", "xy" or "xyz"); the
+    others are periodic.  Grid spacing L/(n-1) on every axis; ng = 3
+    (WENO5) or 4 (WENO7, two-species sets).  Returns cfg, thd, adi, dxi,
+    state, info."""
+    from .capi import BC_NOREFLECTION
+    a = constants()
+    sp = load_species(species)
+    thd = thd_init(sp, a)
+    names = sp["names"]
+    h = L / (nx - 1)
+    x = np.arange(nx) * h
+    y = np.arange(ny) * h
+    z = np.arange(nz) * h
+    Xg, Yg, Zg = np.meshgrid(x, y, z, indexing="ij")
+    r2 = (Xg - x[-1] / 2) ** 2 + (Yg - y[-1] / 2) ** 2
+    s2 = (L / 6.0) ** 2
+    g = np.exp(-r2 / s2)
+    Ya = np.zeros(len(names))
+    Ya[names.index("O2")] = 0.233
+    Ya[names.index("N2")] = 0.767
+    Ys = np.broadcast_to(Ya, Xg.shape + (len(names),)).copy()
+    if blob > 0.0:
+        Ys[..., names.index("H2")] = blob * g
+        Ys[..., names.index("N2")] -= blob * g
+    T = np.full(Xg.shape, 300.0)
+    Wmix_i = np.einsum("...k,k->...", Ys, 1.0 / (np.array(sp["W_gmol"]) * 1e-3))
+    P = 101325.0 * (1.0 + amp * g)
+    rho = P / (a["r_ref"] * Wmix_i * T)
+    u = np.full(Xg.shape, u0)
+    w = np.full(Xg.shape, w0)
+    zero = np.zeros(Xg.shape)
+    state = _state_from_primitives(thd, a, rho, u, zero, w, T, Ys, ng)
+    bc = [BC_PERIODIC] * 6
+    for d, ax in enumerate("xyz"):
+        if ax in faces:
+            bc[2 * d] = bc[2 * d + 1] = BC_NOREFLECTION
+    cfg = make_cfg(nx, ny, nz, len(names), bc=tuple(bc))
+    cfg.ng = ng
+    dxi = [grid_dxi(c, ng, a, lib_dscalar) for c in (x, y, z)]
+    info = {"name": "acoustic pulse %dx%dx%d (%s, non-reflecting %s faces)" % (nx, ny, nz, species, faces),
+            "time_ref": a["time_ref"]}
+    return cfg, thd, adi_struct(a), dxi, state, info
+

@@ -57,6 +57,7 @@ def load_library(path=None):
         "izem_gpu_shock_sensor": (C.c_int, [P]),
         "izem_gpu_euler_flux": (C.c_int, [P, C.c_int]),
         "izem_gpu_visc_flux": (C.c_int, [P]),
+        "izem_gpu_nr_flux": (C.c_int, [P]),
         "izem_gpu_update_primitives": (C.c_int, [P]),
         "izem_gpu_finalize_ic": (C.c_int, [P]),
         "izem_gpu_rk3": (C.c_int, [P, C.c_double, C.c_double]),
@@ -280,6 +281,10 @@ class IzemGPU:
 
     def viscflux_xyz(self):
         self._check(self.lib.izem_gpu_visc_flux(self.h), "viscflux_xyz")
+
+    def NR_boundaries(self):
+        """bc_noreflectionweno on every non-reflecting face (adds to f)."""
+        self._check(self.lib.izem_gpu_nr_flux(self.h), "NR_boundaries")
 
     def update_primitives(self):
         self._check(self.lib.izem_gpu_update_primitives(self.h), "update_primitives")
