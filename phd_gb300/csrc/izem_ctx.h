@@ -49,6 +49,7 @@ struct izem_ctx {
   // one block) and the block-edge faces as seen by the right block
   int sensor_bx = 0;
   int newton_bx = 0;   // x-block size of the Newton stopping test (nx: one block)
+  int nsm = 0;         // SMs of the context's device (the host-transfer kernel's grid)
   double* fhat_edge = nullptr;
   long long nedge = 0;
   // chemistry
