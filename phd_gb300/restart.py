@@ -62,13 +62,28 @@ def _group(d, btree, heap):
 
 
 def _messages(d, oh):
+    """(type, data address, size) of every message of a version-1 object
+    header.  The header's first chunk follows its 16-byte prefix; an object
+    header continuation message (type 0x10: address and length of a further
+    block of messages) adds a chunk, and the prefix's message count covers
+    the messages of every chunk, continuation and NIL messages included."""
     if d[oh] != 1:
         raise ValueError("version-1 object header expected at %#x" % oh)
-    p = oh + 16
-    for _ in range(_u(d, oh + 2, 2)):
-        mtype, msize = _u(d, p, 2), _u(d, p + 2, 2)
-        yield mtype, p + 8, msize
-        p += 8 + msize
+    left = _u(d, oh + 2, 2)
+    chunks = [(oh + 16, _u(d, oh + 8, 4))]
+    while chunks and left > 0:
+        p, n = chunks.pop(0)
+        end = p + n
+        while left > 0 and p + 8 <= end:
+            mtype, msize = _u(d, p, 2), _u(d, p + 2, 2)
+            left -= 1
+            if mtype == 0x10:
+                chunks.append((_u(d, p + 8, 8), _u(d, p + 16, 8)))
+            else:
+                yield mtype, p + 8, msize
+            p += 8 + msize
+    if left > 0:
+        raise ValueError("object header at %#x: %d of its messages lie outside its chunks" % (oh, left))
 
 
 def _dataset(d, oh):

@@ -53,6 +53,53 @@ def test_write_read_round_trip(tmp_path):
     assert all(np.array_equal(a, b) for a, b in zip(got, arrays))
 
 
+def _spill_into_continuation(d, oh):
+    """Rewrite the version-1 object header at oh so that every message after
+    the first sits in a continuation block appended to the file: the first
+    chunk keeps message 1, an object header continuation message (0x10) and
+    a NIL message padding the rest."""
+    d = bytearray(d)
+    nmsg, size = R._u(d, oh + 2, 2), R._u(d, oh + 8, 4)
+    p0 = oh + 16
+    first = 8 + R._u(d, p0 + 2, 2)
+    rest = bytes(d[p0 + first:p0 + size])
+    assert len(rest) >= 24 + 8
+    block = len(d) + (-len(d)) % 8
+    d += b"\0" * (block - len(d)) + rest
+    q = p0 + first
+    d[q:q + 8] = (0x10).to_bytes(2, "little") + (16).to_bytes(2, "little") + bytes(4)
+    d[q + 8:q + 24] = block.to_bytes(8, "little") + len(rest).to_bytes(8, "little")
+    nil = p0 + size - (q + 24) - 8
+    d[q + 24:q + 32] = (0).to_bytes(2, "little") + nil.to_bytes(2, "little") + bytes(4)
+    d[q + 32:p0 + size] = bytes(nil)
+    d[oh + 2:oh + 4] = (nmsg + 2).to_bytes(2, "little")
+    return bytes(d)
+
+
+def test_reads_dataset_headers_with_continuation_blocks(tmp_path):
+    """A dataset whose object header continues in a second block (object
+    header continuation message, as HDF5 writes when messages are added to a
+    full header) reads the same array."""
+    rng = np.random.Generator(np.random.PCG64(5))
+    names = list(R.NIV_NAMES) + ["O2", "N2"]
+    arrays = [np.asfortranarray(rng.standard_normal((6, 5, 2))) for _ in names]
+    p = str(tmp_path / "r.h5")
+    R.write_restart(p, names, arrays, 1.5)
+    d = open(p, "rb").read()
+    groups = R._group(d, R._u(d, 56 + 24, 8), R._u(d, 56 + 32, 8))
+    gb, gh = np.frombuffer(groups["consvar"][2], dtype="<u8")
+    oh = R._group(d, int(gb), int(gh))["rhoE"][0]
+    d2 = _spill_into_continuation(d, oh)
+    before = [t for t, _, _ in R._messages(d, oh)]
+    assert [t for t, _, _ in R._messages(d2, oh)] == before[:1] + [0] + before[1:]
+    q = str(tmp_path / "r2.h5")
+    open(q, "wb").write(d2)
+    got_names, got, time = R.read_restart(q)
+    assert time == 1.5
+    for name, a in zip(names, arrays):
+        assert np.array_equal(got[got_names.index(name)], a), name
+
+
 @refdata.needs_reference
 def test_written_headers_match_reference_file(tmp_path):
     """The dataspace, datatype, fill-value and layout messages of a written
