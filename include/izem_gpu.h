@@ -48,6 +48,9 @@ enum {
 };
 enum { IZEM_FACE_W = 0, IZEM_FACE_E, IZEM_FACE_S, IZEM_FACE_N, IZEM_FACE_B, IZEM_FACE_F };
 
+/* Shock sensors (SHOCK_SENSOR_TYPE, module_solver.f90:758-766). */
+enum { IZEM_SENSOR_ADAMS_SHARIFF = 0, IZEM_SENSOR_DUCROS = 1 };
+
 /* Status codes. */
 enum {
   IZEM_OK = 0,
@@ -195,9 +198,19 @@ int  izem_gpu_download_flux(izem_ctx* ctx, double* fl);
 /* Zero the device flux array (test helper for the accumulating y/z sweeps). */
 int  izem_gpu_zero_flux(izem_ctx* ctx);
 
-/* shock_sensor_modified_adams_shariff (module_tools.f90:2733-2814): sets the
- * sticky mask (never cleared) on the device. */
+/* The stage's shock sensor on the device, setting the sticky mask (never
+ * cleared): shock_sensor_modified_adams_shariff (module_tools.f90:2733-2814)
+ * by default, or compute_duixj + shock_sensor_ducros (:2521-2719) after
+ * izem_gpu_set_shock_sensor(ctx, IZEM_SENSOR_DUCROS, ...). */
 int  izem_gpu_shock_sensor(izem_ctx* ctx);
+
+/* SHOCK_SENSOR_TYPE and DUCROS_TREDUC (module_input.f90:347-348, defaults
+ * ADAMSSHARIFF and 0.2): type IZEM_SENSOR_ADAMS_SHARIFF or
+ * IZEM_SENSOR_DUCROS (2-D and 3-D blocks; the flag is set where
+ * (div u)^2 / ((div u)^2 + |curl u|^2 + 1e-30) > ducros_treduc, the velocity
+ * gradients by dx_fixed1 and its y, z copies).  Takes effect at the next
+ * stage; the RK3 graph is captured again. */
+int  izem_gpu_set_shock_sensor(izem_ctx* ctx, int type, double ducros_treduc);
 
 /* euler_LLF_x/_y/_z (module_weno.f90:537,1055,1595): dir 0 overwrites f,
  * dir 1 and 2 accumulate into f. */

@@ -43,6 +43,7 @@ def load():
         "or_euler_flux": (C.c_int, [P, C.c_int, _dp, _dp, _dp, _dp, _dp, _u8p, _dp]),
         "or_visc_flux": (C.c_int, [P, _dp, _dp, _dp, _dp, _dp, _dp]),
         "or_nr_flux": (C.c_int, [P, _dp, _dp, _dp, _dp, _dp, _dp]),
+        "or_set_shock_sensor": (C.c_int, [P, C.c_int, C.c_double]),
         "or_prim_inv_var": (C.c_int, [P, C.c_int, C.c_int, _dp, _dp, _dp, _dp, _dp]),
         "or_force_sumY": (C.c_int, [P, C.c_int, _dp]),
         "or_update_primitives": (C.c_int, [P, _dp, _dp, _dp, _dp, _dp]),
@@ -223,6 +224,11 @@ class Oracle:
     def visc_flux(self, s, fl):
         v, T, W_i, cp, ha = self._arrs(s)
         self._rc(self.lib.or_visc_flux(self.h, _p(v), _p(T), _p(W_i), _p(cp), _p(ha), _p(fl)), "visc_flux")
+
+    def set_shock_sensor(self, kind="ADAMSSHARIFF", ducros_treduc=0.2):
+        """SHOCK_SENSOR_TYPE ("ADAMSSHARIFF" or "DUCROS") and DUCROS_TREDUC."""
+        t = {"ADAMSSHARIFF": 0, "DUCROS": 1}[kind]
+        self._rc(self.lib.or_set_shock_sensor(self.h, t, float(ducros_treduc)), "set_shock_sensor")
 
     def nr_flux(self, s, fl):
         """NR_boundaries: adds bc_noreflectionweno's term of every

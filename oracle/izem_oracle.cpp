@@ -66,6 +66,8 @@ struct Ctx {
   int newton_it_max = 0;   // most iterations of any prim_inv_var call (test readout)
   int sensor_xblocks = 1;   // x-blocks of the reference's MPI run whose edges the sensor does not cross
   int newton_xblocks = 1;   // x-blocks whose Newton loops stop on their own test
+  int sensor_type = IZEM_SENSOR_ADAMS_SHARIFF;   // SHOCK_SENSOR_TYPE
+  double ducros_treduc = 0.2;                    // DUCROS_TREDUC
   // dvodesimp (module_reaction.f90:173-251): pure fuel Y1f and oxidiser Y0o,
   // H2 and N2 species indices (0-based)
   // LES with the Smagorinsky closure under EGLIB (or_set_les): MU_SGS_FACTOR,
@@ -746,6 +748,54 @@ void deriv(const Ctx& c, int d, const double* in, double* out, bool out_interior
         }
         if (out_interior) out[b.fid(i, j, k)] = res;
         else out[b.id(i, j, k)] = res;
+      }
+}
+
+// compute_duixj + shock_sensor_ducros (module_tools.f90:2521-2719): the
+// velocity gradients by dx_fixed1 / dy_fixed1 / dz_fixed1 of u = rho u * (1 /
+// rho), then the sticky flag where (div u)^2 / ((div u)^2 + |curl u|^2 +
+// eps30) > DUCROS_TREDUC.  The velocities are formed on every point with a
+// density (the reference forms them on the interior and the face slabs,
+// which are all that the derivatives read).
+void shock_sensor_ducros(const Ctx& c, const double* v, uint8_t* sensor) {
+  const Block& b = c.b;
+  const int nd = c.cfg.ndim;
+  const size_t nc = b.ncell, ni = b.nint;
+  std::vector<double> u(3 * nc, 0.0), du(9 * ni, 0.0);
+  for (size_t p = 0; p < nc; ++p) {
+    if (v[p] == 0.0) continue;
+    const double rho_i = 1.0 / v[p];
+    for (int a = 0; a < 3; ++a) u[a * nc + p] = v[(1 + a) * nc + p] * rho_i;
+  }
+  // duixj (.., a nd + d + 1) = d u_a / d x_d: (1) du/dx (2) du/dy [(3) du/dz] ...
+  for (int a = 0; a < nd; ++a)
+    for (int d = 0; d < nd; ++d) deriv(c, d, u.data() + a * nc, du.data() + (a * nd + d) * ni, true);
+  const double eps30 = 1.0e-30;
+  for (int k = 1; k <= b.nz; ++k)
+    for (int j = 1; j <= b.ny; ++j)
+      for (int i = 1; i <= b.nx; ++i) {
+        const size_t f = b.fid(i, j, k);
+        auto D = [&](int q) { return du[(q - 1) * ni + f]; };
+        double div, vort, wrk;
+        if (nd == 3) {
+          div = D(1) + D(5) + D(9);
+          div = div * div;
+          wrk = D(8) - D(6);
+          vort = wrk * wrk;
+          wrk = D(3) - D(7);
+          wrk = wrk * wrk;
+          vort = vort + wrk;
+          wrk = D(4) - D(2);
+          wrk = wrk * wrk;
+          vort = vort + wrk;
+        } else {
+          div = D(1) + D(4);
+          div = div * div;
+          wrk = D(3) - D(2);
+          vort = wrk * wrk;
+        }
+        const double ducloc = div / (div + vort + eps30);
+        if (ducloc > c.ducros_treduc) sensor[b.id(i, j, k)] = 1;
       }
 }
 
@@ -1451,7 +1501,9 @@ int rk3(Ctx& c, double dt, double time0, double* v, double* T, double* W_i, doub
       for (int j = 1; j <= b.ny; ++j)
         for (int i = 1; i <= b.nx; ++i) v0[l * ni + b.fid(i, j, k)] = v[l * nc + b.id(i, j, k)];
   for (int ik = 0; ik < 3; ++ik) {
-    shock_sensor(c, v, T, W_i, sensor);
+    // module_solver.f90:758-766
+    if (c.sensor_type == IZEM_SENSOR_DUCROS) shock_sensor_ducros(c, v, sensor);
+    else shock_sensor(c, v, T, W_i, sensor);
     int rc;
     for (int d = 0; d < c.cfg.ndim; ++d)   // euler_LLF_z only when ndim == 3 (module_solver.f90:769-774)
       if ((rc = euler_flux(c, d, v, T, W_i, cp, ha, sensor, f.data()))) return rc;
@@ -1742,8 +1794,20 @@ void or_cp_scalar(void* h, double T, const double* Y, double* cp) { *cp = cp_sca
 void or_ha_scalar(void* h, double T, double* ha) { ha_scalar(static_cast<Ctx*>(h)->thd, T, ha); }
 
 int or_shock_sensor(void* h, const double* v, const double* T, const double* W_i, uint8_t* sensor) {
-  shock_sensor(*static_cast<Ctx*>(h), v, T, W_i, sensor);
+  Ctx& c = *static_cast<Ctx*>(h);
+  if (c.sensor_type == IZEM_SENSOR_DUCROS) shock_sensor_ducros(c, v, sensor);
+  else shock_sensor(c, v, T, W_i, sensor);
   return 0;
+}
+
+int or_set_shock_sensor(void* h, int type, double ducros_treduc) {
+  Ctx& c = *static_cast<Ctx*>(h);
+  if ((type != IZEM_SENSOR_ADAMS_SHARIFF && type != IZEM_SENSOR_DUCROS) || c.cfg.ndim < 2 ||
+      !(ducros_treduc >= 0.0 && ducros_treduc <= 1.0))
+    return IZEM_ERR_ARG;
+  c.sensor_type = type;
+  c.ducros_treduc = ducros_treduc;
+  return IZEM_OK;
 }
 int or_euler_flux(void* h, int dir, const double* v, const double* T, const double* W_i, const double* cp,
                   const double* ha, const uint8_t* sensor, double* fl) {

@@ -50,6 +50,8 @@ struct izem_ctx {
   int sensor_bx = 0;
   int newton_bx = 0;   // x-block size of the Newton stopping test (nx: one block)
   int nsm = 0;         // SMs of the context's device (the host-transfer kernel's grid)
+  int sensor_type = 0;          // IZEM_SENSOR_ADAMS_SHARIFF or IZEM_SENSOR_DUCROS
+  double ducros_treduc = 0.2;   // DUCROS_TREDUC
   double* fhat_edge = nullptr;
   long long nedge = 0;
   // chemistry

@@ -454,13 +454,31 @@ int enq_update_primitives_after(izem_ctx* c, int stage = -1) {
   return enq_boundaries<NRV>(c, stage >= 0 ? c->d_dt : c->d_dt + 2, stage >= 0 ? tk3[stage] : 0.0);
 }
 
+// The stage's shock sensor (module_solver.f90:758-766): Adams-Shariff on the
+// conserved state, or Ducros on the velocity gradients of the primitives
+// (which it then leaves computed).
+template <int NRV>
+int enq_sensor_prim(izem_ctx* c) {
+  const Geo& g = c->g;
+  int rc;
+  if (c->sensor_type == IZEM_SENSOR_DUCROS) {
+    if ((rc = enq_prim<NRV>(c))) return rc;
+    Metrics mt;
+    for (int d = 0; d < 3; ++d) mt.dxi[d] = c->dxi[d];
+    return launch(c, "sensor", [&] {
+      k_sensor_ducros<<<grid_for(g.nint), kThreads, 0, c->stream>>>(g, mt, c->prim, c->ducros_treduc, c->sensor);
+    });
+  }
+  if ((rc = launch(c, "sensor", [&] { k_sensor<<<grid_for(g.nint), kThreads, 0, c->stream>>>(g, c->cfg.max_rel_weight, c->v, c->T, c->W_i, c->sensor, c->sensor_bx); })))
+    return rc;
+  return enq_prim<NRV>(c);
+}
+
 template <int NRV>
 int enq_stage(izem_ctx* c, int stage) {
   const Geo& g = c->g;
   int rc;
-  if ((rc = launch(c, "sensor", [&] { k_sensor<<<grid_for(g.nint), kThreads, 0, c->stream>>>(g, c->cfg.max_rel_weight, c->v, c->T, c->W_i, c->sensor, c->sensor_bx); })))
-    return rc;
-  if ((rc = enq_prim<NRV>(c))) return rc;
+  if ((rc = enq_sensor_prim<NRV>(c))) return rc;
   for (int d = 0; d < c->cfg.ndim; ++d)   // euler_LLF_z only in 3-D (module_solver.f90:769-774)
     if ((rc = enq_euler<NRV>(c, d))) return rc;
   if (c->cfg.vis)
@@ -539,8 +557,10 @@ int do_timestep(izem_ctx* c) {
   });
 }
 
+// the sensor alone (the Ducros sensor needs the primitives' velocities)
 template <int NRV>
 int do_sensor(izem_ctx* c) {
+  if (c->sensor_type == IZEM_SENSOR_DUCROS) return enq_sensor_prim<NRV>(c);
   const Geo& g = c->g;
   return launch(c, "sensor", [&] { k_sensor<<<grid_for(g.nint), kThreads, 0, c->stream>>>(g, c->cfg.max_rel_weight, c->v, c->T, c->W_i, c->sensor, c->sensor_bx); });
 }
@@ -1376,6 +1396,20 @@ int izem_gpu_set_jet(izem_ctx* c, const izem_jet* p) {
   drop_graphs(c);   // captured graphs hold the jet constants by value
   c->jet_par = *p;
   jet_args(c);
+  return IZEM_OK;
+}
+
+int izem_gpu_set_shock_sensor(izem_ctx* c, int type, double ducros_treduc) {
+  if (!c) return IZEM_ERR_ARG;
+  if (type != IZEM_SENSOR_ADAMS_SHARIFF && type != IZEM_SENSOR_DUCROS)
+    return ctx_fail(c, IZEM_ERR_ARG, "unknown shock sensor type", cudaSuccess);
+  if (type == IZEM_SENSOR_DUCROS && c->cfg.ndim < 2)
+    return ctx_fail(c, IZEM_ERR_ARG, "the Ducros sensor needs a 2-D or 3-D block", cudaSuccess);
+  if (!(ducros_treduc >= 0.0 && ducros_treduc <= 1.0))
+    return ctx_fail(c, IZEM_ERR_ARG, "DUCROS_TREDUC outside [0, 1]", cudaSuccess);
+  drop_graphs(c);   // the captured RK3 graph holds the other sensor kernel
+  c->sensor_type = type;
+  c->ducros_treduc = ducros_treduc;
   return IZEM_OK;
 }
 

@@ -57,6 +57,82 @@ struct Metrics {
   const double* dxi[3];   // indexed (s - 1 + ng)
 };
 
+// d?_fixed1 (module_deriv.f90:926-1171 and the y, z copies) at one interior
+// point in IEEE round-to-nearest operations without contraction, in the
+// reference's loop order (dd = dd + alpha(l) v(i+l), zero weights included,
+// then dd dx_i): the same bits as a host evaluation of those loops.
+__device__ __forceinline__ double deriv_rn(const double* __restrict__ a, long long p, long long stride, int s, int n,
+                                          int lo_b, int hi_b, double di, int ng) {
+  const double a4ol[5] = {-25.0 / 12.0, 48.0 / 12.0, -36.0 / 12.0, 16.0 / 12.0, -3.0 / 12.0};
+  const double a4ul[5] = {-3.0 / 12.0, -10.0 / 12.0, 18.0 / 12.0, -6.0 / 12.0, 1.0 / 12.0};
+  const double a4[5] = {1.0 / 12.0, -8.0 / 12.0, 0.0, 8.0 / 12.0, -1.0 / 12.0};
+  const double a4ur[5] = {1.0 / 12.0, -6.0 / 12.0, 18.0 / 12.0, -10.0 / 12.0, -3.0 / 12.0};
+  const double a4or[5] = {-3.0 / 12.0, 16.0 / 12.0, -36.0 / 12.0, 48.0 / 12.0, -25.0 / 12.0};
+  const double a6[7] = {-1.0 / 60.0, 9.0 / 60.0, -45.0 / 60.0, 0.0, 45.0 / 60.0, -9.0 / 60.0, 1.0 / 60.0};
+  const double a8[9] = {3.0 / 840.0,   -32.0 / 840.0, 168.0 / 840.0, -672.0 / 840.0, 0.0,
+                        672.0 / 840.0, -168.0 / 840.0, 32.0 / 840.0, -3.0 / 840.0};
+  const double* w;
+  int l0, l1;
+  bool neg = false;
+  if (lo_b && s == 1) { w = a4ol; l0 = 0; l1 = 4; }
+  else if (lo_b && s == 2) { w = a4ul; l0 = -1; l1 = 3; }
+  else if (lo_b && s == 3) { w = a4; l0 = -2; l1 = 2; }
+  else if (ng == 4 && ((lo_b && s == 4) || (hi_b && s == n - 3))) { w = a6; l0 = -3; l1 = 3; }
+  else if (hi_b && s == n - 2) { w = a4; l0 = -2; l1 = 2; }
+  else if (hi_b && s == n - 1) { w = a4ur; l0 = -3; l1 = 1; neg = true; }
+  else if (hi_b && s == n) { w = a4or; l0 = -4; l1 = 0; neg = true; }
+  else if (ng == 4) { w = a8; l0 = -4; l1 = 4; }
+  else { w = a6; l0 = -3; l1 = 3; }
+  double dd = 0.0;
+  for (int l = l0; l <= l1; ++l) dd = __dadd_rn(dd, __dmul_rn(w[l - l0], a[p + l * stride]));
+  return neg ? __dmul_rn(-dd, di) : __dmul_rn(dd, di);
+}
+
+// compute_duixj + shock_sensor_ducros (module_tools.f90:2521-2719): at every
+// interior point the velocity gradient tensor (dx_fixed1 of u = rho u / rho),
+// then the flag is set (never cleared) where
+// (div u)^2 / ((div u)^2 + |curl u|^2 + 1e-30) > ducros_treduc.  The
+// criterion's operations are uncontracted, in the reference's order.
+__global__ void k_sensor_ducros(Geo g, Metrics mt, const double* __restrict__ prim, double treduc,
+                                uint8_t* __restrict__ sensor) {
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= g.nint) return;
+  int c[3];
+  c[0] = (int)(idx % g.n[0]) + 1;
+  long long r = idx / g.n[0];
+  c[1] = (int)(r % g.n[1]) + 1;
+  c[2] = (int)(r / g.n[1]) + 1;
+  const long long nc = g.ncell;
+  const long long p = gid(g, c[0], c[1], c[2]);
+  const long long strides[3] = {1LL, (long long)g.g[0], (long long)g.g[0] * g.g[1]};
+  const int nd = g.ndim;
+  double du[9];   // du_a / dx_d at a * nd + d, a = u, v (, w)
+  for (int a = 0; a < nd; ++a)
+    for (int d = 0; d < nd; ++d)
+      du[a * nd + d] = deriv_rn(prim + (PR_U + a) * nc, p, strides[d], c[d], g.n[d], g.bnd[2 * d], g.bnd[2 * d + 1],
+                                mt.dxi[d][c[d] - 1 + g.ng], g.ng);
+  double div, vort, wrk;
+  if (nd == 3) {
+    div = __dadd_rn(__dadd_rn(du[0], du[4]), du[8]);
+    div = __dmul_rn(div, div);
+    wrk = __dsub_rn(du[7], du[5]);
+    vort = __dmul_rn(wrk, wrk);
+    wrk = __dsub_rn(du[2], du[6]);
+    wrk = __dmul_rn(wrk, wrk);
+    vort = __dadd_rn(vort, wrk);
+    wrk = __dsub_rn(du[3], du[1]);
+    wrk = __dmul_rn(wrk, wrk);
+    vort = __dadd_rn(vort, wrk);
+  } else {
+    div = __dadd_rn(du[0], du[3]);
+    div = __dmul_rn(div, div);
+    wrk = __dsub_rn(du[2], du[1]);
+    vort = __dmul_rn(wrk, wrk);
+  }
+  const double ducloc = __ddiv_rn(div, __dadd_rn(__dadd_rn(div, vort), 1.0e-30));
+  if (ducloc > treduc) sensor[p] = 1;
+}
+
 // First derivatives of u, v, w, T (fd 1..12) and of the mole fractions
 // (fd 13.. : 3 per species) at interior points (module_viscflux.f90:1764-1804).
 template <int NRV>

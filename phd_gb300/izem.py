@@ -58,6 +58,7 @@ def load_library(path=None):
         "izem_gpu_euler_flux": (C.c_int, [P, C.c_int]),
         "izem_gpu_visc_flux": (C.c_int, [P]),
         "izem_gpu_nr_flux": (C.c_int, [P]),
+        "izem_gpu_set_shock_sensor": (C.c_int, [P, C.c_int, C.c_double]),
         "izem_gpu_update_primitives": (C.c_int, [P]),
         "izem_gpu_finalize_ic": (C.c_int, [P]),
         "izem_gpu_rk3": (C.c_int, [P, C.c_double, C.c_double]),
@@ -281,6 +282,12 @@ class IzemGPU:
 
     def viscflux_xyz(self):
         self._check(self.lib.izem_gpu_visc_flux(self.h), "viscflux_xyz")
+
+    def set_shock_sensor(self, kind="ADAMSSHARIFF", ducros_treduc=0.2):
+        """SHOCK_SENSOR_TYPE ("ADAMSSHARIFF" or "DUCROS") and DUCROS_TREDUC
+        (izem_gpu_set_shock_sensor)."""
+        t = {"ADAMSSHARIFF": 0, "DUCROS": 1}[kind]
+        self._check(self.lib.izem_gpu_set_shock_sensor(self.h, t, float(ducros_treduc)), "set_shock_sensor")
 
     def NR_boundaries(self):
         """bc_noreflectionweno on every non-reflecting face (adds to f)."""

@@ -425,3 +425,49 @@ def test_rk3_newton_beyond_a_dozen_iterations():
     assert np.all(err <= TOL), err
     errT = np.abs(interior(got["T"]) - interior(st["T"])).max() / np.abs(interior(st["T"])).max()
     assert errT <= TOL, errT
+
+
+@pytest.mark.parametrize("name", ["tgv", "mix"])
+def test_ducros_sensor(name):
+    """SHOCK_SENSOR_TYPE = DUCROS (compute_duixj + shock_sensor_ducros,
+    module_tools.f90:2521-2719): the device's flags equal the oracle's bit
+    for bit (uncontracted derivatives and criterion), on a box whose
+    momenta carry seeded noise; the mixing layer adds the one-sided rows of
+    its y faces."""
+    from test_ducros_cpu import shake_velocity
+    cfg, thd, adi, dxi, st, info, orc = W.case(name, 12)
+    shake_velocity(st)
+    orc.update_primitives(st)
+    st["shock_sensor"][...] = 0
+    g = gpu_from(cfg, thd, adi, dxi, st)
+    for h in (orc, g):
+        h.set_shock_sensor("DUCROS", 0.2)
+    orc.shock_sensor(st)
+    g.shock_sensor()
+    got = g.download()["shock_sensor"]
+    g.close()
+    assert 0 < st["shock_sensor"].sum() < st["shock_sensor"][3:-3, 3:-3, 3:-3].size
+    assert np.array_equal(got, st["shock_sensor"])
+
+
+def test_rk3_steps_ducros():
+    """Three RK3 steps of the mixing layer with the Ducros sensor in the
+    captured graph against the oracle: state to TOL, flags bit for bit."""
+    from test_ducros_cpu import shake_velocity
+    cfg, thd, adi, dxi, st, info, orc = W.case("mix", 12)
+    shake_velocity(st, amp=0.05)
+    orc.update_primitives(st)
+    st["shock_sensor"][...] = 0
+    g = gpu_from(cfg, thd, adi, dxi, st)
+    for h in (orc, g):
+        h.set_shock_sensor("DUCROS", 0.2)
+    for _ in range(3):
+        dt4, dt = orc.timestep(st)
+        orc.rk3(st, dt)
+        g.rk3(dt)
+    got = g.download()
+    g.close()
+    assert st["shock_sensor"].sum() > 0
+    assert np.array_equal(got["shock_sensor"], st["shock_sensor"])
+    err = W.normwise(interior(got["v"]), interior(st["v"]))
+    assert np.all(err <= TOL), err
