@@ -452,11 +452,13 @@ class TimeLoop:
     * without chemistry, ``rk3(dtmin)`` and time += dtmin.
 
     The clipping of dtmin onto statistics times (:256-263) belongs to the
-    caller, who may pass ``dt`` to impose a step.  ``chem`` is the hook that
-    runs a chemistry half step and returns DTmax; subclasses wrap it to log
-    per-half-step statistics."""
+    caller, who may pass ``dt`` to impose a step.  ``fixed_dt`` (seconds) is
+    the deck's FIXEDDT / DT: timestep then returns DT / time_ref for all
+    four criteria without evaluating them (module_solver.f90:240-244).
+    ``chem`` is the hook that runs a chemistry half step and returns DTmax;
+    subclasses wrap it to log per-half-step statistics."""
 
-    def __init__(self, solver, reaction, chem_mode=CHEM_BDF, time=0.0):
+    def __init__(self, solver, reaction, chem_mode=CHEM_BDF, time=0.0, fixed_dt=None):
         self.s = solver
         self.reaction = bool(reaction)
         self.mode = chem_mode
@@ -464,12 +466,19 @@ class TimeLoop:
         self.dtmin = 1.0
         self.DTmax = 0.0
         self.dt4 = None
+        self.fixed_dt = fixed_dt
 
     def chem(self, dt):
         return self.s.reaction_selec(dt, mode=self.mode, time=self.time)
 
+    def timestep(self):
+        if self.fixed_dt is not None:
+            dtmin = float(self.fixed_dt) / self.s.adi.time_ref
+            return np.full(4, dtmin), dtmin
+        return self.s.timestep(DTmax=self.DTmax, dtmin=self.dtmin)
+
     def step(self, dt=None):
-        self.dt4, dtmin = self.s.timestep(DTmax=self.DTmax, dtmin=self.dtmin)
+        self.dt4, dtmin = self.timestep()
         if dt is not None:
             dtmin = float(dt)
         if self.reaction:
