@@ -35,7 +35,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 HBM_FALLBACK_GBS = 6800.0
-FP64_PEAK_GFLOPS = 1194.4   # FP64 FMA rate measured on a GB300 by a dependent-FMA probe kernel
+FP64_PEAK_FALLBACK_GFLOPS = 1194.4   # FP64 FMA rate of an earlier GB300 measurement, if the live one fails
 
 
 def measured_peaks():
@@ -45,6 +45,19 @@ def measured_peaks():
             d = json.load(f)
         return float(d.get("hbm_gbs", HBM_FALLBACK_GBS)), "measured"
     return HBM_FALLBACK_GBS, "fallback"
+
+
+def fp64_peak():
+    """The FP64 peak of the rooflines: the device's FMA throughput measured
+    now (izem_gpu_fp64_rate), or the earlier measurement if that fails."""
+    from phd_gb300.izem import fp64_rate
+    try:
+        r = fp64_rate()
+        if r > 0:
+            return r, "measured in this run (FP64 FMA-throughput kernel, best of 3)"
+    except Exception:
+        pass
+    return FP64_PEAK_FALLBACK_GFLOPS, "fallback (an earlier FP64 FMA-throughput measurement)"
 
 
 class ClockSampler:
@@ -258,6 +271,7 @@ def run_gpu(args, rank, world):
     e2e_value = world * ncell * e2e_steps / e2e_s / 1e6
     # ---- roofline of the dominant kernel
     hbm, hbm_src = measured_peaks()
+    f64, f64_src = fp64_peak()
     dom = max(kt.items(), key=lambda kv: kv[1][1])
     dom_name, (dom_n, dom_ms) = dom
     fx = kt.get("euler_face_x", (0, 0.0))
@@ -274,8 +288,8 @@ def run_gpu(args, rank, world):
                    "reactors_per_launch": nre, "bdf_steps_per_launch": timed_bdf}
         if CHEM_FLOP_PER_BDF_STEP and timed_bdf:
             gf = CHEM_FLOP_PER_BDF_STEP * sum(timed_bdf) / (ms_l * 1e-3) / 1e9
-            rl_chem["fp64"] = {"achieved": gf, "peak": FP64_PEAK_GFLOPS, "unit": "GFLOP/s",
-                               "frac": gf / FP64_PEAK_GFLOPS}
+            rl_chem["fp64"] = {"achieved": gf, "peak": f64, "unit": "GFLOP/s", "frac": gf / f64,
+                               "peak_source": f64_src}
     if fx[0]:
         avg_s = fx[1] / fx[0] * 1e-3
         byts = euler_face_bytes(cfg)
@@ -285,8 +299,8 @@ def run_gpu(args, rank, world):
               "peak_source": hbm_src + " (MEASURED_PEAKS.json hbm_gbs)"}
         if cfg.nrv in EULER_FLOP_PER_FACE:
             flops = nf * EULER_FLOP_PER_FACE[cfg.nrv]
-            rl["fp64"] = {"achieved": flops / avg_s / 1e9, "peak": FP64_PEAK_GFLOPS, "unit": "GFLOP/s",
-                          "frac": flops / avg_s / 1e9 / FP64_PEAK_GFLOPS}
+            rl["fp64"] = {"achieved": flops / avg_s / 1e9, "peak": f64, "unit": "GFLOP/s",
+                          "frac": flops / avg_s / 1e9 / f64, "peak_source": f64_src}
     launches = sum(n for n, _ in kt.values())
     mlp = run_mlp_chem(args, g, stp, ncell, world) if chem and not args.no_mlp else None
     res = {

@@ -459,6 +459,11 @@ int  izem_gpu_set_chem_variant(int variant);
  * mechanism's tables (any other mechanism).  No counterpart in the
  * reference. */
 int  izem_gpu_chem_generated(void);
+/* FP64 FMA throughput of the current device in GFLOP/s (8 independent FMA
+ * chains per thread over 8 x 256 threads per SM, best of three timed
+ * launches): the FP64 peak the rooflines are quoted against.  No
+ * counterpart in the reference. */
+int  izem_gpu_fp64_rate(double* gflops);
 /* allow = 0 makes the chemistry kernels walk the mechanism's tables even
  * for the shipped mechanism (to compare the two forms); allow = 1 (the
  * default) uses the generated form whenever it applies.  Takes effect at

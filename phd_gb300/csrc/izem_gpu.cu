@@ -1442,6 +1442,56 @@ int izem_gpu_set_les(izem_ctx* c, int enable, double mu_sgs_factor, double sc_sg
 
 int izem_gpu_set_chem_variant(int variant) { return chem_set_variant(variant) == 0 ? IZEM_OK : IZEM_ERR_ARG; }
 
+// FP64 FMA throughput of the current device: 8 independent FMA chains per
+// thread, 8 blocks of 256 threads per SM, timed with CUDA events; the
+// denominator of the FP64 rooflines.
+namespace {
+__global__ void k_fp64_fma(double* out, int iters, double a, double b) {
+  double x[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) x[q] = threadIdx.x * 1.0e-3 + q;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int q = 0; q < 8; ++q) x[q] = fma(x[q], a, b);
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) s += x[q];
+  if (s == -1.0) out[0] = s;   // never true; keeps the chains
+}
+}  // namespace
+
+int izem_gpu_fp64_rate(double* gflops) {
+  if (!gflops) return IZEM_ERR_ARG;
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return IZEM_ERR_CUDA;
+  double* out = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (cudaMalloc(&out, sizeof(double)) != cudaSuccess) return IZEM_ERR_NOMEM;
+  int rc = IZEM_OK;
+  const int iters = 2048, threads = 256, blocks = 8 * sms;
+  double best = 0.0;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) rc = IZEM_ERR_CUDA;
+  for (int r = 0; r < 4 && rc == IZEM_OK; ++r) {   // the first launch warms up
+    cudaEventRecord(e0);
+    k_fp64_fma<<<blocks, threads>>>(out, iters, 0.9999999, 1.0e-7);
+    cudaEventRecord(e1);
+    float ms = 0.f;
+    if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+      rc = IZEM_ERR_CUDA;
+      break;
+    }
+    const double flop = 2.0 * 8.0 * iters * (double)threads * blocks;
+    if (r > 0 && ms > 0.f) best = std::max(best, flop / (ms * 1.0e-3) / 1.0e9);
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaFree(out);
+  *gflops = best;
+  return rc;
+}
+
 int izem_gpu_chem_generated(void) { return chem_generated_rhs(); }
 
 int izem_gpu_allow_chem_generated(int allow) {

@@ -80,6 +80,7 @@ def load_library(path=None):
         "izem_gpu_autotune": (C.c_int, [P, C.c_double, C.c_char_p, C.c_int]),
         "izem_gpu_set_chem_variant": (C.c_int, [C.c_int]),
         "izem_gpu_chem_generated": (C.c_int, []),
+        "izem_gpu_fp64_rate": (C.c_int, [_dp]),
         "izem_gpu_allow_chem_generated": (C.c_int, [C.c_int]),
         "izem_gpu_set_sensor_xblocks": (C.c_int, [P, C.c_int]),
         "izem_gpu_set_chem_skip": (C.c_int, [P, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_int]),
@@ -438,6 +439,17 @@ class IzemGPU:
 
 
 CHEM_BDF, CHEM_MLP = 0, 1
+
+
+def fp64_rate():
+    """FP64 FMA throughput of the current device in GFLOP/s
+    (izem_gpu_fp64_rate)."""
+    lib = load_library()
+    out = np.zeros(1)
+    rc = lib.izem_gpu_fp64_rate(out.ctypes.data_as(_dp))
+    if rc:
+        raise IzemError(rc, "izem_gpu_fp64_rate")
+    return float(out[0])
 
 
 class TimeLoop:
