@@ -161,9 +161,9 @@ typedef struct izem_ctx izem_ctx;
 
 /* Create a context on the current CUDA device.  Allocates the device-resident
  * state (v, T, W_i, cp, ha, shock sensor) and the RK3 scratch (v0, f).
- * Supported: ng = 3 (WENO5) in 3-D or 2-D, ng = 4 (WENO7) for two-species
- * sets; ndim = 2 needs nz = 1 (no z sweep, no z derivatives); EGLIB
- * transport in 3-D with ng = 3.  Other configurations return IZEM_ERR_ARG.
+ * Supported: ng = 3 (WENO5) or ng = 4 (WENO7), two or nine species, in 3-D
+ * or 2-D; ndim = 2 needs nz = 1 (no z sweep, no z derivatives); EGLIB
+ * transport in 3-D.  Other configurations return IZEM_ERR_ARG.
  * Replaces the allocations at module_solver.f90:736-739 and the per-call
  * temporaries of module_weno.f90:588-607, module_viscflux.f90:1708-1714. */
 int  izem_gpu_init(const izem_cfg* cfg, const izem_thd* thd, const izem_adi* adi,

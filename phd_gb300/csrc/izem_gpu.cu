@@ -275,12 +275,10 @@ int enq_euler(izem_ctx* c, int d) {
   k_euler_face<NRV, DD, NGV><<<grid_for(nf, c->tb_euler), c->tb_euler, 0, c->stream>>>(                                \
       g, c->cfg.weno_avg, c->cfg.weno5_linear_fix, c->v, c->prim, c->sensor, c->fhat, nf, c->sensor_bx, 0)
   rc = launch(c, names[d], [&] {
-    if (g.ng == 4) {   // WENO7, two-species sets only (checked at init)
-      if constexpr (NRV == 2) {
-        if (d == 0) IZEM_FACE(0, 4);
-        if (d == 1) IZEM_FACE(1, 4);
-        if (d == 2) IZEM_FACE(2, 4);
-      }
+    if (g.ng == 4) {   // WENO7
+      if (d == 0) IZEM_FACE(0, 4);
+      if (d == 1) IZEM_FACE(1, 4);
+      if (d == 2) IZEM_FACE(2, 4);
     } else {
       if (d == 0) IZEM_FACE(0, 3);
       if (d == 1) IZEM_FACE(1, 3);
@@ -294,11 +292,8 @@ int enq_euler(izem_ctx* c, int d) {
 #define IZEM_EDGE(NGV)                                                                                            \
   k_euler_face<NRV, 0, NGV><<<grid_for(c->nedge, c->tb_euler), c->tb_euler, 0, c->stream>>>(                      \
       g, c->cfg.weno_avg, c->cfg.weno5_linear_fix, c->v, c->prim, c->sensor, c->fhat_edge, c->nedge, c->sensor_bx, 1)
-      if (g.ng == 4) {
-        if constexpr (NRV == 2) IZEM_EDGE(4);
-      } else {
-        IZEM_EDGE(3);
-      }
+      if (g.ng == 4) IZEM_EDGE(4);
+      else IZEM_EDGE(3);
 #undef IZEM_EDGE
     });
   }
@@ -376,11 +371,9 @@ int enq_nr(izem_ctx* c) {
 #define IZEM_NR(DD, NGV)                                                                                           \
   k_bc_nr<NRV, DD, NGV><<<grid_for(np), kThreads, 0, c->stream>>>(g, hi, c->v, c->T, c->W_i, c->cp, c->ha, c->dxi[DD], c->f)
       if (g.ng == 4) {
-        if constexpr (NRV == 2) {
-          if (d == 0) IZEM_NR(0, 4);
-          if (d == 1) IZEM_NR(1, 4);
-          if (d == 2) IZEM_NR(2, 4);
-        }
+        if (d == 0) IZEM_NR(0, 4);
+        if (d == 1) IZEM_NR(1, 4);
+        if (d == 2) IZEM_NR(2, 4);
       } else {
         if (d == 0) IZEM_NR(0, 3);
         if (d == 1) IZEM_NR(1, 3);
@@ -649,9 +642,9 @@ extern "C" {
 int izem_gpu_init(const izem_cfg* cfg, const izem_thd* thd, const izem_adi* adi, izem_ctx** out) {
   if (!cfg || !thd || !adi || !out) return IZEM_ERR_ARG;
   *out = nullptr;
-  // WENO5 (ng = 3) in 2-D or 3-D; WENO7 (ng = 4) for two-species sets;
-  // 2-D runs have nz = 1; EGLIB transport in 3-D WENO5 only
-  const bool ng_ok = cfg->ng == 3 || (cfg->ng == 4 && cfg->nrv == 2 && !cfg->eglib);
+  // WENO5 (ng = 3) or WENO7 (ng = 4) in 2-D or 3-D; 2-D runs have nz = 1;
+  // EGLIB transport in 3-D only
+  const bool ng_ok = cfg->ng == 3 || cfg->ng == 4;
   const bool dim_ok = cfg->ndim == 3 || (cfg->ndim == 2 && cfg->nz == 1 && !cfg->eglib);
   if (!ng_ok || !dim_ok || !(cfg->nrv == 2 || cfg->nrv == 9) || thd->nspc != cfg->nrv) return IZEM_ERR_ARG;
   const int nmin = 2 * cfg->ng + 1;

@@ -136,8 +136,9 @@ def tgv(n=64, lib_dscalar=None):
     return cfg, thd, adi_struct(a), dxi, state, info
 
 
-def mixing_layer(nx=256, ny=256, nz=128, Lx=12e-3, Ly=12e-3, Lz=6e-3, seed=SEED, lib_dscalar=None):
-    """Temporal H2/air mixing layer (9 species), x and z periodic, y extrapolation."""
+def mixing_layer(nx=256, ny=256, nz=128, Lx=12e-3, Ly=12e-3, Lz=6e-3, seed=SEED, lib_dscalar=None, ng=3):
+    """Temporal H2/air mixing layer (9 species), x and z periodic, y
+    extrapolation; ng = 3 (WENO5) or 4 (WENO7)."""
     a = constants()
     sp = load_species("h2air9")
     thd = thd_init(sp, a)
@@ -159,10 +160,11 @@ def mixing_layer(nx=256, ny=256, nz=128, Lx=12e-3, Ly=12e-3, Lz=6e-3, seed=SEED,
     w = 0.01 * dU * rng.standard_normal(Xg.shape)
     Wmix_i = np.einsum("...k,k->...", Ys, 1.0 / (np.array(sp["W_gmol"]) * 1e-3))
     rho = p0 / (a["r_ref"] * Wmix_i * T)
-    state = _state_from_primitives(thd, a, rho, u, v, w, T, Ys, 3)
+    state = _state_from_primitives(thd, a, rho, u, v, w, T, Ys, ng)
     bc = (BC_PERIODIC, BC_PERIODIC, BC_EXTRAPOLATION, BC_EXTRAPOLATION, BC_PERIODIC, BC_PERIODIC)
     cfg = make_cfg(nx, ny, nz, 9, bc=bc)
-    dxi = [grid_dxi(x, 3, a, lib_dscalar), grid_dxi(y, 3, a, lib_dscalar), grid_dxi(z, 3, a, lib_dscalar)]
+    cfg.ng = ng
+    dxi = [grid_dxi(x, ng, a, lib_dscalar), grid_dxi(y, ng, a, lib_dscalar), grid_dxi(z, ng, a, lib_dscalar)]
     info = {"name": "H2/air temporal mixing layer %dx%dx%d" % (nx, ny, nz), "delta": delta, "dU": dU, "seed": seed}
     return cfg, thd, adi_struct(a), dxi, state, info
 

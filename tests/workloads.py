@@ -12,17 +12,18 @@ def _copy(state):
     return {k: np.array(v, order="F", copy=True) for k, v in state.items()}
 
 
-def case(name, n=12, seed=ics.SEED, eglib=False, vis_dt=False):
+def case(name, n=12, seed=ics.SEED, eglib=False, vis_dt=False, ng=3):
     """Returns cfg, thd, adi, dxi, finalized state (oracle-closed), info.
     eglib: EGLIB precision-1 transport (cfg.eglib = 1, linking data set on
     the oracle; the caller sets it on the GPU context).  vis_dt: the Fourier
-    criteria of the time step (cfg.vis_dt = 1)."""
+    criteria of the time step (cfg.vis_dt = 1).  ng = 4: WENO7 (mixing
+    layer only)."""
     if name == "tgv":
         cfg, thd, adi, dxi, st, info = ics.tgv(n, lib_dscalar=oracle.metrics_dscalar)
     elif name == "mix":
-        cfg, thd, adi, dxi, st, info = ics.mixing_layer(n, n, max(n // 2, 8), Lx=n * 47e-6, Ly=n * 47e-6,
-                                                         Lz=max(n // 2, 8) * 47e-6, seed=seed,
-                                                         lib_dscalar=oracle.metrics_dscalar)
+        nz = max(n // 2, 8, 2 * ng + 1)
+        cfg, thd, adi, dxi, st, info = ics.mixing_layer(n, n, nz, Lx=n * 47e-6, Ly=n * 47e-6, Lz=nz * 47e-6,
+                                                         seed=seed, lib_dscalar=oracle.metrics_dscalar, ng=ng)
     else:
         raise KeyError(name)
     if eglib:
