@@ -365,7 +365,8 @@ def run_mlp_chem(args, g, stp, ncell, world):
     held = flow_reactors(g, mech, 0.5 * dt, n_max=1 << 17, spread=0.05, seed=6, age=age)
     t_label = time.perf_counter() - t0
     t0 = time.perf_counter()
-    nets = train_on(X, Yt, epochs=42, batch=4096, E=E)
+    epochs = 60
+    nets = train_on(X, Yt, epochs=epochs, batch=4096, E=E)
     t_train = time.perf_counter() - t0
     gate, calib = calibrate_flow_gate(nets, mech, X, Yt, held, target=0.008)
     g.set_surrogate(nets[0], nets[1], gate=gate)
@@ -421,7 +422,7 @@ def run_mlp_chem(args, g, stp, ncell, world):
                                  "ms": lg[:, 3].round(2).tolist(),
                                  "network_ms": lg[:, 4].round(2).tolist()},
             "accuracy_replay": {"half_steps": chk.rows, "max_err_frac_over_states": max(errs) if errs else None},
-            "training": {"samples": int(len(X)), "networks": 2, "epochs": 42, "aged_half_steps_max": age,
+            "training": {"samples": int(len(X)), "networks": 2, "epochs": epochs, "aged_half_steps_max": age,
                          "target": "increment minus dt f(y0)",
                          "label_s": t_label, "train_s": t_train},
             "gate": gate_json(gate), "gate_calibration": calib, "clocks": clk.summary()}

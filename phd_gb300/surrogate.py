@@ -433,7 +433,7 @@ def flow_gate(X, Yt, dT_tol_frac=0.002):
             2.5 * f, float("inf"))
 
 
-FLOW_TOL_LADDER = (0.00025, 0.0005, 0.001, 0.002, 0.004, 0.008)
+FLOW_TOL_LADDER = (0.00025, 0.0005, 0.00075, 0.001, 0.0015, 0.002, 0.003, 0.004, 0.008)
 
 
 def calibrate_flow_gate(nets, mech, X, Yt, held, target=0.005, ladder=FLOW_TOL_LADDER):
