@@ -25,6 +25,7 @@
 #include <cuda_bf16.h>
 #include "../../include/izem_gpu.h"
 #include "chem.h"
+#include "atomics.cuh"
 
 // This source builds two translation units, compiled in parallel:
 // IZEM_CHEM_UNIT 0 (chem.cu) holds the host side and the kernels that walk
@@ -1210,7 +1211,7 @@ __global__ void k_chem_scatter(ChemField f, const double* T, const double* Y, Ch
   const double T0 = f.T[p] * f.t_ref;
   f.T[p] = T[q] * f.tref_i;
   const double dT = fabs(T[q] - T0);
-  atomicMax(&stats->dtmax_bits, (unsigned long long)__double_as_longlong(dT));
+  atomic_max_nonneg_warp(&stats->dtmax_bits, dT);
   double sumY = 0.0;
 #pragma unroll
   for (int l = 0; l < KK - 1; ++l) {
@@ -1264,7 +1265,7 @@ __global__ void k_chem_scatter_list(ChemField f, const int* list, const unsigned
   const double T0 = f.T[p] * f.t_ref;
   f.T[p] = T[q] * f.tref_i;
   const double dT = fabs(T[q] - T0);
-  atomicMax(&stats->dtmax_bits, (unsigned long long)__double_as_longlong(dT));
+  atomic_max_nonneg_warp(&stats->dtmax_bits, dT);
   double sumY = 0.0;
 #pragma unroll
   for (int l = 0; l < KK - 1; ++l) {

@@ -1,6 +1,7 @@
 // Shared device definitions for the IZEM RHS kernels (sm_103a).
 #pragma once
 #include <cstdint>
+#include "atomics.cuh"
 #include <cuda_runtime.h>
 #include "../../include/izem_gpu.h"
 
@@ -78,9 +79,6 @@ struct DevStatus {
   int chem_fail;
 };
 
-__device__ inline void atomic_max_nonneg(unsigned long long* addr, double v) {
-  atomicMax(addr, (unsigned long long)__double_as_longlong(v));
-}
 
 // Seeded fluctuation of the jet inflow: uniform in [-1, 1) from a hash
 // (splitmix64 finaliser, Steele, Lea and Flood 2014) of the seed, the face

@@ -219,8 +219,11 @@ __global__ void k_newton_iter(Geo g, int ghost, const double* __restrict__ v, do
   T[p] = Tn;
   if (check_negT && Tn < 0.0) atomicExch(&st->neg_temperature, 1);
   const double df2 = DF * DF;
-  if (df2 != df2) atomicExch(&st->newton_nan, 1);
-  else atomic_max_nonneg(&st->maxdf_bits[dom], df2);
+  const bool nan = df2 != df2;
+  if (nan) atomicExch(&st->newton_nan, 1);
+  // the sub-domain's largest correction, combined over the warp's lanes of
+  // the same sub-domain (a NaN counts as 0 here; the flag records it)
+  atomic_max_nonneg_warp(&st->maxdf_bits[dom], nan ? 0.0 : df2);
 }
 
 // Stopping test of prim_inv_var (module_thermodynamics.f90:110-115,161-162)
