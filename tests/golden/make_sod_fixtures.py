@@ -18,7 +18,10 @@ rhoE, O2, N2 with shape (ntx, nty, ntz) in Fortran index order, and time)
 tests/golden/sod_grid.npz (the x, y, z coordinates of grid.dat, in
 metres, parsed as the reference's list-directed read parses them) and
 tests/golden/sod_plot_000NN.npz (temperature, pressure, density and x
-velocity of the post-processor's FP32 plot files, dimensional).
+velocity of the post-processor's FP32 plot files, dimensional) and
+tests/golden/sod_weno5_plot_000NN.npz (the same fields of
+testcases/sod/weno5_400, the run repeated with ORDER_WENO = 5; its 400 x 11
+plot files are the only output of that run the reference ships).
 """
 import os
 import sys
@@ -30,6 +33,7 @@ sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 from phd_gb300.restart import read_h5  # noqa: E402
 RESTARTS = (1, 2, 3, 10)
 PLOTS = (1, 3)
+WENO5_PLOTS = (1, 3)   # testcases/sod/weno5_400: the same run with ORDER_WENO = 5
 
 
 def read_grid(path):
@@ -65,12 +69,12 @@ def read_vtr(path):
     return ext, out
 
 
-def plot_fields(sod_dir, n):
-    """The two x-blocks of plot n merged on the 400 x 11 grid (the blocks
-    share the point at x index 200)."""
+def plot_fields(sod_dir, n, sub="plots"):
+    """The two x-blocks of plot n of the directory `sub` merged on the
+    400 x 11 grid (the blocks share the point at x index 200)."""
     fields = {}
     for piece in (0, 1):
-        ext, d = read_vtr(os.path.join(sod_dir, "plots", "plot%05d_%05d.vtr" % (n, piece)))
+        ext, d = read_vtr(os.path.join(sod_dir, sub, "plot%05d_%05d.vtr" % (n, piece)))
         nxp, nyp = ext[1] - ext[0] + 1, ext[3] - ext[2] + 1
         for name, key in (("Temperature", "T"), ("Pressure", "P"), ("Density", "rho"), ("Velocity-X", "u")):
             a = d[name].reshape(nyp, nxp).T
@@ -89,6 +93,9 @@ def main(sod_dir):
         if n in PLOTS:
             np.savez_compressed(os.path.join(HERE, "sod_plot_%05d.npz" % n), **plot_fields(sod_dir, n))
         print(n, {k: v.shape for k, v in arrays.items()}, float(arrays["time"][0]))
+    for n in WENO5_PLOTS:
+        np.savez_compressed(os.path.join(HERE, "sod_weno5_plot_%05d.npz" % n),
+                            **plot_fields(sod_dir, n, sub="weno5_400"))
 
 
 if __name__ == "__main__":

@@ -34,18 +34,22 @@ def golden(n):
     return np.load(os.path.join(HERE, "golden", "sod_restart_%05d.npz" % n))
 
 
-def golden_plot(n):
+def golden_plot(n, weno5=False):
     """Temperature [K], pressure [Pa], density [kg/m^3] and x velocity [m/s]
-    of the reference's plot file n (FP32), shape (ntx, nty)."""
-    return np.load(os.path.join(HERE, "golden", "sod_plot_%05d.npz" % n))
+    of the reference's plot file n (FP32), shape (ntx, nty); weno5: of the
+    run repeated with ORDER_WENO = 5 (testcases/sod/weno5_400)."""
+    name = "sod_weno5_plot_%05d.npz" if weno5 else "sod_plot_%05d.npz"
+    return np.load(os.path.join(HERE, "golden", name % n))
 
 
-def sod_case(xblocks=NX_BLOCKS):
+def sod_case(xblocks=NX_BLOCKS, ng=NG):
     """Configuration, species data, references, oracle, the ghosted initial
     state (closed by finalize_ic) and the metrics (dx_i, dy_i, dz_i) of the
     reference's Sod run.  xblocks: the MPI x-blocks of the reference's run,
     whose effects on the shock sensor and on the Newton stopping test the
-    oracle emulates (1 for a single block)."""
+    oracle emulates (1 for a single block).  ng = 3: the same run with
+    ORDER_WENO = 5 (testcases/sod/weno5_400)."""
+    NG = ng
     a = constants()
     sp = load_species("o2n2")
     thd = thd_init(sp, a)

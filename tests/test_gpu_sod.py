@@ -198,3 +198,35 @@ def test_gpu_resumes_reference_restart(tmp_path):
             assert err <= 1e-10 * rho_max, (name, err)
         else:
             assert err <= 5e-10 * np.abs(vo[..., q]).max(), (name, err / np.abs(vo[..., q]).max())
+
+
+def test_gpu_reproduces_reference_weno5_plots():
+    """The Sod run with ORDER_WENO = 5 on the GPU (two emulated x-blocks, as
+    the reference ran it) against the FP32 plot files of the reference's
+    WENO5 run (testcases/sod/weno5_400) at statistics times 1 and 3: the
+    temperature, pressure, density and x velocity within the oracle's bound
+    (tests/test_sod_pin.py, WENO5_PLOT_TOL)."""
+    from test_sod_pin import WENO5_PLOT_TOL, plot_fields
+    cfg, thd, a, orc, st, grid = S.sod_case(xblocks=S.NX_BLOCKS, ng=3)
+    g = _gpu(cfg, thd, a, grid, st)
+    g.set_sensor_xblocks(S.NX_BLOCKS)
+    timing = S.stat_times(a, 3)
+    time, nb, out = 0.0, 0, []
+    while nb < 3:
+        _, dtmin = g.timestep()
+        write = False
+        if time + dtmin > timing[nb] and time - dtmin < timing[nb]:
+            dtmin = timing[nb] - time
+            write = True
+        g.rk3(dtmin)
+        time = time + dtmin
+        if write:
+            nb += 1
+            out.append(g.download())
+    g.close()
+    for n in (1, 3):
+        d = out[n - 1]
+        ref = S.golden_plot(n, weno5=True)
+        for k, x in plot_fields(a, d["v"], d["T"], d["W_i"], 3).items():
+            err = np.abs(x - ref[k]).max() / np.abs(ref[k]).max()
+            assert err <= WENO5_PLOT_TOL, (n, k, err)
