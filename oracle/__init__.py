@@ -176,7 +176,8 @@ class Oracle:
         self._rc(self.lib.or_set_sensor_xblocks(self.h, int(nblk)), "set_sensor_xblocks")
 
     def set_les(self, mu_sgs_factor=0.18, sc_sgs=0.7, pr_sgs=0.7, percent_weight_sgs=70.0, enable=True):
-        """LES with the Smagorinsky closure under EGLIB (viscflux_eg_LES_xyz)."""
+        """LES with the Smagorinsky closure: viscflux_eg_LES_xyz under EGLIB,
+        viscflux_LES_xyz with the fitted transport."""
         self._rc(self.lib.or_set_les(self.h, int(bool(enable)), float(mu_sgs_factor), float(sc_sgs), float(pr_sgs),
                                      float(percent_weight_sgs)), "set_les")
 

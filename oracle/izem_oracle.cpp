@@ -74,6 +74,10 @@ struct Ctx {
   // SC_SGS, PR_SGS, PERCENT_WEIGHT_SGS
   bool les = false;
   double les_factor = 0.0, les_sc_sgs = 1.0, les_pr_sgs = 1.0, les_pw = 0.0;
+  // mu_SGS of the last viscflux_LES_xyz call (fitted transport), read by the
+  // Fourier time step; zero until then and under EGLIB, whose LES flux
+  // routine keeps its own copy
+  std::vector<double> mu_sgs;
   // coordinates of the interior points (code units) and the domain length
   // in x (Lx, module_tools.f90:319,489) for the jet boundaries
   std::vector<double> crd[3];
@@ -1296,9 +1300,51 @@ int visc_flux_fit(Ctx& c, const double* v, const double* T, const double* W_i, c
   for (int l = 0; l < nrv; ++l)
     for (int d = 0; d < 3; ++d) deriv(c, d, Xa.data() + (size_t)l * nc, fd.data() + (size_t)(nfluid + 3 * l + d) * nc, false);
   comm_periodic(b, nderiv, fd.data(), nc);   // comm_deriv
+  // LES (viscflux_LES_xyz, module_viscflux.f90:2200-2977): the W_i
+  // gradients (fd nSGS+1..3) and, on the interior, the criterion of
+  // shock_det_ducros_slv (module_tools.f90:2099-2181; 1 elsewhere), both
+  // communicated with the other derivatives
+  const bool les = c.les;
+  std::vector<double> gw, crit;
+  if (les) {
+    gw.assign(3 * nc, std::nan(""));
+    crit.assign(nc, 1.0);
+    for (int d = 0; d < 3; ++d) deriv(c, d, W_i, gw.data() + (size_t)d * nc, false);
+    const double eps30 = 1.0e-30;
+    for (int k = 1; k <= b.nz; ++k)
+      for (int j = 1; j <= b.ny; ++j)
+        for (int i = 1; i <= b.nx; ++i) {
+          const size_t p = b.id(i, j, k);
+          auto D = [&](int q) { return fd[(size_t)(q - 1) * nc + p]; };
+          double div = D(1) + D(5) + D(9);
+          div = div * div;
+          double wrk = D(8) - D(6);
+          double vort = wrk * wrk;
+          wrk = D(3) - D(7);
+          wrk = wrk * wrk;
+          vort = vort + wrk;
+          wrk = D(4) - D(2);
+          wrk = wrk * wrk;
+          vort = vort + wrk;
+          const double r = div / (div + vort + eps30);
+          crit[p] = r > c.les_pw ? 0.0 : 1.0;
+        }
+    comm_periodic(b, 3, gw.data(), nc);
+    comm_periodic(b, 1, crit.data(), nc);
+    if (c.mu_sgs.size() != nc) c.mu_sgs.assign(nc, 0.0);
+  }
+  double cs2 = c.les_factor;
+  cs2 = cs2 * cs2 / a.sqgmr;
+  const double sc_sgs_i = 1.0 / c.les_sc_sgs, pr_sgs_i = 1.0 / c.les_pr_sgs;
+  const double third = 1.0 / 3.0;
 
   std::vector<double> sxx(nc, 0.0), sxy(nc, 0.0), sxz(nc, 0.0), syy(nc, 0.0), syz(nc, 0.0), szz(nc, 0.0);
   std::vector<double> qx(nc, 0.0), qy(nc, 0.0), qz(nc, 0.0);
+  std::vector<double> txx, txy, txz, tyy, tyz, tzz;   // LES: the stresses of the momentum divergence
+  if (les) {
+    txx.assign(nc, 0.0); txy.assign(nc, 0.0); txz.assign(nc, 0.0);
+    tyy.assign(nc, 0.0); tyz.assign(nc, 0.0); tzz.assign(nc, 0.0);
+  }
   for (int dom = -3; dom <= 3; ++dom) {
     int i0, i1, j0, j1, k0, k1;
     domain_select(b, dom, i0, i1, j0, j1, k0, k1);
@@ -1318,6 +1364,21 @@ int visc_flux_fit(Ctx& c, const double* v, const double* T, const double* W_i, c
           auto F = [&](int idx) -> double& { return fd[(size_t)(idx - 1) * nc + p]; };
           double rho_i = 1.0 / v[p];
           double uxs = v[nc + p] * rho_i, vys = v[2 * nc + p] * rho_i, wzs = v[3 * nc + p] * rho_i;
+          // mu_SGS_smagorinsky (module_SGS_models.f90:176-304, 3-D branch)
+          // with filter_width's delta; kept for the Fourier time step
+          double mu_sgs = 0.0;
+          if (les) {
+            const double dxv = c.dxi[0][i - 1 + b.ng], dyv = c.dxi[1][j - 1 + b.ng], dzv = c.dxi[2][k - 1 + b.ng];
+            const double delta = 1.0 / std::pow(dxv * dyv * dzv, third);
+            const double d2 = delta * delta;
+            const double s11 = F(1), s12 = 0.5 * (F(2) + F(4)), s13 = 0.5 * (F(3) + F(7));
+            const double s22 = F(5), s23 = 0.5 * (F(6) + F(8)), s33 = F(9);
+            double sb = s11 * s11 + s12 * s12 + s13 * s13 + s12 * s12 + s22 * s22 + s23 * s23 + s13 * s13 +
+                        s23 * s23 + s33 * s33;
+            sb = std::sqrt(sb + sb);
+            mu_sgs = v[p] * cs2 * d2 * sb * crit[p];
+            c.mu_sgs[p] = mu_sgs;
+          }
           double rmu = -a.sqgmr * mu;
           double rvd = rvd0 * v[p];
           sxx[p] = twothirds * rmu * (F(1) + F(1) - (F(5) + F(9)));
@@ -1326,6 +1387,12 @@ int visc_flux_fit(Ctx& c, const double* v, const double* T, const double* W_i, c
           syy[p] = twothirds * rmu * (F(5) + F(5) - (F(1) + F(9)));
           syz[p] = rmu * (F(8) + F(6));
           szz[p] = twothirds * rmu * (F(9) + F(9) - (F(1) + F(5)));
+          if (les) {   // the SGS-scaled stresses of the momentum divergence
+            const double rmu_sgs = -a.sqgmr * mu_sgs / rmu;
+            const double fs = 1.0 + rmu_sgs;
+            txx[p] = sxx[p] * fs; txy[p] = sxy[p] * fs; txz[p] = sxz[p] * fs;
+            tyy[p] = syy[p] * fs; tyz[p] = syz[p] * fs; tzz[p] = szz[p] * fs;
+          }
           double vdcx = 0.0, vdcy = 0.0, vdcz = 0.0;
           for (int l = 1; l <= nrv; ++l) {
             double wrk = dm[l - 1] * t.Wc[l - 1] * W_i[p];
@@ -1334,22 +1401,51 @@ int visc_flux_fit(Ctx& c, const double* v, const double* T, const double* W_i, c
             vdcz = vdcz + wrk * F(nfluid + 3 * l);
           }
           double vdhx = 0.0, vdhy = 0.0, vdhz = 0.0;
-          for (int l = 1; l <= nrv; ++l) {
-            double Ya = v[(NIV + l - 1) * nc + p] * rho_i;
-            double vdtx = vdcx * Ya, vdty = vdcy * Ya, vdtz = vdcz * Ya;
-            double wrk = -dm[l - 1] * t.Wc[l - 1] * W_i[p];
-            vdtx = vdtx + wrk * F(nfluid + 3 * l - 2);
-            vdty = vdty + wrk * F(nfluid + 3 * l - 1);
-            vdtz = vdtz + wrk * F(nfluid + 3 * l);
-            F(nfluid + 3 * l - 2) = rvd * vdtx;
-            F(nfluid + 3 * l - 1) = rvd * vdty;
-            F(nfluid + 3 * l) = rvd * vdtz;
-            double h = ha[(l - 1) * nc + p];
-            vdhx = vdhx + h * F(nfluid + 3 * l - 2);
-            vdhy = vdhy + h * F(nfluid + 3 * l - 1);
-            vdhz = vdhz + h * F(nfluid + 3 * l);
+          if (!les) {
+            for (int l = 1; l <= nrv; ++l) {
+              double Ya = v[(NIV + l - 1) * nc + p] * rho_i;
+              double vdtx = vdcx * Ya, vdty = vdcy * Ya, vdtz = vdcz * Ya;
+              double wrk = -dm[l - 1] * t.Wc[l - 1] * W_i[p];
+              vdtx = vdtx + wrk * F(nfluid + 3 * l - 2);
+              vdty = vdty + wrk * F(nfluid + 3 * l - 1);
+              vdtz = vdtz + wrk * F(nfluid + 3 * l);
+              F(nfluid + 3 * l - 2) = rvd * vdtx;
+              F(nfluid + 3 * l - 1) = rvd * vdty;
+              F(nfluid + 3 * l) = rvd * vdtz;
+              double h = ha[(l - 1) * nc + p];
+              vdhx = vdhx + h * F(nfluid + 3 * l - 2);
+              vdhy = vdhy + h * F(nfluid + 3 * l - 1);
+              vdhz = vdhz + h * F(nfluid + 3 * l);
+            }
+          } else {
+            // the species fluxes of viscflux_LES_xyz: the enthalpy flux from
+            // the molecular part, then the SGS diffusion and the SGS
+            // W_i-gradient terms
+            const double dm_sgs = a.sc * mu_sgs * rho_i * sc_sgs_i;
+            for (int l = 1; l <= nrv; ++l) {
+              const double Ya = v[(NIV + l - 1) * nc + p] * rho_i;
+              double vdtx = vdcx * Ya, vdty = vdcy * Ya, vdtz = vdcz * Ya;
+              const double dxadx = F(nfluid + 3 * l - 2), dxady = F(nfluid + 3 * l - 1), dxadz = F(nfluid + 3 * l);
+              const double dmrw = -dm[l - 1] * t.Wc[l - 1] * W_i[p];
+              const double h = ha[(l - 1) * nc + p];
+              vdhx = vdhx + h * rvd * (vdtx + dmrw * dxadx);
+              vdhy = vdhy + h * rvd * (vdty + dmrw * dxady);
+              vdhz = vdhz + h * rvd * (vdtz + dmrw * dxadz);
+              double wrk = dmrw - dm_sgs * t.Wc[l - 1] * W_i[p];
+              vdtx = vdtx + wrk * dxadx;
+              vdty = vdty + wrk * dxady;
+              vdtz = vdtz + wrk * dxadz;
+              wrk = -dm_sgs * t.Wc[l - 1] * X[l - 1];
+              vdtx = vdtx + wrk * gw[p];
+              vdty = vdty + wrk * gw[nc + p];
+              vdtz = vdtz + wrk * gw[2 * nc + p];
+              F(nfluid + 3 * l - 2) = rvd * vdtx;
+              F(nfluid + 3 * l - 1) = rvd * vdty;
+              F(nfluid + 3 * l) = rvd * vdtz;
+            }
           }
-          double rlam = -rlam0 * ct;
+          const double ct_sgs = les ? a.pr * mu_sgs * cp[p] * pr_sgs_i : 0.0;
+          double rlam = les ? -rlam0 * (ct + ct_sgs) : -rlam0 * ct;
           qx[p] = uxs * sxx[p] + vys * sxy[p] + wzs * sxz[p] + rlam * F(10) + vdhx;
           qy[p] = uxs * sxy[p] + vys * syy[p] + wzs * syz[p] + rlam * F(11) + vdhy;
           qz[p] = uxs * sxz[p] + vys * syz[p] + wzs * szz[p] + rlam * F(12) + vdhz;
@@ -1363,9 +1459,15 @@ int visc_flux_fit(Ctx& c, const double* v, const double* T, const double* W_i, c
     deriv(c, 2, az, wzv.data(), true);
     for (size_t p = 0; p < ni; ++p) fl[var * ni + p] = fl[var * ni + p] + (wx[p] + wy[p] + wzv[p]);
   };
-  accum(1, sxx.data(), sxy.data(), sxz.data());
-  accum(2, sxy.data(), syy.data(), syz.data());
-  accum(3, sxz.data(), syz.data(), szz.data());
+  if (les) {
+    accum(1, txx.data(), txy.data(), txz.data());
+    accum(2, txy.data(), tyy.data(), tyz.data());
+    accum(3, txz.data(), tyz.data(), tzz.data());
+  } else {
+    accum(1, sxx.data(), sxy.data(), sxz.data());
+    accum(2, sxy.data(), syy.data(), syz.data());
+    accum(3, sxz.data(), syz.data(), szz.data());
+  }
   accum(4, qx.data(), qy.data(), qz.data());
   for (int l = 0; l < nrv; ++l)
     accum(NIV + l, fd.data() + (size_t)(nfluid + 3 * l) * nc, fd.data() + (size_t)(nfluid + 3 * l + 1) * nc,
@@ -1549,10 +1651,12 @@ void timestep(const Ctx& c, double DTmax, const double* v, const double* T, cons
     // Fourier criteria (module_solver.f90:294-367) from the simple transport
     // fits (prim_vis_vars_wo_mu, module_thermodynamics.f90:1243-1420) even
     // under EGLIB, with the filter width of filter_width (module_tools.f90:
-    // 2328-2378).  Without LES mu_SGS is zero, so its terms add exactly 0.
+    // 2328-2378), and mu_SGS of the last fitted-transport LES flux (zero
+    // without it, when its terms add exactly 0): ldmax is picked on the
+    // molecular D_k, then the subgrid diffusivity is added to that species'.
     const int nrv = b.nrv;
     const size_t nc = b.ncell, np = (size_t)b.nx * b.ny * b.nz;
-    std::vector<double> dm(nrv * np), d2(np), rct(np);
+    std::vector<double> dm(nrv * np), d2(np), rct(np), dsgs(np);
     const double third = 1.0 / 3.0;
     for (int k = 1; k <= b.nz; ++k)
       for (int j = 1; j <= b.ny; ++j)
@@ -1561,11 +1665,14 @@ void timestep(const Ctx& c, double DTmax, const double* v, const double* T, cons
           double X[IZEM_NSMAX], d[IZEM_NSMAX], mu, ct;
           for (int l = 0; l < nrv; ++l) X[l] = v[(NIV + l) * nc + p] / (v[p] * W_i[p] * t.Wc[l]);
           prim_vis_point(c, v[p], T[p], W_i[p], X, d, &mu, &ct);
+          // the subgrid diffusivity and conductivity of the last LES flux
+          const double msgs = c.mu_sgs.empty() ? 0.0 : c.mu_sgs[p];
           for (int l = 0; l < nrv; ++l) dm[l * np + q] = d[l];
+          dsgs[q] = c.adi.sc * msgs / (v[p] * c.les_sc_sgs);
           const double dx = c.dxi[0][i - 1 + b.ng], dy = c.dxi[1][j - 1 + b.ng], dz = c.dxi[2][k - 1 + b.ng];
           const double delta = c.cfg.ndim == 2 ? 1.0 / std::sqrt(dx * dy) : 1.0 / std::pow(dx * dy * dz, third);
           d2[q] = delta * delta;
-          rct[q] = d2[q] * v[p] / (ct / cp[p]);
+          rct[q] = d2[q] * v[p] / (ct / cp[p] + c.adi.pr * msgs * (1.0 / c.les_pr_sgs));
         }
     // the species of the largest diffusivity: first in (l, k, j, i) order
     int ldmax = 0;
@@ -1573,9 +1680,9 @@ void timestep(const Ctx& c, double DTmax, const double* v, const double* T, cons
     for (int l = 0; l < nrv; ++l)
       for (size_t q = 0; q < np; ++q)
         if (diffmax < dm[l * np + q]) { ldmax = l; diffmax = dm[l * np + q]; }
-    double m2 = d2[0] / dm[ldmax * np], m3 = rct[0];
+    double m2 = d2[0] / (dm[ldmax * np] + dsgs[0]), m3 = rct[0];
     for (size_t q = 0; q < np; ++q) {
-      m2 = std::min(m2, d2[q] / dm[ldmax * np + q]);
+      m2 = std::min(m2, d2[q] / (dm[ldmax * np + q] + dsgs[q]));
       m3 = std::min(m3, rct[q]);
     }
     const double rvd0_i = c.adi.sc / c.adi.sqgmr, rlamcp0_i = c.adi.pr / c.adi.sqgmr;
@@ -1731,10 +1838,11 @@ int or_set_les(void* h, int enable, double mu_sgs_factor, double sc_sgs, double 
   Ctx* c = static_cast<Ctx*>(h);
   if (!enable) {
     c->les = false;
+    c->mu_sgs.clear();
     return IZEM_OK;
   }
-  if (!c->cfg.vis || !c->cfg.eglib || c->cfg.ndim != 3 || !(mu_sgs_factor >= 0.0) || !(sc_sgs > 0.0) ||
-      !(pr_sgs > 0.0) || !(percent_weight_sgs >= 0.0))
+  if (!c->cfg.vis || c->cfg.ndim != 3 || !(mu_sgs_factor >= 0.0) || !(sc_sgs > 0.0) || !(pr_sgs > 0.0) ||
+      !(percent_weight_sgs >= 0.0))
     return IZEM_ERR_ARG;
   c->les_factor = mu_sgs_factor;
   c->les_sc_sgs = sc_sgs;
