@@ -328,15 +328,20 @@ void izem_jet_reference(izem_jet* p);
 /* Installs p for the jet faces of ctx (after izem_gpu_set_coords). */
 int  izem_gpu_set_jet(izem_ctx* ctx, const izem_jet* p);
 
-/* [IFLES] LES = T with MU_SGS_MODEL = SMAGORINSKY under EGLIB: the viscous
- * fluxes of viscflux_eg_LES_xyz (module_eg_lib.f90:2687-3352) with
- * mu_SGS_smagorinsky (module_SGS_models.f90:176-304), MU_SGS_FACTOR,
- * SC_SGS, PR_SGS and the shock-detector threshold PERCENT_WEIGHT_SGS
- * (shock_det_slv, module_tools.f90:1945-2085).  TAU_ISO_SGS_SWITCH = F (the
- * deck default): the isotropic SGS tensor is not built.  Needs cfg.vis,
- * cfg.eglib and ndim = 3; enable = 0 restores the laminar fluxes.  The time
- * step is unchanged: the reference's mu_SGS array seen by timestep stays 0
- * under EGLIB. */
+/* [IFLES] LES = T with MU_SGS_MODEL = SMAGORINSKY: MU_SGS_FACTOR, SC_SGS,
+ * PR_SGS and the shock-detector threshold PERCENT_WEIGHT_SGS, with
+ * mu_SGS_smagorinsky (module_SGS_models.f90:176-304).
+ * - Under EGLIB (cfg.eglib = 1): the viscous fluxes of viscflux_eg_LES_xyz
+ *   (module_eg_lib.f90:2687-3352), the criterion of shock_det_slv
+ *   (module_tools.f90:1945-2085).  The time step is unchanged: the
+ *   reference's mu_SGS array seen by timestep stays 0 under EGLIB.
+ * - With the fitted transport: viscflux_LES_xyz (module_viscflux.f90:
+ *   2200-2977), the criterion of shock_det_ducros_slv (module_tools.f90:
+ *   2099-2181); mu_SGS of every flux evaluation is kept and enters the
+ *   Fourier criteria of izem_gpu_timestep (module_solver.f90:294-367).
+ * TAU_ISO_SGS_SWITCH = F (the deck default): the isotropic SGS tensor is not
+ * built.  Needs cfg.vis and ndim = 3; enable = 0 restores the laminar
+ * fluxes (and zeroes the kept mu_SGS). */
 int  izem_gpu_set_les(izem_ctx* ctx, int enable, double mu_sgs_factor, double sc_sgs, double pr_sgs,
                       double percent_weight_sgs);
 /* Statistics of the last chemistry step: cells whose integration failed

@@ -88,6 +88,8 @@ struct izem_ctx {
   bool les_on = false;
   double les_cs2 = 0.0, les_sc_sgs_i = 0.0, les_pr_sgs_i = 0.0, les_pw = 0.0;
   double* les = nullptr;                  // 4 ghosted components (W_i gradient, criterion)
+  double les_sc_sgs = 1.0;                // SC_SGS
+  double* mu_sgs = nullptr;               // fitted-transport LES: mu_SGS for the Fourier time step (ghosted)
   int newton_warn = 0;
   std::string err;
 };

@@ -318,9 +318,11 @@ int enq_visc(izem_ctx* c) {
     return rc;
   if (eg && (rc = launch(c, "visc_grad_p", [&] { k_grad_p<NRV><<<grid_for(g.nint), kThreads, 0, c->stream>>>(g, mt, c->prim, c->fd); })))
     return rc;
-  const bool les = eg && c->les_on;
+  const bool les = c->les_on;
   if (les && (rc = launch(c, "les_prep", [&] {
-                k_les_prep<<<grid_for(g.nint), kThreads, 0, c->stream>>>(g, mt, c->v, c->T, c->W_i, c->les_pw, c->les);
+                // the criterion of shock_det_slv under EGLIB, of shock_det_ducros_slv with the fitted transport
+                k_les_prep<<<grid_for(g.nint), kThreads, 0, c->stream>>>(g, mt, c->v, c->T, c->W_i, c->les_pw, c->les,
+                                                                         c->prim, eg ? 0 : 1);
               })))
     return rc;
   long long ns = slab_count(g) - g.nint;
@@ -328,8 +330,8 @@ int enq_visc(izem_ctx* c) {
     return rc;
   if (les && (rc = launch(c, "les_wrap", [&] { k_wrap_periodic<<<grid_for(ns), kThreads, 0, c->stream>>>(g, 4, c->les); })))
     return rc;
+  SgsArgs sa{};
   if (les) {
-    SgsArgs sa;
     sa.les = c->les;
     sa.cp = c->cp;
     for (int d = 0; d < 3; ++d) sa.dxi[d] = c->dxi[d];
@@ -337,10 +339,20 @@ int enq_visc(izem_ctx* c) {
     sa.sc = c->adi.sc;
     sa.sc_sgs_i = c->les_sc_sgs_i;
     sa.pr_sgs_i = c->les_pr_sgs_i;
+    sa.pr = c->adi.pr;
+    sa.mu_sgs = c->mu_sgs;
+  }
+  if (les && eg) {
     const long long ns_all = slab_count(g);
     if ((rc = launch(c, "visc_point_eg", [&] {
            k_visc_point_eg<NRV, true><<<grid_for(ns_all, c->tb_visc), c->tb_visc, 0, c->stream>>>(
                g, c->v, c->T, c->W_i, c->ha, c->Xa, c->prim, c->fd, c->tau, c->qv, sa);
+         })))
+      return rc;
+  } else if (les) {
+    if ((rc = launch(c, "visc_point", [&] {
+           k_visc_point<NRV, true><<<grid_for(slab_count(g), c->tb_visc), c->tb_visc, 0, c->stream>>>(
+               g, c->v, c->T, c->W_i, c->ha, c->Xa, c->fd, c->tau, c->qv, sa);
          })))
       return rc;
   } else if (eg) {
@@ -546,7 +558,11 @@ int do_timestep(izem_ctx* c) {
   });
   if (rc || !(c->cfg.vis && c->cfg.vis_dt)) return rc;
   return launch(c, "timestep_fourier", [&] {
-    k_dtv<NRV><<<grid_for(g.nint), kThreads, 0, c->stream>>>(g, mt, c->v, c->T, c->W_i, c->cp, c->d_status);
+    // with the fitted-transport LES, mu_SGS of the last flux evaluation
+    const bool msgs = c->les_on && !c->cfg.eglib && c->mu_sgs;
+    k_dtv<NRV><<<grid_for(g.nint), kThreads, 0, c->stream>>>(g, mt, c->v, c->T, c->W_i, c->cp, c->d_status,
+                                                            msgs ? c->mu_sgs : nullptr, c->adi.sc, c->les_sc_sgs,
+                                                            c->adi.pr, c->les_pr_sgs_i);
   });
 }
 
@@ -782,7 +798,7 @@ void izem_gpu_destroy(izem_ctx* c) {
   if (c->d_chem_stats) cudaFree(c->d_chem_stats);
   if (c->h_chem_stats) cudaFreeHost(c->h_chem_stats);
   cudaFree(c->b_T); cudaFree(c->b_rho); cudaFree(c->b_Y); cudaFree(c->b_dt);
-  cudaFree(c->b_list); cudaFree(c->d_list_count); cudaFree(c->les); cudaFree(c->d_y); cudaFree(c->d_z);
+  cudaFree(c->b_list); cudaFree(c->d_list_count); cudaFree(c->les); cudaFree(c->mu_sgs); cudaFree(c->d_y); cudaFree(c->d_z);
   if (c->h_status) cudaFreeHost(c->h_status);
   if (c->h_dt) cudaFreeHost(c->h_dt);
   for (auto& v : c->kt_pending)
@@ -1413,10 +1429,11 @@ int izem_gpu_set_les(izem_ctx* c, int enable, double mu_sgs_factor, double sc_sg
   drop_graphs(c);
   if (!enable) {
     c->les_on = false;
+    if (c->mu_sgs) CK(cudaMemset(c->mu_sgs, 0, (size_t)c->g.ncell * sizeof(double)));
     return IZEM_OK;
   }
-  if (!c->cfg.vis || !c->cfg.eglib || c->cfg.ndim != 3)
-    return ctx_fail(c, IZEM_ERR_ARG, "LES closure needs VIS, EGLIB and a 3-D block", cudaSuccess);
+  if (!c->cfg.vis || c->cfg.ndim != 3)
+    return ctx_fail(c, IZEM_ERR_ARG, "LES closure needs VIS and a 3-D block", cudaSuccess);
   if (!(mu_sgs_factor >= 0.0) || !(sc_sgs > 0.0) || !(pr_sgs > 0.0) || !(percent_weight_sgs >= 0.0))
     return ctx_fail(c, IZEM_ERR_ARG, "LES parameters out of range", cudaSuccess);
   if (!c->les) {
@@ -1427,7 +1444,12 @@ int izem_gpu_set_les(izem_ctx* c, int enable, double mu_sgs_factor, double sc_sg
   cs2 = cs2 * cs2 / c->adi.sqgmr;
   c->les_cs2 = cs2;
   c->les_sc_sgs_i = 1.0 / sc_sgs;
+  c->les_sc_sgs = sc_sgs;
   c->les_pr_sgs_i = 1.0 / pr_sgs;
+  if (!c->cfg.eglib && !c->mu_sgs) {   // viscflux_LES_xyz hands mu_SGS to the time step
+    CK(cudaMalloc(&c->mu_sgs, (size_t)c->g.ncell * sizeof(double)));
+    CK(cudaMemset(c->mu_sgs, 0, (size_t)c->g.ncell * sizeof(double)));
+  }
   c->les_pw = percent_weight_sgs;
   c->les_on = true;
   return IZEM_OK;

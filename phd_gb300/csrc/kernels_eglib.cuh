@@ -431,18 +431,6 @@ __global__ void k_grad_p(Geo g, Metrics mt, const double* __restrict__ prim, dou
   }
 }
 
-// Smagorinsky closure of viscflux_eg_LES_xyz (module_eg_lib.f90:2687-3352)
-// with mu_SGS_smagorinsky (module_SGS_models.f90:176-304); the isotropic SGS
-// tensor is off (TAU_ISO_SGS_SWITCH = F), so its terms add exactly zero.
-struct SgsArgs {
-  const double* les;     // 4 ghosted components: dW_i/dx, dW_i/dy, dW_i/dz, shock-detector criterion
-  const double* cp;      // ghosted cp (code units)
-  const double* dxi[3];  // inverse spacings, ghosted index
-  double cs2;            // MU_SGS_FACTOR^2 / sqgmr
-  double sc;             // Sc of the reference scales
-  double sc_sgs_i, pr_sgs_i;   // 1 / SC_SGS, 1 / PR_SGS
-};
-
 // The W_i gradients of viscflux_eg_LES_xyz (dx_fixed1 etc., module_eg_lib.f90:
 // 2866-2871) and the criterion of shock_det_slv (module_tools.f90:1945-2085)
 // at the interior points: 0 where, on the 2 ng-point stencil of the point's
@@ -451,8 +439,14 @@ struct SgsArgs {
 // reference's z pass writes with the y pass's final j_l and the final k, a
 // ghost corner that no later step reads, so only the x and y passes shape
 // the criterion.  3-D only.
+// With ducros != 0 (LES with the fitted transport, viscflux_LES_xyz) the
+// criterion is shock_det_ducros_slv's (module_tools.f90:2099-2181): 0 where
+// (div u)^2 / ((div u)^2 + |curl u|^2 + 1e-30) > PERCENT_WEIGHT_SGS, else 1,
+// from velocity gradients by uncontracted dx_fixed1 stencils (deriv_rn), so
+// that the 0/1 decision is the host evaluation's.
 __global__ void k_les_prep(Geo g, Metrics mt, const double* __restrict__ v, const double* __restrict__ T,
-                           const double* __restrict__ W_i, double pw, double* __restrict__ les) {
+                           const double* __restrict__ W_i, double pw, double* __restrict__ les,
+                           const double* __restrict__ prim = nullptr, int ducros = 0) {
   long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (idx >= g.nint) return;
   int c[3];
@@ -469,6 +463,24 @@ __global__ void k_les_prep(Geo g, Metrics mt, const double* __restrict__ v, cons
     les[d * nc + p] = deriv_at(W_i, p, strides[d], c[d], g.n[d], g.bnd[2 * d], g.bnd[2 * d + 1], di, g.ng);
   }
   double crit = 1.0;
+  if (ducros) {
+    double du[9];
+    for (int a = 0; a < 3; ++a)
+      for (int d = 0; d < 3; ++d)
+        du[a * 3 + d] = deriv_rn(prim + (PR_U + a) * nc, p, strides[d], c[d], g.n[d], g.bnd[2 * d], g.bnd[2 * d + 1],
+                                 mt.dxi[d][c[d] - 1 + g.ng], g.ng);
+    double div = __dadd_rn(__dadd_rn(du[0], du[4]), du[8]);
+    div = __dmul_rn(div, div);
+    double wrk = __dsub_rn(du[7], du[5]);
+    double vort = __dmul_rn(wrk, wrk);
+    wrk = __dsub_rn(du[2], du[6]);
+    vort = __dadd_rn(vort, __dmul_rn(wrk, wrk));
+    wrk = __dsub_rn(du[3], du[1]);
+    vort = __dadd_rn(vort, __dmul_rn(wrk, wrk));
+    const double ratio = __ddiv_rn(div, __dadd_rn(__dadd_rn(div, vort), 1.0e-30));
+    les[3 * nc + p] = ratio > pw ? 0.0 : 1.0;
+    return;
+  }
   for (int d = 0; d < 2; ++d)
     for (int st = 1; st <= 2 * g.ng; ++st) {
       const int s = c[d] + st - g.ng;           // i_s, from c - ng + 1 to c + ng

@@ -309,7 +309,9 @@ __device__ inline void atomic_min_pos(unsigned long long* addr, double v) {
 // of the reference (mu_SGS = 0 without LES) add exactly zero and are left out.
 template <int NRV>
 __global__ void k_dtv(Geo g, Metrics mt, const double* __restrict__ v, const double* __restrict__ T,
-                      const double* __restrict__ W_i, const double* __restrict__ cp, DevStatus* st) {
+                      const double* __restrict__ W_i, const double* __restrict__ cp, DevStatus* st,
+                      const double* __restrict__ mu_sgs = nullptr, double sc = 0.0, double sc_sgs = 1.0,
+                      double pr = 0.0, double pr_sgs_i = 1.0) {
   long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   const double big = __longlong_as_double(0x7ff0000000000000LL);   // +inf: identity of min
   double dmx[NRV], dmn[NRV], rct = big;
@@ -363,12 +365,16 @@ __global__ void k_dtv(Geo g, Metrics mt, const double* __restrict__ v, const dou
     const double dx = mt.dxi[0][c[0] - 1 + g.ng], dy = mt.dxi[1][c[1] - 1 + g.ng], dz = mt.dxi[2][c[2] - 1 + g.ng];
     const double delta = g.ndim == 2 ? 1.0 / sqrt(dx * dy) : 1.0 / pow(dx * dy * dz, 1.0 / 3.0);
     const double d2 = delta * delta;
+    // mu_SGS of the last fitted-transport LES flux (null: zero); the species
+    // of the largest molecular D_k is picked on the host from dmx
+    const double msgs = mu_sgs ? mu_sgs[p] : 0.0;
+    const double dsgs = sc * msgs / (rho * sc_sgs);
 #pragma unroll
     for (int l = 0; l < NRV; ++l) {
       dmx[l] = wk1[l] * c_thd.Kd[l] / (dm[l] * P);
-      dmn[l] = d2 / dmx[l];
+      dmn[l] = d2 / (dmx[l] + dsgs);
     }
-    rct = d2 * rho / (ct / cp[p]);
+    rct = d2 * rho / (ct / cp[p] + pr * msgs * pr_sgs_i);
   }
 #pragma unroll
   for (int l = 0; l < NRV; ++l)

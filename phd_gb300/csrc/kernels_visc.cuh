@@ -57,6 +57,21 @@ struct Metrics {
   const double* dxi[3];   // indexed (s - 1 + ng)
 };
 
+// Smagorinsky closure of viscflux_eg_LES_xyz (module_eg_lib.f90:2687-3352)
+// and viscflux_LES_xyz (module_viscflux.f90:2200-2977) with
+// mu_SGS_smagorinsky (module_SGS_models.f90:176-304); the isotropic SGS
+// tensor is off (TAU_ISO_SGS_SWITCH = F), so its terms add exactly zero.
+struct SgsArgs {
+  const double* les;     // 4 ghosted components: dW_i/dx, dW_i/dy, dW_i/dz, shock-detector criterion
+  const double* cp;      // ghosted cp (code units)
+  const double* dxi[3];  // inverse spacings, ghosted index
+  double cs2;            // MU_SGS_FACTOR^2 / sqgmr
+  double sc;             // Sc of the reference scales
+  double sc_sgs_i, pr_sgs_i;   // 1 / SC_SGS, 1 / PR_SGS
+  double pr;             // Pr of the reference scales (fitted transport)
+  double* mu_sgs;        // fitted transport: mu_SGS of every evaluated point, for the time step
+};
+
 // d?_fixed1 (module_deriv.f90:926-1171 and the y, z copies) at one interior
 // point in IEEE round-to-nearest operations without contraction, in the
 // reference's loop order (dd = dd + alpha(l) v(i+l), zero weights included,
@@ -182,11 +197,11 @@ __global__ void k_wrap_periodic(Geo g, int ncomp, double* __restrict__ a) {
 // velocity, and heat flux at interior points and at the ghost slabs of
 // periodic faces (domain_id = -3..3).  Writes tau (6), q (3) and overwrites
 // the species gradients of fd with rho Y_k V_k (module_viscflux.f90:1943-2062).
-template <int NRV>
+template <int NRV, bool LES = false>
 __global__ void k_visc_point(Geo g, const double* __restrict__ v, const double* __restrict__ T,
                              const double* __restrict__ W_i, const double* __restrict__ ha,
                              const double* __restrict__ Xa, double* __restrict__ fd,
-                             double* __restrict__ tau, double* __restrict__ qv) {
+                             double* __restrict__ tau, double* __restrict__ qv, SgsArgs sa = SgsArgs{}) {
   long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   int i, j, k, dom;
   if (!slab_point(g, idx, i, j, k, dom)) return;
@@ -252,6 +267,20 @@ __global__ void k_visc_point(Geo g, const double* __restrict__ v, const double* 
   auto F = [&](int q1) -> double { return fd[(long long)(q1 - 1) * nc + p]; };
   const double rho_i = 1.0 / rho;
   const double uxs = v[nc + p] * rho_i, vys = v[2 * nc + p] * rho_i, wzs = v[3 * nc + p] * rho_i;
+  // LES (viscflux_LES_xyz): mu_SGS_smagorinsky with filter_width's delta,
+  // kept for the Fourier time step
+  double mu_sgs = 0.0;
+  if constexpr (LES) {
+    const double dxv = sa.dxi[0][i - 1 + g.ng], dyv = sa.dxi[1][j - 1 + g.ng], dzv = sa.dxi[2][k - 1 + g.ng];
+    const double delta = 1.0 / pow(dxv * dyv * dzv, 1.0 / 3.0);
+    const double s11 = F(1), s12 = 0.5 * (F(2) + F(4)), s13 = 0.5 * (F(3) + F(7));
+    const double s22 = F(5), s23 = 0.5 * (F(6) + F(8)), s33 = F(9);
+    double sb = s11 * s11 + s12 * s12 + s13 * s13 + s12 * s12 + s22 * s22 + s23 * s23 + s13 * s13 + s23 * s23 +
+                s33 * s33;
+    sb = sqrt(sb + sb);
+    mu_sgs = rho * sa.cs2 * (delta * delta) * sb * sa.les[3 * nc + p];
+    sa.mu_sgs[p] = mu_sgs;
+  }
   const double rmu = -c_thd.sqgmr * mu;
   const double rvd = c_thd.rvd0 * rho;
   const double twothirds = 2.0 / 3.0;
@@ -270,25 +299,64 @@ __global__ void k_visc_point(Geo g, const double* __restrict__ v, const double* 
     vdcz = vdcz + wrk * F(15 + 3 * l);
   }
   double vdhx = 0.0, vdhy = 0.0, vdhz = 0.0;
+  if constexpr (!LES) {
 #pragma unroll
-  for (int l = 0; l < NRV; ++l) {
-    const double Ya = v[(IZEM_NIV + l) * nc + p] * rho_i;
-    const double wrk = -dm[l] * c_thd.Wc[l] * Wi;
-    const double vtx = vdcx * Ya + wrk * F(13 + 3 * l);
-    const double vty = vdcy * Ya + wrk * F(14 + 3 * l);
-    const double vtz = vdcz * Ya + wrk * F(15 + 3 * l);
-    const double jx = rvd * vtx, jy = rvd * vty, jz = rvd * vtz;
-    fd[(long long)(12 + 3 * l) * nc + p] = jx;
-    fd[(long long)(13 + 3 * l) * nc + p] = jy;
-    fd[(long long)(14 + 3 * l) * nc + p] = jz;
-    const double h = ha[l * nc + p];
-    vdhx = vdhx + h * jx;
-    vdhy = vdhy + h * jy;
-    vdhz = vdhz + h * jz;
+    for (int l = 0; l < NRV; ++l) {
+      const double Ya = v[(IZEM_NIV + l) * nc + p] * rho_i;
+      const double wrk = -dm[l] * c_thd.Wc[l] * Wi;
+      const double vtx = vdcx * Ya + wrk * F(13 + 3 * l);
+      const double vty = vdcy * Ya + wrk * F(14 + 3 * l);
+      const double vtz = vdcz * Ya + wrk * F(15 + 3 * l);
+      const double jx = rvd * vtx, jy = rvd * vty, jz = rvd * vtz;
+      fd[(long long)(12 + 3 * l) * nc + p] = jx;
+      fd[(long long)(13 + 3 * l) * nc + p] = jy;
+      fd[(long long)(14 + 3 * l) * nc + p] = jz;
+      const double h = ha[l * nc + p];
+      vdhx = vdhx + h * jx;
+      vdhy = vdhy + h * jy;
+      vdhz = vdhz + h * jz;
+    }
+  } else {
+    // the species fluxes of viscflux_LES_xyz: the enthalpy flux from the
+    // molecular part, then the SGS diffusion and W_i-gradient terms
+    const double dm_sgs = sa.sc * mu_sgs * rho_i * sa.sc_sgs_i;
+    const double gwx = sa.les[p], gwy = sa.les[nc + p], gwz = sa.les[2 * nc + p];
+#pragma unroll
+    for (int l = 0; l < NRV; ++l) {
+      const double Ya = v[(IZEM_NIV + l) * nc + p] * rho_i;
+      const double dxa = F(13 + 3 * l), dya = F(14 + 3 * l), dza = F(15 + 3 * l);
+      const double dmrw = -dm[l] * c_thd.Wc[l] * Wi;
+      double vtx = vdcx * Ya, vty = vdcy * Ya, vtz = vdcz * Ya;
+      const double hr = ha[l * nc + p] * rvd;
+      vdhx = vdhx + hr * (vtx + dmrw * dxa);
+      vdhy = vdhy + hr * (vty + dmrw * dya);
+      vdhz = vdhz + hr * (vtz + dmrw * dza);
+      double wrk = dmrw - dm_sgs * c_thd.Wc[l] * Wi;
+      vtx = vtx + wrk * dxa;
+      vty = vty + wrk * dya;
+      vtz = vtz + wrk * dza;
+      wrk = -dm_sgs * c_thd.Wc[l] * X[l];
+      vtx = vtx + wrk * gwx;
+      vty = vty + wrk * gwy;
+      vtz = vtz + wrk * gwz;
+      fd[(long long)(12 + 3 * l) * nc + p] = rvd * vtx;
+      fd[(long long)(13 + 3 * l) * nc + p] = rvd * vty;
+      fd[(long long)(14 + 3 * l) * nc + p] = rvd * vtz;
+    }
   }
-  const double rlam = -c_thd.rlam0 * ct;
-  tau[0 * nc + p] = sxx; tau[1 * nc + p] = sxy; tau[2 * nc + p] = sxz;
-  tau[3 * nc + p] = syy; tau[4 * nc + p] = syz; tau[5 * nc + p] = szz;
+  double rlam;
+  if constexpr (LES) {
+    rlam = -c_thd.rlam0 * (ct + sa.pr * mu_sgs * sa.cp[p] * sa.pr_sgs_i);
+    // the momentum divergence takes the SGS-scaled stresses, the heat flux
+    // below the molecular ones
+    const double fs = 1.0 + -c_thd.sqgmr * mu_sgs / rmu;
+    tau[0 * nc + p] = sxx * fs; tau[1 * nc + p] = sxy * fs; tau[2 * nc + p] = sxz * fs;
+    tau[3 * nc + p] = syy * fs; tau[4 * nc + p] = syz * fs; tau[5 * nc + p] = szz * fs;
+  } else {
+    rlam = -c_thd.rlam0 * ct;
+    tau[0 * nc + p] = sxx; tau[1 * nc + p] = sxy; tau[2 * nc + p] = sxz;
+    tau[3 * nc + p] = syy; tau[4 * nc + p] = syz; tau[5 * nc + p] = szz;
+  }
   qv[0 * nc + p] = uxs * sxx + vys * sxy + wzs * sxz + rlam * F(10) + vdhx;
   qv[1 * nc + p] = uxs * sxy + vys * syy + wzs * syz + rlam * F(11) + vdhy;
   qv[2 * nc + p] = uxs * sxz + vys * syz + wzs * szz + rlam * F(12) + vdhz;

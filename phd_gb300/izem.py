@@ -336,8 +336,9 @@ class IzemGPU:
         self._check(self.lib.izem_gpu_set_jet(self.h, C.byref(jet)), "set_jet")
 
     def set_les(self, mu_sgs_factor=0.18, sc_sgs=0.7, pr_sgs=0.7, percent_weight_sgs=70.0, enable=True):
-        """[IFLES] LES = T, MU_SGS_MODEL = SMAGORINSKY under EGLIB
-        (izem_gpu_set_les); the deck defaults are the keyword defaults."""
+        """[IFLES] LES = T, MU_SGS_MODEL = SMAGORINSKY (izem_gpu_set_les):
+        viscflux_eg_LES_xyz under EGLIB, viscflux_LES_xyz with the fitted
+        transport; the deck defaults are the keyword defaults."""
         self._check(self.lib.izem_gpu_set_les(self.h, int(bool(enable)), float(mu_sgs_factor), float(sc_sgs),
                                               float(pr_sgs), float(percent_weight_sgs)), "set_les")
 

@@ -532,3 +532,52 @@ def test_rk3_steps_weno7_eglib():
     s = (slice(4, -4),) * 3
     err = W.normwise(got["v"][s], st["v"][s])
     assert np.all(err <= TOL), err
+
+
+@pytest.mark.parametrize("pw", [0.2, 0.6])
+def test_visc_flux_fitted_les(pw):
+    """viscflux_LES_xyz: the fitted-transport fluxes with the Smagorinsky
+    SGS viscosity (MU_SGS_FACTOR 0.17) and the shock_det_ducros_slv
+    criterion at two thresholds (the 0/1 decisions are bit-exact on the
+    device), against the oracle."""
+    from test_ducros_cpu import shake_velocity
+    cfg, thd, adi, dxi, st, info, orc = W.case("mix", 12)
+    shake_velocity(st, amp=0.05)
+    orc.update_primitives(st)
+    orc.set_les(0.17, 0.7, 0.7, pw)
+    g = gpu_from(cfg, thd, adi, dxi, st)
+    g.set_les(0.17, 0.7, 0.7, pw)
+    fl = np.zeros((cfg.nx, cfg.ny, cfg.nz, 5 + cfg.nrv), order="F")
+    orc.visc_flux(st, fl)
+    g.zero_flux()
+    g.viscflux_xyz()
+    err = W.normwise(g.flux(), fl)
+    g.close()
+    # the energy flux (with the enthalpy flux sum_l h_l rho Y_l V_l) and the
+    # species fluxes are sums of terms of both signs; with the SGS terms the
+    # two evaluation orders differ there by up to 1.5e-12 of the largest
+    # value (measured on this shaken field), the momentum by 1e-15
+    assert np.all(err[[1, 2, 3]] <= TOL) and np.all(err <= 2e-12), err
+
+
+def test_rk3_steps_fitted_les_fourier():
+    """Two driver steps of the mixing layer with the fitted-transport LES
+    (MU_SGS_FACTOR 0.05) and the Fourier criteria: each step's criteria see
+    mu_SGS of the previous step's last flux evaluation, as the reference's
+    timestep does; dt and the state against the oracle."""
+    cfg, thd, adi, dxi, st, info, orc = W.case("mix", 12, vis_dt=True)
+    W.perturb(st, 0.02, seed=3)
+    orc.update_primitives(st)
+    orc.set_les(0.05, 0.7, 0.7, 0.5)
+    g = gpu_from(cfg, thd, adi, dxi, st)
+    g.set_les(0.05, 0.7, 0.7, 0.5)
+    for step in range(3):
+        dt4, dt = orc.timestep(st)
+        dt4g, dtg = g.timestep()
+        assert np.allclose(dt4g, dt4, rtol=1e-13, atol=0.0), (step, dt4g, dt4)
+        orc.rk3(st, dt)
+        g.rk3(dt)
+    got = g.download()
+    g.close()
+    err = W.normwise(interior(got["v"]), interior(st["v"]))
+    assert np.all(err <= TOL), err
