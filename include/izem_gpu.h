@@ -469,6 +469,12 @@ int  izem_gpu_chem_generated(void);
  * launches): the FP64 peak the rooflines are quoted against.  No
  * counterpart in the reference. */
 int  izem_gpu_fp64_rate(double* gflops);
+/* Checks the bounded waits of the tensor-core kernels (no counterpart in the
+ * reference): a kernel polls an mbarrier that nothing arrives on `polls`
+ * times (1 .. 2^20), as those kernels poll theirs, and *gave_up receives 1
+ * when it stopped waiting (always, on a working device); the context stays
+ * usable. */
+int  izem_gpu_wait_selftest(int polls, int* gave_up);
 /* allow = 0 makes the chemistry kernels walk the mechanism's tables even
  * for the shipped mechanism (to compare the two forms); allow = 1 (the
  * default) uses the generated form whenever it applies.  Takes effect at

@@ -784,3 +784,44 @@ extern "C" int izem_mlp_forward_noalloc(izem_mlp* m, int M, const float* d_x, fl
   k_na_unpack<<<g1((long long)M * OUT), 256, 0, s>>>(out, M, d_y);
   return cudaGetLastError() == cudaSuccess ? IZEM_OK : IZEM_ERR_CUDA;
 }
+
+// ------------------------------------------------- bounded-wait self-test --
+// The tensor-core kernels poll their mbarriers a bounded number of times and
+// give up with an error flag instead of waiting forever.  This kernel waits,
+// in the same way, on a barrier that nothing arrives on: one thread
+// initialises it for one arrival, polls its first phase `polls` times and
+// records whether it gave up.
+namespace {
+__global__ void k_wait_selftest(int polls, int* gave_up) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x != 0) return;
+  const uint32_t b = mlptc::saddr(&bar);
+  mlptc::mbar_init(b, 1);
+  mlptc::fence_async_smem();
+  int done = 0;
+  for (int i = 0; i < polls && !done; ++i) {
+    uint32_t d;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(d)
+        : "r"(b), "r"(0u)
+        : "memory");
+    done = (int)d;
+  }
+  *gave_up = done ? 0 : 1;
+}
+}  // namespace
+
+extern "C" int izem_gpu_wait_selftest(int polls, int* gave_up) {
+  if (polls < 1 || polls > (1 << 20) || !gave_up) return IZEM_ERR_ARG;
+  int* d = nullptr;
+  if (cudaMalloc(&d, sizeof(int)) != cudaSuccess) return IZEM_ERR_NOMEM;
+  int rc = IZEM_OK;
+  k_wait_selftest<<<1, 32>>>(polls, d);
+  if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess ||
+      cudaMemcpy(gave_up, d, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+    rc = IZEM_ERR_CUDA;
+  cudaFree(d);
+  return rc;
+}
+

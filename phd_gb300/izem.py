@@ -81,6 +81,7 @@ def load_library(path=None):
         "izem_gpu_set_chem_variant": (C.c_int, [C.c_int]),
         "izem_gpu_chem_generated": (C.c_int, []),
         "izem_gpu_fp64_rate": (C.c_int, [_dp]),
+        "izem_gpu_wait_selftest": (C.c_int, [C.c_int, C.POINTER(C.c_int)]),
         "izem_gpu_allow_chem_generated": (C.c_int, [C.c_int]),
         "izem_gpu_set_sensor_xblocks": (C.c_int, [P, C.c_int]),
         "izem_gpu_set_chem_skip": (C.c_int, [P, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_int]),
@@ -451,6 +452,17 @@ def fp64_rate():
     if rc:
         raise IzemError(rc, "izem_gpu_fp64_rate")
     return float(out[0])
+
+
+def wait_selftest(polls=4096):
+    """1 when a kernel polling an mbarrier that nothing arrives on gave up
+    after `polls` polls (izem_gpu_wait_selftest)."""
+    lib = load_library()
+    out = C.c_int(-1)
+    rc = lib.izem_gpu_wait_selftest(int(polls), C.byref(out))
+    if rc:
+        raise IzemError(rc, "izem_gpu_wait_selftest")
+    return out.value
 
 
 class TimeLoop:

@@ -197,3 +197,16 @@ def test_flow_surrogate_error_within_gate():
           % (st["cells"], st["fallback"], err, scale))
     assert st["fallback"] < st["cells"]
     assert err <= 0.05 * scale
+
+
+def test_bounded_wait_gives_up_and_the_device_stays_usable():
+    """Failure detection without a fault: a kernel polls an mbarrier that
+    nothing arrives on, in the way the tensor-core kernels poll theirs, and
+    stops after a bounded number of polls with its error flag set; the
+    context then runs the tensor-core forward normally."""
+    from phd_gb300.izem import wait_selftest
+    assert wait_selftest(4096) == 1
+    s = Surrogate(seed=3)
+    x = np.random.default_rng(0).standard_normal((512, 12)).astype(np.float32)
+    y = s.forward(x)
+    assert np.all(np.isfinite(y))
