@@ -593,6 +593,137 @@ def run_surrogate(args):
     }
 
 
+def run_field_surrogate(args, steps=None, warmup=None):
+    """Learned chemistry on a reacting field: two networks trained on the GPU
+    on args.train reactors of the batched-chemistry distribution (labelled
+    by the FP64 BDF integrator), the gate's dT cap and absolute dT
+    tolerances calibrated on 2^20 held-out ones taken over the field's step
+    (surrogate.calibrate_cap), then inference on a
+    512 x 256 x 256 field
+    (phd_gb300.ics.reacting_field: the same distribution laid out as smooth
+    seeded fields, one chemistry step of args.field_dt seconds, by default
+    3e-7 s) through the library's
+    field chemistry step (reaction_selec, IZEM_CHEM_MLP: tensor-core
+    networks, error gate, BDF on the rejected cells), against the same step
+    with BDF on every cell (IZEM_CHEM_BDF).  State resident on the device;
+    each timed step starts from the same state (re-uploaded outside the
+    timed region)."""
+    from phd_gb300 import ics
+    from phd_gb300.izem import IzemGPU, chem_autotune_device, metrics_dscalar
+    from phd_gb300.mech import h2_mechanism
+    from phd_gb300.surrogate import (ABS_SCALE_LADDER, CAP_LADDER_FINE, DEFAULT_GATE, STRICT_GATE, calibrate_cap,
+                                     train_ensemble)
+    import torch
+    steps = steps if steps is not None else args.steps
+    warmup = warmup if warmup is not None else args.warmup
+    gate = STRICT_GATE if args.gate == "strict" else DEFAULT_GATE
+    mech = h2_mechanism()
+    t0 = time.perf_counter()
+    nets = train_ensemble(mech, n=args.train, seed=31, epochs=args.epochs)
+    t_train = time.perf_counter() - t0
+    calib = None
+    if args.gate == "calibrated":   # the dT cap for this field's step, on 2^20 held-out reactors over it
+        gate, calib = calibrate_cap(nets, mech, DEFAULT_GATE, dt_s=args.field_dt, caps=CAP_LADDER_FINE,
+                                    abs_scales=ABS_SCALE_LADDER)
+    t0 = time.perf_counter()
+    nx, ny, nz = args.field_size
+    cfg, thd, adi, dxi, st, info = ics.reacting_field(nx, ny, nz, dt_s=args.field_dt, lib_dscalar=metrics_dscalar)
+    t_ic = time.perf_counter() - t0
+    g = IzemGPU(cfg, thd, adi)
+    g.set_grid(*dxi)
+    g.upload(**st)
+    del st
+    g.finalize_ic()
+    g.set_mechanism(mech)
+    dt = info["dt_s"] / info["time_ref"]
+    st0 = g.download()
+    ng, nrv = cfg.ng, cfg.nrv
+    # the reaction window of reaction_dvode (interior indices ng+1 .. n-ng-1,
+    # the z bound taken with min(ny, ...)), as ghosted-array slices
+    hi = (min(nx, nx - ng - 1), min(ny, ny - ng - 1), min(ny, nz - ng - 1))
+    win = tuple(slice(2 * ng, h - 1 + ng + 1) for h in hi)
+    # the register-budget variant of the chemistry kernels, tuned on 2^20 window reactors
+    vw = st0["v"][win]
+    Tw = st0["T"][win] * adi.t_ref
+    nsamp = min(1 << 20, Tw.size)
+    pick = np.random.Generator(np.random.PCG64(17)).choice(Tw.size, nsamp, replace=False)
+    rho_s = vw[..., 0].reshape(-1)[pick] * adi.rho_ref * 1e-3
+    Y_s = np.stack([vw[..., 5 + k].reshape(-1)[pick] for k in range(nrv)], axis=1) / (rho_s / (adi.rho_ref * 1e-3))[:, None]
+    dev = [torch.from_numpy(np.ascontiguousarray(a)).to("cuda:0")
+           for a in (Tw.reshape(-1)[pick], rho_s, Y_s, np.full(nsamp, info["dt_s"]))]
+    tuning = chem_autotune_device(mech, nsamp, *dev)
+    del vw, dev
+    T0 = st0["T"][win].copy()
+    # BDF on every window cell (the FP64 reference increments)
+    g.synchronize()
+    g.timer_start()
+    g.reaction_selec(dt, mode=0)
+    bdf_ms = g.timer_stop()
+    bdf_stats = g.chem_stats()
+    dT_ref = (g.download()["T"][win] - T0) * adi.t_ref
+    g.set_surrogate(nets[0], nets[1], gate=gate)
+    for _ in range(warmup):
+        g.upload(**st0)
+        g.reaction_selec(dt, mode=1)
+    runs = []
+    with ClockSampler(0) as clk:
+        for _ in range(steps):
+            g.upload(**st0)
+            g.synchronize()
+            g.timer_start()
+            g.reaction_selec(dt, mode=1)
+            ms = g.timer_stop()
+            sst = g.surrogate_stats()
+            runs.append({"ms": ms, "fallback": sst["fallback"], "cells": sst["cells"], "ms_network": sst["ms_network"]})
+    dT = (g.download()["T"][win] - T0) * adi.t_ref
+    g.close()
+    err = np.abs(dT - dT_ref)
+    scale = float(np.abs(dT_ref).max())
+    ref_abs = np.abs(dT_ref)
+    rel_own = {}
+    for thr in (1.0, 10.0):
+        sel = ref_abs >= thr
+        rel = err[sel] / ref_abs[sel]
+        rel_own["dT_ref_ge_%gK" % thr] = {
+            "cells_frac": float(sel.mean()),
+            "median": float(np.median(rel)) if rel.size else None,
+            "p99": float(np.percentile(rel, 99)) if rel.size else None,
+            "max": float(rel.max()) if rel.size else None}
+    ncell = int(T0.size)
+    ms = float(np.mean([r["ms"] for r in runs]))
+    ms_net = float(np.mean([r["ms_network"] for r in runs]))
+    flop = 2.0 * 2 * 202240 * ncell     # two networks, 202,240 MACs per row
+    tflops = flop / (ms_net * 1e-3) / 1e12 if ms_net > 0 else None
+    peak = 1932.2
+    pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pk):
+        with open(pk) as f:
+            peak = float(json.load(f).get("bf16_tflops", peak))
+    return {
+        "metric": "learned-chemistry field step Mcells/s (gated BF16 tensor-core MLP + FP64 BDF fallback)",
+        "value": ncell / (ms * 1e-3) / 1e6, "unit": "Mcells/s", "n_gpus": 1, "steps": steps, "warmup": warmup,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "bf16 network, f64 integrator", "data": "synthetic (seeded PCG64)",
+        "config": {"workload": info["name"], "grid": [nx, ny, nz], "window_cells": ncell, "dt_s": info["dt_s"],
+                   "training": {"samples": args.train, "epochs": args.epochs, "networks": 2, "seconds": t_train,
+                                "distribution": "independent reactors of the batched-chemistry distribution"},
+                   "gate": {"name": args.gate, "values": gate_json(gate), "calibration": calib},
+                   "autotuned_kernel_variant": tuning, "initial_field_s": t_ic,
+                   "l2": "inputs larger than L2"},
+        "bdf": {"value": ncell / (bdf_ms * 1e-3) / 1e6, "unit": "Mcells/s", "ms": bdf_ms, "stats": bdf_stats},
+        "speedup_vs_bdf": bdf_ms / ms,
+        "fallback_frac": float(np.mean([r["fallback"] / max(1, r["cells"]) for r in runs])),
+        "max_dT_err_K": float(err.max()), "max_dT_K": scale,
+        "max_dT_err_frac": float(err.max()) / scale if scale > 0 else None,
+        "rms_dT_err_K": float(np.sqrt((err ** 2).mean())),
+        "err_rel_to_own_dT": rel_own,
+        "roofline": {"bound": "tensor", "kernel": "k_mlp_tc (two networks, with the feature kernel)",
+                     "achieved": tflops, "peak": peak, "unit": "TFLOP/s",
+                     "frac": tflops / peak if tflops else None, "traffic": None, "network_ms": ms_net},
+        "clocks": clk.summary(),
+    }
+
+
 def run_jet(args, steps=None, warmup=None):
     """The reacting LES jet: the 512 x 512 x 256 planar H2/air jet
     (phd_gb300.ics.jet_les: 2 mm slot of H2/N2 at 300 m/s into 1200 K air
@@ -680,23 +811,22 @@ def run_jet(args, steps=None, warmup=None):
 
 
 def c4_summary(args):
-    """The learned-chemistry workload (--workload surrogate) at its
-    configured size -- 512 x 256 x 256 = 33.5 M reactors of the
-    batched-chemistry distribution, two networks trained on 4 M reactors
-    labelled by the FP64 integrator, calibrated gate -- condensed for the
-    default line: speed-up over BDF on every cell, fallback, errors."""
+    """The learned-chemistry workload on the 512 x 256 x 256 reacting field
+    (--workload field) at its configured size -- two networks trained on
+    4 M reactors of the batched-chemistry distribution labelled by the FP64
+    integrator, calibrated gate -- condensed for the default line: speed-up
+    over BDF on every cell, fallback, errors."""
     import copy
     a = copy.copy(args)
-    a.cells, a.train, a.epochs, a.gate = 512 * 256 * 256, 1 << 22, 24, "calibrated"
-    a.steps, a.warmup = max(1, min(args.steps, 3)), 1
-    r = run_surrogate(a)
-    keys = ("metric", "value", "unit", "ms_per_step", "bdf", "speedup_vs_bdf", "fallback_frac", "max_dT_err_K",
-            "max_dT_K", "max_dT_err_frac", "rms_dT_err_K", "accepted_cells", "accepted_err_rel_to_own_dT",
-            "roofline", "gpu_launches", "clocks")
+    a.train, a.epochs, a.gate = 1 << 22, 24, "calibrated"
+    a.field_size, a.field_dt = [512, 256, 256], 3e-7
+    r = run_field_surrogate(a, steps=max(1, min(args.steps, 3)), warmup=1)
+    keys = ("metric", "value", "unit", "ms_per_step", "steps", "warmup", "bdf", "speedup_vs_bdf", "fallback_frac",
+            "max_dT_err_K", "max_dT_K", "max_dT_err_frac", "rms_dT_err_K", "err_rel_to_own_dT", "roofline", "clocks")
     out = {k: r[k] for k in keys}
-    out["config"] = {"workload": r["config"]["workload"], "cells": r["config"]["cells"],
-                     "training": r["config"]["training"], "gate": r["config"]["gate"]["values"],
-                     "steps": a.steps, "warmup": a.warmup}
+    c = r["config"]
+    out["config"] = {"workload": c["workload"], "window_cells": c["window_cells"], "dt_s": c["dt_s"],
+                     "training": c["training"], "gate": c["gate"]["values"]}
     return out
 
 
@@ -793,7 +923,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="mix", choices=["mix", "tgv", "batch", "surrogate", "jet"])
+    ap.add_argument("--workload", default="mix", choices=["mix", "tgv", "batch", "surrogate", "field", "jet"])
     ap.add_argument("--cells", type=int, default=None,
                     help="reactors of the batch (default 2^20) and surrogate (default 512*256*256) workloads")
     ap.add_argument("--train", type=int, default=1 << 22, help="training reactors of the surrogate workload")
@@ -808,12 +938,17 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-chem", action="store_true", help="mixing layer without the chemistry half-steps")
     ap.add_argument("--no-mlp", action="store_true", help="skip the learned-chemistry leg of the reacting step")
+    ap.add_argument("--field-size", type=int, nargs=3, default=[512, 256, 256],
+                    help="grid of the learned-chemistry reacting field workload")
+    ap.add_argument("--field-dt", type=float, default=3e-7,
+                    help="chemistry step [s] of the reacting field workload (the training range is 1e-8 .. 1e-6)")
     ap.add_argument("--jet-size", type=int, nargs=3, default=[512, 512, 256],
                     help="grid of the reacting LES jet workload")
     ap.add_argument("--no-jet", action="store_true",
                     help="skip the reacting LES jet (512 x 512 x 256) in the default line")
     ap.add_argument("--no-c4", action="store_true",
-                    help="skip the learned-chemistry workload on 33.5 M reactors in the default line")
+                    help="skip the learned-chemistry workload on the 512 x 256 x 256 reacting field in the "
+                         "default line")
     ap.add_argument("--les", type=float, default=None,
                     help="mixing layer with the Smagorinsky closure (EGLIB) at this MU_SGS_FACTOR")
     ap.add_argument("--dvodesimp", action="store_true", help="mixing layer with the dvodesimp chemistry skip")
@@ -855,9 +990,10 @@ def main():
             vis = os.environ.get("CUDA_VISIBLE_DEVICES")
             devs = vis.split(",") if vis else [str(q) for q in range(world)]
             os.environ["CUDA_VISIBLE_DEVICES"] = devs[local % len(devs)]
-    if args.workload in ("batch", "surrogate", "jet"):
+    if args.workload in ("batch", "surrogate", "field", "jet"):
         if rank == 0:
-            run = {"batch": run_batch, "surrogate": run_surrogate, "jet": run_jet}[args.workload]
+            run = {"batch": run_batch, "surrogate": run_surrogate, "field": run_field_surrogate,
+                   "jet": run_jet}[args.workload]
             print(json.dumps(run(args)))
         return
     res = run_gpu(args, rank, world)

@@ -14,6 +14,10 @@ Workloads:
 * ``mixing_layer``  temporal H2/air mixing layer, 9 species, x/z periodic,
                     y zero-gradient; tanh profile of thickness 0.5 mm,
                     dU = 100 m/s, 1% seeded white-noise velocity.
+* ``jet_les``       reacting planar H2/air jet with the jet faces.
+* ``batched_reactors`` independent reactors of the batched-chemistry
+                    distribution; ``reacting_field`` the same distribution as
+                    smooth fields on a grid, for the learned chemistry.
 """
 import math
 
@@ -75,6 +79,26 @@ def _state_from_primitives(thd, a, rho_d, u_d, v_d, w_d, T_d, Y, ng):
     arrays of shape (nx,ny,nz)), ghosts by zero-gradient extension."""
     nx, ny, nz = rho_d.shape
     nrv = thd.nspc
+    cons, T = _cons_from_primitives(thd, a, rho_d, u_d, v_d, w_d, T_d, Y)
+    pad = ((ng, ng), (ng, ng), (ng, ng))
+    vg = np.empty((nx + 2 * ng, ny + 2 * ng, nz + 2 * ng, 5 + nrv), order="F")
+    for q in range(5 + nrv):
+        vg[..., q] = np.pad(cons[..., q], pad, mode="edge")
+    Tg = np.asfortranarray(np.pad(T, pad, mode="edge"))
+    return _state_dict(vg, Tg, nrv)
+
+
+def _state_dict(vg, Tg, nrv):
+    shp = vg.shape[:3]
+    return {"v": vg, "T": Tg, "W_i": np.zeros(shp, order="F"), "cp": np.zeros(shp, order="F"),
+            "ha": np.zeros(shp + (nrv,), order="F"), "shock_sensor": np.zeros(shp, dtype=np.uint8, order="F")}
+
+
+def _cons_from_primitives(thd, a, rho_d, u_d, v_d, w_d, T_d, Y):
+    """Conserved variables (..., 5 + nrv) and the code-unit temperature of
+    dimensional primitives (arrays of one shape; Y with a trailing species
+    axis)."""
+    nrv = thd.nspc
     rho = rho_d / a["rho_ref"]
     u, v, w = u_d / a["u_ref"], v_d / a["u_ref"], w_d / a["u_ref"]
     T = T_d / a["t_ref"]
@@ -84,7 +108,7 @@ def _state_from_primitives(thd, a, rho_d, u_d, v_d, w_d, T_d, Y, ng):
     P = rho * T * W_i
     ha = ha_code(thd, T)
     hm = np.einsum("...k,...k->...", ha, Y)
-    cons = np.empty((nx, ny, nz, 5 + nrv))
+    cons = np.empty(rho.shape + (5 + nrv,))
     cons[..., 0] = rho
     cons[..., 1] = rho * u
     cons[..., 2] = rho * v
@@ -92,14 +116,7 @@ def _state_from_primitives(thd, a, rho_d, u_d, v_d, w_d, T_d, Y, ng):
     cons[..., 4] = rho * hm - P + 0.5 * rho * (u * u + v * v + w * w)
     for k in range(nrv):
         cons[..., 5 + k] = rho * Y[..., k]
-    pad = ((ng, ng), (ng, ng), (ng, ng))
-    vg = np.empty((nx + 2 * ng, ny + 2 * ng, nz + 2 * ng, 5 + nrv), order="F")
-    for q in range(5 + nrv):
-        vg[..., q] = np.pad(cons[..., q], pad, mode="edge")
-    Tg = np.asfortranarray(np.pad(T, pad, mode="edge"))
-    shp = vg.shape[:3]
-    return {"v": vg, "T": Tg, "W_i": np.zeros(shp, order="F"), "cp": np.zeros(shp, order="F"),
-            "ha": np.zeros(shp + (nrv,), order="F"), "shock_sensor": np.zeros(shp, dtype=np.uint8, order="F")}
+    return cons, T
 
 
 def tgv(n=64, lib_dscalar=None):
@@ -274,8 +291,6 @@ def batched_reactors(n, seed=SEED):
     and the excess O2 or H2), dt log-uniform in [1e-8, 1e-6] s.  Returns
     T [K], rho [g/cm^3], Y (n, 9) in the h2air9 species order, dt [s]."""
     sp = load_species("h2air9")
-    names = sp["names"]
-    ix = {nm: q for q, nm in enumerate(names)}
     W = np.array(sp["W_gmol"])
     rng = np.random.Generator(np.random.PCG64(seed))
     T = rng.uniform(800.0, 2400.0, n)
@@ -283,6 +298,18 @@ def batched_reactors(n, seed=SEED):
     phi = rng.uniform(0.3, 3.0, n)
     c = rng.uniform(0.0, 1.0, n)
     dt = 10.0 ** rng.uniform(-8.0, -6.0, n)
+    Y = _blend_composition(phi, c, sp["names"], W)
+    Wmix = 1.0 / (Y / W).sum(axis=1)
+    rho = p * Wmix * 1e-3 / (8.314510 * T) * 1e-3    # kg/m^3 -> g/cm^3
+    return np.ascontiguousarray(T), np.ascontiguousarray(rho), np.ascontiguousarray(Y), np.ascontiguousarray(dt)
+
+
+def _blend_composition(phi, c, names, W):
+    """Mass fractions (n, 9) of H2/air at equivalence ratio phi, blended
+    linearly (weight c) from the unburnt mixture toward the complete-combustion
+    major products: H2O, N2 and the excess O2 (lean) or H2 (rich)."""
+    ix = {nm: q for q, nm in enumerate(names)}
+    n = len(phi)
     Xu = np.zeros((n, 9)); Xb = np.zeros((n, 9))
     Xu[:, ix["H2"]] = 2.0 * phi; Xu[:, ix["O2"]] = 1.0; Xu[:, ix["N2"]] = 3.76
     lean = phi <= 1.0
@@ -292,10 +319,104 @@ def batched_reactors(n, seed=SEED):
     Xb[:, ix["N2"]] = 3.76
     Yu = Xu * W; Yu /= Yu.sum(axis=1, keepdims=True)
     Yb = Xb * W; Yb /= Yb.sum(axis=1, keepdims=True)
-    Y = (1.0 - c)[:, None] * Yu + c[:, None] * Yb
-    Wmix = 1.0 / (Y / W).sum(axis=1)
-    rho = p * Wmix * 1e-3 / (8.314510 * T) * 1e-3    # kg/m^3 -> g/cm^3
-    return np.ascontiguousarray(T), np.ascontiguousarray(rho), np.ascontiguousarray(Y), np.ascontiguousarray(dt)
+    return (1.0 - c)[:, None] * Yu + c[:, None] * Yb
+
+
+def smooth_uniform(shape, corr, rng):
+    """A seeded 3-D field whose value at every point is distributed
+    uniformly on (0, 1) and which varies smoothly over about `corr` cells:
+    independent standard normals on a lattice of spacing `corr`,
+    interpolated trilinearly, divided at each point by the standard
+    deviation of that interpolation (the square root of the sum of the
+    squared corner weights, a product over the axes of (1-t)^2 + t^2), so
+    that every point is exactly N(0, 1), then mapped through the normal
+    distribution function."""
+    lat = rng.standard_normal(tuple(n // corr + 2 for n in shape))
+    return _smooth_eval(lat, corr, shape, 0, shape[2])
+
+
+def _smooth_eval(lat, corr, shape, k0, k1):
+    """smooth_uniform's field on the planes k0 <= k < k1 of the last axis,
+    from its lattice `lat`."""
+    from scipy.special import ndtr
+    out, sd2 = lat, 1.0
+    for ax, idx in enumerate((np.arange(shape[0]), np.arange(shape[1]), np.arange(k0, k1))):
+        s = idx / corr
+        i0 = np.floor(s).astype(np.int64)
+        t = s - i0
+        bshape = [1, 1, 1]
+        bshape[ax] = len(idx)
+        t = t.reshape(bshape)
+        out = (1.0 - t) * np.take(out, i0, axis=ax) + t * np.take(out, i0 + 1, axis=ax)
+        sd2 = sd2 * ((1.0 - t) ** 2 + t ** 2)
+    return ndtr(out / np.sqrt(sd2))
+
+
+def reacting_field(nx=512, ny=256, nz=256, dt_s=3e-7, corr=16, dx=47e-6, seed=SEED, lib_dscalar=None,
+                   threads=None):
+    """A reacting H2/air field at rest for the learned-chemistry workload:
+    at every point T, p, the equivalence ratio and the progress variable
+    follow the batched-reactor distribution (T ~ U[800, 2400] K,
+    p ~ U[1, 10] atm, phi ~ U[0.3, 3], c ~ U[0, 1], the composition blended as
+    in batched_reactors), but each of the four is a smooth seeded field
+    (smooth_uniform, correlation length `corr` cells), so neighbouring cells
+    hold neighbouring reactors.  Every face periodic, uniform spacing dx;
+    the chemistry step is dt_s seconds (info["dt_s"]; the code-unit step is
+    dt_s / info["time_ref"]), by default 3e-7 s, inside the batched
+    distribution's [1e-8, 1e-6] s: over it a few per cent of the cells heat
+    by more than 1 K and the hottest by some 200 K.  The interior is built in z slabs on
+    `threads` host threads (numpy releases the interpreter lock in its
+    array operations); ghosts by zero-gradient extension.  Returns cfg, thd,
+    adi, dxi, state, info."""
+    import os
+    from concurrent.futures import ThreadPoolExecutor
+    a = constants()
+    sp = load_species("h2air9")
+    thd = thd_init(sp, a)
+    W = np.array(sp["W_gmol"])
+    nrv, ng = 9, 3
+    rng = np.random.Generator(np.random.PCG64(seed))
+    shp = (nx, ny, nz)
+    lats = [rng.standard_normal(tuple(n // corr + 2 for n in shp)) for _ in range(4)]
+    gsh = (nx + 2 * ng, ny + 2 * ng, nz + 2 * ng)
+    vg = np.empty(gsh + (5 + nrv,), order="F")
+    Tg = np.empty(gsh, order="F")
+
+    def fill(k0):
+        k1 = min(nz, k0 + 4)
+        sub = (k1 - k0,)
+        T = 800.0 + 1600.0 * _smooth_eval(lats[0], corr, shp, k0, k1)
+        p = (1.0 + 9.0 * _smooth_eval(lats[1], corr, shp, k0, k1)) * 101325.0
+        phi = 0.3 + 2.7 * _smooth_eval(lats[2], corr, shp, k0, k1)
+        c = _smooth_eval(lats[3], corr, shp, k0, k1)
+        Y = _blend_composition(phi.ravel(), c.ravel(), sp["names"], W).reshape(T.shape + (nrv,))
+        Wmix_i = np.einsum("...k,k->...", Y, 1.0 / (W * 1e-3))
+        rho = p / (a["r_ref"] * Wmix_i * T)
+        zero = np.zeros(T.shape)
+        cons, Tc = _cons_from_primitives(thd, a, rho, zero, zero, zero, T, Y)
+        zs = slice(ng + k0, ng + k1)
+        for q in range(5 + nrv):
+            vg[ng:ng + nx, ng:ng + ny, zs, q] = cons[..., q]
+        Tg[ng:ng + nx, ng:ng + ny, zs] = Tc
+        return sub
+
+    with ThreadPoolExecutor(threads or os.cpu_count() or 1) as ex:
+        list(ex.map(fill, range(0, nz, 4)))
+    for arr in [vg[..., q] for q in range(5 + nrv)] + [Tg]:
+        arr[:ng] = arr[ng:ng + 1]
+        arr[ng + nx:] = arr[ng + nx - 1:ng + nx]
+        arr[:, :ng] = arr[:, ng:ng + 1]
+        arr[:, ng + ny:] = arr[:, ng + ny - 1:ng + ny]
+        arr[:, :, :ng] = arr[:, :, ng:ng + 1]
+        arr[:, :, ng + nz:] = arr[:, :, ng + nz - 1:ng + nz]
+    state = _state_dict(vg, Tg, nrv)
+    cfg = make_cfg(nx, ny, nz, nrv)
+    cfg.reaction = 1
+    dxi = [grid_dxi(np.arange(n) * dx, ng, a, lib_dscalar) for n in shp]
+    info = {"name": "reacting H2/air field %dx%dx%d at rest (batched-reactor distribution as smooth fields, "
+                    "correlation length %d cells)" % (nx, ny, nz, corr),
+            "seed": seed, "dt_s": dt_s, "time_ref": a["time_ref"], "corr": corr, "dx_m": dx}
+    return cfg, thd, adi_struct(a), dxi, state, info
 
 
 def jet(nx=24, ny=16, nz=16, species="o2n2", Lx=4e-3, Lr=1.5e-3, uco=20.0, lib_dscalar=None):

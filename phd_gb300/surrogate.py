@@ -256,41 +256,58 @@ def gate10(gate):
 
 
 CAP_LADDER = (10.0, 20.0, 30.0, 50.0, 75.0, 100.0, 150.0, 200.0, 300.0, 400.0, 800.0)
+# with a fixed, short step the increments are small and so is the cap
+CAP_LADDER_FINE = (0.5, 1.0, 2.0, 3.0, 5.0, 7.5) + CAP_LADDER
+ABS_SCALE_LADDER = (1.0, 0.5, 0.25, 0.1, 0.05)
 
 
-def calibrate_cap(nets, mech, gate=DEFAULT_GATE, n=1 << 20, seed=977, target=0.005, caps=CAP_LADDER):
+def calibrate_cap(nets, mech, gate=DEFAULT_GATE, n=1 << 20, seed=977, target=0.005, caps=CAP_LADDER, dt_s=None,
+                  abs_scales=(1.0,)):
     """Choose the gate's cap on the predicted |dT| on held-out reactors: n
     reactors of the batched-chemistry distribution (another seed than the
-    training and test sets) are labelled by the FP64 BDF integrator and run
-    through the gated step without a cap; the cap is the largest value of
-    `caps` for which every accepted cell whose predicted |dT| is at most the
-    cap has an error within target x the largest |dT| of the set.  Returns
-    (gate with that cap, per-cap table)."""
+    training and test sets; with dt_s, all of them over that one step, the
+    step of the field the gate will serve) are labelled by the FP64 BDF
+    integrator and run through the gated step without a cap; the cap is the
+    largest value of `caps` for which every accepted cell whose predicted
+    |dT| is at most the cap has an error within target x the largest |dT|
+    of the set.  With several abs_scales (descending), the gate's absolute
+    tolerances -- the energy-consistency one on dT and the two networks'
+    agreement on dT -- are scaled by each in turn until a cap meets the
+    target: over a short step the increments, and the error that these
+    tolerances let through, are small.  Returns (gate, per-cap table)."""
     from .ics import batched_reactors
     T, rho, Y, dt = batched_reactors(n, seed=seed)
+    if dt_s is not None:
+        dt[:] = dt_s
     Tb, Yb = T.copy(), Y.copy()
     psr_batch(mech, Tb, rho.copy(), Yb, dt.copy())
     ref = Tb - T
-    Ts, Ys = T.copy(), Y.copy()
-    g = list(gate10(gate))
-    g[9] = float("inf")
-    r = nets[0].chem_step(mech, Ts, rho.copy(), Ys, dt.copy(), g, partner=nets[1] if len(nets) > 1 else None)
-    err = np.abs((Ts - T) - ref)
-    acc = np.ones(n, dtype=bool)
-    acc[nets[0].fallback_cells()] = False
-    pred = np.abs(r["dT_pred"])
     scale = float(np.abs(ref).max())
-    table, best = [], None
-    for cap in sorted(caps):
-        keep = acc & (pred <= cap)
-        worst = float(err[keep].max()) if keep.any() else 0.0
-        table.append({"cap_K": cap, "max_err_K": worst, "rejected_by_cap_frac": float((acc & ~keep).sum()) / n})
-        if worst <= target * scale and (best is None or cap > best):
-            best = cap
-        elif worst > target * scale:
+    g0 = list(gate10(gate))
+    table, best, g = [], None, None
+    for f in abs_scales:
+        g = list(g0)
+        g[5], g[7], g[9] = g0[5] * f, g0[7] * f, float("inf")
+        Ts, Ys = T.copy(), Y.copy()
+        r = nets[0].chem_step(mech, Ts, rho.copy(), Ys, dt.copy(), g, partner=nets[1] if len(nets) > 1 else None)
+        err = np.abs((Ts - T) - ref)
+        acc = np.ones(n, dtype=bool)
+        acc[nets[0].fallback_cells()] = False
+        pred = np.abs(r["dT_pred"])
+        for cap in sorted(caps):
+            keep = acc & (pred <= cap)
+            worst = float(err[keep].max()) if keep.any() else 0.0
+            table.append({"abs_scale": f, "cap_K": cap, "max_err_K": worst,
+                          "rejected_frac": float((~keep).sum()) / n})
+            if worst <= target * scale and (best is None or cap > best):
+                best = cap
+            elif worst > target * scale:
+                break
+        if best is not None:
             break
     g[9] = float(best if best is not None else min(caps))
-    return tuple(g), {"cells": n, "seed": seed, "target_frac": target, "scale_K": scale, "table": table}
+    return tuple(g), {"cells": n, "seed": seed, "target_frac": target, "scale_K": scale, "table": table,
+                      "dt_s": dt_s}
 
 
 def train_ensemble(mech, n=1 << 22, seed=31, epochs=30, batch=4096, lr=1e-3, members=2, log=None):

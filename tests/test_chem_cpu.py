@@ -243,3 +243,37 @@ def test_mechanism_species_match_reference_interpreter_output():
     assert [n for n, _ in rows] == names
     for k, (_, w) in enumerate(rows):
         assert abs(m.wt[k] - w) <= 5e-6 * w, (names[k], m.wt[k], w)
+
+
+def _field_reactors(dt_s):
+    """The window reactors of a 20^3 reacting field (ics.reacting_field) as
+    independent reactors: T [K], rho [g/cm^3], Y (n, 9), dt [s]."""
+    cfg, thd, adi, dxi, st, info = ics.reacting_field(20, 20, 20, dt_s=dt_s, corr=4,
+                                                      lib_dscalar=oracle.metrics_dscalar)
+    w = _window(cfg)
+    v = st["v"][w]
+    rho = np.ascontiguousarray(v[..., 0].ravel()) * adi.rho_ref * 1e-3
+    Y = np.ascontiguousarray(np.stack([v[..., 5 + k].ravel() / v[..., 0].ravel() for k in range(9)], axis=1))
+    T = np.ascontiguousarray(st["T"][w].ravel()) * adi.t_ref
+    return T, rho, Y, np.full(len(T), dt_s)
+
+
+def test_reciprocal_form_alone_on_the_reacting_field(host_chem):
+    """As above, on the window reactors of the reacting field over 1e-6 s,
+    where ignition fronts cross many cells within the step and the
+    rounding of the reciprocal form alone moves them further than in the
+    batch: held to workloads.FIELD_LIMITS, which the GPU field step meets
+    against the oracle as well (tests/test_gpu_chem.py)."""
+    import ctypes as C
+    import workloads as W
+    m = h2_mechanism()
+    T, rho, Y, dt = _field_reactors(1e-6)
+    To, Yo = T.copy(), Y.copy()
+    oracle.psr_cells(m, To, rho.copy(), Yo, dt.copy())
+    Th, Yh = T.copy(), Y.copy()
+    ns = np.zeros(len(T), np.int32)
+    host_chem.host_psr_fast(C.byref(m), len(T), _P(Th), _P(rho), _P(Yh), _P(dt), _P(ns))
+    st, msg, ok = W.reactor_error_bounds(Th, Yh, To, Yo, W.FIELD_LIMITS)
+    print(msg, "ignited (dT > 100 K): %d of %d" % (int((To - T > 100).sum()), len(T)))
+    assert ok, msg
+    assert not W.reactor_error_bounds(Th, Yh, To, Yo)[2]   # the batch bounds are too tight here

@@ -66,6 +66,39 @@ def test_field_chem_step_matches_oracle():
     assert st_["failed"] == 0
 
 
+def test_reacting_field_chem_step_matches_oracle():
+    """The field chemistry step on the learned-chemistry workload's reacting
+    field (ics.reacting_field: the batched-reactor distribution as smooth
+    fields) over 1e-6 s, the longest step of the training range, in which
+    ignition fronts cross many cells: within workloads.FIELD_LIMITS, twice
+    what the rounding of the reciprocal form alone gives on the same
+    reactors on the host (tests/test_chem_cpu.py), and DTmax alike."""
+    cfg, thd, adi, dxi, st, info = ics.reacting_field(20, 20, 20, dt_s=1e-6, corr=4,
+                                                      lib_dscalar=oracle.metrics_dscalar)
+    m = h2_mechanism()
+    orc = oracle.Oracle(cfg, thd, adi, *dxi)
+    orc.finalize_ic(st)
+    g = IzemGPU(cfg, thd, adi)
+    g.set_grid(*dxi)
+    g.upload(**st)
+    g.set_mechanism(m)
+    dt = info["dt_s"] / info["time_ref"]
+    T0 = st["T"].copy()
+    dtm_o = orc.chem_step(st, m, dt)
+    dtm_g = g.reaction_selec(dt)
+    got = g.download()
+    g.close()
+    i = (slice(3, -3),) * 3
+    v_o, v_g = st["v"][i], got["v"][i]
+    Yo = np.stack([v_o[..., q] / v_o[..., 0] for q in range(5, 14)], axis=-1).reshape(-1, 9)
+    Yg = np.stack([v_g[..., q] / v_g[..., 0] for q in range(5, 14)], axis=-1).reshape(-1, 9)
+    s_, msg, ok = W.reactor_error_bounds(got["T"][i].ravel(), Yg, st["T"][i].ravel(), Yo, W.FIELD_LIMITS)
+    print(msg, "max window dT %.1f K" % (np.abs(st["T"][i] - T0[i]).max() * adi.t_ref))
+    assert ok, msg
+    assert np.abs(st["T"][i] - T0[i]).max() * adi.t_ref > 100.0     # the field reacts
+    assert abs(dtm_g - dtm_o) <= 100 * (RTOL * abs(dtm_o) + ATOL)
+
+
 def test_chem_autotune_batch_leaves_inputs_and_keeps_results():
     """The batch autotuner times the register-budget variants on copies of a
     sample: the caller's arrays are unchanged, it reports every variant and

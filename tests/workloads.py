@@ -124,17 +124,27 @@ def oracle_step(orc, st, mech, loop):
     return dt
 
 
-def reactor_error_bounds(Tg, Yg, To, Yo):
+# Bounds that any last-bit perturbation of the right-hand side meets on the
+# batched ignition reactors (the reciprocal form alone, on the host, reaches
+# T max 97 and species p99 74).
+BATCH_LIMITS = {"T_median": 1e-3, "T_p99": 10.0, "T_max": 200.0, "Y_median": 1e-2, "Y_p90": 10.0, "Y_rel": 1e-3}
+# On the window reactors of the 20^3 reacting field over 1e-6 s, where
+# ignition fronts cross many cells within the step, the reciprocal form
+# alone reaches T median 0.0016, p99 8.8, max 209; species median 0.081,
+# p90 29; species relative to their largest value 1.33e-3.  These bounds
+# are twice that.
+FIELD_LIMITS = {"T_median": 1e-2, "T_p99": 20.0, "T_max": 400.0, "Y_median": 0.2, "Y_p90": 60.0, "Y_rel": 3e-3}
+
+
+def reactor_error_bounds(Tg, Yg, To, Yo, limits=None):
     """Errors of an integrated reactor batch against the oracle's, in the
     integrator's tolerance units per cell (T, and the largest over the
     species), plus the species error relative to each species' largest
-    value.  Returns (stats dict, message, ok) for the bounds that any
-    last-bit perturbation of the right-hand side meets on the batched
-    ignition reactors (the reciprocal form alone, on the host, reaches
-    T max 97 and species p99 74): T median < 1e-3, p99 <= 10, max <= 200;
-    species median < 1e-2, p90 <= 10; species relative to their largest
-    value plus ATOL <= 1e-3 (a species that stays below ATOL everywhere is
-    rounding noise to the integrator)."""
+    value.  Returns (stats dict, message, ok) for the given limits
+    (BATCH_LIMITS by default): T median, p99 and max; species median and
+    p90; species relative to their largest value plus ATOL (a species that
+    stays below ATOL everywhere is rounding noise to the integrator)."""
+    lim = BATCH_LIMITS if limits is None else limits
     rT = tol_units(Tg, To).ravel()
     rY = tol_units(Yg, Yo).reshape(len(rT), -1).max(axis=1)
     yn = float((np.abs(Yg - Yo) / (np.abs(Yo).max(axis=0) + ATOL)).max())
@@ -142,6 +152,6 @@ def reactor_error_bounds(Tg, Yg, To, Yo):
           "Y": {"median": float(np.median(rY)), "p90": float(np.percentile(rY, 90)), "p99": float(np.percentile(rY, 99)),
                 "max": float(rY.max())},
           "Y_rel_to_max": yn}
-    ok = (st["T"]["median"] < 1e-3 and st["T"]["p99"] <= 10 and st["T"]["max"] <= 200 and
-          st["Y"]["median"] < 1e-2 and st["Y"]["p90"] <= 10 and yn <= 1e-3)
+    ok = (st["T"]["median"] < lim["T_median"] and st["T"]["p99"] <= lim["T_p99"] and st["T"]["max"] <= lim["T_max"]
+          and st["Y"]["median"] < lim["Y_median"] and st["Y"]["p90"] <= lim["Y_p90"] and yn <= lim["Y_rel"])
     return st, "tol units: %s" % st, ok
