@@ -156,7 +156,7 @@ EULER_FLOP_PER_FACE = {9: 1869}
 
 
 def make_stepper(g, chem, mode=0):
-    """The driver's step (phd_gb300.izem.TimeLoop) with per-half-step
+    """The reference main loop's step (phd_gb300.izem.TimeLoop) with per-half-step
     chemistry statistics for the JSON line."""
     from phd_gb300.izem import TimeLoop
 

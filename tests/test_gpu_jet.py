@@ -2,7 +2,7 @@
 16 x 64 x 8 block of the same grid spacing: the jet faces (planar inflow
 with the workload's parameters and seeded fluctuations, characteristic
 outflow), the Smagorinsky closure under EGLIB (MU_SGS_FACTOR 0.17) and the
-Strang chemistry, stepped by the driver's loop (phd_gb300.izem.TimeLoop)
+Strang chemistry, stepped by the reference main loop's sequence (phd_gb300.izem.TimeLoop)
 on the GPU and by the oracle's restatement of the same sequence.
 
 Bounds, written here:

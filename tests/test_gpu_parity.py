@@ -5,7 +5,7 @@ the same operation order; the GPU evaluates the same formulas with fused
 multiply-adds and a structured (sparse) form of the eigenvector products, so
 results agree to rounding.  Every flux and state variable must agree within
 TOL = 1e-12 relative to the maximum magnitude of that variable (the
-north-star bound "1e-12 relative in FP64 per conserved variable").
+path's parity bound: 1e-12 relative in FP64 per conserved variable).
 """
 import numpy as np
 import pytest

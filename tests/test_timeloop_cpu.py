@@ -1,4 +1,4 @@
-"""The driver's step sequence (phd_gb300.izem.TimeLoop, izem.f90:252-281)
+"""The reference main loop's step sequence (phd_gb300.izem.TimeLoop, izem.f90:252-281)
 on a recording stand-in for the device context: the order of the calls,
 the half steps, the time carried, and the FIXEDDT branch of timestep
 (module_solver.f90:240-244)."""
