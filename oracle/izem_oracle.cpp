@@ -183,16 +183,16 @@ void wmix_i(const Ctx& c, int dom, const double* v, double* W_i) {
   const Block& b = c.b;
   int i0, i1, j0, j1, k0, k1;
   domain_select(b, dom, i0, i1, j0, j1, k0, k1);
+  // per point the species are summed in the reference's order
+#pragma omp parallel for collapse(2) schedule(static)
   for (int k = k0; k <= k1; ++k)
     for (int j = j0; j <= j1; ++j)
-      for (int i = i0; i <= i1; ++i) W_i[b.id(i, j, k)] = 0.0;
-  for (int l = 0; l < b.nrv; ++l)
-    for (int k = k0; k <= k1; ++k)
-      for (int j = j0; j <= j1; ++j)
-        for (int i = i0; i <= i1; ++i) {
-          size_t p = b.id(i, j, k);
-          W_i[p] = W_i[p] + (v[(NIV + l) * b.ncell + p] / v[p]) * c.thd.Wc_i[l];
-        }
+      for (int i = i0; i <= i1; ++i) {
+        size_t p = b.id(i, j, k);
+        double w = 0.0;
+        for (int l = 0; l < b.nrv; ++l) w = w + (v[(NIV + l) * b.ncell + p] / v[p]) * c.thd.Wc_i[l];
+        W_i[p] = w;
+      }
 }
 
 // newton (module_thermodynamics.f90:271-508) for one cell; returns DF and
@@ -261,6 +261,8 @@ int prim_inv_var_region(Ctx& c, bool err_mach, int i0, int i1, int j0, int j1, i
     if (it > itmax) break;
     double maxdf = 0.0;
     bool anynan = false;
+    // every point's update is its own; the maximum is the same in any order
+#pragma omp parallel for collapse(2) schedule(static) reduction(max : maxdf) reduction(|| : anynan, negT)
     for (int k = k0; k <= k1; ++k)
       for (int j = j0; j <= j1; ++j)
         for (int i = i0; i <= i1; ++i) {
@@ -319,6 +321,7 @@ void force_sumY(const Ctx& c, int dom, double* v) {
   const Block& b = c.b;
   int i0, i1, j0, j1, k0, k1;
   domain_select(b, dom, i0, i1, j0, j1, k0, k1);
+#pragma omp parallel for collapse(2) schedule(static)
   for (int k = k0; k <= k1; ++k)
     for (int j = j0; j <= j1; ++j)
       for (int i = i0; i <= i1; ++i) {
@@ -340,6 +343,7 @@ void force_sumY(const Ctx& c, int dom, double* v) {
 // comm_cons (module_parallel.f90:1715-1786) for a single periodic block:
 // face-only ghost slabs are filled from the opposite interior side.
 void comm_periodic(const Block& b, int nvar, double* a, size_t stride) {
+#pragma omp parallel for schedule(static)
   for (int l = 0; l < nvar; ++l) {
     double* q = a + l * stride;
     if (b.bc[0] == IZEM_BC_PERIODIC)
@@ -1283,6 +1287,7 @@ int visc_flux_fit(Ctx& c, const double* v, const double* T, const double* W_i, c
   for (int dom = -3; dom <= 3; ++dom) {
     int i0, i1, j0, j1, k0, k1;
     domain_select(b, dom, i0, i1, j0, j1, k0, k1);
+#pragma omp parallel for collapse(2) schedule(static)
     for (int k = k0; k <= k1; ++k)
       for (int j = j0; j <= j1; ++j)
         for (int i = i0; i <= i1; ++i) {
@@ -1457,6 +1462,7 @@ int visc_flux_fit(Ctx& c, const double* v, const double* T, const double* W_i, c
     deriv(c, 0, ax, wx.data(), true);
     deriv(c, 1, ay, wy.data(), true);
     deriv(c, 2, az, wzv.data(), true);
+#pragma omp parallel for schedule(static)
     for (size_t p = 0; p < ni; ++p) fl[var * ni + p] = fl[var * ni + p] + (wx[p] + wy[p] + wzv[p]);
   };
   if (les) {
@@ -1598,6 +1604,7 @@ int rk3(Ctx& c, double dt, double time0, double* v, double* T, double* W_i, doub
   const double ck3[3] = {1.00, 0.25, 2.00 / 3.00};
   const size_t ni = b.nint, nc = b.ncell;
   std::vector<double> v0(ni * b.nv), f(ni * b.nv, 0.0);
+#pragma omp parallel for collapse(2) schedule(static)
   for (int l = 0; l < b.nv; ++l)
     for (int k = 1; k <= b.nz; ++k)
       for (int j = 1; j <= b.ny; ++j)
@@ -1612,6 +1619,7 @@ int rk3(Ctx& c, double dt, double time0, double* v, double* T, double* W_i, doub
     if (c.cfg.vis)
       if ((rc = visc_flux(c, v, T, W_i, cp, ha, f.data()))) return rc;
     nr_boundaries(c, v, T, W_i, cp, ha, f.data());   // module_solver.f90:824
+#pragma omp parallel for collapse(2) schedule(static)
     for (int l = 0; l < b.nv; ++l)
       for (int k = 1; k <= b.nz; ++k)
         for (int j = 1; j <= b.ny; ++j)
