@@ -581,3 +581,52 @@ def test_rk3_steps_fitted_les_fourier():
     g.close()
     err = W.normwise(interior(got["v"]), interior(st["v"]))
     assert np.all(err <= TOL), err
+
+
+@pytest.mark.parametrize("shape", [(13, 11, 9), (7, 7, 7), (37, 8, 10)])
+def test_rk3_and_chemistry_on_ragged_blocks(shape):
+    """Blocks whose extents are odd, unequal, not multiples of any thread
+    block and as small as WENO5 allows (2 ng + 1 = 7 points): two RK3 steps
+    with EGLIB transport and a perturbed state, then a chemistry half step,
+    against the oracle -- the flow to TOL, the chemistry within the bounds
+    of tests/test_gpu_chem.py.  The 7^3 block has an empty reaction window
+    (reaction_dvode skips ng + 1 cells at every face); the 37 x 8 x 10 one a
+    window one cell thick in y."""
+    import oracle
+    from phd_gb300 import ics
+    from phd_gb300.mech import h2_mechanism
+    from phd_gb300.thd import eglib_link, load_species
+    nx, ny, nz = shape
+    cfg, thd, adi, dxi, st, info = ics.mixing_layer(nx, ny, nz, Lx=nx * 47e-6, Ly=ny * 47e-6, Lz=nz * 47e-6,
+                                                    lib_dscalar=oracle.metrics_dscalar)
+    cfg.eglib, cfg.reaction = 1, 1
+    link = eglib_link(load_species("h2air9"))
+    orc = oracle.Oracle(cfg, thd, adi, *dxi)
+    orc.set_eglib(link)
+    orc.finalize_ic(st)
+    W.perturb(st, 0.02, seed=11)
+    orc.update_primitives(st)
+    g = gpu_from(cfg, thd, adi, dxi, st)
+    g.set_eglib(link)
+    for _ in range(2):
+        _, dt = orc.timestep(st)
+        _, dtg = g.timestep()
+        assert abs(dtg - dt) <= 1e-14 * abs(dt)
+        orc.rk3(st, dt)
+        g.rk3(dt)
+    got = g.download()
+    err = W.normwise(interior(got["v"]), interior(st["v"]))
+    assert np.all(err <= TOL), err
+    mech = h2_mechanism()
+    g.set_mechanism(mech)
+    g.upload(**st)
+    dtm_o = orc.chem_step(st, mech, 500.0 * dt)
+    dtm_g = g.reaction_selec(500.0 * dt)
+    got = g.download()
+    g.close()
+    s = W.chem_error_stats(got, st)
+    assert s["T"]["max"] <= 200 and s["Y"]["p99"] <= 10, s
+    # DTmax [K] within the integrator's tolerance on temperatures up to 3000 K
+    assert abs(dtm_g - dtm_o) <= 100 * (W.RTOL * 3000.0 + W.ATOL)
+    if nx == ny == nz == 7:
+        assert dtm_o == 0.0 and dtm_g == 0.0
