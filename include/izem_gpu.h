@@ -119,7 +119,10 @@ typedef struct izem_adi {
  * species molar masses, NASA-7 thermo with CHEMKIN's mid-temperature switch,
  * and per reaction: stoichiometry (up to 3 reactants, 3 products), forward
  * Arrhenius (A, b, E/R), reverse kind, third-body efficiencies, fall-off
- * (LOW + Troe).  Units: mol, cm, s, K, erg. */
+ * (LOW with the Lindemann, SRI or Troe broadening of CKRATX,
+ * vode.f:1185-1236; the collider (+M) or one species (+K)).  Units: mol,
+ * cm, s, K, erg.  The last two members were added after the others; a
+ * zero-filled tail means no SRI reaction and (+M) colliders. */
 #define IZEM_MAXREAC 32
 typedef struct izem_mech {
   int    kk, ii;
@@ -136,9 +139,13 @@ typedef struct izem_mech {
   double rpar[IZEM_MAXREAC][3];           /* REV A, b, E/R                    */
   int    thb[IZEM_MAXREAC];               /* 1: +M or (+M) third body         */
   double eff[IZEM_MAXREAC][IZEM_NSMAX];   /* third-body efficiencies          */
-  int    fall[IZEM_MAXREAC];              /* 0 none, 1 Lindemann, 3/4 Troe    */
+  int    fall[IZEM_MAXREAC];              /* 0 none, 1 Lindemann, 2 SRI,
+                                             3/4 Troe with 3/4 parameters     */
   double low[IZEM_MAXREAC][3];            /* LOW A, b, E/R                    */
   double troe[IZEM_MAXREAC][4];           /* a, T***, T*, T**                 */
+  double sri[IZEM_MAXREAC][5];            /* SRI a, b [K], c [K], d, e        */
+  int    kfal[IZEM_MAXREAC];              /* fall-off collider: 0 (+M), k+1
+                                             species k alone, (+K)            */
 } izem_mech;
 
 /* EGLIB linking data (the contents of the Linkeg file that EGINI reads,

@@ -84,6 +84,7 @@ class IzemMech(C.Structure):
         ("thb", C.c_int * MAXREAC), ("eff", (C.c_double * NSMAX) * MAXREAC),
         ("fall", C.c_int * MAXREAC), ("low", (C.c_double * 3) * MAXREAC),
         ("troe", (C.c_double * 4) * MAXREAC),
+        ("sri", (C.c_double * 5) * MAXREAC), ("kfal", C.c_int * MAXREAC),
     ]
 
 

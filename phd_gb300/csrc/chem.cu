@@ -52,6 +52,7 @@ struct ChemFast {
   double wt_inv[IZEM_NSMAX];          // 1 / W_k
   double ru_wt[IZEM_NSMAX];           // RU / W_k
   double troe_inv[IZEM_MAXREAC][2];   // 1 / T***, 1 / T*
+  double sri_cinv[IZEM_MAXREAC];      // 1 / c of the SRI form
 };
 __constant__ ChemFast c_fast_dev;
 #ifdef IZEM_CHEM_HOST_TEST
@@ -163,10 +164,16 @@ HD void ck_wyr(double rho, double T, const double* Y, double* wdot) {
     const int fo = c_mech.fall[i];
     if (fo) {
       const double rklow = c_mech.low[i][0] * exp(c_mech.low[i][1] * alogt - c_mech.low[i][2] / T);
-      const double pr = rklow * ctb / rkft;
-      ctb = 1.0;
+      const int kf = c_mech.kfal[i];   // collider: (+M), or species kf - 1 alone
+      const double pr = rklow * (kf ? C[kf - 1] : ctb) / rkft;
+      if (!kf) ctb = 1.0;
       double pcor = pr / (1.0 + pr);
-      if (fo > 1) {
+      if (fo == 2) {
+        const double prlog = log10(fmax(pr, 1.0e-300));
+        const double xp = 1.0 / (1.0 + prlog * prlog);
+        const double* sr = c_mech.sri[i];
+        pcor = pow(sr[0] * exp(-sr[1] / T) + exp(-T / sr[2]), xp) * sr[3] * pow(T, sr[4]) * pcor;
+      } else if (fo > 1) {
         const double prlog = log10(fmax(pr, 1.0e-300));
         const double ta = c_mech.troe[i][0];
         double fcent = (1.0 - ta) * exp(-T / c_mech.troe[i][1]) + ta * exp(-T / c_mech.troe[i][2]);
@@ -232,6 +239,7 @@ inline ChemFast chem_fast_constants(const izem_mech& m) {
   for (int i = 0; i < m.ii && i < IZEM_MAXREAC; ++i) {
     f.troe_inv[i][0] = m.troe[i][1] != 0.0 ? 1.0 / m.troe[i][1] : 0.0;
     f.troe_inv[i][1] = m.troe[i][2] != 0.0 ? 1.0 / m.troe[i][2] : 0.0;
+    f.sri_cinv[i] = m.fall[i] == 2 && m.sri[i][2] != 0.0 ? 1.0 / m.sri[i][2] : 0.0;
   }
   return f;
 }
@@ -295,7 +303,10 @@ HD void fun_tpart(double T, FunT<KK>& t) {
     const int fo = c_mech.fall[i];
     if (fo) {
       t.klow[i] = c_mech.low[i][0] * exp(c_mech.low[i][1] * alogt - c_mech.low[i][2] * Tinv);
-      if (fo > 1) {
+      if (fo == 2) {   // SRI: ln(a exp(-b/T) + exp(-T/c)) in the fclog slot
+        const double* sr = c_mech.sri[i];
+        t.fclog[i] = log(sr[0] * exp(-sr[1] * Tinv) + exp(-T * c_fast.sri_cinv[i]));
+      } else if (fo > 1) {
         constexpr double kInvLn10 = 0.4342944819032518277;
         const double ta = c_mech.troe[i][0];
         double fcent = (1.0 - ta) * exp(-T * c_fast.troe_inv[i][0]) + ta * exp(-T * c_fast.troe_inv[i][1]);
@@ -332,10 +343,15 @@ HD void fun_cpart(double rho, const double* z, const FunT<KK>& t, double* zp) {
     }
     const int fo = c_mech.fall[i];
     if (fo) {
-      const double pr = t.klow[i] * ctb / rkft;
-      ctb = 1.0;
+      const int kf = c_mech.kfal[i];   // collider: (+M), or species kf - 1 alone
+      const double pr = t.klow[i] * (kf ? C[kf - 1] : ctb) / rkft;
+      if (!kf) ctb = 1.0;
       double pcor = pr / (1.0 + pr);
-      if (fo > 1) {
+      if (fo == 2) {
+        const double prlog = log(fmax(pr, 1.0e-300)) * kInvLn10;
+        const double xp = 1.0 / (1.0 + prlog * prlog);
+        pcor = exp(xp * t.fclog[i]) * c_mech.sri[i][3] * pow(t.T, c_mech.sri[i][4]) * pcor;
+      } else if (fo > 1) {
         const double prlog = log(fmax(pr, 1.0e-300)) * kInvLn10;
         const double fclog = t.fclog[i];
         const double xn = 0.75 - 1.27 * fclog;
@@ -380,7 +396,7 @@ HD void fun_cpart(double rho, const double* z, const FunT<KK>& t, double* zp) {
 }
 
 // The constant-volume reactor right-hand side of ck_fun with the divisions
-// by T, by the molar masses and by the Troe temperatures replaced by
+// by T, by the molar masses and by the Troe and SRI temperatures replaced by
 // multiplications with reciprocals, and 10^x / log10 by exp / log: the same
 // CHEMKIN expressions (CKCVBS, CKHMS, CKRATT, CKRATX, CKWYR) with different
 // rounding (a few ulp per term) and about a sixth of the FP64 instructions
@@ -394,7 +410,13 @@ HD void ck_fun_fast(double rho, const double* z, double* zp) {
   fun_cpart<KK>(rho, z, t, zp);
 }
 
+// The generated right-hand side: the shipped mechanism's, or another one
+// that mechgen wrote (-DIZEM_CHEM_GEN_HEADER="\"path\"" at build time).
+#ifdef IZEM_CHEM_GEN_HEADER
+#include IZEM_CHEM_GEN_HEADER
+#else
 #include "chem_gen.cuh"
+#endif
 
 // Right-hand-side policies of the BDF driver: the generic form, which walks
 // the uploaded mechanism's tables, and the generated form of the mechanism

@@ -8,8 +8,10 @@ parameters (REV), third-body efficiencies, LOW fall-off and TROE.
 
 Supported syntax: ELEMENTS/SPECIES/REACTIONS/END blocks, '!' comments, the
 REACTIONS units keywords CAL/MOLE KCAL/MOLE JOULES/MOLE KJOULES/MOLE
-KELVINS, '=', '<=>', '=>', '+M', '(+M)', integer stoichiometric prefixes,
-auxiliary keywords REV, LOW, TROE and species efficiencies 'S/val/'.
+KELVINS, '=', '<=>', '=>', '+M', '(+M)', a species as the fall-off collider
+'(+K)', integer stoichiometric prefixes, auxiliary keywords REV, LOW, TROE,
+SRI (3 or 5 parameters; d = 1, e = 0 when 3 are given) and species
+efficiencies 'S/val/'.
 """
 import os
 import re
@@ -30,13 +32,20 @@ def _strip(line):
 
 
 def _side(txt, species):
-    """Parse one side of a reaction equation -> list of (species index, coeff)
-    and whether it carries +M / (+M)."""
+    """Parse one side of a reaction equation -> list of (species index, coeff),
+    whether it carries +M, whether it carries a fall-off collider (+M) or
+    (+K), and the collider as izem_mech's kfal (0: (+M), k+1: species k)."""
     txt = txt.replace(" ", "")
-    fall = False
-    if "(+M)" in txt:
+    fall, kfal = False, 0
+    col = re.search(r"\(\+([^()]+)\)", txt)
+    if col:
         fall = True
-        txt = txt.replace("(+M)", "")
+        nm = col.group(1)
+        if nm.upper() != "M":
+            if nm not in species:
+                raise ValueError("unknown fall-off collider %s" % nm)
+            kfal = species.index(nm) + 1
+        txt = txt.replace(col.group(0), "")
     parts = [p for p in txt.split("+") if p]
     thb = False
     out = {}
@@ -51,7 +60,7 @@ def _side(txt, species):
             raise ValueError("unknown species %s" % nm)
         k = species.index(nm)
         out[k] = out.get(k, 0) + n
-    return sorted(out.items()), thb, fall
+    return sorted(out.items()), thb, fall, kfal
 
 
 def read_mechanism(path, thermo_set="h2air9"):
@@ -93,11 +102,13 @@ def read_mechanism(path, thermo_set="h2air9"):
                         lhs, rhs = eq.split("=>"); rev = 0
                     else:
                         lhs, rhs = eq.split("="); rev = 1
-                    r, thb1, fall1 = _side(lhs, species)
-                    p, thb2, fall2 = _side(rhs, species)
+                    r, thb1, fall1, kfal1 = _side(lhs, species)
+                    p, thb2, fall2, kfal2 = _side(rhs, species)
+                    if fall1 != fall2 or kfal1 != kfal2:
+                        raise ValueError("fall-off collider differs between the sides: %s" % eq)
                     reactions.append({"eq": eq, "reac": r, "prod": p, "par": (A, b, E * escale), "rev": rev,
-                                      "rpar": None, "thb": thb1 or fall1, "fall": 1 if fall1 else 0,
-                                      "low": None, "troe": None, "eff": {}})
+                                      "rpar": None, "thb": thb1 or (fall1 and not kfal1), "fall": 1 if fall1 else 0,
+                                      "kfal": kfal1, "low": None, "troe": None, "sri": None, "eff": {}})
                 else:
                     rx = reactions[-1]
                     for kw, body in re.findall(r"([A-Za-z0-9()]+)\s*/([^/]*)/", l):
@@ -110,7 +121,10 @@ def read_mechanism(path, thermo_set="h2air9"):
                             rx["low"] = (vals[0], vals[1], vals[2] * escale)
                         elif kwu == "TROE":
                             rx["troe"] = vals
-                            rx["fall"] = len(vals)
+                        elif kwu == "SRI":
+                            if len(vals) not in (3, 5):
+                                raise ValueError("SRI takes 3 or 5 parameters: %s" % rx["eq"])
+                            rx["sri"] = vals + [1.0, 0.0][len(vals) - 3:]
                         elif kw in species:
                             rx["eff"][species.index(kw)] = vals[0]
                         else:
@@ -162,12 +176,20 @@ def build_struct(species, reactions, thermo_set):
         if rx["fall"]:
             if rx["low"] is None:
                 raise ValueError("fall-off reaction without LOW: %s" % rx["eq"])
-            m.fall[i] = rx["fall"] if rx["troe"] else 1
+            if rx["troe"] and rx["sri"]:
+                raise ValueError("both TROE and SRI: %s" % rx["eq"])
+            if rx["troe"] and len(rx["troe"]) not in (3, 4):
+                raise ValueError("TROE takes 3 or 4 parameters: %s" % rx["eq"])
+            m.fall[i] = len(rx["troe"]) if rx["troe"] else (2 if rx["sri"] else 1)
+            m.kfal[i] = rx["kfal"]
             for c in range(3):
                 m.low[i][c] = rx["low"][c]
             if rx["troe"]:
                 for c, val in enumerate(rx["troe"]):
                     m.troe[i][c] = val
+            if rx["sri"]:
+                for c, val in enumerate(rx["sri"]):
+                    m.sri[i][c] = val
     return m
 
 

@@ -13,9 +13,10 @@ The arithmetic is the generic form's (fun_tpart / fun_cpart in chem.cu),
 operation for operation, so a host build of the two gives identical bits.
 
 Supported: explicit reverse parameters (REV) and irreversible reactions,
-+M third bodies with efficiencies, Lindemann and Troe (3 or 4 parameter)
-fall-off.  Reactions with equilibrium reverse rates raise
-``NotImplementedError``; such mechanisms use the generic kernels.
++M third bodies with efficiencies, Lindemann, SRI and Troe (3 or 4
+parameter) fall-off with the (+M) collider or one species (+K).  Reactions
+with equilibrium reverse rates raise ``NotImplementedError``; such
+mechanisms use the generic kernels.
 
 ``python -m phd_gb300.mechgen`` rewrites ``csrc/chem_gen.cuh`` from the
 shipped mechanism; a test checks that the committed file is what this
@@ -61,10 +62,11 @@ def _reactions(m):
     for i in range(m.ii):
         r = {"i": i, "nuk": list(m.nuk[i]), "nu": list(m.nu[i]), "par": list(m.par[i]), "rev": m.rev[i],
              "rpar": list(m.rpar[i]), "thb": m.thb[i], "fall": m.fall[i], "low": list(m.low[i]),
-             "troe": list(m.troe[i]), "eff": [m.eff[i][k] for k in range(m.kk)]}
+             "troe": list(m.troe[i]), "sri": list(m.sri[i]), "kfal": m.kfal[i],
+             "eff": [m.eff[i][k] for k in range(m.kk)]}
         if r["rev"] == 1:
             raise NotImplementedError("reaction %d: equilibrium reverse rate" % i)
-        if r["fall"] not in (0, 1, 3, 4):
+        if r["fall"] not in (0, 1, 2, 3, 4):
             raise NotImplementedError("reaction %d: fall-off form %d" % (i, r["fall"]))
         if r["nu"][0] == 0:
             raise NotImplementedError("reaction %d: no reactant" % i)
@@ -138,7 +140,12 @@ def generate(m, name="h2air9", source="phd_gb300/data/h2_sandiego12.inp"):
         if r["fall"]:
             q = r["low"]
             w("  t.klow[%d] = %s * exp(%s * alogt - %s * Tinv);" % (lo_slot[i], lit(q[0]), lit(q[1]), lit(q[2])))
-            if r["fall"] > 1:
+            if r["fall"] == 2:   # SRI: ln(a exp(-b/T) + exp(-T/c)) in the fclog slot
+                sr = r["sri"]
+                cinv = 1.0 / sr[2] if sr[2] != 0.0 else 0.0
+                w("  t.fclog[%d] = log(%s * exp(-%s * Tinv) + exp(-T * %s));" % (tr_slot[i], lit(sr[0]), lit(sr[1]),
+                                                                                  lit(cinv)))
+            elif r["fall"] > 1:
                 ta = r["troe"][0]
                 ti0 = 1.0 / r["troe"][1] if r["troe"][1] != 0.0 else 0.0
                 ti1 = 1.0 / r["troe"][2] if r["troe"][2] != 0.0 else 0.0
@@ -177,10 +184,20 @@ def generate(m, name="h2air9", source="phd_gb300/data/h2_sandiego12.inp"):
             ctb = "ctb"
         if r["fall"]:
             f = lo_slot[i]
-            w("    const double pr = t.klow[%d] * %s / rkft;" % (f, ctb if ctb else "1.0"))
-            ctb = None
+            if r["kfal"]:   # one species is the collider; a third-body factor stays
+                w("    const double pr = t.klow[%d] * C%d / rkft;" % (f, r["kfal"] - 1))
+            else:
+                w("    const double pr = t.klow[%d] * %s / rkft;" % (f, ctb if ctb else "1.0"))
+                ctb = None
             w("    double pcor = pr / (1.0 + pr);")
-            if r["fall"] > 1:
+            if r["fall"] == 2:
+                w("    {")
+                w("      const double prlog = log(fmax(pr, 1.0e-300)) * 0.4342944819032518277;")
+                w("      const double xp = 1.0 / (1.0 + prlog * prlog);")
+                w("      pcor = exp(xp * t.fclog[%d]) * %s * pow(t.T, %s) * pcor;" % (tr_slot[i], lit(r["sri"][3]),
+                                                                                   lit(r["sri"][4])))
+                w("    }")
+            elif r["fall"] > 1:
                 w("    {")
                 w("      const double prlog = log(fmax(pr, 1.0e-300)) * 0.4342944819032518277;")
                 w("      const double fclog = t.fclog[%d];" % tr_slot[i])
@@ -257,9 +274,13 @@ def generate(m, name="h2air9", source="phd_gb300/data/h2_sandiego12.inp"):
             for k in range(kk):
                 conds.append("b(m.eff[%d][%d]) == %s" % (i, k, bits(r["eff"][k])))
         if r["fall"]:
+            conds.append("m.kfal[%d] == %d" % (i, r["kfal"]))
             for j in range(3):
                 conds.append("b(m.low[%d][%d]) == %s" % (i, j, bits(r["low"][j])))
-            if r["fall"] > 1:
+            if r["fall"] == 2:
+                for j in range(5):
+                    conds.append("b(m.sri[%d][%d]) == %s" % (i, j, bits(r["sri"][j])))
+            elif r["fall"] > 1:
                 for j in range(4 if r["fall"] == 4 else 3):
                     conds.append("b(m.troe[%d][%d]) == %s" % (i, j, bits(r["troe"][j])))
     for q in range(0, len(conds), 4):

@@ -89,3 +89,38 @@ def test_entry_points_reject_bad_arguments_before_any_device_call():
     assert lib.izem_gpu_set_chem_skip(None, 1, p, p, 0, 8) == 1
     lib.izem_gpu_set_les.argtypes = [C.c_void_p, C.c_int] + [C.c_double] * 4
     assert lib.izem_gpu_set_les(None, 1, 0.18, 0.7, 0.7, 70.0) == 1
+
+
+def test_struct_layout_matches_a_c_compiler(tmp_path):
+    """The ctypes mirrors of the header's structs have the sizes and member
+    offsets a C compiler gives them (gcc on include/izem_gpu.h), including
+    the mechanism's SRI and collider tables at its end."""
+    import shutil
+    import subprocess
+    from phd_gb300.capi import IzemAdi, IzemCfg, IzemEglib, IzemMech, IzemThd
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        pytest.skip("gcc not available")
+    here = os.path.dirname(os.path.abspath(__file__))
+    inc = os.path.join(os.path.dirname(here), "include")
+    checks = [("izem_cfg", IzemCfg, ["ng", "bc", "cfl", "weno5_linear_fix"]),
+              ("izem_thd", IzemThd, ["heatcap", "cofd", "cofeta"]),
+              ("izem_adi", IzemAdi, ["time_ref", "d_ref"]),
+              ("izem_eglib", IzemEglib, ["cofe", "cofd"]),
+              ("izem_mech", IzemMech, ["a", "eff", "troe", "sri", "kfal"])]
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "izem_gpu.h"', "int main(void) {"]
+    for name, _, members in checks:
+        lines.append('  printf("%%zu\\n", sizeof(%s));' % name)
+        for mem in members:
+            lines.append('  printf("%%zu\\n", offsetof(%s, %s));' % (name, mem))
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = str(tmp_path / "layout")
+    subprocess.check_call([gcc, "-std=c11", "-I", inc, "-o", exe, str(src)])
+    got = [int(x) for x in subprocess.check_output([exe]).split()]
+    want = []
+    for _, cls, members in checks:
+        want.append(C.sizeof(cls))
+        want += [getattr(cls, mem).offset for mem in members]
+    assert got == want

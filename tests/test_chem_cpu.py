@@ -277,3 +277,142 @@ def test_reciprocal_form_alone_on_the_reacting_field(host_chem):
     print(msg, "ignited (dT > 100 K): %d of %d" % (int((To - T > 100).sum()), len(T)))
     assert ok, msg
     assert not W.reactor_error_bounds(Th, Yh, To, Yo)[2]   # the batch bounds are too tight here
+
+
+from workloads import SRI_PARAMS as _SRI_PARAMS, variant_mechanism as _variant_mechanism  # noqa: E402
+
+
+def test_reader_sri_and_species_collider(tmp_path):
+    """SRI / a b c d e / gives fall-off form 2 with its five parameters (three
+    given: d = 1, e = 0); (+H2O) makes H2O the collider (kfal = index + 1)
+    and no third-body sum."""
+    m = _variant_mechanism(tmp_path)
+    assert m.fall[3] == 2 and list(m.sri[3]) == list(_SRI_PARAMS) and m.kfal[3] == 0 and m.thb[3] == 1
+    assert m.fall[11] == 4 and m.kfal[11] == 6 and m.thb[11] == 0     # H2O is species 5
+    text = (tmp_path / "h2_sri_collider.inp").read_text().replace(
+        "SRI / %s /" % "  ".join(repr(x) for x in _SRI_PARAMS), "SRI / 0.45 797.0 979.0 /")
+    (tmp_path / "three.inp").write_text(text)
+    from phd_gb300.mech import read_mechanism
+    m3 = read_mechanism(str(tmp_path / "three.inp"), "h2air9")
+    assert list(m3.sri[3]) == [0.45, 797.0, 979.0, 1.0, 0.0]
+    assert all(m.kfal[i] == 0 for i in range(m.ii) if i != 11)
+
+
+def _only(m, keep):
+    """The mechanism with every reaction but `keep` switched off (A = 0, no
+    fall-off)."""
+    import copy
+    m2 = copy.deepcopy(m)
+    for i in range(m2.ii):
+        if i != keep:
+            m2.par[i][0] = 0.0
+            m2.rpar[i][0] = 0.0
+            m2.fall[i] = 0
+    return m2
+
+
+def _with_radicals(Y):
+    """Batched-reactor compositions with H, O, OH and H2O2 added (1e-3 each,
+    the rest scaled down), so that every reaction has reactants."""
+    Y = Y * (1.0 - 4e-3)
+    for k in (0, 2, 4, 7):
+        Y[:, k] += 1e-3
+    return np.ascontiguousarray(Y)
+
+
+def test_sri_and_collider_rates_against_a_restatement(tmp_path):
+    """The oracle's production rates of each of the two reactions alone
+    against a numpy restatement of CKRATX (vode.f:1185-1236): the SRI factor
+    (a exp(-b/T) + exp(-T/c))^X d T^e with X = 1 / (1 + log10(Pr)^2) and Pr
+    from the efficiency-weighted third body; the Troe factor with Pr from
+    the H2O concentration alone."""
+    m = _variant_mechanism(tmp_path)
+    T, rho, Y, dt = ics.batched_reactors(256, seed=41)
+    Y = _with_radicals(Y)
+    W = np.array([m.wt[k] for k in range(m.kk)])
+    ih, io2, ih2o, ih2o2 = 0, 3, 5, 7
+    for i in (3, 11):
+        mi = _only(m, i)
+        for q in range(len(T)):
+            wdot = oracle.ck_wdot(mi, rho[q], T[q], Y[q])
+            C = rho[q] * Y[q] / W
+            Tq = T[q]
+            A, b, ER = m.par[i][0], m.par[i][1], m.par[i][2]
+            kf = A * np.exp(b * np.log(Tq) - ER / Tq)
+            kl = m.low[i][0] * np.exp(m.low[i][1] * np.log(Tq) - m.low[i][2] / Tq)
+            if i == 3:
+                ctb = C.sum() + sum((m.eff[i][k] - 1.0) * C[k] for k in range(m.kk))
+                pr = kl * ctb / kf
+                a, bb, c, d, e = _SRI_PARAMS
+                x = 1.0 / (1.0 + np.log10(max(pr, 1e-300)) ** 2)
+                fc = (a * np.exp(-bb / Tq) + np.exp(-Tq / c)) ** x * d * Tq ** e
+                rop = kf * fc * pr / (1.0 + pr) * C[ih] * C[io2]
+                ref = {ih: -rop, io2: -rop, 6: rop}
+            else:
+                pr = kl * C[ih2o] / kf
+                ta, t3, t1, t2 = (m.troe[i][k] for k in range(4))
+                fcent = (1 - ta) * np.exp(-Tq / t3) + ta * np.exp(-Tq / t1) + np.exp(-t2 / Tq)
+                lfc = np.log10(fcent)
+                cpr = np.log10(pr) - (0.4 + 0.67 * lfc)
+                nn = 0.75 - 1.27 * lfc
+                fc = 10.0 ** (lfc / (1.0 + (cpr / (nn - 0.14 * cpr)) ** 2))
+                rop = kf * fc * pr / (1.0 + pr) * C[ih2o2]
+                ref = {ih2o2: -rop, 4: 2.0 * rop}
+            for k in range(m.kk):
+                assert abs(wdot[k] - ref.get(k, 0.0)) <= 1e-13 * abs(rop), (i, q, k, wdot[k], ref.get(k, 0.0))
+
+
+def test_sri_and_collider_device_forms_on_the_host(host_chem, tmp_path):
+    """With the variant mechanism, the device integrator in the reference's
+    operation order reproduces the oracle bit for bit on the host, and the
+    reciprocal form agrees with it to 1e-12 of each component's largest
+    rate."""
+    import ctypes as C
+    m = _variant_mechanism(tmp_path)
+    T, rho, Y, dt = ics.batched_reactors(512, seed=43)
+    To, Yo = T.copy(), Y.copy()
+    oracle.psr_cells(m, To, rho.copy(), Yo, dt.copy())
+    Th, Yh = T.copy(), Y.copy()
+    ns = np.zeros(len(T), np.int32)
+    host_chem.host_psr(C.byref(m), len(T), _P(Th), _P(rho), _P(Yh), _P(dt), _P(ns))
+    assert np.array_equal(Th, To) and np.array_equal(Yh, Yo)
+    assert not np.array_equal(To, T)
+    z = np.ascontiguousarray(np.concatenate([T[:, None], Y], axis=1))
+    zr, zf = np.zeros_like(z), np.zeros_like(z)
+    host_chem.host_fun_pair(C.byref(m), len(T), _P(rho), _P(z), _P(zr), _P(zf))
+    scale = np.abs(zr).max(axis=0)
+    err = (np.abs(zf - zr) / np.where(scale == 0, 1.0, scale)).max(axis=0)
+    assert np.all(err < 1e-12), err
+
+
+def test_generated_rhs_for_sri_and_collider(tmp_path):
+    """mechgen writes the variant's right-hand side; compiled into the host
+    harness in place of the shipped header (IZEM_CHEM_GEN_HEADER), it is the
+    reciprocal table form bit for bit, and it recognises its own mechanism."""
+    import ctypes as C
+    import shutil
+    import subprocess
+    from phd_gb300 import mechgen
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(nvcc):
+        pytest.skip("nvcc not available")
+    m = _variant_mechanism(tmp_path)
+    hdr = tmp_path / "chem_gen_variant.cuh"
+    hdr.write_text(mechgen.generate(m, source="the SRI / collider test mechanism"))
+    here = os.path.dirname(os.path.abspath(__file__))
+    so = str(tmp_path / "libchemgen.so")
+    subprocess.check_call([nvcc, "-std=c++17", "-O2", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+                           "-shared", "-gencode", "arch=compute_103a,code=sm_103a",
+                           '-DIZEM_CHEM_GEN_HEADER="%s"' % str(hdr), "-o", so,
+                           os.path.join(here, "harness", "chem_host_harness.cu")])
+    lib = C.CDLL(so)
+    T, rho, Y, dt = ics.batched_reactors(1024, seed=47)
+    z = np.ascontiguousarray(np.concatenate([T[:, None], Y], axis=1))
+    zt, zg = np.zeros_like(z), np.zeros_like(z)
+    ok = C.c_int()
+    lib.host_fun_gen_pair(C.byref(m), len(T), _P(rho), _P(z), _P(zt), _P(zg), C.byref(ok))
+    assert ok.value == 1
+    assert np.array_equal(zt, zg), np.abs(zt - zg).max(axis=0)
+    m.sri[3][4] = 0.2   # another SRI exponent: not the generated mechanism
+    lib.host_fun_gen_pair(C.byref(m), 4, _P(rho), _P(z), _P(np.zeros_like(z)), _P(np.zeros_like(z)), C.byref(ok))
+    assert ok.value == 0

@@ -99,6 +99,23 @@ def test_reacting_field_chem_step_matches_oracle():
     assert abs(dtm_g - dtm_o) <= 100 * (RTOL * abs(dtm_o) + ATOL)
 
 
+def test_psr_batch_with_sri_and_species_collider(tmp_path):
+    """The persistent BDF kernels with a mechanism that uses the SRI fall-off
+    form and a single-species collider (workloads.variant_mechanism; no
+    generated right-hand side matches it, so the kernels walk the tables):
+    within the bounds above against the oracle."""
+    m = W.variant_mechanism(tmp_path)
+    T, rho, Y, dt = ics.batched_reactors(2048, seed=51)
+    To, Yo = T.copy(), Y.copy()
+    ist_o, _ = oracle.psr_cells(m, To, rho.copy(), Yo, dt.copy())
+    Tg, Yg = T.copy(), Y.copy()
+    ist_g, _, _ = psr_batch(m, Tg, rho.copy(), Yg, dt.copy())
+    assert np.all(ist_g == 2) and np.all(ist_o == 2)
+    st, msg, ok = W.reactor_error_bounds(Tg, Yg, To, Yo)
+    print(msg)
+    assert ok, msg
+
+
 def test_chem_autotune_batch_leaves_inputs_and_keeps_results():
     """The batch autotuner times the register-budget variants on copies of a
     sample: the caller's arrays are unchanged, it reports every variant and

@@ -155,3 +155,28 @@ def reactor_error_bounds(Tg, Yg, To, Yo, limits=None):
     ok = (st["T"]["median"] < lim["T_median"] and st["T"]["p99"] <= lim["T_p99"] and st["T"]["max"] <= lim["T_max"]
           and st["Y"]["median"] < lim["Y_median"] and st["Y"]["p90"] <= lim["Y_p90"] and yn <= lim["Y_rel"])
     return st, "tol units: %s" % st, ok
+
+
+# The shipped mechanism with its first fall-off reaction in the SRI form and
+# its second with one species, H2O, as the collider: the CKRATX branches
+# (vode.f:1185-1236) the H2/air set does not use.  The parameters exercise
+# those branches; they are not fitted to any data.
+SRI_PARAMS = (0.45, 797.0, 979.0, 1.2, 0.1)
+
+
+def variant_mechanism(tmp_path):
+    """Write the variant mechanism under tmp_path (a pathlib.Path) and read
+    it with phd_gb300.mech.read_mechanism."""
+    import os
+    from phd_gb300.mech import read_mechanism
+    from phd_gb300.thd import DATA_DIR
+    with open(os.path.join(DATA_DIR, "h2_sandiego12.inp")) as f:
+        text = f.read()
+    text = text.replace("   TROE / 0.5  1.0E-30  1.0E30 /\n",
+                        "   SRI / %s /\n" % "  ".join(repr(x) for x in SRI_PARAMS))
+    text = text.replace("H2O2(+M)=>OH+OH(+M)", "H2O2(+H2O)=>OH+OH(+H2O)")
+    text = text.replace("   TROE / 0.735  94.0  1756.0  5182.0 /\n   H2/2.5/ H2O/6.0/\n",
+                        "   TROE / 0.735  94.0  1756.0  5182.0 /\n")
+    path = tmp_path / "h2_sri_collider.inp"
+    path.write_text(text)
+    return read_mechanism(str(path), "h2air9")
