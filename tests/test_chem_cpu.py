@@ -416,3 +416,19 @@ def test_generated_rhs_for_sri_and_collider(tmp_path):
     m.sri[3][4] = 0.2   # another SRI exponent: not the generated mechanism
     lib.host_fun_gen_pair(C.byref(m), 4, _P(rho), _P(z), _P(np.zeros_like(z)), _P(np.zeros_like(z)), C.byref(ok))
     assert ok.value == 0
+
+
+@pytest.mark.parametrize("line", ["   LT / 1.0 2.0 /\n", "   FORD / H2 0.5 /\n"])
+def test_reader_rejects_rate_forms_it_does_not_build(tmp_path, line):
+    """Landau-Teller and reaction-order auxiliary data are refused, not
+    dropped."""
+    from phd_gb300.mech import read_mechanism
+    from phd_gb300.thd import DATA_DIR
+    with open(os.path.join(DATA_DIR, "h2_sandiego12.inp")) as f:
+        text = f.read()
+    text = text.replace("HO2+H=>OH+OH                 7.08E13   0.00   0.294\n",
+                        "HO2+H=>OH+OH                 7.08E13   0.00   0.294\n" + line)
+    path = tmp_path / "bad.inp"
+    path.write_text(text)
+    with pytest.raises(ValueError):
+        read_mechanism(str(path), "h2air9")
