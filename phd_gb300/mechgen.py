@@ -12,11 +12,10 @@ as literals: reaction loops unrolled, indices fixed, absent terms dropped.
 The arithmetic is the generic form's (fun_tpart / fun_cpart in chem.cu),
 operation for operation, so a host build of the two gives identical bits.
 
-Supported: explicit reverse parameters (REV) and irreversible reactions,
-+M third bodies with efficiencies, Lindemann, SRI and Troe (3 or 4
-parameter) fall-off with the (+M) collider or one species (+K).  Reactions
-with equilibrium reverse rates raise ``NotImplementedError``; such
-mechanisms use the generic kernels.
+Supported: irreversible reactions, reverse rates from the equilibrium
+constant (CKSMH's entropy-enthalpy difference) or from explicit parameters
+(REV), +M third bodies with efficiencies, Lindemann, SRI and Troe (3 or 4
+parameter) fall-off with the (+M) collider or one species (+K).
 
 ``python -m phd_gb300.mechgen`` rewrites ``csrc/chem_gen.cuh`` from the
 shipped mechanism; a test checks that the committed file is what this
@@ -64,8 +63,6 @@ def _reactions(m):
              "rpar": list(m.rpar[i]), "thb": m.thb[i], "fall": m.fall[i], "low": list(m.low[i]),
              "troe": list(m.troe[i]), "sri": list(m.sri[i]), "kfal": m.kfal[i],
              "eff": [m.eff[i][k] for k in range(m.kk)]}
-        if r["rev"] == 1:
-            raise NotImplementedError("reaction %d: equilibrium reverse rate" % i)
         if r["fall"] not in (0, 1, 2, 3, 4):
             raise NotImplementedError("reaction %d: fall-off form %d" % (i, r["fall"]))
         if r["nu"][0] == 0:
@@ -77,7 +74,8 @@ def _reactions(m):
 def generate(m, name="h2air9", source="phd_gb300/data/h2_sandiego12.inp"):
     kk = m.kk
     R = _reactions(m)
-    rev = [r["i"] for r in R if r["rev"] == 2]
+    rev = [r["i"] for r in R if r["rev"] != 0]
+    eqk = any(r["rev"] == 1 for r in R)
     fall = [r["i"] for r in R if r["fall"]]
     troe = [r["i"] for r in R if r["fall"] > 1]
     kr_slot = {i: q for q, i in enumerate(rev)}
@@ -119,16 +117,22 @@ def generate(m, name="h2air9", source="phd_gb300/data/h2_sandiego12.inp"):
     w("  const double T2 = T * T, T3 = T * T2, T4 = T2 * T2;")
     w("  t.T = T;")
     w("  t.rut = T * %s;" % lit(m.ru))
+    if eqk:
+        w("  double %s;   // S/R - H/RT (CKSMH)" % ", ".join("smh%d" % k for k in range(kk)))
     for k in range(kk):
         lo, hi = list(m.a[k][0]), list(m.a[k][1])
         w("  {   // species %d" % k)
         w("    const bool hi = T > %s;" % lit(m.tmid[k]))
-        for j in range(6):
+        for j in range(7 if eqk else 6):
             w("    const double a%d = hi ? %s : %s;" % (j, lit(hi[j]), lit(lo[j])))
         w("    const double cps = a0 + T * a1 + T2 * a2 + T3 * a3 + T4 * a4;")
         w("    t.cvk[%d] = %s * (cps - 1.0);" % (k, lit(ru_wt[k])))
         w("    const double hs = a0 + (0.5 * T) * a1 + (T2 * (1.0 / 3.0)) * a2 + (0.25 * T3) * a3 + (0.2 * T4) * a4;")
         w("    t.h[%d] = t.rut * (hs + a5 * Tinv) * %s;" % (k, lit(wt_inv[k])))
+        if eqk:
+            w("    const double sv = (alogt - 1.0) * a0 + (0.5 * T) * a1 + (T2 * (1.0 / 6.0)) * a2 +")
+            w("                      (T3 * (1.0 / 12.0)) * a3 + (T4 * 0.05) * a4;")
+            w("    smh%d = sv + a6 - a5 * Tinv;" % k)
         w("  }")
     for r in R:
         i = r["i"]
@@ -137,6 +141,16 @@ def generate(m, name="h2air9", source="phd_gb300/data/h2_sandiego12.inp"):
         if r["rev"] == 2:
             q = r["rpar"]
             w("  t.kr[%d] = %s * exp(%s * alogt - %s * Tinv);" % (kr_slot[i], lit(q[0]), lit(q[1]), lit(q[2])))
+        elif r["rev"] == 1:   # k_f / K_c, K_c from the species' S/R - H/RT
+            w("  {")
+            w("    double sumsmh = 0.0;")
+            for n in range(6):
+                if r["nuk"][n] >= 0:
+                    w("    sumsmh = sumsmh + %s * smh%d;" % (lit(float(r["nu"][n])), r["nuk"][n]))
+            w("    double eqk = sumsmh != 0.0 ? exp(fmin(sumsmh, 690.77552789821368)) : 1.0;")
+            w("    eqk = eqk * powi(%s * Tinv / %s, %d);" % (lit(m.patm), lit(m.ru), sum(r["nu"])))
+            w("    t.kr[%d] = t.kf[%d] / fmax(eqk, 1.0e-300);" % (kr_slot[i], i))
+            w("  }")
         if r["fall"]:
             q = r["low"]
             w("  t.klow[%d] = %s * exp(%s * alogt - %s * Tinv);" % (lo_slot[i], lit(q[0]), lit(q[1]), lit(q[2])))
@@ -172,7 +186,7 @@ def generate(m, name="h2air9", source="phd_gb300/data/h2_sandiego12.inp"):
         w("  double rop%d;" % i)
         w("  {   // reaction %d" % i)
         w("    double rkft = t.kf[%d];" % i)
-        isrev = r["rev"] == 2
+        isrev = r["rev"] != 0
         if isrev:
             w("    double rkrt = t.kr[%d];" % kr_slot[i])
         ctb = None

@@ -6,9 +6,17 @@
 #define IZEM_CHEM_HOST_TEST 1
 #include "../../phd_gb300/csrc/chem.cu"
 
+// The host copies of what chem_upload_mech puts in constant memory.
+static void set_mech(const izem_mech* m) {
+  c_mech_host = *m;
+  c_fast_host = chem_fast_constants(*m);
+  c_need_eqk_host = 0;
+  for (int i = 0; i < m->ii; ++i) c_need_eqk_host |= (m->rev[i] == 1);
+}
+
 extern "C" void host_psr(const izem_mech* m, int n, double* T, const double* rho, double* Y, const double* dt,
                          int* nst_out) {
-  c_mech_host = *m;
+  set_mech(m);
   for (int q = 0; q < n; ++q) {
     double z[10];
     z[0] = T[q];
@@ -25,8 +33,7 @@ extern "C" void host_psr(const izem_mech* m, int n, double* T, const double* rho
 // reference-order one (ck_fun), both on the host.
 extern "C" void host_fun_pair(const izem_mech* m, int n, const double* rho, const double* z, double* zp_ref,
                               double* zp_fast) {
-  c_mech_host = *m;
-  c_fast_host = chem_fast_constants(*m);
+  set_mech(m);
   for (int q = 0; q < n; ++q) {
     ck_fun<9>(rho[q], z + 10 * q, zp_ref + 10 * q);
     ck_fun_fast<9>(rho[q], z + 10 * q, zp_fast + 10 * q);
@@ -39,8 +46,7 @@ extern "C" void host_fun_pair(const izem_mech* m, int n, const double* rho, cons
 // oracle, apart from CUDA's exp/log and FMA contraction.
 extern "C" void host_psr_fast(const izem_mech* m, int n, double* T, const double* rho, double* Y, const double* dt,
                               int* nst_out) {
-  c_mech_host = *m;
-  c_fast_host = chem_fast_constants(*m);
+  set_mech(m);
   for (int q = 0; q < n; ++q) {
     Rc<10> r;
     double z[10];
@@ -58,8 +64,7 @@ extern "C" void host_psr_fast(const izem_mech* m, int n, double* T, const double
 // next to the generic device form (ck_fun_fast), both on the host.
 extern "C" void host_fun_gen_pair(const izem_mech* m, int n, const double* rho, const double* z, double* zp_tab,
                                   double* zp_gen, int* matches) {
-  c_mech_host = *m;
-  c_fast_host = chem_fast_constants(*m);
+  set_mech(m);
   *matches = chem_gen::matches(*m) ? 1 : 0;
   for (int q = 0; q < n; ++q) {
     ck_fun_fast<9>(rho[q], z + 10 * q, zp_tab + 10 * q);

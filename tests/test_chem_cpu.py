@@ -362,13 +362,16 @@ def test_sri_and_collider_rates_against_a_restatement(tmp_path):
                 assert abs(wdot[k] - ref.get(k, 0.0)) <= 1e-13 * abs(rop), (i, q, k, wdot[k], ref.get(k, 0.0))
 
 
-def test_sri_and_collider_device_forms_on_the_host(host_chem, tmp_path):
-    """With the variant mechanism, the device integrator in the reference's
-    operation order reproduces the oracle bit for bit on the host, and the
-    reciprocal form agrees with it to 1e-12 of each component's largest
-    rate."""
+@pytest.mark.parametrize("variant", ["sri_collider", "equilibrium"])
+def test_variant_mechanisms_device_forms_on_the_host(host_chem, tmp_path, variant):
+    """With a variant mechanism (the SRI form and a single-species collider,
+    or reverse rates from the equilibrium constant), the device integrator
+    in the reference's operation order reproduces the oracle bit for bit on
+    the host, and the reciprocal form agrees with it to 1e-12 of each
+    component's largest rate."""
     import ctypes as C
-    m = _variant_mechanism(tmp_path)
+    import workloads as W
+    m = W.VARIANTS[variant](tmp_path)
     T, rho, Y, dt = ics.batched_reactors(512, seed=43)
     To, Yo = T.copy(), Y.copy()
     oracle.psr_cells(m, To, rho.copy(), Yo, dt.copy())
@@ -385,20 +388,22 @@ def test_sri_and_collider_device_forms_on_the_host(host_chem, tmp_path):
     assert np.all(err < 1e-12), err
 
 
-def test_generated_rhs_for_sri_and_collider(tmp_path):
-    """mechgen writes the variant's right-hand side; compiled into the host
+@pytest.mark.parametrize("variant", ["sri_collider", "equilibrium"])
+def test_generated_rhs_for_variant_mechanisms(tmp_path, variant):
+    """mechgen writes a variant's right-hand side; compiled into the host
     harness in place of the shipped header (IZEM_CHEM_GEN_HEADER), it is the
     reciprocal table form bit for bit, and it recognises its own mechanism."""
     import ctypes as C
     import shutil
     import subprocess
+    import workloads as W
     from phd_gb300 import mechgen
     nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
     if not os.path.exists(nvcc):
         pytest.skip("nvcc not available")
-    m = _variant_mechanism(tmp_path)
+    m = W.VARIANTS[variant](tmp_path)
     hdr = tmp_path / "chem_gen_variant.cuh"
-    hdr.write_text(mechgen.generate(m, source="the SRI / collider test mechanism"))
+    hdr.write_text(mechgen.generate(m, source="the %s test mechanism" % variant))
     here = os.path.dirname(os.path.abspath(__file__))
     so = str(tmp_path / "libchemgen.so")
     subprocess.check_call([nvcc, "-std=c++17", "-O2", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
@@ -413,7 +418,10 @@ def test_generated_rhs_for_sri_and_collider(tmp_path):
     lib.host_fun_gen_pair(C.byref(m), len(T), _P(rho), _P(z), _P(zt), _P(zg), C.byref(ok))
     assert ok.value == 1
     assert np.array_equal(zt, zg), np.abs(zt - zg).max(axis=0)
-    m.sri[3][4] = 0.2   # another SRI exponent: not the generated mechanism
+    if variant == "sri_collider":
+        m.sri[3][4] = 0.2   # another SRI exponent: not the generated mechanism
+    else:
+        m.rev[0] = 0        # reaction 0 irreversible: not the generated mechanism
     lib.host_fun_gen_pair(C.byref(m), 4, _P(rho), _P(z), _P(np.zeros_like(z)), _P(np.zeros_like(z)), C.byref(ok))
     assert ok.value == 0
 

@@ -99,12 +99,14 @@ def test_reacting_field_chem_step_matches_oracle():
     assert abs(dtm_g - dtm_o) <= 100 * (RTOL * abs(dtm_o) + ATOL)
 
 
-def test_psr_batch_with_sri_and_species_collider(tmp_path):
+@pytest.mark.parametrize("variant", ["sri_collider", "equilibrium"])
+def test_psr_batch_with_variant_mechanisms(tmp_path, variant):
     """The persistent BDF kernels with a mechanism that uses the SRI fall-off
-    form and a single-species collider (workloads.variant_mechanism; no
-    generated right-hand side matches it, so the kernels walk the tables):
-    within the bounds above against the oracle."""
-    m = W.variant_mechanism(tmp_path)
+    form and a single-species collider, or reverse rates from the
+    equilibrium constant (workloads.VARIANTS; no generated right-hand side
+    matches them, so the kernels walk the tables): within the bounds above
+    against the oracle."""
+    m = W.VARIANTS[variant](tmp_path)
     T, rho, Y, dt = ics.batched_reactors(2048, seed=51)
     To, Yo = T.copy(), Y.copy()
     ist_o, _ = oracle.psr_cells(m, To, rho.copy(), Yo, dt.copy())

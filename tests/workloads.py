@@ -180,3 +180,26 @@ def variant_mechanism(tmp_path):
     path = tmp_path / "h2_sri_collider.inp"
     path.write_text(text)
     return read_mechanism(str(path), "h2air9")
+
+
+def equilibrium_variant_mechanism(tmp_path):
+    """The shipped mechanism with the explicit reverse parameters (REV) of
+    its first three reactions and of H+OH+M=H2O+M removed: those reverse
+    rates then come from the equilibrium constant (CKRATT's
+    RKRT = RKFT / EQK, vode.f:1015-1022), the path that the shipped set,
+    whose reverse rates are all explicit, does not take."""
+    import os
+    from phd_gb300.mech import read_mechanism
+    from phd_gb300.thd import DATA_DIR
+    with open(os.path.join(DATA_DIR, "h2_sandiego12.inp")) as f:
+        text = f.read()
+    for rev in ("   REV / 7.04E13  -0.26   0.143 /\n", "   REV / 3.03E04   2.63   4.840 /\n",
+                "   REV / 1.28E10   1.19  18.700 /\n", "   REV / 1.03E23  -1.75 118.580 /\n"):
+        assert rev in text
+        text = text.replace(rev, "")
+    path = tmp_path / "h2_equilibrium.inp"
+    path.write_text(text)
+    return read_mechanism(str(path), "h2air9")
+
+
+VARIANTS = {"sri_collider": variant_mechanism, "equilibrium": equilibrium_variant_mechanism}
