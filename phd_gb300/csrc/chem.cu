@@ -1617,6 +1617,19 @@ int chem_variant_registers(int v) {
   return a.numRegs;
 }
 
+bool chem_mech_valid(const izem_mech* m) {
+  if (!m || m->kk != 9 || m->ii < 0 || m->ii > IZEM_MAXREAC) return false;
+  for (int i = 0; i < m->ii; ++i) {
+    for (int n = 0; n < MXSP; ++n)
+      if (m->nuk[i][n] < -1 || m->nuk[i][n] >= m->kk) return false;
+    if (m->rev[i] < 0 || m->rev[i] > 2 || m->fall[i] < 0 || m->fall[i] > 4) return false;
+    if (m->fall[i] && (m->kfal[i] < 0 || m->kfal[i] > m->kk)) return false;
+    if (m->fall[i] >= 3 && (m->troe[i][1] == 0.0 || m->troe[i][2] == 0.0)) return false;
+    if (m->fall[i] == 2 && m->sri[i][2] == 0.0) return false;
+  }
+  return true;
+}
+
 cudaError_t chem_upload_mech(const izem_mech* m) {
   cudaError_t e = cudaMemcpyToSymbol(c_mech_dev, m, sizeof(izem_mech));
   if (e != cudaSuccess) return e;

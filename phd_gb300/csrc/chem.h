@@ -23,6 +23,12 @@ struct ChemStats {
 };
 
 cudaError_t chem_upload_mech(const izem_mech* m);
+// true when the kernels can evaluate m: 9 species, at most IZEM_MAXREAC
+// reactions, species indices in range, known reverse and fall-off kinds, a
+// collider in range, and nonzero Troe and SRI temperatures where the rate
+// divides by them (the two device forms would otherwise disagree: one
+// divides by zero, the other multiplies by a zero reciprocal)
+bool chem_mech_valid(const izem_mech* m);
 // Register-budget variants of the persistent chemistry kernels (128 threads
 // per block; variant v keeps at least 8 - v blocks resident per SM), chosen
 // by the autotuner.  chem_set_variant returns -1 for an unknown variant.

@@ -1072,6 +1072,9 @@ int izem_gpu_set_mechanism(izem_ctx* c, const izem_mech* mech) {
   if (!c || !mech) return IZEM_ERR_ARG;
   if (mech->kk != c->cfg.nrv || mech->kk != 9 || mech->ii > IZEM_MAXREAC)
     return ctx_fail(c, IZEM_ERR_ARG, "mechanism species count must match nrv (9-species set)", cudaSuccess);
+  if (!chem_mech_valid(mech))
+    return ctx_fail(c, IZEM_ERR_ARG, "mechanism tables out of range (species index, reverse or fall-off kind, "
+                    "collider, or a zero Troe/SRI temperature)", cudaSuccess);
   c->mech = *mech;
   CK(chem_upload_mech(mech));
   if (!c->d_counter) {
@@ -1240,7 +1243,7 @@ int izem_gpu_chem_stats(izem_ctx* c, int* failed, int* max_steps, unsigned long 
 
 int izem_gpu_psr_batch(const izem_mech* mech, int n, double* T, const double* rho, double* Y, const double* dt,
                        int* istate, int* nsteps, int device_ptrs, float* kernel_ms) {
-  if (!mech || n <= 0 || !T || !rho || !Y || !dt || mech->kk != 9) return IZEM_ERR_ARG;
+  if (!mech || n <= 0 || !T || !rho || !Y || !dt || !chem_mech_valid(mech)) return IZEM_ERR_ARG;
   cudaStream_t s = nullptr;
   if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return IZEM_ERR_CUDA;
   unsigned* counter = nullptr;
@@ -1516,7 +1519,7 @@ int izem_gpu_allow_chem_generated(int allow) {
 
 int izem_gpu_chem_autotune(const izem_mech* mech, int n, const double* T, const double* rho, const double* Y,
                            const double* dt, int device_ptrs, char* report, int report_len) {
-  if (!mech || n <= 0 || !T || !rho || !Y || !dt || mech->kk != 9) return IZEM_ERR_ARG;
+  if (!mech || n <= 0 || !T || !rho || !Y || !dt || !chem_mech_valid(mech)) return IZEM_ERR_ARG;
   // the first 2^20 reactors are the sample: a smaller one is dominated by the
   // tail of its slowest cells and ranks the variants differently
   const int ns = n < (1 << 20) ? n : (1 << 20);

@@ -413,7 +413,7 @@ int izem_mlp_set_residual(izem_mlp* m, int residual) {
 
 int izem_gpu_reactor_rhs(const izem_mech* mech, int n, const double* T, const double* rho, const double* Y,
                          double* zdot, int device_ptrs) {
-  if (!mech || n <= 0 || !T || !rho || !Y || !zdot || mech->kk != 9) return IZEM_ERR_ARG;
+  if (!mech || n <= 0 || !T || !rho || !Y || !zdot || !chem_mech_valid(mech)) return IZEM_ERR_ARG;
   (void)cudaGetLastError();
   if (chem_upload_mech(mech) != cudaSuccess) return IZEM_ERR_CUDA;
   if (device_ptrs) {
@@ -590,7 +590,8 @@ int izem_mlp_train(izem_mlp* m, long long n, const float* x, const float* t, int
 int izem_gpu_psr_batch_mlp(izem_mlp* m, izem_mlp* m2, const izem_mech* mech, int n, double* T, const double* rho,
                            double* Y, const double* dt, int device_ptrs, const double* gate10, const int* kncf, int nele,
                            double* dT_pred, int* stats3, float* ms2) {
-  if (!m || !mech || n <= 0 || !T || !rho || !Y || !dt || !gate10 || !kncf || mech->kk != 9) return IZEM_ERR_ARG;
+  if (!m || !mech || n <= 0 || !T || !rho || !Y || !dt || !gate10 || !kncf || !chem_mech_valid(mech))
+    return IZEM_ERR_ARG;
   if (nele <= 0 || nele > 8) return IZEM_ERR_ARG;
   if (m2 && m2->residual != m->residual) return IZEM_ERR_ARG;   // one target form per ensemble
   const int CH = 1 << 20;

@@ -124,3 +124,39 @@ def test_struct_layout_matches_a_c_compiler(tmp_path):
         want.append(C.sizeof(cls))
         want += [getattr(cls, mem).offset for mem in members]
     assert got == want
+
+
+def test_chemistry_entry_points_refuse_bad_mechanism_tables():
+    """A mechanism whose tables the kernels cannot evaluate is refused with
+    IZEM_ERR_ARG before any device work: an unknown fall-off kind, a
+    collider out of range, a zero SRI temperature.  The shipped mechanism
+    passes the same check (the call then fails only for want of a device or
+    succeeds on one)."""
+    import numpy as np
+    from phd_gb300.build import build_gpu
+    from phd_gb300.capi import IzemMech
+    from phd_gb300.mech import h2_mechanism
+    lib = C.CDLL(build_gpu())
+    fn = lib.izem_gpu_psr_batch
+    fn.restype = C.c_int
+    fn.argtypes = [C.POINTER(IzemMech), C.c_int] + [C.c_void_p] * 6 + [C.c_int, C.c_void_p]
+    T, rho, dt = np.full(4, 1500.0), np.full(4, 1e-4), np.full(4, 1e-7)
+    Y = np.zeros((4, 9))
+    Y[:, 8] = 1.0
+
+    def call(m):
+        return fn(C.byref(m), 4, T.ctypes.data, rho.ctypes.data, Y.ctypes.data, dt.ctypes.data, None, None, 0, None)
+
+    for edit in ("fall", "kfal", "sri", "nuk"):
+        m = h2_mechanism()
+        if edit == "fall":
+            m.fall[3] = 5
+        elif edit == "kfal":
+            m.kfal[3] = 10
+        elif edit == "sri":
+            m.fall[3] = 2
+            m.sri[3][2] = 0.0
+        else:
+            m.nuk[0][0] = 9
+        assert call(m) == 1, edit   # IZEM_ERR_ARG
+    assert call(h2_mechanism()) != 1
