@@ -1373,20 +1373,31 @@ __global__ void __launch_bounds__(kChemThreads, MINB) k_psr_batch(int n, double*
 // Inputs of the learned surrogate: T [K], ln p [atm], ln(Y_k + 1e-10),
 // ln dt [s], normalised by the training means / standard deviations.
 // The features are formed in FP64 as on the host that trains the networks,
-// so a device row rounds to the same BF16 values as the host's; one pass
-// writes the inputs of both networks of an ensemble (x2 may be null); rows
-// are 16 BF16 values, written as two 16-byte stores.
+// so a device row rounds to the same BF16 values as the host's (the
+// reciprocal multiplications below move an FP64 value by an ulp at most,
+// which changes its BF16 rounding only when it lies within that ulp of a
+// BF16 rounding boundary); one pass writes the inputs of both networks of
+// an ensemble (x2 may be null); rows are 16 BF16 values, written as two
+// 16-byte stores.  Launched with at least 32 threads per block.
 template <int KK>
 __global__ void k_featurize(int n, const double* T, const double* rho, const double* Y, const double* dt,
                             const float* norm, __nv_bfloat16* x, const float* norm2, __nv_bfloat16* x2) {
   static_assert(KK + 3 <= 16, "one 16-wide input row");
+  // 1 / std of each input of both networks, once per block
+  __shared__ double s_inv[2][16];
+  if (threadIdx.x < 32) {
+    const int net = threadIdx.x >> 4, c = threadIdx.x & 15;
+    const float* nm = net ? norm2 : norm;
+    s_inv[net][c] = (nm && c < KK + 3) ? 1.0 / (double)nm[KK + 3 + c] : 0.0;
+  }
+  __syncthreads();
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= n) return;
   double f[16];
   const double Tq = T[q];
   double wmi = 0.0;
 #pragma unroll
-  for (int k = 0; k < KK; ++k) wmi += fmax(Y[(size_t)q * KK + k], 0.0) / c_mech.wt[k];
+  for (int k = 0; k < KK; ++k) wmi += fmax(Y[(size_t)q * KK + k], 0.0) * c_fast.wt_inv[k];
   const double p_atm = rho[q] * c_mech.ru * Tq * wmi / c_mech.patm;
   f[0] = Tq;
   f[1] = log(p_atm);
@@ -1400,8 +1411,8 @@ __global__ void k_featurize(int n, const double* T, const double* rho, const dou
     uint32_t pk[8];
 #pragma unroll
     for (int c = 0; c < 16; c += 2) {
-      const float a = c < KK + 3 ? (float)((f[c] - nm[c]) / nm[KK + 3 + c]) : 0.f;
-      const float b = c + 1 < KK + 3 ? (float)((f[c + 1] - nm[c + 1]) / nm[KK + 3 + c + 1]) : 0.f;
+      const float a = c < KK + 3 ? (float)((f[c] - nm[c]) * s_inv[net][c]) : 0.f;
+      const float b = c + 1 < KK + 3 ? (float)((f[c + 1] - nm[c + 1]) * s_inv[net][c + 1]) : 0.f;
       __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
       pk[c / 2] = *reinterpret_cast<uint32_t*>(&h);
     }
