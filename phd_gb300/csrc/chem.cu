@@ -1431,6 +1431,29 @@ struct GateArgs {
   int residual;                      // the networks predict the increment minus dt f(y0)
 };
 
+// Mean cv and species h at T (CKCVBS, CKHMS) with the reciprocal constants
+// of ck_fun_fast (the species loop of fun_tpart), and the mixture's specific
+// internal energy sum_k Y_k (h_k - RU T / W_k).  For the surrogate's decode:
+// a few ulp from Thermo's reference-order values, a third of its FP64 work.
+template <int KK>
+__device__ __forceinline__ double thermo_fast_e(double T, const double* Y, double* cvb) {
+  const double Tinv = 1.0 / T;
+  const double T2 = T * T, T3 = T * T2, T4 = T2 * T2;
+  const double rut = T * c_mech.ru;
+  double cv = 0.0, e = 0.0;
+#pragma unroll
+  for (int k = 0; k < KK; ++k) {
+    const double* a = c_mech.a[k][T > c_mech.tmid[k] ? 1 : 0];
+    const double cps = a[0] + T * a[1] + T2 * a[2] + T3 * a[3] + T4 * a[4];
+    cv = cv + Y[k] * (c_fast.ru_wt[k] * (cps - 1.0));
+    const double hs = a[0] + (0.5 * T) * a[1] + (T2 * (1.0 / 3.0)) * a[2] + (0.25 * T3) * a[3] + (0.2 * T4) * a[4];
+    const double h = rut * (hs + a[5] * Tinv) * c_fast.wt_inv[k];
+    e = e + Y[k] * (h - c_fast.ru_wt[k] * T);
+  }
+  *cvb = cv;
+  return e;
+}
+
 // Decode the surrogate output, gate it, and write accepted cells in place.
 // Gate: (1) state inside the training envelope, and a predicted |dT| not
 // above the cap (igniting cells, where the network's error is largest, go
@@ -1440,7 +1463,7 @@ struct GateArgs {
 // (constant-volume reactor) for the predicted composition.  Accepted cells
 // take the energy-consistent temperature.  Rejected cells are appended to
 // `list` as base + q (their index in the whole batch) for the BDF integrator.
-template <int KK>
+template <int KK, class Rhs>
 __global__ void k_decode_gate(int n, const float* out, const float* out2, int ldo, const float* norm, const float* norm2,
                               double* T, const double* rho, double* Y, const double* dt, GateArgs ga, const int* kncf,
                               int nele, int* list, int base, unsigned* count, double* dT_pred, ChemStats* stats) {
@@ -1473,7 +1496,9 @@ __global__ void k_decode_gate(int n, const float* out, const float* out2, int ld
     z0[0] = T0;
 #pragma unroll
     for (int k = 0; k < KK; ++k) z0[1 + k] = Y[(size_t)q * KK + k];
-    ck_fun_fast<KK>(rho[q], z0, f0);
+    typename Rhs::Terms t0;
+    Rhs::tpart(T0, t0);
+    Rhs::cpart(rho[q], z0, t0, f0);
 #pragma unroll
     for (int k = 0; k < KK; ++k) dY[k] = dY[k] + dt[q] * f0[1 + k];
     dTp = dTp + dt[q] * f0[0];
@@ -1484,7 +1509,7 @@ __global__ void k_decode_gate(int n, const float* out, const float* out2, int ld
   for (int e = 0; e < nele && ok; ++e) {
     double r = 0.0, sc = 0.0;
     for (int k = 0; k < KK; ++k) {
-      const double nk = (double)kncf[k * nele + e] / c_mech.wt[k];
+      const double nk = (double)kncf[k * nele + e] * c_fast.wt_inv[k];
       r += nk * dY[k];
       sc += nk * fmax(Y[(size_t)q * KK + k], 0.0);
     }
@@ -1496,20 +1521,15 @@ __global__ void k_decode_gate(int n, const float* out, const float* out2, int ld
 #pragma unroll
   for (int k = 0; k < KK; ++k) Yn[k] = Yn[k] / sum;
   // internal energy balance: sum Y0 u(T0) = sum Yn u(T1), Newton on T1
-  double e0 = 0.0;
-  {
-    double h[KK], cvb;
-    Thermo<KK>::cv_h(T0, Y + (size_t)q * KK, &cvb, h);
+  double cvb;
+  double Y0[KK];
 #pragma unroll
-    for (int k = 0; k < KK; ++k) e0 += Y[(size_t)q * KK + k] * (h[k] - c_mech.ru * T0 / c_mech.wt[k]);
-  }
+  for (int k = 0; k < KK; ++k) Y0[k] = Y[(size_t)q * KK + k];
+  const double e0 = thermo_fast_e<KK>(T0, Y0, &cvb);
   double T1 = T0 + dTp;
   if (!(T1 > 200.0 && T1 < 6000.0)) ok = false;
   for (int it = 0; it < 4 && ok; ++it) {
-    double h[KK], cvb, e1 = 0.0;
-    Thermo<KK>::cv_h(T1, Yn, &cvb, h);
-#pragma unroll
-    for (int k = 0; k < KK; ++k) e1 += Yn[k] * (h[k] - c_mech.ru * T1 / c_mech.wt[k]);
+    const double e1 = thermo_fast_e<KK>(T1, Yn, &cvb);
     T1 = T1 - (e1 - e0) / cvb;
   }
   const double dTe = T1 - T0;
@@ -1525,8 +1545,9 @@ __global__ void k_decode_gate(int n, const float* out, const float* out2, int ld
 }
 
 // The reactor right-hand side dz/dt, z = [T, Y_1..Y_K] (FUN of REACTION_V,
-// the device form ck_fun_fast), at n states; zdot is n x (KK + 1).
-template <int KK>
+// the right-hand side the BDF kernels call: generated for the mechanism or
+// walking its tables), at n states; zdot is n x (KK + 1).
+template <int KK, class Rhs>
 __global__ void k_reactor_rhs(int n, const double* __restrict__ T, const double* __restrict__ rho,
                               const double* __restrict__ Y, double* __restrict__ zdot) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1535,7 +1556,9 @@ __global__ void k_reactor_rhs(int n, const double* __restrict__ T, const double*
   z[0] = T[q];
 #pragma unroll
   for (int k = 0; k < KK; ++k) z[1 + k] = Y[(size_t)q * KK + k];
-  ck_fun_fast<KK>(rho[q], z, f);
+  typename Rhs::Terms t;
+  Rhs::tpart(z[0], t);
+  Rhs::cpart(rho[q], z, t, f);
 #pragma unroll
   for (int c = 0; c <= KK; ++c) zdot[(size_t)q * (KK + 1) + c] = f[c];
 }
@@ -1715,14 +1738,16 @@ cudaError_t chem_launch_decode_gate(int n, const float* out, const float* out2, 
                                     cudaStream_t s) {
   GateArgs ga{gate10[0], gate10[1], gate10[2], gate10[3], gate10[4],
               gate10[5], gate10[6], gate10[7], gate10[8], gate10[9], residual};
-  k_decode_gate<9><<<(n + 127) / 128, 128, 0, s>>>(n, out, out2, ldo, d_norm, d_norm2, T, rho, Y, dt, ga, d_kncf, nele,
+  auto kern = g_chem_gen ? k_decode_gate<9, RhsGenerated> : k_decode_gate<9, RhsTables<9>>;
+  kern<<<(n + 127) / 128, 128, 0, s>>>(n, out, out2, ldo, d_norm, d_norm2, T, rho, Y, dt, ga, d_kncf, nele,
                                                    list, base, count, dT_pred, stats);
   return cudaGetLastError();
 }
 
 cudaError_t chem_launch_rhs(int n, const double* T, const double* rho, const double* Y, double* zdot, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
-  k_reactor_rhs<9><<<(n + 127) / 128, 128, 0, s>>>(n, T, rho, Y, zdot);
+  auto kern = g_chem_gen ? k_reactor_rhs<9, RhsGenerated> : k_reactor_rhs<9, RhsTables<9>>;
+  kern<<<(n + 127) / 128, 128, 0, s>>>(n, T, rho, Y, zdot);
   return cudaGetLastError();
 }
 
