@@ -120,9 +120,10 @@ typedef struct izem_adi {
  * and per reaction: stoichiometry (up to 3 reactants, 3 products), forward
  * Arrhenius (A, b, E/R), reverse kind, third-body efficiencies, fall-off
  * (LOW with the Lindemann, SRI or Troe broadening of CKRATX,
- * vode.f:1185-1236; the collider (+M) or one species (+K)).  Units: mol,
- * cm, s, K, erg.  The last two members were added after the others; a
- * zero-filled tail means no SRI reaction and (+M) colliders. */
+ * vode.f:1185-1236; the collider (+M) or one species (+K)), Landau-Teller
+ * factors (CKRATT, vode.f:973-981, 1032-1041).  Units: mol, cm, s, K,
+ * erg.  The last four members were added after the others; a zero-filled
+ * tail means no SRI reaction, (+M) colliders and no Landau-Teller factor. */
 #define IZEM_MAXREAC 32
 typedef struct izem_mech {
   int    kk, ii;
@@ -146,6 +147,11 @@ typedef struct izem_mech {
   double sri[IZEM_MAXREAC][5];            /* SRI a, b [K], c [K], d, e        */
   int    kfal[IZEM_MAXREAC];              /* fall-off collider: 0 (+M), k+1
                                              species k alone, (+K)            */
+  double lt[IZEM_MAXREAC][2];             /* Landau-Teller B, C of the forward
+                                             rate: k_f exp(B/T^1/3 + C/T^2/3);
+                                             0, 0 for none                    */
+  double rlt[IZEM_MAXREAC][2];            /* the same for an explicit (REV)
+                                             reverse rate (RLT)               */
 } izem_mech;
 
 /* EGLIB linking data (the contents of the Linkeg file that EGINI reads,

@@ -85,6 +85,7 @@ class IzemMech(C.Structure):
         ("fall", C.c_int * MAXREAC), ("low", (C.c_double * 3) * MAXREAC),
         ("troe", (C.c_double * 4) * MAXREAC),
         ("sri", (C.c_double * 5) * MAXREAC), ("kfal", C.c_int * MAXREAC),
+        ("lt", (C.c_double * 2) * MAXREAC), ("rlt", (C.c_double * 2) * MAXREAC),
     ]
 
 

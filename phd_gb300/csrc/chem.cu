@@ -83,6 +83,10 @@ int c_need_eqk_host = 0;
 #endif
 
 constexpr int MXSP = 6;
+// exponents of the Landau-Teller factor exp(B / T^(1/3) + C / T^(2/3))
+// (CKRATT's PM_V_1 and PM_V_2, vode.f:975-976)
+constexpr double kLtP1 = 1.0 / 3.0;
+constexpr double kLtP2 = 2.0 * kLtP1;
 
 HD __forceinline__ double powi(double x, int m) {
   unsigned n = m < 0 ? -m : m;
@@ -139,6 +143,8 @@ HD void ck_wyr(double rho, double T, const double* Y, double* wdot) {
   }
   for (int i = 0; i < ii; ++i) {
     double rkft = c_mech.par[i][0] * exp(c_mech.par[i][1] * alogt - c_mech.par[i][2] / T);
+    if (c_mech.lt[i][0] != 0.0 || c_mech.lt[i][1] != 0.0)   // Landau-Teller
+      rkft = rkft * exp(c_mech.lt[i][0] / pow(T, kLtP1) + c_mech.lt[i][1] / pow(T, kLtP2));
     double rkrt = 0.0;
     const int rv = c_mech.rev[i];
     if (rv == 1) {
@@ -155,6 +161,8 @@ HD void ck_wyr(double rho, double T, const double* Y, double* wdot) {
     } else if (rv == 2) {
       rkrt = c_mech.rpar[i][0] * exp(c_mech.rpar[i][1] * alogt - c_mech.rpar[i][2] / T);
     }
+    if (c_mech.rlt[i][0] != 0.0 || c_mech.rlt[i][1] != 0.0)   // reverse Landau-Teller
+      rkrt = rkrt * exp(c_mech.rlt[i][0] / pow(T, kLtP1) + c_mech.rlt[i][1] / pow(T, kLtP2));
     double ctb = 1.0;
     if (c_mech.thb[i]) {
       ctb = ctot;
@@ -281,7 +289,9 @@ HD void fun_tpart(double T, FunT<KK>& t) {
   }
   const int ii = c_mech.ii;
   for (int i = 0; i < ii; ++i) {
-    const double rkft = c_mech.par[i][0] * exp(c_mech.par[i][1] * alogt - c_mech.par[i][2] * Tinv);
+    double rkft = c_mech.par[i][0] * exp(c_mech.par[i][1] * alogt - c_mech.par[i][2] * Tinv);
+    if (c_mech.lt[i][0] != 0.0 || c_mech.lt[i][1] != 0.0)   // Landau-Teller
+      rkft = rkft * exp(c_mech.lt[i][0] / pow(T, kLtP1) + c_mech.lt[i][1] / pow(T, kLtP2));
     double rkrt = 0.0;
     const int rv = c_mech.rev[i];
     if (rv == 1) {
@@ -298,6 +308,8 @@ HD void fun_tpart(double T, FunT<KK>& t) {
     } else if (rv == 2) {
       rkrt = c_mech.rpar[i][0] * exp(c_mech.rpar[i][1] * alogt - c_mech.rpar[i][2] * Tinv);
     }
+    if (c_mech.rlt[i][0] != 0.0 || c_mech.rlt[i][1] != 0.0)   // reverse Landau-Teller
+      rkrt = rkrt * exp(c_mech.rlt[i][0] / pow(T, kLtP1) + c_mech.rlt[i][1] / pow(T, kLtP2));
     t.kf[i] = rkft;
     t.kr[i] = rkrt;
     const int fo = c_mech.fall[i];
@@ -1660,6 +1672,7 @@ bool chem_mech_valid(const izem_mech* m) {
     if (m->fall[i] && (m->kfal[i] < 0 || m->kfal[i] > m->kk)) return false;
     if (m->fall[i] >= 3 && (m->troe[i][1] == 0.0 || m->troe[i][2] == 0.0)) return false;
     if (m->fall[i] == 2 && m->sri[i][2] == 0.0) return false;
+    if ((m->rlt[i][0] != 0.0 || m->rlt[i][1] != 0.0) && m->rev[i] != 2) return false;   // RLT needs REV
   }
   return true;
 }

@@ -418,47 +418,53 @@ inline bool matches(const izem_mech& m) {
   if (!(b(m.a[8][1][3]) == 0x3ddbc128a9b8a724ULL && b(m.a[8][1][4]) == 0xbcfe6a15668d1fd9ULL && b(m.a[8][1][5]) == 0xc08cd661b089a027ULL && b(m.a[8][1][6]) == 0x4017ec0f88333fc8ULL)) return false;
   if (!(m.nuk[0][0] == 0 && m.nu[0][0] == -1 && m.nuk[0][1] == 3 && m.nu[0][1] == -1 && m.nuk[0][2] == -1 && m.nu[0][2] == 0 && m.nuk[0][3] == 2 && m.nu[0][3] == 1)) return false;
   if (!(m.nuk[0][4] == 4 && m.nu[0][4] == 1 && m.nuk[0][5] == -1 && m.nu[0][5] == 0 && b(m.par[0][0]) == 0x435f438daa060000ULL && b(m.par[0][1]) == 0xbfe6666666666666ULL)) return false;
-  if (!(b(m.par[0][2]) == 0x40c0c6f4493ef159ULL && m.rev[0] == 2 && m.thb[0] == 0 && m.fall[0] == 0 && b(m.rpar[0][0]) == 0x42d001d1bf800000ULL && b(m.rpar[0][1]) == 0xbfd0a3d70a3d70a4ULL)) return false;
-  if (!(b(m.rpar[0][2]) == 0x4051fd705d6afec6ULL && m.nuk[1][0] == 1 && m.nu[1][0] == -1 && m.nuk[1][1] == 2 && m.nu[1][1] == -1 && m.nuk[1][2] == -1 && m.nu[1][2] == 0)) return false;
-  if (!(m.nuk[1][3] == 0 && m.nu[1][3] == 1 && m.nuk[1][4] == 4 && m.nu[1][4] == 1 && m.nuk[1][5] == -1 && m.nu[1][5] == 0 && b(m.par[1][0]) == 0x40e8b50000000000ULL)) return false;
-  if (!(b(m.par[1][1]) == 0x40055c28f5c28f5cULL && b(m.par[1][2]) == 0x40a8bb78dad5b973ULL && m.rev[1] == 2 && m.thb[1] == 0 && m.fall[1] == 0 && b(m.rpar[1][0]) == 0x40dd970000000000ULL)) return false;
+  if (!(b(m.par[0][2]) == 0x40c0c6f4493ef159ULL && m.rev[0] == 2 && m.thb[0] == 0 && m.fall[0] == 0 && b(m.lt[0][0]) == 0x0000000000000000ULL && b(m.rlt[0][0]) == 0x0000000000000000ULL && b(m.lt[0][1]) == 0x0000000000000000ULL && b(m.rlt[0][1]) == 0x0000000000000000ULL)) return false;
+  if (!(b(m.rpar[0][0]) == 0x42d001d1bf800000ULL && b(m.rpar[0][1]) == 0xbfd0a3d70a3d70a4ULL && b(m.rpar[0][2]) == 0x4051fd705d6afec6ULL && m.nuk[1][0] == 1 && m.nu[1][0] == -1)) return false;
+  if (!(m.nuk[1][1] == 2 && m.nu[1][1] == -1 && m.nuk[1][2] == -1 && m.nu[1][2] == 0 && m.nuk[1][3] == 0 && m.nu[1][3] == 1 && m.nuk[1][4] == 4 && m.nu[1][4] == 1)) return false;
+  if (!(m.nuk[1][5] == -1 && m.nu[1][5] == 0 && b(m.par[1][0]) == 0x40e8b50000000000ULL && b(m.par[1][1]) == 0x40055c28f5c28f5cULL && b(m.par[1][2]) == 0x40a8bb78dad5b973ULL)) return false;
+  if (!(m.rev[1] == 2 && m.thb[1] == 0 && m.fall[1] == 0 && b(m.lt[1][0]) == 0x0000000000000000ULL && b(m.rlt[1][0]) == 0x0000000000000000ULL && b(m.lt[1][1]) == 0x0000000000000000ULL && b(m.rlt[1][1]) == 0x0000000000000000ULL && b(m.rpar[1][0]) == 0x40dd970000000000ULL)) return false;
   if (!(b(m.rpar[1][1]) == 0x40050a3d70a3d70aULL && b(m.rpar[1][2]) == 0x40a3072327bb03a1ULL && m.nuk[2][0] == 1 && m.nu[2][0] == -1 && m.nuk[2][1] == 4 && m.nu[2][1] == -1)) return false;
   if (!(m.nuk[2][2] == -1 && m.nu[2][2] == 0 && m.nuk[2][3] == 0 && m.nu[2][3] == 1 && m.nuk[2][4] == 5 && m.nu[2][4] == 1 && m.nuk[2][5] == -1 && m.nu[2][5] == 0)) return false;
   if (!(b(m.par[2][0]) == 0x41d16f3220000000ULL && b(m.par[2][1]) == 0x3ff4cccccccccccdULL && b(m.par[2][2]) == 0x409c94c533be761cULL && m.rev[2] == 2 && m.thb[2] == 0 && m.fall[2] == 0)) return false;
-  if (!(b(m.rpar[2][0]) == 0x4207d78400000000ULL && b(m.rpar[2][1]) == 0x3ff30a3d70a3d70aULL && b(m.rpar[2][2]) == 0x40c2611369490098ULL && m.nuk[3][0] == 0 && m.nu[3][0] == -1)) return false;
-  if (!(m.nuk[3][1] == 3 && m.nu[3][1] == -1 && m.nuk[3][2] == -1 && m.nu[3][2] == 0 && m.nuk[3][3] == 6 && m.nu[3][3] == 1 && m.nuk[3][4] == -1 && m.nu[3][4] == 0)) return false;
-  if (!(m.nuk[3][5] == -1 && m.nu[3][5] == 0 && b(m.par[3][0]) == 0x4290eaa664900000ULL && b(m.par[3][1]) == 0x3fdc28f5c28f5c29ULL && b(m.par[3][2]) == 0x0000000000000000ULL)) return false;
-  if (!(m.rev[3] == 0 && m.thb[3] == 1 && m.fall[3] == 3 && b(m.eff[3][0]) == 0x3ff0000000000000ULL && b(m.eff[3][1]) == 0x4004000000000000ULL && b(m.eff[3][2]) == 0x3ff0000000000000ULL)) return false;
+  if (!(b(m.lt[2][0]) == 0x0000000000000000ULL && b(m.rlt[2][0]) == 0x0000000000000000ULL && b(m.lt[2][1]) == 0x0000000000000000ULL && b(m.rlt[2][1]) == 0x0000000000000000ULL && b(m.rpar[2][0]) == 0x4207d78400000000ULL && b(m.rpar[2][1]) == 0x3ff30a3d70a3d70aULL)) return false;
+  if (!(b(m.rpar[2][2]) == 0x40c2611369490098ULL && m.nuk[3][0] == 0 && m.nu[3][0] == -1 && m.nuk[3][1] == 3 && m.nu[3][1] == -1 && m.nuk[3][2] == -1 && m.nu[3][2] == 0)) return false;
+  if (!(m.nuk[3][3] == 6 && m.nu[3][3] == 1 && m.nuk[3][4] == -1 && m.nu[3][4] == 0 && m.nuk[3][5] == -1 && m.nu[3][5] == 0 && b(m.par[3][0]) == 0x4290eaa664900000ULL)) return false;
+  if (!(b(m.par[3][1]) == 0x3fdc28f5c28f5c29ULL && b(m.par[3][2]) == 0x0000000000000000ULL && m.rev[3] == 0 && m.thb[3] == 1 && m.fall[3] == 3 && b(m.lt[3][0]) == 0x0000000000000000ULL && b(m.rlt[3][0]) == 0x0000000000000000ULL)) return false;
+  if (!(b(m.lt[3][1]) == 0x0000000000000000ULL && b(m.rlt[3][1]) == 0x0000000000000000ULL && b(m.eff[3][0]) == 0x3ff0000000000000ULL && b(m.eff[3][1]) == 0x4004000000000000ULL && b(m.eff[3][2]) == 0x3ff0000000000000ULL)) return false;
   if (!(b(m.eff[3][3]) == 0x3ff0000000000000ULL && b(m.eff[3][4]) == 0x3ff0000000000000ULL && b(m.eff[3][5]) == 0x4030000000000000ULL && b(m.eff[3][6]) == 0x3ff0000000000000ULL)) return false;
   if (!(b(m.eff[3][7]) == 0x3ff0000000000000ULL && b(m.eff[3][8]) == 0x3ff0000000000000ULL && m.kfal[3] == 0 && b(m.low[3][0]) == 0x4408efc84ad0c7b0ULL)) return false;
   if (!(b(m.low[3][1]) == 0xbff6666666666666ULL && b(m.low[3][2]) == 0x0000000000000000ULL && b(m.troe[3][0]) == 0x3fe0000000000000ULL && b(m.troe[3][1]) == 0x39b4484bfeebc2a0ULL)) return false;
   if (!(b(m.troe[3][2]) == 0x46293e5939a08ceaULL && m.nuk[4][0] == 0 && m.nu[4][0] == -1 && m.nuk[4][1] == 6 && m.nu[4][1] == -1 && m.nuk[4][2] == -1 && m.nu[4][2] == 0)) return false;
   if (!(m.nuk[4][3] == 4 && m.nu[4][3] == 2 && m.nuk[4][4] == -1 && m.nu[4][4] == 0 && m.nuk[4][5] == -1 && m.nu[4][5] == 0 && b(m.par[4][0]) == 0x42d0191a36680000ULL)) return false;
-  if (!(b(m.par[4][1]) == 0x0000000000000000ULL && b(m.par[4][2]) == 0x40627e432c1d6dbcULL && m.rev[4] == 0 && m.thb[4] == 0 && m.fall[4] == 0 && m.nuk[5][0] == 0 && m.nu[5][0] == -1)) return false;
-  if (!(m.nuk[5][1] == 6 && m.nu[5][1] == -1 && m.nuk[5][2] == -1 && m.nu[5][2] == 0 && m.nuk[5][3] == 1 && m.nu[5][3] == 1 && m.nuk[5][4] == 3 && m.nu[5][4] == 1)) return false;
-  if (!(m.nuk[5][5] == -1 && m.nu[5][5] == 0 && b(m.par[5][0]) == 0x42ae31fa34e00000ULL && b(m.par[5][1]) == 0x0000000000000000ULL && b(m.par[5][2]) == 0x4079da4e3b0f0481ULL)) return false;
-  if (!(m.rev[5] == 2 && m.thb[5] == 0 && m.fall[5] == 0 && b(m.rpar[5][0]) == 0x42839283f4a00000ULL && b(m.rpar[5][1]) == 0x3fd70a3d70a3d70aULL && b(m.rpar[5][2]) == 0x40db3c1120ab0336ULL)) return false;
+  if (!(b(m.par[4][1]) == 0x0000000000000000ULL && b(m.par[4][2]) == 0x40627e432c1d6dbcULL && m.rev[4] == 0 && m.thb[4] == 0 && m.fall[4] == 0 && b(m.lt[4][0]) == 0x0000000000000000ULL && b(m.rlt[4][0]) == 0x0000000000000000ULL)) return false;
+  if (!(b(m.lt[4][1]) == 0x0000000000000000ULL && b(m.rlt[4][1]) == 0x0000000000000000ULL && m.nuk[5][0] == 0 && m.nu[5][0] == -1 && m.nuk[5][1] == 6 && m.nu[5][1] == -1 && m.nuk[5][2] == -1 && m.nu[5][2] == 0)) return false;
+  if (!(m.nuk[5][3] == 1 && m.nu[5][3] == 1 && m.nuk[5][4] == 3 && m.nu[5][4] == 1 && m.nuk[5][5] == -1 && m.nu[5][5] == 0 && b(m.par[5][0]) == 0x42ae31fa34e00000ULL)) return false;
+  if (!(b(m.par[5][1]) == 0x0000000000000000ULL && b(m.par[5][2]) == 0x4079da4e3b0f0481ULL && m.rev[5] == 2 && m.thb[5] == 0 && m.fall[5] == 0 && b(m.lt[5][0]) == 0x0000000000000000ULL && b(m.rlt[5][0]) == 0x0000000000000000ULL)) return false;
+  if (!(b(m.lt[5][1]) == 0x0000000000000000ULL && b(m.rlt[5][1]) == 0x0000000000000000ULL && b(m.rpar[5][0]) == 0x42839283f4a00000ULL && b(m.rpar[5][1]) == 0x3fd70a3d70a3d70aULL && b(m.rpar[5][2]) == 0x40db3c1120ab0336ULL)) return false;
   if (!(m.nuk[6][0] == 4 && m.nu[6][0] == -1 && m.nuk[6][1] == 6 && m.nu[6][1] == -1 && m.nuk[6][2] == -1 && m.nu[6][2] == 0 && m.nuk[6][3] == 3 && m.nu[6][3] == 1)) return false;
   if (!(m.nuk[6][4] == 5 && m.nu[6][4] == 1 && m.nuk[6][5] == -1 && m.nu[6][5] == 0 && b(m.par[6][0]) == 0x42ba48ce3be80000ULL && b(m.par[6][1]) == 0x0000000000000000ULL)) return false;
-  if (!(b(m.par[6][2]) == 0xc06f4328690d2d50ULL && m.rev[6] == 0 && m.thb[6] == 0 && m.fall[6] == 0 && m.nuk[7][0] == 0 && m.nu[7][0] == -1 && m.nuk[7][1] == 4 && m.nu[7][1] == -1)) return false;
-  if (!(m.nuk[7][2] == -1 && m.nu[7][2] == 0 && m.nuk[7][3] == 5 && m.nu[7][3] == 1 && m.nuk[7][4] == -1 && m.nu[7][4] == 0 && m.nuk[7][5] == -1 && m.nu[7][5] == 0)) return false;
-  if (!(b(m.par[7][0]) == 0x44a0f0cf064dd592ULL && b(m.par[7][1]) == 0xc000000000000000ULL && b(m.par[7][2]) == 0x0000000000000000ULL && m.rev[7] == 2 && m.thb[7] == 1 && m.fall[7] == 0)) return false;
+  if (!(b(m.par[6][2]) == 0xc06f4328690d2d50ULL && m.rev[6] == 0 && m.thb[6] == 0 && m.fall[6] == 0 && b(m.lt[6][0]) == 0x0000000000000000ULL && b(m.rlt[6][0]) == 0x0000000000000000ULL && b(m.lt[6][1]) == 0x0000000000000000ULL && b(m.rlt[6][1]) == 0x0000000000000000ULL)) return false;
+  if (!(m.nuk[7][0] == 0 && m.nu[7][0] == -1 && m.nuk[7][1] == 4 && m.nu[7][1] == -1 && m.nuk[7][2] == -1 && m.nu[7][2] == 0 && m.nuk[7][3] == 5 && m.nu[7][3] == 1)) return false;
+  if (!(m.nuk[7][4] == -1 && m.nu[7][4] == 0 && m.nuk[7][5] == -1 && m.nu[7][5] == 0 && b(m.par[7][0]) == 0x44a0f0cf064dd592ULL && b(m.par[7][1]) == 0xc000000000000000ULL)) return false;
+  if (!(b(m.par[7][2]) == 0x0000000000000000ULL && m.rev[7] == 2 && m.thb[7] == 1 && m.fall[7] == 0 && b(m.lt[7][0]) == 0x0000000000000000ULL && b(m.rlt[7][0]) == 0x0000000000000000ULL && b(m.lt[7][1]) == 0x0000000000000000ULL && b(m.rlt[7][1]) == 0x0000000000000000ULL)) return false;
   if (!(b(m.rpar[7][0]) == 0x44b5cfa424ea9c92ULL && b(m.rpar[7][1]) == 0xbffc000000000000ULL && b(m.rpar[7][2]) == 0x40ed22edd4d65d8eULL && b(m.eff[7][0]) == 0x3ff0000000000000ULL)) return false;
   if (!(b(m.eff[7][1]) == 0x4004000000000000ULL && b(m.eff[7][2]) == 0x3ff0000000000000ULL && b(m.eff[7][3]) == 0x3ff0000000000000ULL && b(m.eff[7][4]) == 0x3ff0000000000000ULL)) return false;
   if (!(b(m.eff[7][5]) == 0x4028000000000000ULL && b(m.eff[7][6]) == 0x3ff0000000000000ULL && b(m.eff[7][7]) == 0x3ff0000000000000ULL && b(m.eff[7][8]) == 0x3ff0000000000000ULL)) return false;
   if (!(m.nuk[8][0] == 0 && m.nu[8][0] == -2 && m.nuk[8][1] == -1 && m.nu[8][1] == 0 && m.nuk[8][2] == -1 && m.nu[8][2] == 0 && m.nuk[8][3] == 1 && m.nu[8][3] == 1)) return false;
   if (!(m.nuk[8][4] == -1 && m.nu[8][4] == 0 && m.nuk[8][5] == -1 && m.nu[8][5] == 0 && b(m.par[8][0]) == 0x43b20a871cc00200ULL && b(m.par[8][1]) == 0xbff0000000000000ULL)) return false;
-  if (!(b(m.par[8][2]) == 0x0000000000000000ULL && m.rev[8] == 2 && m.thb[8] == 1 && m.fall[8] == 0 && b(m.rpar[8][0]) == 0x4390e0198eaee000ULL && b(m.rpar[8][1]) == 0xbfe4cccccccccccdULL)) return false;
-  if (!(b(m.rpar[8][2]) == 0x40e96e5d98de8289ULL && b(m.eff[8][0]) == 0x3ff0000000000000ULL && b(m.eff[8][1]) == 0x4004000000000000ULL && b(m.eff[8][2]) == 0x3ff0000000000000ULL)) return false;
-  if (!(b(m.eff[8][3]) == 0x3ff0000000000000ULL && b(m.eff[8][4]) == 0x3ff0000000000000ULL && b(m.eff[8][5]) == 0x4028000000000000ULL && b(m.eff[8][6]) == 0x3ff0000000000000ULL)) return false;
-  if (!(b(m.eff[8][7]) == 0x3ff0000000000000ULL && b(m.eff[8][8]) == 0x3ff0000000000000ULL && m.nuk[9][0] == 6 && m.nu[9][0] == -2 && m.nuk[9][1] == -1 && m.nu[9][1] == 0)) return false;
-  if (!(m.nuk[9][2] == -1 && m.nu[9][2] == 0 && m.nuk[9][3] == 3 && m.nu[9][3] == 1 && m.nuk[9][4] == 7 && m.nu[9][4] == 1 && m.nuk[9][5] == -1 && m.nu[9][5] == 0)) return false;
-  if (!(b(m.par[9][0]) == 0x4285f93037c00000ULL && b(m.par[9][1]) == 0x0000000000000000ULL && b(m.par[9][2]) == 0x4085dbc4f266b3c5ULL && m.rev[9] == 0 && m.thb[9] == 0 && m.fall[9] == 0)) return false;
+  if (!(b(m.par[8][2]) == 0x0000000000000000ULL && m.rev[8] == 2 && m.thb[8] == 1 && m.fall[8] == 0 && b(m.lt[8][0]) == 0x0000000000000000ULL && b(m.rlt[8][0]) == 0x0000000000000000ULL && b(m.lt[8][1]) == 0x0000000000000000ULL && b(m.rlt[8][1]) == 0x0000000000000000ULL)) return false;
+  if (!(b(m.rpar[8][0]) == 0x4390e0198eaee000ULL && b(m.rpar[8][1]) == 0xbfe4cccccccccccdULL && b(m.rpar[8][2]) == 0x40e96e5d98de8289ULL && b(m.eff[8][0]) == 0x3ff0000000000000ULL)) return false;
+  if (!(b(m.eff[8][1]) == 0x4004000000000000ULL && b(m.eff[8][2]) == 0x3ff0000000000000ULL && b(m.eff[8][3]) == 0x3ff0000000000000ULL && b(m.eff[8][4]) == 0x3ff0000000000000ULL)) return false;
+  if (!(b(m.eff[8][5]) == 0x4028000000000000ULL && b(m.eff[8][6]) == 0x3ff0000000000000ULL && b(m.eff[8][7]) == 0x3ff0000000000000ULL && b(m.eff[8][8]) == 0x3ff0000000000000ULL)) return false;
+  if (!(m.nuk[9][0] == 6 && m.nu[9][0] == -2 && m.nuk[9][1] == -1 && m.nu[9][1] == 0 && m.nuk[9][2] == -1 && m.nu[9][2] == 0 && m.nuk[9][3] == 3 && m.nu[9][3] == 1)) return false;
+  if (!(m.nuk[9][4] == 7 && m.nu[9][4] == 1 && m.nuk[9][5] == -1 && m.nu[9][5] == 0 && b(m.par[9][0]) == 0x4285f93037c00000ULL && b(m.par[9][1]) == 0x0000000000000000ULL)) return false;
+  if (!(b(m.par[9][2]) == 0x4085dbc4f266b3c5ULL && m.rev[9] == 0 && m.thb[9] == 0 && m.fall[9] == 0 && b(m.lt[9][0]) == 0x0000000000000000ULL && b(m.rlt[9][0]) == 0x0000000000000000ULL && b(m.lt[9][1]) == 0x0000000000000000ULL && b(m.rlt[9][1]) == 0x0000000000000000ULL)) return false;
   if (!(m.nuk[10][0] == 1 && m.nu[10][0] == -1 && m.nuk[10][1] == 6 && m.nu[10][1] == -1 && m.nuk[10][2] == -1 && m.nu[10][2] == 0 && m.nuk[10][3] == 0 && m.nu[10][3] == 1)) return false;
   if (!(m.nuk[10][4] == 7 && m.nu[10][4] == 1 && m.nuk[10][5] == -1 && m.nu[10][5] == 0 && b(m.par[10][0]) == 0x4242dbf9ea000000ULL && b(m.par[10][1]) == 0x3fe3851eb851eb85ULL)) return false;
-  if (!(b(m.par[10][2]) == 0x40c784fcc6a9ac05ULL && m.rev[10] == 0 && m.thb[10] == 0 && m.fall[10] == 0 && m.nuk[11][0] == 7 && m.nu[11][0] == -1 && m.nuk[11][1] == -1 && m.nu[11][1] == 0)) return false;
-  if (!(m.nuk[11][2] == -1 && m.nu[11][2] == 0 && m.nuk[11][3] == 4 && m.nu[11][3] == 2 && m.nuk[11][4] == -1 && m.nu[11][4] == 0 && m.nuk[11][5] == -1 && m.nu[11][5] == 0)) return false;
-  if (!(b(m.par[11][0]) == 0x43f6b99192fbb3c0ULL && b(m.par[11][1]) == 0xbff63d70a3d70a3dULL && b(m.par[11][2]) == 0x40d93845131294f1ULL && m.rev[11] == 0 && m.thb[11] == 1 && m.fall[11] == 4)) return false;
+  if (!(b(m.par[10][2]) == 0x40c784fcc6a9ac05ULL && m.rev[10] == 0 && m.thb[10] == 0 && m.fall[10] == 0 && b(m.lt[10][0]) == 0x0000000000000000ULL && b(m.rlt[10][0]) == 0x0000000000000000ULL && b(m.lt[10][1]) == 0x0000000000000000ULL && b(m.rlt[10][1]) == 0x0000000000000000ULL)) return false;
+  if (!(m.nuk[11][0] == 7 && m.nu[11][0] == -1 && m.nuk[11][1] == -1 && m.nu[11][1] == 0 && m.nuk[11][2] == -1 && m.nu[11][2] == 0 && m.nuk[11][3] == 4 && m.nu[11][3] == 2)) return false;
+  if (!(m.nuk[11][4] == -1 && m.nu[11][4] == 0 && m.nuk[11][5] == -1 && m.nu[11][5] == 0 && b(m.par[11][0]) == 0x43f6b99192fbb3c0ULL && b(m.par[11][1]) == 0xbff63d70a3d70a3dULL)) return false;
+  if (!(b(m.par[11][2]) == 0x40d93845131294f1ULL && m.rev[11] == 0 && m.thb[11] == 1 && m.fall[11] == 4 && b(m.lt[11][0]) == 0x0000000000000000ULL && b(m.rlt[11][0]) == 0x0000000000000000ULL && b(m.lt[11][1]) == 0x0000000000000000ULL && b(m.rlt[11][1]) == 0x0000000000000000ULL)) return false;
   if (!(b(m.eff[11][0]) == 0x3ff0000000000000ULL && b(m.eff[11][1]) == 0x4004000000000000ULL && b(m.eff[11][2]) == 0x3ff0000000000000ULL && b(m.eff[11][3]) == 0x3ff0000000000000ULL)) return false;
   if (!(b(m.eff[11][4]) == 0x3ff0000000000000ULL && b(m.eff[11][5]) == 0x4018000000000000ULL && b(m.eff[11][6]) == 0x3ff0000000000000ULL && b(m.eff[11][7]) == 0x3ff0000000000000ULL)) return false;
   if (!(b(m.eff[11][8]) == 0x3ff0000000000000ULL && m.kfal[11] == 0 && b(m.low[11][0]) == 0x44e592a7a2071df8ULL && b(m.low[11][1]) == 0xbffe666666666666ULL)) return false;

@@ -10,8 +10,8 @@ Supported syntax: ELEMENTS/SPECIES/REACTIONS/END blocks, '!' comments, the
 REACTIONS units keywords CAL/MOLE KCAL/MOLE JOULES/MOLE KJOULES/MOLE
 KELVINS, '=', '<=>', '=>', '+M', '(+M)', a species as the fall-off collider
 '(+K)', integer stoichiometric prefixes, auxiliary keywords REV, LOW, TROE,
-SRI (3 or 5 parameters; d = 1, e = 0 when 3 are given) and species
-efficiencies 'S/val/'.
+SRI (3 or 5 parameters; d = 1, e = 0 when 3 are given), LT and RLT
+(Landau-Teller B, C; RLT with REV) and species efficiencies 'S/val/'.
 """
 import os
 import re
@@ -108,7 +108,8 @@ def read_mechanism(path, thermo_set="h2air9"):
                         raise ValueError("fall-off collider differs between the sides: %s" % eq)
                     reactions.append({"eq": eq, "reac": r, "prod": p, "par": (A, b, E * escale), "rev": rev,
                                       "rpar": None, "thb": thb1 or (fall1 and not kfal1), "fall": 1 if fall1 else 0,
-                                      "kfal": kfal1, "low": None, "troe": None, "sri": None, "eff": {}})
+                                      "kfal": kfal1, "low": None, "troe": None, "sri": None, "lt": None,
+                                      "rlt": None, "eff": {}})
                 else:
                     rx = reactions[-1]
                     for kw, body in re.findall(r"([A-Za-z0-9()]+)\s*/([^/]*)/", l):
@@ -121,6 +122,10 @@ def read_mechanism(path, thermo_set="h2air9"):
                             rx["low"] = (vals[0], vals[1], vals[2] * escale)
                         elif kwu == "TROE":
                             rx["troe"] = vals
+                        elif kwu in ("LT", "RLT"):
+                            if len(vals) != 2:
+                                raise ValueError("%s takes 2 parameters: %s" % (kwu, rx["eq"]))
+                            rx[kwu.lower()] = vals
                         elif kwu == "SRI":
                             if len(vals) not in (3, 5):
                                 raise ValueError("SRI takes 3 or 5 parameters: %s" % rx["eq"])
@@ -171,6 +176,12 @@ def build_struct(species, reactions, thermo_set):
             for c in range(3):
                 m.rpar[i][c] = rx["rpar"][c]
         m.thb[i] = 1 if rx["thb"] else 0
+        if rx["rlt"] and rx["rev"] != 2:
+            raise ValueError("RLT without REV: %s" % rx["eq"])
+        for key in ("lt", "rlt"):
+            if rx[key]:
+                for c in range(2):
+                    getattr(m, key)[i][c] = rx[key][c]
         for k in range(len(species)):
             m.eff[i][k] = rx["eff"].get(k, 1.0)
         if rx["fall"]:

@@ -15,7 +15,8 @@ operation for operation, so a host build of the two gives identical bits.
 Supported: irreversible reactions, reverse rates from the equilibrium
 constant (CKSMH's entropy-enthalpy difference) or from explicit parameters
 (REV), +M third bodies with efficiencies, Lindemann, SRI and Troe (3 or 4
-parameter) fall-off with the (+M) collider or one species (+K).
+parameter) fall-off with the (+M) collider or one species (+K), and
+Landau-Teller factors on forward (LT) and explicit reverse (RLT) rates.
 
 ``python -m phd_gb300.mechgen`` rewrites ``csrc/chem_gen.cuh`` from the
 shipped mechanism; a test checks that the committed file is what this
@@ -25,6 +26,8 @@ import os
 import struct
 
 HERE = os.path.dirname(os.path.abspath(__file__))
+LT_P1 = 1.0 / 3.0        # the Landau-Teller exponents of chem.cu (kLtP1, kLtP2)
+LT_P2 = 2.0 * LT_P1
 OUT = os.path.join(HERE, "csrc", "chem_gen.cuh")
 
 
@@ -62,6 +65,7 @@ def _reactions(m):
         r = {"i": i, "nuk": list(m.nuk[i]), "nu": list(m.nu[i]), "par": list(m.par[i]), "rev": m.rev[i],
              "rpar": list(m.rpar[i]), "thb": m.thb[i], "fall": m.fall[i], "low": list(m.low[i]),
              "troe": list(m.troe[i]), "sri": list(m.sri[i]), "kfal": m.kfal[i],
+             "lt": list(m.lt[i]), "rlt": list(m.rlt[i]),
              "eff": [m.eff[i][k] for k in range(m.kk)]}
         if r["fall"] not in (0, 1, 2, 3, 4):
             raise NotImplementedError("reaction %d: fall-off form %d" % (i, r["fall"]))
@@ -138,6 +142,9 @@ def generate(m, name="h2air9", source="phd_gb300/data/h2_sandiego12.inp"):
         i = r["i"]
         p = r["par"]
         w("  t.kf[%d] = %s * exp(%s * alogt - %s * Tinv);" % (i, lit(p[0]), lit(p[1]), lit(p[2])))
+        if any(r["lt"]):   # Landau-Teller: the expression of fun_tpart
+            w("  t.kf[%d] = t.kf[%d] * exp(%s / pow(T, %s) + %s / pow(T, %s));"
+              % (i, i, lit(r["lt"][0]), lit(LT_P1), lit(r["lt"][1]), lit(LT_P2)))
         if r["rev"] == 2:
             q = r["rpar"]
             w("  t.kr[%d] = %s * exp(%s * alogt - %s * Tinv);" % (kr_slot[i], lit(q[0]), lit(q[1]), lit(q[2])))
@@ -151,6 +158,9 @@ def generate(m, name="h2air9", source="phd_gb300/data/h2_sandiego12.inp"):
             w("    eqk = eqk * powi(%s * Tinv / %s, %d);" % (lit(m.patm), lit(m.ru), sum(r["nu"])))
             w("    t.kr[%d] = t.kf[%d] / fmax(eqk, 1.0e-300);" % (kr_slot[i], i))
             w("  }")
+        if any(r["rlt"]):
+            w("  t.kr[%d] = t.kr[%d] * exp(%s / pow(T, %s) + %s / pow(T, %s));"
+              % (kr_slot[i], kr_slot[i], lit(r["rlt"][0]), lit(LT_P1), lit(r["rlt"][1]), lit(LT_P2)))
         if r["fall"]:
             q = r["low"]
             w("  t.klow[%d] = %s * exp(%s * alogt - %s * Tinv);" % (lo_slot[i], lit(q[0]), lit(q[1]), lit(q[2])))
@@ -281,6 +291,9 @@ def generate(m, name="h2air9", source="phd_gb300/data/h2_sandiego12.inp"):
         for j in range(3):
             conds.append("b(m.par[%d][%d]) == %s" % (i, j, bits(r["par"][j])))
         conds.append("m.rev[%d] == %d && m.thb[%d] == %d && m.fall[%d] == %d" % (i, r["rev"], i, r["thb"], i, r["fall"]))
+        for j in range(2):
+            conds.append("b(m.lt[%d][%d]) == %s && b(m.rlt[%d][%d]) == %s" % (i, j, bits(r["lt"][j]), i, j,
+                                                                          bits(r["rlt"][j])))
         if r["rev"] == 2:
             for j in range(3):
                 conds.append("b(m.rpar[%d][%d]) == %s" % (i, j, bits(r["rpar"][j])))

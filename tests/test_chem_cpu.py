@@ -362,7 +362,7 @@ def test_sri_and_collider_rates_against_a_restatement(tmp_path):
                 assert abs(wdot[k] - ref.get(k, 0.0)) <= 1e-13 * abs(rop), (i, q, k, wdot[k], ref.get(k, 0.0))
 
 
-@pytest.mark.parametrize("variant", ["sri_collider", "equilibrium"])
+@pytest.mark.parametrize("variant", ["sri_collider", "equilibrium", "landau_teller"])
 def test_variant_mechanisms_device_forms_on_the_host(host_chem, tmp_path, variant):
     """With a variant mechanism (the SRI form and a single-species collider,
     or reverse rates from the equilibrium constant), the device integrator
@@ -388,7 +388,7 @@ def test_variant_mechanisms_device_forms_on_the_host(host_chem, tmp_path, varian
     assert np.all(err < 1e-12), err
 
 
-@pytest.mark.parametrize("variant", ["sri_collider", "equilibrium"])
+@pytest.mark.parametrize("variant", ["sri_collider", "equilibrium", "landau_teller"])
 def test_generated_rhs_for_variant_mechanisms(tmp_path, variant):
     """mechgen writes a variant's right-hand side; compiled into the host
     harness in place of the shipped header (IZEM_CHEM_GEN_HEADER), it is the
@@ -420,15 +420,18 @@ def test_generated_rhs_for_variant_mechanisms(tmp_path, variant):
     assert np.array_equal(zt, zg), np.abs(zt - zg).max(axis=0)
     if variant == "sri_collider":
         m.sri[3][4] = 0.2   # another SRI exponent: not the generated mechanism
+    elif variant == "landau_teller":
+        m.lt[1][1] = 11.0   # another Landau-Teller C: not the generated mechanism
     else:
         m.rev[0] = 0        # reaction 0 irreversible: not the generated mechanism
     lib.host_fun_gen_pair(C.byref(m), 4, _P(rho), _P(z), _P(np.zeros_like(z)), _P(np.zeros_like(z)), C.byref(ok))
     assert ok.value == 0
 
 
-@pytest.mark.parametrize("line", ["   LT / 1.0 2.0 /\n", "   FORD / H2 0.5 /\n"])
+@pytest.mark.parametrize("line", ["   FORD / H2 0.5 /\n", "   RLT / 1.0 2.0 /\n"])
 def test_reader_rejects_rate_forms_it_does_not_build(tmp_path, line):
-    """Landau-Teller and reaction-order auxiliary data are refused, not
+    """Reaction-order data, and reverse Landau-Teller parameters on a
+    reaction without explicit reverse parameters, are refused, not
     dropped."""
     from phd_gb300.mech import read_mechanism
     from phd_gb300.thd import DATA_DIR
@@ -440,3 +443,31 @@ def test_reader_rejects_rate_forms_it_does_not_build(tmp_path, line):
     path.write_text(text)
     with pytest.raises(ValueError):
         read_mechanism(str(path), "h2air9")
+
+
+def test_landau_teller_rates_against_a_restatement(tmp_path):
+    """H2+O<=>OH+H alone with Landau-Teller factors on both rates, from the
+    oracle, against a numpy restatement of CKRATT: k_f = A T^b exp(-E/RT)
+    exp(B/T^(1/3) + C/T^(2/3)), k_r = the REV rate times the RLT factor."""
+    import workloads as W
+    m = W.landau_teller_variant_mechanism(tmp_path)
+    assert list(m.lt[1]) == list(W.LT_PARAMS) and list(m.rlt[1]) == list(W.RLT_PARAMS)
+    mi = _only(m, 1)
+    T, rho, Y, dt = ics.batched_reactors(128, seed=53)
+    Y = _with_radicals(Y)
+    Wt = np.array([m.wt[k] for k in range(m.kk)])
+    for q in range(len(T)):
+        wdot = oracle.ck_wdot(mi, rho[q], T[q], Y[q])
+        C = rho[q] * Y[q] / Wt
+        Tq = T[q]
+
+        def lt(bc):
+            return np.exp(bc[0] / Tq ** (1.0 / 3.0) + bc[1] / Tq ** (2.0 / 3.0))
+
+        kf = m.par[1][0] * np.exp(m.par[1][1] * np.log(Tq) - m.par[1][2] / Tq) * lt(W.LT_PARAMS)
+        kr = m.rpar[1][0] * np.exp(m.rpar[1][1] * np.log(Tq) - m.rpar[1][2] / Tq) * lt(W.RLT_PARAMS)
+        rop = kf * C[1] * C[2] - kr * C[4] * C[0]       # H2 + O -> OH + H
+        ref = {1: -rop, 2: -rop, 4: rop, 0: rop}
+        scale = max(kf * C[1] * C[2], kr * C[4] * C[0])
+        for k in range(m.kk):
+            assert abs(wdot[k] - ref.get(k, 0.0)) <= 1e-13 * scale, (q, k, wdot[k], ref.get(k, 0.0))

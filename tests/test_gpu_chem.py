@@ -99,13 +99,13 @@ def test_reacting_field_chem_step_matches_oracle():
     assert abs(dtm_g - dtm_o) <= 100 * (RTOL * abs(dtm_o) + ATOL)
 
 
-@pytest.mark.parametrize("variant", ["sri_collider", "equilibrium"])
+@pytest.mark.parametrize("variant", ["sri_collider", "equilibrium", "landau_teller"])
 def test_psr_batch_with_variant_mechanisms(tmp_path, variant):
     """The persistent BDF kernels with a mechanism that uses the SRI fall-off
-    form and a single-species collider, or reverse rates from the
-    equilibrium constant (workloads.VARIANTS; no generated right-hand side
-    matches them, so the kernels walk the tables): within the bounds above
-    against the oracle."""
+    form and a single-species collider, reverse rates from the equilibrium
+    constant, or Landau-Teller factors (workloads.VARIANTS; no generated
+    right-hand side matches them, so the kernels walk the tables): within
+    the bounds above against the oracle."""
     m = W.VARIANTS[variant](tmp_path)
     T, rho, Y, dt = ics.batched_reactors(2048, seed=51)
     To, Yo = T.copy(), Y.copy()

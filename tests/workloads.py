@@ -202,4 +202,26 @@ def equilibrium_variant_mechanism(tmp_path):
     return read_mechanism(str(path), "h2air9")
 
 
-VARIANTS = {"sri_collider": variant_mechanism, "equilibrium": equilibrium_variant_mechanism}
+# Landau-Teller parameters (B, C) put on the forward and the explicit reverse
+# rate of H2+O<=>OH+H: exercise the factors, not fitted to any data.
+LT_PARAMS, RLT_PARAMS = (-25.0, 10.0), (5.0, -2.0)
+
+
+def landau_teller_variant_mechanism(tmp_path):
+    """The shipped mechanism with Landau-Teller factors (LT, RLT; CKRATT,
+    vode.f:973-981, 1032-1041) on H2+O<=>OH+H (reaction 1)."""
+    import os
+    from phd_gb300.mech import read_mechanism
+    from phd_gb300.thd import DATA_DIR
+    with open(os.path.join(DATA_DIR, "h2_sandiego12.inp")) as f:
+        text = f.read()
+    rev = "   REV / 3.03E04   2.63   4.840 /\n"
+    assert rev in text
+    text = text.replace(rev, rev + "   LT / %r %r /\n   RLT / %r %r /\n" % (LT_PARAMS + RLT_PARAMS))
+    path = tmp_path / "h2_landau_teller.inp"
+    path.write_text(text)
+    return read_mechanism(str(path), "h2air9")
+
+
+VARIANTS = {"sri_collider": variant_mechanism, "equilibrium": equilibrium_variant_mechanism,
+            "landau_teller": landau_teller_variant_mechanism}
