@@ -612,7 +612,7 @@ def run_field_surrogate(args, steps=None, warmup=None):
     from phd_gb300.izem import IzemGPU, chem_autotune_device, metrics_dscalar
     from phd_gb300.mech import h2_mechanism
     from phd_gb300.surrogate import (ABS_SCALE_LADDER, CAP_LADDER_FINE, DEFAULT_GATE, STRICT_GATE, calibrate_cap,
-                                     train_ensemble)
+                                     reaction_window, train_ensemble)
     import torch
     steps = steps if steps is not None else args.steps
     warmup = warmup if warmup is not None else args.warmup
@@ -637,11 +637,8 @@ def run_field_surrogate(args, steps=None, warmup=None):
     g.set_mechanism(mech)
     dt = info["dt_s"] / info["time_ref"]
     st0 = g.download()
-    ng, nrv = cfg.ng, cfg.nrv
-    # the reaction window of reaction_dvode (interior indices ng+1 .. n-ng-1,
-    # the z bound taken with min(ny, ...)), as ghosted-array slices
-    hi = (min(nx, nx - ng - 1), min(ny, ny - ng - 1), min(ny, nz - ng - 1))
-    win = tuple(slice(2 * ng, h - 1 + ng + 1) for h in hi)
+    nrv = cfg.nrv
+    win = reaction_window(cfg)
     # the register-budget variant of the chemistry kernels, tuned on 2^20 window reactors
     vw = st0["v"][win]
     Tw = st0["T"][win] * adi.t_ref

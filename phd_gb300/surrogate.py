@@ -343,17 +343,23 @@ def training_set(mech, n, seed):
     return X, Yt
 
 
-def window_reactors(g, dt):
-    """The reactors of one chemistry half step of an IzemGPU block: the
-    reaction_dvode window (ng+1 cells skipped at every face; the z bound
-    uses ey, module_reaction.f90:155-171) in physical units, i fastest.
-    Returns T [K], rho [g/cm^3], Y (n, nrv), dt [s] (n values)."""
-    cfg, adi = g.cfg, g.adi
-    st = g.download()
+def reaction_window(cfg):
+    """The reaction_dvode window (module_reaction.f90:155-171) as slices of
+    the ghosted arrays: interior indices ng+1 .. n-ng-1 on every axis, the
+    z bound taken with min(ny, ...) as the reference writes it."""
     ng = cfg.ng
     fx, fy = min(cfg.nx, cfg.nx - ng - 1), min(cfg.ny, cfg.ny - ng - 1)
     fz = min(cfg.ny, cfg.nz - ng - 1)
-    sl = (slice(2 * ng, fx + ng), slice(2 * ng, fy + ng), slice(2 * ng, fz + ng))
+    return (slice(2 * ng, fx + ng), slice(2 * ng, fy + ng), slice(2 * ng, fz + ng))
+
+
+def window_reactors(g, dt):
+    """The reactors of one chemistry half step of an IzemGPU block: the
+    reaction window (reaction_window) in physical units, i fastest.
+    Returns T [K], rho [g/cm^3], Y (n, nrv), dt [s] (n values)."""
+    cfg, adi = g.cfg, g.adi
+    st = g.download()
+    sl = reaction_window(cfg)
     v = st["v"][sl]
     rho = v[..., 0]
     n = rho.size

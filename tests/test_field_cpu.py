@@ -61,3 +61,23 @@ def test_reacting_field_state():
     T_gen = T.copy()
     orc.finalize_ic(st)
     assert np.abs(st["T"] - T_gen).max() <= 1e-9 * np.abs(T_gen).max()
+
+
+def test_reaction_window_is_where_the_oracle_reacts():
+    """surrogate.reaction_window, which the learned-chemistry bench uses to
+    compare increments, covers exactly the cells the oracle's chemistry
+    step changes on a reacting field with unequal extents."""
+    from phd_gb300.mech import h2_mechanism
+    from phd_gb300.surrogate import reaction_window
+    cfg, thd, adi, dxi, st, info = ics.reacting_field(14, 12, 10, dt_s=1e-6, corr=4,
+                                                      lib_dscalar=oracle.metrics_dscalar)
+    orc = oracle.Oracle(cfg, thd, adi, *dxi)
+    orc.finalize_ic(st)
+    v0 = st["v"].copy()
+    orc.chem_step(st, h2_mechanism(), info["dt_s"] / info["time_ref"])
+    ng = cfg.ng
+    inner = (slice(ng, -ng),) * 3
+    changed = np.any(st["v"][inner][..., 5:] != v0[inner][..., 5:], axis=-1)
+    mask = np.zeros(st["T"].shape, dtype=bool)
+    mask[reaction_window(cfg)] = True
+    assert np.array_equal(changed, mask[inner]) and changed.sum() == 7 * 5 * 3
