@@ -107,7 +107,7 @@ def test_struct_layout_matches_a_c_compiler(tmp_path):
               ("izem_thd", IzemThd, ["heatcap", "cofd", "cofeta"]),
               ("izem_adi", IzemAdi, ["time_ref", "d_ref"]),
               ("izem_eglib", IzemEglib, ["cofe", "cofd"]),
-              ("izem_mech", IzemMech, ["a", "eff", "troe", "sri", "kfal"])]
+              ("izem_mech", IzemMech, ["a", "eff", "troe", "sri", "kfal", "lt", "rlt"])]
     lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "izem_gpu.h"', "int main(void) {"]
     for name, _, members in checks:
         lines.append('  printf("%%zu\\n", sizeof(%s));' % name)
